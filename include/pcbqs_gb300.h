@@ -1,0 +1,97 @@
+/*
+ * pcbqs_gb300 -- C ABI of the GB300 (sm_103a) static-fill and solve backend for pcbqs.
+ *
+ * Plain pointers and sizes only. Every function returns 0 on success or a status code:
+ *   1 invalid argument, 2 CUDA error, 3 non-finite result, 4 device allocation failed,
+ *   5 no convergence, 6 a bounded device wait gave up.
+ * pcbqs_gb300_last_error() returns the calling thread's last message.
+ *
+ * "host" arguments are host memory; "device" arguments are device memory of the context's GPU. Entry points named
+ * *_device take a CUDA stream (cudaStream_t, may be NULL for the legacy default stream) and are asynchronous on it
+ * unless stated; the others are synchronous.
+ *
+ * Each declaration names the reference interface it replaces (paths within the pcbqs project).
+ */
+#ifndef PCBQS_GB300_H
+#define PCBQS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pcbqs_gb300_ctx pcbqs_gb300_ctx;
+
+/* Host views of a prepared fill geometry: the arrays of FillGeometry (src/pcbqs/static_backends.py:94-130) and the
+ * per-level observation rules of _offplane_geometry (src/pcbqs/_numerics/sing.py:56-69), row-major float64:
+ * v (nt,3,2), len (nt,3), tau (nt,3,2), un (nt,3,2), area (nt), p3 (nt,3,2), cent (nt,2), radius (nt), z (nt);
+ * qp[k] (nt,nq[k],2) and qw[k] (nq[k]) for k = 0, 1, 2 (a level that was not prepared may repeat level 0's). */
+typedef struct pcbqs_gb300_geometry {
+    int32_t nt;
+    const double *v, *len, *tau, *un, *area, *p3, *cent, *radius, *z;
+    const double *qp[3];
+    const double *qw[3];
+    int32_t nq[3];
+} pcbqs_gb300_geometry;
+
+/* Upload a geometry to `device` once and keep it resident. Replaces the device setup of a fill backend factory,
+ * factory(FillGeometry, workers, chunk, device) (src/pcbqs/static_backends.py:268-270; the CuPy precedent
+ * src/pcbqs/static_cupy.py:73-106). */
+int pcbqs_gb300_create(const pcbqs_gb300_geometry *geometry, int device, pcbqs_gb300_ctx **ctx);
+void pcbqs_gb300_destroy(pcbqs_gb300_ctx *ctx);
+const char *pcbqs_gb300_last_error(void);
+int32_t pcbqs_gb300_triangles(const pcbqs_gb300_ctx *ctx);
+
+/* Pair protocol: moments of n ordered pairs (p observation, q source) at offsets d with quadrature kind
+ * (-1 far, 0/1/2 analytic level), out (n, 1) if scalar_only else (n, 6) ordered M0, Mro_x, Mro_y, Mrs_x, Mrs_y,
+ * Mrr; host arrays, returns after the results are in `out`. Replaces backend.evaluate(p, q, d, kind, scalar_only)
+ * (src/pcbqs/static_backends.py:1-9, :300-336) and the compiled static_pairs
+ * (src/pcbqs/core/static_kernels.hpp:147-172). Status 3 if a moment is not finite. */
+int pcbqs_gb300_pairs(pcbqs_gb300_ctx *ctx, const int32_t *p, const int32_t *q, const double *d,
+                      const int32_t *kind, int64_t n, int scalar_only, double *out);
+
+/* The same on device arrays (p, q, d, kind, out), ordered on `stream`; synchronizes `stream` at the end to read
+ * back the non-finite flag. */
+int pcbqs_gb300_pairs_device(pcbqs_gb300_ctx *ctx, const int32_t *p, const int32_t *q, const double *d,
+                             const int32_t *kind, int64_t n, int scalar_only, double *out, void *stream);
+
+/* Whole reciprocal moment matrices into host planes (each nt x nt, row-major float64; planes[1..3] unused when
+ * scalar_only): M0, Mx, My, Mrr with [p,q] = Mro, [q,p] = Mrs, the diagonal their average. near < 0 or infinite:
+ * every pair analytic. *analytic receives the number of unordered pairs that were not far.
+ * Replaces fill_symmetric(matrices, near, outer_levels, scalar_only) (src/pcbqs/static.py:35-42,
+ * src/pcbqs/static_cupy.py:127-197) and the compiled static_fill (src/pcbqs/core/static_kernels.hpp:184-252). */
+int pcbqs_gb300_fill(pcbqs_gb300_ctx *ctx, double near, int outer, int scalar_only, double *const *planes,
+                     uint64_t *analytic);
+
+/* The same into device planes of leading dimension ld >= nt; synchronizes `stream` at the end (it reads back the
+ * near-pair counts and the non-finite flag). */
+int pcbqs_gb300_fill_device(pcbqs_gb300_ctx *ctx, double near, int outer, int scalar_only, double *const *planes,
+                            int64_t ld, uint64_t *analytic, void *stream);
+
+/* L = factor diag(scale) combine(moments) diag(scale), symmetric, from device moment planes (leading dimension
+ * ldm) into device L (ne x ne, leading dimension ldl): tri (2,ne) int32 supports T+/T-, alpha (2,ne), vertex
+ * (2,ne,2), scale (ne), all device arrays. Replaces the compiled static_combine
+ * (src/pcbqs/core/static_kernels.hpp:257-310) behind static.edge_inductance (src/pcbqs/static.py:103-128). */
+int pcbqs_gb300_edge_inductance_device(int64_t ne, const int32_t *tri, const double *alpha, const double *vertex,
+                                       const double *scale, double factor, const double *mrr, const double *mx,
+                                       const double *my, const double *m0, int64_t ldm, double *L, int64_t ldl,
+                                       void *stream);
+
+/* Host-array form of the same (static_combine's signature): moments (nt x nt) and L (ne x ne) on the host. */
+int pcbqs_gb300_edge_inductance(int64_t nt, int64_t ne, const int32_t *tri, const double *alpha,
+                                const double *vertex, const double *scale, double factor, const double *mrr,
+                                const double *mx, const double *my, const double *m0, double *L);
+
+/* P = factor * W^T M0 W with W[t, a] = 1/area[a] for the triangles t of charge node a (members[start[a] ..
+ * start[a+1])): device arrays; P (nn x nn, leading dimension ldp). factor = 1/(4 pi eps0 er).
+ * Replaces MQS._set_potential (src/pcbqs/mqs.py:532-552). */
+int pcbqs_gb300_potential_device(int64_t nn, const int64_t *start, const int32_t *members, const double *area,
+                                 const double *m0, int64_t ldm, double factor, double *P, int64_t ldp,
+                                 void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PCBQS_GB300_H */

@@ -1,0 +1,111 @@
+"""ctypes binding of the C ABI in include/pcbqs_gb300.h.
+
+The library is built in-tree (pcbqs_gb300/build.py). There is no CPU fallback: if the library or a CUDA device is
+missing, every entry point raises RuntimeError.
+"""
+import ctypes
+import os
+import threading
+from pathlib import Path
+
+import numpy as np
+
+LIBRARY = Path(__file__).resolve().parent / 'libpcbqs_gb300.so'
+
+STATUS = {0: 'ok', 1: 'invalid argument', 2: 'CUDA error', 3: 'non-finite result', 4: 'device allocation failed',
+          5: 'no convergence', 6: 'bounded device wait gave up'}
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int32_p = ctypes.POINTER(ctypes.c_int32)
+c_int64_p = ctypes.POINTER(ctypes.c_int64)
+c_uint64_p = ctypes.POINTER(ctypes.c_uint64)
+c_void_p = ctypes.c_void_p
+
+
+class Geometry(ctypes.Structure):
+    """pcbqs_gb300_geometry: host views of a prepared fill geometry."""
+    _fields_ = [('nt', ctypes.c_int32),
+                ('v', c_double_p), ('len', c_double_p), ('tau', c_double_p), ('un', c_double_p),
+                ('area', c_double_p), ('p3', c_double_p), ('cent', c_double_p), ('radius', c_double_p),
+                ('z', c_double_p),
+                ('qp', c_double_p * 3), ('qw', c_double_p * 3), ('nq', ctypes.c_int32 * 3)]
+
+
+# name: (restype, argtypes)
+PROTOTYPES = {
+    'pcbqs_gb300_create': (ctypes.c_int, [ctypes.POINTER(Geometry), ctypes.c_int, ctypes.POINTER(c_void_p)]),
+    'pcbqs_gb300_destroy': (None, [c_void_p]),
+    'pcbqs_gb300_last_error': (ctypes.c_char_p, []),
+    'pcbqs_gb300_triangles': (ctypes.c_int32, [c_void_p]),
+    'pcbqs_gb300_pairs': (ctypes.c_int, [c_void_p, c_int32_p, c_int32_p, c_double_p, c_int32_p, ctypes.c_int64,
+                                         ctypes.c_int, c_double_p]),
+    'pcbqs_gb300_pairs_device': (ctypes.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_int64,
+                                                ctypes.c_int, c_void_p, c_void_p]),
+    'pcbqs_gb300_fill': (ctypes.c_int, [c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                        ctypes.POINTER(c_void_p), c_uint64_p]),
+    'pcbqs_gb300_fill_device': (ctypes.c_int, [c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                               ctypes.POINTER(c_void_p), ctypes.c_int64, c_uint64_p, c_void_p]),
+    'pcbqs_gb300_edge_inductance_device': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                          ctypes.c_double, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                          ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p]),
+    'pcbqs_gb300_edge_inductance': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, c_int32_p, c_double_p,
+                                                   c_double_p, c_double_p, ctypes.c_double, c_double_p, c_double_p,
+                                                   c_double_p, c_double_p, c_double_p]),
+    'pcbqs_gb300_potential_device': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                    ctypes.c_int64, ctypes.c_double, c_void_p, ctypes.c_int64,
+                                                    c_void_p]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class DeviceError(RuntimeError):
+    """A status returned by the C ABI."""
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__(message)
+
+
+def load():
+    """The loaded library, with prototypes set. Raises RuntimeError when it was not built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = Path(os.environ.get('PCBQS_GB300_LIBRARY', LIBRARY))
+            if not path.exists():
+                raise RuntimeError(f'pcbqs_gb300 library not built ({path}): run python -m pcbqs_gb300.build')
+            lib = ctypes.CDLL(str(path))
+            for name, (restype, argtypes) in PROTOTYPES.items():
+                fn = getattr(lib, name)
+                fn.restype, fn.argtypes = restype, argtypes
+            _lib = lib
+        return _lib
+
+
+def check(status, lib=None):
+    """Raise the Python exception matching a C status (FloatingPointError for non-finite results)."""
+    if status == 0:
+        return
+    lib = lib or load()
+    message = (lib.pcbqs_gb300_last_error() or b'').decode(errors='replace') or STATUS.get(status, str(status))
+    if status == 3:
+        raise FloatingPointError(message)
+    if status == 1:
+        raise ValueError(message)
+    raise DeviceError(status, message)
+
+
+def ptr(array, ctype=ctypes.c_double):
+    """ctypes pointer to a C-contiguous numpy array's data."""
+    if not array.flags.c_contiguous:
+        raise ValueError('array must be C-contiguous')
+    return array.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)

@@ -1,0 +1,416 @@
+// Triangle-pair 1/R moments on sm_103a: the far three-point product rule, the analytic near/singular source
+// integration, the whole-matrix reciprocal fill (upper tiles, near pairs compacted and integrated separately) and
+// the explicit pair-list protocol.
+//
+// Reference behaviour (paths within the pcbqs project):
+//   src/pcbqs/core/static_kernels.hpp:53-106   static_pair       (far_moments, near_moments)
+//   src/pcbqs/core/static_kernels.hpp:147-172  static_pairs      (k_pairs)
+//   src/pcbqs/core/static_kernels.hpp:184-252  static_fill       (k_fill_tiles + k_fill_near)
+//   src/pcbqs/static_cupy_kernels.py:117-157   device row strips (the compaction of near pairs by level)
+#include <cmath>
+#include "common.cuh"
+#include "fill.cuh"
+#include "tma.cuh"
+
+namespace pq {
+
+// ---------------------------------------------------------------------------------------------------------------
+// Pair moments. m = (M0, Mro_x, Mro_y, Mrs_x, Mrs_y, Mrr) of the ordered pair (observation a, source b).
+
+// Far pairs: g_ij = (A_a A_b / 9) / sqrt(|x_i - s_j|^2 + d^2) over the 3 x 3 rule points; the sums are taken
+// per observation point (row sums) so each point multiplies once.
+__device__ __forceinline__ void far_moments(const FarRec &a, const FarRec &b, double d, bool scalar, double *m) {
+    const double w = a.area * b.area / 9.0;
+    const double d2 = d * d;
+    double m0 = 0, ro_x = 0, ro_y = 0, rs_x = 0, rs_y = 0, rr = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double x = a.p[2 * i], y = a.p[2 * i + 1];
+        double g_sum = 0, gsx = 0, gsy = 0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const double sx = b.p[2 * j], sy = b.p[2 * j + 1];
+            const double dx = x - sx, dy = y - sy;
+            const double g = w / sqrt(dx * dx + dy * dy + d2);
+            g_sum += g;
+            if (!scalar) { gsx += g * sx; gsy += g * sy; }
+        }
+        m0 += g_sum;
+        if (!scalar) {
+            ro_x += g_sum * x; ro_y += g_sum * y;
+            rs_x += gsx; rs_y += gsy;
+            rr += x * gsx + y * gsy;
+        }
+    }
+    m[0] = m0; m[1] = ro_x; m[2] = ro_y; m[3] = rs_x; m[4] = rs_y; m[5] = rr;
+}
+
+// Near pairs: for each observation point x_j of triangle a (level-k rule) and each edge e of source triangle b,
+// the closed-form inner integrals of 1/R and of the edge term over b at height offset d:
+//   s- = (V_e - x).tau_e, s+ = s- + L_e, t0 = (V_e - x).u_e, r0 = sqrt(t0^2 + d^2), r-+ = sqrt(r0^2 + s-+^2)
+//   lg = asinh(s+/r0) - asinh(s-/r0)  (0 when r0 <= 1e-14 L_e)
+//   I1 += t0 lg - |d| (atan2(t0 s+, r0^2 + |d| r+) - atan2(t0 s-, r0^2 + |d| r-))
+//   IR += 1/2 (r0^2 lg + s+ r+ - s- r-) u_e
+// accumulated with weights A_a w_j into M0 = sum w I1, Mro = sum w x I1, Mrs = sum w (IR + x I1),
+// Mrr = sum w x.(IR + x I1).
+__device__ __forceinline__ void near_moments(const double *obs, const double *wts, int nq, double area_a,
+                                             const SrcRec &b, double d, bool scalar, double *m) {
+    const double ad = fabs(d);
+    const double d2 = d * d;
+    double m0 = 0, ro_x = 0, ro_y = 0, rs_x = 0, rs_y = 0, rr = 0;
+    for (int j = 0; j < nq; ++j) {
+        const double x = obs[2 * j], y = obs[2 * j + 1];
+        double i1 = 0, irx = 0, iry = 0;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            const double vx = b.v[2 * e] - x, vy = b.v[2 * e + 1] - y;
+            const double le = b.len[e];
+            const double sm = vx * b.tau[2 * e] + vy * b.tau[2 * e + 1];
+            const double sp = sm + le;
+            const double t0 = vx * b.un[2 * e] + vy * b.un[2 * e + 1];
+            const double r02 = t0 * t0 + d2, r0 = sqrt(r02);
+            const double rm = sqrt(r02 + sm * sm), rp = sqrt(r02 + sp * sp);
+            const double lg = r0 > 1e-14 * le ? asinh(sp / r0) - asinh(sm / r0) : 0.0;
+            double inner = t0 * lg;
+            if (ad > 0) inner -= ad * (atan2(t0 * sp, r02 + ad * rp) - atan2(t0 * sm, r02 + ad * rm));
+            i1 += inner;
+            if (!scalar) {
+                const double er = 0.5 * (r02 * lg + sp * rp - sm * rm);
+                irx += er * b.un[2 * e];
+                iry += er * b.un[2 * e + 1];
+            }
+        }
+        const double w = area_a * wts[j];
+        m0 += w * i1;
+        if (!scalar) {
+            const double sx = irx + x * i1, sy = iry + y * i1;
+            ro_x += w * x * i1; ro_y += w * y * i1;
+            rs_x += w * sx; rs_y += w * sy;
+            rr += w * (x * sx + y * sy);
+        }
+    }
+    m[0] = m0; m[1] = ro_x; m[2] = ro_y; m[3] = rs_x; m[4] = rs_y; m[5] = rr;
+}
+
+__device__ __forceinline__ void pair_moments(const Geometry &g, int a, int b, double d, int k, bool scalar,
+                                             double *m) {
+    if (k < 0) {
+        far_moments(g.far[a], g.far[b], d, scalar, m);
+    } else {
+        const int nq = g.nq[k];
+        near_moments(g.obs[k] + 2 * (size_t)a * nq, g.w[k], nq, g.far[a].area, g.src[b], d, scalar, m);
+    }
+}
+
+__device__ __forceinline__ bool finite6(const double *m, bool scalar) {
+    bool ok = isfinite(m[0]);
+    if (!scalar)
+        for (int j = 1; j < 6; ++j) ok = ok && isfinite(m[j]);
+    return ok;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Explicit pair lists (the plugin's evaluate): kind-sorted so a warp never mixes far and near work.
+
+__global__ void k_kind_count(const int32_t *kind, int64_t n, unsigned long long *count) {
+    __shared__ unsigned int local[4];
+    if (threadIdx.x < 4) local[threadIdx.x] = 0;
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int k = kind[i];
+        if (k >= -1 && k <= 2) atomicAdd(&local[k + 1], 1u);     // invalid kinds are reported by k_pairs
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && local[threadIdx.x]) atomicAdd(&count[threadIdx.x], (unsigned long long)local[threadIdx.x]);
+}
+
+// count[0..3] are the bucket sizes; cursor[0..3] start at the exclusive prefix sums.
+__global__ void k_kind_scatter(const int32_t *kind, int64_t n, unsigned long long *cursor, int64_t *order) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int k = kind[i];
+        if (k < -1 || k > 2) continue;
+        const unsigned long long slot = atomicAdd(&cursor[k + 1], 1ull);
+        order[slot] = i;
+    }
+}
+
+// Positions of pairs with an invalid kind are not in `order`: the tail past the valid buckets is filled with -1
+// so k_pairs skips them (and k_pairs flags every invalid pair when it runs in identity order).
+__global__ void k_order_tail(int64_t *order, int64_t from, int64_t n) {
+    for (int64_t i = from + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        order[i] = -1;
+}
+
+__global__ void k_pairs(Geometry g, const int32_t *p, const int32_t *q, const double *d, const int32_t *kind,
+                        const int64_t *order, int64_t n, int scalar, double *out, int *nonfinite, int *invalid) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int64_t i = order ? order[t] : t;
+    if (i < 0) {                       // a pair whose kind was out of range (dropped by the kind sort)
+        *invalid = 1;
+        return;
+    }
+    const int a = p[i], b = q[i], k = kind[i];
+    if (a < 0 || a >= g.nt || b < 0 || b >= g.nt || k < -1 || k > 2) {
+        *invalid = 1;
+        return;
+    }
+    double m[6];
+    pair_moments(g, a, b, d[i], k, scalar, m);
+    const int width = scalar ? 1 : 6;
+    for (int j = 0; j < width; ++j) out[i * width + j] = m[j];
+    if (!finite6(m, scalar)) *nonfinite = 1;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Whole-matrix fill. Upper tiles of TILE x TILE unordered pairs (p <= q), one CTA per tile, persistent over a
+// row-major tile order. Each tile's row and column geometry is staged into shared memory by bulk copies; far
+// pairs are integrated at once and written to [p,q] (coalesced rows) and [q,p] (transposed through shared memory);
+// near pairs are compacted into per-level lists for k_fill_near.
+
+constexpr int TILE = 32;
+constexpr int FILL_THREADS = 256;
+constexpr int ROWS_PER_WARP = TILE / (FILL_THREADS / 32);
+
+struct FillSmem {
+    FarRec far_r[TILE], far_c[TILE];
+    ClsRec cls_r[TILE], cls_c[TILE];
+    double t[4][TILE][TILE + 1];          // transposed staging: [plane][q_local][p_local]
+    unsigned char keep[TILE][TILE];        // [q_local][p_local]: 1 when the reverse entry is written here
+    uint64_t bar;
+};
+
+__device__ __forceinline__ void tile_of(int64_t t, int nb, int &bp, int &bq) {
+    // Row bp of the upper tile triangle starts at off(bp) = bp*nb - bp*(bp-1)/2.
+    const double b = 2.0 * nb + 1.0;
+    int r = (int)floor((b - sqrt(b * b - 8.0 * (double)t)) * 0.5);
+    r = max(0, min(r, nb - 1));
+    auto off = [nb](int64_t x) { return x * nb - x * (x - 1) / 2; };
+    while (r > 0 && off(r) > t) --r;
+    while (r + 1 < nb && off(r + 1) <= t) ++r;
+    bp = r;
+    bq = r + (int)(t - off(r));
+}
+
+__global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, FillPlanes out, FillRule rule,
+                                                             NearLists lists, int *nonfinite, int *status) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    FillSmem &s = *reinterpret_cast<FillSmem *>(smem_raw);
+    const int nt = g.nt;
+    const int nb = (nt + TILE - 1) / TILE;
+    const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool scalar = out.scalar;
+    if (threadIdx.x == 0) {
+        mbar_init(&s.bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    bool failed = false;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int bp, bq;
+        tile_of(t, nb, bp, bq);
+        const int p0 = bp * TILE, q0 = bq * TILE;
+        const int np = min(TILE, nt - p0), nqn = min(TILE, nt - q0);
+        const bool diagonal = bp == bq;
+        if (threadIdx.x == 0) {
+            const uint32_t bytes = (uint32_t)(np + nqn) * (sizeof(FarRec) + sizeof(ClsRec));
+            mbar_arrive_expect_tx(&s.bar, bytes);
+            bulk_load(s.far_r, g.far + p0, np * sizeof(FarRec), &s.bar);
+            bulk_load(s.cls_r, g.cls + p0, np * sizeof(ClsRec), &s.bar);
+            bulk_load(s.far_c, g.far + q0, nqn * sizeof(FarRec), &s.bar);
+            bulk_load(s.cls_c, g.cls + q0, nqn * sizeof(ClsRec), &s.bar);
+        }
+        if (!mbar_wait_bounded(&s.bar, phase)) failed = true;
+        phase ^= 1;
+        if (__syncthreads_or(failed)) {
+            if (threadIdx.x == 0) atomicExch(status, (int)ERR_TIMEOUT);
+            break;
+        }
+        bool bad = false;
+#pragma unroll 1
+        for (int i = 0; i < ROWS_PER_WARP; ++i) {
+            const int pl = warp + (FILL_THREADS / 32) * i, ql = lane;
+            const int p = p0 + pl, q = q0 + ql;
+            bool valid = pl < np && ql < nqn && (!diagonal || pl <= ql);
+            int k = -2;
+            double d = 0;
+            if (valid) {
+                d = s.cls_r[pl].z - s.cls_c[ql].z;
+                k = classify(s.cls_r[pl], s.cls_c[ql], d, rule.near, rule.all_near, rule.outer);
+            }
+            // Near pairs: warp-aggregated appends to the level's list.
+#pragma unroll
+            for (int level = 0; level < 2; ++level) {
+                const int want = level == 0 ? 0 : rule.outer;
+                if (level == 1 && rule.outer == 0) break;
+                const bool mine = valid && k == want;
+                const unsigned mask = __ballot_sync(0xffffffffu, mine);
+                if (mask) {
+                    unsigned long long base = 0;
+                    const int leader = __ffs(mask) - 1;
+                    if (lane == leader) base = atomicAdd(&lists.count[level], (unsigned long long)__popc(mask));
+                    base = __shfl_sync(0xffffffffu, base, leader);
+                    if (mine) {
+                        const unsigned long long slot = base + __popc(mask & ((1u << lane) - 1u));
+                        if (slot < lists.capacity) lists.pair[level][slot] = make_int2(p, q);
+                    }
+                }
+            }
+            const bool far = valid && k < 0;
+            double m[6] = {0, 0, 0, 0, 0, 0};
+            if (far) {
+                far_moments(s.far_r[pl], s.far_c[ql], d, scalar, m);
+                bad = bad || !finite6(m, scalar);
+                const size_t pq = (size_t)p * out.ld + q;
+                out.m0[pq] = m[0];
+                if (!scalar) {
+                    if (p == q) {
+                        out.mx[pq] = (m[1] + m[3]) / 2;
+                        out.my[pq] = (m[2] + m[4]) / 2;
+                    } else {
+                        out.mx[pq] = m[1];
+                        out.my[pq] = m[2];
+                    }
+                    out.mrr[pq] = m[5];
+                }
+            }
+            const bool reverse = far && p != q;
+            s.keep[ql][pl] = reverse;
+            if (reverse) {
+                s.t[0][ql][pl] = m[0];
+                s.t[1][ql][pl] = m[3];
+                s.t[2][ql][pl] = m[4];
+                s.t[3][ql][pl] = m[5];
+            }
+        }
+        __syncthreads();
+        // Reverse entries: row q, columns p0.., coalesced along p.
+#pragma unroll 1
+        for (int i = 0; i < ROWS_PER_WARP; ++i) {
+            const int ql = warp + (FILL_THREADS / 32) * i, pl = lane;
+            if (ql < nqn && pl < np && s.keep[ql][pl]) {
+                const size_t qp = (size_t)(q0 + ql) * out.ld + (p0 + pl);
+                out.m0[qp] = s.t[0][ql][pl];
+                if (!scalar) {
+                    out.mx[qp] = s.t[1][ql][pl];
+                    out.my[qp] = s.t[2][ql][pl];
+                    out.mrr[qp] = s.t[3][ql][pl];
+                }
+            }
+        }
+        if (bad) *nonfinite = 1;
+        __syncthreads();
+    }
+}
+
+// Near pairs of one level, grid-stride over the compacted list; both reciprocal entries written.
+__global__ void k_fill_near(Geometry g, FillPlanes out, const int2 *list, const unsigned long long *count,
+                            unsigned long long capacity, int level, int *nonfinite) {
+    const unsigned long long n = min(*count, capacity);
+    const bool scalar = out.scalar;
+    bool bad = false;
+    for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n;
+         j += (unsigned long long)gridDim.x * blockDim.x) {
+        const int2 pq = list[j];
+        const int p = pq.x, q = pq.y;
+        const double d = g.cls[p].z - g.cls[q].z;
+        double m[6];
+        pair_moments(g, p, q, d, level, scalar, m);
+        bad = bad || !finite6(m, scalar);
+        const size_t fwd = (size_t)p * out.ld + q, rev = (size_t)q * out.ld + p;
+        out.m0[fwd] = m[0];
+        out.m0[rev] = m[0];
+        if (!scalar) {
+            if (p == q) {
+                out.mx[fwd] = (m[1] + m[3]) / 2;
+                out.my[fwd] = (m[2] + m[4]) / 2;
+            } else {
+                out.mx[fwd] = m[1]; out.my[fwd] = m[2];
+                out.mx[rev] = m[3]; out.my[rev] = m[4];
+            }
+            out.mrr[fwd] = m[5];
+            out.mrr[rev] = m[5];
+        }
+    }
+    if (bad) *nonfinite = 1;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Host launchers.
+
+static int sm_count() {
+    static int count = 0;
+    if (!count) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+        if (count <= 0) count = 1;
+    }
+    return count;
+}
+
+cudaError_t launch_pairs(const Geometry &g, const int32_t *p, const int32_t *q, const double *d,
+                         const int32_t *kind, int64_t n, int scalar, double *out, unsigned long long *count4,
+                         int64_t *order, int *nonfinite, int *invalid, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 128;
+    const int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, (int64_t)sm_count() * 16);
+    const int64_t *ord = nullptr;
+    if (order && n > 1) {
+        cudaMemsetAsync(count4, 0, 8 * sizeof(unsigned long long), stream);
+        k_kind_count<<<blocks, 256, 0, stream>>>(kind, n, count4);
+        unsigned long long host[4];
+        cudaMemcpyAsync(host, count4, sizeof(host), cudaMemcpyDeviceToHost, stream);
+        cudaError_t err = cudaStreamSynchronize(stream);
+        if (err != cudaSuccess) return err;
+        unsigned long long cursor[4], run = 0;
+        for (int b = 0; b < 4; ++b) { cursor[b] = run; run += host[b]; }
+        cudaMemcpyAsync(count4 + 4, cursor, sizeof(cursor), cudaMemcpyHostToDevice, stream);
+        k_kind_scatter<<<blocks, 256, 0, stream>>>(kind, n, count4 + 4, order);
+        if ((int64_t)run < n) k_order_tail<<<blocks, 256, 0, stream>>>(order, (int64_t)run, n);
+        err = cudaStreamSynchronize(stream);     // `cursor` lives on this stack frame
+        if (err != cudaSuccess) return err;
+        ord = order;
+    }
+    k_pairs<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(g, p, q, d, kind, ord, n, scalar, out,
+                                                                            nonfinite, invalid);
+    return cudaGetLastError();
+}
+
+size_t fill_smem_bytes() { return sizeof(FillSmem) + 128; }
+
+cudaError_t launch_fill(const Geometry &g, const FillPlanes &out, const FillRule &rule, const NearLists &lists,
+                        int *nonfinite, int *status, cudaStream_t stream) {
+    const int nb = (g.nt + TILE - 1) / TILE;
+    const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
+    const size_t smem = fill_smem_bytes();
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_fill_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = true;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_tiles, FILL_THREADS, smem);
+    if (per_sm < 1) per_sm = 1;
+    const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sm_count() * per_sm);
+    cudaMemsetAsync(lists.count, 0, 2 * sizeof(unsigned long long), stream);
+    k_fill_tiles<<<(unsigned)grid, FILL_THREADS, smem, stream>>>(g, out, rule, lists, nonfinite, status);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    return cudaSuccess;
+}
+
+cudaError_t launch_fill_near(const Geometry &g, const FillPlanes &out, const FillRule &rule, const NearLists &lists,
+                             int *nonfinite, cudaStream_t stream) {
+    const int threads = 128;
+    const int blocks = sm_count() * 8;
+    k_fill_near<<<blocks, threads, 0, stream>>>(g, out, lists.pair[0], lists.count, lists.capacity, 0, nonfinite);
+    if (rule.outer > 0)
+        k_fill_near<<<blocks, threads, 0, stream>>>(g, out, lists.pair[1], lists.count + 1, lists.capacity,
+                                                    rule.outer, nonfinite);
+    return cudaGetLastError();
+}
+
+}  // namespace pq

@@ -1,0 +1,100 @@
+"""Host logic of the backend: mesh preparation, RWG order, node merging, plugin contract without a device."""
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import oracle as O
+
+
+@pytest.mark.parametrize('board', ['tiny', 'strip'])
+def test_prepare_is_bit_identical_to_reference(board):
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.geometry import prepare
+    b = Board.load(board)
+    gold = load_golden(board)
+    g = prepare(b.nodes, b.tris, b.z, 1)
+    np.testing.assert_array_equal(g.cent, gold['cent'])
+    np.testing.assert_array_equal(g.radius, gold['radius'])
+    np.testing.assert_array_equal(g.nodes, gold['centred'])
+    og = O.Geometry(b.nodes, b.tris, b.z, 1)
+    for level in (0, 1):
+        for a, c in zip(g.levels[level], og.levels[level]):
+            np.testing.assert_array_equal(a, c)
+    np.testing.assert_array_equal(g.points, og.points)
+
+
+@pytest.mark.parametrize('board', ['tiny', 'strip', 'planes'])
+def test_rwg_order_and_nodes_match_reference(board):
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.geometry import prepare
+    from pcbqs_gb300.rwg import RWG
+    b = Board.load(board)
+    gold = load_golden(board)
+    g = prepare(b.nodes, b.tris, b.z, 1)
+    r = RWG(g.nodes, g.tris)
+    assert r.Ne == int(gold['ne'])
+    np.testing.assert_array_equal(r.tp, gold['tp'])
+    np.testing.assert_array_equal(r.tm, gold['tm'])
+    np.testing.assert_array_equal(b.node_of, gold['node_of'])
+
+
+def test_prepare_validation():
+    from pcbqs_gb300.geometry import prepare
+    nodes = np.array([[0, 0], [1, 0], [0, 1.]])
+    with pytest.raises(ValueError, match='counter-clockwise'):
+        prepare(nodes, np.array([[0, 2, 1]]), np.zeros(1))
+    with pytest.raises(ValueError, match='finite planar'):
+        prepare(nodes, np.array([[0, 1, 3]]), np.zeros(1))
+    with pytest.raises(ValueError, match='outer_levels'):
+        prepare(nodes, np.array([[0, 1, 2]]), np.zeros(1), 3)
+
+
+def test_missing_gpu_does_not_fall_back_to_cpu(tiny8):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip('a device is present')
+    from pcbqs_gb300.backend import factory
+    from pcbqs_gb300.geometry import prepare
+    g = prepare(tiny8['nodes'], tiny8['tris'], tiny8['z'], 1)
+    with pytest.raises(RuntimeError, match='GB300 fill unavailable'):
+        factory(g, 1, 16384, None)
+
+
+def test_entry_point_is_declared():
+    import tomllib
+    from pathlib import Path
+    meta = tomllib.loads((Path(__file__).resolve().parents[1] / 'pyproject.toml').read_text())
+    group = meta['project']['entry-points']['pcbqs.static_backends']
+    assert group == {'gb300': 'pcbqs_gb300.backend:factory'}
+
+
+def test_reference_engine_selects_the_plugin_and_raises_without_device(tiny8, monkeypatch):
+    """Through the reference's own FillEngine (where its checkout is present): the entry point is loaded only when
+    `gb300` is selected, and without a device the selection fails loudly instead of falling back."""
+    from oracle import reference
+    if not reference.available():
+        pytest.skip('reference checkout not present')
+    import torch
+    pcbqs = reference.load_reference()
+    import pcbqs.static_backends as backends
+    from types import SimpleNamespace
+    monkeypatch.setattr(backends, '_FACTORIES', dict(backends._FACTORIES))
+    loaded = []
+
+    def load():
+        loaded.append(True)
+        from pcbqs_gb300.backend import factory
+        return factory
+    monkeypatch.setattr(backends.metadata, 'entry_points',
+                        lambda **kw: [SimpleNamespace(name='gb300', load=load)])
+    backends.FillEngine(tiny8['nodes'], tiny8['tris'], tiny8['z'], backend='numpy')
+    assert loaded == []
+    if torch.cuda.is_available():
+        e = backends.FillEngine(tiny8['nodes'], tiny8['tris'], tiny8['z'], backend='gb300')
+        assert loaded == [True] and e.info['backend'] == 'gb300'
+    else:
+        with pytest.raises(RuntimeError, match='GB300 fill unavailable'):
+            backends.FillEngine(tiny8['nodes'], tiny8['tris'], tiny8['z'], backend='gb300')
+        assert loaded == [True]
