@@ -1,0 +1,110 @@
+"""Golden port impedances from the reference's own PEEC solve (pcbqs.peec.solve, dense LU) on the synthetic boards.
+
+    python tests/golden/make_peec_golden.py     (this container only: needs the reference checkout)
+
+The reference's MQS model class needs shapely only for meshing and region handling, which these boards do not use
+(their meshes are given). shapely is absent here, so a stand-in module that only provides its names is put in
+sys.modules before pcbqs.mqs is imported; no stand-in function is ever called. The model object is then built
+around the given mesh with the attributes MQS.__init__ would set (src/pcbqs/mqs.py:300-420): one node per triangle
+with terminals and via fans merged, RWG edges as branches, no via segments (each via joins one sheet here), DC
+sheet resistance, homogeneous dielectric er, capacitance on. Ports are 1 A current sources (MQS.source). The
+reference's own methods then assemble and solve: MQS._assemble/_loops/_sheet_resistance/_set_potential,
+static_moments/edge_inductance (compiled core) and peec.solve.
+
+Writes tests/golden/peec_<board>.npz: freqs, port names, Z (nf, np, np) from the node potentials of each drive
+(Z[f, i, j] = voltage of port i for 1 A in port j), and the reference's own diagonal Result.z.
+"""
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[1]))
+
+
+def stub_shapely():
+    """Names-only stand-ins so that pcbqs.mqs imports without shapely; calling any of them raises."""
+    def unavailable(*args, **kwargs):
+        raise RuntimeError('shapely is not available in this environment')
+
+    class Unavailable:
+        def __init__(self, *args, **kwargs):
+            unavailable()
+    root = types.ModuleType('shapely')
+    for sub in ('geometry', 'ops', 'affinity', 'prepared', 'validation', 'strtree'):
+        m = types.ModuleType(f'shapely.{sub}')
+        m.__getattr__ = lambda name, _u=Unavailable: _u
+        sys.modules[f'shapely.{sub}'] = m
+        setattr(root, sub, m)
+    root.__getattr__ = lambda name: Unavailable
+    sys.modules['shapely'] = root
+
+
+def reference_model(board):
+    from oracle.reference import load_reference
+    stub_shapely()
+    load_reference()
+    from pcbqs.mqs import MQS
+    from pcbqs._numerics.base import RWG
+    q = object.__new__(MQS)
+    q.matrix_backend, q.capacitance, q.dielectric, q.er = 'dense', True, 'homogeneous', board.er
+    q.near, q.outer_levels = 3.0, 1
+    q._fill_options = dict(backend='openmp', workers=None, chunk=16384, device=None)
+    q.fill_info, q.log, q.solve_info = {}, (lambda *a, **k: None), []
+    q.thick_kernel, q._thick_D, q.side_charge = False, None, False
+    q.nodes, q.tris = board.nodes, board.tris
+    q.z_of, q.t_of = board.z, np.full(board.nt, board.thickness)
+    q.layer_of = board.layer
+    q.sigma, q.conductor_loss, q.conductor_faces, q.thickness_sheets = board.sigma, 'dc', 2, 1
+    q.layer_tris = {int(l): np.flatnonzero(board.layer == l) for l in np.unique(board.layer)}
+    q.sheet_layer = {k: k for k in q.layer_tris}
+    q.rwg = RWG(q.nodes, q.tris)
+    q.node_of, q.charge_of = board.node_of, None
+    q.n_nodes = board.n_nodes
+    q.terms = {name: [] for name in board.terminals}
+    q.term_node = {name: board.term_node(name) for name in board.terminals}
+    r = q.rwg
+    q.br = [(int(q.node_of[a]), int(q.node_of[b])) for a, b in zip(r.tp, r.tm)]
+    q.n_rwg = r.Ne
+    q.vseg, q.ne, q.nv = [], r.Ne, 0
+    q.parts, q.plating = [], 25e-6
+    q._mats = q._copper = q._potential = q._peec = q._mqs_iter = None
+    q.ideal_terminals, q.factor_cache_bytes = True, 64 * 1024 ** 2
+    for name, a, b in board.ports:
+        q.source(name, a, b, part_h=0.0)
+    return q
+
+
+def port_matrix(q, board, freqs):
+    names = [p for p, _, _ in board.ports]
+    drives = [{n: (1.0 if n == m else 0.0) for n in names} for m in names]
+    results = q.solve(freqs, drives)
+    nf, npo = len(freqs), len(names)
+    Z = np.zeros((nf, npo, npo), complex)
+    diag = np.zeros((nf, npo), complex)
+    for j, res in enumerate(results):
+        for i, (n, a, b) in enumerate(board.ports):
+            Z[:, i, j] = res.potential[:, board.term_node(b)] - res.potential[:, board.term_node(a)]
+        diag[:, j] = res.z[names[j]]
+    return names, Z, diag
+
+
+def main(boards=('tiny', 'strip')):
+    from pcbqs_gb300.board import Board
+    freqs = np.array([1e5, 1e6, 1e7])
+    for name in boards:
+        b = Board.load(name)
+        q = reference_model(b)
+        names, Z, diag = port_matrix(q, b, freqs)
+        assert np.allclose(np.diagonal(Z, axis1=1, axis2=2), diag, rtol=1e-9), 'port voltage convention'
+        m = q._peec
+        np.savez_compressed(HERE / f'peec_{name}.npz', freqs=freqs, ports=np.array(names), Z=Z, z_diag=diag,
+                            unknowns=m['K'].shape[1], loops=m['nl'], components=m['B'].shape[1])
+        print(name, 'unknowns', m['K'].shape[1], 'loops', m['nl'], 'components', m['B'].shape[1])
+        print(np.round(Z[1], 6))
+
+
+if __name__ == '__main__':
+    main(tuple(sys.argv[1:]) or ('tiny', 'strip'))
