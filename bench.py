@@ -1,0 +1,274 @@
+"""Benchmark: fill + solve seconds per frequency of the plane-pair board on one GB300 (and the CPU reference arm).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--board planes] [--freq 1e6]
+                    [--precondition lu32|block_jacobi]
+
+Workload: the 50 x 50 mm plane pair (0.2 mm FR-4, er 4.3, 35 um copper, 40 vias of 0.3 mm diameter, 8 ports;
+22,554 triangles, 33,368 RWG edges, 22,226 charge nodes, 32,990 loop/tree unknowns), seeded synthetic data meshed by
+pcbqs's constrained-Delaunay core (tests/golden/planes.npz). One step = one frequency (1 MHz) of the whole hot path
+with the mesh resident: the FP64 fill of the triangle-pair moments, the RWG combine into L (33k x 33k), the
+aggregation into P (22k x 22k), the loop/tree system's preconditioner and the batched GMRES of all 8 port drives to a
+1e-8 relative residual, and the port impedance matrix. Inputs (L alone is 8.9 GB) are far larger than the 129 MB
+L2, so no flush is needed between steps.
+
+`value` is seconds per frequency over the whole job (N GPUs solve N frequencies per step: replicas, weak
+scaling); `e2e` is the same through the public API from host arrays (PeecModel(board).solve(f): geometry and
+sparse topology uploaded, port matrix read back). The reference arm (--impl reference) times the CPU restatement
+of the reference's path (the oracle: OpenMP C for the fill, combine and aggregation, run in full) on all host cores,
+with the reference's dense solve (a complex64 LU, MixedLU) estimated from a timed bounded LU sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = 'fill+solve s/freq at 1e-8 residual: learned/mixed vs plain FP64 GPU; fill GB/s'
+FAR_FLOP, NEAR_FLOP = 210, {0: 936, 1: 3744, 2: 14976}   # algorithmic flops per pair (full moments)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=3)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    p.add_argument('--board', default='planes')
+    p.add_argument('--freq', type=float, default=1e6)
+    p.add_argument('--precondition', default='lu32', choices=['lu32', 'block_jacobi'])
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    return p.parse_args()
+
+
+def rank_info():
+    return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', f'--id={index}', f'--query-gpu={self.QUERY}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=['nvidia-smi unavailable'])
+        self.proc.terminate()
+        self.proc.wait()
+        self.file.flush()
+        rows = [r.split(', ') for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].replace('.', '').isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4) if r[5 + i].strip() == 'Active'})
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                    reasons=reasons, samples=len(rows))
+
+
+def fill_roofline(model, fp64_peak_tflops):
+    """The fill kernel pair (far tiles + near lists): algorithmic FP64 flops per launch / its CUDA-event time."""
+    import ctypes
+    from pcbqs_gb300 import _lib
+    counts = (ctypes.c_uint64 * 2)()
+    _lib.check(model.fill.lib.pcbqs_gb300_fill_counts(model.fill.dev.handle, counts))
+    nt = model.fill.nt
+    pairs = nt * (nt + 1) // 2
+    near0, near1 = int(counts[0]), int(counts[1])
+    far = pairs - near0 - near1
+    flops = far * FAR_FLOP + near0 * NEAR_FLOP[0] + near1 * NEAR_FLOP[model.fill.outer_levels]
+    seconds = model.timings['fill_ms'] / 1e3
+    achieved = flops / seconds / 1e12
+    return dict(bound='fp64', kernel='k_fill_tiles+k_fill_near', achieved=round(achieved, 4),
+                peak=round(fp64_peak_tflops, 4), unit='TFLOP/s', frac=round(achieved / fp64_peak_tflops, 4),
+                traffic=None, flops_per_launch=flops, far_pairs=far, near_pairs=[near0, near1],
+                peak_source='measured live: FP64 GEMM (cuBLAS DGEMM 8192^3) on this GPU')
+
+
+def fp64_peak():
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device='cuda')
+    b = torch.randn(n, n, dtype=torch.float64, device='cuda')
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def cpu_reference(board_name, freq):
+    """The CPU restatement of the reference path (oracle), all host cores, seconds per frequency: the fill of the
+    moments, the RWG combine and the P aggregation measured in full (OpenMP C), and the reference's dense solve --
+    a complex64 LU of the loop/tree system (MixedLU) -- estimated from a timed LAPACK getrf of a bounded sample
+    scaled by the cube of the size. Returns (value, details)."""
+    from oracle import oracle as O
+    from oracle import peec_cpu
+    from pcbqs_gb300.board import Board
+    b = Board.load(board_name)
+    threads = O.threads()
+    t0 = time.perf_counter()
+    g = O.Geometry(b.nodes, b.tris, b.z, 1)
+    mats, analytic = O.fill(g, 3.0, 1, False, threads)
+    t1 = time.perf_counter()
+    rwg = O.RWG(g.nodes, g.tris)
+    L = O.combine(rwg, mats, nthreads=threads)
+    t2 = time.perf_counter()
+    P = O.potential(mats[0], g.area, b.node_of, b.er, threads)
+    t3 = time.perf_counter()
+    del mats, L, P
+    n = rwg.Ne - (len(b.terminals) + len(b.fans))      # loop/tree unknowns (within a few of the exact count)
+    lu, sample_s = peec_cpu.lu_seconds(n)
+    return (t3 - t0) + lu, dict(cores=threads, fill_s=round(t1 - t0, 3), combine_s=round(t2 - t1, 3),
+                                potential_s=round(t3 - t2, 3), lu_estimate_s=round(lu, 2),
+                                lu_sample='complex64 getrf 3072^3 in %.3f s, scaled by (n/3072)^3, n=%d' % (sample_s, n))
+
+
+def reference_arm(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    values = []
+    details = None
+    for _ in range(max(1, args.steps)):
+        v, details = cpu_reference(args.board, args.freq)
+        values.append(v)
+    value = statistics.median(values)
+    line = dict(metric=METRIC, value=round(value, 4), unit='s/freq', n_gpus=args.gpus, steps=args.steps,
+                warmup=0, ms_per_step=round(value * 1e3, 2), higher_is_better=False, scaling='weak',
+                vs_baseline=None, dtype='f64', data='synthetic (seeded plane-pair board, CDT mesh)',
+                impl='reference',
+                config=dict(workload=f'{args.board}: fill+solve of all ports at {args.freq:g} Hz', board=args.board,
+                            l2='inputs larger than L2'),
+                cpu_baseline=dict(value=round(value, 4), unit='s/freq', cores=details['cores'], kind='port',
+                                  sample=f'full oracle fill+combine+aggregation; dense solve = complex64 LU '
+                                         f'estimated from a bounded sample ({details})'),
+                e2e=dict(value=round(value, 4), unit='s/freq', h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return reference_arm(args)
+    import torch
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    from pcbqs_gb300 import _lib, build
+    build.build()
+    lib = _lib.load()
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel
+    board = Board.load(args.board)
+    freq = args.freq * (1 + 0.01 * rank)          # replicas: each rank its own frequency
+    model = PeecModel(board, device=local)
+
+    def step():
+        model.assemble()
+        return model.solve([freq], precondition=args.precondition)
+
+    for _ in range(args.warmup):
+        result = step()
+    torch.cuda.synchronize()
+    launches0 = lib.pcbqs_gb300_kernel_launches()
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    timings = []
+    for _ in range(args.steps):
+        result = step()
+        timings.append(dict(model.timings))
+    e1.record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clock_info = clocks.stop()
+    launches = lib.pcbqs_gb300_kernel_launches() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    value = ms / 1e3 / world
+    # fill GB/s: bytes of L and P written once per step, over the fill + combine + aggregation time
+    ne, nn = model.ne, model.nn
+    fill_ms = statistics.median(t['fill_ms'] + t['combine_ms'] + t['potential_ms'] for t in timings)
+    fill_gbs = 8 * (ne * ne + nn * nn) / (fill_ms / 1e3) / 1e9
+    # end to end through the public API from host arrays
+    t_e2e = time.perf_counter()
+    torch.cuda.synchronize()
+    m2 = PeecModel(Board.load(args.board), device=local)
+    r2 = m2.solve([freq], precondition=args.precondition)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t_e2e
+    h2d = m2.fill.dev.nt * (64 + 32 + 192) + sum(a.nbytes for a in m2.fill.geometry.levels[1][5:6])
+    h2d += 16 * m2.n * len(m2.names)                 # right-hand sides
+    d2h = 16 * m2.n * len(m2.names) + r2.impedance.nbytes
+    del m2
+    torch.cuda.empty_cache()
+    if rank != 0:
+        return
+    peak = fp64_peak()
+    line = dict(metric=METRIC, value=round(value, 4), unit='s/freq', n_gpus=world, steps=args.steps,
+                warmup=args.warmup, ms_per_step=round(ms, 2), higher_is_better=False, scaling='weak',
+                vs_baseline=None, dtype='f64', data='synthetic (seeded plane-pair board, CDT mesh)',
+                config=dict(workload=f'{args.board}: fill+solve of all {len(model.names)} ports at {args.freq:g} Hz',
+                            board=args.board, triangles=model.fill.nt, edges=ne, nodes=nn, unknowns=model.n,
+                            precondition=args.precondition, gmres_tol=model.tol,
+                            gmres_iterations=result.iterations.tolist(), parallelism=f'replicas x{world}',
+                            l2='inputs larger than L2 (L 8.9 GB)'),
+                fill_gbs=round(fill_gbs, 2),
+                breakdown_ms={k: round(statistics.median(t.get(k, 0) for t in timings), 2)
+                              for k in ('fill_ms', 'combine_ms', 'potential_ms', 'precondition_ms', 'gmres_ms')},
+                gpu_launches=int(launches),
+                clocks=clock_info,
+                roofline=fill_roofline(model, peak),
+                e2e=dict(value=round(e2e_s, 4), unit='s/freq', h2d_bytes_per_step=int(h2d),
+                         d2h_bytes_per_step=int(d2h)))
+    if not args.no_cpu_baseline:
+        v, details = cpu_reference(args.board, args.freq)
+        line['cpu_baseline'] = dict(value=round(v, 3), unit='s/freq', cores=details['cores'], kind='port',
+                                    sample=f'oracle fill+combine+aggregation in full; dense solve = complex64 LU '
+                                           f'estimated from a bounded sample; {details}')
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -42,6 +42,11 @@ int pcbqs_gb300_create(const pcbqs_gb300_geometry *geometry, int device, pcbqs_g
 void pcbqs_gb300_destroy(pcbqs_gb300_ctx *ctx);
 const char *pcbqs_gb300_last_error(void);
 int32_t pcbqs_gb300_triangles(const pcbqs_gb300_ctx *ctx);
+/* Kernels this library has launched in the process so far (for launch accounting). No reference counterpart. */
+int64_t pcbqs_gb300_kernel_launches(void);
+/* The near-pair counts of the context's last fill: counts[0] at level 0, counts[1] at the refined level. Their
+ * sum is the analytic count static_fill reports (src/pcbqs/core/static_kernels.hpp:251). */
+int pcbqs_gb300_fill_counts(const pcbqs_gb300_ctx *ctx, uint64_t *counts);
 
 /* Pair protocol: moments of n ordered pairs (p observation, q source) at offsets d with quadrature kind
  * (-1 far, 0/1/2 analytic level), out (n, 1) if scalar_only else (n, 6) ordered M0, Mro_x, Mro_y, Mrs_x, Mrs_y,
@@ -89,6 +94,67 @@ int pcbqs_gb300_edge_inductance(int64_t nt, int64_t ne, const int32_t *tri, cons
 int pcbqs_gb300_potential_device(int64_t nn, const int64_t *start, const int32_t *members, const double *area,
                                  const double *m0, int64_t ldm, double factor, double *P, int64_t ldp,
                                  void *stream);
+
+/* ---- Solve: the PEEC operator in loop/tree coordinates and batched GMRES ------------------------------------
+ * Complex vectors of k systems are (n, k) row-major complex128 (interleaved re, im) device arrays. */
+
+/* A sparse matrix in CSR form on the device: ptr (rows+1) int64, idx (nnz) int32, val (nnz) float64. */
+typedef struct pcbqs_gb300_csr {
+    int64_t rows, cols;
+    const int64_t *ptr;
+    const int32_t *idx;
+    const double *val;
+} pcbqs_gb300_csr;
+
+/* The operator of peec_iterative.solve's product (src/pcbqs/peec_iterative.py:267-278) at nsys frequencies:
+ *   out_s = K^T (R + j w_s L) K D_s y / zscale_s + T^T P T y / pscale,  D_s = diag(1 | j w_s zscale_s / pscale)
+ * K (nb x n) the loop/tree basis over passive branches, Kt = K^T, T (nn x n) = A K restricted to the tree unknowns,
+ * Tt = T^T, R (ne x ne) the copper's sparse resistance, L (ne x ne, row stride ldl) and P (nn x nn, ldp) dense
+ * symmetric, is_tree (n) int8 marks the tree unknowns; omega and zscale are host arrays (nsys). The device arrays
+ * must stay alive while the operator is used. */
+typedef struct pcbqs_gb300_peec_desc {
+    int64_t n, nb, ne, nn;
+    pcbqs_gb300_csr K, Kt, T, Tt, R;
+    const double *L;
+    int64_t ldl;
+    const double *P;
+    int64_t ldp;
+    const int8_t *is_tree;
+    double pscale;
+    int32_t nsys;
+    const double *omega, *zscale;
+} pcbqs_gb300_peec_desc;
+
+typedef struct pcbqs_gb300_peec pcbqs_gb300_peec;
+
+/* Replaces the LinearOperator `product` of peec_iterative.solve (src/pcbqs/peec_iterative.py:267-278, 322). */
+int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *desc, pcbqs_gb300_peec **op);
+void pcbqs_gb300_peec_destroy(pcbqs_gb300_peec *op);
+/* out = A_s in for k columns, column c at system sys[c] (host array); synchronizes `stream`. */
+int pcbqs_gb300_peec_apply(pcbqs_gb300_peec *op, int k, const int32_t *sys, const double *in, double *out,
+                           void *stream);
+/* Block-Jacobi preconditioner on consecutive blocks of `bs` unknowns: krk (nblk, bs, bs) device array holds the
+ * diagonal blocks of K^T R K; K^T L K and T^T P T blocks are gathered on the device; every (system, block) is
+ * inverted. New in this backend: the reference preconditions with sparse surrogates
+ * (src/pcbqs/peec_iterative.py:19-84, 283-321). */
+int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *op, int32_t bs, const double *krk, void *stream);
+/* Single-precision direct preconditioner: the dense loop/tree system at system index sys, assembled on the device
+ * (K^T L K and T^T P T formed once from the dense L and P; krk the sparse K^T R K as a device CSR n x n), in
+ * complex64 and LU-factored (cuSOLVER getrf). Mirrors MixedLU (src/pcbqs/kernels.py:125-181): a complex64 factor
+ * with the FP64 operator's GMRES on top in place of its refinement loop. */
+int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, int32_t sys, void *stream);
+/* Batched right-preconditioned restarted GMRES on k columns (b, x device; x holds the initial guess), relative
+ * residual tol per column; iterations and residual (host, k) receive each column's Arnoldi steps and true
+ * relative residual; precondition 0 none, 1 block-Jacobi, 2 the single-precision factor (every column uses it).
+ * Status 5 when a column did not converge. Replaces peec_iterative._gmres
+ * (src/pcbqs/peec_iterative.py:100-112) and mqs_iterative._lockstep_gmres (src/pcbqs/mqs_iterative.py:109-170). */
+int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *op, int k, const int32_t *sys, const double *b, double *x, double tol,
+                           int maxiter, int restart, int precondition, int32_t *iterations, double *residual,
+                           void *stream);
+/* A x = b for a dense real symmetric A (n x n, row stride lda) and k complex columns, Jacobi-preconditioned GMRES.
+ * Replaces peec_iterative.potential_solve (src/pcbqs/peec_iterative.py:115-124), used for P^-1 B. */
+int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, const double *b, double *x, double tol,
+                            int maxiter, int restart, int32_t *iterations, double *residual, void *stream);
 
 #ifdef __cplusplus
 }

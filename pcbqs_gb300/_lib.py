@@ -31,12 +31,29 @@ class Geometry(ctypes.Structure):
                 ('qp', c_double_p * 3), ('qw', c_double_p * 3), ('nq', ctypes.c_int32 * 3)]
 
 
+class CsrDesc(ctypes.Structure):
+    """pcbqs_gb300_csr: a device CSR matrix."""
+    _fields_ = [('rows', ctypes.c_int64), ('cols', ctypes.c_int64), ('ptr', c_void_p), ('idx', c_void_p),
+                ('val', c_void_p)]
+
+
+class PeecDesc(ctypes.Structure):
+    """pcbqs_gb300_peec_desc: the loop/tree PEEC operator's device arrays and frequencies."""
+    _fields_ = [('n', ctypes.c_int64), ('nb', ctypes.c_int64), ('ne', ctypes.c_int64), ('nn', ctypes.c_int64),
+                ('K', CsrDesc), ('Kt', CsrDesc), ('T', CsrDesc), ('Tt', CsrDesc), ('R', CsrDesc),
+                ('L', c_void_p), ('ldl', ctypes.c_int64), ('P', c_void_p), ('ldp', ctypes.c_int64),
+                ('is_tree', c_void_p), ('pscale', ctypes.c_double), ('nsys', ctypes.c_int32),
+                ('omega', c_double_p), ('zscale', c_double_p)]
+
+
 # name: (restype, argtypes)
 PROTOTYPES = {
     'pcbqs_gb300_create': (ctypes.c_int, [ctypes.POINTER(Geometry), ctypes.c_int, ctypes.POINTER(c_void_p)]),
     'pcbqs_gb300_destroy': (None, [c_void_p]),
     'pcbqs_gb300_last_error': (ctypes.c_char_p, []),
     'pcbqs_gb300_triangles': (ctypes.c_int32, [c_void_p]),
+    'pcbqs_gb300_kernel_launches': (ctypes.c_int64, []),
+    'pcbqs_gb300_fill_counts': (ctypes.c_int, [c_void_p, c_uint64_p]),
     'pcbqs_gb300_pairs': (ctypes.c_int, [c_void_p, c_int32_p, c_int32_p, c_double_p, c_int32_p, ctypes.c_int64,
                                          ctypes.c_int, c_double_p]),
     'pcbqs_gb300_pairs_device': (ctypes.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_int64,
@@ -54,6 +71,17 @@ PROTOTYPES = {
     'pcbqs_gb300_potential_device': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                                     ctypes.c_int64, ctypes.c_double, c_void_p, ctypes.c_int64,
                                                     c_void_p]),
+    'pcbqs_gb300_peec_create': (ctypes.c_int, [ctypes.POINTER(PeecDesc), ctypes.POINTER(c_void_p)]),
+    'pcbqs_gb300_peec_destroy': (None, [c_void_p]),
+    'pcbqs_gb300_peec_apply': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_peec_block_jacobi': (ctypes.c_int, [c_void_p, ctypes.c_int32, c_void_p, c_void_p]),
+    'pcbqs_gb300_peec_factor': (ctypes.c_int, [c_void_p, ctypes.POINTER(CsrDesc), ctypes.c_int32, c_void_p]),
+    'pcbqs_gb300_peec_gmres': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p, ctypes.c_double,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, c_int32_p, c_double_p,
+                                              c_void_p]),
+    'pcbqs_gb300_dense_gmres': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, ctypes.c_int, c_void_p,
+                                               c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_int32_p,
+                                               c_double_p, c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -63,7 +63,8 @@ def build(force=False, verbose=False, extra=()):
     objects = [BUILD / (s.stem + '.o') for s in sources()]
     if force or jobs or _stale(LIBRARY, objects):
         tmp = LIBRARY.with_suffix('.so.tmp')
-        run([compiler, *ARCH, '-shared', '-o', str(tmp), *map(str, objects)])
+        run([compiler, *ARCH, '-shared', '-o', str(tmp), *map(str, objects), '-lcublas', '-lcusolver',
+             '-Xlinker', f'-rpath={Path(compiler).resolve().parent.parent / "lib64"}'])
         os.replace(tmp, LIBRARY)
     return LIBRARY
 

@@ -1,4 +1,5 @@
 // C ABI (include/pcbqs_gb300.h): device context, geometry upload, and the fill / combine / potential entry points.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -15,10 +16,14 @@
 using namespace pq;
 
 namespace {
-
 thread_local std::string g_error;
+std::atomic<long long> g_launches{0};
+}  // namespace
 
-int fail(int code, const char *fmt, ...) {
+void pq::note_launches(long long count) { g_launches.fetch_add(count, std::memory_order_relaxed); }
+
+// The calling thread's last error message, shared by every entry point of the library.
+int pq::fail(int code, const char *fmt, ...) {
     char buf[512];
     va_list ap;
     va_start(ap, fmt);
@@ -27,6 +32,8 @@ int fail(int code, const char *fmt, ...) {
     g_error = buf;
     return code;
 }
+
+namespace {
 
 int cuda_fail(cudaError_t err, const char *what) {
     return fail(ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
@@ -71,6 +78,7 @@ struct pcbqs_gb300_ctx {
     DevBuf pair_io;         // pair-list staging (host entry point)
     DevBuf planes;          // device moment planes (host fill entry point)
     size_t planes_ld = 0;
+    uint64_t last_counts[2] = {0, 0};   // near pairs of the last fill: level 0, level `outer`
 };
 
 namespace {
@@ -104,6 +112,15 @@ int read_flags(pcbqs_gb300_ctx *c, cudaStream_t stream, int *host2) {
 extern "C" {
 
 const char *pcbqs_gb300_last_error(void) { return g_error.c_str(); }
+
+int64_t pcbqs_gb300_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int pcbqs_gb300_fill_counts(const pcbqs_gb300_ctx *c, uint64_t *counts) {
+    if (!c || !counts) return fail(ERR_ARGUMENT, "fill_counts: null argument");
+    counts[0] = c->last_counts[0];
+    counts[1] = c->last_counts[1];
+    return OK;
+}
 
 int32_t pcbqs_gb300_triangles(const pcbqs_gb300_ctx *ctx) { return ctx ? ctx->g.nt : 0; }
 
@@ -322,6 +339,8 @@ static int fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_on
         if (host[1]) return fail(host[1], "fill: a bounded wait for staged geometry gave up");
         if (host[0]) return fail(ERR_NONFINITE, "non-finite triangle-pair moments from fill backend");
         if (analytic) *analytic = counts[0] + (rule.outer ? counts[1] : 0);
+        c->last_counts[0] = counts[0];
+        c->last_counts[1] = rule.outer ? counts[1] : 0;
         return OK;
     }
     return fail(ERR_MEMORY, "fill: near-pair lists did not fit");

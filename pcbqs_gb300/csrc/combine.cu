@@ -151,6 +151,7 @@ cudaError_t launch_edge_inductance(const EdgeBasis &e, const MomentPlanes &mo, d
     const int64_t ntiles = nb * (nb + 1) / 2;
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms() * 8);
     k_edge_inductance<<<(unsigned)grid, CT_THREADS, 0, stream>>>(e, mo, factor, L, ldl);
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -161,6 +162,7 @@ cudaError_t launch_potential(const NodeGroups &ng, const double *m0, int64_t ldm
     const int64_t ntiles = nb * (nb + 1) / 2;
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms() * 8);
     k_potential<<<(unsigned)grid, CT_THREADS, 0, stream>>>(ng, m0, ldm, factor, P, ldp);
+    note_launches(1);
     return cudaGetLastError();
 }
 

@@ -17,6 +17,12 @@ enum Status : int {
     ERR_TIMEOUT = 6,       // a bounded device wait gave up
 };
 
+// Record an error message for pcbqs_gb300_last_error() and return `code`.
+int fail(int code, const char *fmt, ...);
+
+// Count kernels launched by this library (reported by pcbqs_gb300_kernel_launches()).
+void note_launches(long long count);
+
 // Per-triangle records in HBM. One record per triangle, 16-byte aligned so a tile of consecutive triangles is
 // one contiguous run that a bulk (TMA) copy can stage into shared memory.
 //   FarRec   64 B: the three-point rule's points (x0,y0,x1,y1,x2,y2), area, z

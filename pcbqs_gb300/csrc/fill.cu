@@ -31,7 +31,7 @@ __device__ __forceinline__ void far_moments(const FarRec &a, const FarRec &b, do
         for (int j = 0; j < 3; ++j) {
             const double sx = b.p[2 * j], sy = b.p[2 * j + 1];
             const double dx = x - sx, dy = y - sy;
-            const double g = w / sqrt(dx * dx + dy * dy + d2);
+            const double g = w * rsqrt(dx * dx + dy * dy + d2);
             g_sum += g;
             if (!scalar) { gsx += g * sx; gsy += g * sy; }
         }
@@ -43,6 +43,27 @@ __device__ __forceinline__ void far_moments(const FarRec &a, const FarRec &b, do
         }
     }
     m[0] = m0; m[1] = ro_x; m[2] = ro_y; m[3] = rs_x; m[4] = rs_y; m[5] = rr;
+}
+
+// asinh(s+/r0) - asinh(s-/r0) with s+ = s- + L, r-+ = sqrt(r0^2 + s-+^2), as one logarithm. From
+// asinh(s/r0) = sign(s) log((|s| + r)/r0): both ends on one side of the foot point give a ratio of two sums of
+// positive terms, straddling ends a product over r0^2 -- no term cancels, where the difference of two inverse
+// hyperbolic sines loses the leading digits when s- and s+ are large and close.
+__device__ __forceinline__ double asinh_difference(double sm, double sp, double rm, double rp, double r02) {
+    if (sm >= 0) return log((sp + rp) / (sm + rm));
+    if (sp <= 0) return log((rm - sm) / (rp - sp));
+    return log((sp + rp) * (rm - sm) / r02);
+}
+
+// atan2(t0 s+, r0^2 + |d| r+) - atan2(t0 s-, r0^2 + |d| r-) as one arctangent: both denominators are positive,
+// so each angle lies in (-pi/2, pi/2) and the difference is atan2(y1 x2 - y2 x1, x1 x2 + y1 y2) with no wrap. The
+// cross term y1 x2 - y2 x1 = t0 (L r0^2 + |d| (s+ r- - s- r+)) is formed without cancellation: for ends on one
+// side, s+ r- - s- r+ = r0^2 L (s+ + s-) / (s+ r- + s- r+); for straddling ends both of its terms are positive.
+__device__ __forceinline__ double atan2_difference(double t0, double sm, double sp, double rm, double rp,
+                                                   double r02, double ad, double le) {
+    const double cross = (sm >= 0 || sp <= 0) ? r02 * le * (sp + sm) / (sp * rm + sm * rp) : sp * rm - sm * rp;
+    const double x1 = r02 + ad * rp, x2 = r02 + ad * rm;
+    return atan2(t0 * (le * r02 + ad * cross), x1 * x2 + t0 * t0 * sp * sm);
 }
 
 // Near pairs: for each observation point x_j of triangle a (level-k rule) and each edge e of source triangle b,
@@ -70,9 +91,9 @@ __device__ __forceinline__ void near_moments(const double *obs, const double *wt
             const double t0 = vx * b.un[2 * e] + vy * b.un[2 * e + 1];
             const double r02 = t0 * t0 + d2, r0 = sqrt(r02);
             const double rm = sqrt(r02 + sm * sm), rp = sqrt(r02 + sp * sp);
-            const double lg = r0 > 1e-14 * le ? asinh(sp / r0) - asinh(sm / r0) : 0.0;
+            const double lg = r0 > 1e-14 * le ? asinh_difference(sm, sp, rm, rp, r02) : 0.0;
             double inner = t0 * lg;
-            if (ad > 0) inner -= ad * (atan2(t0 * sp, r02 + ad * rp) - atan2(t0 * sm, r02 + ad * rm));
+            if (ad > 0) inner -= ad * atan2_difference(t0, sm, sp, rm, rp, r02, ad, le);
             i1 += inner;
             if (!scalar) {
                 const double er = 0.5 * (r02 * lg + sp * rp - sm * rm);
@@ -369,13 +390,18 @@ cudaError_t launch_pairs(const Geometry &g, const int32_t *p, const int32_t *q, 
         for (int b = 0; b < 4; ++b) { cursor[b] = run; run += host[b]; }
         cudaMemcpyAsync(count4 + 4, cursor, sizeof(cursor), cudaMemcpyHostToDevice, stream);
         k_kind_scatter<<<blocks, 256, 0, stream>>>(kind, n, count4 + 4, order);
-        if ((int64_t)run < n) k_order_tail<<<blocks, 256, 0, stream>>>(order, (int64_t)run, n);
+        if ((int64_t)run < n) {
+            k_order_tail<<<blocks, 256, 0, stream>>>(order, (int64_t)run, n);
+            note_launches(1);
+        }
+        note_launches(2);
         err = cudaStreamSynchronize(stream);     // `cursor` lives on this stack frame
         if (err != cudaSuccess) return err;
         ord = order;
     }
     k_pairs<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(g, p, q, d, kind, ord, n, scalar, out,
                                                                             nonfinite, invalid);
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -397,6 +423,7 @@ cudaError_t launch_fill(const Geometry &g, const FillPlanes &out, const FillRule
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sm_count() * per_sm);
     cudaMemsetAsync(lists.count, 0, 2 * sizeof(unsigned long long), stream);
     k_fill_tiles<<<(unsigned)grid, FILL_THREADS, smem, stream>>>(g, out, rule, lists, nonfinite, status);
+    note_launches(1);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     return cudaSuccess;
@@ -410,6 +437,7 @@ cudaError_t launch_fill_near(const Geometry &g, const FillPlanes &out, const Fil
     if (rule.outer > 0)
         k_fill_near<<<blocks, threads, 0, stream>>>(g, out, lists.pair[1], lists.count + 1, lists.capacity,
                                                     rule.outer, nonfinite);
+    note_launches(rule.outer > 0 ? 2 : 1);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,440 @@
+// Batched restarted GMRES(m) in complex128 on the device: every column (a frequency and right-hand side) has its
+// own Krylov space, but each Arnoldi step applies the operator once to all active columns, so the dense matrices
+// are read once per step for the whole batch. Right preconditioning; classical Gram-Schmidt applied twice (CGS2:
+// two block passes instead of j dependent ones, orthogonal to working precision like MGS); complex Givens
+// rotations and per-column convergence masks; converged columns drop out (compaction) at each restart; the true
+// residual |b - A x| / |b| decides convergence. All reductions have a fixed order (two-stage sums over a fixed
+// number of row chunks), so results do not depend on scheduling.
+//
+// Reference behaviour (paths within the pcbqs project): mqs_iterative._lockstep_gmres
+// (src/pcbqs/mqs_iterative.py:109-170: per-column Krylov spaces, one product per step, Givens on each column's
+// Hessenberg, convergence |g_{j+1}|/|b| <= tol, compaction at restart), and the acceptance rule of
+// peec_iterative._gmres (src/pcbqs/peec_iterative.py:100-112).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "solve.cuh"
+
+namespace pq {
+
+constexpr int NCHUNK = 64;       // row chunks of the two-stage reductions
+constexpr int RT = 256;          // reduction block size
+
+__device__ __forceinline__ cd cmul(cd a, cd b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ cd cmulc(cd a, cd b) {      // conj(a) * b
+    return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ cd cadd(cd a, cd b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ cd csub(cd a, cd b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+// partial[chunk][i][s] = sum over the chunk's rows of conj(V_i[r,s]) w[r,s]   (grid: NCHUNK x jc)
+__global__ void __launch_bounds__(RT) k_dots_partial(int64_t n, int k, const cd *V, const cd *w, cd *partial) {
+    __shared__ cd acc[RT];
+    const int chunk = blockIdx.x, i = blockIdx.y;
+    const int64_t r0 = n * chunk / NCHUNK, r1 = n * (chunk + 1) / NCHUNK;
+    const cd *Vi = V + (size_t)i * n * k;
+    cd *out = partial + ((size_t)chunk * gridDim.y + i) * k;
+    if (k <= RT) {
+        const int per = RT / k, t = threadIdx.x;
+        cd a = make_double2(0, 0);
+        if (t < per * k) {
+            const int s = t % k, rr = t / k;
+            for (int64_t r = r0 + rr; r < r1; r += per) a = cadd(a, cmulc(Vi[r * k + s], w[r * k + s]));
+        }
+        acc[t] = a;
+        __syncthreads();
+        if (t < k) {
+            cd sum = make_double2(0, 0);
+            for (int q = 0; q < per; ++q) sum = cadd(sum, acc[t + q * k]);
+            out[t] = sum;
+        }
+    } else {
+        for (int s = threadIdx.x; s < k; s += RT) {
+            cd a = make_double2(0, 0);
+            for (int64_t r = r0; r < r1; ++r) a = cadd(a, cmulc(Vi[r * k + s], w[r * k + s]));
+            out[s] = a;
+        }
+    }
+}
+
+// h[i][s] = sum_chunk partial[chunk][i][s], in chunk order.
+__global__ void k_dots_final(int jc, int k, const cd *partial, cd *h) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= jc * k) return;
+    cd sum = make_double2(0, 0);
+    for (int c = 0; c < NCHUNK; ++c) sum = cadd(sum, partial[(size_t)c * jc * k + idx]);
+    h[idx] = sum;
+}
+
+// w[r,s] -= sum_{i<jc} V_i[r,s] h[i][s]
+__global__ void k_orth_update(int64_t n, int k, int jc, const cd *V, const cd *h, cd *w) {
+    const int64_t total = n * k;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(idx % k);
+        cd a = w[idx];
+        for (int i = 0; i < jc; ++i) a = csub(a, cmul(V[(size_t)i * total + idx], h[i * k + s]));
+        w[idx] = a;
+    }
+}
+
+// Column sums of squares, two stages.
+__global__ void __launch_bounds__(RT) k_norm_partial(int64_t n, int k, const cd *x, double *partial) {
+    __shared__ double acc[RT];
+    const int chunk = blockIdx.x;
+    const int64_t r0 = n * chunk / NCHUNK, r1 = n * (chunk + 1) / NCHUNK;
+    double *out = partial + (size_t)chunk * k;
+    if (k <= RT) {
+        const int per = RT / k, t = threadIdx.x;
+        double a = 0;
+        if (t < per * k) {
+            const int s = t % k, rr = t / k;
+            for (int64_t r = r0 + rr; r < r1; r += per) {
+                const cd v = x[r * k + s];
+                a += v.x * v.x + v.y * v.y;
+            }
+        }
+        acc[t] = a;
+        __syncthreads();
+        if (t < k) {
+            double sum = 0;
+            for (int q = 0; q < per; ++q) sum += acc[t + q * k];
+            out[t] = sum;
+        }
+    } else {
+        for (int s = threadIdx.x; s < k; s += RT) {
+            double a = 0;
+            for (int64_t r = r0; r < r1; ++r) {
+                const cd v = x[r * k + s];
+                a += v.x * v.x + v.y * v.y;
+            }
+            out[s] = a;
+        }
+    }
+}
+
+__global__ void k_norm_final(int k, const double *partial, double *norm) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= k) return;
+    double sum = 0;
+    for (int c = 0; c < NCHUNK; ++c) sum += partial[(size_t)c * k + s];
+    norm[s] = sqrt(sum);
+}
+
+// out[:, s] = in[:, s] / norm[s] (norm 0: out = in, a zero column stays zero)
+__global__ void k_divide(int64_t n, int k, const cd *in, const double *norm, cd *out) {
+    const int64_t total = n * k;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const double d = norm[idx % k];
+        const double inv = d > 0 ? 1.0 / d : 1.0;
+        out[idx] = make_double2(in[idx].x * inv, in[idx].y * inv);
+    }
+}
+
+// a[idx] = b[idx] - a[idx]   (residual from a product)
+__global__ void k_rsub(int64_t total, const cd *b, cd *a) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x)
+        a[idx] = csub(b[idx], a[idx]);
+}
+
+__global__ void k_add(int64_t total, const cd *b, cd *a) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x)
+        a[idx] = cadd(a[idx], b[idx]);
+}
+
+// Gather / scatter columns between the full batch (k columns) and the active set (ka columns).
+__global__ void k_gather_cols(int64_t n, int k, int ka, const int *act, const cd *full, cd *compact) {
+    const int64_t total = n * ka;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / ka;
+        const int c = (int)(idx % ka);
+        compact[idx] = full[r * k + act[c]];
+    }
+}
+
+__global__ void k_scatter_cols(int64_t n, int k, int ka, const int *act, const cd *compact, cd *full) {
+    const int64_t total = n * ka;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / ka;
+        const int c = (int)(idx % ka);
+        full[r * k + act[c]] = compact[idx];
+    }
+}
+
+// Start of a cycle: H = 0, g = (beta, 0, ...), done = 0.
+__global__ void k_cycle_start(int m, int k, const double *beta, cd *H, cd *g, int *done, int *last) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int hsize = (m + 1) * m * k;
+    for (int i = idx; i < hsize; i += gridDim.x * blockDim.x) H[i] = make_double2(0, 0);
+    for (int i = idx; i < (m + 1) * k; i += gridDim.x * blockDim.x)
+        g[i] = i < k ? make_double2(beta[i], 0) : make_double2(0, 0);
+    for (int i = idx; i < k; i += gridDim.x * blockDim.x) {
+        done[i] = 0;
+        last[i] = m - 1;
+    }
+}
+
+// Store column j of H: H[i][j] = h1[i] + h2[i] (i <= j), H[j+1][j] = hn.
+__global__ void k_store_column(int m, int k, int j, const cd *h1, const cd *h2, const double *hn, cd *H) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < (j + 1) * k) {
+        const int i = idx / k, s = idx % k;
+        H[((size_t)i * m + j) * k + s] = cadd(h1[idx], h2[idx]);
+    }
+    if (idx < k) H[((size_t)(j + 1) * m + j) * k + idx] = make_double2(hn[idx], 0);
+}
+
+// Givens least squares of step j for every column; convergence |g_{j+1}| / |b| <= tol.
+__global__ void k_givens(int m, int k, int j, cd *H, cd *cs, cd *sn, cd *g, const double *bnorm, double tol,
+                         int *done, int *last, int *its, int *ndone) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= k) return;
+    auto at = [&](int i) -> cd & { return H[((size_t)i * m + j) * k + s]; };
+    for (int i = 0; i < j; ++i) {
+        const cd a = at(i), b = at(i + 1), c = cs[i * k + s], sv = sn[i * k + s];
+        at(i) = cadd(cmulc(c, a), cmulc(sv, b));
+        at(i + 1) = csub(cmul(c, b), cmul(sv, a));
+    }
+    const cd a = at(j), b = at(j + 1);
+    double den = sqrt(a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y);
+    if (!(den > 0)) den = 1;
+    const cd c = make_double2(a.x / den, a.y / den), sv = make_double2(b.x / den, b.y / den);
+    cs[j * k + s] = c;
+    sn[j * k + s] = sv;
+    at(j) = cadd(cmulc(c, a), cmulc(sv, b));
+    at(j + 1) = make_double2(0, 0);
+    const cd gj = g[j * k + s];
+    const cd gn = cmul(sv, gj);
+    g[(j + 1) * k + s] = make_double2(-gn.x, -gn.y);
+    g[j * k + s] = cmulc(c, gj);
+    const bool was = done[s] != 0;
+    const double res = sqrt(gn.x * gn.x + gn.y * gn.y) / bnorm[s];
+    const bool now = !was && res <= tol;
+    if (now) {
+        last[s] = j;
+        done[s] = 1;
+    }
+    if (!was) its[s] += 1;
+    if (done[s]) atomicAdd(ndone, 1);
+}
+
+// Back substitution per column: y = triu(H[:jj,:jj]) \ g[:jj], jj = last + 1 if done else jcur + 1.
+__global__ void k_trisolve(int m, int k, int jcur, const cd *H, const cd *g, const int *done, const int *last,
+                           cd *y) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= k) return;
+    const int jj = done[s] ? last[s] + 1 : jcur + 1;
+    for (int i = m - 1; i >= jj; --i) y[i * k + s] = make_double2(0, 0);
+    for (int i = jj - 1; i >= 0; --i) {
+        cd acc = g[i * k + s];
+        for (int l = i + 1; l < jj; ++l) acc = csub(acc, cmul(H[((size_t)i * m + l) * k + s], y[l * k + s]));
+        const cd d = H[((size_t)i * m + i) * k + s];
+        const double dd = d.x * d.x + d.y * d.y;
+        y[i * k + s] = dd > 0 ? make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd)
+                              : make_double2(0, 0);
+    }
+}
+
+// out[r,s] = sum_{i<jc} V_i[r,s] y[i][s]
+__global__ void k_combine(int64_t n, int k, int jc, const cd *V, const cd *y, cd *out) {
+    const int64_t total = n * k;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(idx % k);
+        cd a = make_double2(0, 0);
+        for (int i = 0; i < jc; ++i) a = cadd(a, cmul(V[(size_t)i * total + idx], y[i * k + s]));
+        out[idx] = a;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+
+static int grid_for(int64_t total) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)sms * 16));
+}
+
+cudaError_t column_norms(int64_t n, int k, const cd *x, double *out, double *scratch, cudaStream_t s) {
+    k_norm_partial<<<NCHUNK, RT, 0, s>>>(n, k, x, scratch);
+    k_norm_final<<<(k + 127) / 128, 128, 0, s>>>(k, scratch, out);
+    return cudaGetLastError();
+}
+
+namespace {
+
+struct Scratch {
+    std::vector<void *> blocks;
+    cudaError_t err = cudaSuccess;
+    template <class T> T *get(size_t count) {
+        void *p = nullptr;
+        if (err == cudaSuccess) err = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (err == cudaSuccess) blocks.push_back(p);
+        return static_cast<T *>(p);
+    }
+    ~Scratch() {
+        for (void *p : blocks) cudaFree(p);
+    }
+};
+
+}  // namespace
+
+cudaError_t gmres_batched(Operator &A, Preconditioner *M, int k, const int32_t *sys_host, const cd *b, cd *x,
+                          const GmresOptions &opt, GmresReport &report, cudaStream_t st) {
+    const int64_t n = A.n();
+    const int m = std::max(1, std::min(opt.restart, opt.maxiter));
+    report.iterations.assign(k, 0);
+    report.residual.assign(k, 0.0);
+    report.cycles = 0;
+    if (k <= 0 || n <= 0) return cudaSuccess;
+    Scratch mem;
+    const size_t nk = (size_t)n * k;
+    cd *V = mem.get<cd>((size_t)(m + 1) * nk);
+    cd *bc = mem.get<cd>(nk), *xc = mem.get<cd>(nk), *r = mem.get<cd>(nk), *w = mem.get<cd>(nk);
+    cd *z = mem.get<cd>(nk);
+    cd *H = mem.get<cd>((size_t)(m + 1) * m * k), *cs = mem.get<cd>((size_t)m * k), *sn = mem.get<cd>((size_t)m * k);
+    cd *g = mem.get<cd>((size_t)(m + 1) * k), *y = mem.get<cd>((size_t)m * k);
+    cd *h1 = mem.get<cd>((size_t)(m + 1) * k), *h2 = mem.get<cd>((size_t)(m + 1) * k);
+    cd *dpart = mem.get<cd>((size_t)NCHUNK * (m + 1) * k);
+    double *npart = mem.get<double>((size_t)NCHUNK * k), *norm = mem.get<double>(k), *bnorm_all = mem.get<double>(k);
+    double *bnorm = mem.get<double>(k);
+    int *done = mem.get<int>(k), *last = mem.get<int>(k), *its = mem.get<int>(k), *ndone = mem.get<int>(1);
+    int *act_dev = mem.get<int>(k), *sys_dev = mem.get<int>(k);
+    if (mem.err != cudaSuccess) return mem.err;
+    int launches = 0;
+    auto apply = [&](int ka, const cd *in, cd *out) { return A.apply(ka, sys_dev, in, out, st); };
+    auto precond = [&](int ka, const cd *in, cd *out) -> cudaError_t {
+        if (M) return M->apply(ka, sys_dev, in, out, st);
+        return cudaMemcpyAsync(out, in, sizeof(cd) * n * ka, cudaMemcpyDeviceToDevice, st);
+    };
+    cudaError_t err;
+    if ((err = column_norms(n, k, b, bnorm_all, npart, st))) return err;
+    launches += 2;
+    std::vector<double> bn(k), rn(k);
+    cudaMemcpyAsync(bn.data(), bnorm_all, sizeof(double) * k, cudaMemcpyDeviceToHost, st);
+    if ((err = cudaStreamSynchronize(st))) return err;
+    std::vector<int> act(k), its_host(k, 0);
+    for (int c = 0; c < k; ++c) act[c] = c;
+    // Columns whose right-hand side vanishes are solved by x = 0.
+    std::vector<int> keep;
+    for (int c : act) {
+        if (bn[c] > 0) keep.push_back(c);
+        else report.residual[c] = 0.0;
+    }
+    act.swap(keep);
+    std::vector<int> sys_act, its_act;
+    bool first = true;
+    while (!act.empty()) {
+        const int ka = (int)act.size();
+        sys_act.resize(ka);
+        std::vector<double> bn_act(ka);
+        for (int c = 0; c < ka; ++c) {
+            sys_act[c] = sys_host[act[c]];
+            bn_act[c] = bn[act[c]];
+        }
+        cudaMemcpyAsync(act_dev, act.data(), sizeof(int) * ka, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(sys_dev, sys_act.data(), sizeof(int) * ka, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(bnorm, bn_act.data(), sizeof(double) * ka, cudaMemcpyHostToDevice, st);
+        const int gsz = grid_for((int64_t)n * ka);
+        k_gather_cols<<<gsz, 256, 0, st>>>(n, k, ka, act_dev, b, bc);
+        k_gather_cols<<<gsz, 256, 0, st>>>(n, k, ka, act_dev, x, xc);
+        launches += 2;
+        // r = b - A x
+        if ((err = apply(ka, xc, r))) return err;
+        k_rsub<<<gsz, 256, 0, st>>>((int64_t)n * ka, bc, r);
+        if ((err = column_norms(n, ka, r, norm, npart, st))) return err;
+        launches += 3;
+        cudaMemcpyAsync(rn.data(), norm, sizeof(double) * ka, cudaMemcpyDeviceToHost, st);
+        if ((err = cudaStreamSynchronize(st))) return err;
+        if (!first) {
+            // The true residual after the previous cycle decides which columns stay.
+            std::vector<int> next;
+            for (int c = 0; c < ka; ++c) {
+                const double res = rn[c] / bn_act[c];
+                report.residual[act[c]] = res;
+                if (res > opt.tol && its_host[act[c]] < opt.maxiter) next.push_back(act[c]);
+            }
+            if (next.size() != act.size()) {
+                act.swap(next);
+                continue;      // re-gather the smaller active set
+            }
+        } else {
+            std::vector<int> next;
+            for (int c = 0; c < ka; ++c) {
+                const double res = rn[c] / bn_act[c];
+                report.residual[act[c]] = res;
+                if (res > opt.tol) next.push_back(act[c]);
+            }
+            first = false;
+            if (next.size() != act.size()) {
+                act.swap(next);
+                continue;
+            }
+        }
+        int max_its = 0;
+        for (int c : act) max_its = std::max(max_its, its_host[c]);
+        const int steps = std::min(m, opt.maxiter - max_its);
+        if (steps <= 0) break;
+        ++report.cycles;
+        // V0 = r / |r|, g = (|r|, 0, ...)
+        k_divide<<<gsz, 256, 0, st>>>(n, ka, r, norm, V);
+        k_cycle_start<<<grid_for((int64_t)(m + 1) * m * ka), 256, 0, st>>>(m, ka, norm, H, g, done, last);
+        cudaMemsetAsync(its, 0, sizeof(int) * ka, st);
+        launches += 2;
+        int jcur = 0;
+        for (int j = 0; j < steps; ++j) {
+            jcur = j;
+            cd *Vj = V + (size_t)j * n * ka;
+            if ((err = precond(ka, Vj, z))) return err;
+            if ((err = apply(ka, z, w))) return err;
+            const int jc = j + 1;
+            dim3 dgrid(NCHUNK, jc);
+            k_dots_partial<<<dgrid, RT, 0, st>>>(n, ka, V, w, dpart);
+            k_dots_final<<<(jc * ka + 127) / 128, 128, 0, st>>>(jc, ka, dpart, h1);
+            k_orth_update<<<gsz, 256, 0, st>>>(n, ka, jc, V, h1, w);
+            k_dots_partial<<<dgrid, RT, 0, st>>>(n, ka, V, w, dpart);
+            k_dots_final<<<(jc * ka + 127) / 128, 128, 0, st>>>(jc, ka, dpart, h2);
+            k_orth_update<<<gsz, 256, 0, st>>>(n, ka, jc, V, h2, w);
+            column_norms(n, ka, w, norm, npart, st);
+            k_divide<<<gsz, 256, 0, st>>>(n, ka, w, norm, V + (size_t)(j + 1) * n * ka);
+            k_store_column<<<((jc + 1) * ka + 127) / 128, 128, 0, st>>>(m, ka, j, h1, h2, norm, H);
+            cudaMemsetAsync(ndone, 0, sizeof(int), st);
+            k_givens<<<(ka + 127) / 128, 128, 0, st>>>(m, ka, j, H, cs, sn, g, bnorm, opt.tol, done, last, its,
+                                                       ndone);
+            launches += 10;
+            int nd = 0;
+            cudaMemcpyAsync(&nd, ndone, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if ((err = cudaStreamSynchronize(st))) return err;
+            if (nd == ka) break;
+        }
+        // x += M^-1 (V y)
+        k_trisolve<<<(ka + 127) / 128, 128, 0, st>>>(m, ka, jcur, H, g, done, last, y);
+        k_combine<<<gsz, 256, 0, st>>>(n, ka, jcur + 1, V, y, w);
+        if ((err = precond(ka, w, z))) return err;
+        k_add<<<gsz, 256, 0, st>>>((int64_t)n * ka, z, xc);
+        k_scatter_cols<<<gsz, 256, 0, st>>>(n, k, ka, act_dev, xc, x);
+        launches += 4;
+        its_act.resize(ka);
+        cudaMemcpyAsync(its_act.data(), its, sizeof(int) * ka, cudaMemcpyDeviceToHost, st);
+        if ((err = cudaStreamSynchronize(st))) return err;
+        for (int c = 0; c < ka; ++c) its_host[act[c]] += its_act[c];
+    }
+    report.launches = launches;
+    note_launches(launches);
+    for (int c = 0; c < k; ++c) report.iterations[c] = its_host[c];
+    return cudaGetLastError();
+}
+
+}  // namespace pq

@@ -1,0 +1,751 @@
+// The compressed-free PEEC operator in loop/tree coordinates, its block-Jacobi preconditioner, a dense symmetric
+// operator (for P^-1 B), and their C ABI.
+//
+// Operator (src/pcbqs/peec_iterative.py:267-278): for system s at angular frequency w_s,
+//   branch = K (D_s y),  D_s = diag(1 on loop unknowns, j w_s alpha_s on tree unknowns), alpha_s = zscale_s/pscale
+//   out    = K^T (R branch + j w_s L branch) / zscale_s + T^T P T y / pscale
+// with K (branches x unknowns) the loop/tree basis, T = A K_tree (nodes x unknowns, zero on loop columns), R the
+// sparse sheet resistance and L, P the dense partial-inductance and potential matrices on the device. The two dense
+// products run as plain FP64 GEMMs (cuBLAS), every sparse product and combination in this file's kernels.
+//
+// Block-Jacobi: the unknowns are ordered so that consecutive runs of `bs` are geometric clusters; each diagonal
+// block of the operator, (K^T R K + j w K^T L K)_blk D_blk / zscale + (T^T P T)_blk / pscale, is formed on the
+// device (K^T L K and T^T P T blocks gathered from the dense matrices), inverted (Gauss-Jordan with partial
+// pivoting), and applied to every column of its system.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include "../../include/pcbqs_gb300.h"
+#include "common.cuh"
+#include "solve.cuh"
+
+namespace pq {
+
+struct Csr {
+    int64_t rows = 0, cols = 0;
+    const int64_t *ptr = nullptr;
+    const int32_t *idx = nullptr;
+    const double *val = nullptr;
+};
+
+// Y[r, s] = (acc ? Y[r, s] : 0) + scale[sys[s]] * sum_j val_j X[idx_j, s]   (scale nullable: 1)
+__global__ void k_spmm(Csr S, int k, const cd *X, cd *Y, const double *scale, const int *sys, int accumulate) {
+    const int64_t total = S.rows * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const int s = (int)(t % k);
+        double re = 0, im = 0;
+        for (int64_t j = S.ptr[r]; j < S.ptr[r + 1]; ++j) {
+            const double v = S.val[j];
+            const cd x = X[(int64_t)S.idx[j] * k + s];
+            re += v * x.x;
+            im += v * x.y;
+        }
+        if (scale) {
+            const double f = scale[sys[s]];
+            re *= f;
+            im *= f;
+        }
+        if (accumulate) {
+            Y[t].x += re;
+            Y[t].y += im;
+        } else {
+            Y[t] = make_double2(re, im);
+        }
+    }
+}
+
+// U = D_s Y: tree rows times j w_s alpha_s.
+__global__ void k_tree_scale(int64_t n, int k, const int8_t *is_tree, const double *walpha, const int *sys,
+                             const cd *Y, cd *U) {
+    const int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const cd y = Y[t];
+        if (is_tree[r]) {
+            const double f = walpha[sys[(int)(t % k)]];     // j f y = (-f y.im, f y.re)
+            U[t] = make_double2(-f * y.y, f * y.x);
+        } else {
+            U[t] = y;
+        }
+    }
+}
+
+// V[e, s] = sum_f R[e, f] B[f, s] + j w_s LB[e, s] for copper rows e < ne; other passive rows (lumped parts with no
+// impedance here) are zero.
+__global__ void k_impedance(Csr R, int64_t nb, int k, const cd *B, const cd *LB, const double *omega, const int *sys,
+                            cd *V) {
+    const int64_t total = nb * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t / k;
+        const int s = (int)(t % k);
+        double re = 0, im = 0;
+        if (e < R.rows) {
+            for (int64_t j = R.ptr[e]; j < R.ptr[e + 1]; ++j) {
+                const cd b = B[(int64_t)R.idx[j] * k + s];
+                re += R.val[j] * b.x;
+                im += R.val[j] * b.y;
+            }
+            const double w = omega[sys[s]];
+            const cd lb = LB[t];
+            re -= w * lb.y;
+            im += w * lb.x;
+        }
+        V[t] = make_double2(re, im);
+    }
+}
+
+// Diagonal blocks of S^T M S for a dense symmetric M: out[b][i][j] = sum_{e in col i} sum_{f in col j}
+// S_ei S_fj M[e, f], columns of S given as rows of S^T (CSR St). One CTA per block.
+__global__ void k_block_gather(int64_t n, int bs, Csr St, const double *M, int64_t ldm, double *out) {
+    const int64_t b = blockIdx.x;
+    const int64_t c0 = b * bs;
+    for (int t = threadIdx.x; t < bs * bs; t += blockDim.x) {
+        const int i = t / bs, j = t % bs;
+        const int64_t ci = c0 + i, cj = c0 + j;
+        double acc = 0;
+        if (ci < n && cj < n) {
+            for (int64_t a = St.ptr[ci]; a < St.ptr[ci + 1]; ++a) {
+                const double sa = St.val[a];
+                const double *row = M + (int64_t)St.idx[a] * ldm;
+                double part = 0;
+                for (int64_t c = St.ptr[cj]; c < St.ptr[cj + 1]; ++c) part += St.val[c] * row[St.idx[c]];
+                acc += sa * part;
+            }
+        }
+        out[(b * bs + i) * bs + j] = acc;
+    }
+}
+
+// Form and invert every (system, block): A = (KRK + j w KLK) D / zscale + TPT / pscale; padding rows beyond n
+// are identity. Gauss-Jordan with partial pivoting on [A | I] in shared memory; one warp per matrix row group.
+__global__ void k_block_invert(int64_t n, int bs, int64_t nblk, const double *krk, const double *klk,
+                               const double *tpt, const int8_t *is_tree, const double *omega, const double *zscale,
+                               double pscale, cd *inv, int *singular) {
+    extern __shared__ cd aug[];     // bs x 2bs
+    const int64_t b = blockIdx.x;
+    const int s = blockIdx.y;
+    const int w2 = 2 * bs;
+    const double w = omega[s], zs = zscale[s], alpha = zs / pscale;
+    const int64_t c0 = b * bs;
+    for (int t = threadIdx.x; t < bs * w2; t += blockDim.x) {
+        const int i = t / w2, j = t % w2;
+        cd v = make_double2(0, 0);
+        if (j < bs) {
+            const int64_t ci = c0 + i, cj = c0 + j;
+            if (ci < n && cj < n) {
+                const size_t at = (b * bs + i) * bs + j;
+                double re = krk[at] / zs, im = w * klk[at] / zs;
+                if (is_tree[cj]) {       // column scaled by j w alpha
+                    const double f = w * alpha;
+                    const double r2 = -f * im, i2 = f * re;
+                    re = r2;
+                    im = i2;
+                }
+                if (is_tree[ci] && is_tree[cj]) re += tpt[at] / pscale;
+                v = make_double2(re, im);
+            } else if (i == j) {
+                v = make_double2(1, 0);
+            }
+        } else {
+            v = make_double2(j - bs == i ? 1 : 0, 0);
+        }
+        aug[t] = v;
+    }
+    __syncthreads();
+    __shared__ int piv;
+    for (int c = 0; c < bs; ++c) {
+        if (threadIdx.x == 0) {
+            int best = c;
+            double bv = -1;
+            for (int r = c; r < bs; ++r) {
+                const cd a = aug[r * w2 + c];
+                const double m = a.x * a.x + a.y * a.y;
+                if (m > bv) { bv = m; best = r; }
+            }
+            piv = best;
+            if (!(bv > 0)) *singular = 1;
+        }
+        __syncthreads();
+        const int p = piv;
+        if (p != c)
+            for (int j = threadIdx.x; j < w2; j += blockDim.x) {
+                const cd tmp = aug[c * w2 + j];
+                aug[c * w2 + j] = aug[p * w2 + j];
+                aug[p * w2 + j] = tmp;
+            }
+        __syncthreads();
+        const cd d = aug[c * w2 + c];
+        const double dd = d.x * d.x + d.y * d.y;
+        const cd dinv = dd > 0 ? make_double2(d.x / dd, -d.y / dd) : make_double2(0, 0);
+        __syncthreads();
+        for (int j = threadIdx.x; j < w2; j += blockDim.x) {
+            const cd a = aug[c * w2 + j];
+            aug[c * w2 + j] = make_double2(a.x * dinv.x - a.y * dinv.y, a.x * dinv.y + a.y * dinv.x);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < bs * w2; t += blockDim.x) {
+            const int r = t / w2, j = t % w2;
+            if (r == c) continue;
+            const cd f = aug[r * w2 + c];
+            const cd pv = aug[c * w2 + j];
+            if (j != c) {
+                aug[t].x -= f.x * pv.x - f.y * pv.y;
+                aug[t].y -= f.x * pv.y + f.y * pv.x;
+            }
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < bs; r += blockDim.x)
+            if (r != c) aug[r * w2 + c] = make_double2(0, 0);
+        __syncthreads();
+    }
+    cd *out = inv + ((size_t)s * nblk + b) * bs * bs;
+    for (int t = threadIdx.x; t < bs * bs; t += blockDim.x) out[t] = aug[(t / bs) * w2 + bs + t % bs];
+}
+
+// out[r, s] = sum_{c in block(r)} Inv[sys s][blk][r_l][c_l] in[c, s]
+__global__ void k_block_apply(int64_t n, int bs, int64_t nblk, int k, const cd *inv, const int *sys, const cd *in,
+                              cd *out) {
+    const int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const int s = (int)(t % k);
+        const int64_t b = r / bs;
+        const int rl = (int)(r - b * bs);
+        const cd *M = inv + (((size_t)sys[s] * nblk + b) * bs + rl) * bs;
+        const int64_t c0 = b * bs;
+        const int cn = (int)std::min<int64_t>(bs, n - c0);
+        double re = 0, im = 0;
+        for (int c = 0; c < cn; ++c) {
+            const cd m = M[c], x = in[(c0 + c) * k + s];
+            re += m.x * x.x - m.y * x.y;
+            im += m.x * x.y + m.y * x.x;
+        }
+        out[t] = make_double2(re, im);
+    }
+}
+
+// Jacobi: out = in / d
+__global__ void k_diag_apply(int64_t n, int k, const double *d, const cd *in, cd *out) {
+    const int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const double f = 1.0 / d[t / k];
+        out[t] = make_double2(in[t].x * f, in[t].y * f);
+    }
+}
+
+__global__ void k_diag_extract(int64_t n, const double *A, int64_t lda, double *d) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = fabs(A[i * lda + i]);
+        d[i] = v > 0 ? A[i * lda + i] : 1.0;
+    }
+}
+
+static int grid_of(int64_t total) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)sms * 16));
+}
+
+// Real symmetric M (ld) times complex X (rows x k) as one GEMM on the real view: C (rows x 2k row-major).
+static cublasStatus_t gemm_real_sym(cublasHandle_t h, int64_t rows, int k, const double *M, int64_t ld,
+                                    const cd *X, cd *C) {
+    const double one = 1.0, zero = 0.0;
+    return cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, 2 * k, (int)rows, (int)rows, &one,
+                       reinterpret_cast<const double *>(X), 2 * k, M, (int)ld, &zero, reinterpret_cast<double *>(C),
+                       2 * k);
+}
+
+template <class T> static cudaError_t dev_alloc(T **p, size_t count) {
+    return cudaMalloc(reinterpret_cast<void **>(p), std::max<size_t>(count, 1) * sizeof(T));
+}
+
+struct PeecOp : Operator {
+    int64_t n_ = 0, nb = 0, ne = 0, nn = 0;
+    Csr K, Kt, T, Tt, R;
+    const double *L = nullptr, *P = nullptr;
+    int64_t ldl = 0, ldp = 0;
+    const int8_t *is_tree = nullptr;
+    double pscale = 1;
+    int nsys = 0;
+    double *omega = nullptr, *zscale = nullptr, *walpha = nullptr, *inv_z = nullptr, *inv_p = nullptr;
+    cublasHandle_t blas = nullptr;
+    int cap = 0;               // columns the scratch holds
+    cd *u = nullptr, *branch = nullptr, *lb = nullptr, *v = nullptr, *tq = nullptr, *pq = nullptr;
+    int64_t launches = 0;
+
+    int64_t n() const override { return n_; }
+
+    cudaError_t reserve(int k) {
+        if (k <= cap) return cudaSuccess;
+        for (cd *p : {u, branch, lb, v, tq, pq}) cudaFree(p);
+        u = branch = lb = v = tq = pq = nullptr;
+        cudaError_t e;
+        if ((e = dev_alloc(&u, (size_t)n_ * k)) || (e = dev_alloc(&branch, (size_t)nb * k)) ||
+            (e = dev_alloc(&lb, (size_t)ne * k)) || (e = dev_alloc(&v, (size_t)nb * k)) ||
+            (e = dev_alloc(&tq, (size_t)nn * k)) || (e = dev_alloc(&pq, (size_t)nn * k)))
+            return e;
+        cap = k;
+        return cudaSuccess;
+    }
+
+    cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) override {
+        cudaError_t e = reserve(k);
+        if (e) return e;
+        cublasSetStream(blas, s);
+        k_tree_scale<<<grid_of(n_ * k), 256, 0, s>>>(n_, k, is_tree, walpha, sys, in, u);
+        k_spmm<<<grid_of(nb * k), 256, 0, s>>>(K, k, u, branch, nullptr, sys, 0);
+        if (gemm_real_sym(blas, ne, k, L, ldl, branch, lb) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+        k_impedance<<<grid_of(nb * k), 256, 0, s>>>(R, nb, k, branch, lb, omega, sys, v);
+        k_spmm<<<grid_of(n_ * k), 256, 0, s>>>(Kt, k, v, out, inv_z, sys, 0);
+        if (nn > 0) {
+            k_spmm<<<grid_of(nn * k), 256, 0, s>>>(T, k, in, tq, nullptr, sys, 0);
+            if (gemm_real_sym(blas, nn, k, P, ldp, tq, pq) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+            k_spmm<<<grid_of(n_ * k), 256, 0, s>>>(Tt, k, pq, out, inv_p, sys, 1);
+        }
+        launches += nn > 0 ? 6 : 3;
+        note_launches(nn > 0 ? 6 : 3);
+        return cudaGetLastError();
+    }
+
+    ~PeecOp() override {
+        for (cd *p : {u, branch, lb, v, tq, pq}) cudaFree(p);
+        for (double *p : {omega, zscale, walpha, inv_z, inv_p}) cudaFree(p);
+        if (blas) cublasDestroy(blas);
+    }
+};
+
+struct BlockJacobi : Preconditioner {
+    int64_t n = 0, nblk = 0;
+    int bs = 32;
+    cd *inv = nullptr;
+    ~BlockJacobi() override { cudaFree(inv); }
+    cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) override {
+        k_block_apply<<<grid_of(n * k), 256, 0, s>>>(n, bs, nblk, k, inv, sys, in, out);
+        note_launches(1);
+        return cudaGetLastError();
+    }
+};
+
+// ---- dense loop/tree system and its single-precision LU (the MixedLU precedent, src/pcbqs/kernels.py:125-181) ----
+
+// out[j, c] = sum_{a in row j of St} St.val[a] M[St.idx[a], c]  for c < ncols: rows of M combined along the columns of
+// S (St = S^T in CSR). Grid: (column chunks, rows j).
+__global__ void k_rows_combine(Csr St, const double *M, int64_t ldm, int64_t ncols, double *out, int64_t ldo) {
+    const int64_t j = blockIdx.y;
+    const int64_t a0 = St.ptr[j], a1 = St.ptr[j + 1];
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncols; c += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0;
+        for (int64_t a = a0; a < a1; ++a) acc += St.val[a] * M[(int64_t)St.idx[a] * ldm + c];
+        out[j * ldo + c] = acc;
+    }
+}
+
+// out[j, i] = sum_{a in row i of St} St.val[a] W[j, St.idx[a]]: (W S) with S given by St. Grid: (i chunks, rows j).
+__global__ void k_gather_mult(Csr St, const double *W, int64_t ldw, int64_t n, double *out, int64_t ldo) {
+    const int64_t j = blockIdx.y;
+    const double *row = W + j * ldw;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0;
+        for (int64_t a = St.ptr[i]; a < St.ptr[i + 1]; ++a) acc += St.val[a] * row[St.idx[a]];
+        out[j * ldo + i] = acc;
+    }
+}
+
+// A[i, j] = (j w KLK[i,j]) d_j / zs + TPT[i,j] / ps as complex64, d_j = 1 (loop) or j w alpha (tree).
+__global__ void k_assemble_c64(int64_t n, const double *klk, const double *tpt, const int8_t *is_tree, double w,
+                               double zs, double ps, float2 *A) {
+    const int64_t total = n * n;
+    const double f = w * zs / ps;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / n, j = t % n;
+        double re = 0, im = w * klk[t] / zs;
+        if (is_tree[j]) {            // times j f
+            const double r2 = -f * im;
+            im = f * re;
+            re = r2;
+        }
+        if (is_tree[i] && is_tree[j]) re += tpt[t] / ps;
+        A[t] = make_float2((float)re, (float)im);
+    }
+}
+
+// A[i, j] += KRK[i, j] d_j / zs for the sparse K^T R K.
+__global__ void k_add_krk_c64(Csr S, const int8_t *is_tree, double w, double zs, double ps, float2 *A) {
+    const double f = w * zs / ps;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.rows; i += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t a = S.ptr[i]; a < S.ptr[i + 1]; ++a) {
+            const int64_t j = S.idx[a];
+            const double v = S.val[a] / zs;
+            float2 &e = A[i * S.cols + j];
+            if (is_tree[j]) e.y += (float)(f * v);
+            else e.x += (float)v;
+        }
+}
+
+// Row-major (n, k) complex128 <-> column-major (n, k) complex64.
+__global__ void k_to_c64_cols(int64_t n, int k, const cd *in, float2 *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const int s = (int)(t % k);
+        out[(int64_t)s * n + r] = make_float2((float)in[t].x, (float)in[t].y);
+    }
+}
+
+__global__ void k_from_c64_cols(int64_t n, int k, const float2 *in, cd *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const int s = (int)(t % k);
+        const float2 v = in[(int64_t)s * n + r];
+        out[t] = make_double2(v.x, v.y);
+    }
+}
+
+struct LuPrecond : Preconditioner {
+    int64_t n = 0;
+    float2 *lu = nullptr;        // complex64 factor of the row-major system (the transpose, column-major)
+    int *ipiv = nullptr, *info = nullptr;
+    float2 *work = nullptr;      // right-hand sides, column-major
+    int cap = 0;
+    cusolverDnHandle_t solver = nullptr;
+    ~LuPrecond() override {
+        cudaFree(lu);
+        cudaFree(ipiv);
+        cudaFree(info);
+        cudaFree(work);
+        if (solver) cusolverDnDestroy(solver);
+    }
+    cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        if (k > cap) {
+            cudaFree(work);
+            work = nullptr;
+            cudaError_t e = dev_alloc(&work, (size_t)n * k);
+            if (e) return e;
+            cap = k;
+        }
+        cusolverDnSetStream(solver, s);
+        k_to_c64_cols<<<grid_of(n * k), 256, 0, s>>>(n, k, in, work);
+        if (cusolverDnCgetrs(solver, CUBLAS_OP_T, (int)n, k, reinterpret_cast<cuComplex *>(lu), (int)n, ipiv,
+                             reinterpret_cast<cuComplex *>(work), (int)n, info) != CUSOLVER_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        k_from_c64_cols<<<grid_of(n * k), 256, 0, s>>>(n, k, work, out);
+        note_launches(2);
+        return cudaGetLastError();
+    }
+};
+
+struct DenseSym : Operator {
+    int64_t n_ = 0, ld = 0;
+    const double *A = nullptr;
+    cublasHandle_t blas = nullptr;
+    int64_t n() const override { return n_; }
+    cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        cublasSetStream(blas, s);
+        if (gemm_real_sym(blas, n_, k, A, ld, in, out) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+        return cudaSuccess;
+    }
+};
+
+struct Jacobi : Preconditioner {
+    int64_t n = 0;
+    double *d = nullptr;
+    cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        k_diag_apply<<<grid_of(n * k), 256, 0, s>>>(n, k, d, in, out);
+        note_launches(1);
+        return cudaGetLastError();
+    }
+};
+
+}  // namespace pq
+
+using namespace pq;
+
+struct pcbqs_gb300_peec {
+    PeecOp op;
+    BlockJacobi *bj = nullptr;
+    LuPrecond *lu = nullptr;
+    double *klk = nullptr, *tpt = nullptr;   // dense K^T L K and T^T P T (n x n), made once for the factors
+    ~pcbqs_gb300_peec() {
+        delete bj;
+        delete lu;
+        cudaFree(klk);
+        cudaFree(tpt);
+    }
+};
+
+namespace {
+#define pfail pq::fail
+Csr csr_of(const pcbqs_gb300_csr &c) {
+    Csr out;
+    out.rows = c.rows;
+    out.cols = c.cols;
+    out.ptr = c.ptr;
+    out.idx = c.idx;
+    out.val = c.val;
+    return out;
+}
+}  // namespace
+
+extern "C" {
+
+int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *d, pcbqs_gb300_peec **out) {
+    if (!d || !out) return pfail(ERR_ARGUMENT, "peec_create: null argument");
+    *out = nullptr;
+    if (d->n <= 0 || d->nb <= 0 || d->ne < 0 || d->ne > d->nb || d->nn < 0 || d->nsys <= 0 || !d->omega ||
+        !d->zscale || !d->L || !d->is_tree || (d->nn > 0 && !d->P) || !(d->pscale > 0))
+        return pfail(ERR_ARGUMENT, "peec_create: invalid sizes or arrays");
+    if (d->K.rows != d->nb || d->K.cols != d->n || d->Kt.rows != d->n || d->Kt.cols != d->nb ||
+        d->R.rows != d->ne || (d->nn > 0 && (d->T.rows != d->nn || d->T.cols != d->n || d->Tt.rows != d->n)))
+        return pfail(ERR_ARGUMENT, "peec_create: sparse shapes do not match");
+    auto *h = new (std::nothrow) pcbqs_gb300_peec();
+    if (!h) return pfail(ERR_MEMORY, "peec_create: host allocation");
+    PeecOp &op = h->op;
+    op.n_ = d->n; op.nb = d->nb; op.ne = d->ne; op.nn = d->nn;
+    op.K = csr_of(d->K); op.Kt = csr_of(d->Kt); op.T = csr_of(d->T); op.Tt = csr_of(d->Tt); op.R = csr_of(d->R);
+    op.L = d->L; op.ldl = d->ldl; op.P = d->P; op.ldp = d->ldp; op.is_tree = d->is_tree; op.pscale = d->pscale;
+    op.nsys = d->nsys;
+    std::vector<double> w(d->nsys), z(d->nsys), wa(d->nsys), iz(d->nsys), ip(d->nsys, 1.0 / d->pscale);
+    for (int s = 0; s < d->nsys; ++s) {
+        w[s] = d->omega[s];
+        z[s] = d->zscale[s];
+        wa[s] = w[s] * z[s] / d->pscale;
+        iz[s] = 1.0 / z[s];
+    }
+    cudaError_t e;
+    if ((e = dev_alloc(&op.omega, d->nsys)) || (e = dev_alloc(&op.zscale, d->nsys)) ||
+        (e = dev_alloc(&op.walpha, d->nsys)) || (e = dev_alloc(&op.inv_z, d->nsys)) ||
+        (e = dev_alloc(&op.inv_p, d->nsys))) {
+        delete h;
+        return pfail(ERR_MEMORY, "peec_create: %s", cudaGetErrorString(e));
+    }
+    cudaMemcpy(op.omega, w.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
+    cudaMemcpy(op.zscale, z.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
+    cudaMemcpy(op.walpha, wa.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
+    cudaMemcpy(op.inv_z, iz.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
+    cudaMemcpy(op.inv_p, ip.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
+    if (cublasCreate(&op.blas) != CUBLAS_STATUS_SUCCESS) {
+        delete h;
+        return pfail(ERR_CUDA, "peec_create: cuBLAS handle");
+    }
+    *out = h;
+    return OK;
+}
+
+void pcbqs_gb300_peec_destroy(pcbqs_gb300_peec *h) { delete h; }
+
+int pcbqs_gb300_peec_apply(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, const double *in, double *out,
+                           void *stream) {
+    if (!h || k <= 0 || !sys_host || !in || !out) return pfail(ERR_ARGUMENT, "peec_apply: invalid argument");
+    for (int s = 0; s < k; ++s)
+        if (sys_host[s] < 0 || sys_host[s] >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_apply: system index");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int *sys = nullptr;
+    if (dev_alloc(&sys, k)) return pfail(ERR_MEMORY, "peec_apply: allocation");
+    cudaMemcpyAsync(sys, sys_host, sizeof(int) * k, cudaMemcpyHostToDevice, st);
+    cudaError_t e = h->op.apply(k, sys, reinterpret_cast<const cd *>(in), reinterpret_cast<cd *>(out), st);
+    if (!e) e = cudaStreamSynchronize(st);
+    cudaFree(sys);
+    if (e) return pfail(ERR_CUDA, "peec_apply: %s", cudaGetErrorString(e));
+    return OK;
+}
+
+int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double *krk, void *stream) {
+    if (!h || bs <= 0 || bs > 64 || !krk) return pfail(ERR_ARGUMENT, "block_jacobi: invalid argument");
+    PeecOp &op = h->op;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t nblk = (op.n_ + bs - 1) / bs;
+    const size_t bsz = (size_t)nblk * bs * bs;
+    double *klk = nullptr, *tpt = nullptr;
+    int *singular = nullptr;
+    auto *bj = new (std::nothrow) BlockJacobi();
+    if (!bj) return pfail(ERR_MEMORY, "block_jacobi: host allocation");
+    bj->n = op.n_; bj->nblk = nblk; bj->bs = bs;
+    cudaError_t e;
+    if ((e = dev_alloc(&klk, bsz)) || (e = dev_alloc(&tpt, bsz)) || (e = dev_alloc(&singular, 1)) ||
+        (e = dev_alloc(&bj->inv, (size_t)op.nsys * bsz))) {
+        cudaFree(klk); cudaFree(tpt); cudaFree(singular);
+        delete bj;
+        return pfail(ERR_MEMORY, "block_jacobi: %s", cudaGetErrorString(e));
+    }
+    cudaMemsetAsync(singular, 0, sizeof(int), st);
+    cudaMemsetAsync(tpt, 0, sizeof(double) * bsz, st);
+    k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Kt, op.L, op.ldl, klk);
+    if (op.nn > 0) k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Tt, op.P, op.ldp, tpt);
+    dim3 grid((unsigned)nblk, (unsigned)op.nsys);
+    const size_t smem = sizeof(cd) * bs * 2 * bs;
+    cudaFuncSetAttribute(k_block_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_block_invert<<<grid, 256, smem, st>>>(op.n_, bs, nblk, krk, klk, tpt, op.is_tree, op.omega, op.zscale,
+                                             op.pscale, bj->inv, singular);
+    note_launches(op.nn > 0 ? 3 : 2);
+    int sing = 0;
+    cudaMemcpyAsync(&sing, singular, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+    cudaFree(klk); cudaFree(tpt); cudaFree(singular);
+    if (e) {
+        delete bj;
+        return pfail(ERR_CUDA, "block_jacobi: %s", cudaGetErrorString(e));
+    }
+    if (sing) {
+        delete bj;
+        return pfail(ERR_NONFINITE, "block_jacobi: a diagonal block is singular");
+    }
+    delete h->bj;
+    h->bj = bj;
+    return OK;
+}
+
+int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int32_t sys, void *stream) {
+    if (!h || !krk || sys < 0 || sys >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_factor: invalid argument");
+    PeecOp &op = h->op;
+    const int64_t n = op.n_;
+    if (krk->rows != n || krk->cols != n) return pfail(ERR_ARGUMENT, "peec_factor: K^T R K must be n x n");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e;
+    const size_t nn2 = (size_t)n * n;
+    if (!h->klk) {
+        // K^T L K = (K^T L) K and T^T P T = (T^T P) T, each through one dense intermediate of n rows.
+        double *w = nullptr;
+        const int64_t wcols = std::max(op.ne, op.nn);
+        if ((e = dev_alloc(&h->klk, nn2)) || (e = dev_alloc(&h->tpt, nn2)) || (e = dev_alloc(&w, (size_t)n * wcols))) {
+            cudaFree(w);
+            return pfail(ERR_MEMORY, "peec_factor: dense system blocks: %s", cudaGetErrorString(e));
+        }
+        const unsigned chunks = 8;
+        dim3 g1(chunks, (unsigned)n);
+        k_rows_combine<<<g1, 256, 0, st>>>(op.Kt, op.L, op.ldl, op.ne, w, wcols);
+        k_gather_mult<<<g1, 256, 0, st>>>(op.Kt, w, wcols, n, h->klk, n);
+        if (op.nn > 0) {
+            k_rows_combine<<<g1, 256, 0, st>>>(op.Tt, op.P, op.ldp, op.nn, w, wcols);
+            k_gather_mult<<<g1, 256, 0, st>>>(op.Tt, w, wcols, n, h->tpt, n);
+        } else {
+            cudaMemsetAsync(h->tpt, 0, sizeof(double) * nn2, st);
+        }
+        note_launches(op.nn > 0 ? 4 : 2);
+        e = cudaStreamSynchronize(st);
+        cudaFree(w);
+        if (e) return pfail(ERR_CUDA, "peec_factor: %s", cudaGetErrorString(e));
+    }
+    auto *lu = new (std::nothrow) LuPrecond();
+    if (!lu) return pfail(ERR_MEMORY, "peec_factor: host allocation");
+    lu->n = n;
+    if ((e = dev_alloc(&lu->lu, nn2)) || (e = dev_alloc(&lu->ipiv, n)) || (e = dev_alloc(&lu->info, 1))) {
+        delete lu;
+        return pfail(ERR_MEMORY, "peec_factor: factor of %lld unknowns: %s", (long long)n, cudaGetErrorString(e));
+    }
+    double w = 0, zs = 0;
+    cudaMemcpy(&w, op.omega + sys, sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&zs, op.zscale + sys, sizeof(double), cudaMemcpyDeviceToHost);
+    Csr S = csr_of(*krk);
+    k_assemble_c64<<<grid_of((int64_t)nn2), 256, 0, st>>>(n, h->klk, h->tpt, op.is_tree, w, zs, op.pscale, lu->lu);
+    k_add_krk_c64<<<grid_of(n), 256, 0, st>>>(S, op.is_tree, w, zs, op.pscale, lu->lu);
+    note_launches(2);
+    if (cusolverDnCreate(&lu->solver) != CUSOLVER_STATUS_SUCCESS) {
+        delete lu;
+        return pfail(ERR_CUDA, "peec_factor: cuSOLVER handle");
+    }
+    cusolverDnSetStream(lu->solver, st);
+    int lwork = 0;
+    if (cusolverDnCgetrf_bufferSize(lu->solver, (int)n, (int)n, reinterpret_cast<cuComplex *>(lu->lu), (int)n,
+                                    &lwork) != CUSOLVER_STATUS_SUCCESS) {
+        delete lu;
+        return pfail(ERR_CUDA, "peec_factor: workspace query");
+    }
+    float2 *ws = nullptr;
+    if ((e = dev_alloc(&ws, (size_t)lwork))) {
+        delete lu;
+        return pfail(ERR_MEMORY, "peec_factor: workspace");
+    }
+    const cusolverStatus_t cs = cusolverDnCgetrf(lu->solver, (int)n, (int)n, reinterpret_cast<cuComplex *>(lu->lu),
+                                                 (int)n, reinterpret_cast<cuComplex *>(ws), lu->ipiv, lu->info);
+    int info = 0;
+    cudaMemcpyAsync(&info, lu->info, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+    cudaFree(ws);
+    if (cs != CUSOLVER_STATUS_SUCCESS || e || info != 0) {
+        delete lu;
+        return pfail(info ? ERR_NONFINITE : ERR_CUDA, "peec_factor: getrf failed (status %d, info %d, %s)", (int)cs,
+                     info, cudaGetErrorString(e));
+    }
+    delete h->lu;
+    h->lu = lu;
+    return OK;
+}
+
+int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, const double *b, double *x,
+                           double tol, int maxiter, int restart, int precondition, int32_t *iterations,
+                           double *residual, void *stream) {
+    if (!h || k <= 0 || !sys_host || !b || !x || !(tol > 0) || maxiter <= 0 || restart <= 0)
+        return pfail(ERR_ARGUMENT, "peec_gmres: invalid argument");
+    for (int s = 0; s < k; ++s)
+        if (sys_host[s] < 0 || sys_host[s] >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_gmres: system index");
+    if (precondition == 1 && !h->bj) return pfail(ERR_ARGUMENT, "peec_gmres: no block-Jacobi preconditioner set up");
+    if (precondition == 2 && !h->lu) return pfail(ERR_ARGUMENT, "peec_gmres: no factor set up");
+    if (precondition < 0 || precondition > 2) return pfail(ERR_ARGUMENT, "peec_gmres: preconditioner 0, 1 or 2");
+    GmresOptions opt;
+    opt.tol = tol; opt.maxiter = maxiter; opt.restart = restart;
+    GmresReport rep;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Preconditioner *M = precondition == 1 ? static_cast<Preconditioner *>(h->bj)
+                        : precondition == 2 ? static_cast<Preconditioner *>(h->lu) : nullptr;
+    cudaError_t e = gmres_batched(h->op, M, k, sys_host,
+                                  reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x), opt, rep, st);
+    if (e) return pfail(ERR_CUDA, "peec_gmres: %s", cudaGetErrorString(e));
+    bool ok = true;
+    for (int s = 0; s < k; ++s) {
+        if (iterations) iterations[s] = rep.iterations[s];
+        if (residual) residual[s] = rep.residual[s];
+        ok = ok && rep.residual[s] <= tol;
+    }
+    if (!ok) return pfail(ERR_CONVERGENCE, "peec_gmres: not every system reached the tolerance");
+    return OK;
+}
+
+int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, const double *b, double *x, double tol,
+                            int maxiter, int restart, int32_t *iterations, double *residual, void *stream) {
+    if (n <= 0 || !A || lda < n || k <= 0 || !b || !x || !(tol > 0) || maxiter <= 0 || restart <= 0)
+        return pfail(ERR_ARGUMENT, "dense_gmres: invalid argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DenseSym op;
+    op.n_ = n; op.ld = lda; op.A = A;
+    if (cublasCreate(&op.blas) != CUBLAS_STATUS_SUCCESS) return pfail(ERR_CUDA, "dense_gmres: cuBLAS handle");
+    Jacobi M;
+    M.n = n;
+    if (dev_alloc(&M.d, n)) {
+        cublasDestroy(op.blas);
+        return pfail(ERR_MEMORY, "dense_gmres: allocation");
+    }
+    k_diag_extract<<<grid_of(n), 256, 0, st>>>(n, A, lda, M.d);
+    note_launches(1);
+    std::vector<int32_t> sys(k, 0);
+    GmresOptions opt;
+    opt.tol = tol; opt.maxiter = maxiter; opt.restart = restart;
+    GmresReport rep;
+    cudaError_t e = gmres_batched(op, &M, k, sys.data(), reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x),
+                                  opt, rep, st);
+    cudaFree(M.d);
+    cublasDestroy(op.blas);
+    if (e) return pfail(ERR_CUDA, "dense_gmres: %s", cudaGetErrorString(e));
+    bool ok = true;
+    for (int s = 0; s < k; ++s) {
+        if (iterations) iterations[s] = rep.iterations[s];
+        if (residual) residual[s] = rep.residual[s];
+        ok = ok && rep.residual[s] <= tol;
+    }
+    if (!ok) return pfail(ERR_CONVERGENCE, "dense_gmres: not every column reached the tolerance");
+    return OK;
+}
+
+}  // extern "C"

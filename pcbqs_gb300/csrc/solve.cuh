@@ -1,0 +1,47 @@
+// Batched GMRES (complex128) and the operators it runs on: internal interface (gmres.cu, peec_op.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+
+namespace pq {
+
+// Vectors of k systems are stored (n, k) row-major as double2 (re, im): entry (r, s) at r * k + s.
+using cd = double2;
+
+// An operator applied to k systems at once: out = A_s in for each column s. `sys` gives each column's system
+// (frequency) index, so one batch may hold several frequencies.
+struct Operator {
+    virtual ~Operator() = default;
+    virtual int64_t n() const = 0;
+    virtual cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) = 0;
+};
+
+// A right preconditioner: out = M_s^-1 in (out may not alias in).
+struct Preconditioner {
+    virtual ~Preconditioner() = default;
+    virtual cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) = 0;
+};
+
+struct GmresOptions {
+    double tol = 1e-8;       // relative residual |b - A x| / |b| per column
+    int maxiter = 500;       // Arnoldi steps per column
+    int restart = 100;
+};
+
+struct GmresReport {
+    std::vector<int> iterations;      // per column
+    std::vector<double> residual;     // true relative residual per column at exit
+    int cycles = 0;
+    int launches = 0;                 // kernels launched by the driver (operator and preconditioner excluded)
+};
+
+// Solve A_s x_s = b_s for k columns (b, x on the device, (n, k) layout); x holds the initial guess on entry.
+// Returns cudaSuccess; convergence is reported per column in `report` (residual > tol: not converged).
+cudaError_t gmres_batched(Operator &A, Preconditioner *M, int k, const int32_t *sys_host, const cd *b, cd *x,
+                          const GmresOptions &opt, GmresReport &report, cudaStream_t stream);
+
+// Column helpers (device): norms (deterministic two-stage sums) and elementwise updates.
+cudaError_t column_norms(int64_t n, int k, const cd *x, double *out, double *scratch, cudaStream_t s);
+
+}  // namespace pq

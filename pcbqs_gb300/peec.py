@@ -1,0 +1,507 @@
+"""PEEC port impedances on one GB300: device-resident L and P, the loop/tree operator and batched GMRES.
+
+    model = PeecModel(Board.load('planes'))
+    result = model.solve([1e6])                 # all ports driven one at a time: Z (nf, np, np)
+
+Host bookkeeping (sparse topology, O(n) NumPy/SciPy) restates the reference:
+  spanning_tree          src/pcbqs/mqs.py:48-130   (breadth-first forest from central roots; parts join islands)
+  loops                  src/pcbqs/mqs.py:592-637  (fundamental cycles of the cotree; ideal terminals)
+  sheet_resistance       src/pcbqs/mqs.py:478-515  (Gram matrix of the RWG functions at DC sheet resistance)
+  prepare / solve        src/pcbqs/peec_iterative.py:127-161, 229-346 (loop/tree basis K, T = A K_tree,
+                         components and equilibrium charge, scaled operator, currents, charges, source voltages)
+Device work (C ABI): the fill of L and P, the operator products, the block-Jacobi blocks and their inverses, and
+the batched GMRES; P^-1 B for the equilibrium split by the dense GMRES.
+"""
+import collections
+import ctypes
+import time
+
+import numpy as np
+import torch
+from scipy.sparse import coo_matrix, csr_matrix, diags, eye, hstack
+from scipy.sparse.csgraph import connected_components
+from scipy.sparse.linalg import splu
+
+from . import _lib
+from .fill import DeviceFill, EPS0
+from .geometry import BAR3, W3
+
+
+# ---- graph: spanning forest and loop basis --------------------------------------------------------------------
+
+def spanning_tree(n_nodes, ends, is_src, first=None):
+    """(tree, comp, up, upb, ups, depth) of the branches `ends` excluding sources: the first `first` branches
+    (copper) as a breadth-first forest from each island's most central node (the middle of a double sweep's
+    longest path), the remaining non-source branches only joining islands the copper leaves apart."""
+    nb = len(ends)
+    first = nb if first is None else first
+    adj = [[] for _ in range(n_nodes)]
+    for k in range(first):
+        a, b = ends[k]
+        if not is_src[k] and a != b:
+            adj[a].append((b, k))
+            adj[b].append((a, k))
+    tree = np.zeros(nb, bool)
+
+    def sweep(root):
+        dist = {root: 0}
+        queue = collections.deque([root])
+        order = [root]
+        while queue:
+            u = queue.popleft()
+            for v, _ in adj[u]:
+                if v not in dist:
+                    dist[v] = dist[u] + 1
+                    queue.append(v)
+                    order.append(v)
+        return order, dist
+    seen = np.zeros(n_nodes, bool)
+    for s in range(n_nodes):
+        if seen[s]:
+            continue
+        order, _ = sweep(s)
+        seen[order] = True
+        root = s
+        if len(order) > 2:
+            _, d1 = sweep(order[-1])
+            _, d2 = sweep(max(d1, key=d1.get))
+            root = min(order, key=lambda v: max(d1[v], d2[v]))
+        mark = {root}
+        queue = collections.deque([root])
+        while queue:
+            u = queue.popleft()
+            for v, k in adj[u]:
+                if v not in mark:
+                    mark.add(v)
+                    tree[k] = True
+                    queue.append(v)
+    parent = list(range(n_nodes))
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+    for k in np.flatnonzero(tree):
+        a, b = ends[k]
+        parent[find(b)] = find(a)
+    for k in range(first, nb):
+        a, b = ends[k]
+        if not is_src[k] and find(a) != find(b):
+            parent[find(b)] = find(a)
+            tree[k] = True
+    tadj = [[] for _ in range(n_nodes)]
+    for k in np.flatnonzero(tree):
+        a, b = ends[k]
+        tadj[a].append((b, k))
+        tadj[b].append((a, k))
+    up = np.full(n_nodes, -1)
+    upb = np.full(n_nodes, -1)
+    ups = np.zeros(n_nodes, int)
+    depth = np.full(n_nodes, -1)
+    comp = np.full(n_nodes, -1)
+    for root in range(n_nodes):
+        if depth[root] >= 0:
+            continue
+        depth[root] = 0
+        comp[root] = root
+        stack = [root]
+        while stack:
+            u = stack.pop()
+            for v, k in tadj[u]:
+                if depth[v] < 0:
+                    depth[v], up[v], upb[v], comp[v] = depth[u] + 1, u, k, root
+                    ups[v] = 1 if ends[k][0] == u else -1
+                    stack.append(v)
+    return tree, comp, up, upb, ups, depth
+
+
+def loop_basis(n_nodes, ends, is_src, n_rwg, ideal_terminals=True):
+    """(C (nb x ncol) csc, src_cols {branch: col}, tree, col_branch): each non-tree branch's fundamental cycle,
+    oriented with the branch (col_branch[c] is column c's branch); copper edges inside one node are no loop (ideal
+    terminals); branches whose ends lie on islands joined only through them have none."""
+    nb = len(ends)
+    tree, comp, up, upb, ups, depth = spanning_tree(n_nodes, ends, is_src, n_rwg)
+    rows, cols, vals, src_cols, col_branch = [], [], [], {}, []
+    col = 0
+    for k in np.flatnonzero(~tree):
+        a, b = ends[k]
+        if a == b and k < n_rwg and ideal_terminals:
+            continue
+        if comp[a] != comp[b]:
+            continue
+        u, v = b, a
+        pu, pv = [], []
+        while depth[u] > depth[v]:
+            pu.append((upb[u], -ups[u]))
+            u = up[u]
+        while depth[v] > depth[u]:
+            pv.append((upb[v], ups[v]))
+            v = up[v]
+        while u != v:
+            pu.append((upb[u], -ups[u]))
+            u = up[u]
+            pv.append((upb[v], ups[v]))
+            v = up[v]
+        rows.append(k)
+        cols.append(col)
+        vals.append(1.0)
+        for kb, sg in pu + pv[::-1]:
+            rows.append(kb)
+            cols.append(col)
+            vals.append(float(sg))
+        if is_src[k]:
+            src_cols[k] = col
+        col_branch.append(int(k))
+        col += 1
+    C = coo_matrix((vals, (rows, cols)), shape=(nb, col)).tocsc()
+    return C, src_cols, tree, np.asarray(col_branch, np.int64)
+
+
+# ---- resistance: Gram matrix of the RWG functions ---------------------------------------------------------------
+
+def rwg_sparse(rwg, nt):
+    """The RWG functions' sparse triangle maps (A_alpha, B_x, B_y): alpha, alpha v_x, alpha v_y on (T+/-, edge)."""
+    ne = rwg.Ne
+    alpha = np.concatenate([rwg.l / (2 * rwg.area[rwg.tp]), -rwg.l / (2 * rwg.area[rwg.tm])])
+    vv = np.vstack([rwg.vp, rwg.vm])
+    rows = np.r_[rwg.tp, rwg.tm]
+    cols = np.r_[np.arange(ne), np.arange(ne)]
+    sp = lambda values: csr_matrix((values, (rows, cols)), shape=(nt, ne))
+    return sp(alpha), sp(alpha * vv[:, 0]), sp(alpha * vv[:, 1])
+
+
+def qform(S1, M, S2):
+    return (S2.T @ (S1.T @ M).T).T
+
+
+def sheet_resistance(rwg, sigma, thickness):
+    """R (ne x ne, sparse) of total edge currents: diag(1/l) Gram diag(1/l), Gram the integral of f_m . f_n times
+    each triangle's DC sheet resistance 1/(sigma t), with the 3-point rule (mqs.py:478-515)."""
+    nt = len(rwg.tris)
+    A, Bx, By = rwg_sparse(rwg, nt)
+    Ar = rwg.area
+    Pq = np.einsum('qk,tkc->tqc', BAR3, rwg.nodes[rwg.tris])
+    rs = 1.0 / (sigma * np.broadcast_to(thickness, (nt,)))
+    m = lambda v: diags(Ar * rs * (W3[None, :] * v).sum(1))
+    Mrr, Mrx, Mry, M0 = m((Pq ** 2).sum(-1)), m(Pq[..., 0]), m(Pq[..., 1]), diags(Ar * rs)
+    G = (qform(A, Mrr, A) - qform(A, Mrx, Bx) - qform(A, Mry, By) - qform(Bx, Mrx.T, A) - qform(By, Mry.T, A)
+         + qform(Bx, M0, Bx) + qform(By, M0, By))
+    scale = diags(1.0 / rwg.l)
+    return (scale @ G @ scale).tocsr()
+
+
+# ---- ordering for block-Jacobi -----------------------------------------------------------------------------------
+
+def cluster_order(points, bs):
+    """Recursive coordinate bisection of points (n, d) into leaves of exactly `bs` points (the last may be
+    shorter): returns the permutation that makes each leaf a contiguous run."""
+    order = []
+
+    def split(idx):
+        if len(idx) <= bs:
+            order.extend(idx.tolist())
+            return
+        pts = points[idx]
+        axis = int(np.argmax(pts.max(0) - pts.min(0)))
+        half = bs * int(np.ceil(len(idx) / bs / 2))
+        srt = idx[np.argsort(pts[:, axis], kind='stable')]
+        split(srt[:half])
+        split(srt[half:])
+    split(np.arange(len(points)))
+    return np.asarray(order, np.int64)
+
+
+def _dev_csr(S, device):
+    S = csr_matrix(S)
+    S.sum_duplicates()
+    return (torch.as_tensor(S.indptr.astype(np.int64), device=device),
+            torch.as_tensor(S.indices.astype(np.int32), device=device),
+            torch.as_tensor(S.data.astype(np.float64), device=device), S.shape)
+
+
+def _csr_struct(t):
+    ptr, idx, val, shape = t
+    c = _lib.CsrDesc()
+    c.rows, c.cols = shape
+    c.ptr, c.idx, c.val = ptr.data_ptr(), idx.data_ptr(), val.data_ptr()
+    return c
+
+
+class PeecResult:
+    def __init__(self, freqs, names, Z, currents, iterations, residual, timings):
+        self.frequencies, self.names, self.impedance = freqs, names, Z
+        self.currents, self.iterations, self.residual, self.timings = currents, iterations, residual, timings
+
+
+class PeecTopology:
+    """Host side of the PEEC model (peec_iterative.prepare): branches, loop/tree basis K, T = A K_tree, node
+    incidence A, components B and the equilibrium tree factor, the sheet resistance R, and the clustered order of
+    the unknowns. `rwg` is the RWG basis on the centred mesh nodes."""
+
+    def __init__(self, board, rwg, block_size=32, log=None):
+        self.board, self.rwg, self.bs = board, rwg, block_size
+        self.log = log or (lambda *a: None)
+        self._topology()
+
+    def _topology(self):
+        b, r = self.board, self.rwg
+        node_of = b.node_of
+        nn = b.n_nodes
+        self.ne = ne = r.Ne
+        self.names = [p for p, _, _ in b.ports]
+        ends = [(int(node_of[a]), int(node_of[c])) for a, c in zip(r.tp, r.tm)]
+        ends += [(b.term_node(a), b.term_node(c)) for _, a, c in b.ports]
+        nb = len(ends)
+        is_src = np.r_[np.zeros(ne, bool), np.ones(len(b.ports), bool)]
+        C, src_cols, tree, col_branch = loop_basis(nn, ends, is_src, ne)
+        ea, eb = np.asarray(ends).T
+        branch = np.arange(nb)
+        A = coo_matrix((np.r_[np.ones(nb), -np.ones(nb)], (np.r_[ea, eb], np.r_[branch, branch])),
+                       shape=(nn, nb)).tocsc()
+        sources, passive = np.flatnonzero(is_src), np.flatnonzero(~is_src)
+        if not np.array_equal(passive, np.arange(ne)):
+            raise ValueError('only copper edges may be passive branches (no via segments or lumped parts)')
+        cycles = [c for c in range(C.shape[1]) if c not in set(src_cols.values())]
+        K = hstack((C[:, cycles], eye(nb, format='csc')[:, np.flatnonzero(tree)]), format='csc')
+        nl = len(cycles)
+        T = (A @ K[:, nl:]).tocsc()
+        graph = coo_matrix((np.ones(len(passive)), (ea[passive], eb[passive])), shape=(nn, nn))
+        nc, labels = connected_components(graph, directed=False)
+        B = coo_matrix((np.ones(nn), (np.arange(nn), labels)), shape=(nn, nc)).tocsc()
+        roots = np.unique(labels, return_index=True)[1]
+        keep = np.ones(nn, bool)
+        keep[roots] = False
+        self.tree_lu = splu(T[keep].astype(complex).tocsc()) if T.shape[1] else None
+        self.A, self.K, self.T, self.B, self.keep, self.nl = A, K, T, B, keep, nl
+        self.sources, self.passive, self.nn, self.nb = sources, passive, nn, nb
+        self.source_components = np.asarray((A[:, sources].T @ B).todense())
+        self.R = sheet_resistance(r, b.sigma, b.thickness)
+        # K-space unknowns ordered into geometric blocks: a cycle at its defining (cotree) branch, a tree unknown
+        # at its branch; branch positions are RWG edge midpoints at their sheet's height.
+        n = K.shape[1]
+        pos_branch = np.c_[r.mid, 1e3 * b.z[r.tp]]      # sheets far apart in the ordering
+        own = np.r_[col_branch[cycles], np.flatnonzero(tree)]
+        assert len(own) == n and own.max() < ne
+        self.order = cluster_order(pos_branch[own], self.bs)
+        self.Kp = K[passive][:, self.order].tocsc()           # passive rows, clustered columns
+        Tfull = hstack((csr_matrix((nn, nl)), T), format='csc')     # loop columns carry no charge
+        self.Tp = Tfull[:, self.order].tocsc()
+        self.is_tree = np.r_[np.zeros(nl, np.int8), np.ones(n - nl, np.int8)][self.order]
+        self.n = n
+        self.log(f'peec: {nn:,} nodes, {ne:,} edges, {n:,} unknowns ({nl:,} loops), {nc} components')
+
+
+
+class PeecModel(PeecTopology):
+    """A board's surface-charge PEEC model in a homogeneous dielectric, every port a 1 A current source from its
+    first to its second terminal (MQS.source), solved on the device."""
+
+    def __init__(self, board, near=3.0, outer_levels=1, device=0, block_size=32, tol=1e-8, maxiter=2000,
+                 restart=100, log=None):
+        self.tol, self.maxiter, self.restart = tol, maxiter, restart
+        self.device = torch.device('cuda', device)
+        self.timings = {}
+        t0 = time.perf_counter()
+        self.fill = DeviceFill(board.nodes, board.tris, board.z, outer_levels, near, device)
+        PeecTopology.__init__(self, board, self.fill.rwg, block_size, log)
+        self.timings['host_topology_s'] = time.perf_counter() - t0
+        self.L = self.P = None
+
+    # -- device matrices --
+    def assemble(self):
+        """Fill L and P on the device (moments, combine, aggregation); frees the moment planes."""
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record()
+        planes, analytic = self.fill.moments()
+        ev[1].record()
+        self.L = self.fill.inductance(planes)
+        ev[2].record()
+        self.P = self.fill.potential(planes[0], self.board.node_of, self.board.er)
+        ev[3].record()
+        del planes
+        torch.cuda.synchronize()
+        self.analytic = analytic
+        self.timings.update(fill_ms=ev[0].elapsed_time(ev[1]), combine_ms=ev[1].elapsed_time(ev[2]),
+                            potential_ms=ev[2].elapsed_time(ev[3]))
+        self.pscale = float(torch.diagonal(self.P).abs().max())
+        self.ldiag = torch.diagonal(self.L).cpu().numpy()
+        self._pinvb = None
+        return self
+
+    def _operator(self, omegas):
+        dev = self.device
+        R = self.R
+        zscale = np.array([max(float(np.max(np.abs(R.diagonal() + 1j * w * self.ldiag))), np.finfo(float).tiny)
+                           for w in omegas])
+        self._dev = dict(K=_dev_csr(self.Kp, dev), Kt=_dev_csr(self.Kp.T, dev), T=_dev_csr(self.Tp, dev),
+                         Tt=_dev_csr(self.Tp.T, dev), R=_dev_csr(R, dev),
+                         is_tree=torch.as_tensor(self.is_tree, device=dev))
+        d = _lib.PeecDesc()
+        d.n, d.nb, d.ne, d.nn = self.n, len(self.passive), self.ne, self.nn
+        for name in ('K', 'Kt', 'T', 'Tt', 'R'):
+            setattr(d, name, _csr_struct(self._dev[name]))
+        d.L, d.ldl, d.P, d.ldp = self.L.data_ptr(), self.L.stride(0), self.P.data_ptr(), self.P.stride(0)
+        d.is_tree = self._dev['is_tree'].data_ptr()
+        d.pscale = self.pscale
+        d.nsys = len(omegas)
+        self._omega = np.ascontiguousarray(omegas, float)
+        self._zscale = np.ascontiguousarray(zscale, float)
+        d.omega, d.zscale = _lib.ptr(self._omega), _lib.ptr(self._zscale)
+        lib = _lib.load()
+        handle = ctypes.c_void_p()
+        _lib.check(lib.pcbqs_gb300_peec_create(ctypes.byref(d), ctypes.byref(handle)), lib)
+        return handle, zscale
+
+    def _krk_blocks(self):
+        bs, n = self.bs, self.n
+        M = (self.Kp.T @ self.R @ self.Kp).tocoo()
+        same = (M.row // bs) == (M.col // bs)
+        nblk = (n + bs - 1) // bs
+        out = np.zeros((nblk, bs, bs))
+        out[M.row[same] // bs, M.row[same] % bs, M.col[same] % bs] = M.data[same]
+        return torch.as_tensor(out, device=self.device)
+
+    def _equilibrium(self, excitation):
+        """Baseline tree currents and the equilibrium charge of each drive (peec_iterative.solve:240-251)."""
+        A, B = self.A, self.B
+        sources = self.sources
+        drive = np.asarray(A[:, sources] @ excitation)                 # (nn, ndrive)
+        totals = self.source_components.T @ excitation                 # (nc, ndrive)
+        qpart = np.zeros((self.nn, excitation.shape[1]), complex)
+        vpart = np.zeros((B.shape[1], excitation.shape[1]), complex)
+        if np.any(totals):
+            if self._pinvb is None:
+                self._pinvb = self._potential_solve(B.toarray())
+                self._component = np.asarray(B.T @ self._pinvb)
+            vpart = np.linalg.solve(self._component, -totals)
+            qpart = self._pinvb @ vpart
+        y0 = np.zeros((self.K.shape[1] - self.nl, excitation.shape[1]), complex)
+        if self.tree_lu is not None:
+            for c in range(excitation.shape[1]):
+                y0[:, c] = self.tree_lu.solve((-drive[:, c] - qpart[:, c])[self.keep])
+        baseline = np.asarray(self.K[:, self.nl:] @ y0)               # (nb, ndrive)
+        source_voltage = -self.source_components @ vpart                # (nsrc, ndrive)
+        return baseline, qpart, vpart, source_voltage
+
+    def _potential_solve(self, rhs):
+        """P^-1 rhs on the device (Jacobi-preconditioned dense GMRES), rhs (nn, k) real."""
+        k = rhs.shape[1]
+        b = torch.as_tensor(np.ascontiguousarray(rhs.astype(complex)), device=self.device)
+        x = torch.zeros_like(b)
+        its = np.zeros(k, np.int32)
+        res = np.zeros(k)
+        lib = _lib.load()
+        _lib.check(lib.pcbqs_gb300_dense_gmres(self.nn, self.P.data_ptr(), self.P.stride(0), k, b.data_ptr(),
+                                               x.data_ptr(), self.tol * 1e-2, 4000, self.restart,
+                                               _lib.ptr(its, ctypes.c_int32), _lib.ptr(res),
+                                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
+        self.timings['potential_solve_iterations'] = its.tolist()
+        return x.cpu().numpy()
+
+    def _mv_L(self, X):
+        """L X for complex branch vectors X (ne, k) on the device."""
+        Xt = torch.as_tensor(np.ascontiguousarray(X), device=self.device)
+        return (self.L @ Xt.real + 1j * (self.L @ Xt.imag)).cpu().numpy()
+
+    def _mv_P(self, X):
+        Xt = torch.as_tensor(np.ascontiguousarray(X), device=self.device)
+        return (self.P @ Xt.real + 1j * (self.P @ Xt.imag)).cpu().numpy()
+
+    PRECONDITIONERS = {'none': 0, 'block_jacobi': 1, 'lu32': 2}
+
+    def solve(self, freqs, precondition='block_jacobi'):
+        """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
+
+        precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
+        dense loop/tree system at each frequency, FP64 GMRES on top), or 'none'."""
+        if self.L is None:
+            self.assemble()
+        f = np.atleast_1d(np.asarray(freqs, float))
+        if f.ndim != 1 or not np.isfinite(f).all() or (f <= 0).any():
+            raise ValueError('frequencies must be finite and positive')
+        if precondition not in self.PRECONDITIONERS:
+            raise ValueError(f'precondition must be one of {sorted(self.PRECONDITIONERS)}')
+        if precondition == 'lu32' and len(f) > 1:
+            return self._stack([self.solve([fi], precondition) for fi in f])
+        mode = self.PRECONDITIONERS[precondition]
+        t0 = time.perf_counter()
+        npo = len(self.names)
+        excitation = np.eye(npo, dtype=complex)
+        baseline, qpart, vpart, source_voltage = self._equilibrium(excitation)
+        omegas = 2 * np.pi * f
+        handle, zscale = self._operator(omegas)
+        lib = _lib.load()
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        try:
+            ev_p0, ev_p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev_p0.record()
+            if mode == 1:
+                _lib.check(lib.pcbqs_gb300_peec_block_jacobi(handle, self.bs, self._krk_blocks().data_ptr(), stream),
+                           lib)
+            elif mode == 2:
+                krk = _dev_csr(self.Kp.T @ self.R @ self.Kp, self.device)
+                desc = _csr_struct(krk)
+                _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, stream), lib)
+            ev_p1.record()
+            torch.cuda.synchronize()
+            self.timings['precondition_ms'] = ev_p0.elapsed_time(ev_p1)
+            # rhs = -K^T (R + j w L) baseline / zscale, per (frequency, port) column, in the clustered order.
+            Lb = self._mv_L(baseline[:self.ne])
+            Rb = self.R @ baseline[:self.ne]
+            Kpt = self.Kp.T
+            cols, sys = [], []
+            for fi, w in enumerate(omegas):
+                v = Rb + 1j * w * Lb
+                cols.append(-(Kpt @ v) / zscale[fi])
+                sys += [fi] * npo
+            rhs = np.ascontiguousarray(np.concatenate(cols, axis=1))      # (n, nf * np)
+            b = torch.as_tensor(rhs, device=self.device)
+            x = torch.zeros_like(b)
+            k = rhs.shape[1]
+            sys = np.asarray(sys, np.int32)
+            its, res = np.zeros(k, np.int32), np.zeros(k)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record()
+            status = lib.pcbqs_gb300_peec_gmres(handle, k, _lib.ptr(sys, ctypes.c_int32), b.data_ptr(), x.data_ptr(),
+                                                self.tol, self.maxiter, self.restart, mode,
+                                                _lib.ptr(its, ctypes.c_int32), _lib.ptr(res), stream)
+            ev1.record()
+            torch.cuda.synchronize()
+            if status not in (0, 5):
+                _lib.check(status, lib)
+            self.timings['gmres_ms'] = ev0.elapsed_time(ev1)
+            self.timings['gmres_iterations'] = its.tolist()
+            converged = status == 0
+            X = x.cpu().numpy()
+        finally:
+            lib.pcbqs_gb300_peec_destroy(handle)
+        # back to the unclustered order, then currents, charges and source voltages (peec_iterative.py:331-341)
+        Xo = np.empty_like(X)
+        Xo[self.order] = X
+        Z = np.zeros((len(f), npo, npo), complex)
+        currents = np.zeros((len(f), self.nb, npo), complex)
+        Kc, Kt = self.K[:, :self.nl], self.K[:, self.nl:]
+        for fi, w in enumerate(omegas):
+            xs = Xo[:, fi * npo:(fi + 1) * npo]
+            alpha = zscale[fi] / self.pscale
+            correction = alpha * xs[self.nl:]
+            currents[fi] = baseline + Kc @ xs[:self.nl] + 1j * w * (Kt @ correction)
+            currents[fi][self.sources] = excitation
+            pcorrection = self._mv_P(np.asarray(self.T @ correction))
+            voltage = source_voltage / (1j * w) + np.asarray(self.A[:, self.sources].T @ pcorrection)
+            Z[fi] = voltage
+        self.timings['solve_s'] = time.perf_counter() - t0
+        if not converged:
+            raise RuntimeError(f'GMRES did not reach {self.tol:g}: residuals {res.max():.3g}, iterations {its.max()}')
+        return PeecResult(f, self.names, Z, currents, its, res, dict(self.timings))
+
+    @staticmethod
+    def _stack(results):
+        first = results[0]
+        cat = lambda name: np.concatenate([getattr(r, name) for r in results])
+        timings = dict(first.timings)
+        for key in ('precondition_ms', 'gmres_ms', 'solve_s'):
+            timings[key] = sum(r.timings.get(key, 0) for r in results)
+        return PeecResult(cat('frequencies'), first.names, cat('impedance'), cat('currents'), cat('iterations'),
+                          cat('residual'), timings)
