@@ -45,6 +45,10 @@ def parse():
     p.add_argument('--board', default='planes')
     p.add_argument('--freq', type=float, default=1e6)
     p.add_argument('--precondition', default='lu32', choices=['lu32', 'block_jacobi'])
+    p.add_argument('--mode', default='mixed', choices=['mixed', 'fp64'],
+                   help='mixed: FP32 far pairs in local coordinates and FP32 inner Krylov products under FP64 '
+                        'refinement; fp64: the FP64 fill and FP64 GMRES')
+    p.add_argument('--no-comparator', action='store_true', help='skip the one-step FP64 comparator')
     p.add_argument('--no-cpu-baseline', action='store_true')
     return p.parse_args()
 
@@ -85,8 +89,8 @@ class Clocks:
                     reasons=reasons, samples=len(rows))
 
 
-def fill_roofline(model, fp64_peak_tflops):
-    """The fill kernel pair (far tiles + near lists): algorithmic FP64 flops per launch / its CUDA-event time."""
+def fill_roofline(model, fp64_peak_tflops, fill_ms):
+    """The FP64 fill kernel pair (far tiles + near lists): algorithmic FP64 flops per launch / its CUDA-event time."""
     import ctypes
     from pcbqs_gb300 import _lib
     counts = (ctypes.c_uint64 * 2)()
@@ -96,7 +100,7 @@ def fill_roofline(model, fp64_peak_tflops):
     near0, near1 = int(counts[0]), int(counts[1])
     far = pairs - near0 - near1
     flops = far * FAR_FLOP + near0 * NEAR_FLOP[0] + near1 * NEAR_FLOP[model.fill.outer_levels]
-    seconds = model.timings['fill_ms'] / 1e3
+    seconds = fill_ms / 1e3
     achieved = flops / seconds / 1e12
     return dict(bound='fp64', kernel='k_fill_tiles+k_fill_near', achieved=round(achieved, 4),
                 peak=round(fp64_peak_tflops, 4), unit='TFLOP/s', frac=round(achieved / fp64_peak_tflops, 4),
@@ -195,9 +199,11 @@ def main():
     freq = args.freq * (1 + 0.01 * rank)          # replicas: each rank its own frequency
     model = PeecModel(board, device=local)
 
-    def step():
-        model.assemble()
-        return model.solve([freq], precondition=args.precondition)
+    mixed = args.mode == 'mixed'
+
+    def step(mode_mixed=mixed):
+        model.assemble(mixed=mode_mixed)
+        return model.solve([freq], precondition=args.precondition, mixed=mode_mixed)
 
     for _ in range(args.warmup):
         result = step()
@@ -225,6 +231,25 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t)
     value = ms / 1e3 / world
+    Z_headline = result.impedance[0]
+    comparator = None
+    fp64_timings = timings[-1]
+    if mixed and not args.no_comparator:
+        # the FP64 fill + FP64 GMRES on the same step, once (after one warm-up), for the error and speed-up
+        step(False)
+        torch.cuda.synchronize()
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record()
+        r64 = step(False)
+        c1.record()
+        torch.cuda.synchronize()
+        Z64 = r64.impedance[0]
+        fp64_timings = dict(model.timings)
+        comparator = dict(mode='fp64 fill + fp64 GMRES (complex64-LU preconditioned)',
+                          s_per_freq=round(c0.elapsed_time(c1) / 1e3, 4),
+                          speedup_of_mixed=round(c0.elapsed_time(c1) / ms, 3),
+                          port_z_max_rel_err_of_mixed=float(np.abs(Z_headline - Z64).max() / np.abs(Z64).max()),
+                          gmres_iterations=r64.iterations.tolist())
     # fill GB/s: bytes of L and P written once per step, over the fill + combine + aggregation time
     ne, nn = model.ne, model.nn
     fill_ms = statistics.median(t['fill_ms'] + t['combine_ms'] + t['potential_ms'] for t in timings)
@@ -233,7 +258,8 @@ def main():
     t_e2e = time.perf_counter()
     torch.cuda.synchronize()
     m2 = PeecModel(Board.load(args.board), device=local)
-    r2 = m2.solve([freq], precondition=args.precondition)
+    m2.assemble(mixed=mixed)
+    r2 = m2.solve([freq], precondition=args.precondition, mixed=mixed)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t_e2e
     h2d = m2.fill.dev.nt * (64 + 32 + 192) + sum(a.nbytes for a in m2.fill.geometry.levels[1][5:6])
@@ -246,18 +272,21 @@ def main():
     peak = fp64_peak()
     line = dict(metric=METRIC, value=round(value, 4), unit='s/freq', n_gpus=world, steps=args.steps,
                 warmup=args.warmup, ms_per_step=round(ms, 2), higher_is_better=False, scaling='weak',
-                vs_baseline=None, dtype='f64', data='synthetic (seeded plane-pair board, CDT mesh)',
+                vs_baseline=None, dtype='f32+f64' if mixed else 'f64', data='synthetic (seeded plane-pair board, CDT mesh)',
                 config=dict(workload=f'{args.board}: fill+solve of all {len(model.names)} ports at {args.freq:g} Hz',
                             board=args.board, triangles=model.fill.nt, edges=ne, nodes=nn, unknowns=model.n,
-                            precondition=args.precondition, gmres_tol=model.tol,
+                            precondition=args.precondition, mode=args.mode, gmres_tol=model.tol,
                             gmres_iterations=result.iterations.tolist(), parallelism=f'replicas x{world}',
                             l2='inputs larger than L2 (L 8.9 GB)'),
                 fill_gbs=round(fill_gbs, 2),
+                fp64_comparator=comparator,
                 breakdown_ms={k: round(statistics.median(t.get(k, 0) for t in timings), 2)
                               for k in ('fill_ms', 'combine_ms', 'potential_ms', 'precondition_ms', 'gmres_ms')},
+                host_s={k: round(statistics.median(t.get(k, 0) for t in timings), 3)
+                        for k in ('equilibrium_s', 'operator_setup_s', 'rhs_s', 'solve_s')},
                 gpu_launches=int(launches),
                 clocks=clock_info,
-                roofline=fill_roofline(model, peak),
+                roofline=fill_roofline(model, peak, fp64_timings['fill_ms']),
                 e2e=dict(value=round(e2e_s, 4), unit='s/freq', h2d_bytes_per_step=int(h2d),
                          d2h_bytes_per_step=int(d2h)))
     if not args.no_cpu_baseline:

@@ -74,6 +74,13 @@ int pcbqs_gb300_fill(pcbqs_gb300_ctx *ctx, double near, int outer, int scalar_on
 int pcbqs_gb300_fill_device(pcbqs_gb300_ctx *ctx, double near, int outer, int scalar_only, double *const *planes,
                             int64_t ld, uint64_t *analytic, void *stream);
 
+/* Mixed precision: the same fill into FP32 planes holding moments about each triangle's centroid (Mx/My: the
+ * centroid-relative Mro forward and Mrs reverse; Mrr the product of both offsets): far pairs integrated in FP32 in
+ * these local coordinates, near pairs in FP64 and shifted to them. New in this backend (the reference fills FP64
+ * only); its combine is pcbqs_gb300_edge_inductance_local_device. */
+int pcbqs_gb300_fill_local_device(pcbqs_gb300_ctx *ctx, double near, int outer, int scalar_only, float *const *planes,
+                                  int64_t ld, uint64_t *analytic, void *stream);
+
 /* L = factor diag(scale) combine(moments) diag(scale), symmetric, from device moment planes (leading dimension
  * ldm) into device L (ne x ne, leading dimension ldl): tri (2,ne) int32 supports T+/T-, alpha (2,ne), vertex
  * (2,ne,2), scale (ne), all device arrays. Replaces the compiled static_combine
@@ -88,12 +95,63 @@ int pcbqs_gb300_edge_inductance(int64_t nt, int64_t ne, const int32_t *tri, cons
                                 const double *vertex, const double *scale, double factor, const double *mrr,
                                 const double *mx, const double *my, const double *m0, double *L);
 
+/* Mixed precision combine (FP32 arithmetic, no cancellation) of the local moments of
+ * pcbqs_gb300_fill_local_device: off (2,ne,2) holds centroid - free vertex of each support, alpha/off/scale FP32;
+ * writes L (FP64, ldl) and, when Lf is not NULL, its FP32 copy (ldlf). Replaces static_combine for the mixed form. */
+int pcbqs_gb300_edge_inductance_local_device(int64_t ne, const int32_t *tri, const float *alpha, const float *off,
+                                             const float *scale, double factor, const float *mrr, const float *mx,
+                                             const float *my, const float *m0, int64_t ldm, double *L, int64_t ldl,
+                                             float *Lf, int64_t ldlf, void *stream);
+
+/* P from FP32 M0 (the mixed fill), sums in FP64; Pf (NULL or an FP32 copy with the same row stride ldp). */
+int pcbqs_gb300_potential_single_device(int64_t nn, const int64_t *start, const int32_t *members, const double *area,
+                                        const float *m0, int64_t ldm, double factor, double *P, float *Pf,
+                                        int64_t ldp, void *stream);
+
 /* P = factor * W^T M0 W with W[t, a] = 1/area[a] for the triangles t of charge node a (members[start[a] ..
  * start[a+1])): device arrays; P (nn x nn, leading dimension ldp). factor = 1/(4 pi eps0 er).
  * Replaces MQS._set_potential (src/pcbqs/mqs.py:532-552). */
 int pcbqs_gb300_potential_device(int64_t nn, const int64_t *start, const int32_t *members, const double *area,
                                  const double *m0, int64_t ldm, double factor, double *P, int64_t ldp,
                                  void *stream);
+
+/* ---- H-matrix of L ----------------------------------------------------------------------------------------------
+ * kind 0: L over RWG edges (below); kind 1: the potential kernel over triangles, factor M0(t,u) / (A_t A_u) with
+ * factor = 1/(4 pi eps0 er) (PotentialEntries, src/pcbqs/core/hmatrix_build.hpp:54-67; the edge arrays are unused).
+ * Blocks are described by meta (nblocks x 8 int64, device): a offset, a length, b offset, b length (into idx, the
+ * edges of each cluster), store offset, rank cap, same (diagonal block), rank (written by the build: -1 dense,
+ * >= 0 low rank). Edge arrays: tri (2,ne) int32 supports, alpha (2,ne) +-1/(2A), vertex (2,ne,2) centred; entries
+ * factor * sum alpha alpha [Mrr - v.Mro - v.Mrs + v.v M0] of the canonical pair moments.
+ * Build: the `dense` blocks get their la x lb entries (row-major at the store offset); the `lowrank` blocks get a
+ * partial-pivot ACA (U la x cap column-major, V cap x lb, then 32 x lb check rows of scratch), rank cap as given,
+ * accepted when 16 check rows and 16 independent ones are within tol; used: nlow x used_stride bytes of scratch.
+ * Replaces the reference's level build (src/pcbqs/hmatrix.py:179-207 -> core/hmatrix_build.hpp:143-351 aca_blocks,
+ * dense_blocks) with the RwgEntries provider (core/hmatrix_build.hpp:27-52, core/compressed_kernels.hpp:9-38). */
+int pcbqs_gb300_hmatrix_build(const pcbqs_gb300_ctx *ctx, double near, int outer, int kind, const int32_t *tri,
+                              const double *alpha, const double *vertex, int64_t ne, double factor, int64_t *meta,
+                              const int64_t *dense, int64_t ndense, const int64_t *lowrank, int64_t nlow,
+                              const int64_t *idx, double tol, double *store, unsigned char *used,
+                              int64_t used_stride, void *stream);
+/* Y = H X, X and Y (n, k) complex128 device arrays: each block writes its contributions into its slots (slot0:
+ * nblocks x 2 int64, first slot of the a rows and of the transposed b rows), then every row sums its slots
+ * (row_ptr (n+1), slots_of_row) in block order; slots: nslots x k complex128 scratch. Replaces HBlocks.apply
+ * (src/pcbqs/core/hmatrix_kernels.hpp:20-100, packing src/pcbqs/hmatrix.py:234-297). */
+int pcbqs_gb300_hmatrix_apply(int64_t n, int64_t nblocks, const int64_t *meta, const int64_t *slot0,
+                              const int64_t *idx, const double *store, const int64_t *row_ptr,
+                              const int64_t *slots_of_row, int max_rank, int k, const double *x, double *y,
+                              double *slots, void *stream);
+
+/* ---- Biot-Savart near field --------------------------------------------------------------------------------
+ * H at npts points (pts (npts,3) device, m) of sheet currents given as nsrc quadrature points src (nsrc,4: x,y,z,0)
+ * with current moments jx, jy (nsrc, k) complex128 (w J_x, w J_y), accumulated into H (npts, 3, k) complex128;
+ * single != 0 sums in FP32. Replaces biot._h_tris inside h_sheets (src/pcbqs/biot.py:24-79); the quadrature points
+ * and the near refinement are built on the host as h_sheets builds them. */
+int pcbqs_gb300_biot_sheets(int64_t npts, const double *pts, int64_t nsrc, const double *src_xyz4, const double *jx,
+                            const double *jy, int k, int single, double *H, void *stream);
+/* Straight filaments p0 -> p1 ((nseg,3) m) with currents I (nseg, k) complex128, accumulated into H. Replaces
+ * biot.h_segments (src/pcbqs/biot.py:82-105). */
+int pcbqs_gb300_biot_segments(int64_t npts, const double *pts, int64_t nseg, const double *p0, const double *p1,
+                              const double *I, int k, double *H, void *stream);
 
 /* ---- Solve: the PEEC operator in loop/tree coordinates and batched GMRES ------------------------------------
  * Complex vectors of k systems are (n, k) row-major complex128 (interleaved re, im) device arrays. */
@@ -140,9 +198,13 @@ int pcbqs_gb300_peec_apply(pcbqs_gb300_peec *op, int k, const int32_t *sys, cons
 int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *op, int32_t bs, const double *krk, void *stream);
 /* Single-precision direct preconditioner: the dense loop/tree system at system index sys, assembled on the device
  * (K^T L K and T^T P T formed once from the dense L and P; krk the sparse K^T R K as a device CSR n x n), in
- * complex64 and LU-factored (cuSOLVER getrf). Mirrors MixedLU (src/pcbqs/kernels.py:125-181): a complex64 factor
+ * complex64 and LU-factored (cuSOLVER getrf). math 0: FP32 arithmetic; math 1: FP32 emulated with BF16x9 products
+ * on the tensor cores (same FP32 accuracy). Mirrors MixedLU (src/pcbqs/kernels.py:125-181): a complex64 factor
  * with the FP64 operator's GMRES on top in place of its refinement loop. */
-int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, int32_t sys, void *stream);
+int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream);
+/* out = (complex64 factor)^-1 in for k complex128 columns (n, k) row-major, device arrays; the solve step of
+ * MixedLU (src/pcbqs/kernels.py:160-181) without its refinement. Synchronizes `stream`. */
+int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *op, int k, const double *in, double *out, void *stream);
 /* Batched right-preconditioned restarted GMRES on k columns (b, x device; x holds the initial guess), relative
  * residual tol per column; iterations and residual (host, k) receive each column's Arnoldi steps and true
  * relative residual; precondition 0 none, 1 block-Jacobi, 2 the single-precision factor (every column uses it).
@@ -151,10 +213,25 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, in
 int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *op, int k, const int32_t *sys, const double *b, double *x, double tol,
                            int maxiter, int restart, int precondition, int32_t *iterations, double *residual,
                            void *stream);
-/* A x = b for a dense real symmetric A (n x n, row stride lda) and k complex columns, Jacobi-preconditioned GMRES.
- * Replaces peec_iterative.potential_solve (src/pcbqs/peec_iterative.py:115-124), used for P^-1 B. */
+/* Single-precision copies of L and P (device, row strides ldlf/ldpf) for the inner products of the mixed solve,
+ * and the conversion that makes them. */
+int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *stream);
+int pcbqs_gb300_peec_single(pcbqs_gb300_peec *op, const float *Lf, int64_t ldlf, const float *Pf, int64_t ldpf);
+/* Mixed-precision solve: FP64 true residuals b - A x (the outer iterative refinement), each correction from an
+ * inner right-preconditioned GMRES on the single-precision operator to inner_tol of the residual; until every
+ * column's true relative residual <= tol or max_outer corrections. iterations: inner Arnoldi steps per column;
+ * residual: final true relative residual; outer_steps: corrections made. The MixedLU scheme
+ * (src/pcbqs/kernels.py:125-181) with a Krylov inner solve. */
+int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *op, int k, const int32_t *sys, const double *b, double *x,
+                                 double tol, double inner_tol, int max_outer, int inner_maxiter, int restart,
+                                 int precondition, int32_t *iterations, double *residual, int32_t *outer_steps,
+                                 void *stream);
+/* A x = b for a dense real symmetric A (n x n, row stride lda) and k complex columns by GMRES, preconditioned by
+ * A's diagonal (precondition 0, as the reference) or by the single-precision Cholesky factor of A (1, A positive
+ * definite). Replaces peec_iterative.potential_solve (src/pcbqs/peec_iterative.py:115-124), used for P^-1 B. */
 int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, const double *b, double *x, double tol,
-                            int maxiter, int restart, int32_t *iterations, double *residual, void *stream);
+                            int maxiter, int restart, int precondition, int32_t *iterations, double *residual,
+                            void *stream);
 
 #ifdef __cplusplus
 }

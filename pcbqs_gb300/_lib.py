@@ -71,17 +71,46 @@ PROTOTYPES = {
     'pcbqs_gb300_potential_device': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                                     ctypes.c_int64, ctypes.c_double, c_void_p, ctypes.c_int64,
                                                     c_void_p]),
+    'pcbqs_gb300_fill_local_device': (ctypes.c_int, [c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.POINTER(c_void_p), ctypes.c_int64, c_uint64_p, c_void_p]),
+    'pcbqs_gb300_edge_inductance_local_device': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, c_void_p,
+                                                                c_void_p, ctypes.c_double, c_void_p, c_void_p,
+                                                                c_void_p, c_void_p, ctypes.c_int64, c_void_p,
+                                                                ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p]),
+    'pcbqs_gb300_potential_single_device': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                           ctypes.c_int64, ctypes.c_double, c_void_p, c_void_p,
+                                                           ctypes.c_int64, c_void_p]),
+    'pcbqs_gb300_hmatrix_build': (ctypes.c_int, [c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_void_p,
+                                                 c_void_p,
+                                                 c_void_p, ctypes.c_int64, ctypes.c_double, c_void_p, c_void_p,
+                                                 ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p, ctypes.c_double,
+                                                 c_void_p, c_void_p, ctypes.c_int64, c_void_p]),
+    'pcbqs_gb300_hmatrix_apply': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, c_void_p, c_void_p, c_void_p,
+                                                 c_void_p, c_void_p, c_void_p, ctypes.c_int, ctypes.c_int, c_void_p,
+                                                 c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_biot_sheets': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
+                                               c_void_p, ctypes.c_int, ctypes.c_int, c_void_p, c_void_p]),
+    'pcbqs_gb300_biot_segments': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
+                                                 c_void_p, ctypes.c_int, c_void_p, c_void_p]),
     'pcbqs_gb300_peec_create': (ctypes.c_int, [ctypes.POINTER(PeecDesc), ctypes.POINTER(c_void_p)]),
     'pcbqs_gb300_peec_destroy': (None, [c_void_p]),
     'pcbqs_gb300_peec_apply': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p, c_void_p]),
     'pcbqs_gb300_peec_block_jacobi': (ctypes.c_int, [c_void_p, ctypes.c_int32, c_void_p, c_void_p]),
-    'pcbqs_gb300_peec_factor': (ctypes.c_int, [c_void_p, ctypes.POINTER(CsrDesc), ctypes.c_int32, c_void_p]),
+    'pcbqs_gb300_peec_factor': (ctypes.c_int, [c_void_p, ctypes.POINTER(CsrDesc), ctypes.c_int32, ctypes.c_int,
+                                               c_void_p]),
+    'pcbqs_gb300_peec_lu_solve': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_to_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p]),
+    'pcbqs_gb300_peec_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, ctypes.c_int64]),
+    'pcbqs_gb300_peec_solve_mixed': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p,
+                                                    ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                                    ctypes.c_int, ctypes.c_int, c_int32_p, c_double_p, c_int32_p,
+                                                    c_void_p]),
     'pcbqs_gb300_peec_gmres': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p, ctypes.c_double,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_int, c_int32_p, c_double_p,
                                               c_void_p]),
     'pcbqs_gb300_dense_gmres': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, ctypes.c_int, c_void_p,
-                                               c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_int32_p,
-                                               c_double_p, c_void_p]),
+                                               c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                               c_int32_p, c_double_p, c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -109,6 +110,9 @@ int read_flags(pcbqs_gb300_ctx *c, cudaStream_t stream, int *host2) {
 
 }  // namespace
 
+// The device geometry of a context, for the other kernels of the library (hmatrix.cu).
+const Geometry *pcbqs_gb300_geometry_of(const pcbqs_gb300_ctx *ctx) { return &ctx->g; }
+
 extern "C" {
 
 const char *pcbqs_gb300_last_error(void) { return g_error.c_str(); }
@@ -153,7 +157,20 @@ int pcbqs_gb300_create(const pcbqs_gb300_geometry *geo, int device, pcbqs_gb300_
     std::vector<FarRec> far(nt);
     std::vector<ClsRec> cls(nt);
     std::vector<SrcRec> src(nt);
+    std::vector<LocalRec> local(nt);
     for (int t = 0; t < nt; ++t) {
+        const double cx = geo->cent[2 * (size_t)t], cy = geo->cent[2 * (size_t)t + 1];
+        LocalRec &lr = local[t];
+        lr.chi[0] = (float)cx;
+        lr.chi[1] = (float)cy;
+        lr.clo[0] = (float)(cx - (double)lr.chi[0]);
+        lr.clo[1] = (float)(cy - (double)lr.chi[1]);
+        for (int j = 0; j < 3; ++j) {
+            lr.u[2 * j] = (float)(geo->p3[6 * (size_t)t + 2 * j] - cx);
+            lr.u[2 * j + 1] = (float)(geo->p3[6 * (size_t)t + 2 * j + 1] - cy);
+        }
+        lr.area = (float)geo->area[t];
+        lr.z = (float)geo->z[t];
         for (int j = 0; j < 6; ++j) far[t].p[j] = geo->p3[6 * (size_t)t + j];
         far[t].area = geo->area[t];
         far[t].z = geo->z[t];
@@ -170,7 +187,8 @@ int pcbqs_gb300_create(const pcbqs_gb300_geometry *geo, int device, pcbqs_gb300_
     auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t off_far = 0, off_cls = up(off_far + sizeof(FarRec) * (size_t)nt);
     const size_t off_src = up(off_cls + sizeof(ClsRec) * (size_t)nt);
-    size_t off = off_src + sizeof(SrcRec) * (size_t)nt;
+    const size_t off_loc = up(off_src + sizeof(SrcRec) * (size_t)nt);
+    size_t off = off_loc + sizeof(LocalRec) * (size_t)nt;
     size_t off_obs[3], off_w[3];
     for (int k = 0; k < 3; ++k) {
         off = up(off);
@@ -196,6 +214,7 @@ int pcbqs_gb300_create(const pcbqs_gb300_geometry *geo, int device, pcbqs_gb300_
     err = put(off_far, far.data(), sizeof(FarRec) * (size_t)nt);
     if (err == cudaSuccess) err = put(off_cls, cls.data(), sizeof(ClsRec) * (size_t)nt);
     if (err == cudaSuccess) err = put(off_src, src.data(), sizeof(SrcRec) * (size_t)nt);
+    if (err == cudaSuccess) err = put(off_loc, local.data(), sizeof(LocalRec) * (size_t)nt);
     for (int k = 0; k < 3 && err == cudaSuccess; ++k) {
         err = put(off_obs[k], geo->qp[k], sizeof(double) * 2 * (size_t)nt * geo->nq[k]);
         if (err == cudaSuccess) err = put(off_w[k], geo->qw[k], sizeof(double) * geo->nq[k]);
@@ -210,6 +229,7 @@ int pcbqs_gb300_create(const pcbqs_gb300_geometry *geo, int device, pcbqs_gb300_
     c->g.far = reinterpret_cast<const FarRec *>(base + off_far);
     c->g.cls = reinterpret_cast<const ClsRec *>(base + off_cls);
     c->g.src = reinterpret_cast<const SrcRec *>(base + off_src);
+    c->g.local = reinterpret_cast<const LocalRec *>(base + off_loc);
     for (int k = 0; k < 3; ++k) {
         c->g.obs[k] = reinterpret_cast<const double *>(base + off_obs[k]);
         c->g.w[k] = reinterpret_cast<const double *>(base + off_w[k]);
@@ -296,8 +316,12 @@ int pcbqs_gb300_pairs_device(pcbqs_gb300_ctx *c, const int32_t *p, const int32_t
                            static_cast<cudaStream_t>(stream));
 }
 
+}  // extern "C"
+
 // Fill into device planes; lists grow (and the fill reruns) when the near pairs outnumber their capacity.
-static int fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_only, double *const *planes,
+// T = double: the reference's FP64 moments; T = float: mixed precision, moments about each triangle's centroid.
+template <class T>
+static int fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_only, T *const *planes,
                        int64_t ld, uint64_t *analytic, cudaStream_t stream) {
     const int nt = c->g.nt;
     if (outer < 0 || outer > 2) return fail(ERR_ARGUMENT, "fill: outer_levels must be 0, 1 or 2");
@@ -307,8 +331,9 @@ static int fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_on
         return fail(ERR_ARGUMENT, "fill: missing output plane");
     FillRule rule{near, (near < 0 || std::isinf(near)) ? 1 : 0, outer};
     if (rule.all_near) rule.near = 0;
-    FillPlanes fp{planes[0], scalar_only ? nullptr : planes[1], scalar_only ? nullptr : planes[2],
-                  scalar_only ? nullptr : planes[3], ld, scalar_only};
+    Planes<T> fp{planes[0], scalar_only ? nullptr : planes[1], scalar_only ? nullptr : planes[2],
+                 scalar_only ? nullptr : planes[3], ld, scalar_only};
+    constexpr bool local = std::is_same<T, float>::value;
     const unsigned long long pairs = (unsigned long long)nt * (nt + 1) / 2;
     if (!c->near_capacity) {
         unsigned long long guess = std::max<unsigned long long>(1ull << 16, pairs / 16);
@@ -324,7 +349,8 @@ static int fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_on
                         counter_ptr(c),
                         c->near_capacity};
         CK(cudaMemsetAsync(c->flags.ptr, 0, 2 * sizeof(int), stream));
-        CK(launch_fill(c->g, fp, rule, lists, flag_ptr(c), flag_ptr(c) + 1, stream));
+        if constexpr (local) CK(launch_fill_local(c->g, fp, rule, lists, flag_ptr(c), flag_ptr(c) + 1, stream));
+        else CK(launch_fill(c->g, fp, rule, lists, flag_ptr(c), flag_ptr(c) + 1, stream));
         unsigned long long counts[2];
         CK(cudaMemcpyAsync(counts, lists.count, sizeof counts, cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
@@ -332,7 +358,8 @@ static int fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_on
             c->near_capacity = std::min(pairs, std::max(counts[0], counts[1]) + (1ull << 12));
             continue;
         }
-        CK(launch_fill_near(c->g, fp, rule, lists, flag_ptr(c), stream));
+        if constexpr (local) CK(launch_fill_near_local(c->g, fp, rule, lists, flag_ptr(c), stream));
+        else CK(launch_fill_near(c->g, fp, rule, lists, flag_ptr(c), stream));
         int host[2];
         int rc = read_flags(c, stream, host);
         if (rc) return rc;
@@ -346,11 +373,20 @@ static int fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_on
     return fail(ERR_MEMORY, "fill: near-pair lists did not fit");
 }
 
+extern "C" {
+
 int pcbqs_gb300_fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_only, double *const *planes,
                             int64_t ld, uint64_t *analytic, void *stream) {
     if (!c) return fail(ERR_ARGUMENT, "fill_device: null context");
     DeviceGuard guard(c->device);
-    return fill_device(c, near, outer, scalar_only, planes, ld, analytic, static_cast<cudaStream_t>(stream));
+    return fill_device<double>(c, near, outer, scalar_only, planes, ld, analytic, static_cast<cudaStream_t>(stream));
+}
+
+int pcbqs_gb300_fill_local_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_only, float *const *planes,
+                                  int64_t ld, uint64_t *analytic, void *stream) {
+    if (!c) return fail(ERR_ARGUMENT, "fill_local_device: null context");
+    DeviceGuard guard(c->device);
+    return fill_device<float>(c, near, outer, scalar_only, planes, ld, analytic, static_cast<cudaStream_t>(stream));
 }
 
 int pcbqs_gb300_fill(pcbqs_gb300_ctx *c, double near, int outer, int scalar_only, double *const *planes,
@@ -367,7 +403,7 @@ int pcbqs_gb300_fill(pcbqs_gb300_ctx *c, double near, int outer, int scalar_only
         return fail(ERR_MEMORY, "fill: %d device planes of %d x %d: %s", width, nt, nt, cudaGetErrorString(err));
     double *dev[4] = {nullptr, nullptr, nullptr, nullptr};
     for (int k = 0; k < width; ++k) dev[k] = static_cast<double *>(c->planes.ptr) + k * plane;
-    int rc = fill_device(c, near, outer, scalar_only, dev, nt, analytic, c->stream);
+    int rc = fill_device<double>(c, near, outer, scalar_only, dev, nt, analytic, c->stream);
     if (rc) return rc;
     for (int k = 0; k < width; ++k)
         CK(cudaMemcpyAsync(planes[k], dev[k], sizeof(double) * plane, cudaMemcpyDeviceToHost, c->stream));
@@ -430,6 +466,31 @@ int pcbqs_gb300_edge_inductance(int64_t nt, int64_t ne, const int32_t *tri, cons
     if (rc == OK && (err = cudaStreamSynchronize(s))) rc = cuda_fail(err, "edge_inductance");
     buf.release();
     return rc;
+}
+
+int pcbqs_gb300_edge_inductance_local_device(int64_t ne, const int32_t *tri, const float *alpha, const float *off,
+                                             const float *scale, double factor, const float *mrr, const float *mx,
+                                             const float *my, const float *m0, int64_t ldm, double *L, int64_t ldl,
+                                             float *Lf, int64_t ldlf, void *stream) {
+    if (ne < 0 || ldl < ne || (Lf && ldlf < ne)) return fail(ERR_ARGUMENT, "edge_inductance_local: invalid sizes");
+    if (ne == 0) return OK;
+    if (!tri || !alpha || !off || !scale || !mrr || !mx || !my || !m0 || !L)
+        return fail(ERR_ARGUMENT, "edge_inductance_local: null array");
+    EdgeBasisF e{ne, tri, alpha, off, scale};
+    MomentPlanesF mo{m0, mx, my, mrr, ldm};
+    CK(launch_edge_inductance_local(e, mo, (float)factor, L, ldl, Lf, ldlf, static_cast<cudaStream_t>(stream)));
+    return OK;
+}
+
+int pcbqs_gb300_potential_single_device(int64_t nn, const int64_t *start, const int32_t *members, const double *area,
+                                        const float *m0, int64_t ldm, double factor, double *P, float *Pf,
+                                        int64_t ldp, void *stream) {
+    if (nn < 0 || ldp < nn) return fail(ERR_ARGUMENT, "potential_single: invalid sizes");
+    if (nn == 0) return OK;
+    if (!start || !members || !area || !m0 || !P) return fail(ERR_ARGUMENT, "potential_single: null array");
+    NodeGroups ng{nn, start, members, area};
+    CK(launch_potential_single(ng, m0, ldm, factor, P, Pf, ldp, static_cast<cudaStream_t>(stream)));
+    return OK;
 }
 
 int pcbqs_gb300_potential_device(int64_t nn, const int64_t *start, const int32_t *members, const double *area,

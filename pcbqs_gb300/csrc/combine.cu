@@ -90,9 +90,82 @@ __global__ void __launch_bounds__(CT_THREADS) k_edge_inductance(EdgeBasis e, Mom
     }
 }
 
-// P[a,b] = factor * (sum_{t in a} sum_{u in b} M0[t,u]) / (A_a A_b), node members in CSR form.
-__global__ void __launch_bounds__(CT_THREADS) k_potential(NodeGroups ng, const double *m0, int64_t ldm,
-                                                          double factor, double *P, int64_t ldp) {
+// Mixed precision: the same combination from moments about each triangle's centroid c (FP32 planes), with the
+// supports' offsets a = c_p - v_m, b = c_q - v_n:
+//   L[m,n] = factor s_m s_n sum a_mi a_nj [Rr(p,q) + b.Ro(p,q) + a.Ro(q,p) + (a.b) M0(p,q)]
+// Every term is of the size of the triangles, so FP32 arithmetic keeps FP32 accuracy. Writes L in FP64 (the outer
+// refinement's operator) and its FP32 copy (the inner products).
+__global__ void __launch_bounds__(CT_THREADS) k_edge_inductance_local(EdgeBasisF e, MomentPlanesF mo, float factor,
+                                                                      double *L, int64_t ldl, float *Lf,
+                                                                      int64_t ldlf) {
+    __shared__ float tr[CT][CT + 1];
+    const int64_t ne = e.ne;
+    const int nb = (int)((ne + CT - 1) / CT);
+    const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int bm, bn;
+        upper_tile(t, nb, bm, bn);
+        const int64_t m0 = (int64_t)bm * CT, n0 = (int64_t)bn * CT;
+        const bool diagonal = bm == bn;
+        const int64_t n = n0 + lane;
+        int q[2] = {0, 0};
+        float an[2] = {0, 0}, bx[2] = {0, 0}, by[2] = {0, 0}, sn = 0;
+        if (n < ne) {
+            for (int j = 0; j < 2; ++j) {
+                q[j] = e.tri[j * ne + n];
+                an[j] = e.alpha[j * ne + n];
+                bx[j] = e.off[2 * (j * ne + n)];
+                by[j] = e.off[2 * (j * ne + n) + 1];
+            }
+            sn = e.scale[n];
+        }
+#pragma unroll 1
+        for (int i = 0; i < CT_ROWS; ++i) {
+            const int ml = warp + (CT_THREADS / 32) * i;
+            const int64_t m = m0 + ml;
+            const bool valid = m < ne && n < ne && (!diagonal || ml <= lane);
+            float value = 0;
+            if (valid) {
+                float sum = 0;
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    const int64_t p = e.tri[a * ne + m];
+                    const float am = e.alpha[a * ne + m];
+                    const float ax = e.off[2 * (a * ne + m)], ay = e.off[2 * (a * ne + m) + 1];
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) {
+                        const size_t pq = (size_t)p * mo.ld + q[b], qp = (size_t)q[b] * mo.ld + p;
+                        sum += am * an[b] *
+                               (mo.mrr[pq] + bx[b] * mo.mx[pq] + by[b] * mo.my[pq] + ax * mo.mx[qp] +
+                                ay * mo.my[qp] + (ax * bx[b] + ay * by[b]) * mo.m0[pq]);
+                    }
+                }
+                value = factor * e.scale[m] * sn * sum;
+                L[(size_t)m * ldl + n] = value;
+                if (Lf) Lf[(size_t)m * ldlf + n] = value;
+            }
+            tr[lane][ml] = valid ? value : 0.0f;
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int i = 0; i < CT_ROWS; ++i) {
+            const int nl = warp + (CT_THREADS / 32) * i, ml = lane;
+            const int64_t nn = n0 + nl, m = m0 + ml;
+            if (nn < ne && m < ne && (!diagonal || ml < nl)) {
+                L[(size_t)nn * ldl + m] = tr[nl][ml];
+                if (Lf) Lf[(size_t)nn * ldlf + m] = tr[nl][ml];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// P[a,b] = factor * (sum_{t in a} sum_{u in b} M0[t,u]) / (A_a A_b), node members in CSR form; M0 in FP64 or (mixed
+// precision) FP32, the sums in FP64; Pf (nullable) receives an FP32 copy.
+template <class T>
+__global__ void __launch_bounds__(CT_THREADS) k_potential(NodeGroups ng, const T *m0, int64_t ldm, double factor,
+                                                          double *P, int64_t ldp, float *Pf) {
     __shared__ double tr[CT][CT + 1];
     const int64_t nn = ng.nn;
     const int nb = (int)((nn + CT - 1) / CT);
@@ -118,11 +191,12 @@ __global__ void __launch_bounds__(CT_THREADS) k_potential(NodeGroups ng, const d
                 for (int64_t x = ng.start[a]; x < ng.start[a + 1]; ++x) {
                     const size_t row = (size_t)ng.members[x] * ldm;
                     double r = 0;
-                    for (int64_t y = bs; y < be; ++y) r += m0[row + ng.members[y]];
+                    for (int64_t y = bs; y < be; ++y) r += (double)m0[row + ng.members[y]];
                     s += r;
                 }
                 value = s / (ng.area[a] * area_b) * factor;
                 P[(size_t)a * ldp + b] = value;
+                if (Pf) Pf[(size_t)a * ldp + b] = (float)value;
             }
             tr[lane][al] = valid ? value : 0.0;
         }
@@ -131,7 +205,10 @@ __global__ void __launch_bounds__(CT_THREADS) k_potential(NodeGroups ng, const d
         for (int i = 0; i < CT_ROWS; ++i) {
             const int bl = warp + (CT_THREADS / 32) * i, al = lane;
             const int64_t bb2 = b0 + bl, a = a0 + al;
-            if (bb2 < nn && a < nn && (!diagonal || al < bl)) P[(size_t)bb2 * ldp + a] = tr[bl][al];
+            if (bb2 < nn && a < nn && (!diagonal || al < bl)) {
+                P[(size_t)bb2 * ldp + a] = tr[bl][al];
+                if (Pf) Pf[(size_t)bb2 * ldp + a] = (float)tr[bl][al];
+            }
         }
         __syncthreads();
     }
@@ -161,7 +238,29 @@ cudaError_t launch_potential(const NodeGroups &ng, const double *m0, int64_t ldm
     const int64_t nb = (ng.nn + CT - 1) / CT;
     const int64_t ntiles = nb * (nb + 1) / 2;
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms() * 8);
-    k_potential<<<(unsigned)grid, CT_THREADS, 0, stream>>>(ng, m0, ldm, factor, P, ldp);
+    k_potential<double><<<(unsigned)grid, CT_THREADS, 0, stream>>>(ng, m0, ldm, factor, P, ldp, nullptr);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_potential_single(const NodeGroups &ng, const float *m0, int64_t ldm, double factor, double *P,
+                                    float *Pf, int64_t ldp, cudaStream_t stream) {
+    if (ng.nn <= 0) return cudaSuccess;
+    const int64_t nb = (ng.nn + CT - 1) / CT;
+    const int64_t ntiles = nb * (nb + 1) / 2;
+    const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms() * 8);
+    k_potential<float><<<(unsigned)grid, CT_THREADS, 0, stream>>>(ng, m0, ldm, factor, P, ldp, Pf);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edge_inductance_local(const EdgeBasisF &e, const MomentPlanesF &mo, float factor, double *L,
+                                         int64_t ldl, float *Lf, int64_t ldlf, cudaStream_t stream) {
+    if (e.ne <= 0) return cudaSuccess;
+    const int64_t nb = (e.ne + CT - 1) / CT;
+    const int64_t ntiles = nb * (nb + 1) / 2;
+    const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms() * 8);
+    k_edge_inductance_local<<<(unsigned)grid, CT_THREADS, 0, stream>>>(e, mo, factor, L, ldl, Lf, ldlf);
     note_launches(1);
     return cudaGetLastError();
 }

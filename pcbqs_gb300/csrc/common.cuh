@@ -31,6 +31,9 @@ void note_launches(long long count);
 struct alignas(64) FarRec { double p[6]; double area; double z; };
 struct alignas(32) ClsRec { double cx, cy, radius, z; };
 struct alignas(64) SrcRec { double v[6]; double tau[6]; double un[6]; double len[3]; double area; double pad[2]; };
+//   LocalRec 48 B (mixed precision): the centroid split in two floats (chi + clo), the three rule points as float
+//   offsets from the centroid, area and z as floats.
+struct alignas(16) LocalRec { float chi[2]; float clo[2]; float u[6]; float area; float z; };
 
 // Device geometry of one mesh. Observation rules: obs[k] (nt, nq[k], 2) points, w[k] (nq[k]) weights.
 struct Geometry {
@@ -38,6 +41,7 @@ struct Geometry {
     const FarRec *far;
     const ClsRec *cls;
     const SrcRec *src;
+    const LocalRec *local;
     const double *obs[3];
     const double *w[3];
     int nq[3];

@@ -10,125 +10,10 @@
 #include <cmath>
 #include "common.cuh"
 #include "fill.cuh"
+#include "pairs.cuh"
 #include "tma.cuh"
 
 namespace pq {
-
-// ---------------------------------------------------------------------------------------------------------------
-// Pair moments. m = (M0, Mro_x, Mro_y, Mrs_x, Mrs_y, Mrr) of the ordered pair (observation a, source b).
-
-// Far pairs: g_ij = (A_a A_b / 9) / sqrt(|x_i - s_j|^2 + d^2) over the 3 x 3 rule points; the sums are taken
-// per observation point (row sums) so each point multiplies once.
-__device__ __forceinline__ void far_moments(const FarRec &a, const FarRec &b, double d, bool scalar, double *m) {
-    const double w = a.area * b.area / 9.0;
-    const double d2 = d * d;
-    double m0 = 0, ro_x = 0, ro_y = 0, rs_x = 0, rs_y = 0, rr = 0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const double x = a.p[2 * i], y = a.p[2 * i + 1];
-        double g_sum = 0, gsx = 0, gsy = 0;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const double sx = b.p[2 * j], sy = b.p[2 * j + 1];
-            const double dx = x - sx, dy = y - sy;
-            const double g = w * rsqrt(dx * dx + dy * dy + d2);
-            g_sum += g;
-            if (!scalar) { gsx += g * sx; gsy += g * sy; }
-        }
-        m0 += g_sum;
-        if (!scalar) {
-            ro_x += g_sum * x; ro_y += g_sum * y;
-            rs_x += gsx; rs_y += gsy;
-            rr += x * gsx + y * gsy;
-        }
-    }
-    m[0] = m0; m[1] = ro_x; m[2] = ro_y; m[3] = rs_x; m[4] = rs_y; m[5] = rr;
-}
-
-// asinh(s+/r0) - asinh(s-/r0) with s+ = s- + L, r-+ = sqrt(r0^2 + s-+^2), as one logarithm. From
-// asinh(s/r0) = sign(s) log((|s| + r)/r0): both ends on one side of the foot point give a ratio of two sums of
-// positive terms, straddling ends a product over r0^2 -- no term cancels, where the difference of two inverse
-// hyperbolic sines loses the leading digits when s- and s+ are large and close.
-__device__ __forceinline__ double asinh_difference(double sm, double sp, double rm, double rp, double r02) {
-    if (sm >= 0) return log((sp + rp) / (sm + rm));
-    if (sp <= 0) return log((rm - sm) / (rp - sp));
-    return log((sp + rp) * (rm - sm) / r02);
-}
-
-// atan2(t0 s+, r0^2 + |d| r+) - atan2(t0 s-, r0^2 + |d| r-) as one arctangent: both denominators are positive,
-// so each angle lies in (-pi/2, pi/2) and the difference is atan2(y1 x2 - y2 x1, x1 x2 + y1 y2) with no wrap. The
-// cross term y1 x2 - y2 x1 = t0 (L r0^2 + |d| (s+ r- - s- r+)) is formed without cancellation: for ends on one
-// side, s+ r- - s- r+ = r0^2 L (s+ + s-) / (s+ r- + s- r+); for straddling ends both of its terms are positive.
-__device__ __forceinline__ double atan2_difference(double t0, double sm, double sp, double rm, double rp,
-                                                   double r02, double ad, double le) {
-    const double cross = (sm >= 0 || sp <= 0) ? r02 * le * (sp + sm) / (sp * rm + sm * rp) : sp * rm - sm * rp;
-    const double x1 = r02 + ad * rp, x2 = r02 + ad * rm;
-    return atan2(t0 * (le * r02 + ad * cross), x1 * x2 + t0 * t0 * sp * sm);
-}
-
-// Near pairs: for each observation point x_j of triangle a (level-k rule) and each edge e of source triangle b,
-// the closed-form inner integrals of 1/R and of the edge term over b at height offset d:
-//   s- = (V_e - x).tau_e, s+ = s- + L_e, t0 = (V_e - x).u_e, r0 = sqrt(t0^2 + d^2), r-+ = sqrt(r0^2 + s-+^2)
-//   lg = asinh(s+/r0) - asinh(s-/r0)  (0 when r0 <= 1e-14 L_e)
-//   I1 += t0 lg - |d| (atan2(t0 s+, r0^2 + |d| r+) - atan2(t0 s-, r0^2 + |d| r-))
-//   IR += 1/2 (r0^2 lg + s+ r+ - s- r-) u_e
-// accumulated with weights A_a w_j into M0 = sum w I1, Mro = sum w x I1, Mrs = sum w (IR + x I1),
-// Mrr = sum w x.(IR + x I1).
-__device__ __forceinline__ void near_moments(const double *obs, const double *wts, int nq, double area_a,
-                                             const SrcRec &b, double d, bool scalar, double *m) {
-    const double ad = fabs(d);
-    const double d2 = d * d;
-    double m0 = 0, ro_x = 0, ro_y = 0, rs_x = 0, rs_y = 0, rr = 0;
-    for (int j = 0; j < nq; ++j) {
-        const double x = obs[2 * j], y = obs[2 * j + 1];
-        double i1 = 0, irx = 0, iry = 0;
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-            const double vx = b.v[2 * e] - x, vy = b.v[2 * e + 1] - y;
-            const double le = b.len[e];
-            const double sm = vx * b.tau[2 * e] + vy * b.tau[2 * e + 1];
-            const double sp = sm + le;
-            const double t0 = vx * b.un[2 * e] + vy * b.un[2 * e + 1];
-            const double r02 = t0 * t0 + d2, r0 = sqrt(r02);
-            const double rm = sqrt(r02 + sm * sm), rp = sqrt(r02 + sp * sp);
-            const double lg = r0 > 1e-14 * le ? asinh_difference(sm, sp, rm, rp, r02) : 0.0;
-            double inner = t0 * lg;
-            if (ad > 0) inner -= ad * atan2_difference(t0, sm, sp, rm, rp, r02, ad, le);
-            i1 += inner;
-            if (!scalar) {
-                const double er = 0.5 * (r02 * lg + sp * rp - sm * rm);
-                irx += er * b.un[2 * e];
-                iry += er * b.un[2 * e + 1];
-            }
-        }
-        const double w = area_a * wts[j];
-        m0 += w * i1;
-        if (!scalar) {
-            const double sx = irx + x * i1, sy = iry + y * i1;
-            ro_x += w * x * i1; ro_y += w * y * i1;
-            rs_x += w * sx; rs_y += w * sy;
-            rr += w * (x * sx + y * sy);
-        }
-    }
-    m[0] = m0; m[1] = ro_x; m[2] = ro_y; m[3] = rs_x; m[4] = rs_y; m[5] = rr;
-}
-
-__device__ __forceinline__ void pair_moments(const Geometry &g, int a, int b, double d, int k, bool scalar,
-                                             double *m) {
-    if (k < 0) {
-        far_moments(g.far[a], g.far[b], d, scalar, m);
-    } else {
-        const int nq = g.nq[k];
-        near_moments(g.obs[k] + 2 * (size_t)a * nq, g.w[k], nq, g.far[a].area, g.src[b], d, scalar, m);
-    }
-}
-
-__device__ __forceinline__ bool finite6(const double *m, bool scalar) {
-    bool ok = isfinite(m[0]);
-    if (!scalar)
-        for (int j = 1; j < 6; ++j) ok = ok && isfinite(m[j]);
-    return ok;
-}
 
 // ---------------------------------------------------------------------------------------------------------------
 // Explicit pair lists (the plugin's evaluate): kind-sorted so a warp never mixes far and near work.
@@ -195,6 +80,7 @@ constexpr int ROWS_PER_WARP = TILE / (FILL_THREADS / 32);
 
 struct FillSmem {
     FarRec far_r[TILE], far_c[TILE];
+    LocalRec loc_r[TILE], loc_c[TILE];
     ClsRec cls_r[TILE], cls_c[TILE];
     double t[4][TILE][TILE + 1];          // transposed staging: [plane][q_local][p_local]
     unsigned char keep[TILE][TILE];        // [q_local][p_local]: 1 when the reverse entry is written here
@@ -213,7 +99,10 @@ __device__ __forceinline__ void tile_of(int64_t t, int nb, int &bp, int &bq) {
     bq = r + (int)(t - off(r));
 }
 
-__global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, FillPlanes out, FillRule rule,
+// LOCAL = false: the reference's FP64 moments in centred coordinates into FP64 planes (T = double).
+// LOCAL = true:  mixed precision -- far pairs as FP32 local moments, planes in FP32 (T = float).
+template <class T, bool LOCAL>
+__global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, Planes<T> out, FillRule rule,
                                                              NearLists lists, int *nonfinite, int *status) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     FillSmem &s = *reinterpret_cast<FillSmem *>(smem_raw);
@@ -236,11 +125,17 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, FillPla
         const int np = min(TILE, nt - p0), nqn = min(TILE, nt - q0);
         const bool diagonal = bp == bq;
         if (threadIdx.x == 0) {
-            const uint32_t bytes = (uint32_t)(np + nqn) * (sizeof(FarRec) + sizeof(ClsRec));
+            const uint32_t rec = LOCAL ? sizeof(LocalRec) : sizeof(FarRec);
+            const uint32_t bytes = (uint32_t)(np + nqn) * (rec + sizeof(ClsRec));
             mbar_arrive_expect_tx(&s.bar, bytes);
-            bulk_load(s.far_r, g.far + p0, np * sizeof(FarRec), &s.bar);
+            if (LOCAL) {
+                bulk_load(s.loc_r, g.local + p0, np * sizeof(LocalRec), &s.bar);
+                bulk_load(s.loc_c, g.local + q0, nqn * sizeof(LocalRec), &s.bar);
+            } else {
+                bulk_load(s.far_r, g.far + p0, np * sizeof(FarRec), &s.bar);
+                bulk_load(s.far_c, g.far + q0, nqn * sizeof(FarRec), &s.bar);
+            }
             bulk_load(s.cls_r, g.cls + p0, np * sizeof(ClsRec), &s.bar);
-            bulk_load(s.far_c, g.far + q0, nqn * sizeof(FarRec), &s.bar);
             bulk_load(s.cls_c, g.cls + q0, nqn * sizeof(ClsRec), &s.bar);
         }
         if (!mbar_wait_bounded(&s.bar, phase)) failed = true;
@@ -282,19 +177,20 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, FillPla
             const bool far = valid && k < 0;
             double m[6] = {0, 0, 0, 0, 0, 0};
             if (far) {
-                far_moments(s.far_r[pl], s.far_c[ql], d, scalar, m);
+                if (LOCAL) far_local(s.loc_r[pl], s.loc_c[ql], scalar, m);
+                else far_moments(s.far_r[pl], s.far_c[ql], d, scalar, m);
                 bad = bad || !finite6(m, scalar);
                 const size_t pq = (size_t)p * out.ld + q;
-                out.m0[pq] = m[0];
+                out.m0[pq] = (T)m[0];
                 if (!scalar) {
                     if (p == q) {
-                        out.mx[pq] = (m[1] + m[3]) / 2;
-                        out.my[pq] = (m[2] + m[4]) / 2;
+                        out.mx[pq] = (T)((m[1] + m[3]) / 2);
+                        out.my[pq] = (T)((m[2] + m[4]) / 2);
                     } else {
-                        out.mx[pq] = m[1];
-                        out.my[pq] = m[2];
+                        out.mx[pq] = (T)m[1];
+                        out.my[pq] = (T)m[2];
                     }
-                    out.mrr[pq] = m[5];
+                    out.mrr[pq] = (T)m[5];
                 }
             }
             const bool reverse = far && p != q;
@@ -313,11 +209,11 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, FillPla
             const int ql = warp + (FILL_THREADS / 32) * i, pl = lane;
             if (ql < nqn && pl < np && s.keep[ql][pl]) {
                 const size_t qp = (size_t)(q0 + ql) * out.ld + (p0 + pl);
-                out.m0[qp] = s.t[0][ql][pl];
+                out.m0[qp] = (T)s.t[0][ql][pl];
                 if (!scalar) {
-                    out.mx[qp] = s.t[1][ql][pl];
-                    out.my[qp] = s.t[2][ql][pl];
-                    out.mrr[qp] = s.t[3][ql][pl];
+                    out.mx[qp] = (T)s.t[1][ql][pl];
+                    out.my[qp] = (T)s.t[2][ql][pl];
+                    out.mrr[qp] = (T)s.t[3][ql][pl];
                 }
             }
         }
@@ -327,7 +223,8 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, FillPla
 }
 
 // Near pairs of one level, grid-stride over the compacted list; both reciprocal entries written.
-__global__ void k_fill_near(Geometry g, FillPlanes out, const int2 *list, const unsigned long long *count,
+template <class T, bool LOCAL>
+__global__ void k_fill_near(Geometry g, Planes<T> out, const int2 *list, const unsigned long long *count,
                             unsigned long long capacity, int level, int *nonfinite) {
     const unsigned long long n = min(*count, capacity);
     const bool scalar = out.scalar;
@@ -340,19 +237,20 @@ __global__ void k_fill_near(Geometry g, FillPlanes out, const int2 *list, const 
         double m[6];
         pair_moments(g, p, q, d, level, scalar, m);
         bad = bad || !finite6(m, scalar);
+        if (LOCAL && !scalar) to_local(g.cls[p], g.cls[q], m);
         const size_t fwd = (size_t)p * out.ld + q, rev = (size_t)q * out.ld + p;
-        out.m0[fwd] = m[0];
-        out.m0[rev] = m[0];
+        out.m0[fwd] = (T)m[0];
+        out.m0[rev] = (T)m[0];
         if (!scalar) {
             if (p == q) {
-                out.mx[fwd] = (m[1] + m[3]) / 2;
-                out.my[fwd] = (m[2] + m[4]) / 2;
+                out.mx[fwd] = (T)((m[1] + m[3]) / 2);
+                out.my[fwd] = (T)((m[2] + m[4]) / 2);
             } else {
-                out.mx[fwd] = m[1]; out.my[fwd] = m[2];
-                out.mx[rev] = m[3]; out.my[rev] = m[4];
+                out.mx[fwd] = (T)m[1]; out.my[fwd] = (T)m[2];
+                out.mx[rev] = (T)m[3]; out.my[rev] = (T)m[4];
             }
-            out.mrr[fwd] = m[5];
-            out.mrr[rev] = m[5];
+            out.mrr[fwd] = (T)m[5];
+            out.mrr[rev] = (T)m[5];
         }
     }
     if (bad) *nonfinite = 1;
@@ -407,38 +305,59 @@ cudaError_t launch_pairs(const Geometry &g, const int32_t *p, const int32_t *q, 
 
 size_t fill_smem_bytes() { return sizeof(FillSmem) + 128; }
 
-cudaError_t launch_fill(const Geometry &g, const FillPlanes &out, const FillRule &rule, const NearLists &lists,
-                        int *nonfinite, int *status, cudaStream_t stream) {
+template <class T, bool LOCAL>
+static cudaError_t launch_fill_t(const Geometry &g, const Planes<T> &out, const FillRule &rule,
+                                 const NearLists &lists, int *nonfinite, int *status, cudaStream_t stream) {
     const int nb = (g.nt + TILE - 1) / TILE;
     const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
     const size_t smem = fill_smem_bytes();
     static bool configured = false;
     if (!configured) {
-        cudaFuncSetAttribute(k_fill_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_fill_tiles<T, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = true;
     }
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_tiles, FILL_THREADS, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_tiles<T, LOCAL>, FILL_THREADS, smem);
     if (per_sm < 1) per_sm = 1;
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sm_count() * per_sm);
     cudaMemsetAsync(lists.count, 0, 2 * sizeof(unsigned long long), stream);
-    k_fill_tiles<<<(unsigned)grid, FILL_THREADS, smem, stream>>>(g, out, rule, lists, nonfinite, status);
+    k_fill_tiles<T, LOCAL><<<(unsigned)grid, FILL_THREADS, smem, stream>>>(g, out, rule, lists, nonfinite, status);
     note_launches(1);
-    cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) return err;
-    return cudaSuccess;
+    return cudaGetLastError();
+}
+
+template <class T, bool LOCAL>
+static cudaError_t launch_near_t(const Geometry &g, const Planes<T> &out, const FillRule &rule,
+                                 const NearLists &lists, int *nonfinite, cudaStream_t stream) {
+    const int threads = 128;
+    const int blocks = sm_count() * 8;
+    k_fill_near<T, LOCAL><<<blocks, threads, 0, stream>>>(g, out, lists.pair[0], lists.count, lists.capacity, 0,
+                                                          nonfinite);
+    if (rule.outer > 0)
+        k_fill_near<T, LOCAL><<<blocks, threads, 0, stream>>>(g, out, lists.pair[1], lists.count + 1,
+                                                              lists.capacity, rule.outer, nonfinite);
+    note_launches(rule.outer > 0 ? 2 : 1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill(const Geometry &g, const FillPlanes &out, const FillRule &rule, const NearLists &lists,
+                        int *nonfinite, int *status, cudaStream_t stream) {
+    return launch_fill_t<double, false>(g, out, rule, lists, nonfinite, status, stream);
 }
 
 cudaError_t launch_fill_near(const Geometry &g, const FillPlanes &out, const FillRule &rule, const NearLists &lists,
                              int *nonfinite, cudaStream_t stream) {
-    const int threads = 128;
-    const int blocks = sm_count() * 8;
-    k_fill_near<<<blocks, threads, 0, stream>>>(g, out, lists.pair[0], lists.count, lists.capacity, 0, nonfinite);
-    if (rule.outer > 0)
-        k_fill_near<<<blocks, threads, 0, stream>>>(g, out, lists.pair[1], lists.count + 1, lists.capacity,
-                                                    rule.outer, nonfinite);
-    note_launches(rule.outer > 0 ? 2 : 1);
-    return cudaGetLastError();
+    return launch_near_t<double, false>(g, out, rule, lists, nonfinite, stream);
+}
+
+cudaError_t launch_fill_local(const Geometry &g, const Planes<float> &out, const FillRule &rule,
+                              const NearLists &lists, int *nonfinite, int *status, cudaStream_t stream) {
+    return launch_fill_t<float, true>(g, out, rule, lists, nonfinite, status, stream);
+}
+
+cudaError_t launch_fill_near_local(const Geometry &g, const Planes<float> &out, const FillRule &rule,
+                                   const NearLists &lists, int *nonfinite, cudaStream_t stream) {
+    return launch_near_t<float, true>(g, out, rule, lists, nonfinite, stream);
 }
 
 }  // namespace pq

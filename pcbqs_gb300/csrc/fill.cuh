@@ -6,11 +6,12 @@
 namespace pq {
 
 // Output moment planes M0, Mx, My, Mrr (row-major, leading dimension ld >= nt). scalar: M0 only.
-struct FillPlanes {
-    double *m0, *mx, *my, *mrr;
+template <class T> struct Planes {
+    T *m0, *mx, *my, *mrr;
     int64_t ld;
     int scalar;
 };
+using FillPlanes = Planes<double>;
 
 struct FillRule {
     double near;     // analytic when distance <= near * (r_p + r_q)
@@ -32,6 +33,11 @@ cudaError_t launch_fill(const Geometry &g, const FillPlanes &out, const FillRule
                         int *nonfinite, int *status, cudaStream_t stream);
 cudaError_t launch_fill_near(const Geometry &g, const FillPlanes &out, const FillRule &rule, const NearLists &lists,
                              int *nonfinite, cudaStream_t stream);
+// Mixed precision: FP32 planes of moments about each triangle's centroid (far pairs in FP32, near pairs FP64).
+cudaError_t launch_fill_local(const Geometry &g, const Planes<float> &out, const FillRule &rule,
+                              const NearLists &lists, int *nonfinite, int *status, cudaStream_t stream);
+cudaError_t launch_fill_near_local(const Geometry &g, const Planes<float> &out, const FillRule &rule,
+                                   const NearLists &lists, int *nonfinite, cudaStream_t stream);
 size_t fill_smem_bytes();
 
 }  // namespace pq

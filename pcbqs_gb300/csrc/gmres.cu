@@ -273,6 +273,36 @@ cudaError_t column_norms(int64_t n, int k, const cd *x, double *out, double *scr
     return cudaGetLastError();
 }
 
+__global__ void k_scatter_add_cols(int64_t n, int k, int ka, const int *act, const cd *compact, cd *full) {
+    const int64_t total = n * ka;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / ka;
+        const int c = (int)(idx % ka);
+        full[r * k + act[c]] = cadd(full[r * k + act[c]], compact[idx]);
+    }
+}
+
+cudaError_t gather_columns(int64_t n, int k, int ka, const int *act, const cd *full, cd *compact, cudaStream_t s) {
+    k_gather_cols<<<grid_for(n * ka), 256, 0, s>>>(n, k, ka, act, full, compact);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t scatter_add_columns(int64_t n, int k, int ka, const int *act, const cd *compact, cd *full,
+                                cudaStream_t s) {
+    k_scatter_add_cols<<<grid_for(n * ka), 256, 0, s>>>(n, k, ka, act, compact, full);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t subtract_from(int64_t count, const cd *b, cd *a, cudaStream_t s) {
+    k_rsub<<<grid_for(count), 256, 0, s>>>(count, b, a);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+
 namespace {
 
 struct Scratch {
@@ -434,6 +464,64 @@ cudaError_t gmres_batched(Operator &A, Preconditioner *M, int k, const int32_t *
     report.launches = launches;
     note_launches(launches);
     for (int c = 0; c < k; ++c) report.iterations[c] = its_host[c];
+    return cudaGetLastError();
+}
+
+cudaError_t refine_batched(Operator &A, Operator &A32, Preconditioner *M, int k, const int32_t *sys_host,
+                           const cd *b, cd *x, const RefineOptions &opt, GmresReport &report, int &outer_steps,
+                           cudaStream_t st) {
+    const int64_t n = A.n();
+    report.iterations.assign(k, 0);
+    report.residual.assign(k, 0.0);
+    outer_steps = 0;
+    if (k <= 0 || n <= 0) return cudaSuccess;
+    Scratch mem;
+    cd *r = mem.get<cd>((size_t)n * k), *rc = mem.get<cd>((size_t)n * k), *dc = mem.get<cd>((size_t)n * k);
+    double *part = mem.get<double>((size_t)NCHUNK * k), *norm = mem.get<double>(k);
+    int *act_dev = mem.get<int>(k), *sys_dev = mem.get<int>(k);
+    if (mem.err != cudaSuccess) return mem.err;
+    std::vector<int32_t> sys_all(sys_host, sys_host + k);
+    cudaMemcpyAsync(sys_dev, sys_all.data(), sizeof(int) * k, cudaMemcpyHostToDevice, st);
+    cudaError_t err;
+    if ((err = column_norms(n, k, b, norm, part, st))) return err;
+    note_launches(2);
+    std::vector<double> bn(k), rn(k);
+    cudaMemcpyAsync(bn.data(), norm, sizeof(double) * k, cudaMemcpyDeviceToHost, st);
+    if ((err = cudaStreamSynchronize(st))) return err;
+    for (int outer = 0; outer <= opt.max_outer; ++outer) {
+        // the true residual of every column, with the FP64 operator
+        cudaMemcpyAsync(sys_dev, sys_all.data(), sizeof(int) * k, cudaMemcpyHostToDevice, st);
+        if ((err = A.apply(k, sys_dev, x, r, st))) return err;
+        if ((err = subtract_from((int64_t)n * k, b, r, st))) return err;
+        if ((err = column_norms(n, k, r, norm, part, st))) return err;
+        note_launches(2);
+        cudaMemcpyAsync(rn.data(), norm, sizeof(double) * k, cudaMemcpyDeviceToHost, st);
+        if ((err = cudaStreamSynchronize(st))) return err;
+        std::vector<int> act;
+        std::vector<int32_t> sys_act;
+        for (int c = 0; c < k; ++c) {
+            report.residual[c] = bn[c] > 0 ? rn[c] / bn[c] : 0.0;
+            if (report.residual[c] > opt.tol) {
+                act.push_back(c);
+                sys_act.push_back(sys_all[c]);
+            }
+        }
+        if (act.empty() || outer == opt.max_outer) break;
+        ++outer_steps;
+        const int ka = (int)act.size();
+        cudaMemcpyAsync(act_dev, act.data(), sizeof(int) * ka, cudaMemcpyHostToDevice, st);
+        if ((err = gather_columns(n, k, ka, act_dev, r, rc, st))) return err;
+        cudaMemsetAsync(dc, 0, sizeof(cd) * n * ka, st);
+        GmresOptions inner;
+        inner.tol = opt.inner_tol;
+        inner.maxiter = opt.inner_maxiter;
+        inner.restart = opt.restart;
+        GmresReport rep;
+        if ((err = gmres_batched(A32, M, ka, sys_act.data(), rc, dc, inner, rep, st))) return err;
+        for (int c = 0; c < ka; ++c) report.iterations[act[c]] += rep.iterations[c];
+        cudaMemcpyAsync(act_dev, act.data(), sizeof(int) * ka, cudaMemcpyHostToDevice, st);
+        if ((err = scatter_add_columns(n, k, ka, act_dev, dc, x, st))) return err;
+    }
     return cudaGetLastError();
 }
 

@@ -273,6 +273,16 @@ template <class T> static cudaError_t dev_alloc(T **p, size_t count) {
     return cudaMalloc(reinterpret_cast<void **>(p), std::max<size_t>(count, 1) * sizeof(T));
 }
 
+__global__ void k_to_f32(int64_t count, const double *in, float *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x)
+        out[t] = (float)in[t];
+}
+
+__global__ void k_to_f64(int64_t count, const float *in, double *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x)
+        out[t] = (double)in[t];
+}
+
 struct PeecOp : Operator {
     int64_t n_ = 0, nb = 0, ne = 0, nn = 0;
     Csr K, Kt, T, Tt, R;
@@ -302,18 +312,51 @@ struct PeecOp : Operator {
         return cudaSuccess;
     }
 
-    cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) override {
+    // Single-precision copies of L and P for the inner products of the mixed solve (set by peec_single).
+    const float *Lf = nullptr, *Pf = nullptr;
+    int64_t ldlf = 0, ldpf = 0;
+    float *xf = nullptr, *yf = nullptr;
+    int capf = 0;
+
+    // y (rows x k complex128) = M x for a dense symmetric M, in FP64 (cuBLAS DGEMM) or through its single-precision
+    // copy (SGEMM on converted vectors) when `single`.
+    cudaError_t dense(bool single, int64_t rows, int k, const double *M, int64_t ld, const float *Mf, int64_t ldf,
+                      const cd *x, cd *y, cudaStream_t s) {
+        if (!single) {
+            if (gemm_real_sym(blas, rows, k, M, ld, x, y) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+            return cudaSuccess;
+        }
+        const int64_t need = std::max(ne, nn) * 2 * k;
+        if (need > capf) {
+            cudaFree(xf);
+            cudaFree(yf);
+            xf = yf = nullptr;
+            cudaError_t e;
+            if ((e = dev_alloc(&xf, need)) || (e = dev_alloc(&yf, need))) return e;
+            capf = (int)need;
+        }
+        k_to_f32<<<grid_of(rows * 2 * k), 256, 0, s>>>(rows * 2 * k, reinterpret_cast<const double *>(x), xf);
+        const float one = 1.0f, zero = 0.0f;
+        if (cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * k, (int)rows, (int)rows, &one, xf, 2 * k, Mf, (int)ldf,
+                        &zero, yf, 2 * k) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        k_to_f64<<<grid_of(rows * 2 * k), 256, 0, s>>>(rows * 2 * k, yf, reinterpret_cast<double *>(y));
+        note_launches(2);
+        return cudaSuccess;
+    }
+
+    cudaError_t apply_impl(bool single, int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) {
         cudaError_t e = reserve(k);
         if (e) return e;
         cublasSetStream(blas, s);
         k_tree_scale<<<grid_of(n_ * k), 256, 0, s>>>(n_, k, is_tree, walpha, sys, in, u);
         k_spmm<<<grid_of(nb * k), 256, 0, s>>>(K, k, u, branch, nullptr, sys, 0);
-        if (gemm_real_sym(blas, ne, k, L, ldl, branch, lb) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+        if ((e = dense(single, ne, k, L, ldl, Lf, ldlf, branch, lb, s))) return e;
         k_impedance<<<grid_of(nb * k), 256, 0, s>>>(R, nb, k, branch, lb, omega, sys, v);
         k_spmm<<<grid_of(n_ * k), 256, 0, s>>>(Kt, k, v, out, inv_z, sys, 0);
         if (nn > 0) {
             k_spmm<<<grid_of(nn * k), 256, 0, s>>>(T, k, in, tq, nullptr, sys, 0);
-            if (gemm_real_sym(blas, nn, k, P, ldp, tq, pq) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+            if ((e = dense(single, nn, k, P, ldp, Pf, ldpf, tq, pq, s))) return e;
             k_spmm<<<grid_of(n_ * k), 256, 0, s>>>(Tt, k, pq, out, inv_p, sys, 1);
         }
         launches += nn > 0 ? 6 : 3;
@@ -321,10 +364,25 @@ struct PeecOp : Operator {
         return cudaGetLastError();
     }
 
+    cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) override {
+        return apply_impl(false, k, sys, in, out, s);
+    }
+
     ~PeecOp() override {
+        cudaFree(xf);
+        cudaFree(yf);
         for (cd *p : {u, branch, lb, v, tq, pq}) cudaFree(p);
         for (double *p : {omega, zscale, walpha, inv_z, inv_p}) cudaFree(p);
         if (blas) cublasDestroy(blas);
+    }
+};
+
+// The same operator with its dense products in single precision (the inner products of the mixed solve).
+struct SingleView : Operator {
+    PeecOp *op = nullptr;
+    int64_t n() const override { return op->n_; }
+    cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) override {
+        return op->apply_impl(true, k, sys, in, out, s);
     }
 };
 
@@ -442,6 +500,85 @@ struct LuPrecond : Preconditioner {
                              reinterpret_cast<cuComplex *>(work), (int)n, info) != CUSOLVER_STATUS_SUCCESS)
             return cudaErrorUnknown;
         k_from_c64_cols<<<grid_of(n * k), 256, 0, s>>>(n, k, work, out);
+        note_launches(2);
+        return cudaGetLastError();
+    }
+};
+
+// Single-precision Cholesky of a dense real SPD matrix (its FP32 copy, cuSOLVER potrf) as a preconditioner for
+// complex right-hand sides: real and imaginary parts solved as 2k real columns.
+__global__ void k_split_cols(int64_t n, int k, const cd *in, float *out) {     // (n,k) complex -> col-major (n,2k)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const int s = (int)(t % k);
+        out[(int64_t)(2 * s) * n + r] = (float)in[t].x;
+        out[(int64_t)(2 * s + 1) * n + r] = (float)in[t].y;
+    }
+}
+
+__global__ void k_join_cols(int64_t n, int k, const float *in, cd *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const int s = (int)(t % k);
+        out[t] = make_double2(in[(int64_t)(2 * s) * n + r], in[(int64_t)(2 * s + 1) * n + r]);
+    }
+}
+
+struct CholPrecond : Preconditioner {
+    int64_t n = 0;
+    float *chol = nullptr, *work = nullptr;
+    int *info = nullptr;
+    int cap = 0;
+    cusolverDnHandle_t solver = nullptr;
+    ~CholPrecond() override {
+        cudaFree(chol);
+        cudaFree(work);
+        cudaFree(info);
+        if (solver) cusolverDnDestroy(solver);
+    }
+    cudaError_t factor(int64_t n_, const double *A, int64_t lda, cudaStream_t s, int &host_info) {
+        n = n_;
+        cudaError_t e;
+        if ((e = dev_alloc(&chol, (size_t)n * n)) || (e = dev_alloc(&info, 1))) return e;
+        if (lda == n) {
+            k_to_f32<<<grid_of(n * n), 256, 0, s>>>(n * n, A, chol);
+            note_launches(1);
+        } else {
+            for (int64_t r = 0; r < n; ++r) {
+                k_to_f32<<<grid_of(n), 256, 0, s>>>(n, A + r * lda, chol + r * n);
+            }
+            note_launches(n);
+        }
+        if (cusolverDnCreate(&solver) != CUSOLVER_STATUS_SUCCESS) return cudaErrorUnknown;
+        cusolverDnSetStream(solver, s);
+        int lwork = 0;
+        if (cusolverDnSpotrf_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)n, chol, (int)n, &lwork) !=
+            CUSOLVER_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        float *ws = nullptr;
+        if ((e = dev_alloc(&ws, (size_t)lwork))) return e;
+        const cusolverStatus_t cs = cusolverDnSpotrf(solver, CUBLAS_FILL_MODE_LOWER, (int)n, chol, (int)n, ws, lwork,
+                                                     info);
+        cudaMemcpyAsync(&host_info, info, sizeof(int), cudaMemcpyDeviceToHost, s);
+        e = cudaStreamSynchronize(s);
+        cudaFree(ws);
+        if (cs != CUSOLVER_STATUS_SUCCESS) return cudaErrorUnknown;
+        return e;
+    }
+    cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        if (2 * k > cap) {
+            cudaFree(work);
+            work = nullptr;
+            cudaError_t e = dev_alloc(&work, (size_t)n * 2 * k);
+            if (e) return e;
+            cap = 2 * k;
+        }
+        cusolverDnSetStream(solver, s);
+        k_split_cols<<<grid_of(n * k), 256, 0, s>>>(n, k, in, work);
+        if (cusolverDnSpotrs(solver, CUBLAS_FILL_MODE_LOWER, (int)n, 2 * k, chol, (int)n, work, (int)n, info) !=
+            CUSOLVER_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        k_join_cols<<<grid_of(n * k), 256, 0, s>>>(n, k, work, out);
         note_launches(2);
         return cudaGetLastError();
     }
@@ -607,8 +744,9 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     return OK;
 }
 
-int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int32_t sys, void *stream) {
+int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream) {
     if (!h || !krk || sys < 0 || sys >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_factor: invalid argument");
+    if (math != 0 && math != 1) return pfail(ERR_ARGUMENT, "peec_factor: math 0 (FP32) or 1 (BF16x9 FP32 emulation)");
     PeecOp &op = h->op;
     const int64_t n = op.n_;
     if (krk->rows != n || krk->cols != n) return pfail(ERR_ARGUMENT, "peec_factor: K^T R K must be n x n");
@@ -657,6 +795,10 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         return pfail(ERR_CUDA, "peec_factor: cuSOLVER handle");
     }
     cusolverDnSetStream(lu->solver, st);
+    if (math == 1 && cusolverDnSetMathMode(lu->solver, CUSOLVER_FP32_EMULATED_BF16X9_MATH) != CUSOLVER_STATUS_SUCCESS) {
+        delete lu;
+        return pfail(ERR_CUDA, "peec_factor: BF16x9 emulation unavailable in this cuSOLVER");
+    }
     int lwork = 0;
     if (cusolverDnCgetrf_bufferSize(lu->solver, (int)n, (int)n, reinterpret_cast<cuComplex *>(lu->lu), (int)n,
                                     &lwork) != CUSOLVER_STATUS_SUCCESS) {
@@ -681,6 +823,16 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     }
     delete h->lu;
     h->lu = lu;
+    return OK;
+}
+
+int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *h, int k, const double *in, double *out, void *stream) {
+    if (!h || k <= 0 || !in || !out) return pfail(ERR_ARGUMENT, "peec_lu_solve: invalid argument");
+    if (!h->lu) return pfail(ERR_ARGUMENT, "peec_lu_solve: no factor set up");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = h->lu->apply(k, nullptr, reinterpret_cast<const cd *>(in), reinterpret_cast<cd *>(out), st);
+    if (!e) e = cudaStreamSynchronize(st);
+    if (e) return pfail(ERR_CUDA, "peec_lu_solve: %s", cudaGetErrorString(e));
     return OK;
 }
 
@@ -713,29 +865,102 @@ int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
     return OK;
 }
 
+int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *stream) {
+    if (!in || !out || count < 0) return pfail(ERR_ARGUMENT, "to_single: invalid argument");
+    if (!count) return OK;
+    k_to_f32<<<grid_of(count), 256, 0, static_cast<cudaStream_t>(stream)>>>(count, in, out);
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    return e ? pfail(ERR_CUDA, "to_single: %s", cudaGetErrorString(e)) : OK;
+}
+
+int pcbqs_gb300_peec_single(pcbqs_gb300_peec *h, const float *Lf, int64_t ldlf, const float *Pf, int64_t ldpf) {
+    if (!h || !Lf || ldlf < h->op.ne || (h->op.nn > 0 && (!Pf || ldpf < h->op.nn)))
+        return pfail(ERR_ARGUMENT, "peec_single: invalid single-precision matrices");
+    h->op.Lf = Lf;
+    h->op.ldlf = ldlf;
+    h->op.Pf = Pf;
+    h->op.ldpf = ldpf;
+    return OK;
+}
+
+int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, const double *b, double *x,
+                                 double tol, double inner_tol, int max_outer, int inner_maxiter, int restart,
+                                 int precondition, int32_t *iterations, double *residual, int32_t *outer_steps,
+                                 void *stream) {
+    if (!h || k <= 0 || !sys_host || !b || !x || !(tol > 0) || !(inner_tol > 0) || max_outer < 0 ||
+        inner_maxiter <= 0 || restart <= 0)
+        return pfail(ERR_ARGUMENT, "peec_solve_mixed: invalid argument");
+    if (!h->op.Lf) return pfail(ERR_ARGUMENT, "peec_solve_mixed: no single-precision L and P set");
+    for (int s = 0; s < k; ++s)
+        if (sys_host[s] < 0 || sys_host[s] >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_solve_mixed: system");
+    if (precondition == 1 && !h->bj) return pfail(ERR_ARGUMENT, "peec_solve_mixed: no block-Jacobi set up");
+    if (precondition == 2 && !h->lu) return pfail(ERR_ARGUMENT, "peec_solve_mixed: no factor set up");
+    Preconditioner *M = precondition == 1 ? static_cast<Preconditioner *>(h->bj)
+                        : precondition == 2 ? static_cast<Preconditioner *>(h->lu) : nullptr;
+    SingleView single;
+    single.op = &h->op;
+    RefineOptions opt;
+    opt.tol = tol;
+    opt.inner_tol = inner_tol;
+    opt.max_outer = max_outer;
+    opt.inner_maxiter = inner_maxiter;
+    opt.restart = restart;
+    GmresReport rep;
+    int steps = 0;
+    cudaError_t e = refine_batched(h->op, single, M, k, sys_host, reinterpret_cast<const cd *>(b),
+                                   reinterpret_cast<cd *>(x), opt, rep, steps, static_cast<cudaStream_t>(stream));
+    if (e) return pfail(ERR_CUDA, "peec_solve_mixed: %s", cudaGetErrorString(e));
+    if (outer_steps) *outer_steps = steps;
+    bool ok = true;
+    for (int s = 0; s < k; ++s) {
+        if (iterations) iterations[s] = rep.iterations[s];
+        if (residual) residual[s] = rep.residual[s];
+        ok = ok && rep.residual[s] <= tol;
+    }
+    if (!ok) return pfail(ERR_CONVERGENCE, "peec_solve_mixed: not every system reached the tolerance");
+    return OK;
+}
+
 int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, const double *b, double *x, double tol,
-                            int maxiter, int restart, int32_t *iterations, double *residual, void *stream) {
-    if (n <= 0 || !A || lda < n || k <= 0 || !b || !x || !(tol > 0) || maxiter <= 0 || restart <= 0)
+                            int maxiter, int restart, int precondition, int32_t *iterations, double *residual,
+                            void *stream) {
+    if (n <= 0 || !A || lda < n || k <= 0 || !b || !x || !(tol > 0) || maxiter <= 0 || restart <= 0 ||
+        precondition < 0 || precondition > 1)
         return pfail(ERR_ARGUMENT, "dense_gmres: invalid argument");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     DenseSym op;
     op.n_ = n; op.ld = lda; op.A = A;
     if (cublasCreate(&op.blas) != CUBLAS_STATUS_SUCCESS) return pfail(ERR_CUDA, "dense_gmres: cuBLAS handle");
-    Jacobi M;
-    M.n = n;
-    if (dev_alloc(&M.d, n)) {
-        cublasDestroy(op.blas);
-        return pfail(ERR_MEMORY, "dense_gmres: allocation");
+    Jacobi J;
+    CholPrecond C;
+    Preconditioner *M = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (precondition == 0) {
+        J.n = n;
+        if ((e = dev_alloc(&J.d, n))) {
+            cublasDestroy(op.blas);
+            return pfail(ERR_MEMORY, "dense_gmres: allocation");
+        }
+        k_diag_extract<<<grid_of(n), 256, 0, st>>>(n, A, lda, J.d);
+        note_launches(1);
+        M = &J;
+    } else {
+        int info = 0;
+        e = C.factor(n, A, lda, st, info);
+        if (e || info) {
+            cublasDestroy(op.blas);
+            return pfail(info ? ERR_NONFINITE : ERR_CUDA, "dense_gmres: single-precision Cholesky failed (info %d)",
+                         info);
+        }
+        M = &C;
     }
-    k_diag_extract<<<grid_of(n), 256, 0, st>>>(n, A, lda, M.d);
-    note_launches(1);
     std::vector<int32_t> sys(k, 0);
     GmresOptions opt;
     opt.tol = tol; opt.maxiter = maxiter; opt.restart = restart;
     GmresReport rep;
-    cudaError_t e = gmres_batched(op, &M, k, sys.data(), reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x),
-                                  opt, rep, st);
-    cudaFree(M.d);
+    e = gmres_batched(op, M, k, sys.data(), reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x), opt, rep, st);
+    cudaFree(J.d);
     cublasDestroy(op.blas);
     if (e) return pfail(ERR_CUDA, "dense_gmres: %s", cudaGetErrorString(e));
     bool ok = true;

@@ -41,7 +41,25 @@ struct GmresReport {
 cudaError_t gmres_batched(Operator &A, Preconditioner *M, int k, const int32_t *sys_host, const cd *b, cd *x,
                           const GmresOptions &opt, GmresReport &report, cudaStream_t stream);
 
-// Column helpers (device): norms (deterministic two-stage sums) and elementwise updates.
+// Column helpers (device): norms (deterministic two-stage sums; scratch holds 64 * k doubles) and column moves.
 cudaError_t column_norms(int64_t n, int k, const cd *x, double *out, double *scratch, cudaStream_t s);
+cudaError_t gather_columns(int64_t n, int k, int ka, const int *act, const cd *full, cd *compact, cudaStream_t s);
+cudaError_t scatter_add_columns(int64_t n, int k, int ka, const int *act, const cd *compact, cd *full,
+                                cudaStream_t s);
+cudaError_t subtract_from(int64_t count, const cd *b, cd *a, cudaStream_t s);     // a = b - a
+
+// Mixed-precision refinement (the MixedLU scheme with a Krylov inner solve): the true residual r = b - A x with the
+// FP64 operator, then an inner right-preconditioned GMRES on the single-precision operator A32 to `inner_tol` of
+// |r|, x += correction, until |b - A x| / |b| <= tol per column or `max_outer` outer steps.
+struct RefineOptions {
+    double tol = 1e-8;
+    double inner_tol = 1e-4;
+    int max_outer = 8;
+    int inner_maxiter = 200;
+    int restart = 50;
+};
+cudaError_t refine_batched(Operator &A, Operator &A32, Preconditioner *M, int k, const int32_t *sys_host,
+                           const cd *b, cd *x, const RefineOptions &opt, GmresReport &report, int &outer_steps,
+                           cudaStream_t stream);
 
 }  // namespace pq

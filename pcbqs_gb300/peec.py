@@ -298,29 +298,39 @@ class PeecModel(PeecTopology):
     first to its second terminal (MQS.source), solved on the device."""
 
     def __init__(self, board, near=3.0, outer_levels=1, device=0, block_size=32, tol=1e-8, maxiter=2000,
-                 restart=100, log=None):
-        self.tol, self.maxiter, self.restart = tol, maxiter, restart
+                 restart=100, log=None, inner_tol=1e-4):
+        self.tol, self.maxiter, self.restart, self.inner_tol = tol, maxiter, restart, inner_tol
         self.device = torch.device('cuda', device)
         self.timings = {}
         t0 = time.perf_counter()
         self.fill = DeviceFill(board.nodes, board.tris, board.z, outer_levels, near, device)
         PeecTopology.__init__(self, board, self.fill.rwg, block_size, log)
         self.timings['host_topology_s'] = time.perf_counter() - t0
-        self.L = self.P = None
+        self.L = self.P = self.Lf = self.Pf = None
 
     # -- device matrices --
-    def assemble(self):
-        """Fill L and P on the device (moments, combine, aggregation); frees the moment planes."""
+    def assemble(self, mixed=False):
+        """Fill L and P on the device (moments, combine, aggregation); frees the moment planes. mixed=True: far
+        pairs in FP32 local coordinates (near pairs FP64), FP32 combine; L and P kept in FP64 and FP32."""
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        self.L = self.P = self.Lf = self.Pf = None
         ev[0].record()
-        planes, analytic = self.fill.moments()
-        ev[1].record()
-        self.L = self.fill.inductance(planes)
-        ev[2].record()
-        self.P = self.fill.potential(planes[0], self.board.node_of, self.board.er)
+        if mixed:
+            planes, analytic = self.fill.moments_local()
+            ev[1].record()
+            self.L, self.Lf = self.fill.inductance_local(planes)
+            ev[2].record()
+            self.P, self.Pf = self.fill.potential_single(planes[0], self.board.node_of, self.board.er)
+        else:
+            planes, analytic = self.fill.moments()
+            ev[1].record()
+            self.L = self.fill.inductance(planes)
+            ev[2].record()
+            self.P = self.fill.potential(planes[0], self.board.node_of, self.board.er)
         ev[3].record()
         del planes
         torch.cuda.synchronize()
+        self.mixed_fill = mixed
         self.analytic = analytic
         self.timings.update(fill_ms=ev[0].elapsed_time(ev[1]), combine_ms=ev[1].elapsed_time(ev[2]),
                             potential_ms=ev[2].elapsed_time(ev[3]))
@@ -329,14 +339,21 @@ class PeecModel(PeecTopology):
         self._pinvb = None
         return self
 
+    def _krk_device(self):
+        """K^T R K (frequency independent) as a device CSR, made once per model."""
+        if getattr(self, '_krk', None) is None:
+            self._krk = _dev_csr(self.Kp.T @ self.R @ self.Kp, self.device)
+        return self._krk
+
     def _operator(self, omegas):
         dev = self.device
         R = self.R
         zscale = np.array([max(float(np.max(np.abs(R.diagonal() + 1j * w * self.ldiag))), np.finfo(float).tiny)
                            for w in omegas])
-        self._dev = dict(K=_dev_csr(self.Kp, dev), Kt=_dev_csr(self.Kp.T, dev), T=_dev_csr(self.Tp, dev),
-                         Tt=_dev_csr(self.Tp.T, dev), R=_dev_csr(R, dev),
-                         is_tree=torch.as_tensor(self.is_tree, device=dev))
+        if getattr(self, '_dev', None) is None:      # the topology's sparse matrices, uploaded once per model
+            self._dev = dict(K=_dev_csr(self.Kp, dev), Kt=_dev_csr(self.Kp.T, dev), T=_dev_csr(self.Tp, dev),
+                             Tt=_dev_csr(self.Tp.T, dev), R=_dev_csr(R, dev),
+                             is_tree=torch.as_tensor(self.is_tree, device=dev))
         d = _lib.PeecDesc()
         d.n, d.nb, d.ne, d.nn = self.n, len(self.passive), self.ne, self.nn
         for name in ('K', 'Kt', 'T', 'Tt', 'R'):
@@ -385,7 +402,8 @@ class PeecModel(PeecTopology):
         return baseline, qpart, vpart, source_voltage
 
     def _potential_solve(self, rhs):
-        """P^-1 rhs on the device (Jacobi-preconditioned dense GMRES), rhs (nn, k) real."""
+        """P^-1 rhs on the device (dense GMRES preconditioned by P's single-precision Cholesky factor), rhs (nn, k)
+        real."""
         k = rhs.shape[1]
         b = torch.as_tensor(np.ascontiguousarray(rhs.astype(complex)), device=self.device)
         x = torch.zeros_like(b)
@@ -393,7 +411,7 @@ class PeecModel(PeecTopology):
         res = np.zeros(k)
         lib = _lib.load()
         _lib.check(lib.pcbqs_gb300_dense_gmres(self.nn, self.P.data_ptr(), self.P.stride(0), k, b.data_ptr(),
-                                               x.data_ptr(), self.tol * 1e-2, 4000, self.restart,
+                                               x.data_ptr(), self.tol * 1e-2, 4000, self.restart, 1,
                                                _lib.ptr(its, ctypes.c_int32), _lib.ptr(res),
                                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
         self.timings['potential_solve_iterations'] = its.tolist()
@@ -410,11 +428,16 @@ class PeecModel(PeecTopology):
 
     PRECONDITIONERS = {'none': 0, 'block_jacobi': 1, 'lu32': 2}
 
-    def solve(self, freqs, precondition='block_jacobi'):
+    FACTOR_MATH = {'fp32': 0, 'bf16x9': 1}
+
+    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='fp32'):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
 
         precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
-        dense loop/tree system at each frequency, FP64 GMRES on top), or 'none'."""
+        dense loop/tree system at each frequency), or 'none'. mixed=False: FP64 GMRES on the FP64 operator;
+        mixed=True: FP64 iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose
+        dense products run in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of
+        the 'lu32' factorization, 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy)."""
         if self.L is None:
             self.assemble()
         f = np.atleast_1d(np.asarray(freqs, float))
@@ -422,15 +445,19 @@ class PeecModel(PeecTopology):
             raise ValueError('frequencies must be finite and positive')
         if precondition not in self.PRECONDITIONERS:
             raise ValueError(f'precondition must be one of {sorted(self.PRECONDITIONERS)}')
+        if factor_math not in self.FACTOR_MATH:
+            raise ValueError(f'factor_math must be one of {sorted(self.FACTOR_MATH)}')
         if precondition == 'lu32' and len(f) > 1:
-            return self._stack([self.solve([fi], precondition) for fi in f])
+            return self._stack([self.solve([fi], precondition, mixed, factor_math) for fi in f])
         mode = self.PRECONDITIONERS[precondition]
         t0 = time.perf_counter()
         npo = len(self.names)
         excitation = np.eye(npo, dtype=complex)
         baseline, qpart, vpart, source_voltage = self._equilibrium(excitation)
+        t1 = time.perf_counter()
         omegas = 2 * np.pi * f
         handle, zscale = self._operator(omegas)
+        self.timings.update(equilibrium_s=t1 - t0, operator_setup_s=time.perf_counter() - t1)
         lib = _lib.load()
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         try:
@@ -440,13 +467,14 @@ class PeecModel(PeecTopology):
                 _lib.check(lib.pcbqs_gb300_peec_block_jacobi(handle, self.bs, self._krk_blocks().data_ptr(), stream),
                            lib)
             elif mode == 2:
-                krk = _dev_csr(self.Kp.T @ self.R @ self.Kp, self.device)
-                desc = _csr_struct(krk)
-                _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, stream), lib)
+                desc = _csr_struct(self._krk_device())
+                _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, self.FACTOR_MATH[factor_math],
+                                                       stream), lib)
             ev_p1.record()
             torch.cuda.synchronize()
             self.timings['precondition_ms'] = ev_p0.elapsed_time(ev_p1)
             # rhs = -K^T (R + j w L) baseline / zscale, per (frequency, port) column, in the clustered order.
+            t_rhs = time.perf_counter()
             Lb = self._mv_L(baseline[:self.ne])
             Rb = self.R @ baseline[:self.ne]
             Kpt = self.Kp.T
@@ -456,6 +484,7 @@ class PeecModel(PeecTopology):
                 cols.append(-(Kpt @ v) / zscale[fi])
                 sys += [fi] * npo
             rhs = np.ascontiguousarray(np.concatenate(cols, axis=1))      # (n, nf * np)
+            self.timings['rhs_s'] = time.perf_counter() - t_rhs
             b = torch.as_tensor(rhs, device=self.device)
             x = torch.zeros_like(b)
             k = rhs.shape[1]
@@ -463,9 +492,28 @@ class PeecModel(PeecTopology):
             its, res = np.zeros(k, np.int32), np.zeros(k)
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             ev0.record()
-            status = lib.pcbqs_gb300_peec_gmres(handle, k, _lib.ptr(sys, ctypes.c_int32), b.data_ptr(), x.data_ptr(),
-                                                self.tol, self.maxiter, self.restart, mode,
-                                                _lib.ptr(its, ctypes.c_int32), _lib.ptr(res), stream)
+            if mixed:
+                # single-precision copies of L and P for the inner products; FP64 outer residuals
+                Lf, Pf = self.Lf, self.Pf
+                if Lf is None:
+                    Lf = torch.empty(self.L.shape, dtype=torch.float32, device=self.device)
+                    Pf = torch.empty(self.P.shape, dtype=torch.float32, device=self.device)
+                    _lib.check(lib.pcbqs_gb300_to_single(self.L.data_ptr(), Lf.data_ptr(), self.L.numel(), stream),
+                               lib)
+                    _lib.check(lib.pcbqs_gb300_to_single(self.P.data_ptr(), Pf.data_ptr(), self.P.numel(), stream),
+                               lib)
+                _lib.check(lib.pcbqs_gb300_peec_single(handle, Lf.data_ptr(), Lf.stride(0), Pf.data_ptr(),
+                                                       Pf.stride(0)), lib)
+                outer = ctypes.c_int32()
+                status = lib.pcbqs_gb300_peec_solve_mixed(handle, k, _lib.ptr(sys, ctypes.c_int32), b.data_ptr(),
+                                                          x.data_ptr(), self.tol, self.inner_tol, 12, self.maxiter,
+                                                          self.restart, mode, _lib.ptr(its, ctypes.c_int32),
+                                                          _lib.ptr(res), ctypes.byref(outer), stream)
+                self.timings['outer_steps'] = int(outer.value)
+            else:
+                status = lib.pcbqs_gb300_peec_gmres(handle, k, _lib.ptr(sys, ctypes.c_int32), b.data_ptr(),
+                                                    x.data_ptr(), self.tol, self.maxiter, self.restart, mode,
+                                                    _lib.ptr(its, ctypes.c_int32), _lib.ptr(res), stream)
             ev1.record()
             torch.cuda.synchronize()
             if status not in (0, 5):

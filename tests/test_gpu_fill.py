@@ -143,3 +143,28 @@ def test_device_fill_planes_board(device_library):
     i, j = (torch.as_tensor(a, device=P.device) for a in gold['P_at'])
     assert P[i, j].cpu().numpy() == pytest.approx(gold['P_val'], rel=1e-11)
     assert torch.diagonal(P).cpu().numpy() == pytest.approx(gold['P_diag'], rel=1e-11)
+
+
+@pytest.mark.parametrize('board', ['tiny', 'strip'])
+def test_mixed_fill_against_fp64_oracle(device_library, board):
+    """The mixed fill (far pairs in FP32 local coordinates, near pairs FP64, FP32 combine): L and P against the FP64
+    oracle. Stated errors: max |dL| / max |L| < 2e-6 and max |dP| / max |P| < 2e-6; the near-field (diagonal) entries,
+    dominated by the FP64 near pairs, within 1e-5 relative each."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.fill import DeviceFill
+    b = Board.load(board)
+    f = DeviceFill(b.nodes, b.tris, b.z, outer_levels=1, near=3.0)
+    planes, analytic = f.moments_local()
+    og = O.Geometry(b.nodes, b.tris, b.z, 1)
+    mats, oracle_analytic = O.fill(og, 3.0, 1, False)
+    assert analytic == oracle_analytic
+    L, Lf = f.inductance_local(planes)
+    L, Lf = L.cpu().numpy(), Lf.cpu().numpy()
+    Lo = O.combine(O.RWG(og.nodes, og.tris), mats)
+    assert np.array_equal(L, L.T) and np.array_equal(Lf.astype(np.float64), L)
+    assert np.abs(L - Lo).max() / np.abs(Lo).max() < 2e-6
+    assert np.diag(L) == pytest.approx(np.diag(Lo), rel=1e-5)
+    P, Pf = f.potential_single(planes[0], b.node_of, b.er)
+    Po = O.potential(mats[0], og.area, b.node_of, b.er)
+    P = P.cpu().numpy()
+    assert np.abs(P - Po).max() / np.abs(Po).max() < 2e-6
