@@ -45,6 +45,8 @@ def parse():
     p.add_argument('--board', default='planes')
     p.add_argument('--freq', type=float, default=1e6)
     p.add_argument('--precondition', default='lu32', choices=['lu32', 'block_jacobi'])
+    p.add_argument('--factor-math', default='fp32', choices=['fp32', 'bf16x9'],
+                   help='arithmetic of the lu32 factorization (bf16x9: FP32 emulated on the tensor cores)')
     p.add_argument('--mode', default='mixed', choices=['mixed', 'fp64'],
                    help='mixed: FP32 far pairs in local coordinates and FP32 inner Krylov products under FP64 '
                         'refinement; fp64: the FP64 fill and FP64 GMRES')
@@ -89,8 +91,12 @@ class Clocks:
                     reasons=reasons, samples=len(rows))
 
 
-def fill_roofline(model, fp64_peak_tflops, fill_ms):
-    """The FP64 fill kernel pair (far tiles + near lists): algorithmic FP64 flops per launch / its CUDA-event time."""
+def fill_roofline(model, fill_ms, mixed, peaks):
+    """The fill kernel pair (far tiles + near lists): algorithmic flops per launch / their CUDA-event time.
+
+    FP64 fill: every pair on the FP64 pipe, peak = the FP64 GEMM rate. Mixed fill: far pairs on the FP32 pipe and
+    near pairs on the FP64 pipe, so the roofline time of one launch is far_flops / FP32 peak + near_flops / FP64
+    peak, and `peak` is the flop rate that time implies (the pipes' rates weighted by this workload's flop mix)."""
     import ctypes
     from pcbqs_gb300 import _lib
     counts = (ctypes.c_uint64 * 2)()
@@ -99,20 +105,31 @@ def fill_roofline(model, fp64_peak_tflops, fill_ms):
     pairs = nt * (nt + 1) // 2
     near0, near1 = int(counts[0]), int(counts[1])
     far = pairs - near0 - near1
-    flops = far * FAR_FLOP + near0 * NEAR_FLOP[0] + near1 * NEAR_FLOP[model.fill.outer_levels]
-    seconds = fill_ms / 1e3
-    achieved = flops / seconds / 1e12
-    return dict(bound='fp64', kernel='k_fill_tiles+k_fill_near', achieved=round(achieved, 4),
-                peak=round(fp64_peak_tflops, 4), unit='TFLOP/s', frac=round(achieved / fp64_peak_tflops, 4),
-                traffic=None, flops_per_launch=flops, far_pairs=far, near_pairs=[near0, near1],
-                peak_source='measured live: FP64 GEMM (cuBLAS DGEMM 8192^3) on this GPU')
+    far_flops = far * FAR_FLOP
+    near_flops = near0 * NEAR_FLOP[0] + near1 * NEAR_FLOP[model.fill.outer_levels]
+    flops = far_flops + near_flops
+    achieved = flops / (fill_ms / 1e3) / 1e12
+    if mixed:
+        bound_s = far_flops / (peaks['fp32'] * 1e12) + near_flops / (peaks['fp64'] * 1e12)
+        peak, bound = flops / bound_s / 1e12, 'fp32 (far) + fp64 (near)'
+        source = (f"measured live: SGEMM {peaks['fp32']:.1f} and DGEMM {peaks['fp64']:.2f} TFLOP/s (cuBLAS 8192^3) on "
+                  f"this GPU, weighted by the far/near flop split")
+    else:
+        peak, bound = peaks['fp64'], 'fp64'
+        source = 'measured live: FP64 GEMM (cuBLAS DGEMM 8192^3) on this GPU'
+    return dict(bound=bound, kernel='k_fill_tiles+k_fill_near', achieved=round(achieved, 4), peak=round(peak, 4),
+                unit='TFLOP/s', frac=round(achieved / peak, 4), traffic=None, flops_per_launch=flops,
+                far_pairs=far, near_pairs=[near0, near1], peak_source=source)
 
 
-def fp64_peak():
+def gemm_peak(dtype):
+    """Best of three cuBLAS GEMMs of 8192^3 in `dtype` (FP32 without TF32), TFLOP/s."""
     import torch
     n = 8192
-    a = torch.randn(n, n, dtype=torch.float64, device='cuda')
-    b = torch.randn(n, n, dtype=torch.float64, device='cuda')
+    allow = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(n, n, dtype=dtype, device='cuda')
+    b = torch.randn(n, n, dtype=dtype, device='cuda')
     torch.matmul(a, b)
     torch.cuda.synchronize()
     best = 0.0
@@ -123,6 +140,7 @@ def fp64_peak():
         e1.record()
         torch.cuda.synchronize()
         best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = allow
     del a, b
     torch.cuda.empty_cache()
     return best
@@ -203,7 +221,7 @@ def main():
 
     def step(mode_mixed=mixed):
         model.assemble(mixed=mode_mixed)
-        return model.solve([freq], precondition=args.precondition, mixed=mode_mixed)
+        return model.solve([freq], precondition=args.precondition, mixed=mode_mixed, factor_math=args.factor_math)
 
     for _ in range(args.warmup):
         result = step()
@@ -249,7 +267,9 @@ def main():
                           s_per_freq=round(c0.elapsed_time(c1) / 1e3, 4),
                           speedup_of_mixed=round(c0.elapsed_time(c1) / ms, 3),
                           port_z_max_rel_err_of_mixed=float(np.abs(Z_headline - Z64).max() / np.abs(Z64).max()),
-                          gmres_iterations=r64.iterations.tolist())
+                          gmres_iterations=r64.iterations.tolist(),
+                          breakdown_ms={k: round(fp64_timings.get(k, 0), 2) for k in
+                                        ('fill_ms', 'combine_ms', 'potential_ms', 'precondition_ms', 'gmres_ms')})
     # fill GB/s: bytes of L and P written once per step, over the fill + combine + aggregation time
     ne, nn = model.ne, model.nn
     fill_ms = statistics.median(t['fill_ms'] + t['combine_ms'] + t['potential_ms'] for t in timings)
@@ -259,7 +279,7 @@ def main():
     torch.cuda.synchronize()
     m2 = PeecModel(Board.load(args.board), device=local)
     m2.assemble(mixed=mixed)
-    r2 = m2.solve([freq], precondition=args.precondition, mixed=mixed)
+    r2 = m2.solve([freq], precondition=args.precondition, mixed=mixed, factor_math=args.factor_math)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t_e2e
     h2d = m2.fill.dev.nt * (64 + 32 + 192) + sum(a.nbytes for a in m2.fill.geometry.levels[1][5:6])
@@ -269,13 +289,18 @@ def main():
     torch.cuda.empty_cache()
     if rank != 0:
         return
-    peak = fp64_peak()
+    import torch as _torch
+    peaks = dict(fp64=gemm_peak(_torch.float64), fp32=gemm_peak(_torch.float32))
+    head_fill_ms = statistics.median(t['fill_ms'] for t in timings)
+    if comparator:
+        comparator['fill_roofline'] = fill_roofline(model, fp64_timings['fill_ms'], False, peaks)
     line = dict(metric=METRIC, value=round(value, 4), unit='s/freq', n_gpus=world, steps=args.steps,
                 warmup=args.warmup, ms_per_step=round(ms, 2), higher_is_better=False, scaling='weak',
                 vs_baseline=None, dtype='f32+f64' if mixed else 'f64', data='synthetic (seeded plane-pair board, CDT mesh)',
                 config=dict(workload=f'{args.board}: fill+solve of all {len(model.names)} ports at {args.freq:g} Hz',
                             board=args.board, triangles=model.fill.nt, edges=ne, nodes=nn, unknowns=model.n,
-                            precondition=args.precondition, mode=args.mode, gmres_tol=model.tol,
+                            precondition=args.precondition, factor_math=args.factor_math, mode=args.mode,
+                            gmres_tol=model.tol,
                             gmres_iterations=result.iterations.tolist(), parallelism=f'replicas x{world}',
                             l2='inputs larger than L2 (L 8.9 GB)'),
                 fill_gbs=round(fill_gbs, 2),
@@ -286,7 +311,7 @@ def main():
                         for k in ('equilibrium_s', 'operator_setup_s', 'rhs_s', 'solve_s')},
                 gpu_launches=int(launches),
                 clocks=clock_info,
-                roofline=fill_roofline(model, peak, fp64_timings['fill_ms']),
+                roofline=fill_roofline(model, head_fill_ms, mixed, peaks),
                 e2e=dict(value=round(e2e_s, 4), unit='s/freq', h2d_bytes_per_step=int(h2d),
                          d2h_bytes_per_step=int(d2h)))
     if not args.no_cpu_baseline:
