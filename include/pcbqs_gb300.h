@@ -61,6 +61,15 @@ int pcbqs_gb300_pairs(pcbqs_gb300_ctx *ctx, const int32_t *p, const int32_t *q, 
 int pcbqs_gb300_pairs_device(pcbqs_gb300_ctx *ctx, const int32_t *p, const int32_t *q, const double *d,
                              const int32_t *kind, int64_t n, int scalar_only, double *out, void *stream);
 
+/* The same as pcbqs_gb300_pairs_device, for callers that cannot allow device allocation during a call (a
+ * caching allocator already holds the device memory, or a steady-state loop must not stall in cudaMalloc or
+ * cudaFree). It allocates nothing: its scratch is one fixed array in this library's device image, shared by every
+ * call on a device, which limits a call to 1,048,576 pairs (larger n: status 1 with a message). The first call on
+ * a device looks up that array's address and should come before any stream capture on the device. Calls whose
+ * work overlaps on the GPU race on the shared scratch: serialize them. Has no counterpart in the reference. */
+int pcbqs_gb300_pairs_no_alloc(pcbqs_gb300_ctx *ctx, const int32_t *p, const int32_t *q, const double *d,
+                               const int32_t *kind, int64_t n, int scalar_only, double *out, void *stream);
+
 /* Whole reciprocal moment matrices into host planes (each nt x nt, row-major float64; planes[1..3] unused when
  * scalar_only): M0, Mx, My, Mrr with [p,q] = Mro, [q,p] = Mrs, the diagonal their average. near < 0 or infinite:
  * every pair analytic. *analytic receives the number of unordered pairs that were not far.

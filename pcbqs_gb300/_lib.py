@@ -58,6 +58,8 @@ PROTOTYPES = {
                                          ctypes.c_int, c_double_p]),
     'pcbqs_gb300_pairs_device': (ctypes.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_int64,
                                                 ctypes.c_int, c_void_p, c_void_p]),
+    'pcbqs_gb300_pairs_no_alloc': (ctypes.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                  ctypes.c_int64, ctypes.c_int, c_void_p, c_void_p]),
     'pcbqs_gb300_fill': (ctypes.c_int, [c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                         ctypes.POINTER(c_void_p), c_uint64_p]),
     'pcbqs_gb300_fill_device': (ctypes.c_int, [c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,

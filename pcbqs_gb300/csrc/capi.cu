@@ -3,7 +3,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <type_traits>
 #include <string>
@@ -505,3 +507,82 @@ int pcbqs_gb300_potential_device(int64_t nn, const int64_t *start, const int32_t
 }
 
 }  // extern "C"
+
+// ---- Pair evaluation without device allocation -----------------------------------------------------------------
+//
+// pcbqs_gb300_pairs_device grows a per-context buffer with cudaMalloc for the kind-sorted pair order. Some callers
+// cannot let a library allocate at call time: an application whose caching allocator has already reserved the
+// device memory (cudaMalloc then fails even though the memory is free in the application's pool), and a service
+// that must not stall in steady state, since cudaMalloc and cudaFree can synchronize the device. For them,
+// pcbqs_gb300_pairs_no_alloc keeps its scratch (the order array, the kind counters and the status flags) in one
+// array of fixed size that is part of this library's device image: it exists on every device that loads the
+// library, is never allocated or freed by a call, and limits one call to NOALLOC_MAX_PAIRS pairs.
+//
+// Set-up: the first call on a device looks up the array's device address on that device (cudaGetSymbolAddress,
+// which also loads this module there). Make that first call before any stream capture starts on the device.
+//
+// Sharing: every call on a device uses the same array, which still holds the previous call's contents. Each call
+// clears the counters and flags before its kernels run; the order array is fully rewritten before it is read.
+// Two calls whose work overlaps on the GPU (concurrent streams, or host threads calling at once) race on the array
+// and give wrong results: serialize them.
+
+namespace {
+
+constexpr int64_t NOALLOC_MAX_PAIRS = int64_t(1) << 20;    // 8 MB of order entries
+
+struct NoAllocScratch {
+    unsigned long long counters[8];     // per-kind counts [0..3] and scatter cursors [4..7]
+    int flags[2];                       // [0] a moment is not finite, [1] an index or kind is out of range
+    int pad[46];                        // the order array starts 256 bytes in
+    int64_t order[NOALLOC_MAX_PAIRS];
+};
+static_assert(offsetof(NoAllocScratch, order) == 256, "scratch header is 256 bytes");
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+constexpr int NOALLOC_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+NoAllocScratch *g_noalloc_address[NOALLOC_DEVICES] = {};
+
+// The scratch array's address on `device` (the current device), looked up on the first call there.
+int noalloc_scratch(int device, NoAllocScratch **out) {
+    if (device < 0 || device >= NOALLOC_DEVICES)
+        return fail(ERR_ARGUMENT, "pairs_no_alloc: device %d beyond the %d supported", device, NOALLOC_DEVICES);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[device]) {
+        void *ptr = nullptr;
+        const cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (err != cudaSuccess) return cuda_fail(err, "pairs_no_alloc: cudaGetSymbolAddress");
+        g_noalloc_address[device] = static_cast<NoAllocScratch *>(ptr);
+    }
+    *out = g_noalloc_address[device];
+    return OK;
+}
+
+}  // namespace
+
+extern "C" int pcbqs_gb300_pairs_no_alloc(pcbqs_gb300_ctx *c, const int32_t *p, const int32_t *q, const double *d,
+                                          const int32_t *kind, int64_t n, int scalar_only, double *out,
+                                          void *stream) {
+    if (!c) return fail(ERR_ARGUMENT, "pairs_no_alloc: null context");
+    if (n < 0) return fail(ERR_ARGUMENT, "pairs_no_alloc: negative count");
+    if (n > NOALLOC_MAX_PAIRS)
+        return fail(ERR_ARGUMENT, "pairs_no_alloc: %lld pairs exceed the fixed scratch of %lld pairs per call",
+                    (long long)n, (long long)NOALLOC_MAX_PAIRS);
+    if (n == 0) return OK;
+    if (!p || !q || !d || !kind || !out) return fail(ERR_ARGUMENT, "pairs_no_alloc: null array");
+    DeviceGuard guard(c->device);
+    NoAllocScratch *s = nullptr;
+    int rc = noalloc_scratch(c->device, &s);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CK(cudaMemsetAsync(s, 0, offsetof(NoAllocScratch, order), st));     // counters and flags start at zero
+    CK(launch_pairs(c->g, p, q, d, kind, n, scalar_only, out, s->counters, s->order, &s->flags[0], &s->flags[1],
+                    st));
+    int host[2];
+    CK(cudaMemcpyAsync(host, s->flags, sizeof host, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (host[1]) return fail(ERR_ARGUMENT, "pairs_no_alloc: triangle index or kind out of range");
+    if (host[0]) return fail(ERR_NONFINITE, "non-finite triangle-pair moments from fill backend");
+    return OK;
+}
