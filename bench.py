@@ -45,13 +45,16 @@ def parse():
     p.add_argument('--board', default='planes')
     p.add_argument('--freq', type=float, default=1e6)
     p.add_argument('--precondition', default='lu32', choices=['lu32', 'block_jacobi'])
-    p.add_argument('--factor-math', default='fp32', choices=['fp32', 'bf16x9'],
+    p.add_argument('--factor-math', default='bf16x9', choices=['fp32', 'bf16x9'],
                    help='arithmetic of the lu32 factorization (bf16x9: FP32 emulated on the tensor cores)')
     p.add_argument('--mode', default='mixed', choices=['mixed', 'fp64'],
                    help='mixed: FP32 far pairs in local coordinates and FP32 inner Krylov products under FP64 '
                         'refinement; fp64: the FP64 fill and FP64 GMRES')
     p.add_argument('--no-comparator', action='store_true', help='skip the one-step FP64 comparator')
     p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--sweep', type=int, default=0,
+                   help='also time a sweep of this many log-spaced frequencies (1 kHz to 100 MHz), all ports')
+    p.add_argument('--anchors', type=int, default=8, help='complex64 factors shared across the sweep')
     return p.parse_args()
 
 
@@ -308,12 +311,32 @@ def main():
                 breakdown_ms={k: round(statistics.median(t.get(k, 0) for t in timings), 2)
                               for k in ('fill_ms', 'combine_ms', 'potential_ms', 'precondition_ms', 'gmres_ms')},
                 host_s={k: round(statistics.median(t.get(k, 0) for t in timings), 3)
-                        for k in ('equilibrium_s', 'operator_setup_s', 'rhs_s', 'solve_s')},
+                        for k in ('equilibrium_s', 'potential_solve_s', 'operator_setup_s', 'rhs_s', 'solve_s')},
                 gpu_launches=int(launches),
                 clocks=clock_info,
                 roofline=fill_roofline(model, head_fill_ms, mixed, peaks),
                 e2e=dict(value=round(e2e_s, 4), unit='s/freq', h2d_bytes_per_step=int(h2d),
                          d2h_bytes_per_step=int(d2h)))
+    if args.sweep:
+        # the batched sweep: every (frequency, port) column, `anchors` shared factors, one batched GMRES per run
+        fs = np.geomspace(1e3, 1e8, args.sweep)
+        model.assemble(mixed=mixed)
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        rs = model.solve(fs, precondition='lu32', mixed=mixed, factor_math=args.factor_math,
+                         anchors=min(args.anchors, args.sweep))
+        s1.record()
+        torch.cuda.synchronize()
+        its = rs.iterations.reshape(len(fs), -1)
+        line['sweep'] = dict(frequencies=len(fs), range_hz=[1e3, 1e8], ports=len(model.names),
+                             columns=int(its.size), anchors=rs.timings['factorizations'],
+                             s_total=round(s0.elapsed_time(s1) / 1e3, 3),
+                             s_per_freq=round(s0.elapsed_time(s1) / 1e3 / len(fs), 4),
+                             precondition_ms=round(rs.timings['precondition_ms'], 1),
+                             gmres_ms=round(rs.timings['gmres_ms'], 1),
+                             iterations_per_frequency_max=its.max(axis=1).tolist(),
+                             max_residual=float(rs.residual.max()))
     if not args.no_cpu_baseline:
         v, details = cpu_reference(args.board, args.freq)
         line['cpu_baseline'] = dict(value=round(v, 3), unit='s/freq', cores=details['cores'], kind='port',

@@ -44,6 +44,10 @@ const char *pcbqs_gb300_last_error(void);
 int32_t pcbqs_gb300_triangles(const pcbqs_gb300_ctx *ctx);
 /* Kernels this library has launched in the process so far (for launch accounting). No reference counterpart. */
 int64_t pcbqs_gb300_kernel_launches(void);
+/* The solver keeps the device memory of its dense blocks, factors and Krylov bases in a stream-ordered pool after
+ * each call, so that repeated solves reuse it; this returns the unused part of `device`'s pool to the device
+ * (synchronizes the device). No reference counterpart. */
+int pcbqs_gb300_release_memory(int device);
 /* The near-pair counts of the context's last fill: counts[0] at level 0, counts[1] at the refined level. Their
  * sum is the analytic count static_fill reports (src/pcbqs/core/static_kernels.hpp:251). */
 int pcbqs_gb300_fill_counts(const pcbqs_gb300_ctx *ctx, uint64_t *counts);
@@ -212,8 +216,10 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *op, int32_t bs, const double
  * with the FP64 operator's GMRES on top in place of its refinement loop. */
 int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream);
 /* out = (complex64 factor)^-1 in for k complex128 columns (n, k) row-major, device arrays; the solve step of
- * MixedLU (src/pcbqs/kernels.py:160-181) without its refinement. Synchronizes `stream`. */
-int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *op, int k, const double *in, double *out, void *stream);
+ * MixedLU (src/pcbqs/kernels.py:160-181) without its refinement. method 0: this library's streaming triangular
+ * solves (what GMRES uses); method 1: cuSOLVER getrs on the same factor (for validation). Synchronizes `stream`. */
+int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *op, int k, const double *in, double *out, int method,
+                              void *stream);
 /* Batched right-preconditioned restarted GMRES on k columns (b, x device; x holds the initial guess), relative
  * residual tol per column; iterations and residual (host, k) receive each column's Arnoldi steps and true
  * relative residual; precondition 0 none, 1 block-Jacobi, 2 the single-precision factor (every column uses it).

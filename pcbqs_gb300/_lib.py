@@ -53,6 +53,7 @@ PROTOTYPES = {
     'pcbqs_gb300_last_error': (ctypes.c_char_p, []),
     'pcbqs_gb300_triangles': (ctypes.c_int32, [c_void_p]),
     'pcbqs_gb300_kernel_launches': (ctypes.c_int64, []),
+    'pcbqs_gb300_release_memory': (ctypes.c_int, [ctypes.c_int]),
     'pcbqs_gb300_fill_counts': (ctypes.c_int, [c_void_p, c_uint64_p]),
     'pcbqs_gb300_pairs': (ctypes.c_int, [c_void_p, c_int32_p, c_int32_p, c_double_p, c_int32_p, ctypes.c_int64,
                                          ctypes.c_int, c_double_p]),
@@ -100,7 +101,8 @@ PROTOTYPES = {
     'pcbqs_gb300_peec_block_jacobi': (ctypes.c_int, [c_void_p, ctypes.c_int32, c_void_p, c_void_p]),
     'pcbqs_gb300_peec_factor': (ctypes.c_int, [c_void_p, ctypes.POINTER(CsrDesc), ctypes.c_int32, ctypes.c_int,
                                                c_void_p]),
-    'pcbqs_gb300_peec_lu_solve': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_peec_lu_solve': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p, c_void_p, ctypes.c_int,
+                                                 c_void_p]),
     'pcbqs_gb300_to_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p]),
     'pcbqs_gb300_peec_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, ctypes.c_int64]),
     'pcbqs_gb300_peec_solve_mixed': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p,

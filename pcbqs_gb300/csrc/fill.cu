@@ -82,7 +82,8 @@ struct FillSmem {
     FarRec far_r[TILE], far_c[TILE];
     LocalRec loc_r[TILE], loc_c[TILE];
     ClsRec cls_r[TILE], cls_c[TILE];
-    double t[4][TILE][TILE + 1];          // transposed staging: [plane][q_local][p_local]
+    float rad_r[TILE], rad_c[TILE];       // radii as floats (mixed precision classification filter)
+    double t[4][TILE][TILE + 1];          // transposed staging: [plane][q_local][p_local] (float in mixed)
     unsigned char keep[TILE][TILE];        // [q_local][p_local]: 1 when the reverse entry is written here
     uint64_t bar;
 };
@@ -118,6 +119,7 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, Planes<
     __syncthreads();
     uint32_t phase = 0;
     bool failed = false;
+    const float near_f = (float)rule.near;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int bp, bq;
         tile_of(t, nb, bp, bq);
@@ -144,6 +146,11 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, Planes<
             if (threadIdx.x == 0) atomicExch(status, (int)ERR_TIMEOUT);
             break;
         }
+        if (LOCAL) {
+            if (threadIdx.x < np) s.rad_r[threadIdx.x] = (float)s.cls_r[threadIdx.x].radius;
+            if (threadIdx.x >= 32 && threadIdx.x < 32 + nqn) s.rad_c[threadIdx.x - 32] = (float)s.cls_c[threadIdx.x - 32].radius;
+            __syncthreads();
+        }
         bool bad = false;
 #pragma unroll 1
         for (int i = 0; i < ROWS_PER_WARP; ++i) {
@@ -151,10 +158,13 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, Planes<
             const int p = p0 + pl, q = q0 + ql;
             bool valid = pl < np && ql < nqn && (!diagonal || pl <= ql);
             int k = -2;
-            double d = 0;
             if (valid) {
-                d = s.cls_r[pl].z - s.cls_c[ql].z;
-                k = classify(s.cls_r[pl], s.cls_c[ql], d, rule.near, rule.all_near, rule.outer);
+                if (LOCAL)
+                    k = classify_filtered(s.loc_r[pl], s.loc_c[ql], s.rad_r[pl], s.rad_c[ql], s.cls_r[pl], s.cls_c[ql],
+                                          near_f, rule.near, rule.all_near, rule.outer);
+                else
+                    k = classify(s.cls_r[pl], s.cls_c[ql], s.cls_r[pl].z - s.cls_c[ql].z, rule.near, rule.all_near,
+                                 rule.outer);
             }
             // Near pairs: warp-aggregated appends to the level's list.
 #pragma unroll
@@ -175,31 +185,58 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, Planes<
                 }
             }
             const bool far = valid && k < 0;
-            double m[6] = {0, 0, 0, 0, 0, 0};
-            if (far) {
-                if (LOCAL) far_local(s.loc_r[pl], s.loc_c[ql], scalar, m);
-                else far_moments(s.far_r[pl], s.far_c[ql], d, scalar, m);
-                bad = bad || !finite6(m, scalar);
-                const size_t pq = (size_t)p * out.ld + q;
-                out.m0[pq] = (T)m[0];
-                if (!scalar) {
-                    if (p == q) {
-                        out.mx[pq] = (T)((m[1] + m[3]) / 2);
-                        out.my[pq] = (T)((m[2] + m[4]) / 2);
-                    } else {
-                        out.mx[pq] = (T)m[1];
-                        out.my[pq] = (T)m[2];
-                    }
-                    out.mrr[pq] = (T)m[5];
-                }
-            }
             const bool reverse = far && p != q;
             s.keep[ql][pl] = reverse;
-            if (reverse) {
-                s.t[0][ql][pl] = m[0];
-                s.t[1][ql][pl] = m[3];
-                s.t[2][ql][pl] = m[4];
-                s.t[3][ql][pl] = m[5];
+            if (LOCAL) {
+                // FP32 far moments straight into the FP32 planes and the float staging (no FP64 conversions)
+                float m[6] = {0, 0, 0, 0, 0, 0};
+                if (far) {
+                    far_local(s.loc_r[pl], s.loc_c[ql], scalar, m);
+                    bad = bad || !finite6(m, scalar);
+                    const size_t pq = (size_t)p * out.ld + q;
+                    out.m0[pq] = (T)m[0];
+                    if (!scalar) {
+                        if (p == q) {
+                            out.mx[pq] = (T)((m[1] + m[3]) * 0.5f);
+                            out.my[pq] = (T)((m[2] + m[4]) * 0.5f);
+                        } else {
+                            out.mx[pq] = (T)m[1];
+                            out.my[pq] = (T)m[2];
+                        }
+                        out.mrr[pq] = (T)m[5];
+                    }
+                }
+                if (reverse) {
+                    float *tf = reinterpret_cast<float *>(&s.t[0][0][0]);
+                    tf[(0 * TILE + ql) * (TILE + 1) + pl] = m[0];
+                    tf[(1 * TILE + ql) * (TILE + 1) + pl] = m[3];
+                    tf[(2 * TILE + ql) * (TILE + 1) + pl] = m[4];
+                    tf[(3 * TILE + ql) * (TILE + 1) + pl] = m[5];
+                }
+            } else {
+                double m[6] = {0, 0, 0, 0, 0, 0};
+                if (far) {
+                    far_moments(s.far_r[pl], s.far_c[ql], s.cls_r[pl].z - s.cls_c[ql].z, scalar, m);
+                    bad = bad || !finite6(m, scalar);
+                    const size_t pq = (size_t)p * out.ld + q;
+                    out.m0[pq] = (T)m[0];
+                    if (!scalar) {
+                        if (p == q) {
+                            out.mx[pq] = (T)((m[1] + m[3]) / 2);
+                            out.my[pq] = (T)((m[2] + m[4]) / 2);
+                        } else {
+                            out.mx[pq] = (T)m[1];
+                            out.my[pq] = (T)m[2];
+                        }
+                        out.mrr[pq] = (T)m[5];
+                    }
+                }
+                if (reverse) {
+                    s.t[0][ql][pl] = m[0];
+                    s.t[1][ql][pl] = m[3];
+                    s.t[2][ql][pl] = m[4];
+                    s.t[3][ql][pl] = m[5];
+                }
             }
         }
         __syncthreads();
@@ -209,11 +246,21 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, Planes<
             const int ql = warp + (FILL_THREADS / 32) * i, pl = lane;
             if (ql < nqn && pl < np && s.keep[ql][pl]) {
                 const size_t qp = (size_t)(q0 + ql) * out.ld + (p0 + pl);
-                out.m0[qp] = (T)s.t[0][ql][pl];
-                if (!scalar) {
-                    out.mx[qp] = (T)s.t[1][ql][pl];
-                    out.my[qp] = (T)s.t[2][ql][pl];
-                    out.mrr[qp] = (T)s.t[3][ql][pl];
+                if (LOCAL) {
+                    const float *tf = reinterpret_cast<const float *>(&s.t[0][0][0]);
+                    out.m0[qp] = (T)tf[(0 * TILE + ql) * (TILE + 1) + pl];
+                    if (!scalar) {
+                        out.mx[qp] = (T)tf[(1 * TILE + ql) * (TILE + 1) + pl];
+                        out.my[qp] = (T)tf[(2 * TILE + ql) * (TILE + 1) + pl];
+                        out.mrr[qp] = (T)tf[(3 * TILE + ql) * (TILE + 1) + pl];
+                    }
+                } else {
+                    out.m0[qp] = (T)s.t[0][ql][pl];
+                    if (!scalar) {
+                        out.mx[qp] = (T)s.t[1][ql][pl];
+                        out.my[qp] = (T)s.t[2][ql][pl];
+                        out.mrr[qp] = (T)s.t[3][ql][pl];
+                    }
                 }
             }
         }

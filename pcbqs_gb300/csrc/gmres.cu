@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "pool.cuh"
 #include "solve.cuh"
 
 namespace pq {
@@ -306,16 +307,18 @@ cudaError_t subtract_from(int64_t count, const cd *b, cd *a, cudaStream_t s) {
 namespace {
 
 struct Scratch {
+    cudaStream_t stream;
     std::vector<void *> blocks;
     cudaError_t err = cudaSuccess;
+    explicit Scratch(cudaStream_t s) : stream(s) {}
     template <class T> T *get(size_t count) {
-        void *p = nullptr;
-        if (err == cudaSuccess) err = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        T *p = nullptr;
+        if (err == cudaSuccess) err = pool_alloc_n(&p, count, stream);
         if (err == cudaSuccess) blocks.push_back(p);
-        return static_cast<T *>(p);
+        return p;
     }
     ~Scratch() {
-        for (void *p : blocks) cudaFree(p);
+        for (void *p : blocks) pool_free(p, stream);
     }
 };
 
@@ -329,7 +332,7 @@ cudaError_t gmres_batched(Operator &A, Preconditioner *M, int k, const int32_t *
     report.residual.assign(k, 0.0);
     report.cycles = 0;
     if (k <= 0 || n <= 0) return cudaSuccess;
-    Scratch mem;
+    Scratch mem(st);
     const size_t nk = (size_t)n * k;
     cd *V = mem.get<cd>((size_t)(m + 1) * nk);
     cd *bc = mem.get<cd>(nk), *xc = mem.get<cd>(nk), *r = mem.get<cd>(nk), *w = mem.get<cd>(nk);
@@ -475,7 +478,7 @@ cudaError_t refine_batched(Operator &A, Operator &A32, Preconditioner *M, int k,
     report.residual.assign(k, 0.0);
     outer_steps = 0;
     if (k <= 0 || n <= 0) return cudaSuccess;
-    Scratch mem;
+    Scratch mem(st);
     cd *r = mem.get<cd>((size_t)n * k), *rc = mem.get<cd>((size_t)n * k), *dc = mem.get<cd>((size_t)n * k);
     double *part = mem.get<double>((size_t)NCHUNK * k), *norm = mem.get<double>(k);
     int *act_dev = mem.get<int>(k), *sys_dev = mem.get<int>(k);
@@ -485,14 +488,24 @@ cudaError_t refine_batched(Operator &A, Operator &A32, Preconditioner *M, int k,
     cudaError_t err;
     if ((err = column_norms(n, k, b, norm, part, st))) return err;
     note_launches(2);
-    std::vector<double> bn(k), rn(k);
+    std::vector<double> bn(k), rn(k), xn(k);
     cudaMemcpyAsync(bn.data(), norm, sizeof(double) * k, cudaMemcpyDeviceToHost, st);
     if ((err = cudaStreamSynchronize(st))) return err;
+    // a zero initial guess has residual b: the first FP64 product is skipped
+    if ((err = column_norms(n, k, x, norm, part, st))) return err;
+    note_launches(2);
+    cudaMemcpyAsync(xn.data(), norm, sizeof(double) * k, cudaMemcpyDeviceToHost, st);
+    if ((err = cudaStreamSynchronize(st))) return err;
+    const bool zero_guess = std::all_of(xn.begin(), xn.end(), [](double v) { return v == 0.0; });
     for (int outer = 0; outer <= opt.max_outer; ++outer) {
         // the true residual of every column, with the FP64 operator
         cudaMemcpyAsync(sys_dev, sys_all.data(), sizeof(int) * k, cudaMemcpyHostToDevice, st);
-        if ((err = A.apply(k, sys_dev, x, r, st))) return err;
-        if ((err = subtract_from((int64_t)n * k, b, r, st))) return err;
+        if (outer == 0 && zero_guess) {
+            if ((err = cudaMemcpyAsync(r, b, sizeof(cd) * n * k, cudaMemcpyDeviceToDevice, st))) return err;
+        } else {
+            if ((err = A.apply(k, sys_dev, x, r, st))) return err;
+            if ((err = subtract_from((int64_t)n * k, b, r, st))) return err;
+        }
         if ((err = column_norms(n, k, r, norm, part, st))) return err;
         note_launches(2);
         cudaMemcpyAsync(rn.data(), norm, sizeof(double) * k, cudaMemcpyDeviceToHost, st);

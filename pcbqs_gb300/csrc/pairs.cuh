@@ -122,7 +122,7 @@ __device__ __forceinline__ void pair_moments(const Geometry &g, int a, int b, do
 // two-float split of the centroids, the rule points as small offsets u, v. Every term stays of the size of the
 // triangles, so the RWG combine of these moments has no cancellation (the centred-coordinate form cancels by
 // about (board / edge)^2 and cannot be used in FP32).
-__device__ __forceinline__ void far_local(const LocalRec &a, const LocalRec &b, bool scalar, double *m) {
+__device__ __forceinline__ void far_local(const LocalRec &a, const LocalRec &b, bool scalar, float *m) {
     const float dcx = (a.chi[0] - b.chi[0]) + (a.clo[0] - b.clo[0]);
     const float dcy = (a.chi[1] - b.chi[1]) + (a.clo[1] - b.clo[1]);
     const float dz = a.z - b.z, d2 = dz * dz;
@@ -160,11 +160,38 @@ __device__ __forceinline__ void to_local(const ClsRec &ca, const ClsRec &cb, dou
     m[5] = rr - (ca.cx * sx + ca.cy * sy) - (cb.cx * ox + cb.cy * oy) + (ca.cx * cb.cx + ca.cy * cb.cy) * m0;
 }
 
-__device__ __forceinline__ bool finite6(const double *m, bool scalar) {
+template <class V> __device__ __forceinline__ bool finite6(const V *m, bool scalar) {
     bool ok = isfinite(m[0]);
     if (!scalar)
         for (int j = 1; j < 6; ++j) ok = ok && isfinite(m[j]);
     return ok;
+}
+
+// The near/far rule of classify() decided in FP32 from the centroid split (chi + clo) and float radii whenever the
+// FP32 distance clears a threshold by a relative margin of 1e-5 (far above FP32's rounding of these few
+// operations, so the FP64 rule necessarily agrees); only pairs within the margin of a threshold are classified by
+// the exact FP64 rule. Keeps the mixed tile kernel off the FP64 pipe for all but a sliver of pairs.
+__device__ __forceinline__ int classify_filtered(const LocalRec &a, const LocalRec &b, float ra, float rb,
+                                                 const ClsRec &ca, const ClsRec &cb, float near_f, double near,
+                                                 int all_near, int outer) {
+    const float dcx = (a.chi[0] - b.chi[0]) + (a.clo[0] - b.clo[0]);
+    const float dcy = (a.chi[1] - b.chi[1]) + (a.clo[1] - b.clo[1]);
+    const float dz = a.z - b.z;
+    const float dist2 = dcx * dcx + dcy * dcy + dz * dz;
+    const float size = ra + rb;
+    constexpr float lo = 1.0f - 1e-5f, hi = 1.0f + 1e-5f;
+    bool exact = false;
+    if (!all_near) {
+        const float t = near_f * size, t2 = t * t;
+        if (dist2 > t2 * hi) return -1;
+        exact = !(dist2 < t2 * lo);
+    }
+    if (!exact) {
+        const float s2 = size * size;
+        if (dist2 > s2 * hi) return 0;
+        if (dist2 < s2 * lo) return outer;
+    }
+    return classify(ca, cb, ca.z - cb.z, near, all_near, outer);
 }
 
 }  // namespace pq

@@ -25,7 +25,9 @@
 
 #include "../../include/pcbqs_gb300.h"
 #include "common.cuh"
+#include "pool.cuh"
 #include "solve.cuh"
+#include "trsolve.cuh"
 
 namespace pq {
 
@@ -260,18 +262,83 @@ static int grid_of(int64_t total) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)sms * 16));
 }
 
-// Real symmetric M (ld) times complex X (rows x k) as one GEMM on the real view: C (rows x 2k row-major).
-static cublasStatus_t gemm_real_sym(cublasHandle_t h, int64_t rows, int k, const double *M, int64_t ld,
-                                    const cd *X, cd *C) {
-    const double one = 1.0, zero = 0.0;
-    return cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, 2 * k, (int)rows, (int)rows, &one,
-                       reinterpret_cast<const double *>(X), 2 * k, M, (int)ld, &zero, reinterpret_cast<double *>(C),
-                       2 * k);
+// Y = M X for a dense symmetric real M (rows x rows, leading dimension ld, FP64 or its FP32 copy) and complex128
+// X, Y (rows x k, row-major): the real view X (rows x 2k) in passes of up to DENSE_NC real columns. Thread block of
+// 8 warps on 8 * RW rows; every warp streams its rows' entries along i (coalesced) against a 256-entry chunk of X
+// staged in shared memory column by column (conflict-free), so each M entry costs exactly its NC multiply-adds:
+// the FP64 product runs at the FP64 pipe's rate with no padding of the 2k columns, the FP32 one at HBM speed.
+constexpr int DENSE_NC = 16;
+constexpr int DENSE_CHUNK = 256;
+
+template <class T, int RW>
+__global__ void __launch_bounds__(256) k_dense_sym_apply(int64_t rows, const T *__restrict__ M, int64_t ld,
+                                                         const double *__restrict__ X, int xcols, int c0, int nc,
+                                                         double *__restrict__ Y) {
+    __shared__ T xs[DENSE_NC][DENSE_CHUNK];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r0 = ((int64_t)blockIdx.x * 8 + warp) * RW;
+    T acc[RW][DENSE_NC];
+#pragma unroll
+    for (int r = 0; r < RW; ++r)
+#pragma unroll
+        for (int c = 0; c < DENSE_NC; ++c) acc[r][c] = 0;
+    const T *mrow[RW];
+#pragma unroll
+    for (int r = 0; r < RW; ++r) mrow[r] = M + (r0 + r < rows ? r0 + r : 0) * ld;
+    for (int64_t i0 = 0; i0 < rows; i0 += DENSE_CHUNK) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < DENSE_CHUNK * DENSE_NC; t += 256) {
+            const int ii = t / DENSE_NC, c = t % DENSE_NC;
+            const int64_t i = i0 + ii;
+            xs[c][ii] = (i < rows && c < nc) ? (T)X[i * xcols + c0 + c] : (T)0;
+        }
+        __syncthreads();
+        const int span = rows - i0 < DENSE_CHUNK ? (int)(rows - i0) : DENSE_CHUNK;
+        for (int ii = lane; ii < span; ii += 32) {
+            T mv[RW];
+#pragma unroll
+            for (int r = 0; r < RW; ++r) mv[r] = mrow[r][i0 + ii];
+#pragma unroll
+            for (int c = 0; c < DENSE_NC; ++c) {
+                const T xv = xs[c][ii];
+#pragma unroll
+                for (int r = 0; r < RW; ++r) acc[r][c] += mv[r] * xv;
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < RW; ++r)
+#pragma unroll
+        for (int c = 0; c < DENSE_NC; ++c) {
+            T v = acc[r][c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0 && r0 + r < rows && c < nc) Y[(r0 + r) * xcols + c0 + c] = (double)v;
+        }
 }
 
-template <class T> static cudaError_t dev_alloc(T **p, size_t count) {
-    return cudaMalloc(reinterpret_cast<void **>(p), std::max<size_t>(count, 1) * sizeof(T));
+template <class T, int RW>
+static cudaError_t dense_sym_apply(int64_t rows, int k, const T *M, int64_t ld, const cd *X, cd *Y, cudaStream_t s) {
+    const int xcols = 2 * k;
+    const unsigned grid = (unsigned)((rows + 8 * RW - 1) / (8 * RW));
+    for (int c0 = 0; c0 < xcols; c0 += DENSE_NC) {
+        const int nc = std::min(DENSE_NC, xcols - c0);
+        k_dense_sym_apply<T, RW><<<grid, 256, 0, s>>>(rows, M, ld, reinterpret_cast<const double *>(X), xcols, c0,
+                                                      nc, reinterpret_cast<double *>(Y));
+        note_launches(1);
+    }
+    return cudaGetLastError();
 }
+
+
+// Device buffers come from the retained stream-ordered pool (pool.cuh): the dense blocks, factors and work arrays
+// of one solve are reused by the next instead of being mapped and unmapped each time. Buffers that outlive a call
+// are released on the legacy stream, after the call that used them has synchronized its stream.
+template <class T> static cudaError_t dev_alloc(T **p, size_t count, cudaStream_t s = nullptr) {
+    return pool_alloc_n(p, count, s);
+}
+
+static void dev_free(void *p, cudaStream_t s = nullptr) { pool_free(p, s); }
 
 __global__ void k_to_f32(int64_t count, const double *in, float *out) {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x)
@@ -292,21 +359,20 @@ struct PeecOp : Operator {
     double pscale = 1;
     int nsys = 0;
     double *omega = nullptr, *zscale = nullptr, *walpha = nullptr, *inv_z = nullptr, *inv_p = nullptr;
-    cublasHandle_t blas = nullptr;
     int cap = 0;               // columns the scratch holds
     cd *u = nullptr, *branch = nullptr, *lb = nullptr, *v = nullptr, *tq = nullptr, *pq = nullptr;
     int64_t launches = 0;
 
     int64_t n() const override { return n_; }
 
-    cudaError_t reserve(int k) {
+    cudaError_t reserve(int k, cudaStream_t s) {
         if (k <= cap) return cudaSuccess;
-        for (cd *p : {u, branch, lb, v, tq, pq}) cudaFree(p);
+        for (cd *p : {u, branch, lb, v, tq, pq}) dev_free(p, s);
         u = branch = lb = v = tq = pq = nullptr;
         cudaError_t e;
-        if ((e = dev_alloc(&u, (size_t)n_ * k)) || (e = dev_alloc(&branch, (size_t)nb * k)) ||
-            (e = dev_alloc(&lb, (size_t)ne * k)) || (e = dev_alloc(&v, (size_t)nb * k)) ||
-            (e = dev_alloc(&tq, (size_t)nn * k)) || (e = dev_alloc(&pq, (size_t)nn * k)))
+        if ((e = dev_alloc(&u, (size_t)n_ * k, s)) || (e = dev_alloc(&branch, (size_t)nb * k, s)) ||
+            (e = dev_alloc(&lb, (size_t)ne * k, s)) || (e = dev_alloc(&v, (size_t)nb * k, s)) ||
+            (e = dev_alloc(&tq, (size_t)nn * k, s)) || (e = dev_alloc(&pq, (size_t)nn * k, s)))
             return e;
         cap = k;
         return cudaSuccess;
@@ -315,40 +381,18 @@ struct PeecOp : Operator {
     // Single-precision copies of L and P for the inner products of the mixed solve (set by peec_single).
     const float *Lf = nullptr, *Pf = nullptr;
     int64_t ldlf = 0, ldpf = 0;
-    float *xf = nullptr, *yf = nullptr;
-    int capf = 0;
 
     // y (rows x k complex128) = M x for a dense symmetric M, in FP64 (cuBLAS DGEMM) or through its single-precision
     // copy (SGEMM on converted vectors) when `single`.
     cudaError_t dense(bool single, int64_t rows, int k, const double *M, int64_t ld, const float *Mf, int64_t ldf,
                       const cd *x, cd *y, cudaStream_t s) {
-        if (!single) {
-            if (gemm_real_sym(blas, rows, k, M, ld, x, y) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
-            return cudaSuccess;
-        }
-        const int64_t need = std::max(ne, nn) * 2 * k;
-        if (need > capf) {
-            cudaFree(xf);
-            cudaFree(yf);
-            xf = yf = nullptr;
-            cudaError_t e;
-            if ((e = dev_alloc(&xf, need)) || (e = dev_alloc(&yf, need))) return e;
-            capf = (int)need;
-        }
-        k_to_f32<<<grid_of(rows * 2 * k), 256, 0, s>>>(rows * 2 * k, reinterpret_cast<const double *>(x), xf);
-        const float one = 1.0f, zero = 0.0f;
-        if (cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * k, (int)rows, (int)rows, &one, xf, 2 * k, Mf, (int)ldf,
-                        &zero, yf, 2 * k) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        k_to_f64<<<grid_of(rows * 2 * k), 256, 0, s>>>(rows * 2 * k, yf, reinterpret_cast<double *>(y));
-        note_launches(2);
-        return cudaSuccess;
+        if (!single) return dense_sym_apply<double, 2>(rows, k, M, ld, x, y, s);
+        return dense_sym_apply<float, 4>(rows, k, Mf, ldf, x, y, s);
     }
 
     cudaError_t apply_impl(bool single, int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) {
-        cudaError_t e = reserve(k);
+        cudaError_t e = reserve(k, s);
         if (e) return e;
-        cublasSetStream(blas, s);
         k_tree_scale<<<grid_of(n_ * k), 256, 0, s>>>(n_, k, is_tree, walpha, sys, in, u);
         k_spmm<<<grid_of(nb * k), 256, 0, s>>>(K, k, u, branch, nullptr, sys, 0);
         if ((e = dense(single, ne, k, L, ldl, Lf, ldlf, branch, lb, s))) return e;
@@ -369,11 +413,8 @@ struct PeecOp : Operator {
     }
 
     ~PeecOp() override {
-        cudaFree(xf);
-        cudaFree(yf);
-        for (cd *p : {u, branch, lb, v, tq, pq}) cudaFree(p);
-        for (double *p : {omega, zscale, walpha, inv_z, inv_p}) cudaFree(p);
-        if (blas) cublasDestroy(blas);
+        for (cd *p : {u, branch, lb, v, tq, pq}) dev_free(p);
+        for (double *p : {omega, zscale, walpha, inv_z, inv_p}) dev_free(p);
     }
 };
 
@@ -390,7 +431,7 @@ struct BlockJacobi : Preconditioner {
     int64_t n = 0, nblk = 0;
     int bs = 32;
     cd *inv = nullptr;
-    ~BlockJacobi() override { cudaFree(inv); }
+    ~BlockJacobi() override { dev_free(inv); }
     cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) override {
         k_block_apply<<<grid_of(n * k), 256, 0, s>>>(n, bs, nblk, k, inv, sys, in, out);
         note_launches(1);
@@ -412,14 +453,19 @@ __global__ void k_rows_combine(Csr St, const double *M, int64_t ldm, int64_t nco
     }
 }
 
-// out[j, i] = sum_{a in row i of St} St.val[a] W[j, St.idx[a]]: (W S) with S given by St. Grid: (i chunks, rows j).
-__global__ void k_gather_mult(Csr St, const double *W, int64_t ldw, int64_t n, double *out, int64_t ldo) {
-    const int64_t j = blockIdx.y;
-    const double *row = W + j * ldw;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double acc = 0;
-        for (int64_t a = St.ptr[i]; a < St.ptr[i + 1]; ++a) acc += St.val[a] * row[St.idx[a]];
-        out[j * ldo + i] = acc;
+// out (cols x rows) = W^T for W (rows x cols, leading dimension ldw): 32 x 32 tiles through shared memory so that
+// both the reads and the writes are coalesced. Block (32, 8), grid (cols / 32, rows / 32).
+__global__ void k_transpose(const double *W, int64_t rows, int64_t cols, int64_t ldw, double *out, int64_t ldo) {
+    __shared__ double tile[32][33];
+    const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
+    for (int dy = threadIdx.y; dy < 32; dy += 8) {
+        const int64_t r = r0 + dy, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) tile[dy][threadIdx.x] = W[r * ldw + c];
+    }
+    __syncthreads();
+    for (int dy = threadIdx.y; dy < 32; dy += 8) {
+        const int64_t c = c0 + dy, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) out[c * ldo + r] = tile[threadIdx.x][dy];
     }
 }
 
@@ -476,21 +522,27 @@ struct LuPrecond : Preconditioner {
     int64_t n = 0;
     float2 *lu = nullptr;        // complex64 factor of the row-major system (the transpose, column-major)
     int *ipiv = nullptr, *info = nullptr;
-    float2 *work = nullptr;      // right-hand sides, column-major
+    float2 *work = nullptr;      // right-hand sides, column-major (library solve)
     int cap = 0;
     cusolverDnHandle_t solver = nullptr;
+    TriSolver tri;               // streaming triangular solves (the solve every GMRES step uses)
     ~LuPrecond() override {
-        cudaFree(lu);
-        cudaFree(ipiv);
-        cudaFree(info);
-        cudaFree(work);
+        tri.release();
+        dev_free(lu);
+        dev_free(ipiv);
+        dev_free(info);
+        dev_free(work);
         if (solver) cusolverDnDestroy(solver);
     }
     cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        return tri.solve(k, in, out, s);
+    }
+    // The same solve through cuSOLVER getrs, for validation of the streaming solver.
+    cudaError_t apply_library(int k, const cd *in, cd *out, cudaStream_t s) {
         if (k > cap) {
-            cudaFree(work);
+            dev_free(work, s);
             work = nullptr;
-            cudaError_t e = dev_alloc(&work, (size_t)n * k);
+            cudaError_t e = dev_alloc(&work, (size_t)n * k, s);
             if (e) return e;
             cap = k;
         }
@@ -531,15 +583,15 @@ struct CholPrecond : Preconditioner {
     int cap = 0;
     cusolverDnHandle_t solver = nullptr;
     ~CholPrecond() override {
-        cudaFree(chol);
-        cudaFree(work);
-        cudaFree(info);
+        dev_free(chol);
+        dev_free(work);
+        dev_free(info);
         if (solver) cusolverDnDestroy(solver);
     }
     cudaError_t factor(int64_t n_, const double *A, int64_t lda, cudaStream_t s, int &host_info) {
         n = n_;
         cudaError_t e;
-        if ((e = dev_alloc(&chol, (size_t)n * n)) || (e = dev_alloc(&info, 1))) return e;
+        if ((e = dev_alloc(&chol, (size_t)n * n, s)) || (e = dev_alloc(&info, 1, s))) return e;
         if (lda == n) {
             k_to_f32<<<grid_of(n * n), 256, 0, s>>>(n * n, A, chol);
             note_launches(1);
@@ -551,25 +603,27 @@ struct CholPrecond : Preconditioner {
         }
         if (cusolverDnCreate(&solver) != CUSOLVER_STATUS_SUCCESS) return cudaErrorUnknown;
         cusolverDnSetStream(solver, s);
+        // FP32 arithmetic emulated with BF16x9 products on the tensor cores (FP32 accuracy)
+        cusolverDnSetMathMode(solver, CUSOLVER_FP32_EMULATED_BF16X9_MATH);
         int lwork = 0;
         if (cusolverDnSpotrf_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)n, chol, (int)n, &lwork) !=
             CUSOLVER_STATUS_SUCCESS)
             return cudaErrorUnknown;
         float *ws = nullptr;
-        if ((e = dev_alloc(&ws, (size_t)lwork))) return e;
+        if ((e = dev_alloc(&ws, (size_t)lwork, s))) return e;
         const cusolverStatus_t cs = cusolverDnSpotrf(solver, CUBLAS_FILL_MODE_LOWER, (int)n, chol, (int)n, ws, lwork,
                                                      info);
         cudaMemcpyAsync(&host_info, info, sizeof(int), cudaMemcpyDeviceToHost, s);
         e = cudaStreamSynchronize(s);
-        cudaFree(ws);
+        dev_free(ws, s);
         if (cs != CUSOLVER_STATUS_SUCCESS) return cudaErrorUnknown;
         return e;
     }
     cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
         if (2 * k > cap) {
-            cudaFree(work);
+            dev_free(work, s);
             work = nullptr;
-            cudaError_t e = dev_alloc(&work, (size_t)n * 2 * k);
+            cudaError_t e = dev_alloc(&work, (size_t)n * 2 * k, s);
             if (e) return e;
             cap = 2 * k;
         }
@@ -587,12 +641,9 @@ struct CholPrecond : Preconditioner {
 struct DenseSym : Operator {
     int64_t n_ = 0, ld = 0;
     const double *A = nullptr;
-    cublasHandle_t blas = nullptr;
     int64_t n() const override { return n_; }
     cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
-        cublasSetStream(blas, s);
-        if (gemm_real_sym(blas, n_, k, A, ld, in, out) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
-        return cudaSuccess;
+        return dense_sym_apply<double, 2>(n_, k, A, ld, in, out, s);
     }
 };
 
@@ -618,8 +669,8 @@ struct pcbqs_gb300_peec {
     ~pcbqs_gb300_peec() {
         delete bj;
         delete lu;
-        cudaFree(klk);
-        cudaFree(tpt);
+        dev_free(klk);
+        dev_free(tpt);
     }
 };
 
@@ -673,10 +724,6 @@ int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *d, pcbqs_gb300_peec **o
     cudaMemcpy(op.walpha, wa.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
     cudaMemcpy(op.inv_z, iz.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
     cudaMemcpy(op.inv_p, ip.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
-    if (cublasCreate(&op.blas) != CUBLAS_STATUS_SUCCESS) {
-        delete h;
-        return pfail(ERR_CUDA, "peec_create: cuBLAS handle");
-    }
     *out = h;
     return OK;
 }
@@ -690,11 +737,11 @@ int pcbqs_gb300_peec_apply(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
         if (sys_host[s] < 0 || sys_host[s] >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_apply: system index");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int *sys = nullptr;
-    if (dev_alloc(&sys, k)) return pfail(ERR_MEMORY, "peec_apply: allocation");
+    if (dev_alloc(&sys, k, st)) return pfail(ERR_MEMORY, "peec_apply: allocation");
     cudaMemcpyAsync(sys, sys_host, sizeof(int) * k, cudaMemcpyHostToDevice, st);
     cudaError_t e = h->op.apply(k, sys, reinterpret_cast<const cd *>(in), reinterpret_cast<cd *>(out), st);
     if (!e) e = cudaStreamSynchronize(st);
-    cudaFree(sys);
+    dev_free(sys, st);
     if (e) return pfail(ERR_CUDA, "peec_apply: %s", cudaGetErrorString(e));
     return OK;
 }
@@ -711,9 +758,9 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     if (!bj) return pfail(ERR_MEMORY, "block_jacobi: host allocation");
     bj->n = op.n_; bj->nblk = nblk; bj->bs = bs;
     cudaError_t e;
-    if ((e = dev_alloc(&klk, bsz)) || (e = dev_alloc(&tpt, bsz)) || (e = dev_alloc(&singular, 1)) ||
-        (e = dev_alloc(&bj->inv, (size_t)op.nsys * bsz))) {
-        cudaFree(klk); cudaFree(tpt); cudaFree(singular);
+    if ((e = dev_alloc(&klk, bsz, st)) || (e = dev_alloc(&tpt, bsz, st)) || (e = dev_alloc(&singular, 1, st)) ||
+        (e = dev_alloc(&bj->inv, (size_t)op.nsys * bsz, st))) {
+        dev_free(klk, st); dev_free(tpt, st); dev_free(singular, st);
         delete bj;
         return pfail(ERR_MEMORY, "block_jacobi: %s", cudaGetErrorString(e));
     }
@@ -730,7 +777,7 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     int sing = 0;
     cudaMemcpyAsync(&sing, singular, sizeof(int), cudaMemcpyDeviceToHost, st);
     e = cudaStreamSynchronize(st);
-    cudaFree(klk); cudaFree(tpt); cudaFree(singular);
+    dev_free(klk, st); dev_free(tpt, st); dev_free(singular, st);
     if (e) {
         delete bj;
         return pfail(ERR_CUDA, "block_jacobi: %s", cudaGetErrorString(e));
@@ -754,32 +801,40 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     cudaError_t e;
     const size_t nn2 = (size_t)n * n;
     if (!h->klk) {
-        // K^T L K = (K^T L) K and T^T P T = (T^T P) T, each through one dense intermediate of n rows.
-        double *w = nullptr;
+        // K^T L K = K^T (K^T L)^T (L symmetric) and T^T P T likewise: a row combination of L into W = K^T L (n rows),
+        // its transpose, and a second row combination; every pass streams whole rows (no gathers).
+        double *w = nullptr, *wt = nullptr;
         const int64_t wcols = std::max(op.ne, op.nn);
-        if ((e = dev_alloc(&h->klk, nn2)) || (e = dev_alloc(&h->tpt, nn2)) || (e = dev_alloc(&w, (size_t)n * wcols))) {
-            cudaFree(w);
+        if ((e = dev_alloc(&h->klk, nn2, st)) || (e = dev_alloc(&h->tpt, nn2, st)) ||
+            (e = dev_alloc(&w, (size_t)n * wcols, st)) || (e = dev_alloc(&wt, (size_t)n * wcols, st))) {
+            dev_free(w, st);
+            dev_free(wt, st);
             return pfail(ERR_MEMORY, "peec_factor: dense system blocks: %s", cudaGetErrorString(e));
         }
         const unsigned chunks = 8;
         dim3 g1(chunks, (unsigned)n);
-        k_rows_combine<<<g1, 256, 0, st>>>(op.Kt, op.L, op.ldl, op.ne, w, wcols);
-        k_gather_mult<<<g1, 256, 0, st>>>(op.Kt, w, wcols, n, h->klk, n);
+        auto triple = [&](const Csr &St, const double *M, int64_t ldm, int64_t m, double *out) {
+            k_rows_combine<<<g1, 256, 0, st>>>(St, M, ldm, m, w, m);
+            dim3 gt((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
+            k_transpose<<<gt, dim3(32, 8), 0, st>>>(w, n, m, m, wt, n);
+            k_rows_combine<<<g1, 256, 0, st>>>(St, wt, n, n, out, n);
+        };
+        triple(op.Kt, op.L, op.ldl, op.ne, h->klk);
         if (op.nn > 0) {
-            k_rows_combine<<<g1, 256, 0, st>>>(op.Tt, op.P, op.ldp, op.nn, w, wcols);
-            k_gather_mult<<<g1, 256, 0, st>>>(op.Tt, w, wcols, n, h->tpt, n);
+            triple(op.Tt, op.P, op.ldp, op.nn, h->tpt);
         } else {
             cudaMemsetAsync(h->tpt, 0, sizeof(double) * nn2, st);
         }
-        note_launches(op.nn > 0 ? 4 : 2);
+        note_launches(op.nn > 0 ? 6 : 3);
         e = cudaStreamSynchronize(st);
-        cudaFree(w);
+        dev_free(w, st);
+        dev_free(wt, st);
         if (e) return pfail(ERR_CUDA, "peec_factor: %s", cudaGetErrorString(e));
     }
     auto *lu = new (std::nothrow) LuPrecond();
     if (!lu) return pfail(ERR_MEMORY, "peec_factor: host allocation");
     lu->n = n;
-    if ((e = dev_alloc(&lu->lu, nn2)) || (e = dev_alloc(&lu->ipiv, n)) || (e = dev_alloc(&lu->info, 1))) {
+    if ((e = dev_alloc(&lu->lu, nn2, st)) || (e = dev_alloc(&lu->ipiv, n, st)) || (e = dev_alloc(&lu->info, 1, st))) {
         delete lu;
         return pfail(ERR_MEMORY, "peec_factor: factor of %lld unknowns: %s", (long long)n, cudaGetErrorString(e));
     }
@@ -806,7 +861,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         return pfail(ERR_CUDA, "peec_factor: workspace query");
     }
     float2 *ws = nullptr;
-    if ((e = dev_alloc(&ws, (size_t)lwork))) {
+    if ((e = dev_alloc(&ws, (size_t)lwork, st))) {
         delete lu;
         return pfail(ERR_MEMORY, "peec_factor: workspace");
     }
@@ -815,22 +870,30 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     int info = 0;
     cudaMemcpyAsync(&info, lu->info, sizeof(int), cudaMemcpyDeviceToHost, st);
     e = cudaStreamSynchronize(st);
-    cudaFree(ws);
+    dev_free(ws, st);
     if (cs != CUSOLVER_STATUS_SUCCESS || e || info != 0) {
         delete lu;
         return pfail(info ? ERR_NONFINITE : ERR_CUDA, "peec_factor: getrf failed (status %d, info %d, %s)", (int)cs,
                      info, cudaGetErrorString(e));
+    }
+    if ((e = lu->tri.prepare(lu->lu, n, lu->ipiv, st))) {
+        delete lu;
+        return pfail(ERR_CUDA, "peec_factor: triangular-solve set-up: %s", cudaGetErrorString(e));
     }
     delete h->lu;
     h->lu = lu;
     return OK;
 }
 
-int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *h, int k, const double *in, double *out, void *stream) {
-    if (!h || k <= 0 || !in || !out) return pfail(ERR_ARGUMENT, "peec_lu_solve: invalid argument");
+int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *h, int k, const double *in, double *out, int method,
+                              void *stream) {
+    if (!h || k <= 0 || !in || !out || method < 0 || method > 1)
+        return pfail(ERR_ARGUMENT, "peec_lu_solve: invalid argument");
     if (!h->lu) return pfail(ERR_ARGUMENT, "peec_lu_solve: no factor set up");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    cudaError_t e = h->lu->apply(k, nullptr, reinterpret_cast<const cd *>(in), reinterpret_cast<cd *>(out), st);
+    const cd *x = reinterpret_cast<const cd *>(in);
+    cd *y = reinterpret_cast<cd *>(out);
+    cudaError_t e = method == 0 ? h->lu->apply(k, nullptr, x, y, st) : h->lu->apply_library(k, x, y, st);
     if (!e) e = cudaStreamSynchronize(st);
     if (e) return pfail(ERR_CUDA, "peec_lu_solve: %s", cudaGetErrorString(e));
     return OK;
@@ -931,15 +994,13 @@ int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, cons
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     DenseSym op;
     op.n_ = n; op.ld = lda; op.A = A;
-    if (cublasCreate(&op.blas) != CUBLAS_STATUS_SUCCESS) return pfail(ERR_CUDA, "dense_gmres: cuBLAS handle");
     Jacobi J;
     CholPrecond C;
     Preconditioner *M = nullptr;
     cudaError_t e = cudaSuccess;
     if (precondition == 0) {
         J.n = n;
-        if ((e = dev_alloc(&J.d, n))) {
-            cublasDestroy(op.blas);
+        if ((e = dev_alloc(&J.d, n, st))) {
             return pfail(ERR_MEMORY, "dense_gmres: allocation");
         }
         k_diag_extract<<<grid_of(n), 256, 0, st>>>(n, A, lda, J.d);
@@ -949,7 +1010,6 @@ int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, cons
         int info = 0;
         e = C.factor(n, A, lda, st, info);
         if (e || info) {
-            cublasDestroy(op.blas);
             return pfail(info ? ERR_NONFINITE : ERR_CUDA, "dense_gmres: single-precision Cholesky failed (info %d)",
                          info);
         }
@@ -960,8 +1020,7 @@ int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, cons
     opt.tol = tol; opt.maxiter = maxiter; opt.restart = restart;
     GmresReport rep;
     e = gmres_batched(op, M, k, sys.data(), reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x), opt, rep, st);
-    cudaFree(J.d);
-    cublasDestroy(op.blas);
+    dev_free(J.d, st);
     if (e) return pfail(ERR_CUDA, "dense_gmres: %s", cudaGetErrorString(e));
     bool ok = true;
     for (int s = 0; s < k; ++s) {

@@ -1,0 +1,421 @@
+// Triangular solves with the complex64 LU factor of the loop/tree system (trsolve.cuh).
+//
+// cuSOLVER's getrf leaves M = A^T = P L U column-major; read row-major, row r of that array holds row r of U^T
+// (entries 0..r) and row r of L^T (entries r+1..n-1), both contiguous. Solving A x = b = U^T L^T P^T x is a forward
+// sweep with U^T, a backward sweep with L^T and a gather. Each sweep walks super-blocks of TRI_BLOCK rows: the
+// block's rows left (forward) or right (backward) of its diagonal block are streamed against the solved part of the
+// vector, every thread block taking a run of columns of 4 rows (deterministic partial sums, no atomics), then the
+// precomputed inverse of the diagonal block is applied. Both sweeps run in one persistent cooperative kernel whose
+// thread blocks meet at a grid barrier between the phases (bounded waits: a barrier that does not complete within
+// about a second sets a status and every block returns), so the dependency chain of 2 x n / TRI_BLOCK steps costs
+// a barrier each rather than a kernel launch. The factor is read once per sweep, 8 right-hand sides at a time.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "pool.cuh"
+#include "trsolve.cuh"
+
+namespace pq {
+
+namespace {
+
+constexpr int B = TRI_BLOCK;
+constexpr int KC = TRI_COLS;
+constexpr int PANEL_ROWS = 4;                 // rows per thread block of the panel kernel
+constexpr int PANEL_THREADS = 256;
+constexpr int MAX_SPLITS = 16;                // column runs per panel row group
+constexpr int PANEL_UNROLL = 4;               // columns per thread with loads in flight together
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ float2 cdiv(float2 a, float2 b) {
+    const float d = b.x * b.x + b.y * b.y;
+    return make_float2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+// Inverse of the lower-triangular diagonal block J of U^T: D[a][b] = lu[(J B + a) n + J B + b], b <= a. Thread c
+// solves D X[:, c] = e_c down the rows (its own column only, no synchronization), X in shared memory.
+__global__ void k_tri_invert_lower(const float2 *lu, int64_t n, float2 *inv) {
+    extern __shared__ float2 X[];             // B x B
+    const int J = blockIdx.x, c = threadIdx.x;
+    const int64_t base = (int64_t)J * B;
+    const int m = n - base < B ? (int)(n - base) : B;
+    for (int a = 0; a < B; ++a) {
+        float2 v = make_float2(0.f, 0.f);
+        if (a < m && c < m && c <= a) {
+            const float2 *row = lu + (base + a) * n + base;
+            float2 s = make_float2(a == c ? 1.f : 0.f, 0.f);
+            for (int b = c; b < a; ++b) {
+                const float2 t = cmul(__ldg(row + b), X[b * B + c]);
+                s.x -= t.x;
+                s.y -= t.y;
+            }
+            v = cdiv(s, __ldg(row + a));
+        }
+        X[a * B + c] = v;
+    }
+    float2 *out = inv + (int64_t)J * B * B;
+    for (int a = 0; a < B; ++a) out[a * B + c] = X[a * B + c];
+}
+
+// Inverse of the unit upper-triangular diagonal block J of L^T: E[a][b] = lu[(J B + a) n + J B + b], b > a.
+__global__ void k_tri_invert_upper(const float2 *lu, int64_t n, float2 *inv) {
+    extern __shared__ float2 X[];
+    const int J = blockIdx.x, c = threadIdx.x;
+    const int64_t base = (int64_t)J * B;
+    const int m = n - base < B ? (int)(n - base) : B;
+    for (int a = B - 1; a >= 0; --a) {
+        float2 v = make_float2(0.f, 0.f);
+        if (a < m && c < m && a <= c) {
+            const float2 *row = lu + (base + a) * n + base;
+            float2 s = make_float2(a == c ? 1.f : 0.f, 0.f);
+            for (int b = a + 1; b <= c; ++b) {
+                const float2 t = cmul(__ldg(row + b), X[b * B + c]);
+                s.x -= t.x;
+                s.y -= t.y;
+            }
+            v = s;
+        }
+        X[a * B + c] = v;
+    }
+    float2 *out = inv + (int64_t)J * B * B;
+    for (int a = 0; a < B; ++a) out[a * B + c] = X[a * B + c];
+}
+
+// partial[s][r][c] = sum over columns i of run s (of `runs`) of [col0, col1) of lu[(row0 + r) n + i] x[i][c0 + c],
+// for the 4 rows r of row group rg (r < m). Each thread keeps 4 x KC complex sums, so every 8 B of the factor it
+// streams meets 8 complex multiply-adds and a vector entry is loaded once for 4 rows; PANEL_UNROLL columns per
+// thread have their loads in flight together. x is written during the kernel, so it is read through L2 (ld.cg).
+__device__ __forceinline__ void panel_block(const float2 *__restrict__ lu, int64_t n, int64_t row0, int m,
+                                            int64_t col0, int64_t col1, const float2 *x, int kpad, int c0,
+                                            float2 *partial, int rg, int s, int runs) {
+    const int64_t len = col1 - col0;
+    const int64_t i0 = col0 + len * s / runs, i1 = col0 + len * (s + 1) / runs;
+    float acc[PANEL_ROWS][KC][2];
+#pragma unroll
+    for (int r = 0; r < PANEL_ROWS; ++r)
+#pragma unroll
+        for (int c = 0; c < KC; ++c) acc[r][c][0] = acc[r][c][1] = 0.f;
+    const float2 *rows[PANEL_ROWS];
+    bool valid[PANEL_ROWS];
+#pragma unroll
+    for (int r = 0; r < PANEL_ROWS; ++r) {
+        const int rr = rg * PANEL_ROWS + r;
+        valid[r] = rr < m;
+        rows[r] = lu + (row0 + (valid[r] ? rr : 0)) * n;
+    }
+    for (int64_t base = i0 + threadIdx.x; base < i1; base += (int64_t)PANEL_THREADS * PANEL_UNROLL) {
+        float2 xv[PANEL_UNROLL][KC];
+        float2 t[PANEL_UNROLL][PANEL_ROWS];
+#pragma unroll
+        for (int u = 0; u < PANEL_UNROLL; ++u) {
+            const int64_t i = base + (int64_t)u * PANEL_THREADS;
+            const bool in = i < i1;
+            const float4 *xp = reinterpret_cast<const float4 *>(x + (in ? i : i0) * kpad + c0);
+#pragma unroll
+            for (int q = 0; q < KC / 2; ++q) {
+                const float4 v = in ? __ldcg(xp + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+                xv[u][2 * q] = make_float2(v.x, v.y);
+                xv[u][2 * q + 1] = make_float2(v.z, v.w);
+            }
+#pragma unroll
+            for (int r = 0; r < PANEL_ROWS; ++r)
+                t[u][r] = (in && valid[r]) ? __ldg(rows[r] + i) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < PANEL_UNROLL; ++u)
+#pragma unroll
+            for (int r = 0; r < PANEL_ROWS; ++r)
+#pragma unroll
+                for (int c = 0; c < KC; ++c) {
+                    acc[r][c][0] += t[u][r].x * xv[u][c].x - t[u][r].y * xv[u][c].y;
+                    acc[r][c][1] += t[u][r].x * xv[u][c].y + t[u][r].y * xv[u][c].x;
+                }
+    }
+    __shared__ float red[PANEL_THREADS / 32][PANEL_ROWS * KC * 2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < PANEL_ROWS; ++r)
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                float v = acc[r][c][p];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                if (lane == 0) red[warp][(r * KC + c) * 2 + p] = v;
+            }
+    __syncthreads();
+    if (threadIdx.x < PANEL_ROWS * KC * 2) {
+        float v = 0.f;
+#pragma unroll
+        for (int w = 0; w < PANEL_THREADS / 32; ++w) v += red[w][threadIdx.x];
+        const int r = threadIdx.x / (KC * 2), c = (threadIdx.x / 2) % KC, p = threadIdx.x & 1;
+        const int rr = rg * PANEL_ROWS + r;
+        if (rr < m) reinterpret_cast<float *>(partial)[(((int64_t)s * B + rr) * KC + c) * 2 + p] = v;
+    }
+    __syncthreads();
+}
+
+// x[row0 + a][c0 + c] = sum_b inv[a][b] (rhs[row0 + b][c0 + c] - sum_s partial[s][b][c]) for rows a of quarter q
+// (32 rows; 256 threads = 32 rows x 8 columns). The 32 rows of the inverse are staged in shared memory with
+// coalesced loads, so the dot products never wait on a global load.
+__device__ __forceinline__ void diag_block(const float2 *__restrict__ inv, const float2 *partial, int runs,
+                                           const float2 *rhs, float2 *x, int64_t row0, int m, int kpad, int c0,
+                                           int q) {
+    __shared__ float2 acc[B][KC];
+    __shared__ float2 rows_s[32][B + 1];
+    for (int t = threadIdx.x; t < 32 * B; t += blockDim.x) {
+        const int a = t / B, b = t % B;
+        rows_s[a][b] = (32 * q + a < m && b < m) ? __ldg(inv + (int64_t)(32 * q + a) * B + b) : make_float2(0.f, 0.f);
+    }
+    for (int t = threadIdx.x; t < B * KC; t += blockDim.x) {
+        const int b = t / KC, c = t % KC;
+        float2 v = make_float2(0.f, 0.f);
+        if (b < m) {
+            v = __ldcg(rhs + (row0 + b) * kpad + c0 + c);
+            float sx = 0.f, sy = 0.f;
+#pragma unroll 8
+            for (int s = 0; s < runs; ++s) {
+                const float2 p = __ldcg(partial + ((int64_t)s * B + b) * KC + c);
+                sx += p.x;
+                sy += p.y;
+            }
+            v.x -= sx;
+            v.y -= sy;
+        }
+        acc[b][c] = v;
+    }
+    __syncthreads();
+    const int al = threadIdx.x / KC, c = threadIdx.x % KC, a = 32 * q + al;
+    if (a < m) {
+        float re = 0.f, im = 0.f;
+#pragma unroll 8
+        for (int b = 0; b < B; ++b) {
+            const float2 t = rows_s[al][b], v = acc[b][c];
+            re += t.x * v.x - t.y * v.y;
+            im += t.x * v.y + t.y * v.x;
+        }
+        x[(row0 + a) * kpad + c0 + c] = make_float2(re, im);
+    }
+    __syncthreads();
+}
+
+// All thread blocks of the (cooperative, co-resident) grid meet here. Bounded: a block that waits past the limit
+// records TRI_TIMEOUT in *status and the caller returns, so no wait can hang the device.
+constexpr int TRI_TIMEOUT = 1;
+
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *generation, int *status) {
+    __shared__ int ok;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned *gen = generation;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(count, 1u) == gridDim.x - 1) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(generation, 1u);
+        } else {
+            long long spins = 0;
+            while (*gen == g) {
+                if (++spins > (1ll << 24) || *(volatile int *)status) {
+                    atomicExch(status, TRI_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok;
+}
+
+struct SweepArgs {
+    const float2 *lu;
+    int64_t n;
+    int nblk;
+    const float2 *inv_lower, *inv_upper;
+    const float2 *b;
+    float2 *y, *z;
+    int kpad, c0;
+    float2 *partial;
+    unsigned *barrier;     // [0] arrivals, [1] generation
+    int *status;
+};
+
+// Forward sweep b -> y with U^T, then backward sweep y -> z with L^T, for columns c0 .. c0 + 7.
+__global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
+    const int groups = (B + PANEL_ROWS - 1) / PANEL_ROWS;
+    for (int dir = 0; dir < 2; ++dir) {
+        const float2 *inv = dir == 0 ? a.inv_lower : a.inv_upper;
+        const float2 *rhs = dir == 0 ? a.b : a.y;
+        float2 *x = dir == 0 ? a.y : a.z;
+        for (int step = 0; step < a.nblk; ++step) {
+            const int J = dir == 0 ? step : a.nblk - 1 - step;
+            const int64_t row0 = (int64_t)J * B;
+            const int m = a.n - row0 < B ? (int)(a.n - row0) : B;
+            const int64_t col0 = dir == 0 ? 0 : row0 + m, col1 = dir == 0 ? row0 : a.n;
+            const int64_t len = col1 - col0;
+            int runs = 0;
+            if (len > 0) {
+                runs = (int)(gridDim.x / groups);
+                runs = runs < 1 ? 1 : (runs > MAX_SPLITS ? MAX_SPLITS : runs);
+                const int64_t by_len = len / 512;
+                if (by_len < runs) runs = by_len < 1 ? 1 : (int)by_len;
+                const int mg = (m + PANEL_ROWS - 1) / PANEL_ROWS;
+                for (int item = blockIdx.x; item < mg * runs; item += gridDim.x)
+                    panel_block(a.lu, a.n, row0, m, col0, col1, x, a.kpad, a.c0, a.partial, item % mg, item / mg,
+                                runs);
+                if (!grid_barrier(a.barrier, a.barrier + 1, a.status)) return;
+            }
+            for (int q = blockIdx.x; q < B / 32; q += gridDim.x)
+                diag_block(inv + (int64_t)J * B * B, a.partial, runs, rhs, x, row0, m, a.kpad, a.c0, q);
+            if (!grid_barrier(a.barrier, a.barrier + 1, a.status)) return;
+        }
+    }
+}
+
+__global__ void k_tri_in(int64_t n, int k, int kpad, const cd *in, float2 *b) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * kpad;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / kpad;
+        const int c = (int)(t % kpad);
+        const cd v = c < k ? in[i * k + c] : make_double2(0.0, 0.0);
+        b[t] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+__global__ void k_tri_out(int64_t n, int k, int kpad, const float2 *z, const int32_t *gather, cd *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = t / k;
+        const int c = (int)(t % k);
+        const float2 v = z[(int64_t)gather[j] * kpad + c];
+        out[t] = make_double2(v.x, v.y);
+    }
+}
+
+unsigned blocks_for(int64_t work) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 8));
+}
+
+}  // namespace
+
+cudaError_t TriSolver::prepare(const float2 *lu_, int64_t n_, const int *ipiv, cudaStream_t s) {
+    release();
+    lu = lu_;
+    n = n_;
+    nblk = (int)((n + B - 1) / B);
+    const size_t blocks = (size_t)nblk * B * B;
+    cudaError_t e;
+    if ((e = pool_alloc_n(&inv_lower, blocks, s)) || (e = pool_alloc_n(&inv_upper, blocks, s)) ||
+        (e = pool_alloc_n(&gather, (size_t)n, s)))
+        return e;
+    const int smem = B * B * (int)sizeof(float2);
+    if ((e = cudaFuncSetAttribute(k_tri_invert_lower, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+        (e = cudaFuncSetAttribute(k_tri_invert_upper, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
+        return e;
+    k_tri_invert_lower<<<nblk, B, smem, s>>>(lu, n, inv_lower);
+    k_tri_invert_upper<<<nblk, B, smem, s>>>(lu, n, inv_upper);
+    note_launches(2);
+    // the row interchanges (applied last to first) as one gather
+    std::vector<int> piv((size_t)n);
+    if ((e = cudaMemcpyAsync(piv.data(), ipiv, sizeof(int) * n, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+        return e;
+    std::vector<int32_t> idx((size_t)n);
+    for (int64_t i = 0; i < n; ++i) idx[i] = (int32_t)i;
+    for (int64_t i = n - 1; i >= 0; --i) {
+        const int64_t p = (int64_t)piv[i] - 1;
+        if (p < 0 || p >= n) return cudaErrorInvalidValue;
+        std::swap(idx[i], idx[p]);
+    }
+    if ((e = cudaMemcpyAsync(gather, idx.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaStreamSynchronize(s)))
+        return e;
+    return cudaGetLastError();
+}
+
+cudaError_t TriSolver::plan_for(int k, Plan **out) {
+    auto it = plans.find(k);
+    if (it != plans.end()) {
+        *out = &it->second;
+        return cudaSuccess;
+    }
+    Plan p;
+    p.kpad = (k + KC - 1) / KC * KC;
+    const size_t vec = (size_t)n * p.kpad;
+    cudaError_t e;
+    if ((e = pool_alloc_n(&p.b, vec, nullptr)) || (e = pool_alloc_n(&p.y, vec, nullptr)) ||
+        (e = pool_alloc_n(&p.z, vec, nullptr)) ||
+        (e = pool_alloc_n(&p.partial, (size_t)MAX_SPLITS * B * KC, nullptr)) ||
+        (e = pool_alloc_n(&p.sync, 4, nullptr)) || (e = cudaStreamSynchronize(nullptr))) {
+        for (float2 *q : {p.b, p.y, p.z, p.partial}) pool_free(q, nullptr);
+        pool_free(p.sync, nullptr);
+        return e;
+    }
+    auto res = plans.emplace(k, p);
+    *out = &res.first->second;
+    return cudaSuccess;
+}
+
+cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
+    if (!lu || k <= 0) return cudaErrorInvalidValue;
+    Plan *p = nullptr;
+    cudaError_t e = plan_for(k, &p);
+    if (e) return e;
+    if (grid <= 0) {
+        int device = 0, sms = 0, per_sm = 0, coop = 0;
+        if ((e = cudaGetDevice(&device)) ||
+            (e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device)) ||
+            (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) ||
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tri_sweeps, PANEL_THREADS, 0)))
+            return e;
+        if (!coop || per_sm < 1) return cudaErrorNotSupported;
+        grid = sms * per_sm;
+    }
+    k_tri_in<<<blocks_for(n * p->kpad), 256, 0, s>>>(n, k, p->kpad, in, p->b);
+    for (int c0 = 0; c0 < p->kpad; c0 += KC) {
+        if ((e = cudaMemsetAsync(p->sync, 0, 4 * sizeof(unsigned), s))) return e;
+        SweepArgs a{lu, n, nblk, inv_lower, inv_upper, p->b, p->y, p->z, p->kpad, c0, p->partial, p->sync,
+                    reinterpret_cast<int *>(p->sync + 2)};
+        void *args[] = {&a};
+        if ((e = cudaLaunchCooperativeKernel((const void *)k_tri_sweeps, dim3(grid), dim3(PANEL_THREADS), args, 0,
+                                             s)))
+            return e;
+    }
+    k_tri_out<<<blocks_for(n * k), 256, 0, s>>>(n, k, p->kpad, p->z, gather, out);
+    note_launches(2 + p->kpad / KC);
+    // a barrier that gave up leaves its status; the sweeps are then incomplete
+    int status = 0;
+    if ((e = cudaMemcpyAsync(&status, p->sync + 2, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+        return e;
+    if (status) return cudaErrorLaunchTimeout;
+    return cudaGetLastError();
+}
+
+void TriSolver::release() {
+    if (!plans.empty() || inv_lower) cudaDeviceSynchronize();
+    for (auto &kv : plans) {
+        Plan &p = kv.second;
+        for (float2 *q : {p.b, p.y, p.z, p.partial}) pool_free(q, nullptr);
+        pool_free(p.sync, nullptr);
+    }
+    plans.clear();
+    pool_free(inv_lower, nullptr);
+    pool_free(inv_upper, nullptr);
+    pool_free(gather, nullptr);
+    inv_lower = inv_upper = nullptr;
+    gather = nullptr;
+    lu = nullptr;
+}
+
+}  // namespace pq

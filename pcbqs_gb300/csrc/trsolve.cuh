@@ -1,0 +1,46 @@
+// Triangular solves with a complex64 LU factor (cuSOLVER getrf layout) for a few right-hand sides: one persistent
+// cooperative kernel per 8 columns streams the factor once, with grid barriers between its dependent steps.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+
+#include "solve.cuh"
+
+namespace pq {
+
+// The factor M = P L U of M = A^T (A the row-major system; M is its column-major view), as cuSOLVER getrf leaves
+// it, prepared for solving A x = b = U^T L^T P^T x: the diagonal TRI_BLOCK x TRI_BLOCK blocks of U^T (lower) and
+// L^T (unit upper) inverted once, and the row interchanges turned into one gather.
+constexpr int TRI_BLOCK = 128;     // super-block of rows solved at once
+constexpr int TRI_COLS = 8;        // right-hand sides per sweep over the factor
+
+struct TriSolver {
+    int64_t n = 0;
+    int nblk = 0;
+    const float2 *lu = nullptr;    // n x n, column-major (not owned)
+    float2 *inv_lower = nullptr;   // nblk blocks of TRI_BLOCK^2, row-major inverses of U^T's diagonal blocks
+    float2 *inv_upper = nullptr;   // the same for L^T
+    int32_t *gather = nullptr;     // x[j] = z[gather[j]]
+    // per right-hand-side count: work arrays, partial sums and the barrier words
+    struct Plan {
+        int kpad = 0;
+        float2 *b = nullptr, *y = nullptr, *z = nullptr, *partial = nullptr;
+        unsigned *sync = nullptr;     // [0] arrivals, [1] generation, [2] status
+    };
+    std::map<int, Plan> plans;
+    int grid = 0;                     // co-resident thread blocks of the sweep kernel
+
+    // ipiv: the factor's 1-based pivots on the device (getrf output); synchronizes `s`.
+    cudaError_t prepare(const float2 *lu, int64_t n, const int *ipiv, cudaStream_t s);
+    // out (n, k) complex128 row-major = A^-1 in, both device arrays.
+    cudaError_t solve(int k, const cd *in, cd *out, cudaStream_t s);
+    void release();
+    ~TriSolver() { release(); }
+
+  private:
+    cudaError_t plan_for(int k, Plan **out);
+};
+
+}  // namespace pq

@@ -389,8 +389,10 @@ class PeecModel(PeecTopology):
         vpart = np.zeros((B.shape[1], excitation.shape[1]), complex)
         if np.any(totals):
             if self._pinvb is None:
+                t0 = time.perf_counter()
                 self._pinvb = self._potential_solve(B.toarray())
                 self._component = np.asarray(B.T @ self._pinvb)
+                self.timings['potential_solve_s'] = time.perf_counter() - t0
             vpart = np.linalg.solve(self._component, -totals)
             qpart = self._pinvb @ vpart
         y0 = np.zeros((self.K.shape[1] - self.nl, excitation.shape[1]), complex)
@@ -430,14 +432,18 @@ class PeecModel(PeecTopology):
 
     FACTOR_MATH = {'fp32': 0, 'bf16x9': 1}
 
-    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='fp32'):
+    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='bf16x9', anchors=None):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
 
         precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
-        dense loop/tree system at each frequency), or 'none'. mixed=False: FP64 GMRES on the FP64 operator;
-        mixed=True: FP64 iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose
-        dense products run in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of
-        the 'lu32' factorization, 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy)."""
+        dense loop/tree system), or 'none'. mixed=False: FP64 GMRES on the FP64 operator; mixed=True: FP64
+        iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose dense products run
+        in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of the 'lu32'
+        factorization, 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy). anchors ('lu32'
+        only): how many factorizations a sweep shares; the frequencies, in increasing order, are split into that
+        many runs and every run is solved as one batch of (frequency, port) columns preconditioned by the factor
+        at its middle frequency (default: one factor per frequency). Every column still reaches the tolerance of
+        its own frequency's FP64 system; farther from the anchor it takes more iterations."""
         if self.L is None:
             self.assemble()
         f = np.atleast_1d(np.asarray(freqs, float))
@@ -447,8 +453,11 @@ class PeecModel(PeecTopology):
             raise ValueError(f'precondition must be one of {sorted(self.PRECONDITIONERS)}')
         if factor_math not in self.FACTOR_MATH:
             raise ValueError(f'factor_math must be one of {sorted(self.FACTOR_MATH)}')
-        if precondition == 'lu32' and len(f) > 1:
-            return self._stack([self.solve([fi], precondition, mixed, factor_math) for fi in f])
+        nf = len(f)
+        if anchors is None:
+            anchors = nf
+        if not isinstance(anchors, (int, np.integer)) or not 1 <= anchors <= nf:
+            raise ValueError('anchors must be an integer between 1 and the number of frequencies')
         mode = self.PRECONDITIONERS[precondition]
         t0 = time.perf_counter()
         npo = len(self.names)
@@ -458,40 +467,37 @@ class PeecModel(PeecTopology):
         omegas = 2 * np.pi * f
         handle, zscale = self._operator(omegas)
         self.timings.update(equilibrium_s=t1 - t0, operator_setup_s=time.perf_counter() - t1)
+        if mode == 2:
+            runs = np.array_split(np.argsort(f, kind='stable'), anchors)
+            groups = [(int(run[len(run) // 2]), run) for run in runs]
+        else:
+            groups = [(None, np.arange(nf))]
         lib = _lib.load()
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        timed = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        precondition_ms = gmres_ms = 0.0
+        outer_total = 0
         try:
-            ev_p0, ev_p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            ev_p0.record()
-            if mode == 1:
-                _lib.check(lib.pcbqs_gb300_peec_block_jacobi(handle, self.bs, self._krk_blocks().data_ptr(), stream),
-                           lib)
-            elif mode == 2:
-                desc = _csr_struct(self._krk_device())
-                _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, self.FACTOR_MATH[factor_math],
-                                                       stream), lib)
-            ev_p1.record()
-            torch.cuda.synchronize()
-            self.timings['precondition_ms'] = ev_p0.elapsed_time(ev_p1)
             # rhs = -K^T (R + j w L) baseline / zscale, per (frequency, port) column, in the clustered order.
             t_rhs = time.perf_counter()
             Lb = self._mv_L(baseline[:self.ne])
             Rb = self.R @ baseline[:self.ne]
             Kpt = self.Kp.T
-            cols, sys = [], []
-            for fi, w in enumerate(omegas):
-                v = Rb + 1j * w * Lb
-                cols.append(-(Kpt @ v) / zscale[fi])
-                sys += [fi] * npo
-            rhs = np.ascontiguousarray(np.concatenate(cols, axis=1))      # (n, nf * np)
+            cols = [-(Kpt @ (Rb + 1j * w * Lb)) / zscale[fi] for fi, w in enumerate(omegas)]
+            rhs = np.ascontiguousarray(np.concatenate(cols, axis=1))      # (n, nf * np), column fi * np + port
             self.timings['rhs_s'] = time.perf_counter() - t_rhs
-            b = torch.as_tensor(rhs, device=self.device)
-            x = torch.zeros_like(b)
-            k = rhs.shape[1]
-            sys = np.asarray(sys, np.int32)
-            its, res = np.zeros(k, np.int32), np.zeros(k)
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            ev0.record()
+            b_all = torch.as_tensor(rhs, device=self.device)
+            x_all = torch.zeros_like(b_all)
+            k_all = rhs.shape[1]
+            its, res = np.zeros(k_all, np.int32), np.zeros(k_all)
+            if mode == 1:
+                e0, e1 = timed()
+                e0.record()
+                _lib.check(lib.pcbqs_gb300_peec_block_jacobi(handle, self.bs, self._krk_blocks().data_ptr(), stream),
+                           lib)
+                e1.record()
+                torch.cuda.synchronize()
+                precondition_ms += e0.elapsed_time(e1)
             if mixed:
                 # single-precision copies of L and P for the inner products; FP64 outer residuals
                 Lf, Pf = self.Lf, self.Pf
@@ -504,24 +510,52 @@ class PeecModel(PeecTopology):
                                lib)
                 _lib.check(lib.pcbqs_gb300_peec_single(handle, Lf.data_ptr(), Lf.stride(0), Pf.data_ptr(),
                                                        Pf.stride(0)), lib)
-                outer = ctypes.c_int32()
-                status = lib.pcbqs_gb300_peec_solve_mixed(handle, k, _lib.ptr(sys, ctypes.c_int32), b.data_ptr(),
-                                                          x.data_ptr(), self.tol, self.inner_tol, 12, self.maxiter,
-                                                          self.restart, mode, _lib.ptr(its, ctypes.c_int32),
-                                                          _lib.ptr(res), ctypes.byref(outer), stream)
-                self.timings['outer_steps'] = int(outer.value)
-            else:
-                status = lib.pcbqs_gb300_peec_gmres(handle, k, _lib.ptr(sys, ctypes.c_int32), b.data_ptr(),
-                                                    x.data_ptr(), self.tol, self.maxiter, self.restart, mode,
-                                                    _lib.ptr(its, ctypes.c_int32), _lib.ptr(res), stream)
-            ev1.record()
-            torch.cuda.synchronize()
-            if status not in (0, 5):
-                _lib.check(status, lib)
-            self.timings['gmres_ms'] = ev0.elapsed_time(ev1)
-            self.timings['gmres_iterations'] = its.tolist()
-            converged = status == 0
-            X = x.cpu().numpy()
+            converged = True
+            for anchor, members in groups:
+                if mode == 2:
+                    e0, e1 = timed()
+                    e0.record()
+                    desc = _csr_struct(self._krk_device())
+                    _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), anchor,
+                                                           self.FACTOR_MATH[factor_math], stream), lib)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    precondition_ms += e0.elapsed_time(e1)
+                sel = (np.asarray(members)[:, None] * npo + np.arange(npo)).ravel()
+                whole = len(sel) == k_all
+                b = b_all if whole else b_all[:, torch.as_tensor(sel, device=self.device)].contiguous()
+                x = x_all if whole else torch.zeros_like(b)
+                k = len(sel)
+                sys = np.ascontiguousarray(np.repeat(np.asarray(members), npo), np.int32)
+                its_g, res_g = np.zeros(k, np.int32), np.zeros(k)
+                e0, e1 = timed()
+                e0.record()
+                if mixed:
+                    outer = ctypes.c_int32()
+                    status = lib.pcbqs_gb300_peec_solve_mixed(handle, k, _lib.ptr(sys, ctypes.c_int32), b.data_ptr(),
+                                                              x.data_ptr(), self.tol, self.inner_tol, 12,
+                                                              self.maxiter, self.restart, mode,
+                                                              _lib.ptr(its_g, ctypes.c_int32), _lib.ptr(res_g),
+                                                              ctypes.byref(outer), stream)
+                    outer_total = max(outer_total, int(outer.value))
+                else:
+                    status = lib.pcbqs_gb300_peec_gmres(handle, k, _lib.ptr(sys, ctypes.c_int32), b.data_ptr(),
+                                                        x.data_ptr(), self.tol, self.maxiter, self.restart, mode,
+                                                        _lib.ptr(its_g, ctypes.c_int32), _lib.ptr(res_g), stream)
+                e1.record()
+                torch.cuda.synchronize()
+                gmres_ms += e0.elapsed_time(e1)
+                if status not in (0, 5):
+                    _lib.check(status, lib)
+                converged = converged and status == 0
+                if not whole:
+                    x_all[:, torch.as_tensor(sel, device=self.device)] = x
+                its[sel], res[sel] = its_g, res_g
+            self.timings.update(precondition_ms=precondition_ms, gmres_ms=gmres_ms, gmres_iterations=its.tolist(),
+                                factorizations=len(groups) if mode == 2 else 0)
+            if mixed:
+                self.timings['outer_steps'] = outer_total
+            X = x_all.cpu().numpy()
         finally:
             lib.pcbqs_gb300_peec_destroy(handle)
         # back to the unclustered order, then currents, charges and source voltages (peec_iterative.py:331-341)
@@ -543,13 +577,3 @@ class PeecModel(PeecTopology):
         if not converged:
             raise RuntimeError(f'GMRES did not reach {self.tol:g}: residuals {res.max():.3g}, iterations {its.max()}')
         return PeecResult(f, self.names, Z, currents, its, res, dict(self.timings))
-
-    @staticmethod
-    def _stack(results):
-        first = results[0]
-        cat = lambda name: np.concatenate([getattr(r, name) for r in results])
-        timings = dict(first.timings)
-        for key in ('precondition_ms', 'gmres_ms', 'solve_s'):
-            timings[key] = sum(r.timings.get(key, 0) for r in results)
-        return PeecResult(cat('frequencies'), first.names, cat('impedance'), cat('currents'), cat('iterations'),
-                          cat('residual'), timings)

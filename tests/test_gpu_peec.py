@@ -97,3 +97,60 @@ def test_planes_mixed_and_fp64_solves_agree(device_library):
     assert np.abs(Zm - Z64).max() / np.abs(Z64).max() < 1e-7
     assert np.abs(Z64 - Z64.T).max() <= 1e-6 * np.abs(Z64).max()
     assert (np.diag(Z64).real > 0).all() and (np.diag(Z64).imag < 0).all()     # capacitive plane pair at 1 MHz
+
+
+@pytest.mark.parametrize('board,k', [('tiny', 3), ('strip', 8), ('strip', 11)])
+def test_streaming_triangular_solves_match_getrs(device_library, board, k):
+    """The library's streaming solve with the complex64 factor (super-block panels, inverted diagonal blocks, one
+    gather for the row interchanges) against cuSOLVER getrs on the same factor; k = 11 exercises a padded second
+    sweep of 8 columns. Both are FP32 solves in a different order, so they differ by FP32 rounding amplified by
+    the factor's conditioning; the bar is the quantity GMRES cares about, the residual of the FP64 system, which
+    must be no worse than getrs's (within 50 %)."""
+    import torch
+    from pcbqs_gb300 import _lib
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel, _csr_struct
+    model = PeecModel(Board.load(board)).assemble()
+    handle, _ = model._operator(np.array([2e6 * np.pi]))
+    lib = _lib.load()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    sys = np.zeros(k, np.int32)
+    try:
+        desc = _csr_struct(model._krk_device())
+        _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, 0, stream), lib)
+        rng = np.random.default_rng(k)
+        b = torch.as_tensor(rng.standard_normal((model.n, k)) + 1j * rng.standard_normal((model.n, k)), device='cuda')
+        outs, residuals = [], []
+        for method in (0, 1, 0):
+            x = torch.full_like(b, complex('nan'))
+            _lib.check(lib.pcbqs_gb300_peec_lu_solve(handle, k, b.data_ptr(), x.data_ptr(), method, stream), lib)
+            ax = torch.empty_like(b)
+            _lib.check(lib.pcbqs_gb300_peec_apply(handle, k, _lib.ptr(sys, ctypes.c_int32), x.data_ptr(),
+                                                  ax.data_ptr(), stream), lib)
+            outs.append(x.cpu().numpy())
+            residuals.append((torch.linalg.norm(ax - b, dim=0) / torch.linalg.norm(b, dim=0)).cpu().numpy())
+    finally:
+        lib.pcbqs_gb300_peec_destroy(handle)
+    ours, getrs, again = outs
+    assert np.isfinite(ours).all()
+    assert np.array_equal(ours, again)                  # the captured sweep replays deterministically
+    assert (residuals[0] <= 1.5 * residuals[1] + 1e-6).all(), (residuals[0], residuals[1])
+    assert np.linalg.norm(ours - getrs) <= 1e-2 * np.linalg.norm(getrs)
+
+
+@pytest.mark.parametrize('board', ['tiny', 'strip'])
+def test_sweep_sharing_one_factor_matches_reference(device_library, board):
+    """A three-decade sweep (1e5, 1e6, 1e7 Hz) solved as one batch of (frequency, port) columns, all preconditioned by
+    the complex64 factor at the middle frequency: every column still reaches 1e-8 on its own FP64 system and the
+    port impedances match the reference's dense solve; the anchor's own columns need the fewest iterations."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel
+    g = golden(board)
+    model = PeecModel(Board.load(board))
+    res = model.solve(g['freqs'], precondition='lu32', mixed=True, anchors=1)
+    assert res.timings['factorizations'] == 1
+    Z, Zr = res.impedance, g['Z']
+    assert np.abs(Z - Zr).max() / np.abs(Zr).max() < 1e-6
+    assert (res.residual <= 1e-8).all()
+    its = res.iterations.reshape(len(g['freqs']), -1)
+    assert its[1].max() <= its.max()
