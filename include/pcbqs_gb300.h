@@ -154,6 +154,29 @@ int pcbqs_gb300_hmatrix_apply(int64_t n, int64_t nblocks, const int64_t *meta, c
                               const int64_t *slots_of_row, int max_rank, int k, const double *x, double *y,
                               double *slots, void *stream);
 
+/* The PEEC loop basis on the host (src/pcbqs/mqs.py:48-130 spanning_tree, :592-637 _loops): branches k < nb
+ * between nodes ea[k], eb[k] (is_src: current-source branches, never in the tree); the first `first` branches
+ * (copper) form a breadth-first forest from each island's most central node, the other non-source branches only
+ * join islands. tree_out (nb) marks the forest; every other branch (except copper inside one node when
+ * ideal_terminals, and branches between islands) gets its fundamental cycle as COO entries (rows = branch,
+ * cols = cycle index, vals = +-1) and col_branch[cycle] = its branch. Status 1 with *nnz = the entries needed when
+ * capacity is short. No device work. */
+int pcbqs_gb300_loop_basis(int64_t n_nodes, int64_t nb, const int32_t *ea, const int32_t *eb, const uint8_t *is_src,
+                           int64_t first, int ideal_terminals, uint8_t *tree_out, int64_t capacity, int32_t *rows,
+                           int32_t *cols, double *vals, int64_t *nnz, int32_t *col_branch, int64_t *ncol);
+
+/* Layered-dielectric image sums (src/pcbqs/core/layered_kernels.hpp:38-120, layered_pairs) for every pair of
+ * triangles p = rows[i], q = cols[j] (same != 0: the pairs rows[i], rows[j] with j >= i of one layer; cols unused),
+ * written to both (p, q) and (q, p) of two FP64 planes, real and imaginary (ld >= triangles). Images: distances
+ * ascending with the zero-distance images first, complex coefficients (interleaved re, im); spline (optional,
+ * spline_m intervals, breaks x[0..m] from 0 to rho_max, coefficients [4][m] complex, highest power first) of the
+ * smooth positive images. near < 0: every pair analytic. All arrays on the device; synchronizes `stream`. */
+int pcbqs_gb300_layered_device(pcbqs_gb300_ctx *ctx, double near, int outer, const int32_t *rows, int64_t nrows,
+                               const int32_t *cols, int64_t ncols, int same, const double *image_dist,
+                               const double *image_coef, int nimages, const double *spline_x, const double *spline_c,
+                               int64_t spline_m, double rho_max, double *out_re, double *out_im, int64_t ld,
+                               void *stream);
+
 /* ---- Biot-Savart near field --------------------------------------------------------------------------------
  * H at npts points (pts (npts,3) device, m) of sheet currents given as nsrc quadrature points src (nsrc,4: x,y,z,0)
  * with current moments jx, jy (nsrc, k) complex128 (w J_x, w J_y), accumulated into H (npts, 3, k) complex128;

@@ -19,6 +19,7 @@ c_double_p = ctypes.POINTER(ctypes.c_double)
 c_int32_p = ctypes.POINTER(ctypes.c_int32)
 c_int64_p = ctypes.POINTER(ctypes.c_int64)
 c_uint64_p = ctypes.POINTER(ctypes.c_uint64)
+c_uint8_p = ctypes.POINTER(ctypes.c_uint8)
 c_void_p = ctypes.c_void_p
 
 
@@ -91,6 +92,13 @@ PROTOTYPES = {
     'pcbqs_gb300_hmatrix_apply': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, c_void_p, c_void_p, c_void_p,
                                                  c_void_p, c_void_p, c_void_p, ctypes.c_int, ctypes.c_int, c_void_p,
                                                  c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_loop_basis': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, c_int32_p, c_int32_p, c_uint8_p,
+                                              ctypes.c_int64, ctypes.c_int, c_uint8_p, ctypes.c_int64, c_int32_p,
+                                              c_int32_p, c_double_p, c_int64_p, c_int32_p, c_int64_p]),
+    'pcbqs_gb300_layered_device': (ctypes.c_int, [c_void_p, ctypes.c_double, ctypes.c_int, c_void_p, ctypes.c_int64,
+                                                  c_void_p, ctypes.c_int64, ctypes.c_int, c_void_p, c_void_p,
+                                                  ctypes.c_int, c_void_p, c_void_p, ctypes.c_int64, ctypes.c_double,
+                                                  c_void_p, c_void_p, ctypes.c_int64, c_void_p]),
     'pcbqs_gb300_biot_sheets': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
                                                c_void_p, ctypes.c_int, ctypes.c_int, c_void_p, c_void_p]),
     'pcbqs_gb300_biot_segments': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p, c_void_p,

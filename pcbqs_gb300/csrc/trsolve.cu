@@ -160,34 +160,69 @@ __device__ __forceinline__ void panel_block(const float2 *__restrict__ lu, int64
     __syncthreads();
 }
 
-// x[row0 + a][c0 + c] = sum_b inv[a][b] (rhs[row0 + b][c0 + c] - sum_s partial[s][b][c]) for rows a of quarter q
-// (32 rows; 256 threads = 32 rows x 8 columns). The 32 rows of the inverse are staged in shared memory with
-// coalesced loads, so the dot products never wait on a global load.
-__device__ __forceinline__ void diag_block(const float2 *__restrict__ inv, const float2 *partial, int runs,
-                                           const float2 *rhs, float2 *x, int64_t row0, int m, int kpad, int c0,
-                                           int q) {
-    __shared__ float2 acc[B][KC];
-    __shared__ float2 rows_s[32][B + 1];
-    for (int t = threadIdx.x; t < 32 * B; t += blockDim.x) {
-        const int a = t / B, b = t % B;
-        rows_s[a][b] = (32 * q + a < m && b < m) ? __ldg(inv + (int64_t)(32 * q + a) * B + b) : make_float2(0.f, 0.f);
+// The diagonal step for rows a of quarter q (32 rows; 256 threads = 32 rows x 8 columns):
+// x[row0 + a][c0 + c] = sum_b inv[a][b] (rhs[row0 + b][c0 + c] - sum_s partial[s][b][c]).
+// diag_stage loads the quarter's 32 rows of the inverse and the block's right-hand side into shared memory (while
+// the panel work of the same step is still running elsewhere: neither depends on it); diag_finish subtracts the
+// panel sums once they are complete and applies the inverse. All loads are issued before they are used.
+struct DiagSmem {
+    float2 acc[B][KC];
+    float2 rows[32][B + 1];
+};
+
+__device__ __forceinline__ void diag_stage(DiagSmem &sm, const float2 *__restrict__ inv, const float2 *rhs,
+                                           int64_t row0, int m, int kpad, int c0, int q) {
+    constexpr int ROW_LOADS = 32 * B / PANEL_THREADS, RHS_LOADS = B * KC / PANEL_THREADS;
+    float2 v[ROW_LOADS];
+#pragma unroll
+    for (int it = 0; it < ROW_LOADS; ++it) {
+        const int t = threadIdx.x + it * PANEL_THREADS, a = t / B, b = t % B;
+        v[it] = (32 * q + a < m && b < m) ? __ldg(inv + (int64_t)(32 * q + a) * B + b) : make_float2(0.f, 0.f);
     }
-    for (int t = threadIdx.x; t < B * KC; t += blockDim.x) {
-        const int b = t / KC, c = t % KC;
-        float2 v = make_float2(0.f, 0.f);
-        if (b < m) {
-            v = __ldcg(rhs + (row0 + b) * kpad + c0 + c);
-            float sx = 0.f, sy = 0.f;
-#pragma unroll 8
-            for (int s = 0; s < runs; ++s) {
-                const float2 p = __ldcg(partial + ((int64_t)s * B + b) * KC + c);
-                sx += p.x;
-                sy += p.y;
+    float2 r[RHS_LOADS];
+#pragma unroll
+    for (int it = 0; it < RHS_LOADS; ++it) {
+        const int t = threadIdx.x + it * PANEL_THREADS, b = t / KC, c = t % KC;
+        r[it] = b < m ? __ldcg(rhs + (row0 + b) * kpad + c0 + c) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int it = 0; it < ROW_LOADS; ++it) {
+        const int t = threadIdx.x + it * PANEL_THREADS;
+        sm.rows[t / B][t % B] = v[it];
+    }
+#pragma unroll
+    for (int it = 0; it < RHS_LOADS; ++it) {
+        const int t = threadIdx.x + it * PANEL_THREADS;
+        sm.acc[t / KC][t % KC] = r[it];
+    }
+}
+
+__device__ __forceinline__ void diag_finish(DiagSmem &sm, const float2 *partial, int runs, float2 *x, int64_t row0,
+                                            int m, int kpad, int c0, int q) {
+    constexpr int RHS_LOADS = B * KC / PANEL_THREADS;
+    if (runs > 0) {
+        float2 sum[RHS_LOADS];
+#pragma unroll
+        for (int it = 0; it < RHS_LOADS; ++it) sum[it] = make_float2(0.f, 0.f);
+        for (int s = 0; s < runs; ++s) {
+            float2 p[RHS_LOADS];
+#pragma unroll
+            for (int it = 0; it < RHS_LOADS; ++it) {
+                const int t = threadIdx.x + it * PANEL_THREADS, b = t / KC, c = t % KC;
+                p[it] = b < m ? __ldcg(partial + ((int64_t)s * B + b) * KC + c) : make_float2(0.f, 0.f);
             }
-            v.x -= sx;
-            v.y -= sy;
+#pragma unroll
+            for (int it = 0; it < RHS_LOADS; ++it) {
+                sum[it].x += p[it].x;
+                sum[it].y += p[it].y;
+            }
         }
-        acc[b][c] = v;
+#pragma unroll
+        for (int it = 0; it < RHS_LOADS; ++it) {
+            const int t = threadIdx.x + it * PANEL_THREADS;
+            sm.acc[t / KC][t % KC].x -= sum[it].x;
+            sm.acc[t / KC][t % KC].y -= sum[it].y;
+        }
     }
     __syncthreads();
     const int al = threadIdx.x / KC, c = threadIdx.x % KC, a = 32 * q + al;
@@ -195,7 +230,7 @@ __device__ __forceinline__ void diag_block(const float2 *__restrict__ inv, const
         float re = 0.f, im = 0.f;
 #pragma unroll 8
         for (int b = 0; b < B; ++b) {
-            const float2 t = rows_s[al][b], v = acc[b][c];
+            const float2 t = sm.rows[al][b], v = sm.acc[b][c];
             re += t.x * v.x - t.y * v.y;
             im += t.x * v.y + t.y * v.x;
         }
@@ -251,9 +286,16 @@ struct SweepArgs {
     int *status;
 };
 
-// Forward sweep b -> y with U^T, then backward sweep y -> z with L^T, for columns c0 .. c0 + 7.
+// Forward sweep b -> y with U^T, then backward sweep y -> z with L^T, for columns c0 .. c0 + 7. The first
+// DIAG_BLOCKS thread blocks own the diagonal steps (one quarter of the 128 rows each) and stage their inputs while
+// the others stream the panel.
+constexpr int DIAG_BLOCKS = B / 32;
+
 __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
+    __shared__ DiagSmem dsm;
     const int groups = (B + PANEL_ROWS - 1) / PANEL_ROWS;
+    const bool diag = blockIdx.x < DIAG_BLOCKS;
+    const int workers = (int)gridDim.x - DIAG_BLOCKS, me = (int)blockIdx.x - DIAG_BLOCKS;
     for (int dir = 0; dir < 2; ++dir) {
         const float2 *inv = dir == 0 ? a.inv_lower : a.inv_upper;
         const float2 *rhs = dir == 0 ? a.b : a.y;
@@ -266,18 +308,21 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
             const int64_t len = col1 - col0;
             int runs = 0;
             if (len > 0) {
-                runs = (int)(gridDim.x / groups);
+                runs = workers / groups;
                 runs = runs < 1 ? 1 : (runs > MAX_SPLITS ? MAX_SPLITS : runs);
                 const int64_t by_len = len / 512;
                 if (by_len < runs) runs = by_len < 1 ? 1 : (int)by_len;
+            }
+            if (diag) {
+                diag_stage(dsm, inv + (int64_t)J * B * B, rhs, row0, m, a.kpad, a.c0, blockIdx.x);
+            } else if (len > 0) {
                 const int mg = (m + PANEL_ROWS - 1) / PANEL_ROWS;
-                for (int item = blockIdx.x; item < mg * runs; item += gridDim.x)
+                for (int item = me; item < mg * runs; item += workers)
                     panel_block(a.lu, a.n, row0, m, col0, col1, x, a.kpad, a.c0, a.partial, item % mg, item / mg,
                                 runs);
-                if (!grid_barrier(a.barrier, a.barrier + 1, a.status)) return;
             }
-            for (int q = blockIdx.x; q < B / 32; q += gridDim.x)
-                diag_block(inv + (int64_t)J * B * B, a.partial, runs, rhs, x, row0, m, a.kpad, a.c0, q);
+            if (len > 0 && !grid_barrier(a.barrier, a.barrier + 1, a.status)) return;
+            if (diag) diag_finish(dsm, a.partial, runs, x, row0, m, a.kpad, a.c0, blockIdx.x);
             if (!grid_barrier(a.barrier, a.barrier + 1, a.status)) return;
         }
     }
@@ -378,7 +423,7 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
             (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) ||
             (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tri_sweeps, PANEL_THREADS, 0)))
             return e;
-        if (!coop || per_sm < 1) return cudaErrorNotSupported;
+        if (!coop || per_sm < 1 || sms * per_sm <= DIAG_BLOCKS) return cudaErrorNotSupported;
         grid = sms * per_sm;
     }
     k_tri_in<<<blocks_for(n * p->kpad), 256, 0, s>>>(n, k, p->kpad, in, p->b);
