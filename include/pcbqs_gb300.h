@@ -217,6 +217,9 @@ typedef struct pcbqs_gb300_peec_desc {
     double pscale;
     int32_t nsys;
     const double *omega, *zscale;
+    /* per system, the complex factor on R (interleaved re, im; null: 1): a finite-thickness sheet impedance
+     * Zs(f) sigma t, so R(f) = rscale R (src/pcbqs/mqs.py:517-530, conductor.py:12-26) */
+    const double *rscale;
 } pcbqs_gb300_peec_desc;
 
 typedef struct pcbqs_gb300_peec pcbqs_gb300_peec;

@@ -83,8 +83,8 @@ __global__ void k_tree_scale(int64_t n, int k, const int8_t *is_tree, const doub
 
 // V[e, s] = sum_f R[e, f] B[f, s] + j w_s LB[e, s] for copper rows e < ne; other passive rows (lumped parts with no
 // impedance here) are zero.
-__global__ void k_impedance(Csr R, int64_t nb, int k, const cd *B, const cd *LB, const double *omega, const int *sys,
-                            cd *V) {
+__global__ void k_impedance(Csr R, int64_t nb, int k, const cd *B, const cd *LB, const double *omega,
+                            const cd *rscale, const int *sys, cd *V) {
     const int64_t total = nb * k;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t e = t / k;
@@ -96,10 +96,12 @@ __global__ void k_impedance(Csr R, int64_t nb, int k, const cd *B, const cd *LB,
                 re += R.val[j] * b.x;
                 im += R.val[j] * b.y;
             }
+            const cd rs = rscale[sys[s]];
+            const double rr = re * rs.x - im * rs.y, ri = re * rs.y + im * rs.x;
             const double w = omega[sys[s]];
             const cd lb = LB[t];
-            re -= w * lb.y;
-            im += w * lb.x;
+            re = rr - w * lb.y;
+            im = ri + w * lb.x;
         }
         V[t] = make_double2(re, im);
     }
@@ -131,7 +133,7 @@ __global__ void k_block_gather(int64_t n, int bs, Csr St, const double *M, int64
 // are identity. Gauss-Jordan with partial pivoting on [A | I] in shared memory; one warp per matrix row group.
 __global__ void k_block_invert(int64_t n, int bs, int64_t nblk, const double *krk, const double *klk,
                                const double *tpt, const int8_t *is_tree, const double *omega, const double *zscale,
-                               double pscale, cd *inv, int *singular) {
+                               const cd *rscale, double pscale, cd *inv, int *singular) {
     extern __shared__ cd aug[];     // bs x 2bs
     const int64_t b = blockIdx.x;
     const int s = blockIdx.y;
@@ -145,7 +147,8 @@ __global__ void k_block_invert(int64_t n, int bs, int64_t nblk, const double *kr
             const int64_t ci = c0 + i, cj = c0 + j;
             if (ci < n && cj < n) {
                 const size_t at = (b * bs + i) * bs + j;
-                double re = krk[at] / zs, im = w * klk[at] / zs;
+                const cd rs = rscale[s];
+                double re = rs.x * krk[at] / zs, im = (rs.y * krk[at] + w * klk[at]) / zs;
                 if (is_tree[cj]) {       // column scaled by j w alpha
                     const double f = w * alpha;
                     const double r2 = -f * im, i2 = f * re;
@@ -359,6 +362,8 @@ struct PeecOp : Operator {
     double pscale = 1;
     int nsys = 0;
     double *omega = nullptr, *zscale = nullptr, *walpha = nullptr, *inv_z = nullptr, *inv_p = nullptr;
+    cd *rscale = nullptr;                 // per system factor on R (device)
+    std::vector<cd> rscale_host;
     int cap = 0;               // columns the scratch holds
     cd *u = nullptr, *branch = nullptr, *lb = nullptr, *v = nullptr, *tq = nullptr, *pq = nullptr;
     int64_t launches = 0;
@@ -396,7 +401,7 @@ struct PeecOp : Operator {
         k_tree_scale<<<grid_of(n_ * k), 256, 0, s>>>(n_, k, is_tree, walpha, sys, in, u);
         k_spmm<<<grid_of(nb * k), 256, 0, s>>>(K, k, u, branch, nullptr, sys, 0);
         if ((e = dense(single, ne, k, L, ldl, Lf, ldlf, branch, lb, s))) return e;
-        k_impedance<<<grid_of(nb * k), 256, 0, s>>>(R, nb, k, branch, lb, omega, sys, v);
+        k_impedance<<<grid_of(nb * k), 256, 0, s>>>(R, nb, k, branch, lb, omega, rscale, sys, v);
         k_spmm<<<grid_of(n_ * k), 256, 0, s>>>(Kt, k, v, out, inv_z, sys, 0);
         if (nn > 0) {
             k_spmm<<<grid_of(nn * k), 256, 0, s>>>(T, k, in, tq, nullptr, sys, 0);
@@ -415,6 +420,7 @@ struct PeecOp : Operator {
     ~PeecOp() override {
         for (cd *p : {u, branch, lb, v, tq, pq}) dev_free(p);
         for (double *p : {omega, zscale, walpha, inv_z, inv_p}) dev_free(p);
+        dev_free(rscale);
     }
 };
 
@@ -488,15 +494,20 @@ __global__ void k_assemble_c64(int64_t n, const double *klk, const double *tpt, 
 }
 
 // A[i, j] += KRK[i, j] d_j / zs for the sparse K^T R K.
-__global__ void k_add_krk_c64(Csr S, const int8_t *is_tree, double w, double zs, double ps, float2 *A) {
+__global__ void k_add_krk_c64(Csr S, const int8_t *is_tree, double w, double zs, double ps, cd rs, float2 *A) {
     const double f = w * zs / ps;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.rows; i += (int64_t)gridDim.x * blockDim.x)
         for (int64_t a = S.ptr[i]; a < S.ptr[i + 1]; ++a) {
             const int64_t j = S.idx[a];
             const double v = S.val[a] / zs;
             float2 &e = A[i * S.cols + j];
-            if (is_tree[j]) e.y += (float)(f * v);
-            else e.x += (float)v;
+            if (is_tree[j]) {           // times j f
+                e.x += (float)(-f * rs.y * v);
+                e.y += (float)(f * rs.x * v);
+            } else {
+                e.x += (float)(rs.x * v);
+                e.y += (float)(rs.y * v);
+            }
         }
 }
 
@@ -713,9 +724,12 @@ int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *d, pcbqs_gb300_peec **o
         iz[s] = 1.0 / z[s];
     }
     cudaError_t e;
+    op.rscale_host.assign(d->nsys, make_double2(1.0, 0.0));
+    if (d->rscale)
+        for (int s = 0; s < d->nsys; ++s) op.rscale_host[s] = make_double2(d->rscale[2 * s], d->rscale[2 * s + 1]);
     if ((e = dev_alloc(&op.omega, d->nsys)) || (e = dev_alloc(&op.zscale, d->nsys)) ||
         (e = dev_alloc(&op.walpha, d->nsys)) || (e = dev_alloc(&op.inv_z, d->nsys)) ||
-        (e = dev_alloc(&op.inv_p, d->nsys))) {
+        (e = dev_alloc(&op.inv_p, d->nsys)) || (e = dev_alloc(&op.rscale, d->nsys))) {
         delete h;
         return pfail(ERR_MEMORY, "peec_create: %s", cudaGetErrorString(e));
     }
@@ -724,6 +738,7 @@ int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *d, pcbqs_gb300_peec **o
     cudaMemcpy(op.walpha, wa.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
     cudaMemcpy(op.inv_z, iz.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
     cudaMemcpy(op.inv_p, ip.data(), sizeof(double) * d->nsys, cudaMemcpyHostToDevice);
+    cudaMemcpy(op.rscale, op.rscale_host.data(), sizeof(cd) * d->nsys, cudaMemcpyHostToDevice);
     *out = h;
     return OK;
 }
@@ -772,7 +787,7 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     const size_t smem = sizeof(cd) * bs * 2 * bs;
     cudaFuncSetAttribute(k_block_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_block_invert<<<grid, 256, smem, st>>>(op.n_, bs, nblk, krk, klk, tpt, op.is_tree, op.omega, op.zscale,
-                                             op.pscale, bj->inv, singular);
+                                             op.rscale, op.pscale, bj->inv, singular);
     note_launches(op.nn > 0 ? 3 : 2);
     int sing = 0;
     cudaMemcpyAsync(&sing, singular, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -843,7 +858,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     cudaMemcpy(&zs, op.zscale + sys, sizeof(double), cudaMemcpyDeviceToHost);
     Csr S = csr_of(*krk);
     k_assemble_c64<<<grid_of((int64_t)nn2), 256, 0, st>>>(n, h->klk, h->tpt, op.is_tree, w, zs, op.pscale, lu->lu);
-    k_add_krk_c64<<<grid_of(n), 256, 0, st>>>(S, op.is_tree, w, zs, op.pscale, lu->lu);
+    k_add_krk_c64<<<grid_of(n), 256, 0, st>>>(S, op.is_tree, w, zs, op.pscale, op.rscale_host[sys], lu->lu);
     note_launches(2);
     if (cusolverDnCreate(&lu->solver) != CUSOLVER_STATUS_SUCCESS) {
         delete lu;

@@ -239,35 +239,34 @@ __device__ __forceinline__ void diag_finish(DiagSmem &sm, const float2 *partial,
     __syncthreads();
 }
 
-// All thread blocks of the (cooperative, co-resident) grid meet here. Bounded: a block that waits past the limit
-// records TRI_TIMEOUT in *status and the caller returns, so no wait can hang the device.
+// All thread blocks of the (cooperative, co-resident) grid meet here: one arrival counter that only grows, barrier
+// number `index` complete when it reaches (index + 1) x blocks; thread 0 arrives with release semantics (covering its
+// block's writes through the preceding __syncthreads) and polls with acquire loads. Bounded: after about a second
+// of polling (clock64) the block records TRI_TIMEOUT in *status and returns false, as do blocks that see the status.
 constexpr int TRI_TIMEOUT = 1;
 
-__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *generation, int *status) {
+__device__ __forceinline__ unsigned load_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned index, int *status) {
     __shared__ int ok;
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         ok = 1;
-        volatile unsigned *gen = generation;
-        const unsigned g = *gen;
         __threadfence();
-        if (atomicAdd(count, 1u) == gridDim.x - 1) {
-            atomicExch(count, 0u);
-            __threadfence();
-            atomicAdd(generation, 1u);
-        } else {
-            long long spins = 0;
-            while (*gen == g) {
-                if (++spins > (1ll << 24) || *(volatile int *)status) {
-                    atomicExch(status, TRI_TIMEOUT);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
+        atomicAdd(count, 1u);
+        const unsigned target = (index + 1) * gridDim.x;
+        const long long start = clock64();
+        while (load_acquire(count) < target) {
+            if (clock64() - start > (2ll << 30) || *(volatile int *)status) {
+                atomicExch(status, TRI_TIMEOUT);
+                ok = 0;
+                break;
             }
         }
-        __threadfence();
     }
     __syncthreads();
     return ok;
@@ -282,7 +281,7 @@ struct SweepArgs {
     float2 *y, *z;
     int kpad, c0;
     float2 *partial;
-    unsigned *barrier;     // [0] arrivals, [1] generation
+    unsigned *barrier;     // [0] arrivals (grows by one per block and barrier)
     int *status;
 };
 
@@ -296,6 +295,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
     const int groups = (B + PANEL_ROWS - 1) / PANEL_ROWS;
     const bool diag = blockIdx.x < DIAG_BLOCKS;
     const int workers = (int)gridDim.x - DIAG_BLOCKS, me = (int)blockIdx.x - DIAG_BLOCKS;
+    unsigned barriers = 0;
     for (int dir = 0; dir < 2; ++dir) {
         const float2 *inv = dir == 0 ? a.inv_lower : a.inv_upper;
         const float2 *rhs = dir == 0 ? a.b : a.y;
@@ -321,9 +321,9 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
                     panel_block(a.lu, a.n, row0, m, col0, col1, x, a.kpad, a.c0, a.partial, item % mg, item / mg,
                                 runs);
             }
-            if (len > 0 && !grid_barrier(a.barrier, a.barrier + 1, a.status)) return;
+            if (len > 0 && !grid_barrier(a.barrier, barriers++, a.status)) return;
             if (diag) diag_finish(dsm, a.partial, runs, x, row0, m, a.kpad, a.c0, blockIdx.x);
-            if (!grid_barrier(a.barrier, a.barrier + 1, a.status)) return;
+            if (!grid_barrier(a.barrier, barriers++, a.status)) return;
         }
     }
 }

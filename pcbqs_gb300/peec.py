@@ -12,6 +12,7 @@ Host bookkeeping (sparse topology) restates the reference:
 Device work (C ABI): the fill of L and P, the operator products, the block-Jacobi blocks and their inverses, and
 the batched GMRES; P^-1 B for the equilibrium split by the dense GMRES.
 """
+import concurrent.futures
 import ctypes
 import time
 
@@ -22,7 +23,7 @@ from scipy.sparse.csgraph import connected_components
 from scipy.sparse.linalg import splu
 
 from . import _lib
-from .fill import DeviceFill, EPS0
+from .fill import MU0, DeviceFill, EPS0
 from .geometry import BAR3, W3
 
 
@@ -203,8 +204,11 @@ class PeecModel(PeecTopology):
     first to its second terminal (MQS.source), solved on the device."""
 
     def __init__(self, board, near=3.0, outer_levels=1, device=0, block_size=32, tol=1e-8, maxiter=2000,
-                 restart=100, log=None, inner_tol=1e-4):
+                 restart=100, log=None, inner_tol=1e-4, conductor_loss='dc', conductor_faces=2):
+        if conductor_loss not in ('dc', 'slab') or conductor_faces not in (1, 2):
+            raise ValueError('conductor_loss must be dc or slab; conductor_faces must be 1 or 2')
         self.tol, self.maxiter, self.restart, self.inner_tol = tol, maxiter, restart, inner_tol
+        self.conductor_loss, self.conductor_faces = conductor_loss, conductor_faces
         self.device = torch.device('cuda', device)
         self.timings = {}
         t0 = time.perf_counter()
@@ -253,8 +257,9 @@ class PeecModel(PeecTopology):
     def _operator(self, omegas):
         dev = self.device
         R = self.R
-        zscale = np.array([max(float(np.max(np.abs(R.diagonal() + 1j * w * self.ldiag))), np.finfo(float).tiny)
-                           for w in omegas])
+        ratio = self.resistance_ratio(omegas / (2 * np.pi))
+        zscale = np.array([max(float(np.max(np.abs(ratio[i] * R.diagonal() + 1j * w * self.ldiag))),
+                               np.finfo(float).tiny) for i, w in enumerate(omegas)])
         if getattr(self, '_dev', None) is None:      # the topology's sparse matrices, uploaded once per model
             self._dev = dict(K=_dev_csr(self.Kp, dev), Kt=_dev_csr(self.Kp.T, dev), T=_dev_csr(self.Tp, dev),
                              Tt=_dev_csr(self.Tp.T, dev), R=_dev_csr(R, dev),
@@ -270,6 +275,8 @@ class PeecModel(PeecTopology):
         self._omega = np.ascontiguousarray(omegas, float)
         self._zscale = np.ascontiguousarray(zscale, float)
         d.omega, d.zscale = _lib.ptr(self._omega), _lib.ptr(self._zscale)
+        self._rscale = np.ascontiguousarray(np.c_[ratio.real, ratio.imag].ravel())
+        d.rscale = _lib.ptr(self._rscale)
         lib = _lib.load()
         handle = ctypes.c_void_p()
         _lib.check(lib.pcbqs_gb300_peec_create(ctypes.byref(d), ctypes.byref(handle)), lib)
@@ -335,6 +342,42 @@ class PeecModel(PeecTopology):
 
     PRECONDITIONERS = {'none': 0, 'block_jacobi': 1, 'lu32': 2}
 
+    def resistance_ratio(self, freqs):
+        """R(f) / R_dc per frequency: 1 for conductor_loss='dc'; for 'slab' the finite-thickness sheet impedance
+        Zs(f) sigma t of the copper (current entering from one or both faces), so R(f) = ratio R_dc for the
+        single-sheet model (MQS._resistance_delta, src/pcbqs/mqs.py:517-530; surface_impedance,
+        src/pcbqs/conductor.py:12-26)."""
+        f = np.atleast_1d(np.asarray(freqs, float))
+        if self.conductor_loss == 'dc':
+            return np.ones(len(f), complex)
+        sigma, t = float(self.board.sigma), float(self.board.thickness)
+        u = np.sqrt(2j * np.pi * f * MU0 * sigma) * t / self.conductor_faces
+        small = np.abs(u) < 1e-3
+        safe = np.where(small, 1.0, u)
+        return np.where(small, 1 + u * u / 3 - u ** 4 / 45, safe / np.tanh(safe)).astype(complex)
+
+    def _factor_async(self, handle, sys_index, math):
+        """Start pcbqs_gb300_peec_factor for system `sys_index` on a side stream from a helper thread; the returned
+        future yields its device time (ms) or raises its error. L, P and the handle's operator must be complete."""
+        lib = _lib.load()
+        if getattr(self, '_side', None) is None:
+            self._side = torch.cuda.Stream(self.device)
+            self._pool = concurrent.futures.ThreadPoolExecutor(max_workers=1, thread_name_prefix='pcbqs-factor')
+        side = self._side
+        desc = _csr_struct(self._krk_device())
+        torch.cuda.current_stream(self.device).synchronize()
+
+        def work():
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(side)
+            status = lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), sys_index, math,
+                                                 ctypes.c_void_p(side.cuda_stream))
+            e1.record(side)
+            side.synchronize()
+            _lib.check(status, lib)
+            return e0.elapsed_time(e1)
+        return self._pool.submit(work)
+
     FACTOR_MATH = {'fp32': 0, 'bf16x9': 1}
 
     def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='bf16x9', anchors=None):
@@ -367,11 +410,8 @@ class PeecModel(PeecTopology):
         t0 = time.perf_counter()
         npo = len(self.names)
         excitation = np.eye(npo, dtype=complex)
-        baseline, qpart, vpart, source_voltage = self._equilibrium(excitation)
-        t1 = time.perf_counter()
         omegas = 2 * np.pi * f
         handle, zscale = self._operator(omegas)
-        self.timings.update(equilibrium_s=t1 - t0, operator_setup_s=time.perf_counter() - t1)
         if mode == 2:
             runs = np.array_split(np.argsort(f, kind='stable'), anchors)
             groups = [(int(run[len(run) // 2]), run) for run in runs]
@@ -382,15 +422,25 @@ class PeecModel(PeecTopology):
         timed = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         precondition_ms = gmres_ms = 0.0
         outer_total = 0
+        factored = None
         try:
+            if mode == 2:
+                # the first complex64 factorization depends only on L, P and the frequency: it runs on a side
+                # stream from a helper thread while this thread computes the equilibrium charge and the right-hand
+                # sides (the ctypes call releases the interpreter lock)
+                factored = self._factor_async(handle, groups[0][0], self.FACTOR_MATH[factor_math])
+            t1 = time.perf_counter()
+            baseline, qpart, vpart, source_voltage = self._equilibrium(excitation)
+            t2 = time.perf_counter()
+            self.timings.update(equilibrium_s=t2 - t1, operator_setup_s=t1 - t0)
             # rhs = -K^T (R + j w L) baseline / zscale, per (frequency, port) column, in the clustered order.
-            t_rhs = time.perf_counter()
             Lb = self._mv_L(baseline[:self.ne])
             Rb = self.R @ baseline[:self.ne]
             Kpt = self.Kp.T
-            cols = [-(Kpt @ (Rb + 1j * w * Lb)) / zscale[fi] for fi, w in enumerate(omegas)]
+            ratio = self.resistance_ratio(f)
+            cols = [-(Kpt @ (ratio[fi] * Rb + 1j * w * Lb)) / zscale[fi] for fi, w in enumerate(omegas)]
             rhs = np.ascontiguousarray(np.concatenate(cols, axis=1))      # (n, nf * np), column fi * np + port
-            self.timings['rhs_s'] = time.perf_counter() - t_rhs
+            self.timings['rhs_s'] = time.perf_counter() - t2
             b_all = torch.as_tensor(rhs, device=self.device)
             x_all = torch.zeros_like(b_all)
             k_all = rhs.shape[1]
@@ -413,11 +463,15 @@ class PeecModel(PeecTopology):
                                lib)
                     _lib.check(lib.pcbqs_gb300_to_single(self.P.data_ptr(), Pf.data_ptr(), self.P.numel(), stream),
                                lib)
+            if factored is not None:
+                precondition_ms += factored.result()
+                factored = None
+            if mixed:
                 _lib.check(lib.pcbqs_gb300_peec_single(handle, Lf.data_ptr(), Lf.stride(0), Pf.data_ptr(),
                                                        Pf.stride(0)), lib)
             converged = True
-            for anchor, members in groups:
-                if mode == 2:
+            for g, (anchor, members) in enumerate(groups):
+                if mode == 2 and g > 0:
                     e0, e1 = timed()
                     e0.record()
                     desc = _csr_struct(self._krk_device())
@@ -462,6 +516,11 @@ class PeecModel(PeecTopology):
                 self.timings['outer_steps'] = outer_total
             X = x_all.cpu().numpy()
         finally:
+            if factored is not None:        # an error above: let the factorization finish before the handle goes
+                try:
+                    factored.result()
+                except Exception:  # noqa: BLE001 -- the first error is the one raised
+                    pass
             lib.pcbqs_gb300_peec_destroy(handle)
         # back to the unclustered order, then currents, charges and source voltages (peec_iterative.py:331-341)
         Xo = np.empty_like(X)

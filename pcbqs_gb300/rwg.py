@@ -16,15 +16,25 @@ class RWG:
         if not (self.area > 0).all():
             raise ValueError('triangles must be counter-clockwise')
         self.cent = V.mean(1)
-        # Edges keyed by their sorted end nodes, in first-seen order (a dict keeps insertion order).
-        seen = {}
-        for t, (a, b, c) in enumerate(self.tris.tolist()):
-            for i, (u, v) in enumerate(((a, b), (b, c), (c, a))):
-                seen.setdefault((u, v) if u < v else (v, u), []).append((t, i))
-        interior = [(k, s) for k, s in seen.items() if len(s) == 2]
-        self.Ne = len(interior)
-        u, v = np.array([k for k, _ in interior], np.int64).reshape(-1, 2).T
-        (t1, i1), (t2, i2) = np.array([s for _, s in interior], np.int64).reshape(-1, 2, 2).transpose(1, 2, 0)
+        # Edges keyed by their sorted end nodes, in first-seen order (triangle-major, edge (a,b), (b,c), (c,a)), each
+        # with its occurrences in that order: a stable sort by key groups the occurrences of one edge in sequence;
+        # the interior edges are the keys met exactly twice, ordered by their first occurrence.
+        tri = self.tris.astype(np.int64)
+        ends = np.stack([tri, np.roll(tri, -1, axis=1)], axis=2).reshape(-1, 2)      # (3 nt, 2): edge i of t
+        lo, hi = ends.min(1), ends.max(1)
+        key = lo * (int(hi.max()) + 1) + hi
+        order = np.argsort(key, kind='stable')
+        sk = key[order]
+        start = np.flatnonzero(np.r_[True, sk[1:] != sk[:-1]])
+        count = np.diff(np.r_[start, len(sk)])
+        keep = start[count == 2]
+        first, second = order[keep], order[keep + 1]
+        seq = np.argsort(first, kind='stable')
+        first, second = first[seq], second[seq]
+        self.Ne = len(first)
+        u, v = lo[first], hi[first]
+        t1, i1 = first // 3, first % 3
+        t2, i2 = second // 3, second % 3
         self.tp, self.tm = t1, t2
         self.vp = nodes[self.tris[t1, (i1 + 2) % 3]]
         self.vm = nodes[self.tris[t2, (i2 + 2) % 3]]

@@ -42,7 +42,7 @@ def stub_shapely():
     sys.modules['shapely'] = root
 
 
-def reference_model(board):
+def reference_model(board, conductor_loss='dc'):
     from oracle.reference import load_reference
     stub_shapely()
     load_reference()
@@ -57,7 +57,7 @@ def reference_model(board):
     q.nodes, q.tris = board.nodes, board.tris
     q.z_of, q.t_of = board.z, np.full(board.nt, board.thickness)
     q.layer_of = board.layer
-    q.sigma, q.conductor_loss, q.conductor_faces, q.thickness_sheets = board.sigma, 'dc', 2, 1
+    q.sigma, q.conductor_loss, q.conductor_faces, q.thickness_sheets = board.sigma, conductor_loss, 2, 1
     q.layer_tris = {int(l): np.flatnonzero(board.layer == l) for l in np.unique(board.layer)}
     q.sheet_layer = {k: k for k in q.layer_tris}
     q.rwg = RWG(q.nodes, q.tris)
@@ -91,17 +91,22 @@ def port_matrix(q, board, freqs):
     return names, Z, diag
 
 
-def main(boards=('tiny', 'strip')):
+def main(boards=('tiny', 'strip'), losses=('dc', 'slab')):
+    """peec_<board>.npz: DC sheet resistance; peec_<board>_slab.npz: conductor_loss='slab' (finite-thickness sheet
+    impedance, current from both faces, one sheet per layer), where R depends on frequency."""
     from pcbqs_gb300.board import Board
     freqs = np.array([1e5, 1e6, 1e7])
     for name in boards:
+      for loss in losses:
         b = Board.load(name)
-        q = reference_model(b)
+        q = reference_model(b, loss)
         names, Z, diag = port_matrix(q, b, freqs)
         assert np.allclose(np.diagonal(Z, axis1=1, axis2=2), diag, rtol=1e-9), 'port voltage convention'
         m = q._peec
-        np.savez_compressed(HERE / f'peec_{name}.npz', freqs=freqs, ports=np.array(names), Z=Z, z_diag=diag,
-                            unknowns=m['K'].shape[1], loops=m['nl'], components=m['B'].shape[1])
+        suffix = '' if loss == 'dc' else '_' + loss
+        np.savez_compressed(HERE / f'peec_{name}{suffix}.npz', freqs=freqs, ports=np.array(names), Z=Z, z_diag=diag,
+                            unknowns=m['K'].shape[1], loops=m['nl'], components=m['B'].shape[1],
+                            conductor_loss=loss)
         print(name, 'unknowns', m['K'].shape[1], 'loops', m['nl'], 'components', m['B'].shape[1])
         print(np.round(Z[1], 6))
 

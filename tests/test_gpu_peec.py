@@ -156,3 +156,23 @@ def test_sweep_sharing_one_factor_matches_reference(device_library, board):
     assert (res.residual <= 1e-8).all()
     its = res.iterations.reshape(len(g['freqs']), -1)
     assert its[1].max() <= its.max()
+
+
+@pytest.mark.parametrize('board', ['tiny', 'strip'])
+@pytest.mark.parametrize('mixed', [False, True])
+def test_slab_conductor_loss_matches_reference(device_library, board, mixed):
+    """conductor_loss='slab': R(f) = Zs(f) sigma t R_dc per frequency (finite-thickness sheet impedance) in the
+    operator, the factor and the right-hand side; port impedances against the reference's dense solve with the same
+    loss model, and the resistive part against itself."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel
+    g = golden(f'{board}_slab')
+    assert str(g['conductor_loss']) == 'slab'
+    model = PeecModel(Board.load(board), conductor_loss='slab')
+    res = model.solve(g['freqs'], precondition='lu32', mixed=mixed)
+    Z, Zr = res.impedance, g['Z']
+    assert np.abs(Z - Zr).max() / np.abs(Zr).max() < 1e-6
+    assert np.abs(Z.real - Zr.real).max() <= 1e-4 * np.abs(Zr.real).max() + 1e-9 * np.abs(Zr).max()
+    assert (res.residual <= 1e-8).all()
+    ratio = model.resistance_ratio(g['freqs'])
+    assert ratio.real[-1] > ratio.real[0] >= 1.0         # skin effect raises the resistance with frequency
