@@ -189,6 +189,15 @@ int pcbqs_gb300_biot_sheets(int64_t npts, const double *pts, int64_t nsrc, const
 int pcbqs_gb300_biot_segments(int64_t npts, const double *pts, int64_t nseg, const double *p0, const double *p1,
                               const double *I, int k, double *H, void *stream);
 
+/* Cloud-in-cell deposit of sheet-current moments onto a uniform grid (src/pcbqs/_numerics/currents.py:28-61,
+ * current_deposit): point t at (qx[t], qy[t]) with complex moments mom_x, mom_y (npts, k, interleaved re, im) adds
+ * its bilinear shares to jx, jy (nx, ny, k complex, row-major over x then y) at grid x0 + i dx, y0 + j dy; points
+ * outside drop the shares that fall off the grid. Device arrays; the caller zeroes the grids and divides by the
+ * cell area. Asynchronous on `stream`. */
+int pcbqs_gb300_current_deposit(int64_t npts, const double *qx, const double *qy, const double *mom_x,
+                                const double *mom_y, int k, double x0, double y0, double dx, double dy, int64_t nx,
+                                int64_t ny, double *jx, double *jy, void *stream);
+
 /* ---- Solve: the PEEC operator in loop/tree coordinates and batched GMRES ------------------------------------
  * Complex vectors of k systems are (n, k) row-major complex128 (interleaved re, im) device arrays. */
 
@@ -254,6 +263,11 @@ int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *op, int k, const double *in, dou
 int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *op, int k, const int32_t *sys, const double *b, double *x, double tol,
                            int maxiter, int restart, int precondition, int32_t *iterations, double *residual,
                            void *stream);
+/* Y = M X for a dense symmetric real M (rows x rows, leading dimension ld, FP64) and complex128 X, Y (rows x k,
+ * row-major), device arrays, in FP64 (the products of the loop/tree right-hand side and the charge correction,
+ * src/pcbqs/peec_iterative.py:253-256, 331-341). Asynchronous on `stream`. */
+int pcbqs_gb300_dense_apply(int64_t rows, int k, const double *M, int64_t ld, const double *X, double *Y,
+                            void *stream);
 /* Single-precision copies of L and P (device, row strides ldlf/ldpf) for the inner products of the mixed solve,
  * and the conversion that makes them. */
 int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *stream);

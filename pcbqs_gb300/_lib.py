@@ -103,6 +103,10 @@ PROTOTYPES = {
                                                c_void_p, ctypes.c_int, ctypes.c_int, c_void_p, c_void_p]),
     'pcbqs_gb300_biot_segments': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
                                                  c_void_p, ctypes.c_int, c_void_p, c_void_p]),
+    'pcbqs_gb300_current_deposit': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                   ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_int64, ctypes.c_int64, c_void_p,
+                                                   c_void_p, c_void_p]),
     'pcbqs_gb300_peec_create': (ctypes.c_int, [ctypes.POINTER(PeecDesc), ctypes.POINTER(c_void_p)]),
     'pcbqs_gb300_peec_destroy': (None, [c_void_p]),
     'pcbqs_gb300_peec_apply': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p, c_void_p]),
@@ -111,6 +115,8 @@ PROTOTYPES = {
                                                c_void_p]),
     'pcbqs_gb300_peec_lu_solve': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p, c_void_p, ctypes.c_int,
                                                  c_void_p]),
+    'pcbqs_gb300_dense_apply': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64, c_void_p,
+                                               c_void_p, c_void_p]),
     'pcbqs_gb300_to_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p]),
     'pcbqs_gb300_peec_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, ctypes.c_int64]),
     'pcbqs_gb300_peec_solve_mixed': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p,

@@ -111,3 +111,103 @@ def h_segments(p0, p1, I, pts, device=0):
                                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
     out = H.cpu().numpy()
     return out if multi else out[:, :, 0]
+
+
+# ---- the FFT near field on a uniform grid (src/pcbqs/biot.py:108-181, h_grid) ------------------------------------
+
+def current_grid(rwg, I, idx, gx, gy, per_cell=2.0, device=0):
+    """Surface current density of the triangles `idx` on the uniform grid gx, gy (m): (jx, jy) (nx, ny, k) complex
+    A/m on the device, for RWG amplitudes I (ne, k). Triangles larger than `per_cell` cells are split into four
+    until they are not (at most 6 rounds), each integrated by the 6-point rule, each point's current moment spread
+    onto its four grid points (cloud in cell, pcbqs_gb300_current_deposit). Restates current_deposit
+    (src/pcbqs/_numerics/currents.py:28-61) for k excitations at once."""
+    a, b = rwg_currents(rwg, I)
+    V, aa, bb = rwg.nodes[rwg.tris[idx]][:, :, :2], a[idx], b[idx]
+    dx, dy = gx[1] - gx[0], gy[1] - gy[0]
+    area2 = lambda T: (T[:, 1, 0] - T[:, 0, 0]) * (T[:, 2, 1] - T[:, 0, 1]) - \
+        (T[:, 1, 1] - T[:, 0, 1]) * (T[:, 2, 0] - T[:, 0, 0])
+    for _ in range(6):
+        big = np.sqrt(np.abs(area2(V)) / 2) > per_cell * min(dx, dy)
+        if not big.any():
+            break
+        V = np.concatenate([V[~big], split4(V[big])])
+        aa = np.concatenate([aa[~big], np.tile(aa[big], (4, 1))])
+        bb = np.concatenate([bb[~big], np.tile(bb[big], (4, 1, 1))])
+    area = 0.5 * np.abs(area2(V))
+    Q = np.einsum('qk,tkc->tqc', BAR6, V)                                        # (M, 6, 2)
+    w = (area[:, None] * W6[None])[..., None]                                     # (M, 6, 1)
+    mx = ((aa[:, None, :] * Q[..., 0:1] + bb[:, None, 0, :]) * w).reshape(-1, aa.shape[1])
+    my = ((aa[:, None, :] * Q[..., 1:2] + bb[:, None, 1, :]) * w).reshape(-1, aa.shape[1])
+    dev = torch.device('cuda', device)
+    t = lambda arr: torch.as_tensor(np.ascontiguousarray(arr), device=dev)
+    qx, qy, mx_d, my_d = t(Q[..., 0].reshape(-1)), t(Q[..., 1].reshape(-1)), t(mx), t(my)
+    k = aa.shape[1]
+    jx = torch.zeros((len(gx), len(gy), k), dtype=torch.complex128, device=dev)
+    jy = torch.zeros_like(jx)
+    lib = _lib.load()
+    _lib.check(lib.pcbqs_gb300_current_deposit(len(qx), qx.data_ptr(), qy.data_ptr(), mx_d.data_ptr(),
+                                               my_d.data_ptr(), k, float(gx[0]), float(gy[0]), float(dx), float(dy),
+                                               len(gx), len(gy), jx.data_ptr(), jy.data_ptr(),
+                                               ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)), lib)
+    return jx / (dx * dy), jy / (dx * dy)
+
+
+def h_grid(rwg, layer_tris, z_of, I, x, y, heights, refine=1, filaments=None, device=0):
+    """Open-boundary H (nx, ny, nh, 3) complex, or (nx, ny, nh, 3, k) for I (ne, k), on the uniform grids x, y (m) at
+    absolute heights (m), from the RWG amplitudes I of the sheets `layer_tris` {layer: triangle indices} at z_of;
+    `filaments` (p0, p1, currents) are added analytically. Each sheet's current is deposited on a source grid that
+    covers all copper and the window (spacing / refine), and convolved with the magnetostatic kernel by zero-padded
+    FFTs on the device (linear, not periodic, convolution). Restates h_grid (src/pcbqs/biot.py:108-181)."""
+    from scipy.fft import next_fast_len
+    x, y, heights = [np.asarray(v, float) for v in (x, y, np.atleast_1d(heights))]
+    for axis in (x, y):
+        if (axis.ndim != 1 or len(axis) < 2 or not np.isfinite(axis).all() or np.diff(axis).min() <= 0
+                or not np.allclose(np.diff(axis), axis[1] - axis[0], rtol=1e-8, atol=1e-15)):
+            raise ValueError('x and y must be increasing uniform grids (m)')
+    if heights.ndim != 1 or not np.isfinite(heights).all():
+        raise ValueError('heights must be finite absolute z coordinates (m)')
+    if np.any(np.isclose(heights[:, None], np.unique(z_of)[None], rtol=0, atol=1e-15)):
+        raise ValueError('FFT H must be evaluated away from copper planes')
+    if not isinstance(refine, (int, np.integer)) or refine < 1:
+        raise ValueError('refine must be a positive integer')
+    I = np.asarray(I)
+    multi = I.ndim > 1
+    I2 = I if multi else I[:, None]
+    nodes = rwg.nodes
+    dx, dy = (x[1] - x[0]) / refine, (y[1] - y[0]) / refine
+    grids, offsets = [], []
+    for dim, axis, step in ((0, x, dx), (1, y, dy)):
+        lo = min(0, int(np.floor((nodes[:, dim].min() - axis[0]) / step)) - 2)
+        hi = max(refine * (len(axis) - 1), int(np.ceil((nodes[:, dim].max() - axis[0]) / step)) + 2)
+        grids.append(axis[0] + np.arange(lo, hi + 1) * step)
+        offsets.append(-lo)
+    gx, gy = grids
+    nx, ny = len(gx), len(gy)
+    shape = (next_fast_len(3 * nx - 2), next_fast_len(3 * ny - 2))
+    dev = torch.device('cuda', device)
+    rx = torch.arange(1 - nx, nx, device=dev, dtype=torch.float64)[:, None] * dx
+    ry = torch.arange(1 - ny, ny, device=dev, dtype=torch.float64)[None, :] * dy
+    k = I2.shape[1]
+    out = torch.zeros((len(x), len(y), len(heights), 3, k), dtype=torch.complex128, device=dev)
+    cx = slice(nx - 1 + offsets[0], nx - 1 + offsets[0] + refine * len(x), refine)
+    cy = slice(ny - 1 + offsets[1], ny - 1 + offsets[1] + refine * len(y), refine)
+    fft2 = lambda v: torch.fft.fft2(v, s=shape, dim=(0, 1))
+    for idx in layer_tris.values():
+        idx = np.asarray(idx)
+        jx, jy = current_grid(rwg, I2, idx, gx, gy, device=device)
+        Jx, Jy = fft2(jx), fft2(jy)
+        for h, height in enumerate(heights):
+            dz = height - z_of[idx[0]]
+            kernel = dx * dy / (4 * np.pi * (rx * rx + ry * ry + dz * dz) ** 1.5)
+            kx, ky, kz = [fft2((v * kernel).to(torch.complex128))[..., None] for v in (rx + 0 * ry, ry + 0 * rx,
+                                                                                       dz + 0 * rx * ry)]
+            for c, spectrum in enumerate((Jy * kz, -Jx * kz, Jx * ky - Jy * kx)):
+                out[:, :, h, c] += torch.fft.ifft2(spectrum, dim=(0, 1))[cx, cy]
+    H = out.cpu().numpy()
+    if filaments is not None and len(filaments[0]):
+        p0, p1, currents = filaments
+        X, Y, Z = np.meshgrid(x, y, heights, indexing='ij')
+        pts = np.stack([X, Y, Z], axis=-1).reshape(-1, 3)
+        cur = np.asarray(currents)
+        H += h_segments(p0, p1, cur if cur.ndim > 1 else cur[:, None], pts, device).reshape(H.shape)
+    return H if multi else H[..., 0]

@@ -167,3 +167,55 @@ extern "C" int pcbqs_gb300_biot_segments(int64_t npts, const double *pts, int64_
     cudaError_t e = cudaGetLastError();
     return e ? fail(ERR_CUDA, "biot_segments: %s", cudaGetErrorString(e)) : OK;
 }
+
+// ---- the FFT near field's source: sheet current deposited on a uniform grid ----------------------------------------
+//
+// Cloud in cell (src/pcbqs/_numerics/currents.py:28-61, current_deposit): each quadrature point's current moment
+// (A m, complex, k excitations) is split onto the four grid points around it with bilinear weights; the grid holds
+// the sums (divided by the cell area on the host). One thread per point; FP64 atomics (the sums are order-dependent
+// only in their last bits).
+namespace {
+
+__global__ void k_current_deposit(int64_t npts, const double *qx, const double *qy, const double2 *mx,
+                                  const double2 *my, int k, double x0, double y0, double dx, double dy, int64_t nx,
+                                  int64_t ny, double2 *jx, double2 *jy) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < npts; t += (int64_t)gridDim.x * blockDim.x) {
+        const double fx = (qx[t] - x0) / dx, fy = (qy[t] - y0) / dy;
+        const double fi = floor(fx), fj = floor(fy);
+        const int64_t i0 = (int64_t)fi, j0 = (int64_t)fj;
+        const double tx = fx - fi, ty = fy - fj;
+        const double w[4] = {(1 - tx) * (1 - ty), tx * (1 - ty), (1 - tx) * ty, tx * ty};
+        const int di[4] = {0, 1, 0, 1}, dj[4] = {0, 0, 1, 1};
+        for (int c = 0; c < 4; ++c) {
+            const int64_t ii = i0 + di[c], jj = j0 + dj[c];
+            if (ii < 0 || ii >= nx || jj < 0 || jj >= ny) continue;
+            for (int s = 0; s < k; ++s) {
+                const double2 a = mx[t * k + s], b = my[t * k + s];
+                double *gx = reinterpret_cast<double *>(jx + (ii * ny + jj) * k + s);
+                double *gy = reinterpret_cast<double *>(jy + (ii * ny + jj) * k + s);
+                atomicAdd(gx, a.x * w[c]);
+                atomicAdd(gx + 1, a.y * w[c]);
+                atomicAdd(gy, b.x * w[c]);
+                atomicAdd(gy + 1, b.y * w[c]);
+            }
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int pcbqs_gb300_current_deposit(int64_t npts, const double *qx, const double *qy, const double *mom_x,
+                                           const double *mom_y, int k, double x0, double y0, double dx, double dy,
+                                           int64_t nx, int64_t ny, double *jx, double *jy, void *stream) {
+    if (npts < 0 || k <= 0 || nx <= 0 || ny <= 0 || !(dx > 0) || !(dy > 0) || !jx || !jy ||
+        (npts && (!qx || !qy || !mom_x || !mom_y)))
+        return fail(ERR_ARGUMENT, "current_deposit: invalid argument");
+    if (!npts) return OK;
+    const int64_t blocks = std::min<int64_t>((npts + 255) / 256, 152 * 16);
+    k_current_deposit<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        npts, qx, qy, reinterpret_cast<const double2 *>(mom_x), reinterpret_cast<const double2 *>(mom_y), k, x0, y0,
+        dx, dy, nx, ny, reinterpret_cast<double2 *>(jx), reinterpret_cast<double2 *>(jy));
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    return e ? fail(ERR_CUDA, "current_deposit: %s", cudaGetErrorString(e)) : OK;
+}

@@ -15,8 +15,9 @@ constexpr int CT_THREADS = 256;
 constexpr int CT_ROWS = CT / (CT_THREADS / 32);
 
 __device__ __forceinline__ void upper_tile(int64_t t, int nb, int &bm, int &bn) {
-    const double b = 2.0 * nb + 1.0;
-    int r = (int)floor((b - sqrt(b * b - 8.0 * (double)t)) * 0.5);
+    // FP32 estimate of the tile row, corrected exactly in integers (keeps the per-tile math off the FP64 pipe)
+    const float b = 2.0f * (float)nb + 1.0f;
+    int r = (int)floorf((b - sqrtf(fmaxf(b * b - 8.0f * (float)t, 0.0f))) * 0.5f);
     r = max(0, min(r, nb - 1));
     auto off = [nb](int64_t x) { return x * nb - x * (x - 1) / 2; };
     while (r > 0 && off(r) > t) --r;

@@ -89,9 +89,10 @@ struct FillSmem {
 };
 
 __device__ __forceinline__ void tile_of(int64_t t, int nb, int &bp, int &bq) {
-    // Row bp of the upper tile triangle starts at off(bp) = bp*nb - bp*(bp-1)/2.
-    const double b = 2.0 * nb + 1.0;
-    int r = (int)floor((b - sqrt(b * b - 8.0 * (double)t)) * 0.5);
+    // Row bp of the upper tile triangle starts at off(bp) = bp*nb - bp*(bp-1)/2. The FP32 estimate of the row is
+    // corrected exactly in integers below (FP32 here keeps the per-tile index math off the slow FP64 pipe).
+    const float b = 2.0f * (float)nb + 1.0f;
+    int r = (int)floorf((b - sqrtf(fmaxf(b * b - 8.0f * (float)t, 0.0f))) * 0.5f);
     r = max(0, min(r, nb - 1));
     auto off = [nb](int64_t x) { return x * nb - x * (x - 1) / 2; };
     while (r > 0 && off(r) > t) --r;

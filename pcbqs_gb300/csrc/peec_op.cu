@@ -13,6 +13,7 @@
 // device (K^T L K and T^T P T blocks gathered from the dense matrices), inverted (Gauss-Jordan with partial
 // pivoting), and applied to every column of its system.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -320,15 +321,86 @@ __global__ void __launch_bounds__(256) k_dense_sym_apply(int64_t rows, const T *
         }
 }
 
+// The FP32 product is bound by streaming M (4 B an entry), so it skips the shared-memory staging: X is first
+// packed into FP32 rows of DENSE_NC values (64 B, 16-byte aligned), which every warp reads with vector loads that
+// the 8 warps of a block share through L1; each lane then keeps RW x 16 sums and issues its loads for two columns
+// before the multiply-adds.
+__global__ void k_pack_x_f32(int64_t rows, const double *X, int xcols, int c0, int nc, float *Xf) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * DENSE_NC;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / DENSE_NC;
+        const int c = (int)(t % DENSE_NC);
+        Xf[t] = c < nc ? (float)X[i * xcols + c0 + c] : 0.0f;
+    }
+}
+
+template <int RW>
+__global__ void __launch_bounds__(256) k_dense_apply_f32(int64_t rows, const float *__restrict__ M, int64_t ld,
+                                                         const float *__restrict__ Xf, int xcols, int c0, int nc,
+                                                         double *__restrict__ Y) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r0 = ((int64_t)blockIdx.x * 8 + warp) * RW;
+    float acc[RW][DENSE_NC];
+#pragma unroll
+    for (int r = 0; r < RW; ++r)
+#pragma unroll
+        for (int c = 0; c < DENSE_NC; ++c) acc[r][c] = 0.f;
+    const float *mrow[RW];
+#pragma unroll
+    for (int r = 0; r < RW; ++r) mrow[r] = M + (r0 + r < rows ? r0 + r : 0) * ld;
+    for (int64_t i = lane; i < rows; i += 64) {
+        float mv[2][RW];
+        float4 xv[2][DENSE_NC / 4];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int64_t iu = i + 32 * u;
+            const bool in = iu < rows;
+#pragma unroll
+            for (int r = 0; r < RW; ++r) mv[u][r] = in ? __ldg(mrow[r] + iu) : 0.f;
+            const float4 *xp = reinterpret_cast<const float4 *>(Xf + (in ? iu : 0) * DENSE_NC);
+#pragma unroll
+            for (int q = 0; q < DENSE_NC / 4; ++q) xv[u][q] = in ? __ldg(xp + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int q = 0; q < DENSE_NC / 4; ++q)
+#pragma unroll
+                for (int r = 0; r < RW; ++r) {
+                    acc[r][4 * q] += mv[u][r] * xv[u][q].x;
+                    acc[r][4 * q + 1] += mv[u][r] * xv[u][q].y;
+                    acc[r][4 * q + 2] += mv[u][r] * xv[u][q].z;
+                    acc[r][4 * q + 3] += mv[u][r] * xv[u][q].w;
+                }
+    }
+#pragma unroll
+    for (int r = 0; r < RW; ++r)
+#pragma unroll
+        for (int c = 0; c < DENSE_NC; ++c) {
+            float v = acc[r][c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0 && r0 + r < rows && c < nc) Y[(r0 + r) * xcols + c0 + c] = (double)v;
+        }
+}
+
 template <class T, int RW>
-static cudaError_t dense_sym_apply(int64_t rows, int k, const T *M, int64_t ld, const cd *X, cd *Y, cudaStream_t s) {
+static cudaError_t dense_sym_apply(int64_t rows, int k, const T *M, int64_t ld, const cd *X, cd *Y, cudaStream_t s,
+                                   float *xf = nullptr) {
     const int xcols = 2 * k;
     const unsigned grid = (unsigned)((rows + 8 * RW - 1) / (8 * RW));
     for (int c0 = 0; c0 < xcols; c0 += DENSE_NC) {
         const int nc = std::min(DENSE_NC, xcols - c0);
-        k_dense_sym_apply<T, RW><<<grid, 256, 0, s>>>(rows, M, ld, reinterpret_cast<const double *>(X), xcols, c0,
-                                                      nc, reinterpret_cast<double *>(Y));
-        note_launches(1);
+        if constexpr (std::is_same<T, float>::value) {
+            k_pack_x_f32<<<grid_of(rows * DENSE_NC), 256, 0, s>>>(rows, reinterpret_cast<const double *>(X), xcols,
+                                                                 c0, nc, xf);
+            k_dense_apply_f32<RW><<<grid, 256, 0, s>>>(rows, M, ld, xf, xcols, c0, nc, reinterpret_cast<double *>(Y));
+            note_launches(2);
+        } else {
+            k_dense_sym_apply<T, RW><<<grid, 256, 0, s>>>(rows, M, ld, reinterpret_cast<const double *>(X), xcols,
+                                                          c0, nc, reinterpret_cast<double *>(Y));
+            note_launches(1);
+        }
     }
     return cudaGetLastError();
 }
@@ -389,10 +461,21 @@ struct PeecOp : Operator {
 
     // y (rows x k complex128) = M x for a dense symmetric M, in FP64 (cuBLAS DGEMM) or through its single-precision
     // copy (SGEMM on converted vectors) when `single`.
+    float *xf = nullptr;       // packed FP32 right-hand sides of the single-precision products
+    int64_t capf = 0;
+
     cudaError_t dense(bool single, int64_t rows, int k, const double *M, int64_t ld, const float *Mf, int64_t ldf,
                       const cd *x, cd *y, cudaStream_t s) {
         if (!single) return dense_sym_apply<double, 2>(rows, k, M, ld, x, y, s);
-        return dense_sym_apply<float, 4>(rows, k, Mf, ldf, x, y, s);
+        const int64_t need = std::max(ne, nn) * (int64_t)DENSE_NC;
+        if (need > capf) {
+            dev_free(xf, s);
+            xf = nullptr;
+            cudaError_t e = dev_alloc(&xf, (size_t)need, s);
+            if (e) return e;
+            capf = need;
+        }
+        return dense_sym_apply<float, 4>(rows, k, Mf, ldf, x, y, s, xf);
     }
 
     cudaError_t apply_impl(bool single, int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) {
@@ -421,6 +504,7 @@ struct PeecOp : Operator {
         for (cd *p : {u, branch, lb, v, tq, pq}) dev_free(p);
         for (double *p : {omega, zscale, walpha, inv_z, inv_p}) dev_free(p);
         dev_free(rscale);
+        dev_free(xf);
     }
 };
 
@@ -940,6 +1024,15 @@ int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
         ok = ok && rep.residual[s] <= tol;
     }
     if (!ok) return pfail(ERR_CONVERGENCE, "peec_gmres: not every system reached the tolerance");
+    return OK;
+}
+
+int pcbqs_gb300_dense_apply(int64_t rows, int k, const double *M, int64_t ld, const double *X, double *Y,
+                            void *stream) {
+    if (rows <= 0 || k <= 0 || !M || ld < rows || !X || !Y) return pfail(ERR_ARGUMENT, "dense_apply: invalid argument");
+    cudaError_t e = dense_sym_apply<double, 2>(rows, k, M, ld, reinterpret_cast<const cd *>(X), reinterpret_cast<cd *>(Y),
+                                               static_cast<cudaStream_t>(stream));
+    if (e) return pfail(ERR_CUDA, "dense_apply: %s", cudaGetErrorString(e));
     return OK;
 }
 

@@ -85,15 +85,13 @@ __global__ void k_tri_invert_upper(const float2 *lu, int64_t n, float2 *inv) {
     for (int a = 0; a < B; ++a) out[a * B + c] = X[a * B + c];
 }
 
-// partial[s][r][c] = sum over columns i of run s (of `runs`) of [col0, col1) of lu[(row0 + r) n + i] x[i][c0 + c],
-// for the 4 rows r of row group rg (r < m). Each thread keeps 4 x KC complex sums, so every 8 B of the factor it
+// slot[r][c] = sum over columns i in [i0, i1) of lu[(row0 + r) n + i] x[i][c0 + c], for the 4 rows r of row group
+// rg (r < m). Each thread keeps 4 x KC complex sums, so every 8 B of the factor it
 // streams meets 8 complex multiply-adds and a vector entry is loaded once for 4 rows; PANEL_UNROLL columns per
 // thread have their loads in flight together. x is written during the kernel, so it is read through L2 (ld.cg).
 __device__ __forceinline__ void panel_block(const float2 *__restrict__ lu, int64_t n, int64_t row0, int m,
-                                            int64_t col0, int64_t col1, const float2 *x, int kpad, int c0,
-                                            float2 *partial, int rg, int s, int runs) {
-    const int64_t len = col1 - col0;
-    const int64_t i0 = col0 + len * s / runs, i1 = col0 + len * (s + 1) / runs;
+                                            int64_t i0, int64_t i1, const float2 *x, int kpad, int c0, float2 *slot,
+                                            int rg) {
     float acc[PANEL_ROWS][KC][2];
 #pragma unroll
     for (int r = 0; r < PANEL_ROWS; ++r)
@@ -155,7 +153,7 @@ __device__ __forceinline__ void panel_block(const float2 *__restrict__ lu, int64
         for (int w = 0; w < PANEL_THREADS / 32; ++w) v += red[w][threadIdx.x];
         const int r = threadIdx.x / (KC * 2), c = (threadIdx.x / 2) % KC, p = threadIdx.x & 1;
         const int rr = rg * PANEL_ROWS + r;
-        if (rr < m) reinterpret_cast<float *>(partial)[(((int64_t)s * B + rr) * KC + c) * 2 + p] = v;
+        if (rr < m) reinterpret_cast<float *>(slot)[((int64_t)rr * KC + c) * 2 + p] = v;
     }
     __syncthreads();
 }
@@ -280,50 +278,138 @@ struct SweepArgs {
     const float2 *b;
     float2 *y, *z;
     int kpad, c0;
-    float2 *partial;
-    unsigned *barrier;     // [0] arrivals (grows by one per block and barrier)
+    float2 *partial;       // [2][MAX_SPLITS + 1][B][KC]: the panel sums of two consecutive steps
+    unsigned *barrier;     // grid barrier arrivals
+    unsigned *xready;      // [2] per sweep: diagonal quarters finished (4 per step)
+    unsigned *pdone;       // [2][nblk] per sweep and step: panel items finished
     int *status;
 };
 
-// Forward sweep b -> y with U^T, then backward sweep y -> z with L^T, for columns c0 .. c0 + 7. The first
-// DIAG_BLOCKS thread blocks own the diagonal steps (one quarter of the 128 rows each) and stage their inputs while
-// the others stream the panel.
+// Bounded wait until *counter >= target (thread 0 polls with acquire loads; the block then proceeds together).
+__device__ __forceinline__ bool wait_for(const unsigned *counter, unsigned target, int *status) {
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const long long start = clock64();
+        while (load_acquire(counter) < target) {
+            if (clock64() - start > (2ll << 30) || *(volatile int *)status) {
+                atomicExch(status, TRI_TIMEOUT);
+                ok = 0;
+                break;
+            }
+        }
+    }
+    __syncthreads();
+    return ok;
+}
+
+// Release this block's writes, then count one more on *counter.
+__device__ __forceinline__ void signal(unsigned *counter) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(counter, 1u);
+    }
+}
+
+// The columns of one step's panel in two parts: the tail (the block solved just before, needed last) and the bulk
+// (everything solved earlier, split into runs). Forward step s (block J = s): tail [(s-1)B, sB), bulk [0, (s-1)B);
+// backward (block J = nblk-1-s): tail [(J+1)B, (J+2)B), bulk [(J+2)B, n).
+struct StepCols {
+    int64_t tail0, tail1, bulk0, bulk1;
+    int bulk_runs;
+};
+
+__device__ __forceinline__ StepCols step_cols(int dir, int step, int nblk, int64_t n, int bulk_workers) {
+    StepCols c{0, 0, 0, 0, 0};
+    const int groups = (B + PANEL_ROWS - 1) / PANEL_ROWS;
+    if (dir == 0) {
+        if (step >= 1) { c.tail0 = (int64_t)(step - 1) * B; c.tail1 = (int64_t)step * B; }
+        if (step >= 2) { c.bulk0 = 0; c.bulk1 = (int64_t)(step - 1) * B; }
+    } else {
+        const int J = nblk - 1 - step;
+        if (J + 1 < nblk) { c.tail0 = (int64_t)(J + 1) * B; c.tail1 = (int64_t)(J + 2) * B < n ? (int64_t)(J + 2) * B : n; }
+        if (J + 2 < nblk) { c.bulk0 = (int64_t)(J + 2) * B; c.bulk1 = n; }
+    }
+    const int64_t len = c.bulk1 - c.bulk0;
+    if (len > 0) {
+        int runs = bulk_workers / groups;
+        runs = runs < 1 ? 1 : (runs > MAX_SPLITS ? MAX_SPLITS : runs);
+        const int64_t by_len = len / 512;
+        if (by_len < runs) runs = by_len < 1 ? 1 : (int)by_len;
+        c.bulk_runs = runs;
+    }
+    return c;
+}
+
+// Forward sweep b -> y with U^T, then backward sweep y -> z with L^T, for columns c0 .. c0 + 7, with one step of
+// lookahead: while the DIAG_BLOCKS diagonal blocks finish step s, BULK workers already stream step s + 1's bulk
+// (it only needs blocks solved before s), and TAIL workers wait for block s and add its columns. The diagonal step
+// waits for its panel items through a per-step counter and publishes its block through a per-sweep counter, so the
+// dependency chain per step is a short tail product and two flag hand-offs instead of two grid barriers.
 constexpr int DIAG_BLOCKS = B / 32;
+constexpr int TAIL_BLOCKS = (B + PANEL_ROWS - 1) / PANEL_ROWS;     // one per row group of the tail
 
 __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
     __shared__ DiagSmem dsm;
-    const int groups = (B + PANEL_ROWS - 1) / PANEL_ROWS;
-    const bool diag = blockIdx.x < DIAG_BLOCKS;
-    const int workers = (int)gridDim.x - DIAG_BLOCKS, me = (int)blockIdx.x - DIAG_BLOCKS;
-    unsigned barriers = 0;
+    const int role_id = (int)blockIdx.x;
+    const bool diag = role_id < DIAG_BLOCKS;
+    const bool tail = !diag && role_id < DIAG_BLOCKS + TAIL_BLOCKS;
+    const int bulk_workers = (int)gridDim.x - DIAG_BLOCKS - TAIL_BLOCKS;
+    const int me = role_id - DIAG_BLOCKS - TAIL_BLOCKS;
+    const size_t buf = (size_t)(MAX_SPLITS + 1) * B * KC;
     for (int dir = 0; dir < 2; ++dir) {
+        if (dir == 1 && !grid_barrier(a.barrier, 0, a.status)) return;      // the backward sweep needs all of y
         const float2 *inv = dir == 0 ? a.inv_lower : a.inv_upper;
         const float2 *rhs = dir == 0 ? a.b : a.y;
         float2 *x = dir == 0 ? a.y : a.z;
+        unsigned *xready = a.xready + dir, *pdone = a.pdone + (size_t)dir * a.nblk;
+        // bulk workers start with step 1's bulk (empty) and run one step ahead of the diagonal
         for (int step = 0; step < a.nblk; ++step) {
             const int J = dir == 0 ? step : a.nblk - 1 - step;
             const int64_t row0 = (int64_t)J * B;
             const int m = a.n - row0 < B ? (int)(a.n - row0) : B;
-            const int64_t col0 = dir == 0 ? 0 : row0 + m, col1 = dir == 0 ? row0 : a.n;
-            const int64_t len = col1 - col0;
-            int runs = 0;
-            if (len > 0) {
-                runs = workers / groups;
-                runs = runs < 1 ? 1 : (runs > MAX_SPLITS ? MAX_SPLITS : runs);
-                const int64_t by_len = len / 512;
-                if (by_len < runs) runs = by_len < 1 ? 1 : (int)by_len;
-            }
+            const StepCols sc = step_cols(dir, step, a.nblk, a.n, bulk_workers);
+            float2 *slots = a.partial + (size_t)(step & 1) * buf;
+            const int tail_runs = sc.tail1 > sc.tail0 ? 1 : 0;
             if (diag) {
-                diag_stage(dsm, inv + (int64_t)J * B * B, rhs, row0, m, a.kpad, a.c0, blockIdx.x);
-            } else if (len > 0) {
-                const int mg = (m + PANEL_ROWS - 1) / PANEL_ROWS;
-                for (int item = me; item < mg * runs; item += workers)
-                    panel_block(a.lu, a.n, row0, m, col0, col1, x, a.kpad, a.c0, a.partial, item % mg, item / mg,
-                                runs);
+                diag_stage(dsm, inv + (int64_t)J * B * B, rhs, row0, m, a.kpad, a.c0, role_id);
+                const unsigned need = (unsigned)(tail_runs * TAIL_BLOCKS + sc.bulk_runs * ((m + PANEL_ROWS - 1) / PANEL_ROWS));
+                if (need && !wait_for(pdone + step, need, a.status)) return;
+                diag_finish(dsm, slots, tail_runs + sc.bulk_runs, x, row0, m, a.kpad, a.c0, role_id);
+                signal(xready);
+            } else if (tail) {
+                if (tail_runs) {
+                    // block `step - 1` of this sweep must be solved: DIAG_BLOCKS quarters per step
+                    if (!wait_for(xready, (unsigned)(DIAG_BLOCKS * step), a.status)) return;
+                    panel_block(a.lu, a.n, row0, m, sc.tail0, sc.tail1, x, a.kpad, a.c0,
+                                slots + (size_t)sc.bulk_runs * B * KC, role_id - DIAG_BLOCKS);
+                    signal(pdone + step);
+                }
+            } else if (step + 1 < a.nblk) {
+                // the next step's bulk needs the blocks solved up to this step's predecessor
+                const StepCols nx = step_cols(dir, step + 1, a.nblk, a.n, bulk_workers);
+                if (nx.bulk_runs) {
+                    const int Jn = dir == 0 ? step + 1 : a.nblk - 2 - step;
+                    const int64_t rown = (int64_t)Jn * B;
+                    const int mn = a.n - rown < B ? (int)(a.n - rown) : B;
+                    const int mg = (mn + PANEL_ROWS - 1) / PANEL_ROWS;
+                    float2 *nslots = a.partial + (size_t)((step + 1) & 1) * buf;
+                    bool waited = false;
+                    for (int item = me; item < mg * nx.bulk_runs; item += bulk_workers) {
+                        if (!waited) {
+                            if (step > 0 && !wait_for(xready, (unsigned)(DIAG_BLOCKS * step), a.status)) return;
+                            waited = true;
+                        }
+                        const int s = item / mg;
+                        const int64_t len = nx.bulk1 - nx.bulk0;
+                        panel_block(a.lu, a.n, rown, mn, nx.bulk0 + len * s / nx.bulk_runs,
+                                    nx.bulk0 + len * (s + 1) / nx.bulk_runs, x, a.kpad, a.c0,
+                                    nslots + (size_t)s * B * KC, item % mg);
+                        signal(pdone + step + 1);
+                    }
+                }
             }
-            if (len > 0 && !grid_barrier(a.barrier, barriers++, a.status)) return;
-            if (diag) diag_finish(dsm, a.partial, runs, x, row0, m, a.kpad, a.c0, blockIdx.x);
-            if (!grid_barrier(a.barrier, barriers++, a.status)) return;
         }
     }
 }
@@ -400,8 +486,8 @@ cudaError_t TriSolver::plan_for(int k, Plan **out) {
     cudaError_t e;
     if ((e = pool_alloc_n(&p.b, vec, nullptr)) || (e = pool_alloc_n(&p.y, vec, nullptr)) ||
         (e = pool_alloc_n(&p.z, vec, nullptr)) ||
-        (e = pool_alloc_n(&p.partial, (size_t)MAX_SPLITS * B * KC, nullptr)) ||
-        (e = pool_alloc_n(&p.sync, 4, nullptr)) || (e = cudaStreamSynchronize(nullptr))) {
+        (e = pool_alloc_n(&p.partial, 2 * (size_t)(MAX_SPLITS + 1) * B * KC, nullptr)) ||
+        (e = pool_alloc_n(&p.sync, 4 + 2 * (size_t)nblk, nullptr)) || (e = cudaStreamSynchronize(nullptr))) {
         for (float2 *q : {p.b, p.y, p.z, p.partial}) pool_free(q, nullptr);
         pool_free(p.sync, nullptr);
         return e;
@@ -423,14 +509,18 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
             (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) ||
             (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tri_sweeps, PANEL_THREADS, 0)))
             return e;
-        if (!coop || per_sm < 1 || sms * per_sm <= DIAG_BLOCKS) return cudaErrorNotSupported;
+        if (!coop || per_sm < 1 || sms * per_sm < DIAG_BLOCKS + TAIL_BLOCKS + 8) return cudaErrorNotSupported;
         grid = sms * per_sm;
     }
     k_tri_in<<<blocks_for(n * p->kpad), 256, 0, s>>>(n, k, p->kpad, in, p->b);
+    if ((e = cudaMemsetAsync(p->sync, 0, (4 + 2 * (size_t)nblk) * sizeof(unsigned), s))) return e;
     for (int c0 = 0; c0 < p->kpad; c0 += KC) {
-        if ((e = cudaMemsetAsync(p->sync, 0, 4 * sizeof(unsigned), s))) return e;
+        // counters restart for every 8 columns; the status word [3] keeps the first failure
+        if (c0 && ((e = cudaMemsetAsync(p->sync, 0, 3 * sizeof(unsigned), s)) ||
+                   (e = cudaMemsetAsync(p->sync + 4, 0, 2 * (size_t)nblk * sizeof(unsigned), s))))
+            return e;
         SweepArgs a{lu, n, nblk, inv_lower, inv_upper, p->b, p->y, p->z, p->kpad, c0, p->partial, p->sync,
-                    reinterpret_cast<int *>(p->sync + 2)};
+                    p->sync + 1, p->sync + 4, reinterpret_cast<int *>(p->sync + 3)};
         void *args[] = {&a};
         if ((e = cudaLaunchCooperativeKernel((const void *)k_tri_sweeps, dim3(grid), dim3(PANEL_THREADS), args, 0,
                                              s)))
@@ -440,7 +530,7 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
     note_launches(2 + p->kpad / KC);
     // a barrier that gave up leaves its status; the sweeps are then incomplete
     int status = 0;
-    if ((e = cudaMemcpyAsync(&status, p->sync + 2, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+    if ((e = cudaMemcpyAsync(&status, p->sync + 3, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
         return e;
     if (status) return cudaErrorLaunchTimeout;

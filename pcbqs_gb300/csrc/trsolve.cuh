@@ -27,7 +27,7 @@ struct TriSolver {
     struct Plan {
         int kpad = 0;
         float2 *b = nullptr, *y = nullptr, *z = nullptr, *partial = nullptr;
-        unsigned *sync = nullptr;     // [0] arrivals, [1] generation, [2] status
+        unsigned *sync = nullptr;     // [0] barrier, [1..2] solved quarters per sweep, [3] status, [4..] panel items
     };
     std::map<int, Plan> plans;
     int grid = 0;                     // co-resident thread blocks of the sweep kernel

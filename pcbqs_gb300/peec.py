@@ -332,13 +332,20 @@ class PeecModel(PeecTopology):
         return x.cpu().numpy()
 
     def _mv_L(self, X):
-        """L X for complex branch vectors X (ne, k) on the device."""
-        Xt = torch.as_tensor(np.ascontiguousarray(X), device=self.device)
-        return (self.L @ Xt.real + 1j * (self.L @ Xt.imag)).cpu().numpy()
+        """L X for complex branch vectors X (ne, k), FP64 on the device (pcbqs_gb300_dense_apply)."""
+        return self._dense(self.L, X)
 
     def _mv_P(self, X):
-        Xt = torch.as_tensor(np.ascontiguousarray(X), device=self.device)
-        return (self.P @ Xt.real + 1j * (self.P @ Xt.imag)).cpu().numpy()
+        return self._dense(self.P, X)
+
+    def _dense(self, M, X):
+        Xt = torch.as_tensor(np.ascontiguousarray(X, complex), device=self.device)
+        Y = torch.empty_like(Xt)
+        lib = _lib.load()
+        _lib.check(lib.pcbqs_gb300_dense_apply(M.shape[0], Xt.shape[1], M.data_ptr(), M.stride(0), Xt.data_ptr(),
+                                               Y.data_ptr(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                   lib)
+        return Y.cpu().numpy()
 
     PRECONDITIONERS = {'none': 0, 'block_jacobi': 1, 'lu32': 2}
 

@@ -1,0 +1,79 @@
+"""Kernel timing on one GPU, for profiling the hot kernels on cases small enough for a full ncu capture.
+
+    python -m pcbqs_gb300.timing fill <board> [triangles]   # mixed and FP64 fill of the first N triangles
+    python -m pcbqs_gb300.timing lu <board> [k ...]          # the complex64 factor's triangular solves, k columns
+
+Times are CUDA-event times after a warm-up call; boards are the npz meshes of tests/golden (planes, strip, tiny).
+"""
+import ctypes
+import sys
+
+import numpy as np
+import torch
+
+
+def _event_ms(fn):
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    out = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), out
+
+
+def fill(board, triangles=None):
+    from .board import Board
+    from .fill import DeviceFill
+    b = Board.load(board)
+    nt = len(b.tris) if triangles is None else int(triangles)
+    tris = b.tris[:nt]
+    used = np.unique(tris)
+    remap = np.full(len(b.nodes), -1)
+    remap[used] = np.arange(len(used))
+    f = DeviceFill(b.nodes[used], remap[tris], b.z[:nt], 1, 3.0)
+    for mode in ('mixed', 'fp64'):
+        for _ in range(3):
+            ms, (planes, analytic) = _event_ms(f.moments_local if mode == 'mixed' else f.moments)
+            del planes
+            print(f'fill {mode} {nt} triangles: {ms:.2f} ms, {analytic} analytic pairs', flush=True)
+
+
+def lu(board, ks=(8,)):
+    from . import _lib
+    from .board import Board
+    from .peec import PeecModel, _csr_struct
+    m = PeecModel(Board.load(board))
+    m.assemble(mixed=True)
+    lib = _lib.load()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    handle, _ = m._operator(np.array([2 * np.pi * 1e6]))
+    try:
+        desc = _csr_struct(m._krk_device())
+        ms, _ = _event_ms(lambda: _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, 1, stream),
+                                             lib))
+        print(f'factor n={m.n}: {ms:.1f} ms', flush=True)
+        for k in ks:
+            x = torch.randn(m.n, k, dtype=torch.complex128, device='cuda')
+            y = torch.empty_like(x)
+            for _ in range(3):
+                ms, _ = _event_ms(lambda: _lib.check(lib.pcbqs_gb300_peec_lu_solve(handle, k, x.data_ptr(),
+                                                                                   y.data_ptr(), 0, stream), lib))
+                print(f'lu_solve k={k}: {ms:.2f} ms', flush=True)
+    finally:
+        lib.pcbqs_gb300_peec_destroy(handle)
+
+
+def main(argv):
+    if len(argv) < 2 or argv[0] not in ('fill', 'lu'):
+        print(__doc__)
+        return 2
+    if argv[0] == 'fill':
+        fill(argv[1], argv[2] if len(argv) > 2 else None)
+    else:
+        lu(argv[1], tuple(int(v) for v in argv[2:]) or (8,))
+    return 0
+
+
+if __name__ == '__main__':
+    sys.exit(main(sys.argv[1:]))

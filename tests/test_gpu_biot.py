@@ -43,3 +43,24 @@ def test_filament_field_matches_reference(device_library):
     g = golden('strip')
     H = h_segments(g['p0'], g['p1'], g['Iseg'], g['pts'])
     assert np.abs(H - g['Hseg']).max() <= 1e-12 * np.abs(g['Hseg']).max()
+
+
+def test_fft_grid_field_matches_reference(device_library):
+    """h_grid on the device (cloud-in-cell deposit kernel, zero-padded FFT convolution) against the reference's own
+    h_grid for the same branch currents on the tiny two-layer board, refine 2, above and below the copper; FP64
+    throughout (the FFTs' rounding differs: 1e-9 of the field's largest value)."""
+    import numpy as np
+    from pcbqs_gb300.biot import h_grid
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.rwg import RWG
+    g = np.load(GOLDEN / 'hgrid_tiny.npz')
+    b = Board.load('tiny')
+    r = RWG(b.nodes, b.tris)
+    layer_tris = {int(k): np.flatnonzero(b.layer == k) for k in np.unique(b.layer)}
+    I = (g['i'] / r.l[None, :]).T                     # RWG amplitudes (ne, 2)
+    H = h_grid(r, layer_tris, b.z, I, g['x'], g['y'], g['heights'], refine=int(g['refine']))
+    Hr = g['H']
+    assert H.shape == Hr.shape
+    assert np.abs(H - Hr).max() <= 1e-9 * np.abs(Hr).max()
+    one = h_grid(r, layer_tris, b.z, I[:, 1], g['x'], g['y'], g['heights'], refine=int(g['refine']))
+    assert np.abs(one - Hr[..., 1]).max() <= 1e-9 * np.abs(Hr).max()
