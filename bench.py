@@ -180,7 +180,7 @@ def reference_arm(args):
     rank, world, _ = rank_info()
     if rank != 0:
         return
-    from oracle import oracle as O
+    from pcbqs_gb300.board import Board
     values = []
     details = None
     for _ in range(max(1, args.steps)):
@@ -191,8 +191,8 @@ def reference_arm(args):
                 warmup=0, ms_per_step=round(value * 1e3, 2), higher_is_better=False, scaling='weak',
                 vs_baseline=None, dtype='f64', data='synthetic (seeded plane-pair board, CDT mesh)',
                 impl='reference',
-                config=dict(workload=f'{args.board}: fill+solve of all ports at {args.freq:g} Hz', board=args.board,
-                            l2='inputs larger than L2'),
+                config=dict(workload=f'{args.board}: fill+solve of all {len(Board.load(args.board).ports)} ports at '
+                                     f'{args.freq:g} Hz', board=args.board, l2='inputs larger than L2'),
                 cpu_baseline=dict(value=round(value, 4), unit='s/freq', cores=details['cores'], kind='port',
                                   sample=f'full oracle fill+combine+aggregation; dense solve = complex64 LU '
                                          f'estimated from a bounded sample ({details})'),

@@ -229,6 +229,8 @@ typedef struct pcbqs_gb300_peec_desc {
     /* per system, the complex factor on R (interleaved re, im; null: 1): a finite-thickness sheet impedance
      * Zs(f) sigma t, so R(f) = rscale R (src/pcbqs/mqs.py:517-530, conductor.py:12-26) */
     const double *rscale;
+    /* imaginary part of P (same leading dimension; null: P real), for a lossy dielectric stack */
+    const double *Pim;
 } pcbqs_gb300_peec_desc;
 
 typedef struct pcbqs_gb300_peec pcbqs_gb300_peec;
@@ -268,10 +270,14 @@ int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *op, int k, const int32_t *sys, cons
  * src/pcbqs/peec_iterative.py:253-256, 331-341). Asynchronous on `stream`. */
 int pcbqs_gb300_dense_apply(int64_t rows, int k, const double *M, int64_t ld, const double *X, double *Y,
                             void *stream);
+/* The same product from the FP32 copy of M (the mixed solve's inner products), results in FP64. */
+int pcbqs_gb300_dense_apply_single(int64_t rows, int k, const float *Mf, int64_t ld, const double *X, double *Y,
+                                   void *stream);
 /* Single-precision copies of L and P (device, row strides ldlf/ldpf) for the inner products of the mixed solve,
  * and the conversion that makes them. */
 int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *stream);
-int pcbqs_gb300_peec_single(pcbqs_gb300_peec *op, const float *Lf, int64_t ldlf, const float *Pf, int64_t ldpf);
+int pcbqs_gb300_peec_single(pcbqs_gb300_peec *op, const float *Lf, int64_t ldlf, const float *Pf, const float *Pfim,
+                            int64_t ldpf);
 /* Mixed-precision solve: FP64 true residuals b - A x (the outer iterative refinement), each correction from an
  * inner right-preconditioned GMRES on the single-precision operator to inner_tol of the residual; until every
  * column's true relative residual <= tol or max_outer corrections. iterations: inner Arnoldi steps per column;
@@ -281,12 +287,14 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *op, int k, const int32_t *sys
                                  double tol, double inner_tol, int max_outer, int inner_maxiter, int restart,
                                  int precondition, int32_t *iterations, double *residual, int32_t *outer_steps,
                                  void *stream);
-/* A x = b for a dense real symmetric A (n x n, row stride lda) and k complex columns by GMRES, preconditioned by
- * A's diagonal (precondition 0, as the reference) or by the single-precision Cholesky factor of A (1, A positive
- * definite). Replaces peec_iterative.potential_solve (src/pcbqs/peec_iterative.py:115-124), used for P^-1 B. */
-int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, const double *b, double *x, double tol,
-                            int maxiter, int restart, int precondition, int32_t *iterations, double *residual,
-                            void *stream);
+/* A x = b for a dense symmetric A = A_re + j A_im (n x n, row stride lda; A_im nullable: real A) and k complex
+ * columns by GMRES, preconditioned by the diagonal of A_re (precondition 0, as the reference) or by the
+ * single-precision Cholesky factor of A_re (1, A_re positive definite; exact for a real A, a close preconditioner for
+ * a lossy dielectric's complex potential matrix). Replaces peec_iterative.potential_solve
+ * (src/pcbqs/peec_iterative.py:115-124), used for P^-1 B. */
+int pcbqs_gb300_dense_gmres(int64_t n, const double *A, const double *Aim, int64_t lda, int k, const double *b,
+                            double *x, double tol, int maxiter, int restart, int precondition, int32_t *iterations,
+                            double *residual, void *stream);
 
 #ifdef __cplusplus
 }

@@ -44,7 +44,7 @@ class PeecDesc(ctypes.Structure):
                 ('K', CsrDesc), ('Kt', CsrDesc), ('T', CsrDesc), ('Tt', CsrDesc), ('R', CsrDesc),
                 ('L', c_void_p), ('ldl', ctypes.c_int64), ('P', c_void_p), ('ldp', ctypes.c_int64),
                 ('is_tree', c_void_p), ('pscale', ctypes.c_double), ('nsys', ctypes.c_int32),
-                ('omega', c_double_p), ('zscale', c_double_p), ('rscale', c_double_p)]
+                ('omega', c_double_p), ('zscale', c_double_p), ('rscale', c_double_p), ('Pim', c_void_p)]
 
 
 # name: (restype, argtypes)
@@ -117,8 +117,11 @@ PROTOTYPES = {
                                                  c_void_p]),
     'pcbqs_gb300_dense_apply': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64, c_void_p,
                                                c_void_p, c_void_p]),
+    'pcbqs_gb300_dense_apply_single': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64,
+                                                      c_void_p, c_void_p, c_void_p]),
     'pcbqs_gb300_to_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p]),
-    'pcbqs_gb300_peec_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, ctypes.c_int64]),
+    'pcbqs_gb300_peec_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
+                                               ctypes.c_int64]),
     'pcbqs_gb300_peec_solve_mixed': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p,
                                                     ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                                     ctypes.c_int, ctypes.c_int, c_int32_p, c_double_p, c_int32_p,
@@ -126,9 +129,9 @@ PROTOTYPES = {
     'pcbqs_gb300_peec_gmres': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p, ctypes.c_double,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_int, c_int32_p, c_double_p,
                                               c_void_p]),
-    'pcbqs_gb300_dense_gmres': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, ctypes.c_int, c_void_p,
-                                               c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                               c_int32_p, c_double_p, c_void_p]),
+    'pcbqs_gb300_dense_gmres': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, ctypes.c_int64, ctypes.c_int,
+                                               c_void_p, c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, c_int32_p, c_double_p, c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -108,6 +108,14 @@ __global__ void k_impedance(Csr R, int64_t nb, int k, const cd *B, const cd *LB,
     }
 }
 
+// y += j z (the imaginary part of a complex matrix applied through its real view).
+__global__ void k_add_times_j(int64_t count, const cd *z, cd *y) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+        const cd a = z[t];
+        y[t] = make_double2(y[t].x - a.y, y[t].y + a.x);
+    }
+}
+
 // Diagonal blocks of S^T M S for a dense symmetric M: out[b][i][j] = sum_{e in col i} sum_{f in col j}
 // S_ei S_fj M[e, f], columns of S given as rows of S^T (CSR St). One CTA per block.
 __global__ void k_block_gather(int64_t n, int bs, Csr St, const double *M, int64_t ldm, double *out) {
@@ -133,8 +141,8 @@ __global__ void k_block_gather(int64_t n, int bs, Csr St, const double *M, int64
 // Form and invert every (system, block): A = (KRK + j w KLK) D / zscale + TPT / pscale; padding rows beyond n
 // are identity. Gauss-Jordan with partial pivoting on [A | I] in shared memory; one warp per matrix row group.
 __global__ void k_block_invert(int64_t n, int bs, int64_t nblk, const double *krk, const double *klk,
-                               const double *tpt, const int8_t *is_tree, const double *omega, const double *zscale,
-                               const cd *rscale, double pscale, cd *inv, int *singular) {
+                               const double *tpt, const double *tpt_im, const int8_t *is_tree, const double *omega,
+                               const double *zscale, const cd *rscale, double pscale, cd *inv, int *singular) {
     extern __shared__ cd aug[];     // bs x 2bs
     const int64_t b = blockIdx.x;
     const int s = blockIdx.y;
@@ -156,7 +164,10 @@ __global__ void k_block_invert(int64_t n, int bs, int64_t nblk, const double *kr
                     re = r2;
                     im = i2;
                 }
-                if (is_tree[ci] && is_tree[cj]) re += tpt[at] / pscale;
+                if (is_tree[ci] && is_tree[cj]) {
+                    re += tpt[at] / pscale;
+                    if (tpt_im) im += tpt_im[at] / pscale;
+                }
                 v = make_double2(re, im);
             } else if (i == j) {
                 v = make_double2(1, 0);
@@ -429,6 +440,7 @@ struct PeecOp : Operator {
     int64_t n_ = 0, nb = 0, ne = 0, nn = 0;
     Csr K, Kt, T, Tt, R;
     const double *L = nullptr, *P = nullptr;
+    const double *Pim = nullptr;          // imaginary part of P (lossy dielectric stack), or null
     int64_t ldl = 0, ldp = 0;
     const int8_t *is_tree = nullptr;
     double pscale = 1;
@@ -437,26 +449,27 @@ struct PeecOp : Operator {
     cd *rscale = nullptr;                 // per system factor on R (device)
     std::vector<cd> rscale_host;
     int cap = 0;               // columns the scratch holds
-    cd *u = nullptr, *branch = nullptr, *lb = nullptr, *v = nullptr, *tq = nullptr, *pq = nullptr;
+    cd *u = nullptr, *branch = nullptr, *lb = nullptr, *v = nullptr, *tq = nullptr, *pq = nullptr, *pq2 = nullptr;
     int64_t launches = 0;
 
     int64_t n() const override { return n_; }
 
     cudaError_t reserve(int k, cudaStream_t s) {
         if (k <= cap) return cudaSuccess;
-        for (cd *p : {u, branch, lb, v, tq, pq}) dev_free(p, s);
-        u = branch = lb = v = tq = pq = nullptr;
+        for (cd *p : {u, branch, lb, v, tq, pq, pq2}) dev_free(p, s);
+        u = branch = lb = v = tq = pq = pq2 = nullptr;
         cudaError_t e;
         if ((e = dev_alloc(&u, (size_t)n_ * k, s)) || (e = dev_alloc(&branch, (size_t)nb * k, s)) ||
             (e = dev_alloc(&lb, (size_t)ne * k, s)) || (e = dev_alloc(&v, (size_t)nb * k, s)) ||
-            (e = dev_alloc(&tq, (size_t)nn * k, s)) || (e = dev_alloc(&pq, (size_t)nn * k, s)))
+            (e = dev_alloc(&tq, (size_t)nn * k, s)) || (e = dev_alloc(&pq, (size_t)nn * k, s)) ||
+            (e = dev_alloc(&pq2, (size_t)nn * k, s)))
             return e;
         cap = k;
         return cudaSuccess;
     }
 
     // Single-precision copies of L and P for the inner products of the mixed solve (set by peec_single).
-    const float *Lf = nullptr, *Pf = nullptr;
+    const float *Lf = nullptr, *Pf = nullptr, *Pfim = nullptr;
     int64_t ldlf = 0, ldpf = 0;
 
     // y (rows x k complex128) = M x for a dense symmetric M, in FP64 (cuBLAS DGEMM) or through its single-precision
@@ -489,6 +502,11 @@ struct PeecOp : Operator {
         if (nn > 0) {
             k_spmm<<<grid_of(nn * k), 256, 0, s>>>(T, k, in, tq, nullptr, sys, 0);
             if ((e = dense(single, nn, k, P, ldp, Pf, ldpf, tq, pq, s))) return e;
+            if (Pim) {          // complex P: P_re q + j (P_im q)
+                if ((e = dense(single, nn, k, Pim, ldp, Pfim, ldpf, tq, pq2, s))) return e;
+                k_add_times_j<<<grid_of(nn * k), 256, 0, s>>>(nn * k, pq2, pq);
+                note_launches(1);
+            }
             k_spmm<<<grid_of(n_ * k), 256, 0, s>>>(Tt, k, pq, out, inv_p, sys, 1);
         }
         launches += nn > 0 ? 6 : 3;
@@ -501,7 +519,7 @@ struct PeecOp : Operator {
     }
 
     ~PeecOp() override {
-        for (cd *p : {u, branch, lb, v, tq, pq}) dev_free(p);
+        for (cd *p : {u, branch, lb, v, tq, pq, pq2}) dev_free(p);
         for (double *p : {omega, zscale, walpha, inv_z, inv_p}) dev_free(p);
         dev_free(rscale);
         dev_free(xf);
@@ -560,8 +578,8 @@ __global__ void k_transpose(const double *W, int64_t rows, int64_t cols, int64_t
 }
 
 // A[i, j] = (j w KLK[i,j]) d_j / zs + TPT[i,j] / ps as complex64, d_j = 1 (loop) or j w alpha (tree).
-__global__ void k_assemble_c64(int64_t n, const double *klk, const double *tpt, const int8_t *is_tree, double w,
-                               double zs, double ps, float2 *A) {
+__global__ void k_assemble_c64(int64_t n, const double *klk, const double *tpt, const double *tpt_im,
+                               const int8_t *is_tree, double w, double zs, double ps, float2 *A) {
     const int64_t total = n * n;
     const double f = w * zs / ps;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -572,7 +590,10 @@ __global__ void k_assemble_c64(int64_t n, const double *klk, const double *tpt, 
             im = f * re;
             re = r2;
         }
-        if (is_tree[i] && is_tree[j]) re += tpt[t] / ps;
+        if (is_tree[i] && is_tree[j]) {
+            re += tpt[t] / ps;
+            if (tpt_im) im += tpt_im[t] / ps;
+        }
         A[t] = make_float2((float)re, (float)im);
     }
 }
@@ -652,35 +673,35 @@ struct LuPrecond : Preconditioner {
     }
 };
 
-// Single-precision Cholesky of a dense real SPD matrix (its FP32 copy, cuSOLVER potrf) as a preconditioner for
-// complex right-hand sides: real and imaginary parts solved as 2k real columns.
-__global__ void k_split_cols(int64_t n, int k, const cd *in, float *out) {     // (n,k) complex -> col-major (n,2k)
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = t / k;
-        const int s = (int)(t % k);
-        out[(int64_t)(2 * s) * n + r] = (float)in[t].x;
-        out[(int64_t)(2 * s + 1) * n + r] = (float)in[t].y;
+// The FP32 Cholesky factor of P in the LU layout of the streaming triangular solver: P = L L^T = (L D^-1)(D L^T),
+// D = diag(L), so with M = P^T = P the column-major array holds the unit lower L D^-1 below the diagonal and the
+// upper D L^T on and above it (no pivoting), as complex64 with zero imaginary parts.
+__global__ void k_cholesky_to_lu(int64_t n, const float *chol, float2 *lu) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = t / n, i = t % n;            // column-major: t = i + j n
+        const float v = i > j ? chol[i + j * n] / chol[j + j * n] : chol[i + i * n] * chol[j + i * n];
+        lu[t] = make_float2(v, 0.f);
     }
 }
 
-__global__ void k_join_cols(int64_t n, int k, const float *in, cd *out) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = t / k;
-        const int s = (int)(t % k);
-        out[t] = make_double2(in[(int64_t)(2 * s) * n + r], in[(int64_t)(2 * s + 1) * n + r]);
-    }
+__global__ void k_identity_pivots(int64_t n, int *ipiv) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        ipiv[t] = (int)(t + 1);
 }
 
 struct CholPrecond : Preconditioner {
     int64_t n = 0;
-    float *chol = nullptr, *work = nullptr;
-    int *info = nullptr;
-    int cap = 0;
+    float *chol = nullptr;
+    float2 *lu = nullptr;
+    int *info = nullptr, *ipiv = nullptr;
     cusolverDnHandle_t solver = nullptr;
+    TriSolver tri;
     ~CholPrecond() override {
+        tri.release();
         dev_free(chol);
-        dev_free(work);
+        dev_free(lu);
         dev_free(info);
+        dev_free(ipiv);
         if (solver) cusolverDnDestroy(solver);
     }
     cudaError_t factor(int64_t n_, const double *A, int64_t lda, cudaStream_t s, int &host_info) {
@@ -712,33 +733,42 @@ struct CholPrecond : Preconditioner {
         e = cudaStreamSynchronize(s);
         dev_free(ws, s);
         if (cs != CUSOLVER_STATUS_SUCCESS) return cudaErrorUnknown;
-        return e;
+        if (e || host_info) return e;
+        // the factor in the triangular solver's layout; the FP32 copy is not needed afterwards
+        if ((e = dev_alloc(&lu, (size_t)n * n, s)) || (e = dev_alloc(&ipiv, (size_t)n, s))) return e;
+        k_cholesky_to_lu<<<grid_of(n * n), 256, 0, s>>>(n, chol, lu);
+        k_identity_pivots<<<grid_of(n), 256, 0, s>>>(n, ipiv);
+        note_launches(2);
+        if ((e = tri.prepare(lu, n, ipiv, s))) return e;
+        dev_free(chol, s);
+        chol = nullptr;
+        return cudaStreamSynchronize(s);
     }
     cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
-        if (2 * k > cap) {
-            dev_free(work, s);
-            work = nullptr;
-            cudaError_t e = dev_alloc(&work, (size_t)n * 2 * k, s);
-            if (e) return e;
-            cap = 2 * k;
-        }
-        cusolverDnSetStream(solver, s);
-        k_split_cols<<<grid_of(n * k), 256, 0, s>>>(n, k, in, work);
-        if (cusolverDnSpotrs(solver, CUBLAS_FILL_MODE_LOWER, (int)n, 2 * k, chol, (int)n, work, (int)n, info) !=
-            CUSOLVER_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        k_join_cols<<<grid_of(n * k), 256, 0, s>>>(n, k, work, out);
-        note_launches(2);
-        return cudaGetLastError();
+        return tri.solve(k, in, out, s);
     }
 };
 
 struct DenseSym : Operator {
     int64_t n_ = 0, ld = 0;
-    const double *A = nullptr;
+    const double *A = nullptr, *Aim = nullptr;   // real and (nullable) imaginary parts, both symmetric
+    cd *tmp = nullptr;
+    int cap = 0;
     int64_t n() const override { return n_; }
+    ~DenseSym() override { dev_free(tmp); }
     cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
-        return dense_sym_apply<double, 2>(n_, k, A, ld, in, out, s);
+        cudaError_t e = dense_sym_apply<double, 2>(n_, k, A, ld, in, out, s);
+        if (e || !Aim) return e;
+        if (k > cap) {
+            dev_free(tmp, s);
+            tmp = nullptr;
+            if ((e = dev_alloc(&tmp, (size_t)n_ * k, s))) return e;
+            cap = k;
+        }
+        if ((e = dense_sym_apply<double, 2>(n_, k, Aim, ld, in, tmp, s))) return e;
+        k_add_times_j<<<grid_of(n_ * k), 256, 0, s>>>(n_ * k, tmp, out);
+        note_launches(1);
+        return cudaGetLastError();
     }
 };
 
@@ -761,11 +791,13 @@ struct pcbqs_gb300_peec {
     BlockJacobi *bj = nullptr;
     LuPrecond *lu = nullptr;
     double *klk = nullptr, *tpt = nullptr;   // dense K^T L K and T^T P T (n x n), made once for the factors
+    double *tpt_im = nullptr;                // T^T P_im T when P is complex
     ~pcbqs_gb300_peec() {
         delete bj;
         delete lu;
         dev_free(klk);
         dev_free(tpt);
+        dev_free(tpt_im);
     }
 };
 
@@ -799,6 +831,7 @@ int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *d, pcbqs_gb300_peec **o
     op.n_ = d->n; op.nb = d->nb; op.ne = d->ne; op.nn = d->nn;
     op.K = csr_of(d->K); op.Kt = csr_of(d->Kt); op.T = csr_of(d->T); op.Tt = csr_of(d->Tt); op.R = csr_of(d->R);
     op.L = d->L; op.ldl = d->ldl; op.P = d->P; op.ldp = d->ldp; op.is_tree = d->is_tree; op.pscale = d->pscale;
+    op.Pim = d->nn > 0 ? d->Pim : nullptr;
     op.nsys = d->nsys;
     std::vector<double> w(d->nsys), z(d->nsys), wa(d->nsys), iz(d->nsys), ip(d->nsys, 1.0 / d->pscale);
     for (int s = 0; s < d->nsys; ++s) {
@@ -851,15 +884,15 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t nblk = (op.n_ + bs - 1) / bs;
     const size_t bsz = (size_t)nblk * bs * bs;
-    double *klk = nullptr, *tpt = nullptr;
+    double *klk = nullptr, *tpt = nullptr, *tpt_im = nullptr;
     int *singular = nullptr;
     auto *bj = new (std::nothrow) BlockJacobi();
     if (!bj) return pfail(ERR_MEMORY, "block_jacobi: host allocation");
     bj->n = op.n_; bj->nblk = nblk; bj->bs = bs;
     cudaError_t e;
     if ((e = dev_alloc(&klk, bsz, st)) || (e = dev_alloc(&tpt, bsz, st)) || (e = dev_alloc(&singular, 1, st)) ||
-        (e = dev_alloc(&bj->inv, (size_t)op.nsys * bsz, st))) {
-        dev_free(klk, st); dev_free(tpt, st); dev_free(singular, st);
+        (e = dev_alloc(&bj->inv, (size_t)op.nsys * bsz, st)) || (op.Pim && (e = dev_alloc(&tpt_im, bsz, st)))) {
+        dev_free(klk, st); dev_free(tpt, st); dev_free(tpt_im, st); dev_free(singular, st);
         delete bj;
         return pfail(ERR_MEMORY, "block_jacobi: %s", cudaGetErrorString(e));
     }
@@ -867,16 +900,20 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     cudaMemsetAsync(tpt, 0, sizeof(double) * bsz, st);
     k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Kt, op.L, op.ldl, klk);
     if (op.nn > 0) k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Tt, op.P, op.ldp, tpt);
+    if (op.Pim) {
+        k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Tt, op.Pim, op.ldp, tpt_im);
+        note_launches(1);
+    }
     dim3 grid((unsigned)nblk, (unsigned)op.nsys);
     const size_t smem = sizeof(cd) * bs * 2 * bs;
     cudaFuncSetAttribute(k_block_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_block_invert<<<grid, 256, smem, st>>>(op.n_, bs, nblk, krk, klk, tpt, op.is_tree, op.omega, op.zscale,
-                                             op.rscale, op.pscale, bj->inv, singular);
+    k_block_invert<<<grid, 256, smem, st>>>(op.n_, bs, nblk, krk, klk, tpt, tpt_im, op.is_tree, op.omega,
+                                             op.zscale, op.rscale, op.pscale, bj->inv, singular);
     note_launches(op.nn > 0 ? 3 : 2);
     int sing = 0;
     cudaMemcpyAsync(&sing, singular, sizeof(int), cudaMemcpyDeviceToHost, st);
     e = cudaStreamSynchronize(st);
-    dev_free(klk, st); dev_free(tpt, st); dev_free(singular, st);
+    dev_free(klk, st); dev_free(tpt, st); dev_free(tpt_im, st); dev_free(singular, st);
     if (e) {
         delete bj;
         return pfail(ERR_CUDA, "block_jacobi: %s", cudaGetErrorString(e));
@@ -905,6 +942,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         double *w = nullptr, *wt = nullptr;
         const int64_t wcols = std::max(op.ne, op.nn);
         if ((e = dev_alloc(&h->klk, nn2, st)) || (e = dev_alloc(&h->tpt, nn2, st)) ||
+            (op.Pim && (e = dev_alloc(&h->tpt_im, nn2, st))) ||
             (e = dev_alloc(&w, (size_t)n * wcols, st)) || (e = dev_alloc(&wt, (size_t)n * wcols, st))) {
             dev_free(w, st);
             dev_free(wt, st);
@@ -921,6 +959,10 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         triple(op.Kt, op.L, op.ldl, op.ne, h->klk);
         if (op.nn > 0) {
             triple(op.Tt, op.P, op.ldp, op.nn, h->tpt);
+            if (op.Pim) {
+                triple(op.Tt, op.Pim, op.ldp, op.nn, h->tpt_im);
+                note_launches(3);
+            }
         } else {
             cudaMemsetAsync(h->tpt, 0, sizeof(double) * nn2, st);
         }
@@ -941,7 +983,8 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     cudaMemcpy(&w, op.omega + sys, sizeof(double), cudaMemcpyDeviceToHost);
     cudaMemcpy(&zs, op.zscale + sys, sizeof(double), cudaMemcpyDeviceToHost);
     Csr S = csr_of(*krk);
-    k_assemble_c64<<<grid_of((int64_t)nn2), 256, 0, st>>>(n, h->klk, h->tpt, op.is_tree, w, zs, op.pscale, lu->lu);
+    k_assemble_c64<<<grid_of((int64_t)nn2), 256, 0, st>>>(n, h->klk, h->tpt, h->tpt_im, op.is_tree, w, zs,
+                                                         op.pscale, lu->lu);
     k_add_krk_c64<<<grid_of(n), 256, 0, st>>>(S, op.is_tree, w, zs, op.pscale, op.rscale_host[sys], lu->lu);
     note_launches(2);
     if (cusolverDnCreate(&lu->solver) != CUSOLVER_STATUS_SUCCESS) {
@@ -1036,6 +1079,20 @@ int pcbqs_gb300_dense_apply(int64_t rows, int k, const double *M, int64_t ld, co
     return OK;
 }
 
+int pcbqs_gb300_dense_apply_single(int64_t rows, int k, const float *Mf, int64_t ld, const double *X, double *Y,
+                                   void *stream) {
+    if (rows <= 0 || k <= 0 || !Mf || ld < rows || !X || !Y)
+        return pfail(ERR_ARGUMENT, "dense_apply_single: invalid argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float *xf = nullptr;
+    cudaError_t e = dev_alloc(&xf, (size_t)rows * DENSE_NC, st);
+    if (e) return pfail(ERR_MEMORY, "dense_apply_single: %s", cudaGetErrorString(e));
+    e = dense_sym_apply<float, 4>(rows, k, Mf, ld, reinterpret_cast<const cd *>(X), reinterpret_cast<cd *>(Y), st, xf);
+    dev_free(xf, st);
+    if (e) return pfail(ERR_CUDA, "dense_apply_single: %s", cudaGetErrorString(e));
+    return OK;
+}
+
 int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *stream) {
     if (!in || !out || count < 0) return pfail(ERR_ARGUMENT, "to_single: invalid argument");
     if (!count) return OK;
@@ -1045,13 +1102,16 @@ int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *str
     return e ? pfail(ERR_CUDA, "to_single: %s", cudaGetErrorString(e)) : OK;
 }
 
-int pcbqs_gb300_peec_single(pcbqs_gb300_peec *h, const float *Lf, int64_t ldlf, const float *Pf, int64_t ldpf) {
+int pcbqs_gb300_peec_single(pcbqs_gb300_peec *h, const float *Lf, int64_t ldlf, const float *Pf, const float *Pfim,
+                            int64_t ldpf) {
     if (!h || !Lf || ldlf < h->op.ne || (h->op.nn > 0 && (!Pf || ldpf < h->op.nn)))
         return pfail(ERR_ARGUMENT, "peec_single: invalid single-precision matrices");
     h->op.Lf = Lf;
     h->op.ldlf = ldlf;
     h->op.Pf = Pf;
+    h->op.Pfim = Pfim;
     h->op.ldpf = ldpf;
+    if (h->op.Pim && !Pfim) return pfail(ERR_ARGUMENT, "peec_single: P is complex: its FP32 imaginary part is needed");
     return OK;
 }
 
@@ -1093,15 +1153,15 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *h, int k, const int32_t *sys_
     return OK;
 }
 
-int pcbqs_gb300_dense_gmres(int64_t n, const double *A, int64_t lda, int k, const double *b, double *x, double tol,
-                            int maxiter, int restart, int precondition, int32_t *iterations, double *residual,
-                            void *stream) {
+int pcbqs_gb300_dense_gmres(int64_t n, const double *A, const double *Aim, int64_t lda, int k, const double *b,
+                            double *x, double tol, int maxiter, int restart, int precondition, int32_t *iterations,
+                            double *residual, void *stream) {
     if (n <= 0 || !A || lda < n || k <= 0 || !b || !x || !(tol > 0) || maxiter <= 0 || restart <= 0 ||
         precondition < 0 || precondition > 1)
         return pfail(ERR_ARGUMENT, "dense_gmres: invalid argument");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     DenseSym op;
-    op.n_ = n; op.ld = lda; op.A = A;
+    op.n_ = n; op.ld = lda; op.A = A; op.Aim = Aim;
     Jacobi J;
     CholPrecond C;
     Preconditioner *M = nullptr;

@@ -200,15 +200,19 @@ class PeecTopology:
 
 
 class PeecModel(PeecTopology):
-    """A board's surface-charge PEEC model in a homogeneous dielectric, every port a 1 A current source from its
-    first to its second terminal (MQS.source), solved on the device."""
+    """A board's surface-charge PEEC model, every port a 1 A current source from its first to its second terminal
+    (MQS.source), solved on the device. The dielectric is homogeneous (board.er) unless `stack` (a
+    layered.DielectricStack) is given: then P comes from the stack's electrostatic images and is complex for a lossy
+    stack (MQS dielectric='stack', src/pcbqs/mqs.py:555-563)."""
 
     def __init__(self, board, near=3.0, outer_levels=1, device=0, block_size=32, tol=1e-8, maxiter=2000,
-                 restart=100, log=None, inner_tol=1e-4, conductor_loss='dc', conductor_faces=2):
+                 restart=100, log=None, inner_tol=1e-4, conductor_loss='dc', conductor_faces=2, stack=None):
         if conductor_loss not in ('dc', 'slab') or conductor_faces not in (1, 2):
             raise ValueError('conductor_loss must be dc or slab; conductor_faces must be 1 or 2')
         self.tol, self.maxiter, self.restart, self.inner_tol = tol, maxiter, restart, inner_tol
         self.conductor_loss, self.conductor_faces = conductor_loss, conductor_faces
+        self.stack = stack
+        self.Pim = self.Pfim = None
         self.device = torch.device('cuda', device)
         self.timings = {}
         t0 = time.perf_counter()
@@ -222,28 +226,40 @@ class PeecModel(PeecTopology):
         """Fill L and P on the device (moments, combine, aggregation); frees the moment planes. mixed=True: far
         pairs in FP32 local coordinates (near pairs FP64), FP32 combine; L and P kept in FP64 and FP32."""
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-        self.L = self.P = self.Lf = self.Pf = None
+        self.L = self.P = self.Lf = self.Pf = self.Pim = self.Pfim = None
         ev[0].record()
         if mixed:
             planes, analytic = self.fill.moments_local()
             ev[1].record()
             self.L, self.Lf = self.fill.inductance_local(planes)
             ev[2].record()
-            self.P, self.Pf = self.fill.potential_single(planes[0], self.board.node_of, self.board.er)
+            if self.stack is None:
+                self.P, self.Pf = self.fill.potential_single(planes[0], self.board.node_of, self.board.er)
         else:
             planes, analytic = self.fill.moments()
             ev[1].record()
             self.L = self.fill.inductance(planes)
             ev[2].record()
-            self.P = self.fill.potential(planes[0], self.board.node_of, self.board.er)
-        ev[3].record()
+            if self.stack is None:
+                self.P = self.fill.potential(planes[0], self.board.node_of, self.board.er)
         del planes
+        if self.stack is not None:
+            from .layered import LayeredPotential
+            lp = LayeredPotential(self.fill, self.stack, self.board.layer)
+            self.P, Pim = lp.potential_parts(self.board.node_of)
+            self.Pim = Pim if bool(Pim.any()) else None
+            if mixed:
+                self.Pf = self.P.float()
+                self.Pfim = self.Pim.float() if self.Pim is not None else None
+        ev[3].record()
         torch.cuda.synchronize()
         self.mixed_fill = mixed
         self.analytic = analytic
         self.timings.update(fill_ms=ev[0].elapsed_time(ev[1]), combine_ms=ev[1].elapsed_time(ev[2]),
                             potential_ms=ev[2].elapsed_time(ev[3]))
-        self.pscale = float(torch.diagonal(self.P).abs().max())
+        pdiag = torch.diagonal(self.P) if self.Pim is None else torch.complex(torch.diagonal(self.P),
+                                                                               torch.diagonal(self.Pim))
+        self.pscale = float(pdiag.abs().max())
         self.ldiag = torch.diagonal(self.L).cpu().numpy()
         self._pinvb = None
         return self
@@ -271,6 +287,7 @@ class PeecModel(PeecTopology):
         d.L, d.ldl, d.P, d.ldp = self.L.data_ptr(), self.L.stride(0), self.P.data_ptr(), self.P.stride(0)
         d.is_tree = self._dev['is_tree'].data_ptr()
         d.pscale = self.pscale
+        d.Pim = self.Pim.data_ptr() if self.Pim is not None else None
         d.nsys = len(omegas)
         self._omega = np.ascontiguousarray(omegas, float)
         self._zscale = np.ascontiguousarray(zscale, float)
@@ -324,7 +341,8 @@ class PeecModel(PeecTopology):
         its = np.zeros(k, np.int32)
         res = np.zeros(k)
         lib = _lib.load()
-        _lib.check(lib.pcbqs_gb300_dense_gmres(self.nn, self.P.data_ptr(), self.P.stride(0), k, b.data_ptr(),
+        Pim = self.Pim.data_ptr() if self.Pim is not None else None
+        _lib.check(lib.pcbqs_gb300_dense_gmres(self.nn, self.P.data_ptr(), Pim, self.P.stride(0), k, b.data_ptr(),
                                                x.data_ptr(), self.tol * 1e-2, 4000, self.restart, 1,
                                                _lib.ptr(its, ctypes.c_int32), _lib.ptr(res),
                                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
@@ -336,7 +354,8 @@ class PeecModel(PeecTopology):
         return self._dense(self.L, X)
 
     def _mv_P(self, X):
-        return self._dense(self.P, X)
+        Y = self._dense(self.P, X)
+        return Y if self.Pim is None else Y + 1j * self._dense(self.Pim, X)
 
     def _dense(self, M, X):
         Xt = torch.as_tensor(np.ascontiguousarray(X, complex), device=self.device)
@@ -431,15 +450,16 @@ class PeecModel(PeecTopology):
         outer_total = 0
         factored = None
         try:
-            if mode == 2:
-                # the first complex64 factorization depends only on L, P and the frequency: it runs on a side
-                # stream from a helper thread while this thread computes the equilibrium charge and the right-hand
-                # sides (the ctypes call releases the interpreter lock)
-                factored = self._factor_async(handle, groups[0][0], self.FACTOR_MATH[factor_math])
             t1 = time.perf_counter()
             baseline, qpart, vpart, source_voltage = self._equilibrium(excitation)
             t2 = time.perf_counter()
             self.timings.update(equilibrium_s=t2 - t1, operator_setup_s=t1 - t0)
+            if mode == 2:
+                # the first complex64 factorization depends only on L, P and the frequency: it runs on a side
+                # stream from a helper thread while this thread forms the right-hand sides and the single-precision
+                # copies (the ctypes call releases the interpreter lock). It starts after the equilibrium solve,
+                # whose triangular sweeps are cooperative kernels that must not share the device with other work.
+                factored = self._factor_async(handle, groups[0][0], self.FACTOR_MATH[factor_math])
             # rhs = -K^T (R + j w L) baseline / zscale, per (frequency, port) column, in the clustered order.
             Lb = self._mv_L(baseline[:self.ne])
             Rb = self.R @ baseline[:self.ne]
@@ -470,11 +490,16 @@ class PeecModel(PeecTopology):
                                lib)
                     _lib.check(lib.pcbqs_gb300_to_single(self.P.data_ptr(), Pf.data_ptr(), self.P.numel(), stream),
                                lib)
+                if self.Pim is not None and self.Pfim is None:
+                    self.Pfim = torch.empty(self.Pim.shape, dtype=torch.float32, device=self.device)
+                    _lib.check(lib.pcbqs_gb300_to_single(self.Pim.data_ptr(), self.Pfim.data_ptr(), self.Pim.numel(),
+                                                         stream), lib)
             if factored is not None:
                 precondition_ms += factored.result()
                 factored = None
             if mixed:
-                _lib.check(lib.pcbqs_gb300_peec_single(handle, Lf.data_ptr(), Lf.stride(0), Pf.data_ptr(),
+                Pfim = self.Pfim.data_ptr() if self.Pfim is not None else None
+                _lib.check(lib.pcbqs_gb300_peec_single(handle, Lf.data_ptr(), Lf.stride(0), Pf.data_ptr(), Pfim,
                                                        Pf.stride(0)), lib)
             converged = True
             for g, (anchor, members) in enumerate(groups):

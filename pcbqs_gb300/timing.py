@@ -2,6 +2,7 @@
 
     python -m pcbqs_gb300.timing fill <board> [triangles]   # mixed and FP64 fill of the first N triangles
     python -m pcbqs_gb300.timing lu <board> [k ...]          # the complex64 factor's triangular solves, k columns
+    python -m pcbqs_gb300.timing dense <n> [k]               # FP64 and FP32 symmetric dense products, n x n, k columns
 
 Times are CUDA-event times after a warm-up call; boards are the npz meshes of tests/golden (planes, strip, tiny).
 """
@@ -64,12 +65,38 @@ def lu(board, ks=(8,)):
         lib.pcbqs_gb300_peec_destroy(handle)
 
 
+def dense(n, k=8):
+    """A random symmetric n x n matrix (FP64 and its FP32 copy) against k complex columns."""
+    from . import _lib
+    n, k = int(n), int(k)
+    lib = _lib.load()
+    g = torch.Generator(device='cuda').manual_seed(1)
+    M = torch.rand((n, n), dtype=torch.float64, device='cuda', generator=g)
+    M = (M + M.T) / 2
+    Mf = M.float()
+    X = torch.randn((n, k), dtype=torch.complex128, device='cuda', generator=g)
+    Y = torch.empty_like(X)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for name, fn in (('fp64', lambda: lib.pcbqs_gb300_dense_apply(n, k, M.data_ptr(), n, X.data_ptr(), Y.data_ptr(),
+                                                                   stream)),
+                     ('fp32', lambda: lib.pcbqs_gb300_dense_apply_single(n, k, Mf.data_ptr(), n, X.data_ptr(),
+                                                                          Y.data_ptr(), stream))):
+        for _ in range(3):
+            ms, status = _event_ms(fn)
+            _lib.check(status, lib)
+            bytes_ = n * n * (8 if name == 'fp64' else 4)
+            print(f'dense {name} n={n} k={k}: {ms:.3f} ms, {bytes_ / ms / 1e6:.0f} GB/s of matrix, '
+                  f'{2 * n * n * 2 * k / ms / 1e9:.3f} TFLOP/s', flush=True)
+
+
 def main(argv):
-    if len(argv) < 2 or argv[0] not in ('fill', 'lu'):
+    if len(argv) < 2 or argv[0] not in ('fill', 'lu', 'dense'):
         print(__doc__)
         return 2
     if argv[0] == 'fill':
         fill(argv[1], argv[2] if len(argv) > 2 else None)
+    elif argv[0] == 'dense':
+        dense(argv[1], argv[2] if len(argv) > 2 else 8)
     else:
         lu(argv[1], tuple(int(v) for v in argv[2:]) or (8,))
     return 0

@@ -111,5 +111,24 @@ def main(boards=('tiny', 'strip'), losses=('dc', 'slab')):
         print(np.round(Z[1], 6))
 
 
+def stack(name='tiny', slab=(0.0, 0.2e-3, 4.3, 0.02)):
+    """peec_<board>_stack.npz: dielectric='stack' (electrostatic images of a lossy FR-4 slab between the two copper
+    layers, air outside; complex P), DC sheet resistance."""
+    from pcbqs_gb300.board import Board
+    b = Board.load(name)
+    q = reference_model(b)
+    from pcbqs.electrostatic import DielectricStack
+    z0, z1, er, tand = slab
+    q.dielectric = 'stack'
+    q._dielectric_stack = DielectricStack(np.array([z0, z1]), [1.0, er * (1 - 1j * tand), 1.0], tol=1e-8)
+    freqs = np.array([1e5, 1e6, 1e7])
+    names, Z, diag = port_matrix(q, b, freqs)
+    m = q._peec
+    np.savez_compressed(HERE / f'peec_{name}_stack.npz', freqs=freqs, ports=np.array(names), Z=Z, z_diag=diag,
+                        unknowns=m['K'].shape[1], loops=m['nl'], components=m['B'].shape[1], slab=np.array(slab))
+    print(name, 'stack', np.round(Z[1], 6))
+
+
 if __name__ == '__main__':
     main(tuple(sys.argv[1:]) or ('tiny', 'strip'))
+    stack('tiny')

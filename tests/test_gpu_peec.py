@@ -176,3 +176,25 @@ def test_slab_conductor_loss_matches_reference(device_library, board, mixed):
     assert (res.residual <= 1e-8).all()
     ratio = model.resistance_ratio(g['freqs'])
     assert ratio.real[-1] > ratio.real[0] >= 1.0         # skin effect raises the resistance with frequency
+
+
+@pytest.mark.parametrize('mixed', [False, True])
+def test_lossy_stack_dielectric_matches_reference(device_library, mixed):
+    """dielectric='stack': P from the electrostatic images of a lossy FR-4 slab (complex), through the operator, the
+    complex64 factor, the equilibrium solve (GMRES on the complex P preconditioned by Re P's Cholesky) and the
+    charge correction; port impedances against the reference's dense solve with the same stack, and the loss tangent
+    visible as Re Z / -Im Z."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.layered import DielectricStack
+    from pcbqs_gb300.peec import PeecModel
+    g = golden('tiny_stack')
+    z0, z1, er, tand = g['slab']
+    model = PeecModel(Board.load('tiny'), stack=DielectricStack.slab(z0, z1, er, tand))
+    res = model.solve(g['freqs'], precondition='lu32', mixed=mixed)
+    Z, Zr = res.impedance, g['Z']
+    assert np.abs(Z - Zr).max() / np.abs(Zr).max() < 1e-6
+    assert np.abs(Z.real - Zr.real).max() <= 1e-4 * np.abs(Zr.real).max() + 1e-9 * np.abs(Zr).max()
+    assert (res.residual <= 1e-8).all()
+    assert model.Pim is not None
+    ratio = Z[1, 0, 0].real / -Z[1, 0, 0].imag
+    assert 0.5 * tand < ratio < 2 * tand
