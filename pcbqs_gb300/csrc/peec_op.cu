@@ -3,13 +3,15 @@
 //
 // Operator (src/pcbqs/peec_iterative.py:267-278): for system s at angular frequency w_s,
 //   branch = K (D_s y),  D_s = diag(1 on loop unknowns, j w_s alpha_s on tree unknowns), alpha_s = zscale_s/pscale
-//   out    = K^T (R branch + j w_s L branch) / zscale_s + T^T P T y / pscale
+//   out    = K^T (r_s R branch + j w_s L branch) / zscale_s + T^T P T y / pscale
 // with K (branches x unknowns) the loop/tree basis, T = A K_tree (nodes x unknowns, zero on loop columns), R the
-// sparse sheet resistance and L, P the dense partial-inductance and potential matrices on the device. The two dense
-// products run as plain FP64 GEMMs (cuBLAS), every sparse product and combination in this file's kernels.
+// sparse sheet resistance (r_s its per-frequency factor, 1 at DC), L, P the dense partial-inductance and potential
+// matrices on the device (P complex, P_re + j P_im, for a lossy dielectric stack). The dense products run in this
+// file's symmetric dense kernels (FP64, or FP32 for the inner products of the mixed solve), every sparse product
+// and combination in its CSR kernels.
 //
 // Block-Jacobi: the unknowns are ordered so that consecutive runs of `bs` are geometric clusters; each diagonal
-// block of the operator, (K^T R K + j w K^T L K)_blk D_blk / zscale + (T^T P T)_blk / pscale, is formed on the
+// block of the operator, (r K^T R K + j w K^T L K)_blk D_blk / zscale + (T^T P T)_blk / pscale, is formed on the
 // device (K^T L K and T^T P T blocks gathered from the dense matrices), inverted (Gauss-Jordan with partial
 // pivoting), and applied to every column of its system.
 #include <algorithm>
@@ -472,8 +474,8 @@ struct PeecOp : Operator {
     const float *Lf = nullptr, *Pf = nullptr, *Pfim = nullptr;
     int64_t ldlf = 0, ldpf = 0;
 
-    // y (rows x k complex128) = M x for a dense symmetric M, in FP64 (cuBLAS DGEMM) or through its single-precision
-    // copy (SGEMM on converted vectors) when `single`.
+    // y (rows x k complex128) = M x for a dense symmetric M, in FP64 or through its single-precision copy when
+    // `single` (k_dense_sym_apply / k_dense_apply_f32).
     float *xf = nullptr;       // packed FP32 right-hand sides of the single-precision products
     int64_t capf = 0;
 

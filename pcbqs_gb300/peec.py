@@ -9,8 +9,10 @@ Host bookkeeping (sparse topology) restates the reference:
   sheet_resistance       src/pcbqs/mqs.py:478-515  (Gram matrix of the RWG functions at DC sheet resistance)
   prepare / solve        src/pcbqs/peec_iterative.py:127-161, 229-346 (loop/tree basis K, T = A K_tree,
                          components and equilibrium charge, scaled operator, currents, charges, source voltages)
-Device work (C ABI): the fill of L and P, the operator products, the block-Jacobi blocks and their inverses, and
-the batched GMRES; P^-1 B for the equilibrium split by the dense GMRES.
+Device work (C ABI): the fill of L and P (homogeneous, or the layered stack's images), the operator products, the
+block-Jacobi blocks and their inverses, the complex64 factor and its streaming triangular solves, the batched
+GMRES and the mixed-precision refinement; P^-1 B for the equilibrium split by the dense GMRES. The loop basis is
+native host code in the same library.
 """
 import concurrent.futures
 import ctypes
