@@ -120,9 +120,15 @@ def fill_roofline(model, fill_ms, mixed, peaks):
     else:
         peak, bound = peaks['fp64'], 'fp64'
         source = 'measured live: FP64 GEMM (cuBLAS DGEMM 8192^3) on this GPU'
+    # DRAM bytes (read + written) of the far-tile kernel per launch, from an ncu capture of the same kernel on the
+    # first 8,000 triangles of the plane pair (989.2 MB for its 32,004,000 unordered pairs: 30.9 B a pair against
+    # the 32 B of the four FP32 planes written once), scaled by this launch's pair count; the FP64 fill has no
+    # capture at a size above L2, so no figure
+    traffic = round(pairs * 989.2e6 / 32004000) if mixed else None
     return dict(bound=bound, kernel='k_fill_tiles+k_fill_near', achieved=round(achieved, 4), peak=round(peak, 4),
-                unit='TFLOP/s', frac=round(achieved / peak, 4), traffic=None, flops_per_launch=flops,
-                far_pairs=far, near_pairs=[near0, near1], peak_source=source)
+                unit='TFLOP/s', frac=round(achieved / peak, 4), traffic=traffic, flops_per_launch=flops,
+                far_pairs=far, near_pairs=[near0, near1], peak_source=source,
+                traffic_source='ncu dram bytes of k_fill_tiles on 8,000 triangles, scaled by pairs' if mixed else None)
 
 
 def gemm_peak(dtype):

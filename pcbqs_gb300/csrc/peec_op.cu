@@ -19,6 +19,8 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -347,7 +349,7 @@ __global__ void k_pack_x_f32(int64_t rows, const double *X, int xcols, int c0, i
     }
 }
 
-template <int RW>
+template <int RW, int U>
 __global__ void __launch_bounds__(256) k_dense_apply_f32(int64_t rows, const float *__restrict__ M, int64_t ld,
                                                          const float *__restrict__ Xf, int xcols, int c0, int nc,
                                                          double *__restrict__ Y) {
@@ -361,11 +363,11 @@ __global__ void __launch_bounds__(256) k_dense_apply_f32(int64_t rows, const flo
     const float *mrow[RW];
 #pragma unroll
     for (int r = 0; r < RW; ++r) mrow[r] = M + (r0 + r < rows ? r0 + r : 0) * ld;
-    for (int64_t i = lane; i < rows; i += 64) {
-        float mv[2][RW];
-        float4 xv[2][DENSE_NC / 4];
+    for (int64_t i = lane; i < rows; i += 32 * U) {
+        float mv[U][RW];
+        float4 xv[U][DENSE_NC / 4];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < U; ++u) {
             const int64_t iu = i + 32 * u;
             const bool in = iu < rows;
 #pragma unroll
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(256) k_dense_apply_f32(int64_t rows, const flo
             for (int q = 0; q < DENSE_NC / 4; ++q) xv[u][q] = in ? __ldg(xp + q) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
+        for (int u = 0; u < U; ++u)
 #pragma unroll
             for (int q = 0; q < DENSE_NC / 4; ++q)
 #pragma unroll
@@ -397,6 +399,70 @@ __global__ void __launch_bounds__(256) k_dense_apply_f32(int64_t rows, const flo
         }
 }
 
+// The FP32 product's shape (rows per warp RW, columns in flight per lane U) is chosen per device and matrix size
+// by timing the candidates once on first use (the pick is cached), since which of register reuse and loads in
+// flight limits it depends on the size.
+using DenseF32Kernel = void (*)(int64_t, const float *, int64_t, const float *, int, int, int, double *);
+struct DenseF32Variant {
+    int rw, u;
+    DenseF32Kernel kernel;
+};
+static const DenseF32Variant DENSE_F32_VARIANTS[] = {
+    {2, 2, k_dense_apply_f32<2, 2>}, {2, 4, k_dense_apply_f32<2, 4>}, {4, 1, k_dense_apply_f32<4, 1>},
+    {4, 2, k_dense_apply_f32<4, 2>}, {4, 4, k_dense_apply_f32<4, 4>}};
+constexpr int DENSE_F32_COUNT = sizeof(DENSE_F32_VARIANTS) / sizeof(DENSE_F32_VARIANTS[0]);
+
+static std::mutex g_dense_tune_mutex;
+static std::map<std::pair<int, int64_t>, int> g_dense_tune;     // (device, rows) -> variant
+
+static cudaError_t launch_dense_f32(int v, int64_t rows, const float *M, int64_t ld, const float *xf, int xcols,
+                                   int c0, int nc, double *Y, cudaStream_t s) {
+    const DenseF32Variant &d = DENSE_F32_VARIANTS[v];
+    const unsigned grid = (unsigned)((rows + 8 * d.rw - 1) / (8 * d.rw));
+    d.kernel<<<grid, 256, 0, s>>>(rows, M, ld, xf, xcols, c0, nc, Y);
+    return cudaGetLastError();
+}
+
+static cudaError_t tuned_dense_f32(int64_t rows, const float *M, int64_t ld, const float *xf, int xcols, int c0,
+                                   int nc, double *Y, cudaStream_t s, int &choice) {
+    int device = 0;
+    cudaGetDevice(&device);
+    {
+        std::lock_guard<std::mutex> lock(g_dense_tune_mutex);
+        auto it = g_dense_tune.find({device, rows});
+        if (it != g_dense_tune.end()) {
+            choice = it->second;
+            return cudaSuccess;
+        }
+    }
+    cudaEvent_t e0, e1;
+    cudaError_t e;
+    if ((e = cudaEventCreate(&e0)) || (e = cudaEventCreate(&e1))) return e;
+    float best = 1e30f;
+    choice = 0;
+    for (int v = 0; v < DENSE_F32_COUNT && !e; ++v) {
+        float ms = 0;
+        for (int rep = 0; rep < 2 && !e; ++rep) {      // the second run is timed
+            cudaEventRecord(e0, s);
+            e = launch_dense_f32(v, rows, M, ld, xf, xcols, c0, nc, Y, s);
+            cudaEventRecord(e1, s);
+            if (!e) e = cudaEventSynchronize(e1);
+            if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+        }
+        note_launches(2);
+        if (!e && ms < best) {
+            best = ms;
+            choice = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e) return e;
+    std::lock_guard<std::mutex> lock(g_dense_tune_mutex);
+    g_dense_tune[{device, rows}] = choice;
+    return cudaSuccess;
+}
+
 template <class T, int RW>
 static cudaError_t dense_sym_apply(int64_t rows, int k, const T *M, int64_t ld, const cd *X, cd *Y, cudaStream_t s,
                                    float *xf = nullptr) {
@@ -407,8 +473,12 @@ static cudaError_t dense_sym_apply(int64_t rows, int k, const T *M, int64_t ld, 
         if constexpr (std::is_same<T, float>::value) {
             k_pack_x_f32<<<grid_of(rows * DENSE_NC), 256, 0, s>>>(rows, reinterpret_cast<const double *>(X), xcols,
                                                                  c0, nc, xf);
-            k_dense_apply_f32<RW><<<grid, 256, 0, s>>>(rows, M, ld, xf, xcols, c0, nc, reinterpret_cast<double *>(Y));
-            note_launches(2);
+            note_launches(1);
+            int v = 0;
+            cudaError_t e = tuned_dense_f32(rows, M, ld, xf, xcols, c0, nc, reinterpret_cast<double *>(Y), s, v);
+            if (!e) e = launch_dense_f32(v, rows, M, ld, xf, xcols, c0, nc, reinterpret_cast<double *>(Y), s);
+            if (e) return e;
+            note_launches(1);
         } else {
             k_dense_sym_apply<T, RW><<<grid, 256, 0, s>>>(rows, M, ld, reinterpret_cast<const double *>(X), xcols,
                                                           c0, nc, reinterpret_cast<double *>(Y));
@@ -417,7 +487,6 @@ static cudaError_t dense_sym_apply(int64_t rows, int k, const T *M, int64_t ld, 
     }
     return cudaGetLastError();
 }
-
 
 // Device buffers come from the retained stream-ordered pool (pool.cuh): the dense blocks, factors and work arrays
 // of one solve are reused by the next instead of being mapped and unmapped each time. Buffers that outlive a call
