@@ -621,15 +621,22 @@ struct BlockJacobi : Preconditioner {
 // ---- dense loop/tree system and its single-precision LU (the MixedLU precedent, src/pcbqs/kernels.py:125-181) ----
 
 // out[j, c] = sum_{a in row j of St} St.val[a] M[St.idx[a], c]  for c < ncols: rows of M combined along the columns of
-// S (St = S^T in CSR). Grid: (column chunks, rows j).
+// S (St = S^T in CSR). Grid: (column chunks, rows j strided by gridDim.y).
 __global__ void k_rows_combine(Csr St, const double *M, int64_t ldm, int64_t ncols, double *out, int64_t ldo) {
-    const int64_t j = blockIdx.y;
-    const int64_t a0 = St.ptr[j], a1 = St.ptr[j + 1];
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncols; c += (int64_t)gridDim.x * blockDim.x) {
-        double acc = 0;
-        for (int64_t a = a0; a < a1; ++a) acc += St.val[a] * M[(int64_t)St.idx[a] * ldm + c];
-        out[j * ldo + c] = acc;
+    for (int64_t j = blockIdx.y; j < St.rows; j += gridDim.y) {
+        const int64_t a0 = St.ptr[j], a1 = St.ptr[j + 1];
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncols;
+             c += (int64_t)gridDim.x * blockDim.x) {
+            double acc = 0;
+            for (int64_t a = a0; a < a1; ++a) acc += St.val[a] * M[(int64_t)St.idx[a] * ldm + c];
+            out[j * ldo + c] = acc;
+        }
     }
+}
+
+// Grid of (x, rows) blocks with the row count within the launch limit; the kernels stride over the rows.
+static dim3 row_grid(unsigned x, int64_t rows) {
+    return dim3(x, (unsigned)std::min<int64_t>(std::max<int64_t>(rows, 1), 65535));
 }
 
 // out (cols x rows) = W^T for W (rows x cols, leading dimension ldw): 32 x 32 tiles through shared memory so that
@@ -648,25 +655,30 @@ __global__ void k_transpose(const double *W, int64_t rows, int64_t cols, int64_t
     }
 }
 
-// A[i, j] = (j w KLK[i,j]) d_j / zs + TPT[i,j] / ps as complex64, d_j = 1 (loop) or j w alpha (tree).
+// A[i, j] = (j w KLK[i,j]) d_j / zs + TPT[i,j] / ps as complex64, d_j = 1 (loop) or j w alpha (tree). Grid
+// (column chunks, rows strided by gridDim.y): no per-element division.
 __global__ void k_assemble_c64(int64_t n, const double *klk, const double *tpt, const double *tpt_im,
                                const int8_t *is_tree, double w, double zs, double ps, float2 *A) {
-    const int64_t total = n * n;
+  for (int64_t i = blockIdx.y; i < n; i += gridDim.y) {
     const double f = w * zs / ps;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = t / n, j = t % n;
-        double re = 0, im = w * klk[t] / zs;
-        if (is_tree[j]) {            // times j f
+    const bool tree_i = is_tree[i];
+    const double *krow = klk + i * n, *trow = tpt + i * n, *tirow = tpt_im ? tpt_im + i * n : nullptr;
+    float2 *arow = A + i * n;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        double re = 0, im = w * krow[j] / zs;
+        const bool tree_j = is_tree[j];
+        if (tree_j) {                // times j f
             const double r2 = -f * im;
             im = f * re;
             re = r2;
         }
-        if (is_tree[i] && is_tree[j]) {
-            re += tpt[t] / ps;
-            if (tpt_im) im += tpt_im[t] / ps;
+        if (tree_i && tree_j) {
+            re += trow[j] / ps;
+            if (tirow) im += tirow[j] / ps;
         }
-        A[t] = make_float2((float)re, (float)im);
+        arow[j] = make_float2((float)re, (float)im);
     }
+  }
 }
 
 // A[i, j] += KRK[i, j] d_j / zs for the sparse K^T R K.
@@ -748,10 +760,13 @@ struct LuPrecond : Preconditioner {
 // D = diag(L), so with M = P^T = P the column-major array holds the unit lower L D^-1 below the diagonal and the
 // upper D L^T on and above it (no pivoting), as complex64 with zero imaginary parts.
 __global__ void k_cholesky_to_lu(int64_t n, const float *chol, float2 *lu) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = t / n, i = t % n;            // column-major: t = i + j n
-        const float v = i > j ? chol[i + j * n] / chol[j + j * n] : chol[i + i * n] * chol[j + i * n];
-        lu[t] = make_float2(v, 0.f);
+    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {   // column j of the column-major arrays
+        const float djj = chol[j + j * n];
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+             i += (int64_t)gridDim.x * blockDim.x) {
+            const float v = i > j ? chol[i + j * n] / djj : chol[i + i * n] * chol[j + i * n];
+            lu[i + j * n] = make_float2(v, 0.f);
+        }
     }
 }
 
@@ -807,7 +822,7 @@ struct CholPrecond : Preconditioner {
         if (e || host_info) return e;
         // the factor in the triangular solver's layout; the FP32 copy is not needed afterwards
         if ((e = dev_alloc(&lu, (size_t)n * n, s)) || (e = dev_alloc(&ipiv, (size_t)n, s))) return e;
-        k_cholesky_to_lu<<<grid_of(n * n), 256, 0, s>>>(n, chol, lu);
+        k_cholesky_to_lu<<<row_grid((unsigned)std::min<int64_t>((n + 255) / 256, 8), n), 256, 0, s>>>(n, chol, lu);
         k_identity_pivots<<<grid_of(n), 256, 0, s>>>(n, ipiv);
         note_launches(2);
         if ((e = tri.prepare(lu, n, ipiv, s))) return e;
@@ -1020,7 +1035,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
             return pfail(ERR_MEMORY, "peec_factor: dense system blocks: %s", cudaGetErrorString(e));
         }
         const unsigned chunks = 8;
-        dim3 g1(chunks, (unsigned)n);
+        const dim3 g1 = row_grid(chunks, n);
         auto triple = [&](const Csr &St, const double *M, int64_t ldm, int64_t m, double *out) {
             k_rows_combine<<<g1, 256, 0, st>>>(St, M, ldm, m, w, m);
             dim3 gt((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
@@ -1054,8 +1069,8 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     cudaMemcpy(&w, op.omega + sys, sizeof(double), cudaMemcpyDeviceToHost);
     cudaMemcpy(&zs, op.zscale + sys, sizeof(double), cudaMemcpyDeviceToHost);
     Csr S = csr_of(*krk);
-    k_assemble_c64<<<grid_of((int64_t)nn2), 256, 0, st>>>(n, h->klk, h->tpt, h->tpt_im, op.is_tree, w, zs,
-                                                         op.pscale, lu->lu);
+    k_assemble_c64<<<row_grid((unsigned)std::min<int64_t>((n + 255) / 256, 8), n), 256, 0, st>>>(
+        n, h->klk, h->tpt, h->tpt_im, op.is_tree, w, zs, op.pscale, lu->lu);
     k_add_krk_c64<<<grid_of(n), 256, 0, st>>>(S, op.is_tree, w, zs, op.pscale, op.rscale_host[sys], lu->lu);
     note_launches(2);
     if (cusolverDnCreate(&lu->solver) != CUSOLVER_STATUS_SUCCESS) {

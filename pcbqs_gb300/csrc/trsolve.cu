@@ -26,6 +26,7 @@ constexpr int PANEL_ROWS = 4;                 // rows per thread block of the pa
 constexpr int PANEL_THREADS = 256;
 constexpr int MAX_SPLITS = 16;                // column runs per panel row group
 constexpr int PANEL_UNROLL = 4;               // columns per thread with loads in flight together
+constexpr int SYNC_STRIDE = 32;               // counters 128 B apart: pollers of one do not slow updates of another
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -280,8 +281,8 @@ struct SweepArgs {
     int kpad, c0;
     float2 *partial;       // [2][MAX_SPLITS + 1][B][KC]: the panel sums of two consecutive steps
     unsigned *barrier;     // grid barrier arrivals
-    unsigned *xready;      // [2] per sweep: diagonal quarters finished (4 per step)
-    unsigned *pdone;       // [2][nblk] per sweep and step: panel items finished
+    unsigned *xready;      // per sweep (stride SYNC_STRIDE): diagonal quarters finished (4 per step)
+    unsigned *pdone;       // per sweep and step (stride SYNC_STRIDE): panel items finished
     int *status;
 };
 
@@ -297,6 +298,7 @@ __device__ __forceinline__ bool wait_for(const unsigned *counter, unsigned targe
                 ok = 0;
                 break;
             }
+            __nanosleep(32);       // fewer polls on the counter's cache line while its producers update it
         }
     }
     __syncthreads();
@@ -363,7 +365,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
         const float2 *inv = dir == 0 ? a.inv_lower : a.inv_upper;
         const float2 *rhs = dir == 0 ? a.b : a.y;
         float2 *x = dir == 0 ? a.y : a.z;
-        unsigned *xready = a.xready + dir, *pdone = a.pdone + (size_t)dir * a.nblk;
+        unsigned *xready = a.xready + dir * SYNC_STRIDE, *pdone = a.pdone + (size_t)dir * a.nblk * SYNC_STRIDE;
         // bulk workers start with step 1's bulk (empty) and run one step ahead of the diagonal
         for (int step = 0; step < a.nblk; ++step) {
             const int J = dir == 0 ? step : a.nblk - 1 - step;
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
             if (diag) {
                 diag_stage(dsm, inv + (int64_t)J * B * B, rhs, row0, m, a.kpad, a.c0, role_id);
                 const unsigned need = (unsigned)(tail_runs * TAIL_BLOCKS + sc.bulk_runs * ((m + PANEL_ROWS - 1) / PANEL_ROWS));
-                if (need && !wait_for(pdone + step, need, a.status)) return;
+                if (need && !wait_for(pdone + (size_t)step * SYNC_STRIDE, need, a.status)) return;
                 diag_finish(dsm, slots, tail_runs + sc.bulk_runs, x, row0, m, a.kpad, a.c0, role_id);
                 signal(xready);
             } else if (tail) {
@@ -384,7 +386,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
                     if (!wait_for(xready, (unsigned)(DIAG_BLOCKS * step), a.status)) return;
                     panel_block(a.lu, a.n, row0, m, sc.tail0, sc.tail1, x, a.kpad, a.c0,
                                 slots + (size_t)sc.bulk_runs * B * KC, role_id - DIAG_BLOCKS);
-                    signal(pdone + step);
+                    signal(pdone + (size_t)step * SYNC_STRIDE);
                 }
             } else if (step + 1 < a.nblk) {
                 // the next step's bulk needs the blocks solved up to this step's predecessor
@@ -406,7 +408,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
                         panel_block(a.lu, a.n, rown, mn, nx.bulk0 + len * s / nx.bulk_runs,
                                     nx.bulk0 + len * (s + 1) / nx.bulk_runs, x, a.kpad, a.c0,
                                     nslots + (size_t)s * B * KC, item % mg);
-                        signal(pdone + step + 1);
+                        signal(pdone + (size_t)(step + 1) * SYNC_STRIDE);
                     }
                 }
             }
@@ -432,6 +434,9 @@ __global__ void k_tri_out(int64_t n, int k, int kpad, const float2 *z, const int
         out[t] = make_double2(v.x, v.y);
     }
 }
+
+// barrier, two solved-quarter counters and the status word, then one panel counter per sweep and step
+size_t sync_words(int nblk) { return (size_t)(4 + 2 * nblk) * SYNC_STRIDE; }
 
 unsigned blocks_for(int64_t work) {
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 8));
@@ -487,7 +492,7 @@ cudaError_t TriSolver::plan_for(int k, Plan **out) {
     if ((e = pool_alloc_n(&p.b, vec, nullptr)) || (e = pool_alloc_n(&p.y, vec, nullptr)) ||
         (e = pool_alloc_n(&p.z, vec, nullptr)) ||
         (e = pool_alloc_n(&p.partial, 2 * (size_t)(MAX_SPLITS + 1) * B * KC, nullptr)) ||
-        (e = pool_alloc_n(&p.sync, 4 + 2 * (size_t)nblk, nullptr)) || (e = cudaStreamSynchronize(nullptr))) {
+        (e = pool_alloc_n(&p.sync, sync_words(nblk), nullptr)) || (e = cudaStreamSynchronize(nullptr))) {
         for (float2 *q : {p.b, p.y, p.z, p.partial}) pool_free(q, nullptr);
         pool_free(p.sync, nullptr);
         return e;
@@ -513,14 +518,16 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
         grid = sms * per_sm;
     }
     k_tri_in<<<blocks_for(n * p->kpad), 256, 0, s>>>(n, k, p->kpad, in, p->b);
-    if ((e = cudaMemsetAsync(p->sync, 0, (4 + 2 * (size_t)nblk) * sizeof(unsigned), s))) return e;
+    if ((e = cudaMemsetAsync(p->sync, 0, sync_words(nblk) * sizeof(unsigned), s))) return e;
     for (int c0 = 0; c0 < p->kpad; c0 += KC) {
         // counters restart for every 8 columns; the status word [3] keeps the first failure
-        if (c0 && ((e = cudaMemsetAsync(p->sync, 0, 3 * sizeof(unsigned), s)) ||
-                   (e = cudaMemsetAsync(p->sync + 4, 0, 2 * (size_t)nblk * sizeof(unsigned), s))))
+        if (c0 && ((e = cudaMemsetAsync(p->sync, 0, 3 * SYNC_STRIDE * sizeof(unsigned), s)) ||
+                   (e = cudaMemsetAsync(p->sync + 4 * SYNC_STRIDE, 0,
+                                        (sync_words(nblk) - 4 * SYNC_STRIDE) * sizeof(unsigned), s))))
             return e;
         SweepArgs a{lu, n, nblk, inv_lower, inv_upper, p->b, p->y, p->z, p->kpad, c0, p->partial, p->sync,
-                    p->sync + 1, p->sync + 4, reinterpret_cast<int *>(p->sync + 3)};
+                    p->sync + SYNC_STRIDE, p->sync + 4 * SYNC_STRIDE,
+                    reinterpret_cast<int *>(p->sync + 3 * SYNC_STRIDE)};
         void *args[] = {&a};
         if ((e = cudaLaunchCooperativeKernel((const void *)k_tri_sweeps, dim3(grid), dim3(PANEL_THREADS), args, 0,
                                              s)))
@@ -530,7 +537,7 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
     note_launches(2 + p->kpad / KC);
     // a barrier that gave up leaves its status; the sweeps are then incomplete
     int status = 0;
-    if ((e = cudaMemcpyAsync(&status, p->sync + 3, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+    if ((e = cudaMemcpyAsync(&status, p->sync + 3 * SYNC_STRIDE, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
         return e;
     if (status) return cudaErrorLaunchTimeout;

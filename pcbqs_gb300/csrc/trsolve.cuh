@@ -27,7 +27,7 @@ struct TriSolver {
     struct Plan {
         int kpad = 0;
         float2 *b = nullptr, *y = nullptr, *z = nullptr, *partial = nullptr;
-        unsigned *sync = nullptr;     // [0] barrier, [1..2] solved quarters per sweep, [3] status, [4..] panel items
+        unsigned *sync = nullptr;     // barrier, solved quarters per sweep, status, panel items per step (padded)
     };
     std::map<int, Plan> plans;
     int grid = 0;                     // co-resident thread blocks of the sweep kernel
