@@ -45,8 +45,10 @@ def parse():
     p.add_argument('--board', default='planes')
     p.add_argument('--freq', type=float, default=1e6)
     p.add_argument('--precondition', default='lu32', choices=['lu32', 'block_jacobi'])
-    p.add_argument('--factor-math', default='bf16x9', choices=['fp32', 'bf16x9'],
-                   help='arithmetic of the lu32 factorization (bf16x9: FP32 emulated on the tensor cores)')
+    p.add_argument('--factor-math', default='bf16x9-blocked',
+                   choices=['fp32', 'bf16x9', 'bf16x9-blocked', 'fp32-blocked'],
+                   help='the lu32 factorization: cuSOLVER getrf or the blocked LU (-blocked), in FP32 or FP32 '
+                        'emulated on the tensor cores (bf16x9)')
     p.add_argument('--mode', default='mixed', choices=['mixed', 'fp64'],
                    help='mixed: FP32 far pairs in local coordinates and FP32 inner Krylov products under FP64 '
                         'refinement; fp64: the FP64 fill and FP64 GMRES')

@@ -1,0 +1,263 @@
+// Blocked complex64 LU with partial pivoting and one step of lookahead (pq::getrf_blocked, declared in getrf.cuh).
+//
+// Why not cusolverDnCgetrf on the whole matrix: its trailing updates are GEMMs with a small inner dimension, which
+// the BF16x9-emulated FP32 GEMM runs far below its rate (a 32k x 32k x 64 complex GEMM at 19 TFLOP/s against 141
+// at an inner dimension of 1024, measured on GB300), and its panel factorizations sit on the critical path. Here
+// the panels are 1024 columns wide, so each trailing update is one GEMM at the emulation's full rate, and the next
+// panel is factored on a second stream while the rest of the trailing matrix is updated.
+//
+// Step t (columns j .. j+jb of the n x n column-major matrix, rows j .. n):
+//   panel stream: getrf of the panel (cuSOLVER, pivots relative to row j) -> k_lu_pivot_plan turns the pivots into
+//                 global 1-based rows (the getrf convention) and the permutation of the rows they touch
+//   main stream:  k_lu_swap_rows applies that permutation to every other column; triangular solve for the block
+//                 row U12; GEMM of the next panel's columns; (event: the next panel may start); triangular solve
+//                 and GEMM of the remaining columns.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include "../../include/pcbqs_gb300.h"
+#include "common.cuh"
+#include "getrf.cuh"
+#include "pool.cuh"
+
+namespace pq {
+
+namespace {
+
+constexpr int MAX_BLOCK = MAX_BLOCK_PUBLIC;   // widest panel (the swap plan holds 2 * MAX_BLOCK rows)
+constexpr int PLAN = 2 * MAX_BLOCK;
+constexpr int HASH = 2 * MAX_BLOCK;        // open-addressing table of the rows below the panel (load <= 1/2)
+
+// The panel's pivots (1-based, relative to row j) become global rows (1-based, as getrf reports them), and the
+// sequence of swaps "row j+i <-> row piv[i]" becomes one permutation of the rows it touches: after it, row dst[e]
+// holds what row src[e] held before. Rows of the panel take slots 0 .. jb-1; rows below it get the next slots
+// through a small hash table. One block; the swap sequence itself is walked by one thread in shared memory.
+__global__ void k_lu_pivot_plan(int64_t n, int64_t j, int jb, int *ipiv, int *dst, int *src, int *count,
+                                int *error) {
+    __shared__ int keys[HASH], vals[HASH], content[PLAN], rows[PLAN], piv[MAX_BLOCK];
+    __shared__ int used;
+    for (int h = threadIdx.x; h < HASH; h += blockDim.x) keys[h] = -1;
+    for (int s = threadIdx.x; s < jb; s += blockDim.x) {
+        const int g = ipiv[j + s] + (int)j;
+        ipiv[j + s] = g;
+        piv[s] = g - 1;
+        content[s] = rows[s] = (int)j + s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int c = jb;
+        bool bad = false;
+        for (int i = 0; i < jb; ++i) {
+            const int p = piv[i];
+            if (p < j + i || p >= n) {              // not a row at or below row j+i: leave it, report
+                bad = true;
+                continue;
+            }
+            int sp;
+            if (p < j + jb) {
+                sp = p - (int)j;
+            } else {
+                int h = (int)(((unsigned)p * 2654435761u) & (HASH - 1));
+                while (keys[h] != -1 && keys[h] != p) h = (h + 1) & (HASH - 1);
+                if (keys[h] == -1) {
+                    keys[h] = p;
+                    vals[h] = c;
+                    content[c] = rows[c] = p;
+                    ++c;
+                }
+                sp = vals[h];
+            }
+            const int t = content[i];
+            content[i] = content[sp];
+            content[sp] = t;
+        }
+        used = c;
+        *count = c;
+        if (bad) atomicExch(error, 1);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < used; e += blockDim.x) {
+        dst[e] = rows[e];
+        src[e] = content[e];
+    }
+}
+
+// Applies the plan to the columns outside the panel, [0, j) and [j + jb, n): per column, every thread reads its
+// entries of the touched rows, the block synchronises, then writes them to their new rows.
+constexpr int SWAP_THREADS = 256;
+__global__ void __launch_bounds__(SWAP_THREADS) k_lu_swap_rows(int64_t n, int64_t j, int jb, float2 *A,
+                                                               const int *dst, const int *src, const int *count) {
+    __shared__ int sd[PLAN], ss[PLAN];
+    const int c = *count;
+    for (int e = threadIdx.x; e < c; e += blockDim.x) {
+        sd[e] = dst[e];
+        ss[e] = src[e];
+    }
+    __syncthreads();
+    const int64_t cols = n - jb;
+    for (int64_t q = blockIdx.x; q < cols; q += gridDim.x) {
+        const int64_t col = q < j ? q : q + jb;
+        float2 *a = A + col * n;
+        float2 v[PLAN / SWAP_THREADS];
+#pragma unroll
+        for (int r = 0; r < PLAN / SWAP_THREADS; ++r) {
+            const int e = threadIdx.x + r * SWAP_THREADS;
+            if (e < c) v[r] = a[ss[e]];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < PLAN / SWAP_THREADS; ++r) {
+            const int e = threadIdx.x + r * SWAP_THREADS;
+            if (e < c) a[sd[e]] = v[r];
+        }
+    }
+}
+
+struct Resources {
+    cublasHandle_t blas = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+    cudaStream_t panel = nullptr;
+    cudaEvent_t ready = nullptr, next = nullptr;
+    float2 *work = nullptr;
+    int *plan = nullptr, *info = nullptr;
+    cudaStream_t main = nullptr;
+    ~Resources() {
+        if (main) cudaStreamSynchronize(main);
+        if (panel) cudaStreamSynchronize(panel);
+        pool_free(work, main);
+        pool_free(plan, main);
+        pool_free(info, main);
+        if (blas) cublasDestroy(blas);
+        if (solver) cusolverDnDestroy(solver);
+        if (ready) cudaEventDestroy(ready);
+        if (next) cudaEventDestroy(next);
+        if (panel) cudaStreamDestroy(panel);
+    }
+};
+
+}  // namespace
+
+cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular) {
+    *singular = 0;
+    if (n <= 0 || n > (int64_t)0x7fffffff || !A || !ipiv || block < 32 || block > MAX_BLOCK ||
+        (math != LU_GEMM_FP32 && math != LU_GEMM_BF16X9))
+        return cudaErrorInvalidValue;
+    const int nb = (int)std::min<int64_t>(block, n);
+    const int64_t steps = (n + nb - 1) / nb;
+    Resources r;
+    r.main = stream;
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&r.panel, cudaStreamNonBlocking)) ||
+        (e = cudaEventCreateWithFlags(&r.ready, cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&r.next, cudaEventDisableTiming)))
+        return e;
+    if (cublasCreate(&r.blas) != CUBLAS_STATUS_SUCCESS || cusolverDnCreate(&r.solver) != CUSOLVER_STATUS_SUCCESS)
+        return cudaErrorNotSupported;
+    cublasSetStream(r.blas, stream);
+    cusolverDnSetStream(r.solver, r.panel);
+    cublasComputeType_t compute = CUBLAS_COMPUTE_32F;
+    if (math == LU_GEMM_BF16X9) {
+        if (cublasSetEmulationStrategy(r.blas, CUBLAS_EMULATION_STRATEGY_EAGER) != CUBLAS_STATUS_SUCCESS ||
+            cublasSetMathMode(r.blas, CUBLAS_FP32_EMULATED_BF16X9_MATH) != CUBLAS_STATUS_SUCCESS ||
+            cusolverDnSetMathMode(r.solver, CUSOLVER_FP32_EMULATED_BF16X9_MATH) != CUSOLVER_STATUS_SUCCESS)
+            return cudaErrorNotSupported;
+        compute = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+    }
+    int lwork = 0;
+    if (cusolverDnCgetrf_bufferSize(r.solver, (int)n, nb, reinterpret_cast<cuComplex *>(A), (int)n, &lwork) !=
+        CUSOLVER_STATUS_SUCCESS)
+        return cudaErrorUnknown;
+    // plan: dst (PLAN), src (PLAN), count, error
+    if ((e = pool_alloc_n(&r.work, (size_t)std::max(lwork, 1), stream)) ||
+        (e = pool_alloc_n(&r.plan, (size_t)2 * PLAN + 2, stream)) ||
+        (e = pool_alloc_n(&r.info, (size_t)steps, stream)))
+        return e;
+    int *dst = r.plan, *src = r.plan + PLAN, *count = r.plan + 2 * PLAN, *error = count + 1;
+    if ((e = cudaMemsetAsync(error, 0, sizeof(int), stream)) || (e = cudaMemsetAsync(r.info, 0, sizeof(int) * steps,
+                                                                                     stream)))
+        return e;
+    auto at = [&](int64_t row, int64_t col) { return A + row + col * n; };
+    const cuComplex one = {1.f, 0.f}, minus = {-1.f, 0.f};
+    int sms = 0, device = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    auto factor_panel = [&](int64_t j, int jb, int64_t t) -> cudaError_t {
+        if (cusolverDnCgetrf(r.solver, (int)(n - j), jb, reinterpret_cast<cuComplex *>(at(j, j)), (int)n,
+                             reinterpret_cast<cuComplex *>(r.work), ipiv + j, r.info + t) != CUSOLVER_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        k_lu_pivot_plan<<<1, 256, 0, r.panel>>>(n, j, jb, ipiv, dst, src, count, error);
+        note_launches(1);
+        return cudaEventRecord(r.ready, r.panel);
+    };
+    auto gemm = [&](int64_t rows, int64_t cols, int k, const float2 *a, const float2 *b, float2 *c) -> bool {
+        if (rows <= 0 || cols <= 0) return true;
+        return cublasGemmEx(r.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)rows, (int)cols, k, &minus, a, CUDA_C_32F, (int)n,
+                            b, CUDA_C_32F, (int)n, &one, c, CUDA_C_32F, (int)n, compute, CUBLAS_GEMM_DEFAULT) ==
+               CUBLAS_STATUS_SUCCESS;
+    };
+    auto trsm = [&](int64_t j, int jb, int64_t c0, int64_t cols) -> bool {
+        if (cols <= 0) return true;
+        return cublasCtrsm(r.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, jb,
+                           (int)cols, &one, reinterpret_cast<const cuComplex *>(at(j, j)), (int)n,
+                           reinterpret_cast<cuComplex *>(at(j, c0)), (int)n) == CUBLAS_STATUS_SUCCESS;
+    };
+    // the panel stream starts after what the main stream queued before (the matrix's assembly)
+    if ((e = cudaEventRecord(r.next, stream)) || (e = cudaStreamWaitEvent(r.panel, r.next, 0)) ||
+        (e = factor_panel(0, nb, 0)))
+        return e;
+    for (int64_t t = 0; t < steps; ++t) {
+        const int64_t j = t * nb;
+        const int jb = (int)std::min<int64_t>(nb, n - j);
+        const int64_t right = j + jb, rest = n - right;
+        const int jb2 = (int)std::min<int64_t>(nb, rest);
+        if ((e = cudaStreamWaitEvent(stream, r.ready, 0))) return e;
+        const unsigned blocks = (unsigned)std::min<int64_t>(std::max<int64_t>(n - jb, 1), (int64_t)sms * 8);
+        if (n > jb) {
+            k_lu_swap_rows<<<blocks, SWAP_THREADS, 0, stream>>>(n, j, jb, A, dst, src, count);
+            note_launches(1);
+        }
+        if (rest <= 0) break;
+        // next panel's columns first, so that its factorization overlaps the rest of the update
+        if (!trsm(j, jb, right, jb2) || !gemm(rest, jb2, jb, at(right, j), at(j, right), at(right, right)))
+            return cudaErrorUnknown;
+        if ((e = cudaEventRecord(r.next, stream)) || (e = cudaStreamWaitEvent(r.panel, r.next, 0)) ||
+            (e = factor_panel(right, jb2, t + 1)))
+            return e;
+        if (!trsm(j, jb, right + jb2, rest - jb2) ||
+            !gemm(rest, rest - jb2, jb, at(right, j), at(j, right + jb2), at(right, right + jb2)))
+            return cudaErrorUnknown;
+    }
+    if ((e = cudaGetLastError()) || (e = cudaStreamSynchronize(r.panel)) || (e = cudaStreamSynchronize(stream)))
+        return e;
+    std::vector<int> info((size_t)steps);
+    int bad = 0;
+    if ((e = cudaMemcpy(info.data(), r.info, sizeof(int) * steps, cudaMemcpyDeviceToHost)) ||
+        (e = cudaMemcpy(&bad, error, sizeof(int), cudaMemcpyDeviceToHost)))
+        return e;
+    if (bad) return cudaErrorIllegalState;
+    for (int64_t t = 0; t < steps; ++t)
+        if (info[t] > 0) {
+            *singular = (int)(t * nb + info[t]);
+            break;
+        }
+    return cudaSuccess;
+}
+
+}  // namespace pq
+
+extern "C" int pcbqs_gb300_lu_factor_c64(int64_t n, void *a, int32_t *ipiv, int block, int math, int32_t *singular,
+                                         void *stream) {
+    if (n <= 0 || !a || !ipiv || !singular || block < 32 || block > pq::MAX_BLOCK_PUBLIC || (math != 0 && math != 1))
+        return pq::fail(pq::ERR_ARGUMENT, "lu_factor_c64: invalid argument (block 32..%d, math 0 or 1)",
+                        pq::MAX_BLOCK_PUBLIC);
+    int zero = 0;
+    const cudaError_t e = pq::getrf_blocked(n, static_cast<float2 *>(a), ipiv, block, math,
+                                            static_cast<cudaStream_t>(stream), &zero);
+    *singular = zero;
+    if (e) return pq::fail(pq::ERR_CUDA, "lu_factor_c64: %s", cudaGetErrorString(e));
+    return pq::OK;
+}

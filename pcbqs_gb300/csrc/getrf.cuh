@@ -1,0 +1,27 @@
+// Blocked complex64 LU with partial pivoting, in cuSOLVER getrf's column-major layout and pivot convention.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace pq {
+
+// Trailing-update arithmetic of the blocked LU.
+enum LuMath : int {
+    LU_GEMM_FP32 = 0,      // FP32 GEMMs on the CUDA cores
+    LU_GEMM_BF16X9 = 1,    // FP32 GEMMs emulated on the tensor cores with three BF16 terms per operand
+};
+
+// Factors the n x n column-major complex64 matrix A (leading dimension n) in place as P A = L U, L unit lower,
+// with ipiv[i] the 1-based row swapped with row i (the same layout and pivots as cusolverDnCgetrf, so the
+// triangular solvers of that factor apply unchanged). Right-looking in `block`-column panels: each panel is
+// factored by cuSOLVER on a second stream while the main stream finishes the previous step's trailing update
+// (one step of lookahead), its row swaps are applied to the other columns by a gather kernel, the block row of U
+// comes from a triangular solve and the trailing matrix from one large GEMM (`math`). Returns cudaSuccess, or an
+// error; *singular = the first zero pivot's 1-based index (0 if none). Ordered on `stream`; returns after the
+// factor is complete.
+constexpr int MAX_BLOCK_PUBLIC = 1024;   // widest panel getrf_blocked takes
+
+cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular);
+
+}  // namespace pq

@@ -30,6 +30,7 @@
 
 #include "../../include/pcbqs_gb300.h"
 #include "common.cuh"
+#include "getrf.cuh"
 #include "pool.cuh"
 #include "solve.cuh"
 #include "trsolve.cuh"
@@ -889,6 +890,7 @@ struct pcbqs_gb300_peec {
 
 namespace {
 #define pfail pq::fail
+constexpr int LU_BLOCK = 1024;     // panel width of the blocked factorization (math 2 and 3)
 Csr csr_of(const pcbqs_gb300_csr &c) {
     Csr out;
     out.rows = c.rows;
@@ -1015,7 +1017,8 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
 
 int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream) {
     if (!h || !krk || sys < 0 || sys >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_factor: invalid argument");
-    if (math != 0 && math != 1) return pfail(ERR_ARGUMENT, "peec_factor: math 0 (FP32) or 1 (BF16x9 FP32 emulation)");
+    if (math < 0 || math > 3)
+        return pfail(ERR_ARGUMENT, "peec_factor: math 0/1 (cuSOLVER getrf, FP32/BF16x9) or 2/3 (blocked, BF16x9/FP32)");
     PeecOp &op = h->op;
     const int64_t n = op.n_;
     if (krk->rows != n || krk->cols != n) return pfail(ERR_ARGUMENT, "peec_factor: K^T R K must be n x n");
@@ -1078,6 +1081,22 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         return pfail(ERR_CUDA, "peec_factor: cuSOLVER handle");
     }
     cusolverDnSetStream(lu->solver, st);
+    if (math >= 2) {
+        int singular = 0;
+        e = getrf_blocked(n, lu->lu, lu->ipiv, LU_BLOCK, math == 2 ? LU_GEMM_BF16X9 : LU_GEMM_FP32, st, &singular);
+        if (e || singular) {
+            delete lu;
+            return pfail(singular ? ERR_NONFINITE : ERR_CUDA, "peec_factor: blocked getrf failed (zero pivot %d, %s)",
+                         singular, cudaGetErrorString(e));
+        }
+        if ((e = lu->tri.prepare(lu->lu, n, lu->ipiv, st))) {
+            delete lu;
+            return pfail(ERR_CUDA, "peec_factor: triangular-solve set-up: %s", cudaGetErrorString(e));
+        }
+        delete h->lu;
+        h->lu = lu;
+        return OK;
+    }
     if (math == 1 && cusolverDnSetMathMode(lu->solver, CUSOLVER_FP32_EMULATED_BF16X9_MATH) != CUSOLVER_STATUS_SUCCESS) {
         delete lu;
         return pfail(ERR_CUDA, "peec_factor: BF16x9 emulation unavailable in this cuSOLVER");

@@ -406,16 +406,18 @@ class PeecModel(PeecTopology):
             return e0.elapsed_time(e1)
         return self._pool.submit(work)
 
-    FACTOR_MATH = {'fp32': 0, 'bf16x9': 1}
+    FACTOR_MATH = {'fp32': 0, 'bf16x9': 1, 'bf16x9-blocked': 2, 'fp32-blocked': 3}
 
-    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='bf16x9', anchors=None):
+    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='bf16x9-blocked', anchors=None):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
 
         precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
         dense loop/tree system), or 'none'. mixed=False: FP64 GMRES on the FP64 operator; mixed=True: FP64
         iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose dense products run
         in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of the 'lu32'
-        factorization, 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy). anchors ('lu32'
+        factorization: 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy) through cuSOLVER's getrf,
+        'fp32-blocked' or 'bf16x9-blocked' through this library's blocked LU (1024-column panels factored ahead of
+        the trailing GEMMs). anchors ('lu32'
         only): how many factorizations a sweep shares; the frequencies, in increasing order, are split into that
         many runs and every run is solved as one batch of (frequency, port) columns preconditioned by the factor
         at its middle frequency (default: one factor per frequency). Every column still reaches the tolerance of

@@ -3,6 +3,7 @@
     python -m pcbqs_gb300.timing fill <board> [triangles]   # mixed and FP64 fill of the first N triangles
     python -m pcbqs_gb300.timing lu <board> [k ...]          # the complex64 factor's triangular solves, k columns
     python -m pcbqs_gb300.timing dense <n> [k]               # FP64 and FP32 symmetric dense products, n x n, k columns
+    python -m pcbqs_gb300.timing getrf <n> [block ...]       # the blocked complex64 LU of a random n x n matrix
 
 Times are CUDA-event times after a warm-up call; boards are the npz meshes of tests/golden (planes, strip, tiny).
 """
@@ -51,9 +52,10 @@ def lu(board, ks=(8,)):
     handle, _ = m._operator(np.array([2 * np.pi * 1e6]))
     try:
         desc = _csr_struct(m._krk_device())
-        ms, _ = _event_ms(lambda: _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, 1, stream),
-                                             lib))
-        print(f'factor n={m.n}: {ms:.1f} ms', flush=True)
+        for math in (1, 2, 3):
+            ms, _ = _event_ms(lambda: _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, math,
+                                                                             stream), lib))
+            print(f'factor n={m.n} math {math}: {ms:.1f} ms', flush=True)
         for k in ks:
             x = torch.randn(m.n, k, dtype=torch.complex128, device='cuda')
             y = torch.empty_like(x)
@@ -63,6 +65,29 @@ def lu(board, ks=(8,)):
                 print(f'lu_solve k={k}: {ms:.2f} ms', flush=True)
     finally:
         lib.pcbqs_gb300_peec_destroy(handle)
+
+
+def getrf(n, blocks=(1024,)):
+    """The blocked complex64 LU of a random n x n matrix with each panel width, BF16x9 and FP32 GEMMs."""
+    from . import _lib
+    n = int(n)
+    lib = _lib.load()
+    g = torch.Generator(device='cuda').manual_seed(1)
+    A = torch.complex(torch.randn(n, n, device='cuda', generator=g), torch.randn(n, n, device='cuda', generator=g))
+    F = torch.empty_like(A)
+    piv = torch.zeros(n, dtype=torch.int32, device='cuda')
+    singular = ctypes.c_int32(0)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    flops = 8 / 3 * n ** 3
+    for block in blocks:
+        for math in (1, 0):
+            for _ in range(2):
+                F.copy_(A)
+                ms, status = _event_ms(lambda: lib.pcbqs_gb300_lu_factor_c64(n, F.data_ptr(), piv.data_ptr(), block,
+                                                                             math, ctypes.byref(singular), stream))
+                _lib.check(status, lib)
+                print(f'getrf n={n} block {block} math {math}: {ms:.1f} ms, {flops / ms / 1e9:.1f} TFLOP/s',
+                      flush=True)
 
 
 def dense(n, k=8):
@@ -90,11 +115,13 @@ def dense(n, k=8):
 
 
 def main(argv):
-    if len(argv) < 2 or argv[0] not in ('fill', 'lu', 'dense'):
+    if len(argv) < 2 or argv[0] not in ('fill', 'lu', 'dense', 'getrf'):
         print(__doc__)
         return 2
     if argv[0] == 'fill':
         fill(argv[1], argv[2] if len(argv) > 2 else None)
+    elif argv[0] == 'getrf':
+        getrf(argv[1], tuple(int(v) for v in argv[2:]) or (1024,))
     elif argv[0] == 'dense':
         dense(argv[1], argv[2] if len(argv) > 2 else 8)
     else:

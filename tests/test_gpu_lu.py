@@ -1,0 +1,85 @@
+"""pcbqs_gb300_lu_factor_c64, the blocked complex64 LU (panels factored one step ahead of the trailing GEMMs),
+against the definition P A = L U and against cuSOLVER's own getrf (torch.linalg.lu_factor) on the same matrix.
+Both are FP32 factorizations, so the bar is the backward error: ours no worse than 4x the library's, and a
+solve through the standard getrs convention (torch.linalg.lu_solve with our factor and pivots) at FP32 accuracy."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _factor(lib, A, block, math):
+    """Our factor of the complex64 (n, n) torch matrix A: (LU as the matrix (n, n), 1-based pivots)."""
+    import torch
+    from pcbqs_gb300 import _lib
+    n = A.shape[0]
+    F = A.T.contiguous()                 # row-major A^T = column-major A, what getrf takes
+    piv = torch.zeros(n, dtype=torch.int32, device=A.device)
+    singular = ctypes.c_int32(-1)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.pcbqs_gb300_lu_factor_c64(n, F.data_ptr(), piv.data_ptr(), block, math, ctypes.byref(singular),
+                                             stream), lib)
+    assert singular.value == 0
+    return F.T.contiguous(), piv
+
+
+def _backward_error(A, LU, piv):
+    import torch
+    n = A.shape[0]
+    L = torch.tril(LU, -1).to(torch.complex128) + torch.eye(n, dtype=torch.complex128, device=A.device)
+    U = torch.triu(LU).to(torch.complex128)
+    perm = list(range(n))
+    for i, p in enumerate(piv.cpu().tolist()):
+        perm[i], perm[p - 1] = perm[p - 1], perm[i]
+    PA = A.to(torch.complex128)[torch.as_tensor(perm, device=A.device)]
+    return (torch.linalg.norm(PA - L @ U) / torch.linalg.norm(A.to(torch.complex128))).item()
+
+
+@pytest.mark.parametrize('n,block,math', [(300, 64, 0), (1000, 128, 1), (1000, 1000, 1), (2100, 256, 1),
+                                          (2100, 1024, 0), (4097, 512, 1)])
+def test_blocked_lu_matches_getrf(device_library, n, block, math):
+    import torch
+    g = torch.Generator(device='cuda').manual_seed(n + block)
+    A = torch.complex(torch.randn(n, n, device='cuda', generator=g), torch.randn(n, n, device='cuda', generator=g))
+    LU, piv = _factor(device_library, A, block, math)
+    p = piv.cpu().numpy()
+    assert torch.isfinite(torch.view_as_real(LU)).all()
+    assert ((p >= np.arange(1, n + 1)) & (p <= n)).all()          # pivot rows at or below their step
+    ours = _backward_error(A, LU, piv)
+    LUr, pivr = torch.linalg.lu_factor(A)
+    theirs = _backward_error(A, LUr, pivr)
+    assert ours <= 4 * theirs + 1e-7, (ours, theirs)
+    b = torch.complex(torch.randn(n, 3, device='cuda', generator=g), torch.randn(n, 3, device='cuda', generator=g))
+    x = torch.linalg.lu_solve(LU, piv, b)
+    xr = torch.linalg.lu_solve(LUr, pivr, b)
+    res = (torch.linalg.norm(A @ x - b) / torch.linalg.norm(b)).item()
+    resr = (torch.linalg.norm(A @ xr - b) / torch.linalg.norm(b)).item()
+    assert res <= 4 * resr + 1e-6, (res, resr)
+
+
+def test_blocked_lu_is_deterministic(device_library):
+    import torch
+    g = torch.Generator(device='cuda').manual_seed(7)
+    n = 1500
+    A = torch.complex(torch.randn(n, n, device='cuda', generator=g), torch.randn(n, n, device='cuda', generator=g))
+    LU1, p1 = _factor(device_library, A, 256, 1)
+    LU2, p2 = _factor(device_library, A, 256, 1)
+    assert torch.equal(p1, p2)
+    assert torch.equal(torch.view_as_real(LU1), torch.view_as_real(LU2))
+
+
+def test_blocked_lu_rejects_bad_block(device_library):
+    import torch
+    from pcbqs_gb300 import _lib
+    A = torch.eye(64, dtype=torch.complex64, device='cuda')
+    piv = torch.zeros(64, dtype=torch.int32, device='cuda')
+    singular = ctypes.c_int32(0)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for block in (16, 2048):
+        status = device_library.pcbqs_gb300_lu_factor_c64(64, A.data_ptr(), piv.data_ptr(), block, 1,
+                                                          ctypes.byref(singular), stream)
+        assert status == 1
+        with pytest.raises(ValueError, match='block'):
+            _lib.check(status, device_library)

@@ -99,11 +99,13 @@ def test_planes_mixed_and_fp64_solves_agree(device_library):
     assert (np.diag(Z64).real > 0).all() and (np.diag(Z64).imag < 0).all()     # capacitive plane pair at 1 MHz
 
 
-@pytest.mark.parametrize('board,k', [('tiny', 3), ('strip', 8), ('strip', 11)])
-def test_streaming_triangular_solves_match_getrs(device_library, board, k):
+@pytest.mark.parametrize('board,k,math', [('tiny', 3, 0), ('strip', 8, 0), ('strip', 11, 0), ('strip', 8, 2),
+                                          ('strip', 11, 3)])
+def test_streaming_triangular_solves_match_getrs(device_library, board, k, math):
     """The library's streaming solve with the complex64 factor (super-block panels, inverted diagonal blocks, one
     gather for the row interchanges) against cuSOLVER getrs on the same factor; k = 11 exercises a padded second
-    sweep of 8 columns. Both are FP32 solves in a different order, so they differ by FP32 rounding amplified by
+    sweep of 8 columns. math 2 and 3 factor with the library's blocked LU (three 1024-column panels on the strip),
+    so getrs on its output also checks that it keeps getrf's layout and pivots. Both are FP32 solves in a different order, so they differ by FP32 rounding amplified by
     the factor's conditioning; the bar is the quantity GMRES cares about, the residual of the FP64 system, which
     over the batch must be no worse than getrs's (within 50 %)."""
     import torch
@@ -117,7 +119,7 @@ def test_streaming_triangular_solves_match_getrs(device_library, board, k):
     sys = np.zeros(k, np.int32)
     try:
         desc = _csr_struct(model._krk_device())
-        _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, 0, stream), lib)
+        _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, math, stream), lib)
         rng = np.random.default_rng(k)
         b = torch.as_tensor(rng.standard_normal((model.n, k)) + 1j * rng.standard_normal((model.n, k)), device='cuda')
         outs, residuals = [], []
