@@ -250,17 +250,24 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *op, int32_t bs, const double
  * (K^T L K and T^T P T formed once from the dense L and P; krk the sparse K^T R K as a device CSR n x n), in
  * complex64 and LU-factored. math 0: cuSOLVER getrf in FP32 arithmetic; math 1: cuSOLVER getrf, FP32 emulated with
  * BF16x9 products on the tensor cores (same FP32 accuracy); math 2 / 3: this library's blocked factorization
- * (pcbqs_gb300_lu_factor_c64, 1024-column panels) with BF16x9 / FP32 GEMMs. Mirrors MixedLU (src/pcbqs/kernels.py:125-181): a complex64 factor
+ * (pcbqs_gb300_lu_factor_c64, 2048-column panels) with BF16x9 / FP32 GEMMs. Mirrors MixedLU (src/pcbqs/kernels.py:125-181): a complex64 factor
  * with the FP64 operator's GMRES on top in place of its refinement loop. */
 int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream);
 /* Dense complex64 LU with partial pivoting of the n x n column-major device matrix a (leading dimension n), in
  * place, ipiv (device, n) receiving 1-based pivot rows: cusolverDnCgetrf's layout and pivots, so getrs and this
- * library's triangular solvers apply to it. Blocked: `block`-column panels (32 .. 1024) factored on a second stream
+ * library's triangular solvers apply to it. Blocked: `block`-column panels (32 .. 4096) factored on a second stream
  * one step ahead of the trailing GEMMs; math 0: FP32 GEMMs, 1: FP32 GEMMs emulated with BF16x9 on the tensor cores.
  * *singular (host) = 1-based index of the first exactly zero pivot, 0 if none. Synchronizes `stream`. The factor
  * step of MixedLU and lu_factor_rows (src/pcbqs/kernels.py:125-160, :266-285), which LAPACK's cgetrf does there. */
 int pcbqs_gb300_lu_factor_c64(int64_t n, void *a, int32_t *ipiv, int block, int math, int32_t *singular,
                               void *stream);
+/* Dense FP32 Cholesky a = L L^T of the n x n column-major symmetric positive definite device matrix a (leading
+ * dimension n, lower triangle read and overwritten by L; the strict upper triangle is left with intermediate
+ * values), blocked like pcbqs_gb300_lu_factor_c64 (block 32 .. 4096, math 0: FP32 GEMMs, 1: BF16x9). *info
+ * (host) = order of the first leading minor that is not positive definite, 0 if none. Synchronizes `stream`. No
+ * counterpart in the reference: it is the factor of P behind pcbqs_gb300_dense_gmres's preconditioner, exported so
+ * it can be checked on its own. */
+int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int block, int math, int32_t *info, void *stream);
 /* out = (complex64 factor)^-1 in for k complex128 columns (n, k) row-major, device arrays; the solve step of
  * MixedLU (src/pcbqs/kernels.py:160-181) without its refinement. method 0: this library's streaming triangular
  * solves (what GMRES uses); method 1: cuSOLVER getrs on the same factor (for validation). Synchronizes `stream`. */

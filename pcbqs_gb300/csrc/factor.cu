@@ -1,10 +1,12 @@
-// Blocked complex64 LU with partial pivoting and one step of lookahead (pq::getrf_blocked, declared in getrf.cuh).
+// Blocked dense factorizations with one step of lookahead (declared in factor.cuh): the complex64 LU with partial
+// pivoting (pq::getrf_blocked) and the FP32 Cholesky (pq::potrf_blocked).
 //
 // Why not cusolverDnCgetrf on the whole matrix: its trailing updates are GEMMs with a small inner dimension, which
 // the BF16x9-emulated FP32 GEMM runs far below its rate (a 32k x 32k x 64 complex GEMM at 19 TFLOP/s against 141
 // at an inner dimension of 1024, measured on GB300), and its panel factorizations sit on the critical path. Here
-// the panels are 1024 columns wide, so each trailing update is one GEMM at the emulation's full rate, and the next
-// panel is factored on a second stream while the rest of the trailing matrix is updated.
+// the panels are wide (2048 columns in the PEEC factor), so each trailing update is one GEMM near the emulation's
+// full rate, and the next panel is factored on a second, high-priority stream while the rest of the trailing
+// matrix is updated.
 //
 // Step t (columns j .. j+jb of the n x n column-major matrix, rows j .. n):
 //   panel stream: getrf of the panel (cuSOLVER, pivots relative to row j) -> k_lu_pivot_plan turns the pivots into
@@ -21,7 +23,7 @@
 
 #include "../../include/pcbqs_gb300.h"
 #include "common.cuh"
-#include "getrf.cuh"
+#include "factor.cuh"
 #include "pool.cuh"
 
 namespace pq {
@@ -36,9 +38,12 @@ constexpr int HASH = 2 * MAX_BLOCK;        // open-addressing table of the rows 
 // sequence of swaps "row j+i <-> row piv[i]" becomes one permutation of the rows it touches: after it, row dst[e]
 // holds what row src[e] held before. Rows of the panel take slots 0 .. jb-1; rows below it get the next slots
 // through a small hash table. One block; the swap sequence itself is walked by one thread in shared memory.
+constexpr size_t PLAN_SMEM = sizeof(int) * (2 * HASH + 2 * PLAN + MAX_BLOCK);
+
 __global__ void k_lu_pivot_plan(int64_t n, int64_t j, int jb, int *ipiv, int *dst, int *src, int *count,
                                 int *error) {
-    __shared__ int keys[HASH], vals[HASH], content[PLAN], rows[PLAN], piv[MAX_BLOCK];
+    extern __shared__ int plan_smem[];
+    int *keys = plan_smem, *vals = keys + HASH, *content = vals + HASH, *rows = content + PLAN, *piv = rows + PLAN;
     __shared__ int used;
     for (int h = threadIdx.x; h < HASH; h += blockDim.x) keys[h] = -1;
     for (int s = threadIdx.x; s < jb; s += blockDim.x) {
@@ -88,10 +93,12 @@ __global__ void k_lu_pivot_plan(int64_t n, int64_t j, int jb, int *ipiv, int *ds
 
 // Applies the plan to the columns outside the panel, [0, j) and [j + jb, n): per column, every thread reads its
 // entries of the touched rows, the block synchronises, then writes them to their new rows.
-constexpr int SWAP_THREADS = 256;
+constexpr int SWAP_THREADS = 512;
+constexpr size_t SWAP_SMEM = sizeof(int) * 2 * PLAN;
 __global__ void __launch_bounds__(SWAP_THREADS) k_lu_swap_rows(int64_t n, int64_t j, int jb, float2 *A,
                                                                const int *dst, const int *src, const int *count) {
-    __shared__ int sd[PLAN], ss[PLAN];
+    extern __shared__ int swap_smem[];
+    int *sd = swap_smem, *ss = swap_smem + PLAN;
     const int c = *count;
     for (int e = threadIdx.x; e < c; e += blockDim.x) {
         sd[e] = dst[e];
@@ -115,6 +122,15 @@ __global__ void __launch_bounds__(SWAP_THREADS) k_lu_swap_rows(int64_t n, int64_
             if (e < c) a[sd[e]] = v[r];
         }
     }
+}
+
+// The stream of the panel factorizations, at the device's highest priority: their small latency-bound kernels
+// then take SMs as soon as the trailing GEMM's blocks retire, instead of queueing behind its later waves.
+cudaError_t panel_stream(cudaStream_t *stream) {
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e) return e;
+    return cudaStreamCreateWithPriority(stream, cudaStreamNonBlocking, greatest);
 }
 
 struct Resources {
@@ -151,8 +167,7 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
     Resources r;
     r.main = stream;
     cudaError_t e;
-    if ((e = cudaStreamCreateWithFlags(&r.panel, cudaStreamNonBlocking)) ||
-        (e = cudaEventCreateWithFlags(&r.ready, cudaEventDisableTiming)) ||
+    if ((e = panel_stream(&r.panel)) || (e = cudaEventCreateWithFlags(&r.ready, cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&r.next, cudaEventDisableTiming)))
         return e;
     if (cublasCreate(&r.blas) != CUBLAS_STATUS_SUCCESS || cusolverDnCreate(&r.solver) != CUSOLVER_STATUS_SUCCESS)
@@ -162,11 +177,16 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
     cublasComputeType_t compute = CUBLAS_COMPUTE_32F;
     if (math == LU_GEMM_BF16X9) {
         if (cublasSetEmulationStrategy(r.blas, CUBLAS_EMULATION_STRATEGY_EAGER) != CUBLAS_STATUS_SUCCESS ||
+            cublasSetEmulationSpecialValuesSupport(r.blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE) !=
+                CUBLAS_STATUS_SUCCESS ||
             cublasSetMathMode(r.blas, CUBLAS_FP32_EMULATED_BF16X9_MATH) != CUBLAS_STATUS_SUCCESS ||
             cusolverDnSetMathMode(r.solver, CUSOLVER_FP32_EMULATED_BF16X9_MATH) != CUSOLVER_STATUS_SUCCESS)
             return cudaErrorNotSupported;
         compute = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
     }
+    if ((e = cudaFuncSetAttribute(k_lu_pivot_plan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PLAN_SMEM)) ||
+        (e = cudaFuncSetAttribute(k_lu_swap_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWAP_SMEM)))
+        return e;
     int lwork = 0;
     if (cusolverDnCgetrf_bufferSize(r.solver, (int)n, nb, reinterpret_cast<cuComplex *>(A), (int)n, &lwork) !=
         CUSOLVER_STATUS_SUCCESS)
@@ -189,7 +209,7 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
         if (cusolverDnCgetrf(r.solver, (int)(n - j), jb, reinterpret_cast<cuComplex *>(at(j, j)), (int)n,
                              reinterpret_cast<cuComplex *>(r.work), ipiv + j, r.info + t) != CUSOLVER_STATUS_SUCCESS)
             return cudaErrorUnknown;
-        k_lu_pivot_plan<<<1, 256, 0, r.panel>>>(n, j, jb, ipiv, dst, src, count, error);
+        k_lu_pivot_plan<<<1, 256, PLAN_SMEM, r.panel>>>(n, j, jb, ipiv, dst, src, count, error);
         note_launches(1);
         return cudaEventRecord(r.ready, r.panel);
     };
@@ -215,9 +235,9 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
         const int64_t right = j + jb, rest = n - right;
         const int jb2 = (int)std::min<int64_t>(nb, rest);
         if ((e = cudaStreamWaitEvent(stream, r.ready, 0))) return e;
-        const unsigned blocks = (unsigned)std::min<int64_t>(std::max<int64_t>(n - jb, 1), (int64_t)sms * 8);
+        const unsigned blocks = (unsigned)std::min<int64_t>(std::max<int64_t>(n - jb, 1), (int64_t)sms * 4);
         if (n > jb) {
-            k_lu_swap_rows<<<blocks, SWAP_THREADS, 0, stream>>>(n, j, jb, A, dst, src, count);
+            k_lu_swap_rows<<<blocks, SWAP_THREADS, SWAP_SMEM, stream>>>(n, j, jb, A, dst, src, count);
             note_launches(1);
         }
         if (rest <= 0) break;
@@ -247,7 +267,135 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
     return cudaSuccess;
 }
 
+namespace {
+
+struct CholResources {
+    cublasHandle_t blas = nullptr, blas_panel = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+    cudaStream_t panel = nullptr, main = nullptr;
+    cudaEvent_t ready = nullptr, next = nullptr;
+    float *work = nullptr;
+    int *info = nullptr;
+    ~CholResources() {
+        if (main) cudaStreamSynchronize(main);
+        if (panel) cudaStreamSynchronize(panel);
+        pool_free(work, main);
+        pool_free(info, main);
+        if (blas) cublasDestroy(blas);
+        if (blas_panel) cublasDestroy(blas_panel);
+        if (solver) cusolverDnDestroy(solver);
+        if (ready) cudaEventDestroy(ready);
+        if (next) cudaEventDestroy(next);
+        if (panel) cudaStreamDestroy(panel);
+    }
+};
+
+}  // namespace
+
+// Step t (columns j .. j+jb):
+//   panel stream: potrf of the diagonal block A[j:j+jb, j:j+jb]; L21 = A[j+jb:, j:j+jb] L11^-T (triangular solve)
+//   main stream:  A[c:, c:c+w] -= L21[c-j-jb:] L21[c-j-jb : c-j-jb+w]^T for the block columns c of the trailing
+//                 lower triangle, the next panel's block column first (then the panel stream may start it).
+cudaError_t potrf_blocked(int64_t n, float *A, int block, int math, cudaStream_t stream, int *info_out) {
+    *info_out = 0;
+    if (n <= 0 || n > (int64_t)0x7fffffff || !A || block < 32 || block > MAX_BLOCK ||
+        (math != LU_GEMM_FP32 && math != LU_GEMM_BF16X9))
+        return cudaErrorInvalidValue;
+    const int nb = (int)std::min<int64_t>(block, n);
+    const int64_t steps = (n + nb - 1) / nb;
+    CholResources r;
+    r.main = stream;
+    cudaError_t e;
+    if ((e = panel_stream(&r.panel)) || (e = cudaEventCreateWithFlags(&r.ready, cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&r.next, cudaEventDisableTiming)))
+        return e;
+    if (cublasCreate(&r.blas) != CUBLAS_STATUS_SUCCESS || cublasCreate(&r.blas_panel) != CUBLAS_STATUS_SUCCESS ||
+        cusolverDnCreate(&r.solver) != CUSOLVER_STATUS_SUCCESS)
+        return cudaErrorNotSupported;
+    cublasSetStream(r.blas, stream);
+    cublasSetStream(r.blas_panel, r.panel);
+    cusolverDnSetStream(r.solver, r.panel);
+    cublasComputeType_t compute = CUBLAS_COMPUTE_32F;
+    if (math == LU_GEMM_BF16X9) {
+        if (cublasSetEmulationStrategy(r.blas, CUBLAS_EMULATION_STRATEGY_EAGER) != CUBLAS_STATUS_SUCCESS ||
+            cublasSetEmulationSpecialValuesSupport(r.blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE) !=
+                CUBLAS_STATUS_SUCCESS ||
+            cublasSetMathMode(r.blas, CUBLAS_FP32_EMULATED_BF16X9_MATH) != CUBLAS_STATUS_SUCCESS ||
+            cublasSetMathMode(r.blas_panel, CUBLAS_FP32_EMULATED_BF16X9_MATH) != CUBLAS_STATUS_SUCCESS ||
+            cusolverDnSetMathMode(r.solver, CUSOLVER_FP32_EMULATED_BF16X9_MATH) != CUSOLVER_STATUS_SUCCESS)
+            return cudaErrorNotSupported;
+        compute = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+    }
+    int lwork = 0;
+    if (cusolverDnSpotrf_bufferSize(r.solver, CUBLAS_FILL_MODE_LOWER, nb, A, (int)n, &lwork) !=
+        CUSOLVER_STATUS_SUCCESS)
+        return cudaErrorUnknown;
+    if ((e = pool_alloc_n(&r.work, (size_t)std::max(lwork, 1), stream)) ||
+        (e = pool_alloc_n(&r.info, (size_t)steps, stream)) ||
+        (e = cudaMemsetAsync(r.info, 0, sizeof(int) * steps, stream)))
+        return e;
+    auto at = [&](int64_t row, int64_t col) { return A + row + col * n; };
+    const float one = 1.f, minus = -1.f;
+    auto factor_panel = [&](int64_t j, int jb, int64_t t) -> cudaError_t {
+        if (cusolverDnSpotrf(r.solver, CUBLAS_FILL_MODE_LOWER, jb, at(j, j), (int)n, r.work, lwork, r.info + t) !=
+            CUSOLVER_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        const int64_t below = n - j - jb;
+        if (below > 0 &&
+            cublasStrsm(r.blas_panel, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT,
+                        (int)below, jb, &one, at(j, j), (int)n, at(j + jb, j), (int)n) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        return cudaEventRecord(r.ready, r.panel);
+    };
+    // A[c:, c:c+w] -= L21[c-r0:] L21[c-r0 : c-r0+w]^T, L21 = A[r0:, j:j+jb]
+    auto update = [&](int64_t j, int jb, int64_t c, int64_t w) -> bool {
+        const int64_t rows = n - c;
+        if (rows <= 0 || w <= 0) return true;
+        return cublasGemmEx(r.blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)rows, (int)w, jb, &minus, at(c, j), CUDA_R_32F,
+                            (int)n, at(c, j), CUDA_R_32F, (int)n, &one, at(c, c), CUDA_R_32F, (int)n, compute,
+                            CUBLAS_GEMM_DEFAULT) == CUBLAS_STATUS_SUCCESS;
+    };
+    if ((e = cudaEventRecord(r.next, stream)) || (e = cudaStreamWaitEvent(r.panel, r.next, 0)) ||
+        (e = factor_panel(0, nb, 0)))
+        return e;
+    for (int64_t t = 0; t < steps; ++t) {
+        const int64_t j = t * nb;
+        const int jb = (int)std::min<int64_t>(nb, n - j);
+        const int64_t right = j + jb;
+        if ((e = cudaStreamWaitEvent(stream, r.ready, 0))) return e;
+        if (right >= n) break;
+        const int64_t w0 = std::min<int64_t>(nb, n - right);
+        if (!update(j, jb, right, w0)) return cudaErrorUnknown;
+        if ((e = cudaEventRecord(r.next, stream)) || (e = cudaStreamWaitEvent(r.panel, r.next, 0)) ||
+            (e = factor_panel(right, (int)w0, t + 1)))
+            return e;
+        for (int64_t c = right + w0; c < n; c += nb)
+            if (!update(j, jb, c, std::min<int64_t>(nb, n - c))) return cudaErrorUnknown;
+    }
+    if ((e = cudaGetLastError()) || (e = cudaStreamSynchronize(r.panel)) || (e = cudaStreamSynchronize(stream)))
+        return e;
+    std::vector<int> info((size_t)steps);
+    if ((e = cudaMemcpy(info.data(), r.info, sizeof(int) * steps, cudaMemcpyDeviceToHost))) return e;
+    for (int64_t t = 0; t < steps; ++t)
+        if (info[t] > 0) {
+            *info_out = (int)(t * nb + info[t]);
+            break;
+        }
+    return cudaSuccess;
+}
+
 }  // namespace pq
+
+extern "C" int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int block, int math, int32_t *info, void *stream) {
+    if (n <= 0 || !a || !info || block < 32 || block > pq::MAX_BLOCK_PUBLIC || (math != 0 && math != 1))
+        return pq::fail(pq::ERR_ARGUMENT, "cholesky_f32: invalid argument (block 32..%d, math 0 or 1)",
+                        pq::MAX_BLOCK_PUBLIC);
+    int order = 0;
+    const cudaError_t e = pq::potrf_blocked(n, a, block, math, static_cast<cudaStream_t>(stream), &order);
+    *info = order;
+    if (e) return pq::fail(pq::ERR_CUDA, "cholesky_f32: %s", cudaGetErrorString(e));
+    return pq::OK;
+}
 
 extern "C" int pcbqs_gb300_lu_factor_c64(int64_t n, void *a, int32_t *ipiv, int block, int math, int32_t *singular,
                                          void *stream) {

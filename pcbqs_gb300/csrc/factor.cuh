@@ -1,4 +1,5 @@
-// Blocked complex64 LU with partial pivoting, in cuSOLVER getrf's column-major layout and pivot convention.
+// Blocked dense factorizations on the device: the complex64 LU with partial pivoting (cuSOLVER getrf's layout and
+// pivot convention) and the FP32 Cholesky (potrf's layout), both with their trailing updates as large GEMMs.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -20,8 +21,16 @@ enum LuMath : int {
 // comes from a triangular solve and the trailing matrix from one large GEMM (`math`). Returns cudaSuccess, or an
 // error; *singular = the first zero pivot's 1-based index (0 if none). Ordered on `stream`; returns after the
 // factor is complete.
-constexpr int MAX_BLOCK_PUBLIC = 1024;   // widest panel getrf_blocked takes
+constexpr int MAX_BLOCK_PUBLIC = 4096;   // widest panel the blocked factorizations take
 
 cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular);
+
+// Factors the n x n column-major symmetric positive definite FP32 matrix A (leading dimension n; the lower
+// triangle is read) in place as A = L L^T, L in the lower triangle (cusolverDnSpotrf's layout; the strict upper
+// triangle is left with intermediate values). Right-looking in `block`-column panels: the diagonal block by
+// cuSOLVER potrf and the panel below it by a triangular solve, both on a second stream one step ahead, and the
+// trailing lower triangle by one GEMM per block column (`math`). *info = the 1-based order of the first leading
+// minor that is not positive definite (0 if none). Ordered on `stream`; returns after the factor is complete.
+cudaError_t potrf_blocked(int64_t n, float *A, int block, int math, cudaStream_t stream, int *info);
 
 }  // namespace pq

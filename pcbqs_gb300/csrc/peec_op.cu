@@ -30,7 +30,7 @@
 
 #include "../../include/pcbqs_gb300.h"
 #include "common.cuh"
-#include "getrf.cuh"
+#include "factor.cuh"
 #include "pool.cuh"
 #include "solve.cuh"
 #include "trsolve.cuh"
@@ -776,25 +776,24 @@ __global__ void k_identity_pivots(int64_t n, int *ipiv) {
         ipiv[t] = (int)(t + 1);
 }
 
+constexpr int CHOL_BLOCK = 1024;   // panel width of the blocked Cholesky
+
 struct CholPrecond : Preconditioner {
     int64_t n = 0;
     float *chol = nullptr;
     float2 *lu = nullptr;
-    int *info = nullptr, *ipiv = nullptr;
-    cusolverDnHandle_t solver = nullptr;
+    int *ipiv = nullptr;
     TriSolver tri;
     ~CholPrecond() override {
         tri.release();
         dev_free(chol);
         dev_free(lu);
-        dev_free(info);
         dev_free(ipiv);
-        if (solver) cusolverDnDestroy(solver);
     }
     cudaError_t factor(int64_t n_, const double *A, int64_t lda, cudaStream_t s, int &host_info) {
         n = n_;
         cudaError_t e;
-        if ((e = dev_alloc(&chol, (size_t)n * n, s)) || (e = dev_alloc(&info, 1, s))) return e;
+        if ((e = dev_alloc(&chol, (size_t)n * n, s))) return e;
         if (lda == n) {
             k_to_f32<<<grid_of(n * n), 256, 0, s>>>(n * n, A, chol);
             note_launches(1);
@@ -804,23 +803,8 @@ struct CholPrecond : Preconditioner {
             }
             note_launches(n);
         }
-        if (cusolverDnCreate(&solver) != CUSOLVER_STATUS_SUCCESS) return cudaErrorUnknown;
-        cusolverDnSetStream(solver, s);
-        // FP32 arithmetic emulated with BF16x9 products on the tensor cores (FP32 accuracy)
-        cusolverDnSetMathMode(solver, CUSOLVER_FP32_EMULATED_BF16X9_MATH);
-        int lwork = 0;
-        if (cusolverDnSpotrf_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)n, chol, (int)n, &lwork) !=
-            CUSOLVER_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        float *ws = nullptr;
-        if ((e = dev_alloc(&ws, (size_t)lwork, s))) return e;
-        const cusolverStatus_t cs = cusolverDnSpotrf(solver, CUBLAS_FILL_MODE_LOWER, (int)n, chol, (int)n, ws, lwork,
-                                                     info);
-        cudaMemcpyAsync(&host_info, info, sizeof(int), cudaMemcpyDeviceToHost, s);
-        e = cudaStreamSynchronize(s);
-        dev_free(ws, s);
-        if (cs != CUSOLVER_STATUS_SUCCESS) return cudaErrorUnknown;
-        if (e || host_info) return e;
+        // blocked, FP32 arithmetic emulated with BF16x9 products on the tensor cores (FP32 accuracy)
+        if ((e = potrf_blocked(n, chol, CHOL_BLOCK, LU_GEMM_BF16X9, s, &host_info)) || host_info) return e;
         // the factor in the triangular solver's layout; the FP32 copy is not needed afterwards
         if ((e = dev_alloc(&lu, (size_t)n * n, s)) || (e = dev_alloc(&ipiv, (size_t)n, s))) return e;
         k_cholesky_to_lu<<<row_grid((unsigned)std::min<int64_t>((n + 255) / 256, 8), n), 256, 0, s>>>(n, chol, lu);
@@ -890,7 +874,7 @@ struct pcbqs_gb300_peec {
 
 namespace {
 #define pfail pq::fail
-constexpr int LU_BLOCK = 1024;     // panel width of the blocked factorization (math 2 and 3)
+constexpr int LU_BLOCK = 2048;     // panel width of the blocked factorization (math 2 and 3)
 Csr csr_of(const pcbqs_gb300_csr &c) {
     Csr out;
     out.rows = c.rows;

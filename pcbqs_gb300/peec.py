@@ -416,7 +416,7 @@ class PeecModel(PeecTopology):
         iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose dense products run
         in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of the 'lu32'
         factorization: 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy) through cuSOLVER's getrf,
-        'fp32-blocked' or 'bf16x9-blocked' through this library's blocked LU (1024-column panels factored ahead of
+        'fp32-blocked' or 'bf16x9-blocked' through this library's blocked LU (2048-column panels factored ahead of
         the trailing GEMMs). anchors ('lu32'
         only): how many factorizations a sweep shares; the frequencies, in increasing order, are split into that
         many runs and every run is solved as one batch of (frequency, port) columns preconditioned by the factor

@@ -4,6 +4,7 @@
     python -m pcbqs_gb300.timing lu <board> [k ...]          # the complex64 factor's triangular solves, k columns
     python -m pcbqs_gb300.timing dense <n> [k]               # FP64 and FP32 symmetric dense products, n x n, k columns
     python -m pcbqs_gb300.timing getrf <n> [block ...]       # the blocked complex64 LU of a random n x n matrix
+    python -m pcbqs_gb300.timing potrf <n> [block ...]       # the blocked FP32 Cholesky of a random SPD matrix
 
 Times are CUDA-event times after a warm-up call; boards are the npz meshes of tests/golden (planes, strip, tiny).
 """
@@ -90,6 +91,31 @@ def getrf(n, blocks=(1024,)):
                       flush=True)
 
 
+def potrf(n, blocks=(1024,)):
+    """The blocked FP32 Cholesky of a random n x n positive definite matrix, against cuSOLVER's potrf."""
+    from . import _lib
+    n = int(n)
+    lib = _lib.load()
+    g = torch.Generator(device='cuda').manual_seed(1)
+    M = torch.randn(n, n, device='cuda', generator=g)
+    A = M @ M.T / n + 0.05 * torch.eye(n, device='cuda')
+    F = torch.empty_like(A)
+    info = ctypes.c_int32(0)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for block in blocks:
+        for math in (1, 0):
+            for _ in range(2):
+                F.copy_(A)
+                ms, status = _event_ms(lambda: lib.pcbqs_gb300_cholesky_f32(n, F.data_ptr(), block, math,
+                                                                            ctypes.byref(info), stream))
+                _lib.check(status, lib)
+                print(f'potrf n={n} block {block} math {math}: {ms:.1f} ms, {n ** 3 / 3 / ms / 1e9:.1f} TFLOP/s',
+                      flush=True)
+    for _ in range(2):
+        ms, _ = _event_ms(lambda: torch.linalg.cholesky(A))
+        print(f'potrf n={n} cuSOLVER (torch): {ms:.1f} ms', flush=True)
+
+
 def dense(n, k=8):
     """A random symmetric n x n matrix (FP64 and its FP32 copy) against k complex columns."""
     from . import _lib
@@ -115,11 +141,13 @@ def dense(n, k=8):
 
 
 def main(argv):
-    if len(argv) < 2 or argv[0] not in ('fill', 'lu', 'dense', 'getrf'):
+    if len(argv) < 2 or argv[0] not in ('fill', 'lu', 'dense', 'getrf', 'potrf'):
         print(__doc__)
         return 2
     if argv[0] == 'fill':
         fill(argv[1], argv[2] if len(argv) > 2 else None)
+    elif argv[0] == 'potrf':
+        potrf(argv[1], tuple(int(v) for v in argv[2:]) or (1024,))
     elif argv[0] == 'getrf':
         getrf(argv[1], tuple(int(v) for v in argv[2:]) or (1024,))
     elif argv[0] == 'dense':

@@ -38,7 +38,7 @@ def _backward_error(A, LU, piv):
 
 
 @pytest.mark.parametrize('n,block,math', [(300, 64, 0), (1000, 128, 1), (1000, 1000, 1), (2100, 256, 1),
-                                          (2100, 1024, 0), (4097, 512, 1)])
+                                          (2100, 1024, 0), (4097, 512, 1), (4500, 2048, 1), (6000, 4096, 1)])
 def test_blocked_lu_matches_getrf(device_library, n, block, math):
     import torch
     g = torch.Generator(device='cuda').manual_seed(n + block)
@@ -77,9 +77,47 @@ def test_blocked_lu_rejects_bad_block(device_library):
     piv = torch.zeros(64, dtype=torch.int32, device='cuda')
     singular = ctypes.c_int32(0)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for block in (16, 2048):
+    for block in (16, 8192):
         status = device_library.pcbqs_gb300_lu_factor_c64(64, A.data_ptr(), piv.data_ptr(), block, 1,
                                                           ctypes.byref(singular), stream)
         assert status == 1
         with pytest.raises(ValueError, match='block'):
             _lib.check(status, device_library)
+
+
+def _cholesky(lib, A, block, math):
+    import torch
+    from pcbqs_gb300 import _lib
+    F = A.T.contiguous()                 # column-major A (symmetric: the same values)
+    info = ctypes.c_int32(-1)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.pcbqs_gb300_cholesky_f32(A.shape[0], F.data_ptr(), block, math, ctypes.byref(info), stream), lib)
+    return torch.tril(F.T), info.value
+
+
+@pytest.mark.parametrize('n,block,math', [(300, 64, 1), (2100, 512, 1), (2100, 1024, 0), (4097, 1024, 1)])
+def test_blocked_cholesky_matches_potrf(device_library, n, block, math):
+    """pcbqs_gb300_cholesky_f32 against A = L L^T, no worse than 4x cuSOLVER's own FP32 potrf (torch.cholesky)."""
+    import torch
+    g = torch.Generator(device='cuda').manual_seed(n + block)
+    M = torch.randn(n, n, device='cuda', generator=g)
+    A = M @ M.T / n + 0.05 * torch.eye(n, device='cuda')
+    L, info = _cholesky(device_library, A, block, math)
+    assert info == 0
+    assert torch.isfinite(L).all() and (torch.diagonal(L) > 0).all()
+    A64 = A.double()
+    ours = (torch.linalg.norm(A64 - L.double() @ L.double().T) / torch.linalg.norm(A64)).item()
+    Lr = torch.linalg.cholesky(A)
+    theirs = (torch.linalg.norm(A64 - Lr.double() @ Lr.double().T) / torch.linalg.norm(A64)).item()
+    assert ours <= 4 * theirs + 1e-7, (ours, theirs)
+
+
+def test_blocked_cholesky_reports_indefinite(device_library):
+    """A matrix whose 70th leading minor is not positive definite: info = 70 (found by the second 64-column
+    block's own potrf), as potrf reports it."""
+    import torch
+    n = 200
+    A = torch.eye(n, device='cuda')
+    A[69, 69] = -1.0
+    _, info = _cholesky(device_library, A, 64, 1)
+    assert info == 70

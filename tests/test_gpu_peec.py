@@ -104,7 +104,7 @@ def test_planes_mixed_and_fp64_solves_agree(device_library):
 def test_streaming_triangular_solves_match_getrs(device_library, board, k, math):
     """The library's streaming solve with the complex64 factor (super-block panels, inverted diagonal blocks, one
     gather for the row interchanges) against cuSOLVER getrs on the same factor; k = 11 exercises a padded second
-    sweep of 8 columns. math 2 and 3 factor with the library's blocked LU (three 1024-column panels on the strip),
+    sweep of 8 columns. math 2 and 3 factor with the library's blocked LU (two 2048-column panels on the strip),
     so getrs on its output also checks that it keeps getrf's layout and pivots. Both are FP32 solves in a different order, so they differ by FP32 rounding amplified by
     the factor's conditioning; the bar is the quantity GMRES cares about, the residual of the FP64 system, which
     over the batch must be no worse than getrs's (within 50 %)."""
