@@ -305,8 +305,10 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *op, int k, const int32_t *sys
                                  void *stream);
 /* A x = b for a dense symmetric A = A_re + j A_im (n x n, row stride lda; A_im nullable: real A) and k complex
  * columns by GMRES, preconditioned by the diagonal of A_re (precondition 0, as the reference) or by the
- * single-precision Cholesky factor of A_re (1, A_re positive definite; exact for a real A, a close preconditioner for
- * a lossy dielectric's complex potential matrix). Replaces peec_iterative.potential_solve
+ * single-precision Cholesky factor of A_re (A_re positive definite; exact for a real A, a close preconditioner for
+ * a lossy dielectric's complex potential matrix), its triangular solves by this library's streaming sweeps
+ * (precondition 1: cooperative kernels, which need the device to themselves) or by cuBLAS (2: ordinary kernels, so
+ * the solve may run while other work, such as a factorization on another stream, is in flight). Replaces peec_iterative.potential_solve
  * (src/pcbqs/peec_iterative.py:115-124), used for P^-1 B. */
 int pcbqs_gb300_dense_gmres(int64_t n, const double *A, const double *Aim, int64_t lda, int k, const double *b,
                             double *x, double tol, int maxiter, int restart, int precondition, int32_t *iterations,

@@ -778,17 +778,45 @@ __global__ void k_identity_pivots(int64_t n, int *ipiv) {
 
 constexpr int CHOL_BLOCK = 1024;   // panel width of the blocked Cholesky
 
+// Row-major (n, k) complex128 -> column-major (n, 2k) FP32: the real parts in columns 0..k-1, the imaginary parts
+// in k..2k-1 (real right-hand sides for a real factor); and back.
+__global__ void k_split_cols_f32(int64_t n, int k, const cd *in, float *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const int c = (int)(t % k);
+        out[(int64_t)c * n + r] = (float)in[t].x;
+        out[(int64_t)(k + c) * n + r] = (float)in[t].y;
+    }
+}
+
+__global__ void k_join_cols_f32(int64_t n, int k, const float *in, cd *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / k;
+        const int c = (int)(t % k);
+        out[t] = make_double2(in[(int64_t)c * n + r], in[(int64_t)(k + c) * n + r]);
+    }
+}
+
 struct CholPrecond : Preconditioner {
     int64_t n = 0;
     float *chol = nullptr;
     float2 *lu = nullptr;
     int *ipiv = nullptr;
     TriSolver tri;
+    // library = true: solves with cuBLAS triangular solves on the FP32 factor instead of the streaming sweeps.
+    // Slower alone, but ordinary kernels, so the solve may run beside other work on the device (the sweeps are
+    // cooperative kernels that must have it to themselves).
+    bool library = false;
+    cublasHandle_t blas = nullptr;
+    float *work = nullptr;
+    int cap = 0;
     ~CholPrecond() override {
         tri.release();
         dev_free(chol);
         dev_free(lu);
         dev_free(ipiv);
+        dev_free(work);
+        if (blas) cublasDestroy(blas);
     }
     cudaError_t factor(int64_t n_, const double *A, int64_t lda, cudaStream_t s, int &host_info) {
         n = n_;
@@ -805,6 +833,10 @@ struct CholPrecond : Preconditioner {
         }
         // blocked, FP32 arithmetic emulated with BF16x9 products on the tensor cores (FP32 accuracy)
         if ((e = potrf_blocked(n, chol, CHOL_BLOCK, LU_GEMM_BF16X9, s, &host_info)) || host_info) return e;
+        if (library) {
+            if (cublasCreate(&blas) != CUBLAS_STATUS_SUCCESS) return cudaErrorNotSupported;
+            return cudaStreamSynchronize(s);
+        }
         // the factor in the triangular solver's layout; the FP32 copy is not needed afterwards
         if ((e = dev_alloc(&lu, (size_t)n * n, s)) || (e = dev_alloc(&ipiv, (size_t)n, s))) return e;
         k_cholesky_to_lu<<<row_grid((unsigned)std::min<int64_t>((n + 255) / 256, 8), n), 256, 0, s>>>(n, chol, lu);
@@ -816,7 +848,25 @@ struct CholPrecond : Preconditioner {
         return cudaStreamSynchronize(s);
     }
     cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
-        return tri.solve(k, in, out, s);
+        if (!library) return tri.solve(k, in, out, s);
+        if (2 * k > cap) {
+            dev_free(work, s);
+            work = nullptr;
+            cudaError_t e = dev_alloc(&work, (size_t)n * 2 * k, s);
+            if (e) return e;
+            cap = 2 * k;
+        }
+        const float one = 1.f;
+        cublasSetStream(blas, s);
+        k_split_cols_f32<<<grid_of(n * k), 256, 0, s>>>(n, k, in, work);
+        if (cublasStrsm(blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, (int)n,
+                        2 * k, &one, chol, (int)n, work, (int)n) != CUBLAS_STATUS_SUCCESS ||
+            cublasStrsm(blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, (int)n,
+                        2 * k, &one, chol, (int)n, work, (int)n) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        k_join_cols_f32<<<grid_of(n * k), 256, 0, s>>>(n, k, work, out);
+        note_launches(2);
+        return cudaGetLastError();
     }
 };
 
@@ -1246,7 +1296,7 @@ int pcbqs_gb300_dense_gmres(int64_t n, const double *A, const double *Aim, int64
                             double *x, double tol, int maxiter, int restart, int precondition, int32_t *iterations,
                             double *residual, void *stream) {
     if (n <= 0 || !A || lda < n || k <= 0 || !b || !x || !(tol > 0) || maxiter <= 0 || restart <= 0 ||
-        precondition < 0 || precondition > 1)
+        precondition < 0 || precondition > 2)
         return pfail(ERR_ARGUMENT, "dense_gmres: invalid argument");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     DenseSym op;
@@ -1265,6 +1315,7 @@ int pcbqs_gb300_dense_gmres(int64_t n, const double *A, const double *Aim, int64
         M = &J;
     } else {
         int info = 0;
+        C.library = precondition == 2;
         e = C.factor(n, A, lda, st, info);
         if (e || info) {
             return pfail(info ? ERR_NONFINITE : ERR_CUDA, "dense_gmres: single-precision Cholesky failed (info %d)",

@@ -310,8 +310,10 @@ class PeecModel(PeecTopology):
         out[M.row[same] // bs, M.row[same] % bs, M.col[same] % bs] = M.data[same]
         return torch.as_tensor(out, device=self.device)
 
-    def _equilibrium(self, excitation):
-        """Baseline tree currents and the equilibrium charge of each drive (peec_iterative.solve:240-251)."""
+    def _equilibrium(self, excitation, beside=False):
+        """Baseline tree currents and the equilibrium charge of each drive (peec_iterative.solve:240-251).
+        beside=True: a factorization is in flight on another stream, so P's solves must not use the cooperative
+        triangular sweeps (they need the device to themselves)."""
         A, B = self.A, self.B
         sources = self.sources
         drive = np.asarray(A[:, sources] @ excitation)                 # (nn, ndrive)
@@ -321,7 +323,7 @@ class PeecModel(PeecTopology):
         if np.any(totals):
             if self._pinvb is None:
                 t0 = time.perf_counter()
-                self._pinvb = self._potential_solve(B.toarray())
+                self._pinvb = self._potential_solve(B.toarray(), precondition=2 if beside else 1)
                 self._component = np.asarray(B.T @ self._pinvb)
                 self.timings['potential_solve_s'] = time.perf_counter() - t0
             vpart = np.linalg.solve(self._component, -totals)
@@ -334,9 +336,9 @@ class PeecModel(PeecTopology):
         source_voltage = -self.source_components @ vpart                # (nsrc, ndrive)
         return baseline, qpart, vpart, source_voltage
 
-    def _potential_solve(self, rhs):
-        """P^-1 rhs on the device (dense GMRES preconditioned by P's single-precision Cholesky factor), rhs (nn, k)
-        real."""
+    def _potential_solve(self, rhs, precondition=1):
+        """P^-1 rhs on the device (dense GMRES preconditioned by P's single-precision Cholesky factor, its solves by
+        the streaming sweeps (1) or cuBLAS (2)), rhs (nn, k) real."""
         k = rhs.shape[1]
         b = torch.as_tensor(np.ascontiguousarray(rhs.astype(complex)), device=self.device)
         x = torch.zeros_like(b)
@@ -345,7 +347,7 @@ class PeecModel(PeecTopology):
         lib = _lib.load()
         Pim = self.Pim.data_ptr() if self.Pim is not None else None
         _lib.check(lib.pcbqs_gb300_dense_gmres(self.nn, self.P.data_ptr(), Pim, self.P.stride(0), k, b.data_ptr(),
-                                               x.data_ptr(), self.tol * 1e-2, 4000, self.restart, 1,
+                                               x.data_ptr(), self.tol * 1e-2, 4000, self.restart, precondition,
                                                _lib.ptr(its, ctypes.c_int32), _lib.ptr(res),
                                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
         self.timings['potential_solve_iterations'] = its.tolist()
@@ -455,15 +457,26 @@ class PeecModel(PeecTopology):
         factored = None
         try:
             t1 = time.perf_counter()
-            baseline, qpart, vpart, source_voltage = self._equilibrium(excitation)
-            t2 = time.perf_counter()
-            self.timings.update(equilibrium_s=t2 - t1, operator_setup_s=t1 - t0)
             if mode == 2:
                 # the first complex64 factorization depends only on L, P and the frequency: it runs on a side
-                # stream from a helper thread while this thread forms the right-hand sides and the single-precision
-                # copies (the ctypes call releases the interpreter lock). It starts after the equilibrium solve,
-                # whose triangular sweeps are cooperative kernels that must not share the device with other work.
+                # stream from a helper thread while this thread solves for the equilibrium charge and forms the
+                # right-hand sides and the single-precision copies (the ctypes calls release the interpreter lock).
+                # Meanwhile nothing here may launch the cooperative triangular sweeps: the equilibrium solve uses
+                # cuBLAS triangular solves instead.
                 factored = self._factor_async(handle, groups[0][0], self.FACTOR_MATH[factor_math])
+            if mode == 2:
+                # at the device's highest priority, so its short dependent kernels are not queued behind the
+                # factorization's GEMMs
+                if getattr(self, '_urgent', None) is None:
+                    self._urgent = torch.cuda.Stream(self.device, priority=-1)
+                self._urgent.wait_stream(torch.cuda.current_stream(self.device))
+                with torch.cuda.stream(self._urgent):
+                    baseline, qpart, vpart, source_voltage = self._equilibrium(excitation, beside=True)
+                torch.cuda.current_stream(self.device).wait_stream(self._urgent)
+            else:
+                baseline, qpart, vpart, source_voltage = self._equilibrium(excitation)
+            t2 = time.perf_counter()
+            self.timings.update(equilibrium_s=t2 - t1, operator_setup_s=t1 - t0)
             # rhs = -K^T (R + j w L) baseline / zscale, per (frequency, port) column, in the clustered order.
             Lb = self._mv_L(baseline[:self.ne])
             Rb = self.R @ baseline[:self.ne]

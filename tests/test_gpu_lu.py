@@ -121,3 +121,33 @@ def test_blocked_cholesky_reports_indefinite(device_library):
     A[69, 69] = -1.0
     _, info = _cholesky(device_library, A, 64, 1)
     assert info == 70
+
+
+@pytest.mark.parametrize('precondition', [0, 1, 2])
+@pytest.mark.parametrize('lossy', [False, True])
+def test_dense_gmres_solves_potential_systems(device_library, precondition, lossy):
+    """pcbqs_gb300_dense_gmres (the equilibrium charge's P^-1 B) with the diagonal (0) or the FP32 Cholesky factor,
+    its solves by the streaming sweeps (1) or by cuBLAS (2), on a symmetric positive definite A (+ j A_im for a
+    lossy dielectric): every column to 1e-10, and x against the FP64 direct solve."""
+    import torch
+    from pcbqs_gb300 import _lib
+    n, k = 1500, 3
+    g = torch.Generator(device='cuda').manual_seed(11)
+    M = torch.randn(n, n, device='cuda', dtype=torch.float64, generator=g)
+    A = M @ M.T / n + torch.eye(n, device='cuda', dtype=torch.float64)
+    Aim = (0.02 * A).contiguous() if lossy else None
+    b = torch.complex(torch.randn(n, k, device='cuda', dtype=torch.float64, generator=g),
+                      torch.randn(n, k, device='cuda', dtype=torch.float64, generator=g))
+    x = torch.zeros_like(b)
+    its, res = np.zeros(k, np.int32), np.zeros(k)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(device_library.pcbqs_gb300_dense_gmres(n, A.data_ptr(), Aim.data_ptr() if lossy else None, n, k,
+                                                      b.data_ptr(), x.data_ptr(), 1e-10, 2000, 100, precondition,
+                                                      _lib.ptr(its, ctypes.c_int32), _lib.ptr(res), stream),
+               device_library)
+    assert (res <= 1e-10).all()
+    Ac = torch.complex(A, Aim if lossy else torch.zeros_like(A))
+    ref = torch.linalg.solve(Ac, b)
+    assert (torch.linalg.norm(x - ref) / torch.linalg.norm(ref)).item() < 1e-8
+    if precondition:
+        assert its.max() <= (8 if lossy else 4), its
