@@ -16,6 +16,10 @@ scaling); `e2e` is the same through the public API from host arrays (PeecModel(b
 sparse topology uploaded, port matrix read back). The reference arm (--impl reference) times the CPU restatement
 of the reference's path (the oracle: OpenMP C for the fill, combine and aggregation, run in full) on all host cores,
 with the reference's dense solve (a complex64 LU, MixedLU) estimated from a timed bounded LU sample.
+
+`roofline` is the step's dominant stage, the blocked complex64 LU of the 'lu32' preconditioner (about 55 % of the
+step's kernel time), against the BF16x9 emulation's tensor ceiling; `fill_roofline` is the fill kernels' (FP32 far
+pairs, FP64 near pairs) against the measured FP32/FP64 GEMM rates.
 """
 import argparse
 import json
@@ -131,6 +135,34 @@ def fill_roofline(model, fill_ms, mixed, peaks):
                 unit='TFLOP/s', frac=round(achieved / peak, 4), traffic=traffic, flops_per_launch=flops,
                 far_pairs=far, near_pairs=[near0, near1], peak_source=source,
                 traffic_source='ncu dram bytes of k_fill_tiles on 8,000 triangles, scaled by pairs' if mixed else None)
+
+
+def measured_peaks():
+    """MEASURED_PEAKS.json beside this file (copy bandwidth and cuBLAS bf16 rates measured on this GPU model), or
+    None."""
+    path = Path(__file__).resolve().parent / 'MEASURED_PEAKS.json'
+    try:
+        return json.loads(path.read_text())
+    except (OSError, ValueError):
+        return None
+
+
+def factor_roofline(model, lu_ms):
+    """The dominant stage: the blocked complex64 LU (8 n^3 / 3 flops) against the BF16x9 emulation's ceiling, the
+    measured sustained bf16 tensor rate / 9 (each FP32 product is nine BF16 products; the LU runs for most of a
+    second inside the step, so the sustained figure). Time: CUDA events around the LU on its stream, per step."""
+    n = model.n
+    flops = 8 * n ** 3 / 3
+    peaks = measured_peaks()
+    if peaks and peaks.get('bf16_tflops_sustained'):
+        bf16, source = float(peaks['bf16_tflops_sustained']), 'MEASURED_PEAKS.json bf16_tflops_sustained / 9'
+    else:
+        bf16, source = 1700.0, 'fallback sustained bf16 1,700 TFLOP/s / 9'
+    peak = bf16 / 9
+    achieved = flops / (lu_ms / 1e3) / 1e12
+    return dict(bound='tensor', kernel='getrf_blocked (cuBLAS BF16x9 complex trailing GEMMs + cuSOLVER panels)',
+                achieved=round(achieved, 2), peak=round(peak, 2), unit='TFLOP/s', frac=round(achieved / peak, 4),
+                traffic=None, flops_per_launch=flops, lu_ms=round(lu_ms, 2), peak_source=source + ' (of measured)')
 
 
 def gemm_peak(dtype):
@@ -322,7 +354,9 @@ def main():
                         for k in ('equilibrium_s', 'potential_solve_s', 'operator_setup_s', 'rhs_s', 'solve_s')},
                 gpu_launches=int(launches),
                 clocks=clock_info,
-                roofline=fill_roofline(model, head_fill_ms, mixed, peaks),
+                roofline=(factor_roofline(model, statistics.median(t['factor_lu_ms'] for t in timings))
+                          if args.precondition == 'lu32' else fill_roofline(model, head_fill_ms, mixed, peaks)),
+                fill_roofline=fill_roofline(model, head_fill_ms, mixed, peaks),
                 e2e=dict(value=round(e2e_s, 4), unit='s/freq', h2d_bytes_per_step=int(h2d),
                          d2h_bytes_per_step=int(d2h)))
     if args.sweep:

@@ -253,6 +253,10 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *op, int32_t bs, const double
  * (pcbqs_gb300_lu_factor_c64, 2048-column panels) with BF16x9 / FP32 GEMMs. Mirrors MixedLU (src/pcbqs/kernels.py:125-181): a complex64 factor
  * with the FP64 operator's GMRES on top in place of its refinement loop. */
 int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream);
+/* CUDA-event times (ms, on the factorization's stream) of the last pcbqs_gb300_peec_factor: the dense system's
+ * assembly (with K^T L K and T^T P T when first formed) and the LU itself. No counterpart in the reference (its
+ * factor is LAPACK on the host); for the roofline of the factorization. */
+int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *op, double *assemble_ms, double *getrf_ms);
 /* Dense complex64 LU with partial pivoting of the n x n column-major device matrix a (leading dimension n), in
  * place, ipiv (device, n) receiving 1-based pivot rows: cusolverDnCgetrf's layout and pivots, so getrs and this
  * library's triangular solvers apply to it. Blocked: `block`-column panels (32 .. 4096) factored on a second stream

@@ -913,6 +913,7 @@ struct pcbqs_gb300_peec {
     LuPrecond *lu = nullptr;
     double *klk = nullptr, *tpt = nullptr;   // dense K^T L K and T^T P T (n x n), made once for the factors
     double *tpt_im = nullptr;                // T^T P_im T when P is complex
+    float assemble_ms = 0, getrf_ms = 0;     // CUDA-event times of the last factorization's two stages
     ~pcbqs_gb300_peec() {
         delete bj;
         delete lu;
@@ -1059,6 +1060,24 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e;
     const size_t nn2 = (size_t)n * n;
+    // stage times: ev[0] start, ev[1] system assembled, ev[2] factored
+    struct Events {
+        cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+        ~Events() {
+            for (cudaEvent_t x : ev)
+                if (x) cudaEventDestroy(x);
+        }
+    } t;
+    for (cudaEvent_t &x : t.ev) cudaEventCreate(&x);
+    cudaEventRecord(t.ev[0], st);
+    auto stage_times = [&]() {
+        float a = 0, b = 0;
+        if (cudaEventSynchronize(t.ev[2]) == cudaSuccess && cudaEventElapsedTime(&a, t.ev[0], t.ev[1]) == cudaSuccess &&
+            cudaEventElapsedTime(&b, t.ev[1], t.ev[2]) == cudaSuccess) {
+            h->assemble_ms = a;
+            h->getrf_ms = b;
+        }
+    };
     if (!h->klk) {
         // K^T L K = K^T (K^T L)^T (L symmetric) and T^T P T likewise: a row combination of L into W = K^T L (n rows),
         // its transpose, and a second row combination; every pass streams whole rows (no gathers).
@@ -1110,6 +1129,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         n, h->klk, h->tpt, h->tpt_im, op.is_tree, w, zs, op.pscale, lu->lu);
     k_add_krk_c64<<<grid_of(n), 256, 0, st>>>(S, op.is_tree, w, zs, op.pscale, op.rscale_host[sys], lu->lu);
     note_launches(2);
+    cudaEventRecord(t.ev[1], st);
     if (cusolverDnCreate(&lu->solver) != CUSOLVER_STATUS_SUCCESS) {
         delete lu;
         return pfail(ERR_CUDA, "peec_factor: cuSOLVER handle");
@@ -1118,6 +1138,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     if (math >= 2) {
         int singular = 0;
         e = getrf_blocked(n, lu->lu, lu->ipiv, LU_BLOCK, math == 2 ? LU_GEMM_BF16X9 : LU_GEMM_FP32, st, &singular);
+        cudaEventRecord(t.ev[2], st);
         if (e || singular) {
             delete lu;
             return pfail(singular ? ERR_NONFINITE : ERR_CUDA, "peec_factor: blocked getrf failed (zero pivot %d, %s)",
@@ -1129,6 +1150,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         }
         delete h->lu;
         h->lu = lu;
+        stage_times();
         return OK;
     }
     if (math == 1 && cusolverDnSetMathMode(lu->solver, CUSOLVER_FP32_EMULATED_BF16X9_MATH) != CUSOLVER_STATUS_SUCCESS) {
@@ -1148,6 +1170,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     }
     const cusolverStatus_t cs = cusolverDnCgetrf(lu->solver, (int)n, (int)n, reinterpret_cast<cuComplex *>(lu->lu),
                                                  (int)n, reinterpret_cast<cuComplex *>(ws), lu->ipiv, lu->info);
+    cudaEventRecord(t.ev[2], st);
     int info = 0;
     cudaMemcpyAsync(&info, lu->info, sizeof(int), cudaMemcpyDeviceToHost, st);
     e = cudaStreamSynchronize(st);
@@ -1163,6 +1186,15 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     }
     delete h->lu;
     h->lu = lu;
+    stage_times();
+    return OK;
+}
+
+int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *h, double *assemble_ms, double *getrf_ms) {
+    if (!h || !assemble_ms || !getrf_ms) return pfail(ERR_ARGUMENT, "peec_factor_times: invalid argument");
+    if (!h->lu) return pfail(ERR_ARGUMENT, "peec_factor_times: no factor set up");
+    *assemble_ms = h->assemble_ms;
+    *getrf_ms = h->getrf_ms;
     return OK;
 }
 

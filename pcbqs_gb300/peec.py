@@ -453,8 +453,14 @@ class PeecModel(PeecTopology):
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         timed = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         precondition_ms = gmres_ms = 0.0
+        stage_ms = np.zeros(2)             # the factorizations' assembly and LU times
         outer_total = 0
         factored = None
+
+        def factor_stages():
+            a, b = ctypes.c_double(), ctypes.c_double()
+            _lib.check(lib.pcbqs_gb300_peec_factor_times(handle, ctypes.byref(a), ctypes.byref(b)), lib)
+            stage_ms[:] += (a.value, b.value)
         try:
             t1 = time.perf_counter()
             if mode == 2:
@@ -514,6 +520,7 @@ class PeecModel(PeecTopology):
             if factored is not None:
                 precondition_ms += factored.result()
                 factored = None
+                factor_stages()
             if mixed:
                 Pfim = self.Pfim.data_ptr() if self.Pfim is not None else None
                 _lib.check(lib.pcbqs_gb300_peec_single(handle, Lf.data_ptr(), Lf.stride(0), Pf.data_ptr(), Pfim,
@@ -529,6 +536,7 @@ class PeecModel(PeecTopology):
                     e1.record()
                     torch.cuda.synchronize()
                     precondition_ms += e0.elapsed_time(e1)
+                    factor_stages()
                 sel = (np.asarray(members)[:, None] * npo + np.arange(npo)).ravel()
                 whole = len(sel) == k_all
                 b = b_all if whole else b_all[:, torch.as_tensor(sel, device=self.device)].contiguous()
@@ -560,7 +568,8 @@ class PeecModel(PeecTopology):
                     x_all[:, torch.as_tensor(sel, device=self.device)] = x
                 its[sel], res[sel] = its_g, res_g
             self.timings.update(precondition_ms=precondition_ms, gmres_ms=gmres_ms, gmres_iterations=its.tolist(),
-                                factorizations=len(groups) if mode == 2 else 0)
+                                factorizations=len(groups) if mode == 2 else 0, factor_assemble_ms=stage_ms[0],
+                                factor_lu_ms=stage_ms[1])
             if mixed:
                 self.timings['outer_steps'] = outer_total
             X = x_all.cpu().numpy()
