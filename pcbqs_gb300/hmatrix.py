@@ -210,6 +210,28 @@ class DeviceHMatrix:
                          bytes=self.bytes, dense_bytes=self.n * self.n * 8, evaluated_entries=self.entries,
                          tolerance=self.tol, leaf=self.leaf, eta=self.eta)
 
+    _ARRAYS = ('store', 'meta', 'idx', 'slot0', 'row_ptr', 'slots_of_row')
+
+    def __getstate__(self):
+        """Pickle support, as HMatrix.__getstate__ (src/pcbqs/hmatrix.py:308-316): the blocks and the product's
+        index arrays go to host memory; the fill (its device context, the exact-entry source) is not kept, so a
+        loaded matrix applies its blocks but evaluates no new entries. The triangle areas stay for
+        potential_operator."""
+        state = {k: v for k, v in self.__dict__.items() if k not in ('fill', '_edges') + self._ARRAYS}
+        for k in self._ARRAYS:
+            state[k] = getattr(self, k).cpu().numpy()
+        state['area'] = np.asarray(self.fill.geometry.area) if self.fill is not None else self.__dict__.get('area')
+        return state
+
+    def __setstate__(self, state):
+        """Uploads the arrays to the current CUDA device (HMatrix.__setstate__ re-packs its blocks likewise)."""
+        arrays = {k: state.pop(k) for k in self._ARRAYS}
+        self.__dict__.update(state)
+        self.fill, self._edges = None, None
+        dev = torch.device('cuda', torch.cuda.current_device())
+        for k, v in arrays.items():
+            setattr(self, k, torch.as_tensor(v, device=dev))
+
     def potential_operator(self, node_of):
         """P x = W^T H W x for the charge nodes (compressed.PotentialOperator, src/pcbqs/compressed.py:194-204):
         W[t, node] = A_t / A_node. Returns a function of (nn, k) complex device tensors."""
@@ -217,12 +239,13 @@ class DeviceHMatrix:
             raise ValueError('a potential operator needs the potential kernel')
         node_of = np.asarray(node_of)
         nn = int(node_of.max()) + 1
-        area_t = self.fill.geometry.area
+        area_t = self.fill.geometry.area if self.fill is not None else self.area
+        device = self.store.device
         area_n = np.bincount(node_of, weights=area_t, minlength=nn)
         from scipy.sparse import coo_matrix
         W = coo_matrix((area_t / area_n[node_of], (np.arange(self.n), node_of)), shape=(self.n, nn))
         Wd = torch.sparse_coo_tensor(np.vstack([W.row, W.col]), W.data.astype(complex), W.shape,
-                                     device=self.fill.device).coalesce()
+                                     device=device).coalesce()
         Wt = Wd.t().coalesce()
 
         def apply(x):

@@ -51,3 +51,28 @@ def test_compressed_potential_matches_dense(device_library):
     Yd = (P.to(torch.complex128) @ X).cpu().numpy()
     assert np.abs(Y - Yd).max() <= 50 * 1e-6 * np.abs(Yd).max()
     assert H.info['low_rank_blocks'] > 0
+
+
+@pytest.mark.parametrize('kernel', ['inductance', 'potential'])
+def test_hmatrix_pickle_round_trip(device_library, kernel):
+    """A pickled and reloaded operator (the operator cache of HMatrix.__getstate__/__setstate__,
+    src/pcbqs/hmatrix.py:308-316) applies bit for bit as the original; it keeps no fill (no exact entries)."""
+    import pickle
+    import torch
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.fill import DeviceFill
+    from pcbqs_gb300.hmatrix import DeviceHMatrix
+    b = Board.load('strip')
+    fill = DeviceFill(b.nodes, b.tris, b.z, outer_levels=1, near=3.0)
+    H = DeviceHMatrix(fill, tol=1e-6, leaf=64, eta=1.0, rank=32, kernel=kernel, er=b.er)
+    blob = pickle.dumps(H)
+    G = pickle.loads(blob)
+    assert G.fill is None and G.info == H.info
+    rng = np.random.default_rng(5)
+    X = torch.as_tensor(rng.standard_normal((H.n, 3)) + 1j * rng.standard_normal((H.n, 3)), device='cuda')
+    assert torch.equal(H.matmat(X), G.matmat(X))
+    if kernel == 'potential':
+        nn = int(b.node_of.max()) + 1
+        Xn = X[:nn].contiguous()
+        Yh, Yg = H.potential_operator(b.node_of)(Xn), G.potential_operator(b.node_of)(Xn)
+        assert torch.allclose(Yh, Yg, rtol=1e-13, atol=1e-13 * Yh.abs().max().item())   # sparse W products

@@ -1,0 +1,64 @@
+"""The device copper-port reduction (pcbqs_gb300.ports: FP64 fill of L, loop matrices on the device, direct
+elimination of the free loops) against the reference's own CopperPorts on the strip (tests/golden/ports_strip.npz,
+made by make_ports_golden.py), DC included, for DC and slab sheet resistance; and the device MixedLU."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def golden():
+    with np.load(GOLDEN / 'ports_strip.npz') as d:
+        return {k: d[k] for k in d.files}
+
+
+@pytest.mark.parametrize('loss', ['dc', 'slab'])
+def test_copper_ports_match_reference(device_library, loss):
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.ports import CopperPorts, MagneticModel
+    g = golden()
+    r = CopperPorts(MagneticModel(Board.load('strip'), conductor_loss=loss)).extract(g['freqs'])
+    assert list(r.names) == [str(n) for n in g['ports']]
+    Z, Zr = r.impedance, g[f'Z_{loss}']
+    for fi in range(len(g['freqs'])):
+        assert np.abs(Z[fi] - Zr[fi]).max() <= 1e-8 * np.abs(Zr[fi]).max(), fi
+    I, Ir = r.currents, g[f'currents_{loss}']
+    assert I.shape == Ir.shape
+    assert np.abs(I - Ir).max() <= 1e-8 * np.abs(Ir).max()
+    assert np.abs(Z - Z.transpose(0, 2, 1)).max() <= 1e-9 * np.abs(Z).max()      # reciprocity
+    assert (np.abs(I[:, -len(r.names):]) == 0).all()                             # port connectors carry none
+
+
+def test_copper_ports_need_a_loop(device_library):
+    """The tiny board's ports join two islands (a plane pair): no magnetic loop, as the reference reports."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.ports import MagneticModel
+    with pytest.raises(ValueError, match='island'):
+        MagneticModel(Board.load('tiny'))
+
+
+def test_device_mixed_lu_refines_to_double(device_library):
+    """DeviceMixedLU (complex64 blocked LU + FP64 refinement) on 4,500 unknowns: the residual reaches 1e-12 and the
+    solution matches the FP64 solve; lu_factor_rows picks it at and above 4,000 unknowns, as the reference."""
+    import torch
+    from pcbqs_gb300.mixedlu import DeviceMixedLU, lu_factor_rows, lu_solve_rows
+    n = 4500
+    g = torch.Generator(device='cuda').manual_seed(3)
+    A = torch.complex(torch.randn(n, n, device='cuda', dtype=torch.float64, generator=g),
+                      torch.randn(n, n, device='cuda', dtype=torch.float64, generator=g))
+    A += 4 * np.sqrt(n) * torch.eye(n, device='cuda', dtype=torch.complex128)
+    b = torch.complex(torch.randn(n, 3, device='cuda', dtype=torch.float64, generator=g),
+                      torch.randn(n, 3, device='cuda', dtype=torch.float64, generator=g))
+    lu = lu_factor_rows(A)
+    assert isinstance(lu, DeviceMixedLU)
+    x = lu_solve_rows(lu, b)
+    assert lu.double is None                                  # refined, not refactored in double
+    assert (torch.linalg.norm(b - A @ x) / torch.linalg.norm(b)).item() <= 1e-12
+    ref = torch.linalg.solve(A, b)
+    assert (torch.linalg.norm(x - ref) / torch.linalg.norm(ref)).item() <= 1e-11
+    x1 = lu_solve_rows(lu, b[:, 0])
+    assert x1.shape == (n,)
+    small = lu_factor_rows(A[:100, :100])
+    assert not isinstance(small, DeviceMixedLU)
