@@ -95,3 +95,58 @@ def lu_solve_rows(lu, b):
     one_column = b.dim() == 1
     x = torch.linalg.lu_solve(lu[0], lu[1], b.reshape(b.shape[0], -1).to(lu[0].dtype))
     return x[:, 0] if one_column else x
+
+
+class DevicePencil:
+    """(R + s L + P^T diag(z) P)^-1 for any s from one generalized eigendecomposition, on the device (the
+    reference's Pencil, src/pcbqs/kernels.py:205-245): R, L real symmetric (n, n) with R positive definite, P an
+    optional dense (k, n) incidence of k parts of impedance z(s). With R = C C^T and C^-1 L C^-T = W diag(lam) W^T,
+    G = C^-T W gives (R + s L)^-1 = G diag(1 / (1 + s lam)) G^T, and the parts enter by Woodbury (a k x k solve).
+    FP64 throughout (cuSOLVER potrf and syevd, cuBLAS); torch.linalg.LinAlgError where R is not positive definite."""
+
+    def __init__(self, R, L, P=None):
+        R = R.to(torch.float64)
+        L = L.to(torch.float64)
+        c = torch.linalg.cholesky(R)
+        X = torch.linalg.solve_triangular(c, L, upper=False)
+        X = torch.linalg.solve_triangular(c, X.T.contiguous(), upper=False)
+        X = (X + X.T) / 2
+        self.lam, W = torch.linalg.eigh(X)
+        del X
+        self.G = torch.linalg.solve_triangular(c.T, W, upper=True)
+        self.P = None if P is None or P.shape[0] == 0 else P.to(torch.float64)
+        self.PG = None if self.P is None else self.P @ self.G
+
+    def _real_times(self, M, v):
+        """M v for a real M and a complex v without a complex copy of M."""
+        return torch.complex(M @ v.real.contiguous(), M @ v.imag.contiguous())
+
+    def solve(self, s, z, b):
+        """x of (R + s L + P^T diag(z) P) x = b, b (n,) or (n, m) (complex)."""
+        b = b.to(torch.complex128)
+        one_column = b.dim() == 1
+        B = b.reshape(b.shape[0], -1)
+        d = 1 / (1 + complex(s) * self.lam.to(torch.complex128))
+        u = d[:, None] * self._real_times(self.G.T, B)
+        x = self._real_times(self.G, u)
+        if self.PG is not None and z is not None and bool(torch.as_tensor(z).abs().gt(0).any()):
+            z = torch.as_tensor(np.asarray(z, complex), device=B.device)
+            PGc = self.PG.to(torch.complex128)
+            S = (PGc * d[None, :]) @ PGc.T                            # P Z0^-1 P^T
+            k = len(z)
+            t = torch.linalg.solve(torch.eye(k, dtype=torch.complex128, device=B.device) + z[:, None] * S,
+                                   z[:, None] * (PGc @ u))
+            x = x - self._real_times(self.G, d[:, None] * (PGc.T @ t))
+        return x[:, 0] if one_column else x
+
+
+def pencil_lus(n):
+    """About how many complex LUs of n unknowns a pencil's eigendecomposition costs (the reference's CPU estimate,
+    kernels.py:248-251)."""
+    return 4.0 + 1.6 * n / 1000
+
+
+def pencil_pays(n, frequencies):
+    """Whether a sweep of `frequencies` on n loops is quicker by one pencil than by an LU each (kernels.py:254-263,
+    without its host-memory probe: the device holds the four n x n matrices)."""
+    return n >= 200 and frequencies >= 1.25 * pencil_lus(n) + 1
