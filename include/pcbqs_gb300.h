@@ -266,12 +266,12 @@ int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *op, double *assemble_m
 int pcbqs_gb300_lu_factor_c64(int64_t n, void *a, int32_t *ipiv, int block, int math, int32_t *singular,
                               void *stream);
 /* Dense FP32 Cholesky a = L L^T of the n x n column-major symmetric positive definite device matrix a (leading
- * dimension n, lower triangle read and overwritten by L; the strict upper triangle is left with intermediate
- * values), blocked like pcbqs_gb300_lu_factor_c64 (block 32 .. 4096, math 0: FP32 GEMMs, 1: BF16x9). *info
+ * dimension lda >= n, a multiple of 32 for the tensor-core GEMM forms; lower triangle read and overwritten by L;
+ * the strict upper triangle is left with intermediate values), blocked like pcbqs_gb300_lu_factor_c64 (block 32 .. 4096, math 0: FP32 GEMMs, 1: BF16x9). *info
  * (host) = order of the first leading minor that is not positive definite, 0 if none. Synchronizes `stream`. No
  * counterpart in the reference: it is the factor of P behind pcbqs_gb300_dense_gmres's preconditioner, exported so
  * it can be checked on its own. */
-int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int block, int math, int32_t *info, void *stream);
+int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int64_t lda, int block, int math, int32_t *info, void *stream);
 /* out = (complex64 factor)^-1 in for k complex128 columns (n, k) row-major, device arrays; the solve step of
  * MixedLU (src/pcbqs/kernels.py:160-181) without its refinement. method 0: this library's streaming triangular
  * solves (what GMRES uses); method 1: cuSOLVER getrs on the same factor (for validation). Synchronizes `stream`. */

@@ -119,8 +119,8 @@ PROTOTYPES = {
                                                      ctypes.POINTER(ctypes.c_double)]),
     'pcbqs_gb300_lu_factor_c64': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, ctypes.c_int, ctypes.c_int,
                                                  c_int32_p, c_void_p]),
-    'pcbqs_gb300_cholesky_f32': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int, ctypes.c_int, c_int32_p,
-                                                c_void_p]),
+    'pcbqs_gb300_cholesky_f32': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                                c_int32_p, c_void_p]),
     'pcbqs_gb300_dense_apply': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64, c_void_p,
                                                c_void_p, c_void_p]),
     'pcbqs_gb300_dense_apply_single': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64,

@@ -327,9 +327,10 @@ struct CholResources {
 //   panel stream: potrf of the diagonal block A[j:j+jb, j:j+jb]; L21 = A[j+jb:, j:j+jb] L11^-T (triangular solve)
 //   main stream:  A[c:, c:c+w] -= L21[c-j-jb:] L21[c-j-jb : c-j-jb+w]^T for the block columns c of the trailing
 //                 lower triangle, the next panel's block column first (then the panel stream may start it).
-cudaError_t potrf_blocked(int64_t n, float *A, int block, int math, cudaStream_t stream, int *info_out) {
+cudaError_t potrf_blocked(int64_t n, float *A, int64_t lda, int block, int math, cudaStream_t stream,
+                          int *info_out) {
     *info_out = 0;
-    if (n <= 0 || n > (int64_t)0x7fffffff || !A || block < 32 || block > MAX_BLOCK ||
+    if (n <= 0 || lda < n || lda > (int64_t)0x7fffffff || !A || block < 32 || block > MAX_BLOCK ||
         (math != LU_GEMM_FP32 && math != LU_GEMM_BF16X9))
         return cudaErrorInvalidValue;
     const int nb = (int)std::min<int64_t>(block, n);
@@ -358,23 +359,23 @@ cudaError_t potrf_blocked(int64_t n, float *A, int block, int math, cudaStream_t
         compute = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
     }
     int lwork = 0;
-    if (cusolverDnSpotrf_bufferSize(r.solver, CUBLAS_FILL_MODE_LOWER, nb, A, (int)n, &lwork) !=
+    if (cusolverDnSpotrf_bufferSize(r.solver, CUBLAS_FILL_MODE_LOWER, nb, A, (int)lda, &lwork) !=
         CUSOLVER_STATUS_SUCCESS)
         return cudaErrorUnknown;
     if ((e = pool_alloc_n(&r.work, (size_t)std::max(lwork, 1), stream)) ||
         (e = pool_alloc_n(&r.info, (size_t)steps, stream)) ||
         (e = cudaMemsetAsync(r.info, 0, sizeof(int) * steps, stream)))
         return e;
-    auto at = [&](int64_t row, int64_t col) { return A + row + col * n; };
+    auto at = [&](int64_t row, int64_t col) { return A + row + col * lda; };
     const float one = 1.f, minus = -1.f;
     auto factor_panel = [&](int64_t j, int jb, int64_t t) -> cudaError_t {
-        if (cusolverDnSpotrf(r.solver, CUBLAS_FILL_MODE_LOWER, jb, at(j, j), (int)n, r.work, lwork, r.info + t) !=
+        if (cusolverDnSpotrf(r.solver, CUBLAS_FILL_MODE_LOWER, jb, at(j, j), (int)lda, r.work, lwork, r.info + t) !=
             CUSOLVER_STATUS_SUCCESS)
             return cudaErrorUnknown;
         const int64_t below = n - j - jb;
         if (below > 0 &&
             cublasStrsm(r.blas_panel, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT,
-                        (int)below, jb, &one, at(j, j), (int)n, at(j + jb, j), (int)n) != CUBLAS_STATUS_SUCCESS)
+                        (int)below, jb, &one, at(j, j), (int)lda, at(j + jb, j), (int)lda) != CUBLAS_STATUS_SUCCESS)
             return cudaErrorUnknown;
         return cudaEventRecord(r.ready, r.panel);
     };
@@ -383,7 +384,7 @@ cudaError_t potrf_blocked(int64_t n, float *A, int block, int math, cudaStream_t
         const int64_t rows = n - c;
         if (rows <= 0 || w <= 0) return true;
         return cublasGemmEx(r.blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)rows, (int)w, jb, &minus, at(c, j), CUDA_R_32F,
-                            (int)n, at(c, j), CUDA_R_32F, (int)n, &one, at(c, c), CUDA_R_32F, (int)n, compute,
+                            (int)lda, at(c, j), CUDA_R_32F, (int)lda, &one, at(c, c), CUDA_R_32F, (int)lda, compute,
                             CUBLAS_GEMM_DEFAULT) == CUBLAS_STATUS_SUCCESS;
     };
     if ((e = cudaEventRecord(r.next, stream)) || (e = cudaStreamWaitEvent(r.panel, r.next, 0)) ||
@@ -417,12 +418,13 @@ cudaError_t potrf_blocked(int64_t n, float *A, int block, int math, cudaStream_t
 
 }  // namespace pq
 
-extern "C" int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int block, int math, int32_t *info, void *stream) {
-    if (n <= 0 || !a || !info || block < 32 || block > pq::MAX_BLOCK_PUBLIC || (math != 0 && math != 1))
-        return pq::fail(pq::ERR_ARGUMENT, "cholesky_f32: invalid argument (block 32..%d, math 0 or 1)",
+extern "C" int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int64_t lda, int block, int math, int32_t *info,
+                                        void *stream) {
+    if (n <= 0 || lda < n || !a || !info || block < 32 || block > pq::MAX_BLOCK_PUBLIC || (math != 0 && math != 1))
+        return pq::fail(pq::ERR_ARGUMENT, "cholesky_f32: invalid argument (lda >= n, block 32..%d, math 0 or 1)",
                         pq::MAX_BLOCK_PUBLIC);
     int order = 0;
-    const cudaError_t e = pq::potrf_blocked(n, a, block, math, static_cast<cudaStream_t>(stream), &order);
+    const cudaError_t e = pq::potrf_blocked(n, a, lda, block, math, static_cast<cudaStream_t>(stream), &order);
     *info = order;
     if (e) return pq::fail(pq::ERR_CUDA, "cholesky_f32: %s", cudaGetErrorString(e));
     return pq::OK;

@@ -25,12 +25,12 @@ constexpr int MAX_BLOCK_PUBLIC = 4096;   // widest panel the blocked factorizati
 
 cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular);
 
-// Factors the n x n column-major symmetric positive definite FP32 matrix A (leading dimension n; the lower
-// triangle is read) in place as A = L L^T, L in the lower triangle (cusolverDnSpotrf's layout; the strict upper
+// Factors the n x n column-major symmetric positive definite FP32 matrix A (leading dimension lda >= n, best a
+// multiple of 32 so that the GEMMs take their aligned, tensor-core forms; the lower triangle is read) in place as A = L L^T, L in the lower triangle (cusolverDnSpotrf's layout; the strict upper
 // triangle is left with intermediate values). Right-looking in `block`-column panels: the diagonal block by
 // cuSOLVER potrf and the panel below it by a triangular solve, both on a second stream one step ahead, and the
 // trailing lower triangle by one GEMM per block column (`math`). *info = the 1-based order of the first leading
 // minor that is not positive definite (0 if none). Ordered on `stream`; returns after the factor is complete.
-cudaError_t potrf_blocked(int64_t n, float *A, int block, int math, cudaStream_t stream, int *info);
+cudaError_t potrf_blocked(int64_t n, float *A, int64_t lda, int block, int math, cudaStream_t stream, int *info);
 
 }  // namespace pq

@@ -760,12 +760,12 @@ struct LuPrecond : Preconditioner {
 // The FP32 Cholesky factor of P in the LU layout of the streaming triangular solver: P = L L^T = (L D^-1)(D L^T),
 // D = diag(L), so with M = P^T = P the column-major array holds the unit lower L D^-1 below the diagonal and the
 // upper D L^T on and above it (no pivoting), as complex64 with zero imaginary parts.
-__global__ void k_cholesky_to_lu(int64_t n, const float *chol, float2 *lu) {
+__global__ void k_cholesky_to_lu(int64_t n, const float *chol, int64_t ldc, float2 *lu) {
     for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {   // column j of the column-major arrays
-        const float djj = chol[j + j * n];
+        const float djj = chol[j + j * ldc];
         for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
              i += (int64_t)gridDim.x * blockDim.x) {
-            const float v = i > j ? chol[i + j * n] / djj : chol[i + i * n] * chol[j + i * n];
+            const float v = i > j ? chol[i + j * ldc] / djj : chol[i + i * ldc] * chol[j + i * ldc];
             lu[i + j * n] = make_float2(v, 0.f);
         }
     }
@@ -797,8 +797,15 @@ __global__ void k_join_cols_f32(int64_t n, int k, const float *in, cd *out) {
     }
 }
 
+// out (n x n, leading dimension ldo) = in (n x n, leading dimension ldi) in FP32.
+__global__ void k_to_f32_strided(int64_t n, const double *in, int64_t ldi, float *out, int64_t ldo) {
+    for (int64_t r = blockIdx.y; r < n; r += gridDim.y)
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+            out[r * ldo + c] = (float)in[r * ldi + c];
+}
+
 struct CholPrecond : Preconditioner {
-    int64_t n = 0;
+    int64_t n = 0, ldc = 0;      // the FP32 factor's leading dimension: n rounded up to 32 (aligned GEMM forms)
     float *chol = nullptr;
     float2 *lu = nullptr;
     int *ipiv = nullptr;
@@ -820,26 +827,23 @@ struct CholPrecond : Preconditioner {
     }
     cudaError_t factor(int64_t n_, const double *A, int64_t lda, cudaStream_t s, int &host_info) {
         n = n_;
+        ldc = (n + 31) / 32 * 32;
         cudaError_t e;
-        if ((e = dev_alloc(&chol, (size_t)n * n, s))) return e;
-        if (lda == n) {
-            k_to_f32<<<grid_of(n * n), 256, 0, s>>>(n * n, A, chol);
-            note_launches(1);
-        } else {
-            for (int64_t r = 0; r < n; ++r) {
-                k_to_f32<<<grid_of(n), 256, 0, s>>>(n, A + r * lda, chol + r * n);
-            }
-            note_launches(n);
-        }
+        if ((e = dev_alloc(&chol, (size_t)n * ldc, s))) return e;
+        // A symmetric: its rows are the columns of the column-major copy
+        k_to_f32_strided<<<row_grid((unsigned)std::min<int64_t>((n + 255) / 256, 8), n), 256, 0, s>>>(n, A, lda, chol,
+                                                                                                     ldc);
+        note_launches(1);
         // blocked, FP32 arithmetic emulated with BF16x9 products on the tensor cores (FP32 accuracy)
-        if ((e = potrf_blocked(n, chol, CHOL_BLOCK, LU_GEMM_BF16X9, s, &host_info)) || host_info) return e;
+        if ((e = potrf_blocked(n, chol, ldc, CHOL_BLOCK, LU_GEMM_BF16X9, s, &host_info)) || host_info) return e;
         if (library) {
             if (cublasCreate(&blas) != CUBLAS_STATUS_SUCCESS) return cudaErrorNotSupported;
             return cudaStreamSynchronize(s);
         }
         // the factor in the triangular solver's layout; the FP32 copy is not needed afterwards
         if ((e = dev_alloc(&lu, (size_t)n * n, s)) || (e = dev_alloc(&ipiv, (size_t)n, s))) return e;
-        k_cholesky_to_lu<<<row_grid((unsigned)std::min<int64_t>((n + 255) / 256, 8), n), 256, 0, s>>>(n, chol, lu);
+        k_cholesky_to_lu<<<row_grid((unsigned)std::min<int64_t>((n + 255) / 256, 8), n), 256, 0, s>>>(n, chol, ldc,
+                                                                                                     lu);
         k_identity_pivots<<<grid_of(n), 256, 0, s>>>(n, ipiv);
         note_launches(2);
         if ((e = tri.prepare(lu, n, ipiv, s))) return e;
@@ -860,9 +864,9 @@ struct CholPrecond : Preconditioner {
         cublasSetStream(blas, s);
         k_split_cols_f32<<<grid_of(n * k), 256, 0, s>>>(n, k, in, work);
         if (cublasStrsm(blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, (int)n,
-                        2 * k, &one, chol, (int)n, work, (int)n) != CUBLAS_STATUS_SUCCESS ||
+                        2 * k, &one, chol, (int)ldc, work, (int)n) != CUBLAS_STATUS_SUCCESS ||
             cublasStrsm(blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, (int)n,
-                        2 * k, &one, chol, (int)n, work, (int)n) != CUBLAS_STATUS_SUCCESS)
+                        2 * k, &one, chol, (int)ldc, work, (int)n) != CUBLAS_STATUS_SUCCESS)
             return cudaErrorUnknown;
         k_join_cols_f32<<<grid_of(n * k), 256, 0, s>>>(n, k, work, out);
         note_launches(2);

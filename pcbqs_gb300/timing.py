@@ -99,18 +99,19 @@ def potrf(n, blocks=(1024,)):
     g = torch.Generator(device='cuda').manual_seed(1)
     M = torch.randn(n, n, device='cuda', generator=g)
     A = M @ M.T / n + 0.05 * torch.eye(n, device='cuda')
-    F = torch.empty_like(A)
+    ld = (n + 31) // 32 * 32                      # the padded leading dimension the library's own factor uses
+    F = torch.zeros(n, ld, device='cuda')
     info = ctypes.c_int32(0)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for block in blocks:
         for math in (1, 0):
             for _ in range(2):
-                F.copy_(A)
-                ms, status = _event_ms(lambda: lib.pcbqs_gb300_cholesky_f32(n, F.data_ptr(), block, math,
+                F[:, :n].copy_(A)
+                ms, status = _event_ms(lambda: lib.pcbqs_gb300_cholesky_f32(n, F.data_ptr(), ld, block, math,
                                                                             ctypes.byref(info), stream))
                 _lib.check(status, lib)
-                print(f'potrf n={n} block {block} math {math}: {ms:.1f} ms, {n ** 3 / 3 / ms / 1e9:.1f} TFLOP/s',
-                      flush=True)
+                print(f'potrf n={n} ld {ld} block {block} math {math}: {ms:.1f} ms, '
+                      f'{n ** 3 / 3 / ms / 1e9:.1f} TFLOP/s', flush=True)
     for _ in range(2):
         ms, _ = _event_ms(lambda: torch.linalg.cholesky(A))
         print(f'potrf n={n} cuSOLVER (torch): {ms:.1f} ms', flush=True)

@@ -85,24 +85,28 @@ def test_blocked_lu_rejects_bad_block(device_library):
             _lib.check(status, device_library)
 
 
-def _cholesky(lib, A, block, math):
+def _cholesky(lib, A, block, math, pad=0):
+    """Our Cholesky of A, its column-major copy stored with leading dimension n + pad."""
     import torch
     from pcbqs_gb300 import _lib
-    F = A.T.contiguous()                 # column-major A (symmetric: the same values)
+    n = A.shape[0]
+    F = torch.zeros(n, n + pad, dtype=A.dtype, device=A.device)     # row r of F = column r of the matrix
+    F[:, :n] = A.T
     info = ctypes.c_int32(-1)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    _lib.check(lib.pcbqs_gb300_cholesky_f32(A.shape[0], F.data_ptr(), block, math, ctypes.byref(info), stream), lib)
-    return torch.tril(F.T), info.value
+    _lib.check(lib.pcbqs_gb300_cholesky_f32(n, F.data_ptr(), n + pad, block, math, ctypes.byref(info), stream), lib)
+    return torch.tril(F[:, :n].T), info.value
 
 
-@pytest.mark.parametrize('n,block,math', [(300, 64, 1), (2100, 512, 1), (2100, 1024, 0), (4097, 1024, 1)])
-def test_blocked_cholesky_matches_potrf(device_library, n, block, math):
+@pytest.mark.parametrize('n,block,math,pad', [(300, 64, 1, 0), (2100, 512, 1, 0), (2100, 1024, 0, 12),
+                                              (4097, 1024, 1, 31)])
+def test_blocked_cholesky_matches_potrf(device_library, n, block, math, pad):
     """pcbqs_gb300_cholesky_f32 against A = L L^T, no worse than 4x cuSOLVER's own FP32 potrf (torch.cholesky)."""
     import torch
     g = torch.Generator(device='cuda').manual_seed(n + block)
     M = torch.randn(n, n, device='cuda', generator=g)
     A = M @ M.T / n + 0.05 * torch.eye(n, device='cuda')
-    L, info = _cholesky(device_library, A, block, math)
+    L, info = _cholesky(device_library, A, block, math, pad)
     assert info == 0
     assert torch.isfinite(L).all() and (torch.diagonal(L) > 0).all()
     A64 = A.double()

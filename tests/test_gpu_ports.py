@@ -62,3 +62,17 @@ def test_device_mixed_lu_refines_to_double(device_library):
     assert x1.shape == (n,)
     small = lu_factor_rows(A[:100, :100])
     assert not isinstance(small, DeviceMixedLU)
+
+
+def test_copper_ports_by_pencil_match_reference(device_library):
+    """The whole sweep from one generalized eigendecomposition (method='pencil') gives the reference's direct
+    reduction too; it refuses a frequency-dependent resistance."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.ports import CopperPorts, MagneticModel
+    g = golden()
+    r = CopperPorts(MagneticModel(Board.load('strip'))).extract(g['freqs'], method='pencil')
+    for fi in range(len(g['freqs'])):
+        assert np.abs(r.impedance[fi] - g['Z_dc'][fi]).max() <= 1e-8 * np.abs(g['Z_dc'][fi]).max(), fi
+    assert np.abs(r.currents - g['currents_dc']).max() <= 1e-8 * np.abs(g['currents_dc']).max()
+    with pytest.raises(ValueError, match='pencil'):
+        CopperPorts(MagneticModel(Board.load('strip'), conductor_loss='slab')).extract(g['freqs'], method='pencil')
