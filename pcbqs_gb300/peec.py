@@ -158,8 +158,8 @@ class PeecTopology:
         nn = b.n_nodes
         self.ne = ne = r.Ne
         self.names = [p for p, _, _ in b.ports]
-        ends = [(int(node_of[a]), int(node_of[c])) for a, c in zip(r.tp, r.tm)]
-        ends += [(b.term_node(a), b.term_node(c)) for _, a, c in b.ports]
+        ends = np.r_[np.c_[node_of[r.tp], node_of[r.tm]],
+                     np.array([(b.term_node(a), b.term_node(c)) for _, a, c in b.ports], np.int64).reshape(-1, 2)]
         nb = len(ends)
         is_src = np.r_[np.zeros(ne, bool), np.ones(len(b.ports), bool)]
         C, src_cols, tree, col_branch = loop_basis(nn, ends, is_src, ne)
@@ -170,7 +170,7 @@ class PeecTopology:
         sources, passive = np.flatnonzero(is_src), np.flatnonzero(~is_src)
         if not np.array_equal(passive, np.arange(ne)):
             raise ValueError('only copper edges may be passive branches (no via segments or lumped parts)')
-        cycles = [c for c in range(C.shape[1]) if c not in set(src_cols.values())]
+        cycles = np.setdiff1d(np.arange(C.shape[1]), np.fromiter(src_cols.values(), np.int64, len(src_cols)))
         K = hstack((C[:, cycles], eye(nb, format='csc')[:, np.flatnonzero(tree)]), format='csc')
         nl = len(cycles)
         T = (A @ K[:, nl:]).tocsc()
@@ -201,6 +201,17 @@ class PeecTopology:
 
 
 
+_HOST_POOL = None
+
+
+def _host_pool():
+    """One helper thread for host-side preparation that overlaps device work."""
+    global _HOST_POOL
+    if _HOST_POOL is None:
+        _HOST_POOL = concurrent.futures.ThreadPoolExecutor(max_workers=1, thread_name_prefix='pcbqs-host')
+    return _HOST_POOL
+
+
 class PeecModel(PeecTopology):
     """A board's surface-charge PEEC model, every port a 1 A current source from its first to its second terminal
     (MQS.source), solved on the device. The dielectric is homogeneous (board.er) unless `stack` (a
@@ -217,11 +228,27 @@ class PeecModel(PeecTopology):
         self.Pim = self.Pfim = None
         self.device = torch.device('cuda', device)
         self.timings = {}
-        t0 = time.perf_counter()
+        self.board = board
         self.fill = DeviceFill(board.nodes, board.tris, board.z, outer_levels, near, device)
-        PeecTopology.__init__(self, board, self.fill.rwg, block_size, log)
-        self.timings['host_topology_s'] = time.perf_counter() - t0
         self.L = self.P = self.Lf = self.Pf = None
+        # the host topology (loop basis, incidences, sheet resistance, ordering) needs no device: it is built on a
+        # helper thread while the caller's first assemble() fills L and P; the first use of one of its attributes
+        # waits for it (__getattr__) and raises its error, if any
+        rwg = self.fill.rwg
+
+        def topology():
+            t0 = time.perf_counter()
+            PeecTopology.__init__(self, board, rwg, block_size, log)
+            self.timings['host_topology_s'] = time.perf_counter() - t0
+        self._topology_job = _host_pool().submit(topology)
+
+    def __getattr__(self, name):
+        job = self.__dict__.get('_topology_job')
+        if job is None:
+            raise AttributeError(name)
+        job.result()                        # the topology's error, raised at every use until it is fixed
+        self.__dict__['_topology_job'] = None
+        return getattr(self, name)
 
     # -- device matrices --
     def assemble(self, mixed=False):
