@@ -307,6 +307,12 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *op, int k, const int32_t *sys
                                  double tol, double inner_tol, int max_outer, int inner_maxiter, int restart,
                                  int precondition, int32_t *iterations, double *residual, int32_t *outer_steps,
                                  void *stream);
+/* Partial inductance matrix of nv plated via segments (filaments along z): seg (device, nv x 5) rows (x, y, r, z0,
+ * z1) in m, L (device, nv x nv, row stride ld) = scale [g(z1a - z0b) + g(z0a - z1b) - g(z1a - z1b) - g(z0a - z0b)],
+ * g(u) = u asinh(u / s) - sqrt(u^2 + s^2), s the axis distance or, for coaxial segments and the self terms, the
+ * larger radius; scale = mu0 / 4 pi. Ordered on `stream` (no synchronization). Replaces via_inductance and
+ * filament_mutual (src/pcbqs/mqs.py:40-45, :140-153). */
+int pcbqs_gb300_via_inductance(int64_t nv, const double *seg, double scale, double *L, int64_t ld, void *stream);
 /* A x = b for a dense symmetric A = A_re + j A_im (n x n, row stride lda; A_im nullable: real A) and k complex
  * columns by GMRES, preconditioned by the diagonal of A_re (precondition 0, as the reference) or by the
  * single-precision Cholesky factor of A_re (A_re positive definite; exact for a real A, a close preconditioner for

@@ -30,6 +30,9 @@ class Board:
     sigma: float = 5.8e7
     er: float = 1.0
     description: str = ''
+    via_seg: np.ndarray = None   # (nv, 5): x, y, r, z0, z1 (m) of each plated via segment (MQS.vseg), or None
+    via_fans: np.ndarray = None  # (nv, 2): the fans (merged nodes) the segment joins
+    plating: float = 25e-6       # via barrel plating (m)
     _node_of: np.ndarray = field(default=None, repr=False)
 
     @classmethod
@@ -42,8 +45,9 @@ class Board:
             terms = dict(zip(names, _csr_groups(d['term_ptr'], d['term_tris'])))
             fans = _csr_groups(d['fan_ptr'], d['fan_tris'])
             ports = [(str(p), names[a], names[b]) for p, a, b in zip(d['port_names'], d['port_a'], d['port_b'])]
+            vias = (d['via_seg'].copy(), d['via_fans'].copy()) if 'via_seg' in d.files else (None, None)
             return cls(d['nodes'].copy(), d['tris'].copy(), d['z'].copy(), d['layer'].copy(), terms, fans, ports,
-                       float(d['thickness']), float(d['sigma']), float(d['er']), str(d['description']))
+                       float(d['thickness']), float(d['sigma']), float(d['er']), str(d['description']), *vias)
 
     @property
     def nt(self):
@@ -76,6 +80,17 @@ class Board:
 
     def term_node(self, name):
         return int(self.node_of[self.terminals[name][0]])
+
+    @property
+    def nv(self):
+        return 0 if self.via_seg is None else len(self.via_seg)
+
+    def via_ends(self):
+        """(nv, 2) nodes each via segment joins (the branches after the RWG edges, MQS.br)."""
+        if not self.nv:
+            return np.zeros((0, 2), np.int64)
+        first = np.array([int(f[0]) for f in self.fans], np.int64)
+        return self.node_of[first[np.asarray(self.via_fans)]]
 
     def node_groups(self, area):
         """CSR of nodes -> member triangles (start (nn+1) int64, members (nt) int32) and node areas."""

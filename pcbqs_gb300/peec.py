@@ -20,7 +20,7 @@ import time
 
 import numpy as np
 import torch
-from scipy.sparse import coo_matrix, csr_matrix, diags, eye, hstack
+from scipy.sparse import block_diag, coo_matrix, csr_matrix, diags, eye, hstack
 from scipy.sparse.csgraph import connected_components
 from scipy.sparse.linalg import splu
 
@@ -99,6 +99,46 @@ def sheet_resistance(rwg, sigma, thickness):
     return (scale @ G @ scale).tocsr()
 
 
+# ---- plated vias: filament segments along z ----------------------------------------------------------------------
+
+def via_resistance(seg, sigma, plating):
+    """DC resistance (ohm) of each via segment's plated barrel, seg rows (x, y, r, z0, z1) m: length over sigma
+    times the plated ring's area (src/pcbqs/mqs.py:132-137)."""
+    v = np.asarray(seg, float).reshape(-1, 5)
+    outer = v[:, 2]
+    inner = np.maximum(outer - plating, 0.0)
+    return (v[:, 4] - v[:, 3]) / (sigma * np.pi * (outer ** 2 - inner ** 2))
+
+
+def via_inductance(seg, out, device):
+    """The via segments' partial inductance matrix written into `out` (a (nv, nv) FP64 CUDA view, any row stride)
+    by the device kernel (pcbqs_gb300_via_inductance: filaments along z, Grover's formula)."""
+    v = torch.as_tensor(np.ascontiguousarray(seg, float).reshape(-1, 5), device=device)
+    lib = _lib.load()
+    _lib.check(lib.pcbqs_gb300_via_inductance(len(v), v.data_ptr(), MU0 / (4 * np.pi), out.data_ptr(), out.stride(0),
+                                              ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)), lib)
+    return out
+
+
+def with_vias(board, L, Lf=None):
+    """The inductance of every branch with impedance, the edges' L and the via segments' as one block-diagonal
+    matrix (edges first): the reference couples neither to the other (MQS._loops keeps them as separate blocks,
+    src/pcbqs/mqs.py:655-662). L, Lf unchanged for a board without vias; Lf (FP32 copy) optional."""
+    nv = board.nv
+    if not nv:
+        return L, Lf
+    ne = L.shape[0]
+    full = torch.zeros((ne + nv, ne + nv), dtype=L.dtype, device=L.device)
+    full[:ne, :ne] = L
+    via_inductance(board.via_seg, full[ne:, ne:], L.device)
+    fullf = None
+    if Lf is not None:
+        fullf = torch.zeros((ne + nv, ne + nv), dtype=torch.float32, device=L.device)
+        fullf[:ne, :ne] = Lf
+        fullf[ne:, ne:] = full[ne:, ne:]
+    return full, fullf
+
+
 # ---- ordering for block-Jacobi -----------------------------------------------------------------------------------
 
 def cluster_order(points, bs):
@@ -157,19 +197,21 @@ class PeecTopology:
         node_of = b.node_of
         nn = b.n_nodes
         self.ne = ne = r.Ne
+        self.nv = nv = b.nv
+        self.ni = ne + nv                 # branches with impedance: RWG edges, then plated via segments
         self.names = [p for p, _, _ in b.ports]
-        ends = np.r_[np.c_[node_of[r.tp], node_of[r.tm]],
+        ends = np.r_[np.c_[node_of[r.tp], node_of[r.tm]], b.via_ends(),
                      np.array([(b.term_node(a), b.term_node(c)) for _, a, c in b.ports], np.int64).reshape(-1, 2)]
         nb = len(ends)
-        is_src = np.r_[np.zeros(ne, bool), np.ones(len(b.ports), bool)]
+        is_src = np.r_[np.zeros(ne + nv, bool), np.ones(len(b.ports), bool)]
         C, src_cols, tree, col_branch = loop_basis(nn, ends, is_src, ne)
         ea, eb = np.asarray(ends).T
         branch = np.arange(nb)
         A = coo_matrix((np.r_[np.ones(nb), -np.ones(nb)], (np.r_[ea, eb], np.r_[branch, branch])),
                        shape=(nn, nb)).tocsc()
         sources, passive = np.flatnonzero(is_src), np.flatnonzero(~is_src)
-        if not np.array_equal(passive, np.arange(ne)):
-            raise ValueError('only copper edges may be passive branches (no via segments or lumped parts)')
+        if not np.array_equal(passive, np.arange(ne + nv)):
+            raise ValueError('only copper edges and via segments may be passive branches (no lumped parts)')
         cycles = np.setdiff1d(np.arange(C.shape[1]), np.fromiter(src_cols.values(), np.int64, len(src_cols)))
         K = hstack((C[:, cycles], eye(nb, format='csc')[:, np.flatnonzero(tree)]), format='csc')
         nl = len(cycles)
@@ -185,12 +227,18 @@ class PeecTopology:
         self.sources, self.passive, self.nn, self.nb = sources, passive, nn, nb
         self.source_components = np.asarray((A[:, sources].T @ B).todense())
         self.R = sheet_resistance(r, b.sigma, b.thickness)
+        if nv:
+            self.R = block_diag((self.R, diags(via_resistance(b.via_seg, b.sigma, b.plating))), format='csr')
         # K-space unknowns ordered into geometric blocks: a cycle at its defining (cotree) branch, a tree unknown
-        # at its branch; branch positions are RWG edge midpoints at their sheet's height.
+        # at its branch; branch positions are RWG edge midpoints at their sheet's height, via segments their axis
+        # at mid height.
         n = K.shape[1]
         pos_branch = np.c_[r.mid, 1e3 * b.z[r.tp]]      # sheets far apart in the ordering
+        if nv:
+            v = np.asarray(b.via_seg)
+            pos_branch = np.r_[pos_branch, np.c_[v[:, :2], 1e3 * (v[:, 3] + v[:, 4]) / 2]]
         own = np.r_[col_branch[cycles], np.flatnonzero(tree)]
-        assert len(own) == n and own.max() < ne
+        assert len(own) == n and own.max() < ne + nv
         self.order = cluster_order(pos_branch[own], self.bs)
         self.Kp = K[passive][:, self.order].tocsc()           # passive rows, clustered columns
         Tfull = hstack((csr_matrix((nn, nl)), T), format='csc')     # loop columns carry no charge
@@ -222,6 +270,9 @@ class PeecModel(PeecTopology):
                  restart=100, log=None, inner_tol=1e-4, conductor_loss='dc', conductor_faces=2, stack=None):
         if conductor_loss not in ('dc', 'slab') or conductor_faces not in (1, 2):
             raise ValueError('conductor_loss must be dc or slab; conductor_faces must be 1 or 2')
+        if conductor_loss == 'slab' and board.nv:
+            raise ValueError("conductor_loss='slab' with plated via segments is not supported by the PEEC solve (the "
+                             "barrels keep their DC resistance); the magnetic port reduction supports it")
         self.tol, self.maxiter, self.restart, self.inner_tol = tol, maxiter, restart, inner_tol
         self.conductor_loss, self.conductor_faces = conductor_loss, conductor_faces
         self.stack = stack
@@ -260,14 +311,14 @@ class PeecModel(PeecTopology):
         if mixed:
             planes, analytic = self.fill.moments_local()
             ev[1].record()
-            self.L, self.Lf = self.fill.inductance_local(planes)
+            self.L, self.Lf = with_vias(self.board, *self.fill.inductance_local(planes))
             ev[2].record()
             if self.stack is None:
                 self.P, self.Pf = self.fill.potential_single(planes[0], self.board.node_of, self.board.er)
         else:
             planes, analytic = self.fill.moments()
             ev[1].record()
-            self.L = self.fill.inductance(planes)
+            self.L, _ = with_vias(self.board, self.fill.inductance(planes))
             ev[2].record()
             if self.stack is None:
                 self.P = self.fill.potential(planes[0], self.board.node_of, self.board.er)
@@ -310,7 +361,7 @@ class PeecModel(PeecTopology):
                              Tt=_dev_csr(self.Tp.T, dev), R=_dev_csr(R, dev),
                              is_tree=torch.as_tensor(self.is_tree, device=dev))
         d = _lib.PeecDesc()
-        d.n, d.nb, d.ne, d.nn = self.n, len(self.passive), self.ne, self.nn
+        d.n, d.nb, d.ne, d.nn = self.n, len(self.passive), self.ni, self.nn
         for name in ('K', 'Kt', 'T', 'Tt', 'R'):
             setattr(d, name, _csr_struct(self._dev[name]))
         d.L, d.ldl, d.P, d.ldp = self.L.data_ptr(), self.L.stride(0), self.P.data_ptr(), self.P.stride(0)
@@ -511,8 +562,8 @@ class PeecModel(PeecTopology):
             t2 = time.perf_counter()
             self.timings.update(equilibrium_s=t2 - t1, operator_setup_s=t1 - t0)
             # rhs = -K^T (R + j w L) baseline / zscale, per (frequency, port) column, in the clustered order.
-            Lb = self._mv_L(baseline[:self.ne])
-            Rb = self.R @ baseline[:self.ne]
+            Lb = self._mv_L(baseline[:self.ni])
+            Rb = self.R @ baseline[:self.ni]
             Kpt = self.Kp.T
             ratio = self.resistance_ratio(f)
             cols = [-(Kpt @ (ratio[fi] * Rb + 1j * w * Lb)) / zscale[fi] for fi, w in enumerate(omegas)]

@@ -13,6 +13,11 @@ The boards themselves are synthetic stand-ins with the shapes and sizes of the b
   strip  20 x 5 mm trace, h 0.31 mm, three terminals (both ends, middle), two ports         (~2,200 triangles)
   planes two 50 x 50 mm planes 0.2 mm apart, 40 vias (r 0.15 mm, seed-uniform), 8 ports   (~20,000 triangles)
   tiny   a 4 x 2 mm two-layer board for fast parity tests                                   (~300 triangles)
+  viapair a 10 x 2 mm strip over its return strip 0.2 mm below, joined at the far end by two plated vias
+          (via segments: via_seg (x, y, r, z0, z1) m and via_fans, the fan of each end), one port at the near
+          end between the strips                                                              (~800 triangles)
+
+    python tests/golden/make_meshes.py viapair    (that board alone; the others keep their meshes)
 """
 import sys
 from pathlib import Path
@@ -124,7 +129,7 @@ def inside_box(cen, box):
     return np.flatnonzero((cen[:, 0] > x0) & (cen[:, 0] < x1) & (cen[:, 1] > y0) & (cen[:, 1] < y1))
 
 
-def assemble(sheets, terminals, fans, ports, meta):
+def assemble(sheets, terminals, fans, ports, meta, vias=()):
     """Stack sheets (mm) into one mesh (m); terminals: name -> [(sheet, box mm)]; fans: [(sheet, centre mm)]."""
     nodes, tris, z, layer = [], [], [], []
     off = 0
@@ -155,7 +160,12 @@ def assemble(sheets, terminals, fans, ports, meta):
         fan.append(np.sort(ids))
     ptr = lambda groups: np.r_[0, np.cumsum([len(g) for g in groups])].astype(np.int64)
     cat = lambda groups: (np.concatenate(groups) if groups else np.zeros(0, int)).astype(np.int64)
-    return dict(nodes=nodes, tris=tris.astype(np.int64), z=np.array(z), layer=layer,
+    extra = {}
+    if len(vias):     # (x, y, r mm, sheet a, sheet b, fan a, fan b): a plated barrel between two sheets' fans
+        extra = dict(via_seg=np.array([(x * 1e-3, y * 1e-3, r * 1e-3, sheets[a][2] * 1e-3, sheets[b][2] * 1e-3)
+                                       for x, y, r, a, b, _, _ in vias]),
+                     via_fans=np.array([(fa, fb) for *_, fa, fb in vias], np.int64))
+    return dict(**extra, nodes=nodes, tris=tris.astype(np.int64), z=np.array(z), layer=layer,
                 term_names=np.array(names), term_ptr=ptr(term), term_tris=cat(term),
                 fan_ptr=ptr(fan), fan_tris=cat(fan),
                 port_a=np.array([names.index(a) for _, a, _ in ports]),
@@ -226,6 +236,29 @@ def planes(core, size=50.0, gap=0.2, n_vias=40, n_ports=8, h=0.75, seed=7, margi
                                      f'{n_ports} ports, h {h} mm'))
 
 
+def viapair(core, length=10.0, width=2.0, gap=0.2, h=0.3):
+    """A strip (z = gap) over its return strip (z = 0), joined near the far end by two plated vias (r 0.15 mm,
+    hexagonal rings, each a fan in both sheets); the port drives the near end from the top strip's pad to the bottom
+    one's, so the current loop closes through the vias (magnetic and capacitive solves alike)."""
+    r_via = 0.15
+    sites = [(length - 1.0, 0.6), (length - 1.0, width - 0.6)]
+    sheets, fans, vias = [], [], []
+    for s, zz in ((0, 0.0), (1, gap)):
+        loops = [ngon(x, y, r_via, 6) for x, y in sites]
+        vert, tri = mesh_sheet(core, rect_loop(0, 0, length, width, h), loops, [], sites, h,
+                               lines=[((0.6, 0.0), (0.6, width))])
+        sheets.append((vert, tri, zz))
+        for x, y in sites:
+            fans.append((s, (x, y)))
+    for k, (x, y) in enumerate(sites):
+        vias.append((x, y, r_via, 0, 1, k, len(sites) + k))
+    terminals = {'top': [(1, (0.0, 0.0, 0.6, width))], 'bottom': [(0, (0.0, 0.0, 0.6, width))]}
+    return assemble(sheets, terminals, fans, [('loop', 'top', 'bottom')],
+                    dict(thickness=0.035e-3, sigma=5.8e7, er=4.3,
+                         description=f'{length:g} x {width:g} mm strip pair {gap} mm apart, 2 vias, h {h} mm'),
+                    vias)
+
+
 RNG = np.random.default_rng(20261203)
 
 
@@ -244,4 +277,10 @@ def main():
 
 
 if __name__ == '__main__':
-    main()
+    if sys.argv[1:] == ['viapair']:
+        RNG = np.random.default_rng(4)
+        data = viapair(reference_core())
+        np.savez_compressed(HERE / 'viapair.npz', **data)
+        print('viapair', len(data['tris']), 'triangles', len(data['nodes']), 'nodes', len(data['via_seg']), 'vias')
+    else:
+        main()

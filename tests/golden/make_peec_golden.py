@@ -6,8 +6,9 @@ The reference's MQS model class needs shapely only for meshing and region handli
 (their meshes are given). shapely is absent here, so a stand-in module that only provides its names is put in
 sys.modules before pcbqs.mqs is imported; no stand-in function is ever called. The model object is then built
 around the given mesh with the attributes MQS.__init__ would set (src/pcbqs/mqs.py:300-420): one node per triangle
-with terminals and via fans merged, RWG edges as branches, no via segments (each via joins one sheet here), DC
-sheet resistance, homogeneous dielectric er, capacitance on. Ports are 1 A current sources (MQS.source). The
+with terminals and via fans merged, RWG edges as branches, then the board's plated via segments (the via pair; the
+other boards' vias each join one sheet and have none), DC sheet resistance, homogeneous dielectric er, capacitance
+on. Ports are 1 A current sources (MQS.source). The
 reference's own methods then assemble and solve: MQS._assemble/_loops/_sheet_resistance/_set_potential,
 static_moments/edge_inductance (compiled core) and peec.solve.
 
@@ -69,6 +70,12 @@ def reference_model(board, conductor_loss='dc'):
     q.br = [(int(q.node_of[a]), int(q.node_of[b])) for a, b in zip(r.tp, r.tm)]
     q.n_rwg = r.Ne
     q.vseg, q.ne, q.nv = [], r.Ne, 0
+    # plated via segments (a board that has them): branches after the RWG edges, from the lower sheet's fan node to
+    # the upper one's (MQS.__init__, src/pcbqs/mqs.py:404-416)
+    for (x, y, rr, z0, z1), (a, b) in zip(board.via_seg if board.nv else [], board.via_ends()):
+        q.br.append((int(a), int(b)))
+        q.vseg.append((float(x), float(y), float(rr), float(z0), float(z1)))
+    q.nv = len(q.vseg)
     q.parts, q.plating = [], 25e-6
     q._mats = q._copper = q._potential = q._peec = q._mqs_iter = None
     q.ideal_terminals, q.factor_cache_bytes = True, 64 * 1024 ** 2
@@ -130,5 +137,8 @@ def stack(name='tiny', slab=(0.0, 0.2e-3, 4.3, 0.02)):
 
 
 if __name__ == '__main__':
-    main(tuple(sys.argv[1:]) or ('tiny', 'strip'))
-    stack('tiny')
+    if sys.argv[1:] == ['viapair']:
+        main(('viapair',), ('dc',))
+    else:
+        main(tuple(sys.argv[1:]) or ('tiny', 'strip'))
+        stack('tiny')

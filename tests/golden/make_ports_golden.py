@@ -5,11 +5,14 @@
 The model object is the one make_peec_golden.py builds around a given mesh (src/pcbqs/mqs.py:300-420), with
 capacitance off, so that pcbqs.mqs_ports.CopperPorts (src/pcbqs/mqs_ports.py:27-53) reduces the copper to its
 current ports by the reference's dense direct solve (direct_ports, :56-69). Only boards whose ports join terminals of
-one connected net qualify (the strip: p1 left->mid, p2 mid->right).
+one connected net qualify (the strip: p1 left->mid, p2 mid->right; the via pair: its loop through two plated vias).
 
-Writes tests/golden/ports_strip.npz: freqs (DC included), port names, Z (nf, np, np) and branch currents
+Writes tests/golden/ports_<board>.npz: freqs (DC included), port names, Z (nf, np, np) and branch currents
 (nf, nbranch, np) for conductor_loss 'dc' and 'slab', and the reference's rl_equivalent of the 'dc' response at its
-highest frequency (R_ohm, L_H).
+highest frequency (R_ohm, L_H); for a board with plated vias (the via pair) also the reference's via_resistance and
+via_inductance of its segments (src/pcbqs/mqs.py:132-153).
+
+    python tests/golden/make_ports_golden.py [strip|viapair]
 """
 import sys
 from pathlib import Path
@@ -41,8 +44,12 @@ def main(name='strip'):
             out['rl_R'], out['rl_L'] = np.array(rl['R_ohm']), np.array(rl['L_H'])
             out['rl_reference_Hz'] = rl['reference_Hz']
         print(name, loss, 'loops', q._assemble()['C'].shape, np.round(r.impedance[2], 9))
+    if b.nv:
+        from pcbqs.mqs import via_inductance, via_resistance
+        out['via_R'] = via_resistance(q.vseg, q.sigma, q.plating)
+        out['via_L'] = via_inductance(q.vseg)
     np.savez_compressed(HERE / f'ports_{name}.npz', **out)
 
 
 if __name__ == '__main__':
-    main()
+    main(*sys.argv[1:2])

@@ -76,3 +76,36 @@ def test_copper_ports_by_pencil_match_reference(device_library):
     assert np.abs(r.currents - g['currents_dc']).max() <= 1e-8 * np.abs(g['currents_dc']).max()
     with pytest.raises(ValueError, match='pencil'):
         CopperPorts(MagneticModel(Board.load('strip'), conductor_loss='slab')).extract(g['freqs'], method='pencil')
+
+
+def via_golden():
+    with np.load(GOLDEN / 'ports_viapair.npz') as d:
+        return {k: d[k] for k in d.files}
+
+
+def test_via_filaments_match_reference(device_library):
+    """Via segments' R (host) and L (device filament kernel, pcbqs_gb300_via_inductance) against the reference's
+    via_resistance / via_inductance of the via pair's segments."""
+    import torch
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import via_inductance, via_resistance
+    g, b = via_golden(), Board.load('viapair')
+    np.testing.assert_allclose(via_resistance(b.via_seg, b.sigma, b.plating), g['via_R'], rtol=1e-14)
+    out = torch.full((b.nv + 3, b.nv + 5), float('nan'), dtype=torch.float64, device='cuda')
+    via_inductance(b.via_seg, out[1:1 + b.nv, 2:2 + b.nv], out.device)
+    L = out[1:1 + b.nv, 2:2 + b.nv].cpu().numpy()
+    np.testing.assert_allclose(L, g['via_L'], rtol=1e-13)
+    assert torch.isnan(out[0]).all() and torch.isnan(out[1 + b.nv:]).all()      # writes stay in the view
+
+
+@pytest.mark.parametrize('loss', ['dc', 'slab'])
+def test_copper_ports_through_vias_match_reference(device_library, loss):
+    """The via pair's loop closes through its two plated vias: port Z and branch currents (via segments included)
+    against the reference's CopperPorts; the barrels keep their DC resistance under slab loss."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.ports import CopperPorts, MagneticModel
+    g = via_golden()
+    r = CopperPorts(MagneticModel(Board.load('viapair'), conductor_loss=loss)).extract(g['freqs'])
+    for fi in range(len(g['freqs'])):
+        assert np.abs(r.impedance[fi] - g[f'Z_{loss}'][fi]).max() <= 1e-8 * np.abs(g[f'Z_{loss}'][fi]).max(), fi
+    assert np.abs(r.currents - g[f'currents_{loss}']).max() <= 1e-8 * np.abs(g[f'currents_{loss}']).max()
