@@ -231,6 +231,10 @@ typedef struct pcbqs_gb300_peec_desc {
     const double *rscale;
     /* imaginary part of P (same leading dimension; null: P real), for a lossy dielectric stack */
     const double *Pim;
+    /* rscale applies to the first nscaled rows of R (the sheets' edges) and not to the rest (plated via barrels,
+     * which keep their DC resistance); 0: to every row. The preconditioners scale all of K^T R K (they need not be
+     * exact); the operator is exact. */
+    int64_t nscaled;
 } pcbqs_gb300_peec_desc;
 
 typedef struct pcbqs_gb300_peec pcbqs_gb300_peec;

@@ -44,7 +44,8 @@ class PeecDesc(ctypes.Structure):
                 ('K', CsrDesc), ('Kt', CsrDesc), ('T', CsrDesc), ('Tt', CsrDesc), ('R', CsrDesc),
                 ('L', c_void_p), ('ldl', ctypes.c_int64), ('P', c_void_p), ('ldp', ctypes.c_int64),
                 ('is_tree', c_void_p), ('pscale', ctypes.c_double), ('nsys', ctypes.c_int32),
-                ('omega', c_double_p), ('zscale', c_double_p), ('rscale', c_double_p), ('Pim', c_void_p)]
+                ('omega', c_double_p), ('zscale', c_double_p), ('rscale', c_double_p), ('Pim', c_void_p),
+                ('nscaled', ctypes.c_int64)]
 
 
 # name: (restype, argtypes)

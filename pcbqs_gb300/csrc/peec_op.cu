@@ -90,7 +90,7 @@ __global__ void k_tree_scale(int64_t n, int k, const int8_t *is_tree, const doub
 // V[e, s] = sum_f R[e, f] B[f, s] + j w_s LB[e, s] for copper rows e < ne; other passive rows (lumped parts with no
 // impedance here) are zero.
 __global__ void k_impedance(Csr R, int64_t nb, int k, const cd *B, const cd *LB, const double *omega,
-                            const cd *rscale, const int *sys, cd *V) {
+                            const cd *rscale, int64_t nscaled, const int *sys, cd *V) {
     const int64_t total = nb * k;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t e = t / k;
@@ -102,7 +102,7 @@ __global__ void k_impedance(Csr R, int64_t nb, int k, const cd *B, const cd *LB,
                 re += R.val[j] * b.x;
                 im += R.val[j] * b.y;
             }
-            const cd rs = rscale[sys[s]];
+            const cd rs = e < nscaled ? rscale[sys[s]] : make_double2(1.0, 0.0);
             const double rr = re * rs.x - im * rs.y, ri = re * rs.y + im * rs.x;
             const double w = omega[sys[s]];
             const cd lb = LB[t];
@@ -520,6 +520,7 @@ struct PeecOp : Operator {
     double *omega = nullptr, *zscale = nullptr, *walpha = nullptr, *inv_z = nullptr, *inv_p = nullptr;
     cd *rscale = nullptr;                 // per system factor on R (device)
     std::vector<cd> rscale_host;
+    int64_t nscaled = 0;                  // rows of R the factor applies to (the rest keep theirs)
     int cap = 0;               // columns the scratch holds
     cd *u = nullptr, *branch = nullptr, *lb = nullptr, *v = nullptr, *tq = nullptr, *pq = nullptr, *pq2 = nullptr;
     int64_t launches = 0;
@@ -569,7 +570,7 @@ struct PeecOp : Operator {
         k_tree_scale<<<grid_of(n_ * k), 256, 0, s>>>(n_, k, is_tree, walpha, sys, in, u);
         k_spmm<<<grid_of(nb * k), 256, 0, s>>>(K, k, u, branch, nullptr, sys, 0);
         if ((e = dense(single, ne, k, L, ldl, Lf, ldlf, branch, lb, s))) return e;
-        k_impedance<<<grid_of(nb * k), 256, 0, s>>>(R, nb, k, branch, lb, omega, rscale, sys, v);
+        k_impedance<<<grid_of(nb * k), 256, 0, s>>>(R, nb, k, branch, lb, omega, rscale, nscaled, sys, v);
         k_spmm<<<grid_of(n_ * k), 256, 0, s>>>(Kt, k, v, out, inv_z, sys, 0);
         if (nn > 0) {
             k_spmm<<<grid_of(nn * k), 256, 0, s>>>(T, k, in, tq, nullptr, sys, 0);
@@ -960,6 +961,7 @@ int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *d, pcbqs_gb300_peec **o
     op.L = d->L; op.ldl = d->ldl; op.P = d->P; op.ldp = d->ldp; op.is_tree = d->is_tree; op.pscale = d->pscale;
     op.Pim = d->nn > 0 ? d->Pim : nullptr;
     op.nsys = d->nsys;
+    op.nscaled = d->nscaled > 0 && d->nscaled < d->nb ? d->nscaled : d->nb;
     std::vector<double> w(d->nsys), z(d->nsys), wa(d->nsys), iz(d->nsys), ip(d->nsys, 1.0 / d->pscale);
     for (int s = 0; s < d->nsys; ++s) {
         w[s] = d->omega[s];

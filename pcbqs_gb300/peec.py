@@ -270,9 +270,6 @@ class PeecModel(PeecTopology):
                  restart=100, log=None, inner_tol=1e-4, conductor_loss='dc', conductor_faces=2, stack=None):
         if conductor_loss not in ('dc', 'slab') or conductor_faces not in (1, 2):
             raise ValueError('conductor_loss must be dc or slab; conductor_faces must be 1 or 2')
-        if conductor_loss == 'slab' and board.nv:
-            raise ValueError("conductor_loss='slab' with plated via segments is not supported by the PEEC solve (the "
-                             "barrels keep their DC resistance); the magnetic port reduction supports it")
         self.tol, self.maxiter, self.restart, self.inner_tol = tol, maxiter, restart, inner_tol
         self.conductor_loss, self.conductor_faces = conductor_loss, conductor_faces
         self.stack = stack
@@ -368,6 +365,7 @@ class PeecModel(PeecTopology):
         d.is_tree = self._dev['is_tree'].data_ptr()
         d.pscale = self.pscale
         d.Pim = self.Pim.data_ptr() if self.Pim is not None else None
+        d.nscaled = self.ne                 # the sheets' rows: via barrels keep their DC resistance
         d.nsys = len(omegas)
         self._omega = np.ascontiguousarray(omegas, float)
         self._zscale = np.ascontiguousarray(zscale, float)
@@ -564,9 +562,12 @@ class PeecModel(PeecTopology):
             # rhs = -K^T (R + j w L) baseline / zscale, per (frequency, port) column, in the clustered order.
             Lb = self._mv_L(baseline[:self.ni])
             Rb = self.R @ baseline[:self.ni]
+            Rv = np.zeros_like(Rb)             # the via barrels' part keeps its DC value
+            Rv[self.ne:] = Rb[self.ne:]
+            Rb[self.ne:] = 0
             Kpt = self.Kp.T
             ratio = self.resistance_ratio(f)
-            cols = [-(Kpt @ (ratio[fi] * Rb + 1j * w * Lb)) / zscale[fi] for fi, w in enumerate(omegas)]
+            cols = [-(Kpt @ (ratio[fi] * Rb + Rv + 1j * w * Lb)) / zscale[fi] for fi, w in enumerate(omegas)]
             rhs = np.ascontiguousarray(np.concatenate(cols, axis=1))      # (n, nf * np), column fi * np + port
             self.timings['rhs_s'] = time.perf_counter() - t2
             b_all = torch.as_tensor(rhs, device=self.device)

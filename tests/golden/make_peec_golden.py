@@ -138,7 +138,7 @@ def stack(name='tiny', slab=(0.0, 0.2e-3, 4.3, 0.02)):
 
 if __name__ == '__main__':
     if sys.argv[1:] == ['viapair']:
-        main(('viapair',), ('dc',))
+        main(('viapair',), ('dc', 'slab'))
     else:
         main(tuple(sys.argv[1:]) or ('tiny', 'strip'))
         stack('tiny')
