@@ -113,6 +113,30 @@ def h_segments(p0, p1, I, pts, device=0):
     return out if multi else out[:, :, 0]
 
 
+def h_field(board, currents, pts, device=0):
+    """H (n, 3) complex at pts (n, 3) m of a board's branch currents (nbranch,) or (nbranch, k) (edges' total
+    currents, then the plated via segments', then the ports'): the sheets' RWG currents by Biot-Savart and the via
+    segments as filaments along z; the ports are ideal sources without a radiating connector (the copper-port
+    reduction zeroes their currents). MQS.h_field (src/pcbqs/mqs.py:891-913) for boards without lumped parts."""
+    from .rwg import RWG
+    I = np.asarray(currents)
+    multi = I.ndim > 1
+    I2 = I if multi else I[:, None]
+    r = RWG(board.nodes, board.tris)             # the board's own coordinates (the fill's are centred)
+    ne, nv = r.Ne, board.nv
+    if I2.shape[0] < ne + nv:
+        raise ValueError('currents must hold every edge and via segment')
+    a, b = rwg_currents(r, I2[:ne] / r.l[:, None])
+    sheets = [(board.nodes, board.tris[idx], a[idx], b[idx], float(board.z[idx[0]]))
+              for idx in (np.flatnonzero(board.layer == lay) for lay in np.unique(board.layer))]
+    H = h_sheets(sheets, pts, device=device)
+    if nv:
+        v = np.asarray(board.via_seg)
+        H = H + h_segments(np.c_[v[:, 0], v[:, 1], v[:, 3]], np.c_[v[:, 0], v[:, 1], v[:, 4]], I2[ne:ne + nv], pts,
+                           device)
+    return H if multi else H[..., 0]
+
+
 # ---- the FFT near field on a uniform grid (src/pcbqs/biot.py:108-181, h_grid) ------------------------------------
 
 def current_grid(rwg, I, idx, gx, gy, per_cell=2.0, device=0):

@@ -65,6 +65,7 @@ def reference_model(board, conductor_loss='dc'):
     q.node_of, q.charge_of = board.node_of, None
     q.n_nodes = board.n_nodes
     q.terms = {name: [] for name in board.terminals}
+    q.term_tris = {name: np.asarray(ts) for name, ts in board.terminals.items()}
     q.term_node = {name: board.term_node(name) for name in board.terminals}
     r = q.rwg
     q.br = [(int(q.node_of[a]), int(q.node_of[b])) for a, b in zip(r.tp, r.tm)]

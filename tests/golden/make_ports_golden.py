@@ -48,6 +48,14 @@ def main(name='strip'):
         from pcbqs.mqs import via_inductance, via_resistance
         out['via_R'] = via_resistance(q.vseg, q.sigma, q.plating)
         out['via_L'] = via_inductance(q.vseg)
+        # the field of the last ('slab') response driven 1 A per port, sheets and vias, at 1 MHz, from the
+        # reference's MQS.h_field, on a line of points 0.5 mm over the upper strip and beside the vias
+        res = r.drive(np.ones((len(freqs), len(r.names))))
+        xs = np.linspace(-1e-3, 11e-3, 25)
+        pts = np.r_[np.c_[xs, np.full(25, 1e-3), np.full(25, 0.7e-3)], np.c_[np.full(5, 9e-3), np.full(5, 1e-3),
+                                                                             np.linspace(0.02e-3, 0.18e-3, 5)]]
+        out['field_pts'], out['field_fi'] = pts, 2
+        out['field_H'] = q.h_field(res, 2, pts)
     np.savez_compressed(HERE / f'ports_{name}.npz', **out)
 
 

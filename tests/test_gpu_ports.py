@@ -109,3 +109,20 @@ def test_copper_ports_through_vias_match_reference(device_library, loss):
     for fi in range(len(g['freqs'])):
         assert np.abs(r.impedance[fi] - g[f'Z_{loss}'][fi]).max() <= 1e-8 * np.abs(g[f'Z_{loss}'][fi]).max(), fi
     assert np.abs(r.currents - g[f'currents_{loss}']).max() <= 1e-8 * np.abs(g[f'currents_{loss}']).max()
+
+
+def test_field_of_port_currents_through_vias_matches_reference(device_library):
+    """H of the via pair's currents (1 A per port, slab loss, 1 MHz): the sheets by Biot-Savart and the via
+    segments as filaments (pcbqs_gb300.biot.h_field), against the reference's MQS.h_field of its own response."""
+    from pcbqs_gb300.biot import h_field
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.ports import CopperPorts, MagneticModel
+    g = via_golden()
+    b = Board.load('viapair')
+    r = CopperPorts(MagneticModel(b, conductor_loss='slab')).extract(g['freqs'])
+    res = r.drive(np.ones((len(g['freqs']), len(r.names))))
+    H = h_field(b, res.i[int(g['field_fi'])], g['field_pts'])
+    assert H.shape == g['field_H'].shape
+    assert np.abs(H - g['field_H']).max() <= 1e-7 * np.abs(g['field_H']).max()
+    Hk = h_field(b, res.i[[int(g['field_fi'])]].T, g['field_pts'])          # (n, 3, k) form
+    assert np.allclose(Hk[..., 0], H, rtol=0, atol=1e-12 * np.abs(H).max())
