@@ -317,6 +317,34 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *op, int k, const int32_t *sys
  * larger radius; scale = mu0 / 4 pi. Ordered on `stream` (no synchronization). Replaces via_inductance and
  * filament_mutual (src/pcbqs/mqs.py:40-45, :140-153). */
 int pcbqs_gb300_via_inductance(int64_t nv, const double *seg, double scale, double *L, int64_t ld, void *stream);
+/* The learned block preconditioner (no counterpart in the reference, whose GMRES uses sparse surrogates; block
+ * Jacobi is its fallback and the baseline it is trained against): out = y - sum_e g_e D_b^-1 A_bc y_c, y = D^-1 in,
+ * over edges e = (b <- c) between blocks of bs unknowns, gains g_e = w2 . tanh(W1 phi_e + b1) + b2 from the edge
+ * features phi_e (nfeat) with nhidden hidden units. params (device): W1 (nhidden x nfeat, row-major), b1, w2, b2.
+ * Device arrays, FP64, complex interleaved; dinv (nblk, bs, bs) the inverted diagonal blocks (identity-padded),
+ * E (nedge, bs, bs) the off-diagonal blocks (zero-padded), eptr (nblk + 1) / ecol (nedge) the edges grouped by
+ * destination block. Ordered on `stream` (no synchronization) except learned_gmres. */
+int pcbqs_gb300_learned_forward(int64_t nedge, int nfeat, int nhidden, const double *phi, const double *params,
+                                double *hidden, double *gains, void *stream);
+/* grad (device, nhidden * nfeat + 2 nhidden + 1) = dL/dparams for dgains = dL/dgains (deterministic sums). */
+int pcbqs_gb300_learned_backward(int64_t nedge, int nfeat, int nhidden, const double *phi, const double *params,
+                                 const double *hidden, const double *dgains, double *grad, void *stream);
+/* out (n, k) = M^-1 in (gains null: block-Jacobi alone); corrections (nedge, bs, k), if not null, receives the
+ * vectors u_e = D_b^-1 A_bc y_c (what the gains multiply). */
+int pcbqs_gb300_learned_apply(int64_t n, int bs, int64_t nblk, const int64_t *eptr, const int32_t *ecol,
+                              const double *dinv, const double *E, const double *gains, int k, const double *in,
+                              double *out, double *corrections, void *stream);
+/* dots[e] = sum over rows of block b and the k columns of Re(conj(S) u_e): with S = A^H r, the residual r's
+ * derivative along each gain is -2 dots / |z|^2 for the loss |A M^-1 z - z|^2 / |z|^2. */
+int pcbqs_gb300_learned_edge_dots(int64_t n, int bs, int64_t nblk, const int64_t *eptr, int k, const double *S,
+                                  const double *corrections, double *dots, void *stream);
+/* GMRES (this library's batched solver) on a dense complex row-major system A (n x n, row stride lda), k columns,
+ * right-preconditioned by block-Jacobi (gains null) or the learned preconditioner; status 5 if a column did not
+ * reach tol. iterations, residual: host arrays (k). Synchronizes `stream`. */
+int pcbqs_gb300_learned_gmres(int64_t n, const double *A, int64_t lda, int k, const double *b, double *x, double tol,
+                              int maxiter, int restart, int bs, int64_t nblk, const int64_t *eptr,
+                              const int32_t *ecol, const double *dinv, const double *E, const double *gains,
+                              int32_t *iterations, double *residual, void *stream);
 /* A x = b for a dense symmetric A = A_re + j A_im (n x n, row stride lda; A_im nullable: real A) and k complex
  * columns by GMRES, preconditioned by the diagonal of A_re (precondition 0, as the reference) or by the
  * single-precision Cholesky factor of A_re (A_re positive definite; exact for a real A, a close preconditioner for

@@ -120,6 +120,19 @@ PROTOTYPES = {
                                                      ctypes.POINTER(ctypes.c_double)]),
     'pcbqs_gb300_via_inductance': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_double, c_void_p,
                                                   ctypes.c_int64, c_void_p]),
+    'pcbqs_gb300_learned_forward': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, ctypes.c_int, c_void_p, c_void_p,
+                                                   c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_learned_backward': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, ctypes.c_int, c_void_p, c_void_p,
+                                                    c_void_p, c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_learned_apply': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, ctypes.c_int64, c_void_p, c_void_p,
+                                                 c_void_p, c_void_p, c_void_p, ctypes.c_int, c_void_p, c_void_p,
+                                                 c_void_p, c_void_p]),
+    'pcbqs_gb300_learned_edge_dots': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, ctypes.c_int64, c_void_p,
+                                                     ctypes.c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_learned_gmres': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, ctypes.c_int, c_void_p,
+                                                 c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                 c_int32_p, c_double_p, c_void_p]),
     'pcbqs_gb300_lu_factor_c64': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, ctypes.c_int, ctypes.c_int,
                                                  c_int32_p, c_void_p]),
     'pcbqs_gb300_cholesky_f32': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,

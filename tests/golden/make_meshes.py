@@ -18,6 +18,9 @@ The boards themselves are synthetic stand-ins with the shapes and sizes of the b
           end between the strips                                                              (~800 triangles)
 
     python tests/golden/make_meshes.py viapair    (that board alone; the others keep their meshes)
+    python tests/golden/make_meshes.py train      (train_0 .. train_5: seeded random small boards, alternately a
+                                                   plane pair and a via-joined strip pair of random sizes, vias and
+                                                   mesh sizes; the learned preconditioner's training systems)
 """
 import sys
 from pathlib import Path
@@ -259,6 +262,23 @@ def viapair(core, length=10.0, width=2.0, gap=0.2, h=0.3):
                     vias)
 
 
+def training_board(core, seed):
+    """A seeded random small board: a plane pair (even seeds) or a via-joined strip pair (odd seeds)."""
+    rng = np.random.default_rng(1000 + seed)
+    if seed % 2 == 0:
+        size = float(rng.uniform(3.5, 6.0))
+        gap, n_vias, h = float(rng.uniform(0.15, 0.4)), int(rng.integers(2, 5)), float(rng.uniform(0.38, 0.5))
+        for _ in range(20):              # a site draw that fits the vias and ports
+            try:
+                return planes(core, size=size, gap=gap, n_vias=n_vias, n_ports=2, h=h, seed=int(rng.integers(1 << 30)),
+                              margin=0.8, spacing=1.1)
+            except ValueError:
+                continue
+        raise ValueError('no site draw fits')
+    return viapair(core, length=float(rng.uniform(6.0, 12.0)), width=float(rng.uniform(1.6, 2.8)),
+                   gap=float(rng.uniform(0.15, 0.4)), h=float(rng.uniform(0.3, 0.42)))
+
+
 RNG = np.random.default_rng(20261203)
 
 
@@ -282,5 +302,12 @@ if __name__ == '__main__':
         data = viapair(reference_core())
         np.savez_compressed(HERE / 'viapair.npz', **data)
         print('viapair', len(data['tris']), 'triangles', len(data['nodes']), 'nodes', len(data['via_seg']), 'vias')
+    elif sys.argv[1:] == ['train']:
+        core = reference_core()
+        for i in range(6):
+            RNG = np.random.default_rng(100 + i)
+            data = training_board(core, i)
+            np.savez_compressed(HERE / f'train_{i}.npz', **data)
+            print(f'train_{i}', len(data['tris']), 'triangles', data['description'])
     else:
         main()
