@@ -14,7 +14,7 @@ passes, the preconditioner and the gradient dots are the CUDA kernels of csrc/le
 the dense products with A and A^H are cuBLAS. Training data: the systems of seeded random boards
 (tests/golden/train_*.npz) at random frequencies; the boards named in the tests are held out.
 
-    python -m pcbqs_gb300.learned train [out.npz]    # train on the random boards and save the parameters
+    python -m pcbqs_gb300.learned train [out.npz [l2]]    # train on the random boards and save the parameters
 """
 import ctypes
 import sys
@@ -168,8 +168,9 @@ def apply(system, gains, X, corrections=False):
     return (out, U) if corrections else out
 
 
-def loss_and_gradient(system, params, Z):
-    """(loss |A M^-1 Z - Z|^2 / |Z|^2, dloss/dparams) through the device kernels."""
+def loss_and_gradient(system, params, Z, l2=0.0):
+    """(loss |A M^-1 Z - Z|^2 / |Z|^2, dloss/dparams) through the device kernels; l2 > 0 adds l2 mean(g^2) to
+    the gradient (not to the loss reported)."""
     lib = _lib.load()
     hidden, gains = forward(system, params)
     X, U = apply(system, gains, Z, corrections=True)
@@ -181,6 +182,8 @@ def loss_and_gradient(system, params, Z):
                                                  S.data_ptr(), U.data_ptr(), dots.data_ptr(), _stream(Z.device)),
                lib)
     dgains = (-2 / zz) * dots[:system.nedge]
+    if l2 and system.nedge:
+        dgains = dgains + (2 * l2 / system.nedge) * gains
     loss = float(torch.vdot(R.flatten(), R.flatten()).real) / zz
     return loss, backward(system, params, hidden, dgains.contiguous())
 
@@ -200,9 +203,10 @@ def probes(system, k=16, seed=0):
                          torch.randn(shape, dtype=torch.float64, device=system.A.device, generator=g))
 
 
-def train(systems, steps=300, lr=0.02, k=16, seed=0, log=None):
-    """Adam on the mean over systems of loss / block-Jacobi's loss, fixed probes per system. Returns (params,
-    history of the mean relative loss)."""
+def train(systems, steps=300, lr=0.02, k=16, seed=0, l2=0.0, log=None):
+    """Adam on the mean over systems of loss / block-Jacobi's loss (+ l2 times the mean squared gain, which keeps
+    the corrections modest where the probes do not ask for them), fixed probes per system. Returns (params, history
+    of the mean relative loss)."""
     dev = systems[0].A.device
     params = initial_params(seed, dev)
     Zs = [probes(s, k, seed + i) for i, s in enumerate(systems)]
@@ -216,7 +220,7 @@ def train(systems, steps=300, lr=0.02, k=16, seed=0, log=None):
         grad = torch.zeros_like(params)
         total = 0.0
         for s, Z, b in zip(systems, Zs, base):
-            loss, gr = loss_and_gradient(s, params, Z)
+            loss, gr = loss_and_gradient(s, params, Z, l2 * b)
             total += loss / b
             grad += gr / b
         grad /= len(systems)
@@ -291,9 +295,11 @@ def main(argv):
         print(__doc__)
         return 2
     out = Path(argv[1]) if len(argv) > 1 else PARAMS
+    l2 = float(argv[2]) if len(argv) > 2 else 0.0
     systems = training_systems(log=print)
-    params, history = train(systems, log=print)
-    save(params, out, history=np.asarray(history), boards=np.array(TRAIN_BOARDS), freqs=np.array(TRAIN_FREQS))
+    params, history = train(systems, l2=l2, log=print)
+    save(params, out, history=np.asarray(history), boards=np.array(TRAIN_BOARDS), freqs=np.array(TRAIN_FREQS),
+         l2=l2)
     print(f'saved {out}: relative loss {history[0]:.4f} -> {history[-1]:.4f}')
     return 0
 
