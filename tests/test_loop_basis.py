@@ -15,8 +15,10 @@ def lib():
     return _lib.load()
 
 
-@pytest.mark.parametrize('board', ['tiny', 'strip', 'planes'])
+@pytest.mark.parametrize('board', ['tiny', 'strip', 'planes', 'viapair'])
 def test_native_loop_basis_matches_restatement(lib, board):
+    """The via pair adds its plated via segments as branches after the RWG edges (non-source branches that join
+    the two sheets' islands), as MQS does."""
     from pcbqs_gb300.board import Board
     from pcbqs_gb300.geometry import prepare
     from pcbqs_gb300.peec import loop_basis
@@ -26,8 +28,9 @@ def test_native_loop_basis_matches_restatement(lib, board):
     r = RWG(g.nodes, g.tris)
     of = b.node_of
     ends = [(int(of[a]), int(of[c])) for a, c in zip(r.tp, r.tm)]
+    ends += [tuple(int(v) for v in e) for e in b.via_ends()]
     ends += [(b.term_node(a), b.term_node(c)) for _, a, c in b.ports]
-    is_src = np.r_[np.zeros(r.Ne, bool), np.ones(len(b.ports), bool)]
+    is_src = np.r_[np.zeros(r.Ne + b.nv, bool), np.ones(len(b.ports), bool)]
     C, src, tree, col_branch = loop_basis(b.n_nodes, ends, is_src, r.Ne)
     Co, srco, treeo, col_brancho = G.loop_basis(b.n_nodes, ends, is_src, r.Ne)
     assert np.array_equal(tree, treeo)

@@ -44,3 +44,19 @@ def test_drive_is_the_weighted_sum_of_port_responses():
     np.testing.assert_allclose(i, (r.currents * a[:, None, :]).sum(-1), rtol=1e-14, atol=0)
     with pytest.raises(ValueError, match='amplitudes'):
         r.drive(np.ones((nf + 1, npo)))
+
+
+def test_via_segments_of_the_via_pair():
+    """The via pair's plated segments: read from the board, the branches they add (lower sheet's fan node to the
+    upper one's, as MQS orders them), and their barrel resistance against the reference's via_resistance."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import via_resistance
+    b = Board.load('viapair')
+    assert b.nv == 2 and b.via_seg.shape == (2, 5)
+    ends = b.via_ends()
+    lower, upper = b.layer[[b.fans[f][0] for f in b.via_fans[:, 0]]], b.layer[[b.fans[f][0] for f in b.via_fans[:, 1]]]
+    assert (lower == 0).all() and (upper == 1).all() and (ends[:, 0] != ends[:, 1]).all()
+    with np.load(GOLDEN / 'ports_viapair.npz') as d:
+        ref = d['via_R']
+    np.testing.assert_allclose(via_resistance(b.via_seg, b.sigma, b.plating), ref, rtol=1e-14)
+    assert Board.load('planes').nv == 0 and Board.load('planes').via_ends().shape == (0, 2)
