@@ -344,7 +344,8 @@ def main():
                             board=args.board, triangles=model.fill.nt, edges=ne, nodes=nn, unknowns=model.n,
                             precondition=args.precondition, factor_math=args.factor_math, mode=args.mode,
                             gmres_tol=model.tol,
-                            gmres_iterations=result.iterations.tolist(), parallelism=f'replicas x{world}',
+                            gmres_iterations=result.iterations.tolist(),
+                            gmres_outer_steps=timings[-1].get('outer_steps'), parallelism=f'replicas x{world}',
                             l2='inputs larger than L2 (L 8.9 GB)'),
                 fill_gbs=round(fill_gbs, 2),
                 fp64_comparator=comparator,
