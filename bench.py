@@ -68,6 +68,22 @@ def rank_info():
     return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
 
 
+def replica_frequency(freq, rank):
+    """Replicas: each rank solves its own frequency (1 % apart), the same work per rank (weak scaling)."""
+    return freq * (1 + 0.01 * rank)
+
+
+def job_seconds_per_frequency(ms_local, world, dist=None, device='cuda'):
+    """(step ms, the maximum over ranks; whole-job seconds per frequency: world frequencies per step)."""
+    ms = float(ms_local)
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    return ms, ms / 1e3 / world
+
+
 class Clocks:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
     QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
@@ -257,7 +273,7 @@ def main():
     from pcbqs_gb300.board import Board
     from pcbqs_gb300.peec import PeecModel
     board = Board.load(args.board)
-    freq = args.freq * (1 + 0.01 * rank)          # replicas: each rank its own frequency
+    freq = replica_frequency(args.freq, rank)
     model = PeecModel(board, device=local)
 
     mixed = args.mode == 'mixed'
@@ -286,12 +302,7 @@ def main():
         dist.barrier()
     clock_info = clocks.stop()
     launches = lib.pcbqs_gb300_kernel_launches() - launches0
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t)
-    value = ms / 1e3 / world
+    ms, value = job_seconds_per_frequency(e0.elapsed_time(e1) / args.steps, world, dist)
     Z_headline = result.impedance[0]
     comparator = None
     fp64_timings = timings[-1]
