@@ -12,8 +12,8 @@
 //   panel stream: getrf of the panel (cuSOLVER, pivots relative to row j) -> k_lu_pivot_plan turns the pivots into
 //                 global 1-based rows (the getrf convention) and the permutation of the rows they touch
 //   main stream:  k_lu_swap_rows applies that permutation to every other column; triangular solve for the block
-//                 row U12; GEMM of the next panel's columns; (event: the next panel may start); triangular solve
-//                 and GEMM of the remaining columns.
+//                 row U12; the next panel's columns updated (GEMM into scratch, k_trailing_subtract); (event: the
+//                 next panel may start); triangular solve and update of the remaining columns.
 #include <algorithm>
 #include <cstdio>
 #include <vector>

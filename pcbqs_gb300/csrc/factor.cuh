@@ -13,21 +13,21 @@ enum LuMath : int {
     LU_GEMM_BF16X9 = 1,    // FP32 GEMMs emulated on the tensor cores with three BF16 terms per operand
 };
 
+constexpr int MAX_BLOCK_PUBLIC = 4096;   // widest panel the blocked factorizations take
+
 // Factors the n x n column-major complex64 matrix A (leading dimension n) in place as P A = L U, L unit lower,
 // with ipiv[i] the 1-based row swapped with row i (the same layout and pivots as cusolverDnCgetrf, so the
 // triangular solvers of that factor apply unchanged). Right-looking in `block`-column panels: each panel is
 // factored by cuSOLVER on a second stream while the main stream finishes the previous step's trailing update
 // (one step of lookahead), its row swaps are applied to the other columns by a gather kernel, the block row of U
-// comes from a triangular solve and the trailing matrix from one large GEMM (`math`). Returns cudaSuccess, or an
-// error; *singular = the first zero pivot's 1-based index (0 if none). Ordered on `stream`; returns after the
-// factor is complete.
-constexpr int MAX_BLOCK_PUBLIC = 4096;   // widest panel the blocked factorizations take
-
+// comes from a triangular solve and the trailing update from one large GEMM (`math`) into a scratch matrix and a
+// subtract pass. Returns cudaSuccess, or an error; *singular = the first zero pivot's 1-based index (0 if none).
+// Ordered on `stream`; returns after the factor is complete.
 cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular);
 
 // Factors the n x n column-major symmetric positive definite FP32 matrix A (leading dimension lda >= n, best a
-// multiple of 32 so that the GEMMs take their aligned, tensor-core forms; the lower triangle is read) in place as A = L L^T, L in the lower triangle (cusolverDnSpotrf's layout; the strict upper
-// triangle is left with intermediate values). Right-looking in `block`-column panels: the diagonal block by
+// multiple of 32 so that the GEMMs take their aligned forms; the lower triangle is read) in place as A = L L^T,
+// L in the lower triangle (cusolverDnSpotrf's layout; the strict upper triangle is left with intermediate values). Right-looking in `block`-column panels: the diagonal block by
 // cuSOLVER potrf and the panel below it by a triangular solve, both on a second stream one step ahead, and the
 // trailing lower triangle by one GEMM per block column (`math`). *info = the 1-based order of the first leading
 // minor that is not positive definite (0 if none). Ordered on `stream`; returns after the factor is complete.
