@@ -27,7 +27,7 @@ def _rank(rank, world, port, out):
 def test_replicas_take_the_slowest_rank():
     import torch.multiprocessing as mp
     world = 2
-    with mp.Manager() as manager:
+    with mp.get_context('spawn').Manager() as manager:          # no fork of this multi-threaded process
         out = manager.dict()
         mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
         results = dict(out)
