@@ -44,9 +44,11 @@ def build():
 
 def build_reference():
     """Compile the reference's own core into oracle/_ref/ where its sources exist (this container only)."""
-    if not Path(os.environ.get('PCBQS_REFERENCE_CORE', '/root/reference/src/pcbqs/core')).exists():
+    from .reference import SOURCE
+    core = SOURCE / 'pcbqs' / 'core' if SOURCE is not None else None
+    if core is None or not core.exists():
         return None
-    subprocess.run(['make', '-s', '-C', str(HERE), 'ref'], check=True)
+    subprocess.run(['make', '-s', '-C', str(HERE), 'ref', f'REF_SRC={core}'], check=True)
     found = sorted((HERE / '_ref').glob('_core*.so'))
     return found[0] if found else None
 

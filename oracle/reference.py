@@ -11,11 +11,12 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-SOURCE = Path(os.environ.get('PCBQS_REFERENCE_SRC', '/root/reference/src'))
+_SOURCE = os.environ.get('PCBQS_REFERENCE_SRC')      # the reference checkout's src/ directory (required)
+SOURCE = Path(_SOURCE) if _SOURCE else None
 
 
 def available():
-    return (SOURCE / 'pcbqs' / '__init__.py').exists()
+    return SOURCE is not None and (SOURCE / 'pcbqs' / '__init__.py').exists()
 
 
 def load_reference(build=True):
@@ -24,7 +25,8 @@ def load_reference(build=True):
     if 'pcbqs' in sys.modules and hasattr(sys.modules['pcbqs'], '_core'):
         return sys.modules['pcbqs']
     if not available():
-        raise ImportError(f'reference checkout not found at {SOURCE}')
+        raise ImportError(f'reference checkout not found (PCBQS_REFERENCE_SRC={SOURCE}): set it to the checkout\'s src '
+                          'directory')
     found = sorted(glob.glob(str(HERE / '_ref' / '_core*.so')))
     if not found and build:
         from .oracle import build_reference

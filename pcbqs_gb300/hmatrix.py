@@ -4,14 +4,14 @@ near leaves and ACA far blocks built by device kernels, and the compressed produ
     H = DeviceHMatrix(fill, tol=1e-6, leaf=64, eta=1.0, rank=32)     # fill: a DeviceFill (its geometry and RWG)
     Y = H.matmat(X)                                                    # X (ne, k) complex torch tensor on the GPU
 
-Restates pcbqs's HMatrix (src/pcbqs/hmatrix.py:59-221): the bisection tree on support-box centres (widest axis,
-stable sort, halves), admissibility gap > eta * max(diameter) with 3-D boxes, level-by-level construction where a
-block whose ACA is not accepted is subdivided (or made dense when both clusters are leaves), and diagonal blocks
-symmetrized. The entries are those of compressed.edge_inductance (src/pcbqs/compressed.py:60-96) with the support
+The counterpart of pcbqs's HMatrix (src/pcbqs/hmatrix.py:59-221), with a tree of its own: a flat-array binary tree
+cut at the median of the support-box centres along their principal axis; the reference's admissibility (box gap >
+eta * the larger diagonal, 3-D boxes); blocks decided a tree level at a time, both clusters refined together, a
+block whose ACA is not accepted refined further (or made dense when both clusters are leaves), and only the upper
+half of the symmetric block structure stored (each block applied both ways, diagonal blocks symmetrized). The entries are those of compressed.edge_inductance (src/pcbqs/compressed.py:60-96) with the support
 boxes of compressed._boxes (:54-57). ACA runs one CTA per block with a rank cap min(rank, 0.7 m n / (m + n)).
 """
 import ctypes
-from dataclasses import dataclass
 
 import numpy as np
 import torch
@@ -20,40 +20,65 @@ from . import _lib
 from .fill import EPS0, MU0
 
 
-@dataclass
-class Cluster:
-    ids: np.ndarray
-    lo: np.ndarray
-    hi: np.ndarray
-    children: tuple = ()
+class ClusterTree:
+    """A binary cluster tree over n items with 3-D bounding boxes (lo, hi), held in flat arrays.
 
+    Node k owns the items perm[start[k]:stop[k]]; kids[k] = (left, right) node indices, or (-1, -1) at a leaf.
+    Nodes are made breadth first: a node with more than `leaf` items is cut through the median of its box
+    centres projected on their principal axis (the dominant eigenvector of their covariance), so both halves hold
+    half the items whatever the cloud's orientation, and every level of the tree is balanced."""
 
-def cluster_tree(lo, hi, leaf):
-    def tree(ids):
-        node = Cluster(ids, lo[ids].min(0), hi[ids].max(0))
-        if len(ids) > leaf:
-            centers = (lo[ids] + hi[ids]) / 2
-            axis = np.argmax(np.ptp(centers, axis=0))
-            order = ids[np.argsort(centers[:, axis], kind='stable')]
-            mid = len(ids) // 2
-            node.children = (tree(order[:mid]), tree(order[mid:]))
-        return node
-    return tree(np.arange(len(lo)))
+    def __init__(self, lo, hi, leaf):
+        lo, hi = np.asarray(lo, float), np.asarray(hi, float)
+        centre = 0.5 * (lo + hi)
+        self.perm = np.arange(len(lo))
+        start, stop, kids = [0], [len(lo)], [[-1, -1]]
+        k = 0
+        while k < len(start):
+            a, b = start[k], stop[k]
+            if b - a > leaf:
+                seg = self.perm[a:b]
+                c = centre[seg] - centre[seg].mean(0)
+                _, vec = np.linalg.eigh(c.T @ c)
+                proj = c @ vec[:, -1]
+                half = (b - a) // 2
+                self.perm[a:b] = seg[np.argpartition(proj, half)]
+                kids[k] = [len(start), len(start) + 1]
+                start += [a, a + half]
+                stop += [a + half, b]
+                kids += [[-1, -1], [-1, -1]]
+            k += 1
+        self.start, self.stop = np.asarray(start), np.asarray(stop)
+        self.kids = np.asarray(kids)
+        self.lo = np.array([lo[self.ids(k)].min(0) for k in range(len(start))])
+        self.hi = np.array([hi[self.ids(k)].max(0) for k in range(len(start))])
+        self.diam2 = ((self.hi - self.lo) ** 2).sum(1)
 
+    def ids(self, k):
+        return self.perm[self.start[k]:self.stop[k]]
 
-def _admissible(a, b, eta):
-    gap = np.linalg.norm(np.maximum(0, np.maximum(a.lo - b.hi, b.lo - a.hi)))
-    diameter = max(np.linalg.norm(a.hi - a.lo), np.linalg.norm(b.hi - b.lo))
-    return a is not b and gap > eta * diameter
+    def size(self, k):
+        return int(self.stop[k] - self.start[k])
 
+    def leaf(self, k):
+        return self.kids[k, 0] < 0
 
-def _children(a, b):
-    if a is b:
-        x, y = a.children
-        return [(x, x), (x, y), (y, y)]
-    if a.children and (not b.children or len(a.ids) >= len(b.ids)):
-        return [(child, b) for child in a.children]
-    return [(a, child) for child in b.children]
+    def separated(self, i, j, eta):
+        """Whether the block (i, j) is far enough to compress: the distance between the two boxes exceeds eta
+        times the larger box diagonal (the admissibility of the reference's HMatrix, src/pcbqs/hmatrix.py:152-156,
+        compared here in squares)."""
+        if i == j:
+            return False
+        gap = np.maximum(0.0, np.maximum(self.lo[i] - self.hi[j], self.lo[j] - self.hi[i]))
+        return float(gap @ gap) > eta * eta * max(self.diam2[i], self.diam2[j])
+
+    def refine(self, i, j):
+        """The sub-blocks that replace the block (i, j): both clusters cut where both have children (only the
+        one that has, otherwise). A diagonal block keeps the upper pairs (p <= q) of its children, since a block
+        below the diagonal is the transpose of one above it and the product applies each stored block both ways."""
+        left = [i] if self.leaf(i) else list(self.kids[i])
+        right = [j] if self.leaf(j) else list(self.kids[j])
+        return [(int(p), int(q)) for p in left for q in right if i != j or p <= q]
 
 
 def support_boxes(fill):
@@ -90,60 +115,59 @@ class DeviceHMatrix:
             lo, hi = np.c_[v.min(1), g.z], np.c_[v.max(1), g.z]
         else:
             raise ValueError("kernel must be 'inductance' or 'potential'")
-        root = cluster_tree(lo, hi, leaf)
+        tree = ClusterTree(lo, hi, leaf)
+        self.tree = tree
         lib = _lib.load()
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-        near = float(fill.near)
         blocks, stores = [], []       # final (a_ids, b_ids, store index, offset, rank, cap, same)
-        pending = [(root, root)]
+        level = [(0, 0)]              # the block (root, root), then each level's undecided blocks
         self.entries = 0
-        while pending:
-            admissible, dense, following = [], [], []
-            for a, b in pending:
-                if _admissible(a, b, eta):
-                    cap = min(rank, int(0.7 * len(a.ids) * len(b.ids) / (len(a.ids) + len(b.ids))))
+        while level:
+            compress, exact, deeper = [], [], []
+            for i, j in level:
+                if tree.separated(i, j, eta):
+                    m, n = tree.size(i), tree.size(j)
+                    cap = min(rank, int(0.7 * m * n / (m + n)))
                     if cap >= 1:
-                        admissible.append((a, b, cap))
+                        compress.append((i, j, cap))
                         continue
-                if not a.children and not b.children:
-                    dense.append((a, b))
-                else:
-                    following.extend(_children(a, b))
-            failed_leaves = []
-            if admissible:
-                ranks, store, offsets = self._aca_round(admissible, lib, stream)
-                for (a, b, cap), off, rk in zip(admissible, offsets, ranks):
+                (exact if tree.leaf(i) and tree.leaf(j) else deeper).append((i, j))
+            deeper = [sub for i, j in deeper for sub in tree.refine(i, j)]
+            if compress:
+                ranks, store, offsets = self._aca_round(compress, lib, stream)
+                for (i, j, cap), off, rk in zip(compress, offsets, ranks):
                     if rk >= 0:
-                        self.entries += cap * (len(a.ids) + len(b.ids))
-                        blocks.append((a.ids, b.ids, len(stores), off, int(rk), cap, False))
-                    elif not a.children and not b.children:
-                        failed_leaves.append((a, b))        # not compressible: a dense leaf
+                        self.entries += cap * (tree.size(i) + tree.size(j))
+                        blocks.append((tree.ids(i), tree.ids(j), len(stores), off, int(rk), cap, False))
+                    elif tree.leaf(i) and tree.leaf(j):
+                        exact.append((i, j))                # ACA not accepted on two leaves: a dense block
                     else:
-                        following.extend(_children(a, b))
+                        deeper.extend(tree.refine(i, j))
                 stores.append(store)
-            if dense or failed_leaves:
-                self._dense_round(dense + failed_leaves, blocks, stores, lib, stream)
+            if exact:
+                self._dense_round(exact, blocks, stores, lib, stream)
             if log:
                 log(f'hmatrix: {len(blocks):,} blocks so far')
-            pending = following
+            level = deeper
         self._pack(blocks, stores)
 
     def _aca_round(self, admissible, lib, stream):
-        """ACA of one level's admissible blocks on the device: (ranks (-1: not accepted), store, store offsets)."""
-        dev = self.fill.device
+        """ACA of one level's admissible blocks (tree node pairs) on the device: (ranks (-1: not accepted), store,
+        store offsets)."""
+        dev, tree = self.fill.device, self.tree
         idx, meta, offset, ioff, offsets = [], [], 0, 0, []
-        for a, b, cap in admissible:
-            la, lb = len(a.ids), len(b.ids)
+        for i, j, cap in admissible:
+            la, lb = tree.size(i), tree.size(j)
             meta.append([ioff, la, ioff + la, lb, offset, cap, 0, -1])
             offsets.append(offset)
-            idx += [a.ids, b.ids]
+            idx += [tree.ids(i), tree.ids(j)]
             ioff += la + lb
             offset += la * cap + cap * lb + 32 * lb            # U, V and the check rows
         meta_d = torch.as_tensor(np.asarray(meta, np.int64), device=dev)
         idx_d = torch.as_tensor(np.concatenate(idx).astype(np.int64), device=dev)
         store = torch.empty(max(offset, 1), dtype=torch.float64, device=dev)
         ids = torch.as_tensor(np.arange(len(admissible), dtype=np.int64), device=dev)
-        used_stride = max(len(a.ids) for a, _, _ in admissible)
+        used_stride = max(tree.size(i) for i, _, _ in admissible)
         used = torch.empty(len(admissible) * used_stride, dtype=torch.uint8, device=dev)
         near = float(self.fill.near)
         _lib.check(lib.pcbqs_gb300_hmatrix_build(
@@ -154,12 +178,14 @@ class DeviceHMatrix:
         return meta_d[:, 7].cpu().numpy(), store, offsets
 
     def _dense_round(self, pairs, blocks, stores, lib, stream):
-        dev = self.fill.device
+        """Exact dense blocks (tree node pairs) on the device, appended to `blocks`; a diagonal block is stored
+        symmetrized."""
+        dev, tree = self.fill.device, self.tree
         idx, meta, offset, ioff = [], [], 0, 0
-        for a, b in pairs:
-            la, lb = len(a.ids), len(b.ids)
-            meta.append([ioff, la, ioff + la, lb, offset, 0, int(a is b), -1])
-            idx += [a.ids, b.ids]
+        for i, j in pairs:
+            la, lb = tree.size(i), tree.size(j)
+            meta.append([ioff, la, ioff + la, lb, offset, 0, int(i == j), -1])
+            idx += [tree.ids(i), tree.ids(j)]
             ioff += la + lb
             offset += la * lb
         meta_d = torch.as_tensor(np.asarray(meta, np.int64), device=dev)
@@ -172,9 +198,9 @@ class DeviceHMatrix:
             self._edges[0].data_ptr(), self._edges[1].data_ptr(), self._edges[2].data_ptr(), self.ne,
             self.factor, meta_d.data_ptr(), ids.data_ptr(), len(pairs), None, 0, idx_d.data_ptr(),
             self.tol, store.data_ptr(), None, 0, stream), lib)
-        for (a, b), m in zip(pairs, meta):
-            self.entries += len(a.ids) * len(b.ids)
-            blocks.append((a.ids, b.ids, len(stores), m[4], -1, 0, a is b))
+        for (i, j), m in zip(pairs, meta):
+            self.entries += tree.size(i) * tree.size(j)
+            blocks.append((tree.ids(i), tree.ids(j), len(stores), m[4], -1, 0, i == j))
         stores.append(store)
 
     def _pack(self, blocks, stores):

@@ -8,6 +8,9 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 GOLDEN = ROOT / 'tests' / 'golden'
 sys.path.insert(0, str(ROOT))
+import __graft_entry__  # noqa: E402
+
+__graft_entry__.reference_source()
 
 
 def pytest_configure(config):

@@ -22,9 +22,9 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 sys.path.insert(0, str(ROOT))
 
-from oracle.reference import load_reference  # noqa: E402
+from oracle.reference import SOURCE, load_reference  # noqa: E402
 
-REFERENCE = Path('/root/reference')
+REFERENCE = SOURCE.parent if SOURCE is not None else None      # the reference checkout
 SLAB = dict(z0=0.0, z1=0.2e-3, er=4.3, tand=0.02)
 
 

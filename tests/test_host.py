@@ -98,3 +98,41 @@ def test_reference_engine_selects_the_plugin_and_raises_without_device(tiny8, mo
         with pytest.raises(RuntimeError, match='GB300 fill unavailable'):
             backends.FillEngine(tiny8['nodes'], tiny8['tris'], tiny8['z'], backend='gb300')
         assert loaded == [True]
+
+
+@pytest.mark.parametrize('board', ['tiny', 'strip'])
+def test_cluster_tree_partition_covers_each_entry_once(board):
+    """The H-matrix block structure: every (row, column) of the symmetric matrix lies in exactly one stored block
+    or in the transpose of one (diagonal blocks only once), and every compressed block is admissible."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.geometry import prepare
+    from pcbqs_gb300.hmatrix import ClusterTree
+    from pcbqs_gb300.rwg import RWG
+    b = Board.load(board)
+    g = prepare(b.nodes, b.tris, b.z, 1)
+    r = RWG(g.nodes, g.tris)
+    v = g.nodes[g.tris]
+    lo_t, hi_t = np.c_[v.min(1), g.z], np.c_[v.max(1), g.z]
+    support = np.stack((r.tp, r.tm), axis=1)
+    lo, hi = lo_t[support].min(1), hi_t[support].max(1)
+    tree = ClusterTree(lo, hi, 16)
+    leaves = np.concatenate([tree.ids(k) for k in range(len(tree.start)) if tree.leaf(k)])
+    np.testing.assert_array_equal(np.sort(leaves), np.arange(r.Ne))
+    assert all(tree.size(k) <= 16 for k in range(len(tree.start)) if tree.leaf(k))
+    count = np.zeros((r.Ne, r.Ne), np.int32)
+    level, far = [(0, 0)], 0
+    while level:
+        deeper = []
+        for i, j in level:
+            if tree.separated(i, j, 1.0):
+                far += 1
+            elif not (tree.leaf(i) and tree.leaf(j)):
+                deeper += tree.refine(i, j)
+                continue
+            a, c = tree.ids(i), tree.ids(j)
+            count[np.ix_(a, c)] += 1
+            if i != j:
+                count[np.ix_(c, a)] += 1
+        level = deeper
+    assert far > 0
+    np.testing.assert_array_equal(count, 1)
