@@ -64,7 +64,7 @@ def parse():
     p.add_argument('--case', default=None,
                    help='time one kernel case small enough for a full ncu capture instead of the benchmark: '
                         'fill:BOARD[:TRIANGLES] | lu:BOARD[:K...] | dense:N[:K] | getrf:N[:BLOCK...] | '
-                        'potrf:N[:BLOCK...] (CUDA-event times after a warm-up call)')
+                        'potrf:N[:BLOCK...] | update:ROWS:COLS:K (CUDA-event times after a warm-up call)')
     return p.parse_args()
 
 
@@ -209,13 +209,10 @@ def gemm_peak(dtype):
     return best
 
 
-def cpu_reference(board_name, freq):
-    """The CPU restatement of the reference path (oracle), all host cores, seconds per frequency: the fill of the
-    moments, the RWG combine and the P aggregation measured in full (OpenMP C), and the reference's dense solve --
-    a complex64 LU of the loop/tree system (MixedLU) -- estimated from a timed LAPACK getrf of a bounded sample
-    scaled by the cube of the size. Returns (value, details)."""
+def cpu_front(board_name):
+    """The oracle's fill of the moments, RWG combine into L and aggregation into P on every host core:
+    (board, rwg, L, P, details)."""
     from oracle import oracle as O
-    from oracle import peec_cpu
     from pcbqs_gb300.board import Board
     b = Board.load(board_name)
     threads = O.threads()
@@ -228,34 +225,79 @@ def cpu_reference(board_name, freq):
     t2 = time.perf_counter()
     P = O.potential(mats[0], g.area, b.node_of, b.er, threads)
     t3 = time.perf_counter()
-    del mats, L, P
-    n = rwg.Ne - (len(b.terminals) + len(b.fans))      # loop/tree unknowns (within a few of the exact count)
-    lu, sample_s = peec_cpu.lu_seconds(n)
-    return (t3 - t0) + lu, dict(cores=threads, fill_s=round(t1 - t0, 3), combine_s=round(t2 - t1, 3),
-                                potential_s=round(t3 - t2, 3), lu_estimate_s=round(lu, 2),
-                                lu_sample='complex64 getrf 3072^3 in %.3f s, scaled by (n/3072)^3, n=%d' % (sample_s, n))
+    del mats
+    return b, rwg, L, P, dict(cores=threads, fill_s=round(t1 - t0, 3), combine_s=round(t2 - t1, 3),
+                              potential_s=round(t3 - t2, 3))
+
+
+def cpu_reference(board_name, freq):
+    """The CPU restatement of the reference's whole path (oracle), every host core, one frequency, in full: the fill
+    of the moments, the RWG combine and the P aggregation (OpenMP C), then the reference's dense PEEC solve
+    (oracle/peec_cpu.py: topology and projections, the scaled system, its complex64 LU with MixedLU's FP64
+    refinement, every port drive). Returns (seconds, details, port impedance matrix, unknowns)."""
+    from oracle import peec_cpu
+    t0 = time.perf_counter()
+    b, rwg, L, P, details = cpu_front(board_name)
+    solver = peec_cpu.DenseSolve(b, rwg, L, P, details)
+    del L
+    Z = solver.solve(freq, details)
+    seconds = time.perf_counter() - t0
+    n = solver.n
+    del solver
+    return seconds, details, Z, n
+
+
+def cpu_sample(board_name, n):
+    """The bounded CPU baseline beside the GPU line: the oracle's fill, combine and aggregation in full, and the
+    dense solve's complex64 LU from a timed 6144^2 LAPACK getrf scaled by (n / 6144)^3 (the factorization is most
+    of the reference's solve; `--impl reference` runs it in full). Returns (seconds per frequency, details)."""
+    from oracle import peec_cpu
+    t0 = time.perf_counter()
+    *_, details = cpu_front(board_name)
+    front = time.perf_counter() - t0
+    lu, sample_s = peec_cpu.lu_seconds(n, sample=6144, repeats=1)
+    details.update(lu_estimate_s=round(lu, 2),
+                   lu_sample='complex64 getrf 6144^2 in %.3f s, scaled by (n/6144)^3, n=%d' % (sample_s, n))
+    return front + lu, details
+
+
+def board_config(board_name, freq, unknowns=None, world=1):
+    """The workload's configuration, the same keys on both arms."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.rwg import RWG
+    from pcbqs_gb300.geometry import prepare
+    b = Board.load(board_name)
+    g = prepare(b.nodes, b.tris, b.z, 1)
+    return dict(workload=f'{board_name}: fill+solve of all {len(b.ports)} ports at {freq:g} Hz', board=board_name,
+                triangles=int(b.nt), edges=int(RWG(g.nodes, g.tris).Ne), nodes=int(b.n_nodes),
+                unknowns=None if unknowns is None else int(unknowns), parallelism=f'replicas x{world}',
+                l2='inputs larger than L2 (L 8.9 GB)' if board_name == 'planes' else 'inputs larger than L2')
 
 
 def reference_arm(args):
+    """The reference's CPU path on the host cores, run in full once (a step is minutes of CPU work: the complex64 LU
+    of the 32,990-unknown system alone is about 10^14 flops), so `steps` reports the one step timed whatever
+    --steps asked; no warm-up (nothing is cached between steps)."""
     rank, world, _ = rank_info()
     if rank != 0:
         return
-    from pcbqs_gb300.board import Board
-    values = []
-    details = None
-    for _ in range(max(1, args.steps)):
-        v, details = cpu_reference(args.board, args.freq)
-        values.append(v)
-    value = statistics.median(values)
-    line = dict(metric=METRIC, value=round(value, 4), unit='s/freq', n_gpus=args.gpus, steps=args.steps,
-                warmup=0, ms_per_step=round(value * 1e3, 2), higher_is_better=False, scaling='weak',
-                vs_baseline=None, dtype='f64', data='synthetic (seeded plane-pair board, CDT mesh)',
-                impl='reference',
-                config=dict(workload=f'{args.board}: fill+solve of all {len(Board.load(args.board).ports)} ports at '
-                                     f'{args.freq:g} Hz', board=args.board, l2='inputs larger than L2'),
+    value, details, Z, n = cpu_reference(args.board, args.freq)
+    golden = ROOT / 'tests' / 'golden' / f'peec_{args.board}.npz'
+    if golden.exists():
+        with np.load(golden) as ref:
+            hit = np.flatnonzero(np.isclose(ref['freqs'], args.freq))
+            if len(hit):
+                Zr = ref['Z'][hit[0]]
+                details['port_z_max_rel_err_vs_reference'] = float(np.abs(Z - Zr).max() / np.abs(Zr).max())
+    line = dict(metric=METRIC, value=round(value, 4), unit='s/freq', n_gpus=args.gpus, steps=1,
+                steps_requested=args.steps, warmup=0, ms_per_step=round(value * 1e3, 2), higher_is_better=False,
+                scaling='weak', vs_baseline=None, dtype='f64 (complex64 LU refined in f64)',
+                data='synthetic (seeded plane-pair board, CDT mesh)', impl='reference',
+                config=board_config(args.board, args.freq, n, 1),
                 cpu_baseline=dict(value=round(value, 4), unit='s/freq', cores=details['cores'], kind='port',
-                                  sample=f'full oracle fill+combine+aggregation; dense solve = complex64 LU '
-                                         f'estimated from a bounded sample ({details})'),
+                                  sample=f'the whole path once, in full: oracle fill+combine+aggregation (OpenMP C) '
+                                         f'and the restated dense PEEC solve ({details["lu"]} of all {n} unknowns, '
+                                         f'MixedLU refinement, {len(Z)} drives); {details}'),
                 e2e=dict(value=round(value, 4), unit='s/freq', h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line))
 
@@ -321,7 +363,8 @@ def case_lu(board, *ks):
 
 
 def case_getrf(n, *blocks):
-    """The blocked complex64 LU of a random n x n matrix with each panel width, each trailing-product math."""
+    """The blocked complex64 LU of a random n x n matrix with each panel width and each trailing update: cuBLAS
+    BF16x9 (math 1), this library's tcgen05 update with 3 and 6 BF16 part products (math 2, 3)."""
     import ctypes
     import torch
     from pcbqs_gb300 import _lib
@@ -335,7 +378,7 @@ def case_getrf(n, *blocks):
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     flops = 8 / 3 * n ** 3
     for block in (blocks or (2048,)):
-        for math in (1, 0):
+        for math in (1, 2, 3):
             for _ in range(2):
                 F.copy_(A)
                 ms, status = _event_ms(lambda: lib.pcbqs_gb300_lu_factor_c64(n, F.data_ptr(), piv.data_ptr(),
@@ -344,6 +387,36 @@ def case_getrf(n, *blocks):
                 _lib.check(status, lib)
                 print(f'getrf n={n} block {block} math {math}: {ms:.1f} ms, {flops / ms / 1e9:.1f} TFLOP/s',
                       flush=True)
+
+
+def case_update(rows, cols, k):
+    """C -= A B (complex64, rows x k times k x cols) by this library's tcgen05 update with 3 and 6 BF16 part
+    products, against cuBLAS's FP32 complex GEMM (torch complex64 matmul, TF32 off): TFLOP/s of 8 rows cols k."""
+    import ctypes
+    import torch
+    from pcbqs_gb300 import _lib
+    rows, cols, k = int(rows), int(cols), int(k)
+    lib = _lib.load()
+    g = torch.Generator(device='cuda').manual_seed(2)
+    a = torch.complex(torch.randn(k, rows, device='cuda', generator=g), torch.randn(k, rows, device='cuda', generator=g))
+    b = torch.complex(torch.randn(cols, k, device='cuda', generator=g), torch.randn(cols, k, device='cuda', generator=g))
+    c = torch.zeros(cols, rows, dtype=torch.complex64, device='cuda')
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    flops = 8.0 * rows * cols * k
+    for terms in (3, 6):
+        for _ in range(3):
+            ms, status = _event_ms(lambda: lib.pcbqs_gb300_complex_update(rows, cols, k, a.data_ptr(), rows,
+                                                                          b.data_ptr(), k, c.data_ptr(), rows, terms,
+                                                                          1 << 32, stream))
+            _lib.check(status, lib)
+            print(f'update {rows}x{cols}x{k} terms {terms}: {ms:.2f} ms, {flops / ms / 1e9:.1f} TFLOP/s', flush=True)
+    allow = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    at, bt = a.T, b.T
+    for _ in range(3):
+        ms, _ = _event_ms(lambda: torch.matmul(at, bt))
+        print(f'cuBLAS complex64 GEMM {rows}x{cols}x{k}: {ms:.2f} ms, {flops / ms / 1e9:.1f} TFLOP/s', flush=True)
+    torch.backends.cuda.matmul.allow_tf32 = allow
 
 
 def case_potrf(n, *blocks):
@@ -397,7 +470,7 @@ def case_dense(n, k=8):
                   f'{2 * n * n * 2 * k / ms / 1e9:.3f} TFLOP/s', flush=True)
 
 
-CASES = dict(fill=case_fill, lu=case_lu, getrf=case_getrf, potrf=case_potrf, dense=case_dense)
+CASES = dict(fill=case_fill, lu=case_lu, getrf=case_getrf, potrf=case_potrf, dense=case_dense, update=case_update)
 
 
 def kernel_case(spec):
@@ -485,37 +558,57 @@ def main():
     ne, nn = model.ne, model.nn
     fill_ms = statistics.median(t['fill_ms'] + t['combine_ms'] + t['potential_ms'] for t in timings)
     fill_gbs = 8 * (ne * ne + nn * nn) / (fill_ms / 1e3) / 1e9
-    # end to end through the public API from host arrays
-    t_e2e = time.perf_counter()
-    torch.cuda.synchronize()
-    m2 = PeecModel(Board.load(args.board), device=local)
-    m2.assemble(mixed=mixed)
-    r2 = m2.solve([freq], precondition=args.precondition, mixed=mixed, factor_math=args.factor_math)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t_e2e
-    h2d = m2.fill.dev.nt * (64 + 32 + 192) + sum(a.nbytes for a in m2.fill.geometry.levels[1][5:6])
-    h2d += 16 * m2.n * len(m2.names)                 # right-hand sides
-    d2h = 16 * m2.n * len(m2.names) + r2.impedance.nbytes
-    del m2
-    torch.cuda.empty_cache()
+    # end to end through the public API from host arrays: a new model from the board's host arrays each time (the
+    # median of three, each timed by the host clock around a synchronized call)
+    e2e_runs = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t_e2e = time.perf_counter()
+        m2 = PeecModel(Board.load(args.board), device=local)
+        m2.assemble(mixed=mixed)
+        r2 = m2.solve([freq], precondition=args.precondition, mixed=mixed, factor_math=args.factor_math)
+        torch.cuda.synchronize()
+        e2e_runs.append(time.perf_counter() - t_e2e)
+        h2d = m2.fill.dev.nt * (64 + 32 + 192) + sum(a.nbytes for a in m2.fill.geometry.levels[1][5:6])
+        h2d += 16 * m2.n * len(m2.names)                 # right-hand sides
+        d2h = 16 * m2.n * len(m2.names) + r2.impedance.nbytes
+        del m2, r2
+        torch.cuda.empty_cache()
+    e2e_s = statistics.median(e2e_runs)
     if rank != 0:
         return
     import torch as _torch
     peaks = dict(fp64=gemm_peak(_torch.float64), fp32=gemm_peak(_torch.float32))
     head_fill_ms = statistics.median(t['fill_ms'] for t in timings)
+    # the port impedances against the reference's own dense solve of this board (tests/golden/peec_<board>.npz)
+    z_err_ref = None
+    golden = ROOT / 'tests' / 'golden' / f'peec_{args.board}.npz'
+    if golden.exists():
+        with np.load(golden) as ref:
+            hit = np.flatnonzero(np.isclose(ref['freqs'], freq))
+            if len(hit):
+                Zr = ref['Z'][hit[0]]
+                z_err_ref = dict(headline=float(np.abs(Z_headline - Zr).max() / np.abs(Zr).max()))
+                if comparator:
+                    z_err_ref['fp64_comparator'] = float(np.abs(Z64 - Zr).max() / np.abs(Zr).max())
+    # pair integrals per second: the fill's unordered triangle pairs (far and near, each kind counted) over its time
+    nt = model.fill.nt
+    fr = fill_roofline(model, head_fill_ms, mixed, peaks)
+    pair_rate = dict(value=round(nt * (nt + 1) / 2 / (head_fill_ms / 1e3), 1), unit='pairs/s',
+                     far=fr['far_pairs'], near_level0=fr['near_pairs'][0], near_level1=fr['near_pairs'][1],
+                     fill_ms=round(head_fill_ms, 2))
     if comparator:
         comparator['fill_roofline'] = fill_roofline(model, fp64_timings['fill_ms'], False, peaks)
     line = dict(metric=METRIC, value=round(value, 4), unit='s/freq', n_gpus=world, steps=args.steps,
                 warmup=args.warmup, ms_per_step=round(ms, 2), higher_is_better=False, scaling='weak',
                 vs_baseline=None, dtype='f32+f64' if mixed else 'f64', data='synthetic (seeded plane-pair board, CDT mesh)',
-                config=dict(workload=f'{args.board}: fill+solve of all {len(model.names)} ports at {args.freq:g} Hz',
-                            board=args.board, triangles=model.fill.nt, edges=ne, nodes=nn, unknowns=model.n,
-                            precondition=args.precondition, factor_math=args.factor_math, mode=args.mode,
-                            gmres_tol=model.tol,
-                            gmres_iterations=result.iterations.tolist(),
-                            gmres_outer_steps=timings[-1].get('outer_steps'), parallelism=f'replicas x{world}',
-                            l2='inputs larger than L2 (L 8.9 GB)'),
+                config=board_config(args.board, args.freq, model.n, world),
+                solver=dict(precondition=args.precondition, factor_math=args.factor_math, mode=args.mode,
+                            gmres_tol=model.tol, gmres_iterations=result.iterations.tolist(),
+                            gmres_outer_steps=timings[-1].get('outer_steps')),
+                port_z_max_rel_err_vs_reference=z_err_ref,
                 fill_gbs=round(fill_gbs, 2),
+                pair_integrals_per_s=pair_rate,
                 fp64_comparator=comparator,
                 breakdown_ms={k: round(statistics.median(t.get(k, 0) for t in timings), 2)
                               for k in ('fill_ms', 'combine_ms', 'potential_ms', 'precondition_ms', 'gmres_ms')},
@@ -526,7 +619,8 @@ def main():
                 roofline=(factor_roofline(model, statistics.median(t['factor_lu_ms'] for t in timings))
                           if args.precondition == 'lu32' else fill_roofline(model, head_fill_ms, mixed, peaks)),
                 fill_roofline=fill_roofline(model, head_fill_ms, mixed, peaks),
-                e2e=dict(value=round(e2e_s, 4), unit='s/freq', h2d_bytes_per_step=int(h2d),
+                e2e=dict(value=round(e2e_s, 4), unit='s/freq', runs_s=[round(v, 4) for v in e2e_runs],
+                         h2d_bytes_per_step=int(h2d),
                          d2h_bytes_per_step=int(d2h)))
     if args.sweep:
         # the batched sweep: every (frequency, port) column, `anchors` shared factors, one batched GMRES per run
@@ -549,10 +643,11 @@ def main():
                              iterations_per_frequency_max=its.max(axis=1).tolist(),
                              max_residual=float(rs.residual.max()))
     if not args.no_cpu_baseline:
-        v, details = cpu_reference(args.board, args.freq)
+        v, details = cpu_sample(args.board, model.n)
         line['cpu_baseline'] = dict(value=round(v, 3), unit='s/freq', cores=details['cores'], kind='port',
                                     sample=f'oracle fill+combine+aggregation in full; dense solve = complex64 LU '
-                                           f'estimated from a bounded sample; {details}')
+                                           f'estimated from a bounded sample (--impl reference runs it in full); '
+                                           f'{details}')
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

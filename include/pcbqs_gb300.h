@@ -264,11 +264,29 @@ int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *op, double *assemble_m
 /* Dense complex64 LU with partial pivoting of the n x n column-major device matrix a (leading dimension n), in
  * place, ipiv (device, n) receiving 1-based pivot rows: cusolverDnCgetrf's layout and pivots, so getrs and this
  * library's triangular solvers apply to it. Blocked: `block`-column panels (32 .. 4096) factored on a second stream
- * one step ahead of the trailing GEMMs; math 0: FP32 GEMMs, 1: FP32 GEMMs emulated with BF16x9 on the tensor cores.
+ * one step ahead of the trailing GEMMs; math 0: FP32 GEMMs (cuBLAS), 1: FP32 GEMMs emulated with BF16x9 on the
+ * tensor cores (cuBLAS), 2 / 3: this library's tcgen05 update (pcbqs_gb300_complex_update) with 3 / 6 BF16 part
+ * products, the subtraction fused into its epilogue. Returns status 6 if a bounded wait of that update gave up.
  * *singular (host) = 1-based index of the first exactly zero pivot, 0 if none. Synchronizes `stream`. The factor
  * step of MixedLU and lu_factor_rows (src/pcbqs/kernels.py:125-160, :266-285), which LAPACK's cgetrf does there. */
 int pcbqs_gb300_lu_factor_c64(int64_t n, void *a, int32_t *ipiv, int block, int math, int32_t *singular,
                               void *stream);
+/* Limit, in SM clocks, of the library's bounded device waits (a kernel waiting for its own copies, for other blocks
+ * of a cooperative grid, or for its tensor-core products): a wait that runs out makes the call return
+ * status 6 with the device context still usable. 0 restores the default (2^31, about a second).
+ * Process-wide; read when a call launches its kernels. No counterpart in the reference (its CPU code has no device
+ * waits); it lets a test make the waits run out without a fault. */
+int pcbqs_gb300_set_wait_cycles(uint64_t cycles);
+/* c -= a b for complex64 column-major device matrices (rows x k, k x cols, rows x cols; leading dimensions lda >= rows,
+ * ldb >= k, ldc >= rows) on the tensor cores: this library's tcgen05 GEMM on BF16 parts of the FP32 values (terms 3:
+ * h.h + h.m + m.h, about 2^-16 relative error per product; terms 6: also h.l + m.m + l.h, FP32's accuracy) with
+ * FP32 accumulation, as one real GEMM of inner dimension terms * 2k. The trailing update of the blocked LU
+ * (pcbqs_gb300_lu_factor_c64 math 2 and 3), exported so it can be checked on its own; the reference's counterpart is
+ * LAPACK's cgemm inside cgetrf (MixedLU, src/pcbqs/kernels.py:150-151). Every wait inside the kernel gives up after
+ * wait_cycles SM clocks (status 6). Takes its scratch from the library's memory pool; synchronizes
+ * `stream`. */
+int pcbqs_gb300_complex_update(int64_t rows, int64_t cols, int k, const void *a, int64_t lda, const void *b,
+                               int64_t ldb, void *c, int64_t ldc, int terms, uint64_t wait_cycles, void *stream);
 /* Dense FP32 Cholesky a = L L^T of the n x n column-major symmetric positive definite device matrix a (leading
  * dimension lda >= n, a multiple of 32 for the tensor-core GEMM forms; lower triangle read and overwritten by L;
  * the strict upper triangle is left with intermediate values), blocked like pcbqs_gb300_lu_factor_c64 (block 32 .. 4096, math 0: FP32 GEMMs, 1: BF16x9). *info

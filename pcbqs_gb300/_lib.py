@@ -14,6 +14,7 @@ LIBRARY = Path(__file__).resolve().parent / 'libpcbqs_gb300.so'
 
 STATUS = {0: 'ok', 1: 'invalid argument', 2: 'CUDA error', 3: 'non-finite result', 4: 'device allocation failed',
           5: 'no convergence', 6: 'bounded device wait gave up'}
+OK, ERR_ARGUMENT, ERR_CUDA, ERR_NONFINITE, ERR_MEMORY, ERR_CONVERGENCE, ERR_TIMEOUT = range(7)
 
 c_double_p = ctypes.POINTER(ctypes.c_double)
 c_int32_p = ctypes.POINTER(ctypes.c_int32)
@@ -135,6 +136,10 @@ PROTOTYPES = {
                                                  c_int32_p, c_double_p, c_void_p]),
     'pcbqs_gb300_lu_factor_c64': (ctypes.c_int, [ctypes.c_int64, c_void_p, c_void_p, ctypes.c_int, ctypes.c_int,
                                                  c_int32_p, c_void_p]),
+    'pcbqs_gb300_set_wait_cycles': (ctypes.c_int, [ctypes.c_uint64]),
+    'pcbqs_gb300_complex_update': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int, c_void_p,
+                                                  ctypes.c_int64, c_void_p, ctypes.c_int64, c_void_p, ctypes.c_int64,
+                                                  ctypes.c_int, ctypes.c_uint64, c_void_p]),
     'pcbqs_gb300_cholesky_f32': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                                 c_int32_p, c_void_p]),
     'pcbqs_gb300_dense_apply': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64, c_void_p,

@@ -21,9 +21,20 @@ using namespace pq;
 namespace {
 thread_local std::string g_error;
 std::atomic<long long> g_launches{0};
+std::atomic<unsigned long long> g_wait_cycles{0};
 }  // namespace
 
 void pq::note_launches(long long count) { g_launches.fetch_add(count, std::memory_order_relaxed); }
+
+unsigned long long pq::wait_cycles() {
+    const unsigned long long w = g_wait_cycles.load(std::memory_order_relaxed);
+    return w ? w : DEFAULT_WAIT_CYCLES;
+}
+
+extern "C" int pcbqs_gb300_set_wait_cycles(uint64_t cycles) {
+    g_wait_cycles.store(cycles, std::memory_order_relaxed);
+    return OK;
+}
 
 // The calling thread's last error message, shared by every entry point of the library.
 int pq::fail(int code, const char *fmt, ...) {
@@ -331,7 +342,7 @@ static int fill_device(pcbqs_gb300_ctx *c, double near, int outer, int scalar_on
     if (ld < nt) return fail(ERR_ARGUMENT, "fill: leading dimension %lld below %d", (long long)ld, nt);
     if (!planes || !planes[0] || (!scalar_only && (!planes[1] || !planes[2] || !planes[3])))
         return fail(ERR_ARGUMENT, "fill: missing output plane");
-    FillRule rule{near, (near < 0 || std::isinf(near)) ? 1 : 0, outer};
+    FillRule rule{near, (near < 0 || std::isinf(near)) ? 1 : 0, outer, wait_cycles()};
     if (rule.all_near) rule.near = 0;
     Planes<T> fp{planes[0], scalar_only ? nullptr : planes[1], scalar_only ? nullptr : planes[2],
                  scalar_only ? nullptr : planes[3], ld, scalar_only};

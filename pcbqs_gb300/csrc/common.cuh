@@ -23,6 +23,14 @@ int fail(int code, const char *fmt, ...);
 // Count kernels launched by this library (reported by pcbqs_gb300_kernel_launches()).
 void note_launches(long long count);
 
+// Limit, in SM clocks, of the library's bounded device waits on the progress of other threads, blocks or copies
+// (pcbqs_gb300_set_wait_cycles; DEFAULT_WAIT_CYCLES, about a second at 2 GHz, unless set).
+constexpr unsigned long long DEFAULT_WAIT_CYCLES = 1ull << 31;
+unsigned long long wait_cycles();
+// Limit of the waits for a block's own asynchronous copies or products before it exits after giving up (these
+// complete by themselves; about four seconds).
+constexpr unsigned long long DRAIN_WAIT_CYCLES = 1ull << 33;
+
 // Per-triangle records in HBM. One record per triangle, 16-byte aligned so a tile of consecutive triangles is
 // one contiguous run that a bulk (TMA) copy can stage into shared memory.
 //   FarRec   64 B: the three-point rule's points (x0,y0,x1,y1,x2,y2), area, z

@@ -25,6 +25,7 @@
 #include "common.cuh"
 #include "factor.cuh"
 #include "pool.cuh"
+#include "tcgemm.cuh"
 
 namespace pq {
 
@@ -157,6 +158,7 @@ struct Resources {
     cudaStream_t panel = nullptr;
     cudaEvent_t ready = nullptr, next = nullptr;
     float2 *work = nullptr, *product = nullptr;
+    uint8_t *planes = nullptr;
     int *plan = nullptr, *info = nullptr;
     cudaStream_t main = nullptr;
     ~Resources() {
@@ -164,6 +166,7 @@ struct Resources {
         if (panel) cudaStreamSynchronize(panel);
         pool_free(work, main);
         pool_free(product, main);
+        pool_free(planes, main);
         pool_free(plan, main);
         pool_free(info, main);
         if (blas) cublasDestroy(blas);
@@ -179,8 +182,10 @@ struct Resources {
 cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular) {
     *singular = 0;
     if (n <= 0 || n > (int64_t)0x7fffffff || !A || !ipiv || block < 32 || block > MAX_BLOCK ||
-        (math != LU_GEMM_FP32 && math != LU_GEMM_BF16X9))
+        (math != LU_GEMM_FP32 && math != LU_GEMM_BF16X9 && math != LU_GEMM_TC3 && math != LU_GEMM_TC6))
         return cudaErrorInvalidValue;
+    const bool tc = math == LU_GEMM_TC3 || math == LU_GEMM_TC6;
+    const int terms = math == LU_GEMM_TC3 ? 3 : 6;
     const int nb = (int)std::min<int64_t>(block, n);
     const int64_t steps = (n + nb - 1) / nb;
     Resources r;
@@ -194,7 +199,7 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
     cublasSetStream(r.blas, stream);
     cusolverDnSetStream(r.solver, r.panel);
     cublasComputeType_t compute = CUBLAS_COMPUTE_32F;
-    if (math == LU_GEMM_BF16X9) {
+    if (math != LU_GEMM_FP32) {       // (the tcgen05 forms keep the emulated FP32 in the panels' own GEMMs)
         if (cublasSetEmulationStrategy(r.blas, CUBLAS_EMULATION_STRATEGY_EAGER) != CUBLAS_STATUS_SUCCESS ||
             cublasSetEmulationSpecialValuesSupport(r.blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE) !=
                 CUBLAS_STATUS_SUCCESS ||
@@ -210,18 +215,20 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
     if (cusolverDnCgetrf_bufferSize(r.solver, (int)n, nb, reinterpret_cast<cuComplex *>(A), (int)n, &lwork) !=
         CUSOLVER_STATUS_SUCCESS)
         return cudaErrorUnknown;
-    // plan: dst (PLAN), src (PLAN), count, error
-    // the trailing products go to a scratch matrix (beta = 0) and are subtracted by k_trailing_subtract; the
-    // largest is (n - nb) x (n - nb)
+    // plan: dst (PLAN), src (PLAN), count, error, the tcgen05 update's timeout flag
+    // cuBLAS: the trailing products go to a scratch matrix (beta = 0) and are subtracted by k_trailing_subtract; the
+    // largest is (n - nb) x (n - nb). tcgen05: the BF16 planes of the largest update ((n - nb) rows and columns).
     const int64_t trail = n - nb;
     if ((e = pool_alloc_n(&r.work, (size_t)std::max(lwork, 1), stream)) ||
-        (e = pool_alloc_n(&r.plan, (size_t)2 * PLAN + 2, stream)) ||
-        (e = pool_alloc_n(&r.info, (size_t)steps, stream)) ||
-        (trail > 0 && (e = pool_alloc_n(&r.product, (size_t)trail * trail, stream))))
+        (e = pool_alloc_n(&r.plan, (size_t)2 * PLAN + 3, stream)) ||
+        (e = pool_alloc_n(&r.info, (size_t)steps, stream)))
         return e;
-    int *dst = r.plan, *src = r.plan + PLAN, *count = r.plan + 2 * PLAN, *error = count + 1;
-    if ((e = cudaMemsetAsync(error, 0, sizeof(int), stream)) || (e = cudaMemsetAsync(r.info, 0, sizeof(int) * steps,
-                                                                                     stream)))
+    if (trail > 0 && !tc && (e = pool_alloc_n(&r.product, (size_t)trail * trail, stream))) return e;
+    if (trail > 0 && tc && (e = pool_alloc_n(&r.planes, tc_update_scratch_bytes(trail, trail, nb, terms), stream)))
+        return e;
+    int *dst = r.plan, *src = r.plan + PLAN, *count = r.plan + 2 * PLAN, *error = count + 1, *tc_error = count + 2;
+    if ((e = cudaMemsetAsync(error, 0, 2 * sizeof(int), stream)) ||
+        (e = cudaMemsetAsync(r.info, 0, sizeof(int) * steps, stream)))
         return e;
     auto at = [&](int64_t row, int64_t col) { return A + row + col * n; };
     const cuComplex one = {1.f, 0.f};
@@ -237,8 +244,13 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
         return cudaEventRecord(r.ready, r.panel);
     };
     const cuComplex zero = {0.f, 0.f};
-    auto gemm = [&](int64_t rows, int64_t cols, int k, const float2 *a, const float2 *b, float2 *c) -> bool {
+    // a_packed: the panel's planes were packed by this step's first update
+    auto gemm = [&](int64_t rows, int64_t cols, int k, const float2 *a, const float2 *b, float2 *c,
+                    bool a_packed) -> bool {
         if (rows <= 0 || cols <= 0) return true;
+        if (tc)
+            return tc_update_c64(rows, cols, k, a, n, b, n, c, n, terms, r.planes, a_packed, tc_error,
+                                 wait_cycles(), stream) == cudaSuccess;
         if (rows > trail || cols > trail) return false;
         if (cublasGemmEx(r.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)rows, (int)cols, k, &one, a, CUDA_C_32F, (int)n, b,
                          CUDA_C_32F, (int)n, &zero, r.product, CUDA_C_32F, (int)rows, compute, CUBLAS_GEMM_DEFAULT) !=
@@ -273,23 +285,24 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
         }
         if (rest <= 0) break;
         // next panel's columns first, so that its factorization overlaps the rest of the update
-        if (!trsm(j, jb, right, jb2) || !gemm(rest, jb2, jb, at(right, j), at(j, right), at(right, right)))
+        if (!trsm(j, jb, right, jb2) || !gemm(rest, jb2, jb, at(right, j), at(j, right), at(right, right), false))
             return cudaErrorUnknown;
         if ((e = cudaEventRecord(r.next, stream)) || (e = cudaStreamWaitEvent(r.panel, r.next, 0)) ||
             (e = factor_panel(right, jb2, t + 1)))
             return e;
         if (!trsm(j, jb, right + jb2, rest - jb2) ||
-            !gemm(rest, rest - jb2, jb, at(right, j), at(j, right + jb2), at(right, right + jb2)))
+            !gemm(rest, rest - jb2, jb, at(right, j), at(j, right + jb2), at(right, right + jb2), jb2 > 0))
             return cudaErrorUnknown;
     }
     if ((e = cudaGetLastError()) || (e = cudaStreamSynchronize(r.panel)) || (e = cudaStreamSynchronize(stream)))
         return e;
     std::vector<int> info((size_t)steps);
-    int bad = 0;
+    int flags[2] = {0, 0};
     if ((e = cudaMemcpy(info.data(), r.info, sizeof(int) * steps, cudaMemcpyDeviceToHost)) ||
-        (e = cudaMemcpy(&bad, error, sizeof(int), cudaMemcpyDeviceToHost)))
+        (e = cudaMemcpy(flags, error, 2 * sizeof(int), cudaMemcpyDeviceToHost)))
         return e;
-    if (bad) return cudaErrorIllegalState;
+    if (flags[1]) return cudaErrorLaunchTimeout;
+    if (flags[0]) return cudaErrorIllegalState;
     for (int64_t t = 0; t < steps; ++t)
         if (info[t] > 0) {
             *singular = (int)(t * nb + info[t]);
@@ -432,13 +445,46 @@ extern "C" int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int64_t lda, int bl
 
 extern "C" int pcbqs_gb300_lu_factor_c64(int64_t n, void *a, int32_t *ipiv, int block, int math, int32_t *singular,
                                          void *stream) {
-    if (n <= 0 || !a || !ipiv || !singular || block < 32 || block > pq::MAX_BLOCK_PUBLIC || (math != 0 && math != 1))
-        return pq::fail(pq::ERR_ARGUMENT, "lu_factor_c64: invalid argument (block 32..%d, math 0 or 1)",
+    if (n <= 0 || !a || !ipiv || !singular || block < 32 || block > pq::MAX_BLOCK_PUBLIC || math < 0 || math > 3)
+        return pq::fail(pq::ERR_ARGUMENT, "lu_factor_c64: invalid argument (block 32..%d, math 0..3)",
                         pq::MAX_BLOCK_PUBLIC);
     int zero = 0;
     const cudaError_t e = pq::getrf_blocked(n, static_cast<float2 *>(a), ipiv, block, math,
                                             static_cast<cudaStream_t>(stream), &zero);
     *singular = zero;
+    if (e == cudaErrorLaunchTimeout)
+        return pq::fail(pq::ERR_TIMEOUT, "lu_factor_c64: a bounded wait of the tensor-core update gave up");
     if (e) return pq::fail(pq::ERR_CUDA, "lu_factor_c64: %s", cudaGetErrorString(e));
+    return pq::OK;
+}
+
+extern "C" int pcbqs_gb300_complex_update(int64_t rows, int64_t cols, int k, const void *a, int64_t lda,
+                                          const void *b, int64_t ldb, void *c, int64_t ldc, int terms,
+                                          uint64_t wait_cycles, void *stream) {
+    if (rows < 0 || cols < 0 || k < 0 || !a || !b || !c || lda < rows || ldb < k || ldc < rows ||
+        (terms != 3 && terms != 6) || wait_cycles == 0)
+        return pq::fail(pq::ERR_ARGUMENT, "complex_update: invalid argument (terms 3 or 6, lda >= rows, ldb >= k, "
+                                          "ldc >= rows, wait_cycles > 0)");
+    if (rows == 0 || cols == 0 || k == 0) return pq::OK;
+    auto st = static_cast<cudaStream_t>(stream);
+    uint8_t *scratch = nullptr;
+    int *flag = nullptr;
+    cudaError_t e;
+    if ((e = pq::pool_alloc_n(&scratch, pq::tc_update_scratch_bytes(rows, cols, k, terms), st)) ||
+        (e = pq::pool_alloc_n(&flag, 1, st))) {
+        pq::pool_free(scratch, st);
+        return pq::fail(pq::ERR_MEMORY, "complex_update: scratch: %s", cudaGetErrorString(e));
+    }
+    int timed_out = 0;
+    if (!(e = cudaMemsetAsync(flag, 0, sizeof(int), st)))
+        e = pq::tc_update_c64(rows, cols, k, static_cast<const float2 *>(a), lda, static_cast<const float2 *>(b), ldb,
+                              static_cast<float2 *>(c), ldc, terms, scratch, false, flag,
+                              (unsigned long long)wait_cycles, st);
+    if (!e) e = cudaMemcpyAsync(&timed_out, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    pq::pool_free(scratch, st);
+    pq::pool_free(flag, st);
+    if (e) return pq::fail(pq::ERR_CUDA, "complex_update: %s", cudaGetErrorString(e));
+    if (timed_out) return pq::fail(pq::ERR_TIMEOUT, "complex_update: a bounded wait of the tensor-core GEMM gave up");
     return pq::OK;
 }

@@ -11,6 +11,8 @@ namespace pq {
 enum LuMath : int {
     LU_GEMM_FP32 = 0,      // FP32 GEMMs on the CUDA cores
     LU_GEMM_BF16X9 = 1,    // FP32 GEMMs emulated on the tensor cores with three BF16 terms per operand
+    LU_GEMM_TC3 = 2,       // this library's tcgen05 GEMM, three BF16 part products (about 16 correct bits)
+    LU_GEMM_TC6 = 3,       // this library's tcgen05 GEMM, six BF16 part products (FP32's accuracy)
 };
 
 constexpr int MAX_BLOCK_PUBLIC = 4096;   // widest panel the blocked factorizations take
@@ -20,9 +22,11 @@ constexpr int MAX_BLOCK_PUBLIC = 4096;   // widest panel the blocked factorizati
 // triangular solvers of that factor apply unchanged). Right-looking in `block`-column panels: each panel is
 // factored by cuSOLVER on a second stream while the main stream finishes the previous step's trailing update
 // (one step of lookahead), its row swaps are applied to the other columns by a gather kernel, the block row of U
-// comes from a triangular solve and the trailing update from one large GEMM (`math`) into a scratch matrix and a
-// subtract pass. Returns cudaSuccess, or an error; *singular = the first zero pivot's 1-based index (0 if none).
-// Ordered on `stream`; returns after the factor is complete.
+// comes from a triangular solve and the trailing update from one large GEMM (`math`): cuBLAS into a scratch matrix
+// and a subtract pass (LU_GEMM_FP32, LU_GEMM_BF16X9), or this library's tcgen05 update C -= A B with the subtraction
+// fused (LU_GEMM_TC3, LU_GEMM_TC6: tc_update_c64, the panel's BF16 planes packed once per step). Returns
+// cudaSuccess, or an error (cudaErrorLaunchTimeout: a bounded wait of the tcgen05 update gave up); *singular = the
+// first zero pivot's 1-based index (0 if none). Ordered on `stream`; returns after the factor is complete.
 cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular);
 
 // Factors the n x n column-major symmetric positive definite FP32 matrix A (leading dimension lda >= n, best a

@@ -141,12 +141,18 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill_tiles(Geometry g, Planes<
             bulk_load(s.cls_r, g.cls + p0, np * sizeof(ClsRec), &s.bar);
             bulk_load(s.cls_c, g.cls + q0, nqn * sizeof(ClsRec), &s.bar);
         }
-        if (!mbar_wait_bounded(&s.bar, phase)) failed = true;
-        phase ^= 1;
+        if (!mbar_wait_bounded(&s.bar, phase, rule.wait)) failed = true;
         if (__syncthreads_or(failed)) {
-            if (threadIdx.x == 0) atomicExch(status, (int)ERR_TIMEOUT);
+            // the tile's copies may still be landing in this block's shared memory: wait for them (they complete
+            // by themselves) before the block leaves, so no copy outlives it
+            if (threadIdx.x == 0) {
+                atomicExch(status, (int)ERR_TIMEOUT);
+                mbar_wait_bounded(&s.bar, phase, DRAIN_WAIT_CYCLES);
+            }
+            __syncthreads();
             break;
         }
+        phase ^= 1;
         if (LOCAL) {
             if (threadIdx.x < np) s.rad_r[threadIdx.x] = (float)s.cls_r[threadIdx.x].radius;
             if (threadIdx.x >= 32 && threadIdx.x < 32 + nqn) s.rad_c[threadIdx.x - 32] = (float)s.cls_c[threadIdx.x - 32].radius;

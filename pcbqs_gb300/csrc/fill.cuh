@@ -17,6 +17,7 @@ struct FillRule {
     double near;     // analytic when distance <= near * (r_p + r_q)
     int all_near;    // near = infinity: every pair analytic
     int outer;       // refinement level of pairs within the radii sum (0, 1 or 2)
+    unsigned long long wait;   // limit (SM clocks) of the waits for a tile's geometry copies
 };
 
 // Compacted near pairs, one list per level slot (0: level 0, 1: level `outer`), and their counts.

@@ -930,7 +930,7 @@ struct pcbqs_gb300_peec {
 
 namespace {
 #define pfail pq::fail
-constexpr int LU_BLOCK = 2048;     // panel width of the blocked factorization (math 2 and 3)
+constexpr int LU_BLOCK = 2048;     // panel width of the blocked factorization (math 2 .. 5)
 Csr csr_of(const pcbqs_gb300_csr &c) {
     Csr out;
     out.rows = c.rows;
@@ -1058,8 +1058,9 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
 
 int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream) {
     if (!h || !krk || sys < 0 || sys >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_factor: invalid argument");
-    if (math < 0 || math > 3)
-        return pfail(ERR_ARGUMENT, "peec_factor: math 0/1 (cuSOLVER getrf, FP32/BF16x9) or 2/3 (blocked, BF16x9/FP32)");
+    if (math < 0 || math > 5)
+        return pfail(ERR_ARGUMENT, "peec_factor: math 0/1 (cuSOLVER getrf, FP32/BF16x9) or 2..5 (blocked: BF16x9, "
+                                   "FP32, tcgen05 with 3 or 6 BF16 part products)");
     PeecOp &op = h->op;
     const int64_t n = op.n_;
     if (krk->rows != n || krk->cols != n) return pfail(ERR_ARGUMENT, "peec_factor: K^T R K must be n x n");
@@ -1143,12 +1144,13 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     cusolverDnSetStream(lu->solver, st);
     if (math >= 2) {
         int singular = 0;
-        e = getrf_blocked(n, lu->lu, lu->ipiv, LU_BLOCK, math == 2 ? LU_GEMM_BF16X9 : LU_GEMM_FP32, st, &singular);
+        const int gemm = math == 2 ? LU_GEMM_BF16X9 : math == 3 ? LU_GEMM_FP32 : math == 4 ? LU_GEMM_TC3 : LU_GEMM_TC6;
+        e = getrf_blocked(n, lu->lu, lu->ipiv, LU_BLOCK, gemm, st, &singular);
         cudaEventRecord(t.ev[2], st);
         if (e || singular) {
             delete lu;
-            return pfail(singular ? ERR_NONFINITE : ERR_CUDA, "peec_factor: blocked getrf failed (zero pivot %d, %s)",
-                         singular, cudaGetErrorString(e));
+            return pfail(singular ? ERR_NONFINITE : e == cudaErrorLaunchTimeout ? ERR_TIMEOUT : ERR_CUDA,
+                         "peec_factor: blocked getrf failed (zero pivot %d, %s)", singular, cudaGetErrorString(e));
         }
         if ((e = lu->tri.prepare(lu->lu, n, lu->ipiv, st))) {
             delete lu;

@@ -1,0 +1,420 @@
+// C -= A B for complex64 matrices on the tcgen05 tensor cores (declared in tcgemm.cuh).
+//
+// The complex product is one real GEMM. With A = Ar + i Ai (rows x k) and B = Br + i Bi (k x cols):
+//   Re C -= [Ar | Ai] [Br; -Bi],   Im C -= [Ar | Ai] [Bi; Br].
+// Each FP32 value is split into BF16 parts x = h + m + l (h = bf16(x), m = bf16(x - h), l = bf16(x - h - m)), and
+// the part products kept (3: hh, hm, mh; 6: also hl, mm, lh) are laid side by side along the inner dimension:
+// A's plane holds, for every row, the segments [a_p(s) of Ar | Ai] and B's plane, for every output column (real
+// and imaginary columns interleaved: plane row 2j is Re of column j, 2j + 1 its Im), the matching [b_q(s)]. One
+// BF16 GEMM with FP32 accumulation of inner dimension K = terms · 2k then yields the FP32-accurate product
+// (terms = 6) or one with about 16 correct bits (terms = 3).
+//
+// The GEMM: one CTA per 128 x 256 tile of the real product (128 rows of C by 128 of its complex columns), four
+// warps. Warp 0's elected thread streams 64-wide K slices of both planes into a 4-stage shared-memory ring by TMA
+// (128-byte swizzle, one mbarrier per stage carrying the transaction bytes); warp 1's elected thread issues the
+// tcgen05.mma (kind::f16, BF16 inputs, M 128, N 256, K 16: four per slice) with the accumulator in tensor memory
+// (256 columns) and frees each stage through tcgen05.commit; after the last slice all four warps read their 32
+// tensor-memory lanes (tcgen05.ld 32x32b) and subtract the tile from C, a warp's 32 rows of one column being 256
+// contiguous bytes. One tile per CTA (not persistent) so that the LU's high-priority panel factorizations get SMs as
+// tiles retire. Every wait is bounded in SM clocks; on timeout the CTA records ERR_TIMEOUT, waits (bounded) for its
+// own copies and products in flight, frees its tensor memory and exits.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "common.cuh"
+#include "tcgemm.cuh"
+#include "tma.cuh"
+
+namespace pq {
+
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4, THREADS = 128;
+constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int TMEM_COLS = 256;
+constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;   // ring, 1024-byte alignment slack, barriers
+constexpr int KPAD = 32;                                             // k padded to a multiple of 32 (K % 64 == 0)
+// limit of the waits for this CTA's own copies and products in flight before it exits (these complete on their
+// own; the caller's limit only bounds the waits on the pipeline's progress)
+constexpr unsigned long long DRAIN_CYCLES = DRAIN_WAIT_CYCLES;
+
+// part indices of A and B in each product segment
+__constant__ int8_t SEG_A[6] = {0, 0, 1, 0, 1, 2};
+__constant__ int8_t SEG_B[6] = {0, 1, 0, 2, 1, 0};
+
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
+    h = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(h);
+    m = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(m);
+    l = __float2bfloat16_rn(r2);
+}
+
+__device__ __forceinline__ __nv_bfloat16 pick(int p, __nv_bfloat16 h, __nv_bfloat16 m, __nv_bfloat16 l) {
+    return p == 0 ? h : (p == 1 ? m : l);
+}
+
+// A's plane: row r, segment s, position 2t + c = part SEG_A[s] of component c (re, im) of A[r, t]; zero for t >= k.
+// 32 rows x 32 k per block, transposed through shared memory so both the column-major reads and the row writes
+// are contiguous.
+__global__ void __launch_bounds__(256) k_pack_a(int64_t rows, int k, int kp, int terms, const float2 *A, int64_t lda,
+                                                __nv_bfloat162 *out) {
+    __shared__ float2 tile[32][33];
+    const int64_t r0 = (int64_t)blockIdx.x * 32;
+    const int t0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int j = ty; j < 32; j += 8) {
+        const int64_t r = r0 + tx;
+        const int t = t0 + j;
+        tile[j][tx] = (r < rows && t < k) ? A[r + (int64_t)t * lda] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int64_t K2 = (int64_t)kp;          // bf16 pairs per segment (kp complex values)
+    for (int j = ty; j < 32; j += 8) {
+        const int64_t r = r0 + j;
+        if (r >= rows) continue;
+        const int t = t0 + tx;
+        const float2 v = tile[tx][j];
+        __nv_bfloat16 rh, rm, rl, ih, im, il;
+        split3(v.x, rh, rm, rl);
+        split3(v.y, ih, im, il);
+        __nv_bfloat162 *row = out + r * (K2 * terms);
+        for (int s = 0; s < terms; ++s) {
+            const int p = SEG_A[s];
+            row[s * K2 + t] = __halves2bfloat162(pick(p, rh, rm, rl), pick(p, ih, im, il));
+        }
+    }
+}
+
+// B's plane: row 2j (Re of column j) holds (Br, -Bi) at positions (2t, 2t + 1), row 2j + 1 (Im) holds (Bi, Br),
+// each value's part SEG_B[s] in segment s. B's columns are contiguous in t, as are the plane's rows.
+__global__ void __launch_bounds__(256) k_pack_b(int64_t cols, int k, int kp, int terms, const float2 *B, int64_t ldb,
+                                                __nv_bfloat162 *out) {
+    const int64_t K2 = (int64_t)kp;
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y) {
+        const float2 *col = B + j * ldb;
+        __nv_bfloat162 *re = out + (2 * j) * (K2 * terms), *imr = re + K2 * terms;
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < kp; t += gridDim.x * blockDim.x) {
+            const float2 v = t < k ? col[t] : make_float2(0.f, 0.f);
+            __nv_bfloat16 rh, rm, rl, ih, im, il;
+            split3(v.x, rh, rm, rl);
+            split3(v.y, ih, im, il);
+            for (int s = 0; s < terms; ++s) {
+                const int q = SEG_B[s];
+                const __nv_bfloat16 br = pick(q, rh, rm, rl), bi = pick(q, ih, im, il);
+                re[s * K2 + t] = __halves2bfloat162(br, __hneg(bi));
+                imr[s * K2 + t] = __halves2bfloat162(bi, br);
+            }
+        }
+    }
+}
+
+// ---- tcgen05 / TMA primitives (inline PTX, sm_100 family) ----
+
+// Shared-memory matrix descriptor of a K-major operand tile in the 128-byte swizzle layout that TMA writes with
+// CU_TENSOR_MAP_SWIZZLE_128B: rows of 128 bytes, 8-row groups 1024 bytes apart (stride byte offset), the leading
+// byte offset unused for this layout, descriptor version 1, layout type 2 (128-byte swizzle). The tile base is
+// 1024-byte aligned; a K step of 16 elements inside the 128-byte row adds 32 bytes to the start address.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1), both
+// K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch(const CUtensorMap *map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive on `bar` once every tcgen05.mma issued so far by this thread has completed.
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Wait for phase parity `parity` of `bar`, giving up after `limit` SM clocks or, when `abort` is given, as soon as
+// another thread of the CTA has given up (*abort set). Returns false on giving up.
+__device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t parity, unsigned long long limit,
+                                             volatile int *abort) {
+    const long long t0 = clock64();
+    const bool probe = limit < PROBE_BELOW_CYCLES;
+    for (uint32_t i = 0;; ++i) {
+        if (probe ? mbar_test_wait(bar, parity) : mbar_try_wait(bar, parity)) return true;
+        if ((unsigned long long)(clock64() - t0) > limit || ((i & 15) == 15 && abort && *abort)) return false;
+    }
+}
+
+struct TileArgs {
+    int64_t rows, cols;          // C's size (complex)
+    float2 *C;
+    int64_t ldc;
+    int kblocks;                 // K / 64
+    int tiles_m, tiles_n;        // row and column tiles
+    int *error;
+    unsigned long long wait;
+};
+
+__global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant__ CUtensorMap map_a,
+                                                          const __grid_constant__ CUtensorMap map_b, TileArgs args) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *done = empty + STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // tiles in groups of GROUP row tiles, the row tile fastest within a group: the CTAs resident at one time share
+    // a few A strips and B strips in L2
+    constexpr int GROUP = 16;
+    const int per_group = GROUP * args.tiles_n;
+    const int first_m = (int)(blockIdx.x / per_group) * GROUP;
+    const int in_group = (int)(blockIdx.x % per_group);
+    const int gm = min(GROUP, args.tiles_m - first_m);
+    const int m_tile = first_m + in_group % gm, n_tile = in_group / gm;
+    const int64_t m0 = (int64_t)m_tile * BM;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort = 0;
+        mbar_fence_init();
+        tma_prefetch(&map_a);
+        tma_prefetch(&map_b);
+    }
+    __syncwarp();
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t ring = smem_addr(smem);
+    const int kb_total = args.kblocks;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0) {
+        // producer: slice kb into stage kb % STAGES once the MMA has released it
+        int issued_last[STAGES];
+        for (int s = 0; s < STAGES; ++s) issued_last[s] = -1;
+        for (int kb = 0; kb < kb_total && ok; ++kb) {
+            const int s = kb % STAGES;
+            const uint32_t parity = ((kb / STAGES) & 1) ^ 1;
+            if (!wait_bounded(&empty[s], parity, args.wait, abort)) {
+                ok = false;
+                break;
+            }
+            mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+            const uint32_t a_dst = ring + s * STAGE_BYTES, b_dst = a_dst + A_BYTES;
+            tma_load_2d(a_dst, &map_a, kb * BK, (int)m0, smem_addr(&full[s]));
+            tma_load_2d(b_dst, &map_b, kb * BK, n_tile * BN, smem_addr(&full[s]));
+            issued_last[s] = kb;
+        }
+        if (!ok) {
+            *abort = 1;
+            atomicExch(args.error, ERR_TIMEOUT);
+        }
+        // every copy issued has landed before the CTA may exit (already true when the MMA consumed them all)
+        for (int s = 0; s < STAGES; ++s)
+            if (issued_last[s] >= 0) wait_bounded(&full[s], (issued_last[s] / STAGES) & 1, DRAIN_CYCLES, nullptr);
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        for (int kb = 0; kb < kb_total; ++kb) {
+            const int s = kb % STAGES;
+            if (!wait_bounded(&full[s], (kb / STAGES) & 1, args.wait, abort)) {
+                ok = false;
+                break;
+            }
+            fence_after_sync();
+            const uint32_t a_base = ring + s * STAGE_BYTES, b_base = a_base + A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk)
+                mma_bf16(tmem, sw128_desc(a_base + kk * 32), sw128_desc(b_base + kk * 32), (kb | kk) != 0);
+            mma_commit(smem_addr(&empty[s]));
+        }
+        if (!ok) {
+            *abort = 1;
+            atomicExch(args.error, ERR_TIMEOUT);
+        }
+        mma_commit(smem_addr(done));          // after every product issued (also on the way out)
+    }
+    __syncwarp();
+    // epilogue: all four warps, warp w owning tensor-memory lanes (tile rows) 32w .. 32w + 31. The wait for `done`
+    // does not stop early on an abort: the products in flight must finish before the tensor memory is freed (the
+    // MMA thread commits `done` on every path, at the latest one wait limit after an abort).
+    const bool finished = wait_bounded(done, 0, args.wait + DRAIN_CYCLES, nullptr);
+    fence_after_sync();
+    const int go = __shfl_sync(0xffffffffu, (int)(finished && !*abort), 0);
+    if (go) {
+        const int64_t row = m0 + warp * 32 + lane;
+        const int64_t c0 = (int64_t)n_tile * (BN / 2);
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int ch = 0; ch < BN / 32; ++ch) {
+            uint32_t r[32];
+            tmem_ld32(taddr + ch * 32, r);
+            if (row < args.rows) {
+                float2 *base = args.C + row;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int64_t col = c0 + ch * 16 + j;
+                    if (col < args.cols) {
+                        float2 *p = base + col * args.ldc;
+                        float2 v = *p;
+                        v.x -= __uint_as_float(r[2 * j]);
+                        v.y -= __uint_as_float(r[2 * j + 1]);
+                        *p = v;
+                    }
+                }
+            }
+        }
+    } else if (threadIdx.x == 0) {
+        *abort = 1;
+        atomicExch(args.error, ERR_TIMEOUT);
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        fence_after_sync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// A row-major BF16 plane (rows x K, K contiguous) as a TMA map of 64 x box_rows tiles, 128-byte swizzle.
+bool plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int box_rows) {
+    auto encode = encode_fn();
+    if (!encode) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int64_t padded_k(int k) { return ((int64_t)k + KPAD - 1) / KPAD * KPAD; }
+int64_t align1k(int64_t b) { return (b + 1023) / 1024 * 1024; }
+
+}  // namespace
+
+size_t tc_update_scratch_bytes(int64_t rows, int64_t cols, int k, int terms) {
+    const int64_t K = terms * 2 * padded_k(k);
+    return (size_t)(align1k(rows * K * 2) + align1k(2 * cols * K * 2));
+}
+
+cudaError_t tc_update_c64(int64_t rows, int64_t cols, int k, const float2 *A, int64_t lda, const float2 *B,
+                          int64_t ldb, float2 *C, int64_t ldc, int terms, void *scratch, bool a_packed, int *error,
+                          unsigned long long wait_cycles, cudaStream_t stream) {
+    if (rows <= 0 || cols <= 0 || k <= 0) return cudaSuccess;
+    if ((terms != 3 && terms != 6) || !A || !B || !C || !scratch || !error || lda < rows || ldb < k || ldc < rows ||
+        rows > (int64_t)0x7fffff00 || 2 * cols > (int64_t)0x7fffff00)
+        return cudaErrorInvalidValue;
+    static bool configured[64] = {};
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e) return e;
+    if (device < 64 && !configured[device]) {
+        if ((e = cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
+            return e;
+        configured[device] = true;
+    }
+    const int kp = (int)padded_k(k);
+    const int64_t K = (int64_t)terms * 2 * kp;
+    auto *pa = static_cast<__nv_bfloat162 *>(scratch);
+    auto *pb = reinterpret_cast<__nv_bfloat162 *>(static_cast<uint8_t *>(scratch) + align1k(rows * K * 2));
+    if (!a_packed) {
+        const dim3 grid((unsigned)((rows + 31) / 32), (unsigned)(kp / 32));
+        k_pack_a<<<grid, 256, 0, stream>>>(rows, k, kp, terms, A, lda, pa);
+        note_launches(1);
+    }
+    {
+        const dim3 grid((unsigned)std::max<int64_t>(1, (kp + 255) / 256), (unsigned)std::min<int64_t>(cols, 65535));
+        k_pack_b<<<grid, 256, 0, stream>>>(cols, k, kp, terms, B, ldb, pb);
+        note_launches(1);
+    }
+    CUtensorMap ma, mb;
+    if (!plane_map(&ma, pa, rows, K, BM) || !plane_map(&mb, pb, 2 * cols, K, BN)) return cudaErrorNotSupported;
+    TileArgs args;
+    args.rows = rows;
+    args.cols = cols;
+    args.C = C;
+    args.ldc = ldc;
+    args.kblocks = (int)(K / BK);
+    args.tiles_m = (int)((rows + BM - 1) / BM);
+    args.tiles_n = (int)((2 * cols + BN - 1) / BN);
+    args.error = error;
+    args.wait = wait_cycles;
+    const int64_t tiles = (int64_t)args.tiles_m * args.tiles_n;
+    if (tiles > 0x7fffffff) return cudaErrorInvalidValue;
+    k_tc_update<<<(unsigned)tiles, THREADS, SMEM, stream>>>(ma, mb, args);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+}  // namespace pq

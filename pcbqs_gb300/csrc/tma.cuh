@@ -47,12 +47,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
     return ok != 0;
 }
 
-// Wait for phase `phase` of `bar` with an iteration limit (each try_wait already suspends for a while).
-// Returns false when the limit ran out; the caller records the failure and stops using the buffer.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase, uint32_t limit = 1u << 22) {
-    for (uint32_t i = 0; i < limit; ++i)
-        if (mbar_try_wait(bar, phase)) return true;
-    return false;
+// Non-blocking probe of phase `phase`.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Limits below this many SM clocks are polled with the non-blocking probe: try_wait may itself suspend the thread
+// until the phase completes (a system-dependent time), which would outlast a short limit.
+constexpr unsigned long long PROBE_BELOW_CYCLES = 1ull << 16;
+
+// Wait for phase `phase` of `bar` for at most `limit` SM clocks. Returns false when the limit ran out; the caller
+// records the failure and, before its block exits, waits again (with a long limit) for the copies it issued.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase, unsigned long long limit) {
+    const long long t0 = clock64();
+    const bool probe = limit < PROBE_BELOW_CYCLES;
+    for (;;) {
+        if (probe ? mbar_test_wait(bar, phase) : mbar_try_wait(bar, phase)) return true;
+        if ((unsigned long long)(clock64() - t0) > limit) return false;
+    }
 }
 
 }  // namespace pq

@@ -241,7 +241,8 @@ __device__ __forceinline__ void diag_finish(DiagSmem &sm, const float2 *partial,
 // All thread blocks of the (cooperative, co-resident) grid meet here: one arrival counter that only grows, barrier
 // number `index` complete when it reaches (index + 1) x blocks; thread 0 arrives with release semantics (covering its
 // block's writes through the preceding __syncthreads) and polls with acquire loads. Bounded: after about a second
-// of polling (clock64) the block records TRI_TIMEOUT in *status and returns false, as do blocks that see the status.
+// of polling (clock64; the library's wait limit) the block records TRI_TIMEOUT in *status and returns false, as do
+// blocks that see the status.
 constexpr int TRI_TIMEOUT = 1;
 
 __device__ __forceinline__ unsigned load_acquire(const unsigned *p) {
@@ -250,7 +251,7 @@ __device__ __forceinline__ unsigned load_acquire(const unsigned *p) {
     return v;
 }
 
-__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned index, int *status) {
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned index, int *status, long long limit) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -260,7 +261,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned index, in
         const unsigned target = (index + 1) * gridDim.x;
         const long long start = clock64();
         while (load_acquire(count) < target) {
-            if (clock64() - start > (2ll << 30) || *(volatile int *)status) {
+            if (clock64() - start > limit || *(volatile int *)status) {
                 atomicExch(status, TRI_TIMEOUT);
                 ok = 0;
                 break;
@@ -284,16 +285,17 @@ struct SweepArgs {
     unsigned *xready;      // per sweep (stride SYNC_STRIDE): diagonal quarters finished (4 per step)
     unsigned *pdone;       // per sweep and step (stride SYNC_STRIDE): panel items finished
     int *status;
+    long long wait;        // limit (SM clocks) of each bounded wait
 };
 
 // Bounded wait until *counter >= target (thread 0 polls with acquire loads; the block then proceeds together).
-__device__ __forceinline__ bool wait_for(const unsigned *counter, unsigned target, int *status) {
+__device__ __forceinline__ bool wait_for(const unsigned *counter, unsigned target, int *status, long long limit) {
     __shared__ int ok;
     if (threadIdx.x == 0) {
         ok = 1;
         const long long start = clock64();
         while (load_acquire(counter) < target) {
-            if (clock64() - start > (2ll << 30) || *(volatile int *)status) {
+            if (clock64() - start > limit || *(volatile int *)status) {
                 atomicExch(status, TRI_TIMEOUT);
                 ok = 0;
                 break;
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
     const int me = role_id - DIAG_BLOCKS - TAIL_BLOCKS;
     const size_t buf = (size_t)(MAX_SPLITS + 1) * B * KC;
     for (int dir = 0; dir < 2; ++dir) {
-        if (dir == 1 && !grid_barrier(a.barrier, 0, a.status)) return;      // the backward sweep needs all of y
+        if (dir == 1 && !grid_barrier(a.barrier, 0, a.status, a.wait)) return;      // the backward sweep needs all of y
         const float2 *inv = dir == 0 ? a.inv_lower : a.inv_upper;
         const float2 *rhs = dir == 0 ? a.b : a.y;
         float2 *x = dir == 0 ? a.y : a.z;
@@ -377,13 +379,13 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
             if (diag) {
                 diag_stage(dsm, inv + (int64_t)J * B * B, rhs, row0, m, a.kpad, a.c0, role_id);
                 const unsigned need = (unsigned)(tail_runs * TAIL_BLOCKS + sc.bulk_runs * ((m + PANEL_ROWS - 1) / PANEL_ROWS));
-                if (need && !wait_for(pdone + (size_t)step * SYNC_STRIDE, need, a.status)) return;
+                if (need && !wait_for(pdone + (size_t)step * SYNC_STRIDE, need, a.status, a.wait)) return;
                 diag_finish(dsm, slots, tail_runs + sc.bulk_runs, x, row0, m, a.kpad, a.c0, role_id);
                 signal(xready);
             } else if (tail) {
                 if (tail_runs) {
                     // block `step - 1` of this sweep must be solved: DIAG_BLOCKS quarters per step
-                    if (!wait_for(xready, (unsigned)(DIAG_BLOCKS * step), a.status)) return;
+                    if (!wait_for(xready, (unsigned)(DIAG_BLOCKS * step), a.status, a.wait)) return;
                     panel_block(a.lu, a.n, row0, m, sc.tail0, sc.tail1, x, a.kpad, a.c0,
                                 slots + (size_t)sc.bulk_runs * B * KC, role_id - DIAG_BLOCKS);
                     signal(pdone + (size_t)step * SYNC_STRIDE);
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_tri_sweeps(SweepArgs a) {
                     bool waited = false;
                     for (int item = me; item < mg * nx.bulk_runs; item += bulk_workers) {
                         if (!waited) {
-                            if (step > 0 && !wait_for(xready, (unsigned)(DIAG_BLOCKS * step), a.status)) return;
+                            if (step > 0 && !wait_for(xready, (unsigned)(DIAG_BLOCKS * step), a.status, a.wait)) return;
                             waited = true;
                         }
                         const int s = item / mg;
@@ -527,7 +529,7 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
             return e;
         SweepArgs a{lu, n, nblk, inv_lower, inv_upper, p->b, p->y, p->z, p->kpad, c0, p->partial, p->sync,
                     p->sync + SYNC_STRIDE, p->sync + 4 * SYNC_STRIDE,
-                    reinterpret_cast<int *>(p->sync + 3 * SYNC_STRIDE)};
+                    reinterpret_cast<int *>(p->sync + 3 * SYNC_STRIDE), (long long)wait_cycles()};
         void *args[] = {&a};
         if ((e = cudaLaunchCooperativeKernel((const void *)k_tri_sweeps, dim3(grid), dim3(PANEL_THREADS), args, 0,
                                              s)))

@@ -507,7 +507,8 @@ class PeecModel(PeecTopology):
             return e0.elapsed_time(e1)
         return self._pool.submit(work)
 
-    FACTOR_MATH = {'fp32': 0, 'bf16x9': 1, 'bf16x9-blocked': 2, 'fp32-blocked': 3}
+    FACTOR_MATH = {'fp32': 0, 'bf16x9': 1, 'bf16x9-blocked': 2, 'fp32-blocked': 3, 'tc3-blocked': 4,
+                   'tc6-blocked': 5}
 
     def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='bf16x9-blocked', anchors=None):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).

@@ -1,7 +1,7 @@
 """Golden Biot-Savart fields from the reference itself (pcbqs.biot.h_sheets / h_segments, pcbqs._numerics.currents
 .rwg_currents) on the synthetic boards with seeded random RWG currents.
 
-    python tests/golden/make_biot_golden.py      (this container only: needs the reference checkout)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_biot_golden.py      (this container only: needs the reference checkout)
 
 Writes tests/golden/biot_<board>.npz: the RWG coefficients I (ne, k), observation points (grids at 0.5 and 2 mm
 above the top sheet and points 50 um above the copper, inside the near-refinement zone), each sheet's field from

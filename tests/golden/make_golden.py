@@ -1,7 +1,7 @@
 """Golden vectors from the reference pcbqs itself (its NumPy path and its compiled core), for the oracle and the
 device parity tests.
 
-    python tests/golden/make_golden.py     (this container only: needs the reference checkout; builds oracle/_ref)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_golden.py     (this container only: needs the reference checkout; builds oracle/_ref)
 
 Writes tests/golden/golden_tiny8.npz and golden_<board>.npz for the boards of make_meshes.py:
   tiny8     the reference test suite's 8-triangle two-layer fixture (tests/test_static_backends.py:14-24):

@@ -2,7 +2,7 @@
 current_deposit, for seeded random branch currents on the tiny two-layer board (this container only: needs the
 reference checkout).
 
-    python tests/golden/make_hgrid_golden.py
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_hgrid_golden.py
 
 Writes tests/golden/hgrid_tiny.npz: the branch currents i (2, ne) (two excitations), the grids x, y, the heights, the
 refinement and the field (nx, ny, nh, 3, 2).

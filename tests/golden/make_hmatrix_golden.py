@@ -2,7 +2,7 @@
 RwgEntries provider, exactly as compressed.edge_inductance builds the compressed inductance
 (src/pcbqs/compressed.py:60-96), applied to seeded random complex vectors.
 
-    python tests/golden/make_hmatrix_golden.py      (this container only: needs the reference checkout)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_hmatrix_golden.py      (this container only: needs the reference checkout)
 
 Writes tests/golden/hmatrix_<board>.npz: X (ne, 3) complex, Y_h = H X (the reference's compressed product),
 Y_dense = L X with the reference's dense L (static_moments + edge_inductance), and the build info.

@@ -1,7 +1,7 @@
 """Golden layered-dielectric vectors from the reference itself (this container only: needs the reference checkout
 and its compiled core in oracle/_ref).
 
-    python tests/golden/make_layered_golden.py
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_layered_golden.py
 
 Writes
   tests/golden/layered_spectral.npz  the reference's own spectral-network fixture for the image series

@@ -1,6 +1,6 @@
 """Generate the seeded synthetic boards used by the tests and the benchmark, meshed with pcbqs's own mesher core.
 
-    python tests/golden/make_meshes.py            (needs the reference checkout and oracle/_ref, this container)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py            (needs the reference checkout and oracle/_ref, this container)
 
 Each board is written as tests/golden/<name>.npz with: nodes (N, 2) m, tris (nt, 3), z (nt) m, layer (nt),
 terminal triangles (term_names, term_ptr, term_tris: CSR), via fans (fan_ptr, fan_tris: CSR, each merged into one
@@ -17,8 +17,8 @@ The boards themselves are synthetic stand-ins with the shapes and sizes of the b
           (via segments: via_seg (x, y, r, z0, z1) m and via_fans, the fan of each end), one port at the near
           end between the strips                                                              (~800 triangles)
 
-    python tests/golden/make_meshes.py viapair    (that board alone; the others keep their meshes)
-    python tests/golden/make_meshes.py train      (train_0 .. train_5: seeded random small boards, alternately a
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py viapair    (that board alone; the others keep their meshes)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py train      (train_0 .. train_5: seeded random small boards, alternately a
                                                    plane pair and a via-joined strip pair of random sizes, vias and
                                                    mesh sizes; the learned preconditioner's training systems)
 """

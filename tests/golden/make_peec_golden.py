@@ -1,6 +1,6 @@
 """Golden port impedances from the reference's own PEEC solve (pcbqs.peec.solve, dense LU) on the synthetic boards.
 
-    python tests/golden/make_peec_golden.py     (this container only: needs the reference checkout)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_peec_golden.py [planes | viapair | board ...]
 
 The reference's MQS model class needs shapely only for meshing and region handling, which these boards do not use
 (their meshes are given). shapely is absent here, so a stand-in module that only provides its names is put in
@@ -137,9 +137,42 @@ def stack(name='tiny', slab=(0.0, 0.2e-3, 4.3, 0.02)):
     print(name, 'stack', np.round(Z[1], 6))
 
 
+def planes(freqs=(1e6,)):
+    """peec_planes.npz: the plane pair (22,554 triangles, 32,990 unknowns, 8 ports), DC sheet resistance, at the
+    benchmark's 1 MHz. The reference's MQS._solve_charge factors each frequency once for all 8 drives. The system
+    is factored by the reference's double-precision path of lu_factor_rows (PCBQS_LU=double: LAPACK zgetrf in the
+    system's own memory, src/pcbqs/kernels.py:265-284) rather than MixedLU, whose complex64 copy and kept double
+    matrix do not fit beside the model's dense R, L and potential projections in a 62 GB host; MixedLU refines to
+    1e-12 of that same double solve (kernels.py:157-172). The edge matrices (MQS._mats and the copper cache
+    MQS._copper, src/pcbqs/mqs.py:639-661) are dropped once peec.prepare has projected them: with DC resistance the
+    solve reads only the projections."""
+    import os
+    import time
+    os.environ['PCBQS_LU'] = 'double'
+    from pcbqs_gb300.board import Board
+    b = Board.load('planes')
+    q = reference_model(b)
+    from pcbqs.peec import prepare
+    t = time.perf_counter()
+    m = prepare(q)
+    print(f'prepare {time.perf_counter() - t:.1f} s, unknowns {m["K"].shape[1]}', flush=True)
+    q._mats = q._copper = None
+    freqs = np.asarray(freqs, float)
+    t = time.perf_counter()
+    names, Z, diag = port_matrix(q, b, freqs)
+    print(f'solve {time.perf_counter() - t:.1f} s', flush=True)
+    assert np.allclose(np.diagonal(Z, axis1=1, axis2=2), diag, rtol=1e-9), 'port voltage convention'
+    np.savez_compressed(HERE / 'peec_planes.npz', freqs=freqs, ports=np.array(names), Z=Z, z_diag=diag,
+                        unknowns=m['K'].shape[1], loops=m['nl'], components=m['B'].shape[1],
+                        conductor_loss='dc', lu='double')
+    print('planes', np.round(Z[0], 6))
+
+
 if __name__ == '__main__':
     if sys.argv[1:] == ['viapair']:
         main(('viapair',), ('dc', 'slab'))
+    elif sys.argv[1:] == ['planes']:
+        planes()
     else:
         main(tuple(sys.argv[1:]) or ('tiny', 'strip'))
         stack('tiny')

@@ -1,6 +1,6 @@
 """Golden copper-port reductions from the reference's own CopperPorts (magnetic MQS, no capacitance).
 
-    python tests/golden/make_ports_golden.py     (this container only: needs the reference checkout)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_ports_golden.py     (this container only: needs the reference checkout)
 
 The model object is the one make_peec_golden.py builds around a given mesh (src/pcbqs/mqs.py:300-420), with
 capacitance off, so that pcbqs.mqs_ports.CopperPorts (src/pcbqs/mqs_ports.py:27-53) reduces the copper to its
@@ -12,7 +12,7 @@ Writes tests/golden/ports_<board>.npz: freqs (DC included), port names, Z (nf, n
 highest frequency (R_ohm, L_H); for a board with plated vias (the via pair) also the reference's via_resistance and
 via_inductance of its segments (src/pcbqs/mqs.py:132-153).
 
-    python tests/golden/make_ports_golden.py [strip|viapair]
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_ports_golden.py [strip|viapair]
 """
 import sys
 from pathlib import Path

@@ -168,3 +168,39 @@ def test_mixed_fill_against_fp64_oracle(device_library, board):
     Po = O.potential(mats[0], og.area, b.node_of, b.er)
     P = P.cpu().numpy()
     assert np.abs(P - Po).max() / np.abs(Po).max() < 2e-6
+
+
+def test_mixed_fill_planes_against_reference_rows(device_library):
+    """The mixed fill on the benchmarked board (22,554 triangles, 33,368 edges): L and P at the reference's sampled
+    rows (golden_planes.npz: the reference's FP64 static_combine and _set_potential) within 2e-6 of their largest
+    entry, the diagonals within 1e-5 relative, and the analytic pair count exact."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.fill import DeviceFill
+    gold = load_golden('planes')
+    b = Board.load('planes')
+    f = DeviceFill(b.nodes, b.tris, b.z, outer_levels=1, near=3.0)
+    planes, analytic = f.moments_local()
+    assert analytic == int(gold['analytic'])
+    L, Lf = f.inductance_local(planes)
+    rows = torch_rows(L, gold['edge_rows'])
+    scale = np.abs(gold['L_rows']).max()
+    errL = np.abs(rows - gold['L_rows']).max() / scale
+    assert errL < 2e-6, errL
+    assert torch_diag(L) == pytest.approx(gold['L_diag'], rel=1e-5)
+    del L, Lf
+    P, Pf = f.potential_single(planes[0], b.node_of, b.er)
+    prow = torch_rows(P, gold['node_rows'])
+    errP = np.abs(prow - gold['P_rows']).max() / np.abs(gold['P_rows']).max()
+    assert errP < 2e-6, errP
+    assert torch_diag(P) == pytest.approx(gold['P_diag'], rel=1e-5)
+    print(f'planes mixed fill: L error {errL:.2e}, P error {errP:.2e} of the largest sampled entry')
+
+
+def torch_rows(M, rows):
+    import torch
+    return M[torch.as_tensor(np.asarray(rows), device=M.device)].cpu().numpy()
+
+
+def torch_diag(M):
+    import torch
+    return torch.diagonal(M).cpu().numpy()

@@ -38,7 +38,9 @@ def _backward_error(A, LU, piv):
 
 
 @pytest.mark.parametrize('n,block,math', [(300, 64, 0), (1000, 128, 1), (1000, 1000, 1), (2100, 256, 1),
-                                          (2100, 1024, 0), (4097, 512, 1), (4500, 2048, 1), (6000, 4096, 1)])
+                                          (2100, 1024, 0), (4097, 512, 1), (4500, 2048, 1), (6000, 4096, 1),
+                                          (300, 64, 3), (1000, 128, 3), (2100, 256, 3), (4097, 512, 3),
+                                          (4500, 2048, 3), (6000, 4096, 3)])
 def test_blocked_lu_matches_getrf(device_library, n, block, math):
     import torch
     g = torch.Generator(device='cuda').manual_seed(n + block)
@@ -155,3 +157,24 @@ def test_dense_gmres_solves_potential_systems(device_library, precondition, loss
     assert (torch.linalg.norm(x - ref) / torch.linalg.norm(ref)).item() < 1e-8
     if precondition:
         assert its.max() <= (8 if lossy else 4), its
+
+
+@pytest.mark.parametrize('n,block', [(1000, 128), (4500, 2048)])
+def test_blocked_lu_three_term_update(device_library, n, block):
+    """math 2: the tcgen05 trailing update with three BF16 part products (about 16 correct bits per product): a
+    factor with a backward error near 1e-5 rather than FP32's, which still brings a solve close enough for
+    iterative refinement (one refinement step with the FP32 factor lowers the residual)."""
+    import torch
+    g = torch.Generator(device='cuda').manual_seed(n + block + 2)
+    A = torch.complex(torch.randn(n, n, device='cuda', generator=g), torch.randn(n, n, device='cuda', generator=g))
+    LU, piv = _factor(device_library, A, block, 2)
+    assert torch.isfinite(torch.view_as_real(LU)).all()
+    ours = _backward_error(A, LU, piv)
+    assert ours < 1e-4, ours
+    b = torch.complex(torch.randn(n, 2, device='cuda', generator=g), torch.randn(n, 2, device='cuda', generator=g))
+    x = torch.linalg.lu_solve(LU, piv, b)
+    r = b - A @ x
+    res0 = (torch.linalg.norm(r) / torch.linalg.norm(b)).item()
+    x = x + torch.linalg.lu_solve(LU, piv, r)
+    res1 = (torch.linalg.norm(b - A @ x) / torch.linalg.norm(b)).item()
+    assert res1 < 0.5 * res0, (res0, res1)

@@ -83,18 +83,32 @@ def test_mixed_precision_solve_matches_reference(device_library, board):
     assert model.timings['outer_steps'] >= 1
 
 
-def test_planes_mixed_and_fp64_solves_agree(device_library):
-    """The 22,554-triangle plane pair at 1 MHz: the mixed solve and the FP64-operator GMRES (both preconditioned by
-    the complex64 factor) reach 1e-8 and agree on every port impedance to 1e-7; the matrix is reciprocal and its
-    real part (loss) non-negative on the diagonal."""
+@pytest.mark.parametrize('factor_math', ['bf16x9-blocked', 'tc6-blocked', 'tc3-blocked'])
+def test_planes_solves_match_reference(device_library, factor_math):
+    """The benchmarked board, the 22,554-triangle plane pair (32,990 unknowns, 8 ports) at 1 MHz, against the
+    reference's own dense solve of it (tests/golden/peec_planes.npz: pcbqs.peec.solve through MQS, LAPACK's double
+    LU): the FP64 path (FP64 fill and operator) and the mixed path (FP32 far pairs and inner products under FP64
+    refinement), both with the complex64-factor preconditioner of each trailing-update arithmetic, reach a 1e-8
+    relative residual and match every port impedance to 1e-6 of the largest. The part of Z that differs between
+    ports (Z minus its mean entry: the inductive and resistive coupling under the common plane capacitance) to 1e-3
+    of its own largest entry. The matrix is reciprocal, with non-negative loss on the diagonal."""
     from pcbqs_gb300.board import Board
     from pcbqs_gb300.peec import PeecModel
+    from conftest import GOLDEN
+    with np.load(GOLDEN / 'peec_planes.npz') as g:
+        f, Zr = float(g['freqs'][0]), g['Z'][0]
     model = PeecModel(Board.load('planes'))
-    fp64 = model.solve([1e6], precondition='lu32')
-    mixed = model.solve([1e6], precondition='lu32', mixed=True)
+    fp64 = model.solve([f], precondition='lu32', factor_math=factor_math)
+    model.assemble(mixed=True)
+    mixed = model.solve([f], precondition='lu32', mixed=True, factor_math=factor_math)
     Z64, Zm = fp64.impedance[0], mixed.impedance[0]
     assert (fp64.residual <= 1e-8).all() and (mixed.residual <= 1e-8).all()
-    assert np.abs(Zm - Z64).max() / np.abs(Z64).max() < 1e-7
+    scale, Dr = np.abs(Zr).max(), Zr - Zr.mean()
+    for Z in (Z64, Zm):
+        err, derr = np.abs(Z - Zr).max() / scale, np.abs((Z - Z.mean()) - Dr).max() / np.abs(Dr).max()
+        print(f'{factor_math}: port Z error {err:.2e} of max |Z|, coupling error {derr:.2e}; GMRES '
+              f'{fp64.iterations.max()} / {mixed.iterations.max()} steps')
+        assert err < 1e-6 and derr < 1e-3, (err, derr)
     assert np.abs(Z64 - Z64.T).max() <= 1e-6 * np.abs(Z64).max()
     assert (np.diag(Z64).real > 0).all() and (np.diag(Z64).imag < 0).all()     # capacitive plane pair at 1 MHz
 

@@ -1,5 +1,6 @@
 """The CPU oracle pinned against the reference's own outputs (tests/golden/, made by make_golden.py)."""
 import platform
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -114,3 +115,23 @@ def test_oracle_on_boards(board):
     assert P[gold['node_rows']] == pytest.approx(gold['P_rows'], rel=1e-12)
     i, j = gold['P_at']
     assert P[i, j] == pytest.approx(gold['P_val'], rel=1e-12)
+
+
+@pytest.mark.parametrize('board,mixed', [('tiny', False), ('strip', False), ('strip', True)])
+def test_cpu_dense_solve_matches_reference(board, mixed):
+    """The CPU restatement of the reference's dense PEEC solve (the benchmark's reference arm) against the
+    reference's own port impedances: the C oracle's fill, combine and aggregation, then topology, projections, the
+    scaled system, LU (double, or MixedLU's complex64 factor with refinement) and every drive."""
+    from oracle import peec_cpu
+    from pcbqs_gb300.board import Board
+    b = Board.load(board)
+    g = O.Geometry(b.nodes, b.tris, b.z, 1)
+    mats, _ = O.fill(g, 3.0, 1, False)
+    rwg = O.RWG(g.nodes, g.tris)
+    L = O.combine(rwg, mats)
+    P = O.potential(mats[0], g.area, b.node_of, b.er)
+    solver = peec_cpu.DenseSolve(b, rwg, L, P)
+    with np.load(Path(__file__).parent / 'golden' / f'peec_{board}.npz') as ref:
+        for f, Zref in zip(ref['freqs'], ref['Z']):
+            Z = solver.solve(float(f), mixed=mixed)
+            assert np.abs(Z - Zref).max() / np.abs(Zref).max() < 1e-8
