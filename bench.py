@@ -63,7 +63,7 @@ def parse():
     p.add_argument('--anchors', type=int, default=8, help='complex64 factors shared across the sweep')
     p.add_argument('--case', default=None,
                    help='time one kernel case small enough for a full ncu capture instead of the benchmark: '
-                        'fill:BOARD[:TRIANGLES] | lu:BOARD[:K...] | dense:N[:K] | getrf:N[:BLOCK...] | '
+                        'fill:BOARD[:TRIANGLES] | lu:BOARD[:K...] | dense:N[:K] | getrf:N[:BLOCK[:MATH...]] | '
                         'potrf:N[:BLOCK...] | update:ROWS:COLS:K (CUDA-event times after a warm-up call)')
     return p.parse_args()
 
@@ -362,9 +362,9 @@ def case_lu(board, *ks):
         lib.pcbqs_gb300_peec_destroy(handle)
 
 
-def case_getrf(n, *blocks):
-    """The blocked complex64 LU of a random n x n matrix with each panel width and each trailing update: cuBLAS
-    BF16x9 (math 1), this library's tcgen05 update with 3 and 6 BF16 part products (math 2, 3)."""
+def case_getrf(n, block=2048, *maths):
+    """The blocked complex64 LU of a random n x n matrix with `block`-column panels, twice with each trailing update
+    given (default all: cuBLAS BF16x9 = 1, this library's tcgen05 update with 3 and 6 BF16 part products = 2, 3)."""
     import ctypes
     import torch
     from pcbqs_gb300 import _lib
@@ -377,8 +377,8 @@ def case_getrf(n, *blocks):
     singular = ctypes.c_int32(0)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     flops = 8 / 3 * n ** 3
-    for block in (blocks or (2048,)):
-        for math in (1, 2, 3):
+    for block in (int(block),):
+        for math in tuple(int(m) for m in maths) or (1, 2, 3):
             for _ in range(2):
                 F.copy_(A)
                 ms, status = _event_ms(lambda: lib.pcbqs_gb300_lu_factor_c64(n, F.data_ptr(), piv.data_ptr(),

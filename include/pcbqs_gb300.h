@@ -69,8 +69,9 @@ int pcbqs_gb300_pairs_device(pcbqs_gb300_ctx *ctx, const int32_t *p, const int32
  * caching allocator already holds the device memory, or a steady-state loop must not stall in cudaMalloc or
  * cudaFree). It allocates nothing: its scratch is one fixed array in this library's device image, shared by every
  * call on a device, which limits a call to 1,048,576 pairs (larger n: status 1 with a message). The first call on
- * a device looks up that array's address and should come before any stream capture on the device. Calls whose
- * work overlaps on the GPU race on the shared scratch: serialize them. Has no counterpart in the reference. */
+ * a device looks up that array's address there. Every call synchronizes `stream` and reads its status flags back
+ * into host memory, so a call cannot be captured into a CUDA graph. Calls whose work overlaps on the GPU race on
+ * the shared scratch: serialize them. Has no counterpart in the reference. */
 int pcbqs_gb300_pairs_no_alloc(pcbqs_gb300_ctx *ctx, const int32_t *p, const int32_t *q, const double *d,
                                const int32_t *kind, int64_t n, int scalar_only, double *out, void *stream);
 

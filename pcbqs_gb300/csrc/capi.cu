@@ -530,7 +530,8 @@ int pcbqs_gb300_potential_device(int64_t nn, const int64_t *start, const int32_t
 // library, is never allocated or freed by a call, and limits one call to NOALLOC_MAX_PAIRS pairs.
 //
 // Set-up: the first call on a device looks up the array's device address on that device (cudaGetSymbolAddress,
-// which also loads this module there). Make that first call before any stream capture starts on the device.
+// which also loads this module there). Every call then synchronizes its stream to read the status flags back into
+// host memory, so no call can be captured into a CUDA graph.
 //
 // Sharing: every call on a device uses the same array, which still holds the previous call's contents. Each call
 // clears the counters and flags before its kernels run; the order array is fully rewritten before it is read.

@@ -7,6 +7,7 @@
 //   src/pcbqs/core/static_kernels.hpp:147-172  static_pairs      (k_pairs)
 //   src/pcbqs/core/static_kernels.hpp:184-252  static_fill       (k_fill_tiles + k_fill_near)
 //   src/pcbqs/static_cupy_kernels.py:117-157   device row strips (the compaction of near pairs by level)
+#include <atomic>
 #include <cmath>
 #include "common.cuh"
 #include "fill.cuh"
@@ -313,13 +314,18 @@ __global__ void k_fill_near(Geometry g, Planes<T> out, const int2 *list, const u
 // ---------------------------------------------------------------------------------------------------------------
 // Host launchers.
 
+// SM count of the current device, looked up once per device.
+constexpr int MAX_DEVICES = 64;
 static int sm_count() {
-    static int count = 0;
+    static std::atomic<int> counts[MAX_DEVICES];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= MAX_DEVICES) dev = 0;
+    int count = counts[dev].load(std::memory_order_relaxed);
     if (!count) {
-        int dev = 0;
-        cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
         if (count <= 0) count = 1;
+        counts[dev].store(count, std::memory_order_relaxed);
     }
     return count;
 }
@@ -365,10 +371,15 @@ static cudaError_t launch_fill_t(const Geometry &g, const Planes<T> &out, const 
     const int nb = (g.nt + TILE - 1) / TILE;
     const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
     const size_t smem = fill_smem_bytes();
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_fill_tiles<T, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        configured = true;
+    // the dynamic shared-memory limit is a per-device attribute of the kernel: raised once on each device
+    static std::atomic<bool> configured[MAX_DEVICES];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= MAX_DEVICES || !configured[dev].load(std::memory_order_relaxed)) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_fill_tiles<T, LOCAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        if (dev >= 0 && dev < MAX_DEVICES) configured[dev].store(true, std::memory_order_relaxed);
     }
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_tiles<T, LOCAL>, FILL_THREADS, smem);

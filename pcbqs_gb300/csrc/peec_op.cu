@@ -930,6 +930,10 @@ struct pcbqs_gb300_peec {
 
 namespace {
 #define pfail pq::fail
+
+// A failed CUDA call's status: 6 when a bounded device wait gave up (cudaErrorLaunchTimeout from this library's
+// own kernels), 2 otherwise.
+static int cuda_status(cudaError_t e) { return e == cudaErrorLaunchTimeout ? ERR_TIMEOUT : ERR_CUDA; }
 constexpr int LU_BLOCK = 2048;     // panel width of the blocked factorization (math 2 .. 5)
 Csr csr_of(const pcbqs_gb300_csr &c) {
     Csr out;
@@ -1003,7 +1007,7 @@ int pcbqs_gb300_peec_apply(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
     cudaError_t e = h->op.apply(k, sys, reinterpret_cast<const cd *>(in), reinterpret_cast<cd *>(out), st);
     if (!e) e = cudaStreamSynchronize(st);
     dev_free(sys, st);
-    if (e) return pfail(ERR_CUDA, "peec_apply: %s", cudaGetErrorString(e));
+    if (e) return pfail(cuda_status(e), "peec_apply: %s", cudaGetErrorString(e));
     return OK;
 }
 
@@ -1045,7 +1049,7 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     dev_free(klk, st); dev_free(tpt, st); dev_free(tpt_im, st); dev_free(singular, st);
     if (e) {
         delete bj;
-        return pfail(ERR_CUDA, "block_jacobi: %s", cudaGetErrorString(e));
+        return pfail(cuda_status(e), "block_jacobi: %s", cudaGetErrorString(e));
     }
     if (sing) {
         delete bj;
@@ -1119,7 +1123,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         e = cudaStreamSynchronize(st);
         dev_free(w, st);
         dev_free(wt, st);
-        if (e) return pfail(ERR_CUDA, "peec_factor: %s", cudaGetErrorString(e));
+        if (e) return pfail(cuda_status(e), "peec_factor: %s", cudaGetErrorString(e));
     }
     auto *lu = new (std::nothrow) LuPrecond();
     if (!lu) return pfail(ERR_MEMORY, "peec_factor: host allocation");
@@ -1154,7 +1158,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         }
         if ((e = lu->tri.prepare(lu->lu, n, lu->ipiv, st))) {
             delete lu;
-            return pfail(ERR_CUDA, "peec_factor: triangular-solve set-up: %s", cudaGetErrorString(e));
+            return pfail(cuda_status(e), "peec_factor: triangular-solve set-up: %s", cudaGetErrorString(e));
         }
         delete h->lu;
         h->lu = lu;
@@ -1190,7 +1194,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     }
     if ((e = lu->tri.prepare(lu->lu, n, lu->ipiv, st))) {
         delete lu;
-        return pfail(ERR_CUDA, "peec_factor: triangular-solve set-up: %s", cudaGetErrorString(e));
+        return pfail(cuda_status(e), "peec_factor: triangular-solve set-up: %s", cudaGetErrorString(e));
     }
     delete h->lu;
     h->lu = lu;
@@ -1216,7 +1220,7 @@ int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *h, int k, const double *in, doub
     cd *y = reinterpret_cast<cd *>(out);
     cudaError_t e = method == 0 ? h->lu->apply(k, nullptr, x, y, st) : h->lu->apply_library(k, x, y, st);
     if (!e) e = cudaStreamSynchronize(st);
-    if (e) return pfail(ERR_CUDA, "peec_lu_solve: %s", cudaGetErrorString(e));
+    if (e) return pfail(cuda_status(e), "peec_lu_solve: %s", cudaGetErrorString(e));
     return OK;
 }
 
@@ -1238,7 +1242,7 @@ int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
                         : precondition == 2 ? static_cast<Preconditioner *>(h->lu) : nullptr;
     cudaError_t e = gmres_batched(h->op, M, k, sys_host,
                                   reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x), opt, rep, st);
-    if (e) return pfail(ERR_CUDA, "peec_gmres: %s", cudaGetErrorString(e));
+    if (e) return pfail(cuda_status(e), "peec_gmres: %s", cudaGetErrorString(e));
     bool ok = true;
     for (int s = 0; s < k; ++s) {
         if (iterations) iterations[s] = rep.iterations[s];
@@ -1254,7 +1258,7 @@ int pcbqs_gb300_dense_apply(int64_t rows, int k, const double *M, int64_t ld, co
     if (rows <= 0 || k <= 0 || !M || ld < rows || !X || !Y) return pfail(ERR_ARGUMENT, "dense_apply: invalid argument");
     cudaError_t e = dense_sym_apply<double, 2>(rows, k, M, ld, reinterpret_cast<const cd *>(X), reinterpret_cast<cd *>(Y),
                                                static_cast<cudaStream_t>(stream));
-    if (e) return pfail(ERR_CUDA, "dense_apply: %s", cudaGetErrorString(e));
+    if (e) return pfail(cuda_status(e), "dense_apply: %s", cudaGetErrorString(e));
     return OK;
 }
 
@@ -1268,7 +1272,7 @@ int pcbqs_gb300_dense_apply_single(int64_t rows, int k, const float *Mf, int64_t
     if (e) return pfail(ERR_MEMORY, "dense_apply_single: %s", cudaGetErrorString(e));
     e = dense_sym_apply<float, 4>(rows, k, Mf, ld, reinterpret_cast<const cd *>(X), reinterpret_cast<cd *>(Y), st, xf);
     dev_free(xf, st);
-    if (e) return pfail(ERR_CUDA, "dense_apply_single: %s", cudaGetErrorString(e));
+    if (e) return pfail(cuda_status(e), "dense_apply_single: %s", cudaGetErrorString(e));
     return OK;
 }
 
@@ -1278,7 +1282,7 @@ int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *str
     k_to_f32<<<grid_of(count), 256, 0, static_cast<cudaStream_t>(stream)>>>(count, in, out);
     note_launches(1);
     cudaError_t e = cudaGetLastError();
-    return e ? pfail(ERR_CUDA, "to_single: %s", cudaGetErrorString(e)) : OK;
+    return e ? pfail(cuda_status(e), "to_single: %s", cudaGetErrorString(e)) : OK;
 }
 
 int pcbqs_gb300_peec_single(pcbqs_gb300_peec *h, const float *Lf, int64_t ldlf, const float *Pf, const float *Pfim,
@@ -1320,7 +1324,7 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *h, int k, const int32_t *sys_
     int steps = 0;
     cudaError_t e = refine_batched(h->op, single, M, k, sys_host, reinterpret_cast<const cd *>(b),
                                    reinterpret_cast<cd *>(x), opt, rep, steps, static_cast<cudaStream_t>(stream));
-    if (e) return pfail(ERR_CUDA, "peec_solve_mixed: %s", cudaGetErrorString(e));
+    if (e) return pfail(cuda_status(e), "peec_solve_mixed: %s", cudaGetErrorString(e));
     if (outer_steps) *outer_steps = steps;
     bool ok = true;
     for (int s = 0; s < k; ++s) {
@@ -1369,7 +1373,7 @@ int pcbqs_gb300_dense_gmres(int64_t n, const double *A, const double *Aim, int64
     GmresReport rep;
     e = gmres_batched(op, M, k, sys.data(), reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x), opt, rep, st);
     dev_free(J.d, st);
-    if (e) return pfail(ERR_CUDA, "dense_gmres: %s", cudaGetErrorString(e));
+    if (e) return pfail(cuda_status(e), "dense_gmres: %s", cudaGetErrorString(e));
     bool ok = true;
     for (int s = 0; s < k; ++s) {
         if (iterations) iterations[s] = rep.iterations[s];

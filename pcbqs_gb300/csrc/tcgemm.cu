@@ -9,12 +9,14 @@
 // BF16 GEMM with FP32 accumulation of inner dimension K = terms · 2k then yields the FP32-accurate product
 // (terms = 6) or one with about 16 correct bits (terms = 3).
 //
-// The GEMM: one CTA per 128 x 256 tile of the real product (128 rows of C by 128 of its complex columns), four
-// warps. Warp 0's elected thread streams 64-wide K slices of both planes into a 4-stage shared-memory ring by TMA
-// (128-byte swizzle, one mbarrier per stage carrying the transaction bytes); warp 1's elected thread issues the
-// tcgen05.mma (kind::f16, BF16 inputs, M 128, N 256, K 16: four per slice) with the accumulator in tensor memory
-// (256 columns) and frees each stage through tcgen05.commit; after the last slice all four warps read their 32
-// tensor-memory lanes (tcgen05.ld 32x32b) and subtract the tile from C, a warp's 32 rows of one column being 256
+// The GEMM: one CTA per 128 x 256 tile of the real product (128 rows of C by 128 of its complex columns), ten
+// warps. Warp 8's elected thread streams 64-wide K slices of both planes into a 4-stage shared-memory ring by TMA
+// (128-byte swizzle, one mbarrier per stage carrying the transaction bytes); warp 9's elected thread issues the
+// tcgen05.mma (kind::f16, BF16 inputs, M 128, N 256, K 16: four per slice) and frees each stage through
+// tcgen05.commit. Every 4 slices the sum restarts in the other of two 256-column tensor-memory buffers, and warps
+// 0-7 add the finished buffer into FP32 registers (tcgen05.ld 32x32b, 128 sums a thread): the tensor core's own
+// accumulation then never runs over more than 256 of the inner dimension, which keeps the six-term product at
+// FP32's accuracy. At the end warps 0-7 subtract their sums from C, a warp's 32 rows of one column being 256
 // contiguous bytes. One tile per CTA (not persistent) so that the LU's high-priority panel factorizations get SMs as
 // tiles retire. Every wait is bounded in SM clocks; on timeout the CTA records ERR_TIMEOUT, waits (bounded) for its
 // own copies and products in flight, frees its tensor memory and exits.
@@ -33,9 +35,16 @@ namespace pq {
 
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4, THREADS = 128;
+constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
+constexpr int FOLD_WARPS = 8, PRODUCER_WARP = 8, MMA_WARP = 9, THREADS = 320;
+constexpr int FOLD_THREADS = FOLD_WARPS * 32;
 constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int TMEM_COLS = 256;
+// The accumulator is promoted to FP32 registers every CHUNK K slices (256 of the inner dimension): the tensor
+// core's own FP32 accumulation over a long inner dimension loses accuracy with every product it adds (measured: a
+// normwise error of 1.25e-6 over 24,576 terms against cuBLAS FP32's 1.6e-8), so each chunk starts a fresh sum in
+// one of two 256-column tensor-memory buffers while the fold warps add the previous chunk's into registers.
+constexpr int CHUNK = 4;
+constexpr int TMEM_COLS = 2 * BN;
 constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;   // ring, 1024-byte alignment slack, barriers
 constexpr int KPAD = 32;                                             // k padded to a multiple of 32 (K % 64 == 0)
 // limit of the waits for this CTA's own copies and products in flight before it exits (these complete on their
@@ -171,6 +180,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 __device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -202,8 +215,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
     uint64_t *empty = full + STAGES;
-    uint64_t *done = empty + STAGES;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    uint64_t *cfull = empty + STAGES;      // [2] a chunk's sum is complete in tensor-memory buffer b
+    uint64_t *cempty = cfull + 2;          // [2] the fold warps have read buffer b
+    uint64_t *drained = cempty + 2;        // every product issued has completed
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drained + 1);
     volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -216,20 +231,26 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
     const int gm = min(GROUP, args.tiles_m - first_m);
     const int m_tile = first_m + in_group % gm, n_tile = in_group / gm;
     const int64_t m0 = (int64_t)m_tile * BM;
+    const int kb_total = args.kblocks;
+    const int nchunks = (kb_total + CHUNK - 1) / CHUNK;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&cfull[b], 1);
+            mbar_init(&cempty[b], FOLD_THREADS);
+        }
+        mbar_init(drained, 1);
         *abort = 0;
         mbar_fence_init();
         tma_prefetch(&map_a);
         tma_prefetch(&map_b);
     }
     __syncwarp();
-    if (warp == 0) {
+    if (warp == PRODUCER_WARP) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
                      "r"(TMEM_COLS)
                      : "memory");
@@ -240,91 +261,127 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
     fence_after_sync();
     const uint32_t tmem = *tmem_slot;
     const uint32_t ring = smem_addr(smem);
-    const int kb_total = args.kblocks;
-    bool ok = true;
 
-    if (warp == 0 && lane == 0) {
-        // producer: slice kb into stage kb % STAGES once the MMA has released it
-        int issued_last[STAGES];
-        for (int s = 0; s < STAGES; ++s) issued_last[s] = -1;
-        for (int kb = 0; kb < kb_total && ok; ++kb) {
-            const int s = kb % STAGES;
-            const uint32_t parity = ((kb / STAGES) & 1) ^ 1;
-            if (!wait_bounded(&empty[s], parity, args.wait, abort)) {
-                ok = false;
-                break;
+    if (warp == PRODUCER_WARP) {
+        if (lane == 0) {
+            // producer: slice kb into stage kb % STAGES once the MMA has released it
+            bool ok = true;
+            int issued_last[STAGES];
+            for (int s = 0; s < STAGES; ++s) issued_last[s] = -1;
+            for (int kb = 0; kb < kb_total; ++kb) {
+                const int s = kb % STAGES;
+                if (!wait_bounded(&empty[s], ((kb / STAGES) & 1) ^ 1, args.wait, abort)) {
+                    ok = false;
+                    break;
+                }
+                mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+                const uint32_t a_dst = ring + s * STAGE_BYTES, b_dst = a_dst + A_BYTES;
+                tma_load_2d(a_dst, &map_a, kb * BK, (int)m0, smem_addr(&full[s]));
+                tma_load_2d(b_dst, &map_b, kb * BK, n_tile * BN, smem_addr(&full[s]));
+                issued_last[s] = kb;
             }
-            mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-            const uint32_t a_dst = ring + s * STAGE_BYTES, b_dst = a_dst + A_BYTES;
-            tma_load_2d(a_dst, &map_a, kb * BK, (int)m0, smem_addr(&full[s]));
-            tma_load_2d(b_dst, &map_b, kb * BK, n_tile * BN, smem_addr(&full[s]));
-            issued_last[s] = kb;
+            if (!ok) {
+                *abort = 1;
+                atomicExch(args.error, ERR_TIMEOUT);
+            }
+            // every copy issued has landed before the CTA may exit (already true when the MMA consumed them all)
+            for (int s = 0; s < STAGES; ++s)
+                if (issued_last[s] >= 0)
+                    wait_bounded(&full[s], (issued_last[s] / STAGES) & 1, DRAIN_CYCLES, nullptr);
         }
-        if (!ok) {
-            *abort = 1;
-            atomicExch(args.error, ERR_TIMEOUT);
+    } else if (warp == MMA_WARP) {
+        if (lane == 0) {
+            // MMA issuer: chunk c accumulates afresh in buffer c & 1 once the fold warps have read its last use
+            bool ok = true;
+            for (int kb = 0; kb < kb_total; ++kb) {
+                const int c = kb / CHUNK, buf = c & 1;
+                const bool first = kb % CHUNK == 0;
+                if (first) {
+                    if (!wait_bounded(&cempty[buf], ((c >> 1) & 1) ^ 1, args.wait, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after_sync();
+                }
+                const int s = kb % STAGES;
+                if (!wait_bounded(&full[s], (kb / STAGES) & 1, args.wait, abort)) {
+                    ok = false;
+                    break;
+                }
+                fence_after_sync();
+                const uint32_t a_base = ring + s * STAGE_BYTES, b_base = a_base + A_BYTES;
+                const uint32_t d = tmem + buf * BN;
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk)
+                    mma_bf16(d, sw128_desc(a_base + kk * 32), sw128_desc(b_base + kk * 32), !first || kk != 0);
+                mma_commit(smem_addr(&empty[s]));
+                if (kb % CHUNK == CHUNK - 1 || kb == kb_total - 1) mma_commit(smem_addr(&cfull[buf]));
+            }
+            if (!ok) {
+                *abort = 1;
+                atomicExch(args.error, ERR_TIMEOUT);
+            }
+            mma_commit(smem_addr(drained));       // after every product issued (also on the way out)
         }
-        // every copy issued has landed before the CTA may exit (already true when the MMA consumed them all)
-        for (int s = 0; s < STAGES; ++s)
-            if (issued_last[s] >= 0) wait_bounded(&full[s], (issued_last[s] / STAGES) & 1, DRAIN_CYCLES, nullptr);
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        for (int kb = 0; kb < kb_total; ++kb) {
-            const int s = kb % STAGES;
-            if (!wait_bounded(&full[s], (kb / STAGES) & 1, args.wait, abort)) {
-                ok = false;
+    } else {
+        // fold warps: warp w reads tensor-memory lanes (tile rows) 32 (w % 4) .. + 31, columns 128 (w / 4) .. + 127,
+        // and keeps their running FP32 sums in registers; then subtracts them from C, a warp's 32 rows of one
+        // column being 256 contiguous bytes
+        const int q = warp & 3, h = warp >> 2;
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + h * (BN / 2);
+        float acc[BN / 2];
+#pragma unroll
+        for (int i = 0; i < BN / 2; ++i) acc[i] = 0.f;
+        bool good = true;
+        for (int c = 0; c < nchunks; ++c) {
+            const int buf = c & 1;
+            const bool landed = wait_bounded(&cfull[buf], (c >> 1) & 1, args.wait, abort);
+            if (!__all_sync(0xffffffffu, landed)) {
+                good = false;
                 break;
             }
             fence_after_sync();
-            const uint32_t a_base = ring + s * STAGE_BYTES, b_base = a_base + A_BYTES;
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk)
-                mma_bf16(tmem, sw128_desc(a_base + kk * 32), sw128_desc(b_base + kk * 32), (kb | kk) != 0);
-            mma_commit(smem_addr(&empty[s]));
+            for (int j = 0; j < BN / 2 / 32; ++j) {
+                uint32_t r[32];
+                tmem_ld32(taddr + buf * BN + j * 32, r);
+#pragma unroll
+                for (int i = 0; i < 32; ++i) acc[j * 32 + i] += __uint_as_float(r[i]);
+            }
+            fence_before_sync();
+            mbar_arrive(&cempty[buf]);
         }
-        if (!ok) {
-            *abort = 1;
-            atomicExch(args.error, ERR_TIMEOUT);
-        }
-        mma_commit(smem_addr(done));          // after every product issued (also on the way out)
-    }
-    __syncwarp();
-    // epilogue: all four warps, warp w owning tensor-memory lanes (tile rows) 32w .. 32w + 31. The wait for `done`
-    // does not stop early on an abort: the products in flight must finish before the tensor memory is freed (the
-    // MMA thread commits `done` on every path, at the latest one wait limit after an abort).
-    const bool finished = wait_bounded(done, 0, args.wait + DRAIN_CYCLES, nullptr);
-    fence_after_sync();
-    const int go = __shfl_sync(0xffffffffu, (int)(finished && !*abort), 0);
-    if (go) {
-        const int64_t row = m0 + warp * 32 + lane;
-        const int64_t c0 = (int64_t)n_tile * (BN / 2);
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll 1
-        for (int ch = 0; ch < BN / 32; ++ch) {
-            uint32_t r[32];
-            tmem_ld32(taddr + ch * 32, r);
+        if (!good) {
+            if (lane == 0) {
+                *abort = 1;
+                atomicExch(args.error, ERR_TIMEOUT);
+            }
+        } else if (!*abort) {
+            const int64_t row = m0 + q * 32 + lane;
+            const int64_t c0 = (int64_t)n_tile * (BN / 2) + h * (BN / 4);
             if (row < args.rows) {
                 float2 *base = args.C + row;
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int64_t col = c0 + ch * 16 + j;
+                for (int j = 0; j < BN / 4; ++j) {
+                    const int64_t col = c0 + j;
                     if (col < args.cols) {
                         float2 *p = base + col * args.ldc;
                         float2 v = *p;
-                        v.x -= __uint_as_float(r[2 * j]);
-                        v.y -= __uint_as_float(r[2 * j + 1]);
+                        v.x -= acc[2 * j];
+                        v.y -= acc[2 * j + 1];
                         *p = v;
                     }
                 }
             }
         }
-    } else if (threadIdx.x == 0) {
-        *abort = 1;
-        atomicExch(args.error, ERR_TIMEOUT);
     }
     fence_before_sync();
     __syncthreads();
-    if (warp == 0) {
+    if (warp == PRODUCER_WARP) {
+        __syncwarp();
+        // the products in flight finish before the tensor memory is freed (at once on the normal path; after an
+        // abort the MMA thread committed `drained` behind its last product)
+        wait_bounded(drained, 0, args.wait + DRAIN_CYCLES, nullptr);
         __syncwarp();
         fence_after_sync();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");

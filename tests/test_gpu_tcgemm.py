@@ -8,7 +8,10 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {6: 2e-6, 3: 2e-4}     # six terms: FP32's level; three terms: about 2^-16 per product
+# normwise error bounds relative to |a| |b| + |c|: six terms at FP32's level (and within 5x cuBLAS's FP32 GEMM on the
+# same inputs: the tensor core's accumulation is restarted every 256 of the inner dimension and the chunks summed in
+# FP32 registers); three terms about 2^-16 per product (the dropped part products).
+TOL = {6: 2e-6, 3: 2e-4}
 
 
 def _update(lib, a, b, c, terms, wait=1 << 32):
@@ -54,7 +57,7 @@ def test_complex_update_matches_complex128(device_library, rows, cols, k, terms)
     print(f'update {rows}x{cols}x{k} terms {terms}: error {err:.3e} of |a||b| + |c|, cuBLAS FP32 {fp32:.3e}')
     assert err < TOL[terms], err
     if terms == 6:
-        assert err <= 10 * fp32 + 3e-7, (err, fp32)
+        assert err <= 5 * fp32 + 5e-8, (err, fp32)
     store[:cols, :rows] = guard[:cols, :rows]
     assert torch.equal(store, guard)               # nothing outside C written
 

@@ -75,3 +75,37 @@ def test_no_alloc_rejects_more_pairs_than_its_scratch(device_library):
             _lib.check(status, lib)
     finally:
         dg.close()
+
+
+def test_no_alloc_clears_flags_left_by_a_rejected_call(device_library):
+    """A call whose pairs hold an out-of-range triangle index, then one with an out-of-range kind (both made on the
+    host and caught by the kernels' own index checks), each return status 1 and leave the shared scratch's invalid
+    flag set; the valid call after them must clear it, return 0 and match pcbqs_gb300_pairs_device."""
+    import torch
+    from pcbqs_gb300 import _lib
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.geometry import DeviceGeometry, prepare
+    lib = device_library
+    b = Board.load('strip')
+    g = prepare(b.nodes, b.tris, b.z, 1)
+    dg = DeviceGeometry(g, 0)
+    try:
+        rng = np.random.default_rng(5)
+        p, q, d, kind = _pair_set(g, rng, 20_000)
+        bad_index, bad_kind = p.copy(), kind.copy()
+        bad_index[123] = len(g.tris)
+        bad_kind[4567] = 7
+        for arrays in ((bad_index, q, d, kind), (p, q, d, bad_kind)):
+            pt, qt, dt, kt = (torch.as_tensor(a, device='cuda') for a in arrays)
+            out = torch.zeros((len(pt), 6), dtype=torch.float64, device='cuda')
+            stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+            status = lib.pcbqs_gb300_pairs_no_alloc(dg.handle, pt.data_ptr(), qt.data_ptr(), dt.data_ptr(),
+                                                    kt.data_ptr(), len(pt), 0, out.data_ptr(), stream)
+            assert status == 1
+            with pytest.raises(ValueError, match='out of range'):
+                _lib.check(status, lib)
+        expected = _call(lib, 'pcbqs_gb300_pairs_device', dg.handle, (p, q, d, kind), False, 6)
+        got = _call(lib, 'pcbqs_gb300_pairs_no_alloc', dg.handle, (p, q, d, kind), False, 6)
+        assert got == pytest.approx(expected, rel=2e-10, abs=1e-26)
+    finally:
+        dg.close()
