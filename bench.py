@@ -49,14 +49,17 @@ def parse():
     p.add_argument('--board', default='planes')
     p.add_argument('--freq', type=float, default=1e6)
     p.add_argument('--precondition', default='lu32', choices=['lu32', 'block_jacobi'])
-    p.add_argument('--factor-math', default='bf16x9-blocked',
-                   choices=['fp32', 'bf16x9', 'bf16x9-blocked', 'fp32-blocked'],
-                   help='the lu32 factorization: cuSOLVER getrf or the blocked LU (-blocked), in FP32 or FP32 '
-                        'emulated on the tensor cores (bf16x9)')
+    p.add_argument('--factor-math', default='tc6-blocked',
+                   choices=['fp32', 'bf16x9', 'bf16x9-blocked', 'fp32-blocked', 'tc6-blocked', 'tc3-blocked'],
+                   help='the lu32 factorization: cuSOLVER getrf or the blocked LU (-blocked) with cuBLAS trailing GEMMs '
+                        'in FP32 or FP32 emulated on the tensor cores (bf16x9), or with this library\'s tcgen05 '
+                        'update on six (tc6, FP32 accuracy) or three (tc3) BF16 part products')
     p.add_argument('--mode', default='mixed', choices=['mixed', 'fp64'],
                    help='mixed: FP32 far pairs in local coordinates and FP32 inner Krylov products under FP64 '
                         'refinement; fp64: the FP64 fill and FP64 GMRES')
     p.add_argument('--no-comparator', action='store_true', help='skip the one-step FP64 comparator')
+    p.add_argument('--plain', action='store_true',
+                   help='also time, once, the plain FP64 path: FP64 fill and block-Jacobi GMRES to the same residual')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--sweep', type=int, default=0,
                    help='also time a sweep of this many log-spaced frequencies (1 kHz to 100 MHz), all ports')
@@ -167,22 +170,47 @@ def measured_peaks():
         return None
 
 
-def factor_roofline(model, lu_ms):
-    """The dominant stage: the blocked complex64 LU (8 n^3 / 3 flops) against the BF16x9 emulation's ceiling, the
-    measured sustained bf16 tensor rate / 9 (each FP32 product is nine BF16 products; the LU runs for most of a
-    second inside the step, so the sustained figure). Time: CUDA events around the LU on its stream, per step."""
+# DRAM bytes (read + written) per complex flop of the tcgen05 update, from an ncu capture of one six-term launch of
+# C (8192 x 8192) -= A (8192 x 2048) B (2048 x 8192): 7.400 GB read + 0.529 GB written for 1.100e12 complex flops
+TC_UPDATE_BYTES_PER_FLOP = (7.399611e9 + 0.529117e9) / (8.0 * 8192 * 8192 * 2048)
+
+
+def factor_roofline(model, timings, factor_math):
+    """The dominant stage's kernel. With the tcgen05 factor (tc3/tc6): this library's trailing update, its complex
+    flops (8 rows cols k per launch) over its CUDA-event time summed on the factorization's stream, against the
+    emulation's ceiling, the measured sustained BF16 tensor rate / terms (each complex-FP32 product is `terms` BF16
+    part products; the updates run for most of a second inside the step, so the sustained figure); the whole LU
+    (8 n^3 / 3 flops over its time) beside it. With cuBLAS's BF16x9 GEMMs: the LU against the bf16 rate / 9."""
     n = model.n
-    flops = 8 * n ** 3 / 3
+    lu_ms = statistics.median(t['factor_lu_ms'] for t in timings)
+    lu_flops = 8 * n ** 3 / 3
     peaks = measured_peaks()
     if peaks and peaks.get('bf16_tflops_sustained'):
-        bf16, source = float(peaks['bf16_tflops_sustained']), 'MEASURED_PEAKS.json bf16_tflops_sustained / 9'
+        bf16, source = float(peaks['bf16_tflops_sustained']), 'MEASURED_PEAKS.json bf16_tflops_sustained'
     else:
-        bf16, source = 1700.0, 'fallback sustained bf16 1,700 TFLOP/s / 9'
+        bf16, source = 1700.0, 'fallback sustained bf16 1,700 TFLOP/s'
+    if factor_math in ('tc6-blocked', 'tc3-blocked'):
+        terms = 6 if factor_math == 'tc6-blocked' else 3
+        t = timings[len(timings) // 2]
+        ms, flops, launches = t['factor_update_ms'], t['factor_update_flops'], t['factor_update_launches']
+        peak = bf16 / terms
+        achieved = flops / (ms / 1e3) / 1e12
+        per_launch = flops / max(launches, 1)
+        return dict(bound='tensor', kernel=f'k_tc_update (this library: tcgen05 BF16x{terms} complex trailing update, '
+                                           f'with its operand packing)',
+                    achieved=round(achieved, 2), peak=round(peak, 2), unit='TFLOP/s', frac=round(achieved / peak, 4),
+                    traffic=round(per_launch * TC_UPDATE_BYTES_PER_FLOP),
+                    traffic_source='ncu dram bytes of one six-term launch (8192^2 x 2048), scaled by flops per launch',
+                    flops_per_launch=per_launch, launches=launches, update_ms=round(ms, 2),
+                    bf16_part_product_tflops=round(achieved * terms, 1),
+                    peak_source=f'{source} / {terms} (of measured)',
+                    lu=dict(ms=round(lu_ms, 2), tflops=round(lu_flops / (lu_ms / 1e3) / 1e12, 2),
+                            update_share=round(ms / lu_ms, 3)))
     peak = bf16 / 9
-    achieved = flops / (lu_ms / 1e3) / 1e12
+    achieved = lu_flops / (lu_ms / 1e3) / 1e12
     return dict(bound='tensor', kernel='getrf_blocked (cuBLAS BF16x9 complex trailing GEMMs + cuSOLVER panels)',
                 achieved=round(achieved, 2), peak=round(peak, 2), unit='TFLOP/s', frac=round(achieved / peak, 4),
-                traffic=None, flops_per_launch=flops, lu_ms=round(lu_ms, 2), peak_source=source + ' (of measured)')
+                traffic=None, flops_per_launch=lu_flops, lu_ms=round(lu_ms, 2), peak_source=source + ' / 9 (of measured)')
 
 
 def gemm_peak(dtype):
@@ -616,12 +644,27 @@ def main():
                         for k in ('equilibrium_s', 'potential_solve_s', 'operator_setup_s', 'rhs_s', 'solve_s')},
                 gpu_launches=int(launches),
                 clocks=clock_info,
-                roofline=(factor_roofline(model, statistics.median(t['factor_lu_ms'] for t in timings))
+                roofline=(factor_roofline(model, timings, args.factor_math)
                           if args.precondition == 'lu32' else fill_roofline(model, head_fill_ms, mixed, peaks)),
                 fill_roofline=fill_roofline(model, head_fill_ms, mixed, peaks),
                 e2e=dict(value=round(e2e_s, 4), unit='s/freq', runs_s=[round(v, 4) for v in e2e_runs],
                          h2d_bytes_per_step=int(h2d),
                          d2h_bytes_per_step=int(d2h)))
+    if args.plain:
+        # the plain FP64 GPU path of the same step (FP64 fill, FP64 operator, block-Jacobi GMRES), timed once
+        model.assemble(mixed=False)
+        torch.cuda.synchronize()
+        p0 = time.perf_counter()
+        try:
+            rp = model.solve([freq], precondition='block_jacobi', mixed=False)
+            plain = dict(s_per_freq=round(time.perf_counter() - p0, 3), gmres_iterations=rp.iterations.tolist(),
+                         max_residual=float(rp.residual.max()))
+            if z_err_ref is not None:
+                plain['port_z_max_rel_err_vs_reference'] = float(np.abs(rp.impedance[0] - Zr).max() / np.abs(Zr).max())
+        except RuntimeError as exc:
+            plain = dict(s_per_freq=round(time.perf_counter() - p0, 3), error=str(exc)[:200])
+        plain['speedup_of_headline'] = round(plain['s_per_freq'] / value, 2)
+        line['plain_fp64_block_jacobi'] = plain
     if args.sweep:
         # the batched sweep: every (frequency, port) column, `anchors` shared factors, one batched GMRES per run
         fs = np.geomspace(1e3, 1e8, args.sweep)

@@ -262,6 +262,11 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, in
  * assembly (with K^T L K and T^T P T when first formed) and the LU itself. No counterpart in the reference (its
  * factor is LAPACK on the host); for the roofline of the factorization. */
 int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *op, double *assemble_ms, double *getrf_ms);
+/* The tcgen05 trailing updates of the last pcbqs_gb300_peec_factor with math 4 or 5: their summed CUDA-event time
+ * (ms, on the factorization's stream), complex flops (8 rows cols k each) and count; zeros after any other math.
+ * No counterpart in the reference; for the roofline of the update kernel. */
+int pcbqs_gb300_peec_factor_updates(const pcbqs_gb300_peec *op, double *update_ms, double *update_flops,
+                                    int32_t *launches);
 /* Dense complex64 LU with partial pivoting of the n x n column-major device matrix a (leading dimension n), in
  * place, ipiv (device, n) receiving 1-based pivot rows: cusolverDnCgetrf's layout and pivots, so getrs and this
  * library's triangular solvers apply to it. Blocked: `block`-column panels (32 .. 4096) factored on a second stream

@@ -157,6 +157,7 @@ struct Resources {
     cusolverDnHandle_t solver = nullptr;
     cudaStream_t panel = nullptr;
     cudaEvent_t ready = nullptr, next = nullptr;
+    std::vector<cudaEvent_t> marks;          // around each tcgen05 update (when timed)
     float2 *work = nullptr, *product = nullptr;
     uint8_t *planes = nullptr;
     int *plan = nullptr, *info = nullptr;
@@ -173,19 +174,22 @@ struct Resources {
         if (solver) cusolverDnDestroy(solver);
         if (ready) cudaEventDestroy(ready);
         if (next) cudaEventDestroy(next);
+        for (cudaEvent_t e : marks) cudaEventDestroy(e);
         if (panel) cudaStreamDestroy(panel);
     }
 };
 
 }  // namespace
 
-cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular) {
+cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular,
+                          LuUpdateStats *stats) {
     *singular = 0;
     if (n <= 0 || n > (int64_t)0x7fffffff || !A || !ipiv || block < 32 || block > MAX_BLOCK ||
         (math != LU_GEMM_FP32 && math != LU_GEMM_BF16X9 && math != LU_GEMM_TC3 && math != LU_GEMM_TC6))
         return cudaErrorInvalidValue;
     const bool tc = math == LU_GEMM_TC3 || math == LU_GEMM_TC6;
     const int terms = math == LU_GEMM_TC3 ? 3 : 6;
+    if (stats) *stats = LuUpdateStats{};
     const int nb = (int)std::min<int64_t>(block, n);
     const int64_t steps = (n + nb - 1) / nb;
     Resources r;
@@ -248,9 +252,21 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
     auto gemm = [&](int64_t rows, int64_t cols, int k, const float2 *a, const float2 *b, float2 *c,
                     bool a_packed) -> bool {
         if (rows <= 0 || cols <= 0) return true;
-        if (tc)
-            return tc_update_c64(rows, cols, k, a, n, b, n, c, n, terms, r.planes, a_packed, tc_error,
-                                 wait_cycles(), stream) == cudaSuccess;
+        if (tc) {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (stats && (cudaEventCreate(&e0) || cudaEventCreate(&e1) || cudaEventRecord(e0, stream))) return false;
+            if (tc_update_c64(rows, cols, k, a, n, b, n, c, n, terms, r.planes, a_packed, tc_error, wait_cycles(),
+                              stream) != cudaSuccess)
+                return false;
+            if (stats) {
+                if (cudaEventRecord(e1, stream)) return false;
+                r.marks.push_back(e0);
+                r.marks.push_back(e1);
+                stats->flops += 8.0 * (double)rows * (double)cols * (double)k;
+                ++stats->launches;
+            }
+            return true;
+        }
         if (rows > trail || cols > trail) return false;
         if (cublasGemmEx(r.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)rows, (int)cols, k, &one, a, CUDA_C_32F, (int)n, b,
                          CUDA_C_32F, (int)n, &zero, r.product, CUDA_C_32F, (int)rows, compute, CUBLAS_GEMM_DEFAULT) !=
@@ -303,6 +319,11 @@ cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, 
         return e;
     if (flags[1]) return cudaErrorLaunchTimeout;
     if (flags[0]) return cudaErrorIllegalState;
+    if (stats)
+        for (size_t i = 0; i + 1 < r.marks.size(); i += 2) {
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, r.marks[i], r.marks[i + 1]) == cudaSuccess) stats->ms += ms;
+        }
     for (int64_t t = 0; t < steps; ++t)
         if (info[t] > 0) {
             *singular = (int)(t * nb + info[t]);

@@ -27,7 +27,15 @@ constexpr int MAX_BLOCK_PUBLIC = 4096;   // widest panel the blocked factorizati
 // fused (LU_GEMM_TC3, LU_GEMM_TC6: tc_update_c64, the panel's BF16 planes packed once per step). Returns
 // cudaSuccess, or an error (cudaErrorLaunchTimeout: a bounded wait of the tcgen05 update gave up); *singular = the
 // first zero pivot's 1-based index (0 if none). Ordered on `stream`; returns after the factor is complete.
-cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular);
+// The trailing updates of the last tcgen05 factorization: their summed CUDA-event time on the main stream, their
+// complex flops (8 rows cols k each) and how many there were.
+struct LuUpdateStats {
+    double ms = 0, flops = 0;
+    int launches = 0;
+};
+
+cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular,
+                          LuUpdateStats *stats = nullptr);
 
 // Factors the n x n column-major symmetric positive definite FP32 matrix A (leading dimension lda >= n, best a
 // multiple of 32 so that the GEMMs take their aligned forms; the lower triangle is read) in place as A = L L^T,

@@ -919,6 +919,7 @@ struct pcbqs_gb300_peec {
     double *klk = nullptr, *tpt = nullptr;   // dense K^T L K and T^T P T (n x n), made once for the factors
     double *tpt_im = nullptr;                // T^T P_im T when P is complex
     float assemble_ms = 0, getrf_ms = 0;     // CUDA-event times of the last factorization's two stages
+    LuUpdateStats updates;                   // its tcgen05 trailing updates (math 4, 5)
     ~pcbqs_gb300_peec() {
         delete bj;
         delete lu;
@@ -1149,7 +1150,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     if (math >= 2) {
         int singular = 0;
         const int gemm = math == 2 ? LU_GEMM_BF16X9 : math == 3 ? LU_GEMM_FP32 : math == 4 ? LU_GEMM_TC3 : LU_GEMM_TC6;
-        e = getrf_blocked(n, lu->lu, lu->ipiv, LU_BLOCK, gemm, st, &singular);
+        e = getrf_blocked(n, lu->lu, lu->ipiv, LU_BLOCK, gemm, st, &singular, &h->updates);
         cudaEventRecord(t.ev[2], st);
         if (e || singular) {
             delete lu;
@@ -1207,6 +1208,16 @@ int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *h, double *assemble_ms
     if (!h->lu) return pfail(ERR_ARGUMENT, "peec_factor_times: no factor set up");
     *assemble_ms = h->assemble_ms;
     *getrf_ms = h->getrf_ms;
+    return OK;
+}
+
+int pcbqs_gb300_peec_factor_updates(const pcbqs_gb300_peec *h, double *update_ms, double *update_flops,
+                                    int32_t *launches) {
+    if (!h || !update_ms || !update_flops || !launches)
+        return pfail(ERR_ARGUMENT, "peec_factor_updates: invalid argument");
+    *update_ms = h->updates.ms;
+    *update_flops = h->updates.flops;
+    *launches = h->updates.launches;
     return OK;
 }
 

@@ -510,16 +510,18 @@ class PeecModel(PeecTopology):
     FACTOR_MATH = {'fp32': 0, 'bf16x9': 1, 'bf16x9-blocked': 2, 'fp32-blocked': 3, 'tc3-blocked': 4,
                    'tc6-blocked': 5}
 
-    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='bf16x9-blocked', anchors=None):
+    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='tc6-blocked', anchors=None):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
 
         precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
         dense loop/tree system), or 'none'. mixed=False: FP64 GMRES on the FP64 operator; mixed=True: FP64
         iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose dense products run
         in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of the 'lu32'
-        factorization: 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy) through cuSOLVER's getrf,
-        'fp32-blocked' or 'bf16x9-blocked' through this library's blocked LU (2048-column panels factored ahead of
-        the trailing GEMMs). anchors ('lu32'
+        factorization: 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy) through cuSOLVER's getrf;
+        through this library's blocked LU (2048-column panels factored ahead of the trailing updates) 'fp32-blocked'
+        or 'bf16x9-blocked' with cuBLAS trailing GEMMs, or 'tc6-blocked' (the default) / 'tc3-blocked' with this
+        library's tcgen05 update on six / three BF16 part products (six: FP32's accuracy; three: about 16 bits, a
+        weaker preconditioner that costs GMRES steps). anchors ('lu32'
         only): how many factorizations a sweep shares; the frequencies, in increasing order, are split into that
         many runs and every run is solved as one batch of (frequency, port) columns preconditioned by the factor
         at its middle frequency (default: one factor per frequency). Every column still reaches the tolerance of
@@ -554,6 +556,7 @@ class PeecModel(PeecTopology):
         timed = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         precondition_ms = gmres_ms = 0.0
         stage_ms = np.zeros(2)             # the factorizations' assembly and LU times
+        updates = np.zeros(3)              # their tcgen05 trailing updates: ms, complex flops, launches
         outer_total = 0
         factored = None
 
@@ -561,6 +564,10 @@ class PeecModel(PeecTopology):
             a, b = ctypes.c_double(), ctypes.c_double()
             _lib.check(lib.pcbqs_gb300_peec_factor_times(handle, ctypes.byref(a), ctypes.byref(b)), lib)
             stage_ms[:] += (a.value, b.value)
+            c = ctypes.c_int32()
+            _lib.check(lib.pcbqs_gb300_peec_factor_updates(handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+                       lib)
+            updates[:] += (a.value, b.value, c.value)
         try:
             t1 = time.perf_counter()
             if mode == 2:
@@ -672,7 +679,8 @@ class PeecModel(PeecTopology):
                 its[sel], res[sel] = its_g, res_g
             self.timings.update(precondition_ms=precondition_ms, gmres_ms=gmres_ms, gmres_iterations=its.tolist(),
                                 factorizations=len(groups) if mode == 2 else 0, factor_assemble_ms=stage_ms[0],
-                                factor_lu_ms=stage_ms[1])
+                                factor_lu_ms=stage_ms[1], factor_update_ms=updates[0],
+                                factor_update_flops=updates[1], factor_update_launches=int(updates[2]))
             if mixed:
                 self.timings['outer_steps'] = outer_total
             X = x_all.cpu().numpy()
