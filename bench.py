@@ -64,6 +64,7 @@ def parse():
     p.add_argument('--sweep', type=int, default=0,
                    help='also time a sweep of this many log-spaced frequencies (1 kHz to 100 MHz), all ports')
     p.add_argument('--anchors', type=int, default=8, help='complex64 factors shared across the sweep')
+    p.add_argument('--sweep-board', default='planes16', help='the sweep\'s board (default: the 16-port plane pair)')
     p.add_argument('--case', default=None,
                    help='time one kernel case small enough for a full ncu capture instead of the benchmark: '
                         'fill:BOARD[:TRIANGLES] | lu:BOARD[:K...] | dense:N[:K] | getrf:N[:BLOCK[:MATH...]] | '
@@ -650,6 +651,7 @@ def main():
                 e2e=dict(value=round(e2e_s, 4), unit='s/freq', runs_s=[round(v, 4) for v in e2e_runs],
                          h2d_bytes_per_step=int(h2d),
                          d2h_bytes_per_step=int(d2h)))
+    head_n = model.n
     if args.plain:
         # the plain FP64 GPU path of the same step (FP64 fill, FP64 operator, block-Jacobi GMRES), timed once
         model.assemble(mixed=False)
@@ -666,18 +668,35 @@ def main():
         plain['speedup_of_headline'] = round(plain['s_per_freq'] / value, 2)
         line['plain_fp64_block_jacobi'] = plain
     if args.sweep:
-        # the batched sweep: every (frequency, port) column, `anchors` shared factors, one batched GMRES per run
+        # the batched sweep (config C3): every (frequency, port) column of the sweep board, `anchors` shared factors,
+        # one batched GMRES per run of frequencies, each restart cycle one CUDA graph launch
         fs = np.geomspace(1e3, 1e8, args.sweep)
+        if args.sweep_board != args.board:
+            del model
+            torch.cuda.empty_cache()
+            model = PeecModel(Board.load(args.sweep_board), device=local)
         model.assemble(mixed=mixed)
         torch.cuda.synchronize()
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record()
         rs = model.solve(fs, precondition='lu32', mixed=mixed, factor_math=args.factor_math,
-                         anchors=min(args.anchors, args.sweep))
+                         anchors=min(args.anchors, args.sweep), captured=True)
         s1.record()
         torch.cuda.synchronize()
         its = rs.iterations.reshape(len(fs), -1)
-        line['sweep'] = dict(frequencies=len(fs), range_hz=[1e3, 1e8], ports=len(model.names),
+        sweep_err = None
+        golden = ROOT / 'tests' / 'golden' / f'peec_{args.sweep_board}.npz'
+        if golden.exists():
+            with np.load(golden) as ref:
+                errs = []
+                for f, Zr in zip(ref['freqs'], ref['Z']):
+                    fi = int(np.argmin(np.abs(fs - f)))
+                    if abs(fs[fi] / f - 1) < 1e-9:
+                        errs.append([float(f), float(np.abs(rs.impedance[fi] - Zr).max() / np.abs(Zr).max())])
+                sweep_err = errs or None
+        line['sweep'] = dict(board=args.sweep_board, unknowns=model.n, captured_cycles=True,
+                             port_z_max_rel_err_vs_reference=sweep_err,
+                             frequencies=len(fs), range_hz=[1e3, 1e8], ports=len(model.names),
                              columns=int(its.size), anchors=rs.timings['factorizations'],
                              s_total=round(s0.elapsed_time(s1) / 1e3, 3),
                              s_per_freq=round(s0.elapsed_time(s1) / 1e3 / len(fs), 4),
@@ -686,7 +705,7 @@ def main():
                              iterations_per_frequency_max=its.max(axis=1).tolist(),
                              max_residual=float(rs.residual.max()))
     if not args.no_cpu_baseline:
-        v, details = cpu_sample(args.board, model.n)
+        v, details = cpu_sample(args.board, head_n)
         line['cpu_baseline'] = dict(value=round(v, 3), unit='s/freq', cores=details['cores'], kind='port',
                                     sample=f'oracle fill+combine+aggregation in full; dense solve = complex64 LU '
                                            f'estimated from a bounded sample (--impl reference runs it in full); '

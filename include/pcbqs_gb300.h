@@ -262,6 +262,13 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, in
  * assembly (with K^T L K and T^T P T when first formed) and the LU itself. No counterpart in the reference (its
  * factor is LAPACK on the host); for the roofline of the factorization. */
 int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *op, double *assemble_ms, double *getrf_ms);
+/* captured = 1: the GMRES of pcbqs_gb300_peec_gmres and of pcbqs_gb300_peec_solve_mixed (its inner solves) runs each
+ * restart cycle as one CUDA graph launch: the Arnoldi steps in a conditional WHILE node whose condition a device
+ * kernel sets (a column still active, steps left), each column's convergence mask on the device, no host
+ * synchronization between steps; the graph is captured once per active-set size. The same kernels in the same
+ * order as captured = 0 (the default: one host check per step), so the same results. The reference's batched
+ * counterpart is mqs_iterative._lockstep_gmres (src/pcbqs/mqs_iterative.py:109-170), a host loop per step. */
+int pcbqs_gb300_peec_set_captured(pcbqs_gb300_peec *op, int captured);
 /* The tcgen05 trailing updates of the last pcbqs_gb300_peec_factor with math 4 or 5: their summed CUDA-event time
  * (ms, on the factorization's stream), complex flops (8 rows cols k each) and count; zeros after any other math.
  * No counterpart in the reference; for the roofline of the update kernel. */

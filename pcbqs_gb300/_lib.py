@@ -119,6 +119,7 @@ PROTOTYPES = {
                                                  c_void_p]),
     'pcbqs_gb300_peec_factor_times': (ctypes.c_int, [c_void_p, ctypes.POINTER(ctypes.c_double),
                                                      ctypes.POINTER(ctypes.c_double)]),
+    'pcbqs_gb300_peec_set_captured': (ctypes.c_int, [c_void_p, ctypes.c_int]),
     'pcbqs_gb300_peec_factor_updates': (ctypes.c_int, [c_void_p, ctypes.POINTER(ctypes.c_double),
                                                        ctypes.POINTER(ctypes.c_double), c_int32_p]),
     'pcbqs_gb300_via_inductance': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_double, c_void_p,

@@ -255,6 +255,171 @@ __global__ void k_combine(int64_t n, int k, int jc, const cd *V, const cd *y, cd
     }
 }
 
+// ---- the captured cycle: the same steps with the step index in device memory ------------------------------------
+// state[0] = j, the step about to run; state[1] = the cycle's step limit (set before each launch); state[2] = the
+// last step run. A conditional WHILE node repeats the step body while k_step_end leaves its condition at 1.
+
+__global__ void k_state_init(int *state) {
+    state[0] = 0;
+    state[2] = 0;
+}
+
+__global__ void k_copy_basis(int64_t n, int k, const cd *V, const int *state, cd *out) {
+    const int64_t total = n * k;
+    const cd *Vj = V + (size_t)state[0] * total;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x)
+        out[idx] = Vj[idx];
+}
+
+// k_dots_partial with i < jc = j + 1 (grid NCHUNK x (m + 1): blocks past jc return), partials laid out with a fixed
+// stride of m + 1 rows.
+__global__ void __launch_bounds__(RT) k_dots_partial_d(int64_t n, int k, const cd *V, const cd *w, cd *partial,
+                                                       const int *state) {
+    __shared__ cd acc[RT];
+    const int chunk = blockIdx.x, i = blockIdx.y;
+    if (i > state[0]) return;
+    const int64_t r0 = n * chunk / NCHUNK, r1 = n * (chunk + 1) / NCHUNK;
+    const cd *Vi = V + (size_t)i * n * k;
+    cd *out = partial + ((size_t)chunk * gridDim.y + i) * k;
+    if (k <= RT) {
+        const int per = RT / k, t = threadIdx.x;
+        cd a = make_double2(0, 0);
+        if (t < per * k) {
+            const int s = t % k, rr = t / k;
+            for (int64_t r = r0 + rr; r < r1; r += per) a = cadd(a, cmulc(Vi[r * k + s], w[r * k + s]));
+        }
+        acc[t] = a;
+        __syncthreads();
+        if (t < k) {
+            cd sum = make_double2(0, 0);
+            for (int q = 0; q < per; ++q) sum = cadd(sum, acc[t + q * k]);
+            out[t] = sum;
+        }
+    } else {
+        for (int s = threadIdx.x; s < k; s += RT) {
+            cd a = make_double2(0, 0);
+            for (int64_t r = r0; r < r1; ++r) a = cadd(a, cmulc(Vi[r * k + s], w[r * k + s]));
+            out[s] = a;
+        }
+    }
+}
+
+__global__ void k_dots_final_d(int stride, int k, const cd *partial, cd *h, const int *state) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (state[0] + 1) * k) return;
+    cd sum = make_double2(0, 0);
+    for (int c = 0; c < NCHUNK; ++c) sum = cadd(sum, partial[(size_t)c * stride * k + idx]);
+    h[idx] = sum;
+}
+
+__global__ void k_orth_update_d(int64_t n, int k, const cd *V, const cd *h, cd *w, const int *state) {
+    const int jc = state[0] + 1;
+    const int64_t total = n * k;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(idx % k);
+        cd a = w[idx];
+        for (int i = 0; i < jc; ++i) a = csub(a, cmul(V[(size_t)i * total + idx], h[i * k + s]));
+        w[idx] = a;
+    }
+}
+
+// V_{j+1} = w / |w|
+__global__ void k_divide_next(int64_t n, int k, const cd *in, const double *norm, cd *V, const int *state) {
+    const int64_t total = n * k;
+    cd *out = V + (size_t)(state[0] + 1) * total;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const double d = norm[idx % k];
+        const double inv = d > 0 ? 1.0 / d : 1.0;
+        out[idx] = make_double2(in[idx].x * inv, in[idx].y * inv);
+    }
+}
+
+__global__ void k_store_column_d(int m, int k, const cd *h1, const cd *h2, const double *hn, cd *H,
+                                 const int *state) {
+    const int j = state[0];
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < (j + 1) * k) {
+        const int i = idx / k, s = idx % k;
+        H[((size_t)i * m + j) * k + s] = cadd(h1[idx], h2[idx]);
+    }
+    if (idx < k) H[((size_t)(j + 1) * m + j) * k + idx] = make_double2(hn[idx], 0);
+}
+
+__global__ void k_givens_d(int m, int k, cd *H, cd *cs, cd *sn, cd *g, const double *bnorm, double tol, int *done,
+                           int *last, int *its, int *ndone, const int *state) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= k) return;
+    const int j = state[0];
+    auto at = [&](int i) -> cd & { return H[((size_t)i * m + j) * k + s]; };
+    for (int i = 0; i < j; ++i) {
+        const cd a = at(i), b = at(i + 1), c = cs[i * k + s], sv = sn[i * k + s];
+        at(i) = cadd(cmulc(c, a), cmulc(sv, b));
+        at(i + 1) = csub(cmul(c, b), cmul(sv, a));
+    }
+    const cd a = at(j), b = at(j + 1);
+    double den = sqrt(a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y);
+    if (!(den > 0)) den = 1;
+    const cd c = make_double2(a.x / den, a.y / den), sv = make_double2(b.x / den, b.y / den);
+    cs[j * k + s] = c;
+    sn[j * k + s] = sv;
+    at(j) = cadd(cmulc(c, a), cmulc(sv, b));
+    at(j + 1) = make_double2(0, 0);
+    const cd gj = g[j * k + s];
+    const cd gn = cmul(sv, gj);
+    g[(j + 1) * k + s] = make_double2(-gn.x, -gn.y);
+    g[j * k + s] = cmulc(c, gj);
+    const bool was = done[s] != 0;
+    const double res = sqrt(gn.x * gn.x + gn.y * gn.y) / bnorm[s];
+    const bool now = !was && res <= tol;
+    if (now) {
+        last[s] = j;
+        done[s] = 1;
+    }
+    if (!was) its[s] += 1;
+    if (done[s]) atomicAdd(ndone, 1);
+}
+
+// End of a step: advance j and leave the WHILE condition at 1 while a column is active and steps remain.
+__global__ void k_step_end(int *state, const int *ndone, int k, cudaGraphConditionalHandle handle) {
+    if (threadIdx.x || blockIdx.x) return;
+    const int j = state[0] + 1;
+    state[0] = j;
+    state[2] = j - 1;
+    cudaGraphSetConditional(handle, (*ndone < k && j < state[1]) ? 1u : 0u);
+}
+
+__global__ void k_trisolve_d(int m, int k, const cd *H, const cd *g, const int *done, const int *last, cd *y,
+                             const int *state) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= k) return;
+    const int jcur = state[2];
+    const int jj = done[s] ? last[s] + 1 : jcur + 1;
+    for (int i = m - 1; i >= jj; --i) y[i * k + s] = make_double2(0, 0);
+    for (int i = jj - 1; i >= 0; --i) {
+        cd acc = g[i * k + s];
+        for (int l = i + 1; l < jj; ++l) acc = csub(acc, cmul(H[((size_t)i * m + l) * k + s], y[l * k + s]));
+        const cd d = H[((size_t)i * m + i) * k + s];
+        const double dd = d.x * d.x + d.y * d.y;
+        y[i * k + s] = dd > 0 ? make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd)
+                              : make_double2(0, 0);
+    }
+}
+
+__global__ void k_combine_d(int64_t n, int k, const cd *V, const cd *y, cd *out, const int *state) {
+    const int jc = state[2] + 1;
+    const int64_t total = n * k;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(idx % k);
+        cd a = make_double2(0, 0);
+        for (int i = 0; i < jc; ++i) a = cadd(a, cmul(V[(size_t)i * total + idx], y[i * k + s]));
+        out[idx] = a;
+    }
+}
+
 // ---------------------------------------------------------------------------------------------------------------
 
 static int grid_for(int64_t total) {
@@ -306,6 +471,129 @@ cudaError_t subtract_from(int64_t count, const cd *b, cd *a, cudaStream_t s) {
 
 namespace {
 
+// The captured restart cycle: its graph (rebuilt when the active set's size changes) and the buffers it runs on.
+struct CycleGraph {
+    int ka = -1;
+    int kernels = 0;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t capture[2] = {nullptr, nullptr};
+    ~CycleGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (cudaStream_t s : capture)
+            if (s) cudaStreamDestroy(s);
+    }
+};
+
+struct CycleBuffers {
+    int64_t n;
+    int k, ka, m;
+    double tol;
+    cd *V, *r;
+    double *norm;
+    cd *H, *cs, *sn, *g, *y, *h1, *h2, *dpart;
+    double *npart;
+    cd *w, *z, *vj, *xc, *x;
+    double *bnorm;
+    int *done, *last, *its, *ndone, *act_dev, *sys_dev, *state;
+};
+
+int grid_of_total(int64_t total) { return (int)std::min<int64_t>(std::max<int64_t>((total + 255) / 256, 1), 4096); }
+
+// Capture one restart cycle on its own streams: the start (V0 = r / |r|, the least-squares state), a conditional
+// WHILE node whose body is one Arnoldi step read from and counted in device memory, and the update x += M^-1 V y
+// with the active columns scattered back. Same kernels and order as the host-driven cycle, so the same result.
+cudaError_t build_cycle_graph(Operator &A, Preconditioner *M, const CycleBuffers &b, CycleGraph &graph) {
+    cudaError_t e;
+    for (cudaStream_t &s : graph.capture)
+        if (!s && (e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking))) return e;
+    if (graph.exec) {
+        cudaGraphExecDestroy(graph.exec);
+        graph.exec = nullptr;
+    }
+    graph.ka = -1;
+    cudaStream_t s0 = graph.capture[0], s1 = graph.capture[1];
+    const int64_t n = b.n;
+    const int ka = b.ka, m = b.m;
+    const int gsz = grid_of_total(n * ka);
+    int kernels = 0;
+    auto precond = [&](const cd *in, cd *out, cudaStream_t s) -> cudaError_t {
+        if (M) return M->apply_deferred(ka, b.sys_dev, in, out, s);
+        return cudaMemcpyAsync(out, in, sizeof(cd) * n * ka, cudaMemcpyDeviceToDevice, s);
+    };
+    cudaGraph_t whole = nullptr;
+    auto abandon = [&](cudaError_t err) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(s1, &g);
+        if (g) cudaGraphDestroy(g);
+        g = nullptr;
+        cudaStreamEndCapture(s0, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return err;
+    };
+    if ((e = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal))) return e;
+    k_divide<<<gsz, 256, 0, s0>>>(n, ka, b.r, b.norm, b.V);
+    k_cycle_start<<<grid_of_total((int64_t)(m + 1) * m * ka), 256, 0, s0>>>(m, ka, b.norm, b.H, b.g, b.done, b.last);
+    if ((e = cudaMemsetAsync(b.its, 0, sizeof(int) * ka, s0))) return abandon(e);
+    k_state_init<<<1, 1, 0, s0>>>(b.state);
+    kernels += 3;
+    cudaStreamCaptureStatus status;
+    cudaGraph_t captured = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edges = nullptr;
+    size_t ndeps = 0;
+    if ((e = cudaStreamGetCaptureInfo(s0, &status, nullptr, &captured, &deps, &edges, &ndeps))) return abandon(e);
+    cudaGraphConditionalHandle handle;
+    if ((e = cudaGraphConditionalHandleCreate(&handle, captured, 1, cudaGraphCondAssignDefault))) return abandon(e);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop;
+    if ((e = cudaGraphAddNode(&loop, captured, deps, edges, ndeps, &cp)) ||
+        (e = cudaStreamUpdateCaptureDependencies(s0, &loop, nullptr, 1, cudaStreamSetCaptureDependencies)))
+        return abandon(e);
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((e = cudaStreamBeginCaptureToGraph(s1, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)))
+        return abandon(e);
+    {
+        // one Arnoldi step (the host-driven cycle's loop body)
+        k_copy_basis<<<gsz, 256, 0, s1>>>(n, ka, b.V, b.state, b.vj);
+        if ((e = precond(b.vj, b.z, s1)) || (e = A.apply(ka, b.sys_dev, b.z, b.w, s1))) return abandon(e);
+        const dim3 dgrid(NCHUNK, m + 1);
+        const int hgrid = ((m + 1) * ka + 127) / 128;
+        for (cd *h : {b.h1, b.h2}) {
+            k_dots_partial_d<<<dgrid, RT, 0, s1>>>(n, ka, b.V, b.w, b.dpart, b.state);
+            k_dots_final_d<<<hgrid, 128, 0, s1>>>(m + 1, ka, b.dpart, h, b.state);
+            k_orth_update_d<<<gsz, 256, 0, s1>>>(n, ka, b.V, h, b.w, b.state);
+        }
+        if ((e = column_norms(n, ka, b.w, b.norm, b.npart, s1))) return abandon(e);
+        k_divide_next<<<gsz, 256, 0, s1>>>(n, ka, b.w, b.norm, b.V, b.state);
+        k_store_column_d<<<hgrid, 128, 0, s1>>>(m, ka, b.h1, b.h2, b.norm, b.H, b.state);
+        if ((e = cudaMemsetAsync(b.ndone, 0, sizeof(int), s1))) return abandon(e);
+        k_givens_d<<<(ka + 127) / 128, 128, 0, s1>>>(m, ka, b.H, b.cs, b.sn, b.g, b.bnorm, b.tol, b.done, b.last,
+                                                     b.its, b.ndone, b.state);
+        k_step_end<<<1, 32, 0, s1>>>(b.state, b.ndone, ka, handle);
+        kernels += 13;
+    }
+    if ((e = cudaStreamEndCapture(s1, &body))) return abandon(e);
+    // x += M^-1 (V y), the active columns back into x
+    k_trisolve_d<<<(ka + 127) / 128, 128, 0, s0>>>(m, ka, b.H, b.g, b.done, b.last, b.y, b.state);
+    k_combine_d<<<gsz, 256, 0, s0>>>(n, ka, b.V, b.y, b.w, b.state);
+    if ((e = precond(b.w, b.z, s0))) return abandon(e);
+    k_add<<<gsz, 256, 0, s0>>>((int64_t)n * ka, b.z, b.xc);
+    k_scatter_cols<<<gsz, 256, 0, s0>>>(n, b.k, ka, b.act_dev, b.xc, b.x);
+    kernels += 4;
+    if ((e = cudaStreamEndCapture(s0, &whole))) return abandon(e);
+    e = cudaGraphInstantiate(&graph.exec, whole, 0);
+    cudaGraphDestroy(whole);
+    if (e) return e;
+    graph.ka = ka;
+    graph.kernels = kernels;
+    return cudaGetLastError();
+}
+
 struct Scratch {
     cudaStream_t stream;
     std::vector<void *> blocks;
@@ -345,7 +633,10 @@ cudaError_t gmres_batched(Operator &A, Preconditioner *M, int k, const int32_t *
     double *bnorm = mem.get<double>(k);
     int *done = mem.get<int>(k), *last = mem.get<int>(k), *its = mem.get<int>(k), *ndone = mem.get<int>(1);
     int *act_dev = mem.get<int>(k), *sys_dev = mem.get<int>(k);
+    cd *vj = opt.captured ? mem.get<cd>(nk) : nullptr;           // the basis vector a captured step works on
+    int *state = opt.captured ? mem.get<int>(4) : nullptr;       // the captured cycle's step counters
     if (mem.err != cudaSuccess) return mem.err;
+    CycleGraph graph;
     int launches = 0;
     auto apply = [&](int ka, const cd *in, cd *out) { return A.apply(ka, sys_dev, in, out, st); };
     auto precond = [&](int ka, const cd *in, cd *out) -> cudaError_t {
@@ -421,6 +712,26 @@ cudaError_t gmres_batched(Operator &A, Preconditioner *M, int k, const int32_t *
         const int steps = std::min(m, opt.maxiter - max_its);
         if (steps <= 0) break;
         ++report.cycles;
+        if (opt.captured) {
+            if (graph.ka != ka) {
+                // one uncaptured application of each with ka columns first: work buffers, plans and the product
+                // shapes' tuning are set up outside the capture
+                if ((err = precond(ka, r, z)) || (err = apply(ka, z, w))) return err;
+                CycleBuffers cb{n, k, ka, m, opt.tol, V, r, norm, H, cs, sn, g, y, h1, h2, dpart, npart, w, z, vj,
+                                xc, x, bnorm, done, last, its, ndone, act_dev, sys_dev, state};
+                if ((err = build_cycle_graph(A, M, cb, graph))) return err;
+            }
+            if ((err = cudaMemcpyAsync(state + 1, &steps, sizeof(int), cudaMemcpyHostToDevice, st)) ||
+                (err = cudaGraphLaunch(graph.exec, st)))
+                return err;
+            if (M && (err = M->deferred_status(st))) return err;
+            launches += graph.kernels;
+            its_act.resize(ka);
+            cudaMemcpyAsync(its_act.data(), its, sizeof(int) * ka, cudaMemcpyDeviceToHost, st);
+            if ((err = cudaStreamSynchronize(st))) return err;
+            for (int c = 0; c < ka; ++c) its_host[act[c]] += its_act[c];
+            continue;
+        }
         // V0 = r / |r|, g = (|r|, 0, ...)
         k_divide<<<gsz, 256, 0, st>>>(n, ka, r, norm, V);
         k_cycle_start<<<grid_for((int64_t)(m + 1) * m * ka), 256, 0, st>>>(m, ka, norm, H, g, done, last);
@@ -529,6 +840,7 @@ cudaError_t refine_batched(Operator &A, Operator &A32, Preconditioner *M, int k,
         inner.tol = opt.inner_tol;
         inner.maxiter = opt.inner_maxiter;
         inner.restart = opt.restart;
+        inner.captured = opt.captured;
         GmresReport rep;
         if ((err = gmres_batched(A32, M, ka, sys_act.data(), rc, dc, inner, rep, st))) return err;
         for (int c = 0; c < ka; ++c) report.iterations[act[c]] += rep.iterations[c];

@@ -738,6 +738,14 @@ struct LuPrecond : Preconditioner {
     cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
         return tri.solve(k, in, out, s);
     }
+    int deferred_k = 0;
+    cudaError_t apply_deferred(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        deferred_k = k;
+        return tri.solve(k, in, out, s, true);
+    }
+    cudaError_t deferred_status(cudaStream_t s) override {
+        return deferred_k ? tri.read_status(deferred_k, s) : cudaSuccess;
+    }
     // The same solve through cuSOLVER getrs, for validation of the streaming solver.
     cudaError_t apply_library(int k, const cd *in, cd *out, cudaStream_t s) {
         if (k > cap) {
@@ -919,6 +927,7 @@ struct pcbqs_gb300_peec {
     double *klk = nullptr, *tpt = nullptr;   // dense K^T L K and T^T P T (n x n), made once for the factors
     double *tpt_im = nullptr;                // T^T P_im T when P is complex
     float assemble_ms = 0, getrf_ms = 0;     // CUDA-event times of the last factorization's two stages
+    bool captured = false;                   // GMRES restart cycles as CUDA graph launches
     LuUpdateStats updates;                   // its tcgen05 trailing updates (math 4, 5)
     ~pcbqs_gb300_peec() {
         delete bj;
@@ -1211,6 +1220,12 @@ int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *h, double *assemble_ms
     return OK;
 }
 
+int pcbqs_gb300_peec_set_captured(pcbqs_gb300_peec *h, int captured) {
+    if (!h || (captured != 0 && captured != 1)) return pfail(ERR_ARGUMENT, "peec_set_captured: invalid argument");
+    h->captured = captured != 0;
+    return OK;
+}
+
 int pcbqs_gb300_peec_factor_updates(const pcbqs_gb300_peec *h, double *update_ms, double *update_flops,
                                     int32_t *launches) {
     if (!h || !update_ms || !update_flops || !launches)
@@ -1247,6 +1262,7 @@ int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
     if (precondition < 0 || precondition > 2) return pfail(ERR_ARGUMENT, "peec_gmres: preconditioner 0, 1 or 2");
     GmresOptions opt;
     opt.tol = tol; opt.maxiter = maxiter; opt.restart = restart;
+    opt.captured = h->captured;
     GmresReport rep;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Preconditioner *M = precondition == 1 ? static_cast<Preconditioner *>(h->bj)
@@ -1331,6 +1347,7 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *h, int k, const int32_t *sys_
     opt.max_outer = max_outer;
     opt.inner_maxiter = inner_maxiter;
     opt.restart = restart;
+    opt.captured = h->captured;
     GmresReport rep;
     int steps = 0;
     cudaError_t e = refine_batched(h->op, single, M, k, sys_host, reinterpret_cast<const cd *>(b),

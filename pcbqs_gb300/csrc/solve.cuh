@@ -21,12 +21,23 @@ struct Operator {
 struct Preconditioner {
     virtual ~Preconditioner() = default;
     virtual cudaError_t apply(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) = 0;
+    // The same without any host synchronization or allocation (after one apply with this k), so that it can be
+    // captured into a CUDA graph; whatever status it would have checked is read later by deferred_status.
+    virtual cudaError_t apply_deferred(int k, const int32_t *sys, const cd *in, cd *out, cudaStream_t s) {
+        return apply(k, sys, in, out, s);
+    }
+    virtual cudaError_t deferred_status(cudaStream_t) { return cudaSuccess; }
 };
 
 struct GmresOptions {
     double tol = 1e-8;       // relative residual |b - A x| / |b| per column
     int maxiter = 500;       // Arnoldi steps per column
     int restart = 100;
+    // Each restart cycle (its Arnoldi steps, least squares and update) as one CUDA graph launch: the steps run in a
+    // conditional WHILE node whose condition a kernel sets on the device (any column still active, steps left),
+    // with no host synchronization between steps. The operator's and preconditioner's kernels must be capturable
+    // (Preconditioner::apply_deferred) after one warm-up application. Same arithmetic, same result.
+    bool captured = false;
 };
 
 struct GmresReport {
@@ -57,6 +68,7 @@ struct RefineOptions {
     int max_outer = 8;
     int inner_maxiter = 200;
     int restart = 50;
+    bool captured = false;   // the inner GMRES's cycles as graph launches (GmresOptions::captured)
 };
 cudaError_t refine_batched(Operator &A, Operator &A32, Preconditioner *M, int k, const int32_t *sys_host,
                            const cd *b, cd *x, const RefineOptions &opt, GmresReport &report, int &outer_steps,

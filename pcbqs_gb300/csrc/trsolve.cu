@@ -504,7 +504,7 @@ cudaError_t TriSolver::plan_for(int k, Plan **out) {
     return cudaSuccess;
 }
 
-cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
+cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s, bool deferred) {
     if (!lu || k <= 0) return cudaErrorInvalidValue;
     Plan *p = nullptr;
     cudaError_t e = plan_for(k, &p);
@@ -520,10 +520,12 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
         grid = sms * per_sm;
     }
     k_tri_in<<<blocks_for(n * p->kpad), 256, 0, s>>>(n, k, p->kpad, in, p->b);
-    if ((e = cudaMemsetAsync(p->sync, 0, sync_words(nblk) * sizeof(unsigned), s))) return e;
+    // a deferred solve keeps the status word of earlier deferred solves (read_status clears it); otherwise every
+    // word starts at zero
+    if (!deferred && (e = cudaMemsetAsync(p->sync, 0, sync_words(nblk) * sizeof(unsigned), s))) return e;
     for (int c0 = 0; c0 < p->kpad; c0 += KC) {
         // counters restart for every 8 columns; the status word [3] keeps the first failure
-        if (c0 && ((e = cudaMemsetAsync(p->sync, 0, 3 * SYNC_STRIDE * sizeof(unsigned), s)) ||
+        if ((c0 || deferred) && ((e = cudaMemsetAsync(p->sync, 0, 3 * SYNC_STRIDE * sizeof(unsigned), s)) ||
                    (e = cudaMemsetAsync(p->sync + 4 * SYNC_STRIDE, 0,
                                         (sync_words(nblk) - 4 * SYNC_STRIDE) * sizeof(unsigned), s))))
             return e;
@@ -537,6 +539,7 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
     }
     k_tri_out<<<blocks_for(n * k), 256, 0, s>>>(n, k, p->kpad, p->z, gather, out);
     note_launches(2 + p->kpad / KC);
+    if (deferred) return cudaGetLastError();
     // a barrier that gave up leaves its status; the sweeps are then incomplete
     int status = 0;
     if ((e = cudaMemcpyAsync(&status, p->sync + 3 * SYNC_STRIDE, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
@@ -544,6 +547,18 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s) {
         return e;
     if (status) return cudaErrorLaunchTimeout;
     return cudaGetLastError();
+}
+
+cudaError_t TriSolver::read_status(int k, cudaStream_t s) {
+    auto it = plans.find(k);
+    if (it == plans.end()) return cudaSuccess;
+    int *word = reinterpret_cast<int *>(it->second.sync + 3 * SYNC_STRIDE);
+    int status = 0;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(&status, word, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemsetAsync(word, 0, sizeof(int), s)) || (e = cudaStreamSynchronize(s)))
+        return e;
+    return status ? cudaErrorLaunchTimeout : cudaSuccess;
 }
 
 void TriSolver::release() {

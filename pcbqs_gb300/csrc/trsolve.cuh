@@ -34,8 +34,11 @@ struct TriSolver {
 
     // ipiv: the factor's 1-based pivots on the device (getrf output); synchronizes `s`.
     cudaError_t prepare(const float2 *lu, int64_t n, const int *ipiv, cudaStream_t s);
-    // out (n, k) complex128 row-major = A^-1 in, both device arrays.
-    cudaError_t solve(int k, const cd *in, cd *out, cudaStream_t s);
+    // out (n, k) complex128 row-major = A^-1 in, both device arrays. deferred: no read-back of the barriers' status
+    // (and no host synchronization), so the call can be captured into a graph; read_status checks it afterwards.
+    cudaError_t solve(int k, const cd *in, cd *out, cudaStream_t s, bool deferred = false);
+    // cudaErrorLaunchTimeout if a bounded wait of a deferred solve with k columns gave up; synchronizes `s`.
+    cudaError_t read_status(int k, cudaStream_t s);
     void release();
     ~TriSolver() { release(); }
 

@@ -510,7 +510,8 @@ class PeecModel(PeecTopology):
     FACTOR_MATH = {'fp32': 0, 'bf16x9': 1, 'bf16x9-blocked': 2, 'fp32-blocked': 3, 'tc3-blocked': 4,
                    'tc6-blocked': 5}
 
-    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='tc6-blocked', anchors=None):
+    def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='tc6-blocked', anchors=None,
+              captured=False):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
 
         precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
@@ -525,7 +526,9 @@ class PeecModel(PeecTopology):
         only): how many factorizations a sweep shares; the frequencies, in increasing order, are split into that
         many runs and every run is solved as one batch of (frequency, port) columns preconditioned by the factor
         at its middle frequency (default: one factor per frequency). Every column still reaches the tolerance of
-        its own frequency's FP64 system; farther from the anchor it takes more iterations."""
+        its own frequency's FP64 system; farther from the anchor it takes more iterations. captured=True: each GMRES
+        restart cycle is one CUDA graph launch (its Arnoldi steps in a device-controlled conditional loop, no host
+        synchronization between steps; pcbqs_gb300_peec_set_captured), with the same results."""
         if self.L is None:
             self.assemble()
         f = np.atleast_1d(np.asarray(freqs, float))
@@ -569,6 +572,7 @@ class PeecModel(PeecTopology):
                        lib)
             updates[:] += (a.value, b.value, c.value)
         try:
+            _lib.check(lib.pcbqs_gb300_peec_set_captured(handle, int(bool(captured))), lib)
             t1 = time.perf_counter()
             if mode == 2:
                 # the first complex64 factorization depends only on L, P and the frequency: it runs on a side

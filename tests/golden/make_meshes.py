@@ -18,6 +18,8 @@ The boards themselves are synthetic stand-ins with the shapes and sizes of the b
           end between the strips                                                              (~800 triangles)
 
     PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py viapair    (that board alone; the others keep their meshes)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py planes16   (the plane pair with 16 ports, the batched
+                                                   sweep's board)
     PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py train      (train_0 .. train_5: seeded random small boards, alternately a
                                                    plane pair and a via-joined strip pair of random sizes, vias and
                                                    mesh sizes; the learned preconditioner's training systems)
@@ -302,6 +304,13 @@ if __name__ == '__main__':
         data = viapair(reference_core())
         np.savez_compressed(HERE / 'viapair.npz', **data)
         print('viapair', len(data['tris']), 'triangles', len(data['nodes']), 'nodes', len(data['via_seg']), 'vias')
+    elif sys.argv[1:] == ['planes16']:
+        # the batched sweep's board: the plane pair with 16 ports (the same seed, so the first 40 sites are the same
+        # vias and the first 8 ports the same pads)
+        RNG = np.random.default_rng(3)
+        data = planes(reference_core(), n_ports=16)
+        np.savez_compressed(HERE / 'planes16.npz', **data)
+        print('planes16', len(data['tris']), 'triangles', len(data['nodes']), 'nodes')
     elif sys.argv[1:] == ['train']:
         core = reference_core()
         for i in range(6):

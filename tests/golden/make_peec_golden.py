@@ -137,9 +137,9 @@ def stack(name='tiny', slab=(0.0, 0.2e-3, 4.3, 0.02)):
     print(name, 'stack', np.round(Z[1], 6))
 
 
-def planes(freqs=(1e6,)):
+def planes(freqs=(1e6,), board='planes'):
     """peec_planes.npz: the plane pair (22,554 triangles, 32,990 unknowns, 8 ports), DC sheet resistance, at the
-    benchmark's 1 MHz. The reference's MQS._solve_charge factors each frequency once for all 8 drives. The system
+    benchmark's 1 MHz (peec_planes16.npz: its 16-port variant at two frequencies of the batched sweep). The reference's MQS._solve_charge factors each frequency once for all 8 drives. The system
     is factored by the reference's double-precision path of lu_factor_rows (PCBQS_LU=double: LAPACK zgetrf in the
     system's own memory, src/pcbqs/kernels.py:265-284) rather than MixedLU, whose complex64 copy and kept double
     matrix do not fit beside the model's dense R, L and potential projections in a 62 GB host; MixedLU refines to
@@ -150,7 +150,7 @@ def planes(freqs=(1e6,)):
     import time
     os.environ['PCBQS_LU'] = 'double'
     from pcbqs_gb300.board import Board
-    b = Board.load('planes')
+    b = Board.load(board)
     q = reference_model(b)
     from pcbqs.peec import prepare
     t = time.perf_counter()
@@ -162,10 +162,10 @@ def planes(freqs=(1e6,)):
     names, Z, diag = port_matrix(q, b, freqs)
     print(f'solve {time.perf_counter() - t:.1f} s', flush=True)
     assert np.allclose(np.diagonal(Z, axis1=1, axis2=2), diag, rtol=1e-9), 'port voltage convention'
-    np.savez_compressed(HERE / 'peec_planes.npz', freqs=freqs, ports=np.array(names), Z=Z, z_diag=diag,
+    np.savez_compressed(HERE / f'peec_{board}.npz', freqs=freqs, ports=np.array(names), Z=Z, z_diag=diag,
                         unknowns=m['K'].shape[1], loops=m['nl'], components=m['B'].shape[1],
                         conductor_loss='dc', lu='double')
-    print('planes', np.round(Z[0], 6))
+    print(board, np.round(Z[0], 6))
 
 
 if __name__ == '__main__':
@@ -173,6 +173,10 @@ if __name__ == '__main__':
         main(('viapair',), ('dc', 'slab'))
     elif sys.argv[1:] == ['planes']:
         planes()
+    elif sys.argv[1:] == ['planes16']:
+        # two frequencies of the batched sweep (np.geomspace(1e3, 1e8, 64)): its first and its 39th (1.04 MHz)
+        sweep = np.geomspace(1e3, 1e8, 64)
+        planes((sweep[0], sweep[38]), board='planes16')
     else:
         main(tuple(sys.argv[1:]) or ('tiny', 'strip'))
         stack('tiny')
