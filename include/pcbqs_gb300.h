@@ -308,8 +308,11 @@ int pcbqs_gb300_complex_update(int64_t rows, int64_t cols, int k, const void *a,
  * it can be checked on its own. */
 int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int64_t lda, int block, int math, int32_t *info, void *stream);
 /* out = (complex64 factor)^-1 in for k complex128 columns (n, k) row-major, device arrays; the solve step of
- * MixedLU (src/pcbqs/kernels.py:160-181) without its refinement. method 0: this library's streaming triangular
- * solves (what GMRES uses); method 1: cuSOLVER getrs on the same factor (for validation). Synchronizes `stream`. */
+ * MixedLU (src/pcbqs/kernels.py:160-181) without its refinement. method 0: what GMRES uses, this library's
+ * streaming triangular sweeps (8 columns per pass over the factor) or its blocked solve whose off-diagonal products
+ * run on the tcgen05 update (the factor read once for all columns), whichever the first call with this column
+ * count timed faster; 2 / 3: the streaming / the blocked solve (validation); 1: cuSOLVER getrs on the same factor
+ * (validation). Synchronizes `stream`. */
 int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *op, int k, const double *in, double *out, int method,
                               void *stream);
 /* Batched right-preconditioned restarted GMRES on k columns (b, x device; x holds the initial guess), relative

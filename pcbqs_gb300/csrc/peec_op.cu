@@ -1238,13 +1238,20 @@ int pcbqs_gb300_peec_factor_updates(const pcbqs_gb300_peec *h, double *update_ms
 
 int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *h, int k, const double *in, double *out, int method,
                               void *stream) {
-    if (!h || k <= 0 || !in || !out || method < 0 || method > 1)
+    if (!h || k <= 0 || !in || !out || method < 0 || method > 3)
         return pfail(ERR_ARGUMENT, "peec_lu_solve: invalid argument");
     if (!h->lu) return pfail(ERR_ARGUMENT, "peec_lu_solve: no factor set up");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const cd *x = reinterpret_cast<const cd *>(in);
     cd *y = reinterpret_cast<cd *>(out);
-    cudaError_t e = method == 0 ? h->lu->apply(k, nullptr, x, y, st) : h->lu->apply_library(k, x, y, st);
+    cudaError_t e;
+    if (method == 1) {
+        e = h->lu->apply_library(k, x, y, st);
+    } else {
+        h->lu->tri.force = method == 2 ? 0 : method == 3 ? 1 : -1;
+        e = h->lu->apply(k, nullptr, x, y, st);
+        h->lu->tri.force = -1;
+    }
     if (!e) e = cudaStreamSynchronize(st);
     if (e) return pfail(cuda_status(e), "peec_lu_solve: %s", cudaGetErrorString(e));
     return OK;

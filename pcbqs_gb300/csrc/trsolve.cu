@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "pool.cuh"
+#include "tcgemm.cuh"
 #include "trsolve.cuh"
 
 namespace pq {
@@ -494,7 +495,9 @@ cudaError_t TriSolver::plan_for(int k, Plan **out) {
     if ((e = pool_alloc_n(&p.b, vec, nullptr)) || (e = pool_alloc_n(&p.y, vec, nullptr)) ||
         (e = pool_alloc_n(&p.z, vec, nullptr)) ||
         (e = pool_alloc_n(&p.partial, 2 * (size_t)(MAX_SPLITS + 1) * B * KC, nullptr)) ||
-        (e = pool_alloc_n(&p.sync, sync_words(nblk), nullptr)) || (e = cudaStreamSynchronize(nullptr))) {
+        (e = pool_alloc_n(&p.sync, sync_words(nblk), nullptr)) ||
+        (e = cudaMemsetAsync(p.sync, 0, sync_words(nblk) * sizeof(unsigned), nullptr)) ||    // status words start at 0
+        (e = cudaStreamSynchronize(nullptr))) {
         for (float2 *q : {p.b, p.y, p.z, p.partial}) pool_free(q, nullptr);
         pool_free(p.sync, nullptr);
         return e;
@@ -509,6 +512,181 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s, bool 
     Plan *p = nullptr;
     cudaError_t e = plan_for(k, &p);
     if (e) return e;
+    if (force == 0 || force == 1) {            // a method asked for (validation): not timed, not remembered
+        if (force == 0) return solve_streaming(p, k, in, out, s, deferred);
+        if ((e = solve_blocked(p, k, in, out, s))) return e;
+        return deferred ? cudaGetLastError() : read_status(k, s);
+    }
+    if (p->method < 0 && p->kpad < 4 * KC) p->method = 0;      // a few columns: the streaming sweeps
+    // column counts in one power-of-two bucket share the timing (a GMRES active set shrinks through many counts)
+    int bucket = 4 * KC;
+    while (bucket < p->kpad) bucket *= 2;
+    if (p->method < 0) {
+        auto it = method_by_bucket.find(bucket);
+        if (it != method_by_bucket.end()) p->method = it->second;
+    }
+    if (p->method < 0 && !deferred) {
+        // the first call with this many columns: the blocked solve once to set it up, then each method timed once;
+        // the faster is kept (its result is the one left in `out`)
+        if ((e = solve_blocked(p, k, in, out, s)) || (e = cudaStreamSynchronize(s))) return e;
+        cudaEvent_t ev[3];
+        for (cudaEvent_t &x : ev)
+            if ((e = cudaEventCreate(&x))) return e;
+        float streaming = 0, blocked = 0;
+        if (!(e = cudaEventRecord(ev[0], s)) && !(e = solve_streaming(p, k, in, out, s, false)) &&
+            !(e = cudaEventRecord(ev[1], s)) && !(e = solve_blocked(p, k, in, out, s)) &&
+            !(e = cudaEventRecord(ev[2], s)) && !(e = cudaEventSynchronize(ev[2])) &&
+            !(e = cudaEventElapsedTime(&streaming, ev[0], ev[1])))
+            e = cudaEventElapsedTime(&blocked, ev[1], ev[2]);
+        for (cudaEvent_t x : ev) cudaEventDestroy(x);
+        if (e) return e;
+        p->method = blocked < streaming ? 1 : 0;
+        method_by_bucket[bucket] = p->method;
+        return read_status(k, s);
+    }
+    if (p->method == 1) {
+        if ((e = solve_blocked(p, k, in, out, s))) return e;
+        return deferred ? cudaGetLastError() : read_status(k, s);
+    }
+    return solve_streaming(p, k, in, out, s, deferred);
+}
+
+int TriSolver::method_for(int k) const {
+    auto it = plans.find(k);
+    return it == plans.end() ? -1 : it->second.method;
+}
+
+// The diagonal TRI_PANEL-row block of the blocked solve, for 8 right-hand sides per CTA (grid kpad / 8), in the
+// original view: forward (lower = true) U^T_II y_I = b_I with U^T lower, backward L^T_II z_I = y_I with L^T unit
+// upper, T[r][c] = lu[r n + c]. The block is walked in TRI_BLOCK-row sub-blocks (forward first to last, backward
+// last to first): acc = rhs_s - T[s, solved] x[solved], the solved part staged in shared memory and T's rows in
+// 64-column tiles, then x_s = inv_s acc with the precomputed inverse of the sub-block's diagonal block.
+constexpr int DIAG_COLS = 8, DIAG_TILE = 64, DIAG_THREADS = 256;
+constexpr size_t DIAG_SMEM = sizeof(float2) * ((size_t)TRI_PANEL * DIAG_COLS + (size_t)B * DIAG_TILE);
+
+__global__ void __launch_bounds__(DIAG_THREADS) k_diag_block(const float2 *lu, int64_t n, int64_t I0, int nb,
+                                                             const float2 *inv, const float2 *rhs, float2 *x, int kp,
+                                                             int lower) {
+    extern __shared__ float2 diag_smem[];
+    float2 *xs = diag_smem;                                  // [TRI_PANEL][DIAG_COLS] the block's solution
+    float2 *ut = diag_smem + (size_t)TRI_PANEL * DIAG_COLS;  // [B][DIAG_TILE] a tile of T's rows
+    const int c0 = blockIdx.x * DIAG_COLS;
+    const int t = threadIdx.x;
+    const int r = t >> 1, ch = (t & 1) * 4;                  // this thread's row of the sub-block and 4 columns
+    const int nsub = (nb + B - 1) / B;
+    for (int q = 0; q < nsub; ++q) {
+        const int s = lower ? q : nsub - 1 - q;
+        const int s0 = s * B, rows = min(B, nb - s0);
+        // solved columns of T's rows: forward [0, s0), backward [s0 + rows, nb)
+        const int j0 = lower ? 0 : s0 + rows, j1 = lower ? s0 : nb;
+        float2 acc[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            acc[c] = r < rows ? rhs[(I0 + s0 + r) * kp + c0 + ch + c] : make_float2(0.f, 0.f);
+        for (int jt = j0; jt < j1; jt += DIAG_TILE) {
+            const int w = min(DIAG_TILE, j1 - jt);
+            __syncthreads();
+            for (int e = t; e < B * DIAG_TILE; e += DIAG_THREADS) {
+                const int rr = e / DIAG_TILE, jj = e % DIAG_TILE;
+                ut[e] = (rr < rows && jj < w) ? lu[(I0 + s0 + rr) * n + I0 + jt + jj] : make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+            if (r < rows) {
+                // the tile's partial sums first, then into the running sums: rounding errors grow with the tile
+                // length and the tile count rather than with the whole row
+                float2 part[4] = {};
+                for (int jj = 0; jj < w; ++jj) {
+                    const float2 u = ut[r * DIAG_TILE + jj];
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const float2 v = xs[(jt + jj) * DIAG_COLS + ch + c];
+                        part[c].x += u.x * v.x - u.y * v.y;
+                        part[c].y += u.x * v.y + u.y * v.x;
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    acc[c].x -= part[c].x;
+                    acc[c].y -= part[c].y;
+                }
+            }
+        }
+        // acc staged in the sub-block's rows of xs, then x_s = inv_s acc (inv row-major B x B)
+        __syncthreads();
+        if (r < B)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) xs[(s0 + r) * DIAG_COLS + ch + c] = r < rows ? acc[c] : make_float2(0.f, 0.f);
+        __syncthreads();
+        float2 out[4] = {};
+        const float2 *iv = inv + ((size_t)(I0 / B + s) * B + r) * B;
+        if (r < rows)
+            for (int b = 0; b < rows; ++b) {
+                const float2 m = iv[b];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const float2 v = xs[(s0 + b) * DIAG_COLS + ch + c];
+                    out[c].x += m.x * v.x - m.y * v.y;
+                    out[c].y += m.x * v.y + m.y * v.x;
+                }
+            }
+        __syncthreads();
+        if (r < rows)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) xs[(s0 + r) * DIAG_COLS + ch + c] = out[c];
+    }
+    __syncthreads();
+    for (int e = t; e < nb * DIAG_COLS; e += DIAG_THREADS)
+        x[(I0 + e / DIAG_COLS) * kp + c0 + e % DIAG_COLS] = xs[e];
+}
+
+// The blocked solve for many right-hand sides. Each TRI_PANEL-row step solves its diagonal block (k_diag_block)
+// and subtracts the block's product with the off-diagonal panel from the rows still to come, on the tcgen05 update
+// with six BF16 part products (FP32's accuracy), in the transposed view: the work arrays (n, kpad) row-major are the
+// column-major kpad x n matrices B^T, Y^T, Z^T, and with T[r][c] = lu[r n + c] (A = U^T L^T P^T read row-major) the
+// forward update b_rest^T -= y_I^T U_(I, rest) takes U_(I, rest) as the column-major nb x rest block at
+// lu + I1 n + I0 (leading dimension n), the backward y_above^T -= z_I^T L_(I, above) the block at lu + I0. The
+// factor is read once per sweep for all columns instead of once per 8.
+cudaError_t TriSolver::solve_blocked(Plan *p, int k, const cd *in, cd *out, cudaStream_t s) {
+    cudaError_t e;
+    const int kp = p->kpad;
+    if (!p->planes) {
+        if ((e = cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DIAG_SMEM)) ||
+            (e = pool_alloc(&p->planes, tc_update_scratch_bytes(kp, n, TRI_PANEL, 6), s)) ||
+            (e = pool_alloc_n(&p->update_error, 1, s)) || (e = cudaMemsetAsync(p->update_error, 0, sizeof(int), s)))
+            return e;
+    }
+    k_tri_in<<<blocks_for(n * kp), 256, 0, s>>>(n, k, kp, in, p->b);
+    const int64_t steps = (n + TRI_PANEL - 1) / TRI_PANEL;
+    const unsigned long long wait = wait_cycles();
+    const unsigned diag_grid = (unsigned)(kp / DIAG_COLS);
+    int launches = 2;
+    // forward: U^T y = b, block by block; the rest of b then loses the block's product (y^T U = b^T transposed)
+    for (int64_t I = 0; I < steps; ++I) {
+        const int64_t I0 = I * TRI_PANEL, I1 = std::min<int64_t>(I0 + TRI_PANEL, n);
+        const int nb = (int)(I1 - I0);
+        k_diag_block<<<diag_grid, DIAG_THREADS, DIAG_SMEM, s>>>(lu, n, I0, nb, inv_lower, p->b, p->y, kp, 1);
+        ++launches;
+        if (I1 < n && (e = tc_update_c64(kp, n - I1, nb, p->y + I0 * kp, kp, lu + I1 * n + I0, n, p->b + I1 * kp, kp,
+                                         6, p->planes, false, p->update_error, wait, s)))
+            return e;
+    }
+    // backward: L^T z = y, last block first; the rows above then lose the block's product (z^T L = y^T)
+    for (int64_t I = steps - 1; I >= 0; --I) {
+        const int64_t I0 = I * TRI_PANEL, I1 = std::min<int64_t>(I0 + TRI_PANEL, n);
+        const int nb = (int)(I1 - I0);
+        k_diag_block<<<diag_grid, DIAG_THREADS, DIAG_SMEM, s>>>(lu, n, I0, nb, inv_upper, p->y, p->z, kp, 0);
+        ++launches;
+        if (I0 > 0 && (e = tc_update_c64(kp, I0, nb, p->z + I0 * kp, kp, lu + I0, n, p->y, kp, 6, p->planes, false,
+                                         p->update_error, wait, s)))
+            return e;
+    }
+    k_tri_out<<<blocks_for(n * k), 256, 0, s>>>(n, k, kp, p->z, gather, out);
+    note_launches(launches);
+    return cudaGetLastError();
+}
+
+cudaError_t TriSolver::solve_streaming(Plan *p, int k, const cd *in, cd *out, cudaStream_t s, bool deferred) {
+    cudaError_t e;
     if (grid <= 0) {
         int device = 0, sms = 0, per_sm = 0, coop = 0;
         if ((e = cudaGetDevice(&device)) ||
@@ -552,13 +730,18 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s, bool 
 cudaError_t TriSolver::read_status(int k, cudaStream_t s) {
     auto it = plans.find(k);
     if (it == plans.end()) return cudaSuccess;
-    int *word = reinterpret_cast<int *>(it->second.sync + 3 * SYNC_STRIDE);
-    int status = 0;
+    Plan &p = it->second;
+    int *word = reinterpret_cast<int *>(p.sync + 3 * SYNC_STRIDE);
+    int status[2] = {0, 0};
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(&status, word, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
-        (e = cudaMemsetAsync(word, 0, sizeof(int), s)) || (e = cudaStreamSynchronize(s)))
+    if ((e = cudaMemcpyAsync(&status[0], word, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemsetAsync(word, 0, sizeof(int), s)))
         return e;
-    return status ? cudaErrorLaunchTimeout : cudaSuccess;
+    if (p.update_error && ((e = cudaMemcpyAsync(&status[1], p.update_error, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+                           (e = cudaMemsetAsync(p.update_error, 0, sizeof(int), s))))
+        return e;
+    if ((e = cudaStreamSynchronize(s))) return e;
+    return status[0] || status[1] ? cudaErrorLaunchTimeout : cudaSuccess;
 }
 
 void TriSolver::release() {
@@ -567,8 +750,12 @@ void TriSolver::release() {
         Plan &p = kv.second;
         for (float2 *q : {p.b, p.y, p.z, p.partial}) pool_free(q, nullptr);
         pool_free(p.sync, nullptr);
+        pool_free(p.planes, nullptr);
+        pool_free(p.update_error, nullptr);
     }
+
     plans.clear();
+    method_by_bucket.clear();
     pool_free(inv_lower, nullptr);
     pool_free(inv_upper, nullptr);
     pool_free(gather, nullptr);
