@@ -168,11 +168,48 @@ def planes(freqs=(1e6,), board='planes'):
     print(board, np.round(Z[0], 6))
 
 
+def graph(boards=('tiny', 'strip', 'viapair'), freqs=(1e5, 1e6, 1e7), maxiter=3000):
+    """graph_<board>.npz: the reference's iterative PEEC solve (peec_iterative.solve, src/pcbqs/peec_iterative.py:
+    229-346) on its compressed model with its graph preconditioner (solver_preconditioner='graph': the exact inverse of the loop block of
+    a diagonal branch impedance through the node Laplacian's incomplete LU, then the charge-tree solve,
+    peec_iterative.py:44-84), every port driven alone at each frequency: SciPy GMRES (restart 100, relative
+    tolerance 1e-8) iterations and true residual per (frequency, drive), and the port impedance matrix. The
+    comparator of the library's block-Jacobi and learned preconditioners."""
+    from pcbqs_gb300.board import Board
+    freqs = np.asarray(freqs, float)
+    for name in boards:
+        b = Board.load(name)
+        q = reference_model(b)
+        from pcbqs.peec_iterative import solve
+        # the reference's compressed model, the one its iterative solve runs on (MQS(matrix_backend=
+        # 'hierarchical'), src/pcbqs/mqs.py:220-221: H-matrix L and potential at their default compression)
+        q.matrix_backend = 'hierarchical'
+        q._compression_options = dict(tol=1e-6, leaf=64, eta=1.0)
+        q.solver_tol, q.solver_maxiter, q.solver_restart, q.solver_preconditioner = 1e-8, maxiter, 100, 'graph'
+        names = [p for p, _, _ in b.ports]
+        its = np.zeros((len(freqs), len(names)), int)
+        res = np.zeros((len(freqs), len(names)))
+        Z = np.zeros((len(freqs), len(names), len(names)), complex)
+        kinds = set()
+        for j, drive in enumerate(names):
+            r = solve(q, freqs, {n: (1.0 if n == drive else 0.0) for n in names})
+            for fi, info in enumerate(q.solve_info):
+                its[fi, j], res[fi, j] = info['iterations'], info['relative_residual']
+                kinds.add(info['preconditioner'])
+            for i, (n, a, c) in enumerate(b.ports):
+                Z[:, i, j] = r.potential[:, b.term_node(c)] - r.potential[:, b.term_node(a)]
+        np.savez_compressed(HERE / f'graph_{name}.npz', freqs=freqs, ports=np.array(names), iterations=its,
+                            residual=res, Z=Z, preconditioner=np.array(sorted(kinds)))
+        print(name, sorted(kinds), its.tolist(), float(res.max()))
+
+
 if __name__ == '__main__':
     if sys.argv[1:] == ['viapair']:
         main(('viapair',), ('dc', 'slab'))
     elif sys.argv[1:] == ['planes']:
         planes()
+    elif sys.argv[1:] == ['graph']:
+        graph()
     elif sys.argv[1:] == ['planes16']:
         # a frequency of the batched sweep (np.geomspace(1e3, 1e8, 64)): its 39th, 1.04 MHz
         sweep = np.geomspace(1e3, 1e8, 64)

@@ -306,3 +306,26 @@ def test_port_impedance_through_vias_matches_reference(device_library, precondit
     err = np.abs(res.impedance - g['Z']).max() / np.abs(g['Z']).max()
     assert err < 1e-6, err
     assert (res.residual <= 1e-8).all()
+
+
+@pytest.mark.parametrize('board', ['tiny', 'strip', 'viapair'])
+def test_preconditioners_against_the_reference_graph_preconditioner(device_library, board):
+    """The reference's own iterative solve with its graph preconditioner (tests/golden/graph_<board>.npz:
+    peec_iterative.solve on its compressed model, solver_preconditioner='graph', SciPy GMRES restart 100 to 1e-8,
+    every port driven alone) beside this library's preconditioners on the same board and frequencies: the port
+    impedances agree within the compression tolerance (1e-6 relative), and the GMRES step counts are reported per
+    preconditioner (printed: block-Jacobi, the complex64 factor, the reference's graph ILU)."""
+    from conftest import GOLDEN
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel
+    with np.load(GOLDEN / f'graph_{board}.npz') as g:
+        freqs, its_graph, Zg = g['freqs'], g['iterations'], g['Z']
+    model = PeecModel(Board.load(board))
+    for precondition in ('block_jacobi', 'lu32'):
+        res = model.solve(freqs, precondition=precondition)
+        its = res.iterations.reshape(len(freqs), -1)
+        err = np.abs(res.impedance - Zg).max() / np.abs(Zg).max()
+        print(f'{board} {precondition}: GMRES steps {its.max(axis=1).tolist()} (reference graph ILU '
+              f'{its_graph.max(axis=1).tolist()}), port Z against the reference iterative solve {err:.2e}')
+        assert (res.residual <= 1e-8).all()
+        assert err < 1e-5, err
