@@ -65,6 +65,8 @@ def parse():
                    help='also time a sweep of this many log-spaced frequencies (1 kHz to 100 MHz), all ports')
     p.add_argument('--anchors', type=int, default=8, help='complex64 factors shared across the sweep')
     p.add_argument('--sweep-board', default='planes16', help='the sweep\'s board (default: the 16-port plane pair)')
+    p.add_argument('--product', default='tc3', choices=['tc3', 'tc6', 'fp32'],
+                   help='the mixed solve\'s inner dense products over 16 or more columns')
     p.add_argument('--case', default=None,
                    help='time one kernel case small enough for a full ncu capture instead of the benchmark: '
                         'fill:BOARD[:TRIANGLES] | lu:BOARD[:K...] | dense:N[:K] | getrf:N[:BLOCK[:MATH...]] | '
@@ -680,7 +682,7 @@ def main():
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record()
         rs = model.solve(fs, precondition='lu32', mixed=mixed, factor_math=args.factor_math,
-                         anchors=min(args.anchors, args.sweep), captured=True)
+                         anchors=min(args.anchors, args.sweep), captured=True, product=args.product)
         s1.record()
         torch.cuda.synchronize()
         its = rs.iterations.reshape(len(fs), -1)
@@ -695,6 +697,7 @@ def main():
                         errs.append([float(f), float(np.abs(rs.impedance[fi] - Zr).max() / np.abs(Zr).max())])
                 sweep_err = errs or None
         line['sweep'] = dict(board=args.sweep_board, unknowns=model.n, captured_cycles=True,
+                             inner_product=args.product, outer_steps=rs.timings.get('outer_steps'),
                              port_z_max_rel_err_vs_reference=sweep_err,
                              frequencies=len(fs), range_hz=[1e3, 1e8], ports=len(model.names),
                              columns=int(its.size), anchors=rs.timings['factorizations'],

@@ -269,6 +269,17 @@ int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *op, double *assemble_m
  * order as captured = 0 (the default: one host check per step), so the same results. The reference's batched
  * counterpart is mqs_iterative._lockstep_gmres (src/pcbqs/mqs_iterative.py:109-170), a host loop per step. */
 int pcbqs_gb300_peec_set_captured(pcbqs_gb300_peec *op, int captured);
+/* The inner products of pcbqs_gb300_peec_solve_mixed over 16 or more right-hand sides: terms = 3 (the default) or 6
+ * BF16 parts on the tensor cores (pcbqs_gb300_dense_apply_tensor; L and P packed once after each
+ * pcbqs_gb300_peec_single), 0 for the FP32 product throughout. The FP64 outer refinement sets the answer's accuracy
+ * either way; the parts kept change the inner solves' work. No counterpart in the reference, whose inner products are
+ * NumPy's (src/pcbqs/peec_iterative.py:253-256). */
+int pcbqs_gb300_peec_set_product(pcbqs_gb300_peec *op, int terms);
+/* The operator's FP64 dense products (pcbqs_gb300_peec_apply, the FP64 GMRES, the mixed solve's outer residuals)
+ * over 4 or more right-hand sides: slices = 2..7 on the tensor cores (pcbqs_gb300_dense_apply_sliced; L and P sliced
+ * once), 0 (the default) on the FP64 pipe. No counterpart in the reference, whose products are NumPy's FP64
+ * (src/pcbqs/peec_iterative.py:253-256). */
+int pcbqs_gb300_peec_set_fp64_product(pcbqs_gb300_peec *op, int slices);
 /* The tcgen05 trailing updates of the last pcbqs_gb300_peec_factor with math 4 or 5: their summed CUDA-event time
  * (ms, on the factorization's stream), complex flops (8 rows cols k each) and count; zeros after any other math.
  * No counterpart in the reference; for the roofline of the update kernel. */
@@ -331,6 +342,21 @@ int pcbqs_gb300_dense_apply(int64_t rows, int k, const double *M, int64_t ld, co
 /* The same product from the FP32 copy of M (the mixed solve's inner products), results in FP64. */
 int pcbqs_gb300_dense_apply_single(int64_t rows, int k, const float *Mf, int64_t ld, const double *X, double *Y,
                                    void *stream);
+/* The same product on the tcgen05 tensor cores: M's FP32 copy and X (rounded to FP32) split into BF16 parts, terms
+ * 3 (relative error about 2^-16) or 6 (FP32's), one GEMM of inner dimension terms * rows against X's real and
+ * imaginary columns side by side, FP32 accumulation. Packs M for this call only (the mixed solve packs L and P once
+ * and reuses them) and synchronizes `stream`. Status 6 when a bounded wait (wait_cycles SM clocks) gave up. The
+ * mixed solve's inner products take this path over 16 or more right-hand sides (pcbqs_gb300_peec_set_product). */
+int pcbqs_gb300_dense_apply_tensor(int64_t rows, int k, const float *Mf, int64_t ld, const double *X, double *Y,
+                                   int terms, uint64_t wait_cycles, void *stream);
+/* The FP64 product (M FP64) to FP64's accuracy on the tcgen05 tensor cores: every row of M and every real column
+ * of X is cut into `slices` (2..7) 8-bit integer slices under its own power-of-two scale (exact in BF16), the slice
+ * products of each level summed exactly (FP32 over 256-long chunks, 32-bit integers across them) and the levels
+ * carried into FP64. Error about 2^(-8 slices) of max_t |M[r,t]| sum_t |X[t,c]| (slices 6: 2^-48). Packs M for this
+ * call only and synchronizes `stream`; status 6 when a bounded wait gave up. The operator's FP64 products take this
+ * path over 4 or more right-hand sides after pcbqs_gb300_peec_set_fp64_product. */
+int pcbqs_gb300_dense_apply_sliced(int64_t rows, int k, const double *M, int64_t ld, const double *X, double *Y,
+                                   int slices, uint64_t wait_cycles, void *stream);
 /* Single-precision copies of L and P (device, row strides ldlf/ldpf) for the inner products of the mixed solve,
  * and the conversion that makes them. */
 int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *stream);

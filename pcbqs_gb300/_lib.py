@@ -120,6 +120,8 @@ PROTOTYPES = {
     'pcbqs_gb300_peec_factor_times': (ctypes.c_int, [c_void_p, ctypes.POINTER(ctypes.c_double),
                                                      ctypes.POINTER(ctypes.c_double)]),
     'pcbqs_gb300_peec_set_captured': (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    'pcbqs_gb300_peec_set_product': (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    'pcbqs_gb300_peec_set_fp64_product': (ctypes.c_int, [c_void_p, ctypes.c_int]),
     'pcbqs_gb300_peec_factor_updates': (ctypes.c_int, [c_void_p, ctypes.POINTER(ctypes.c_double),
                                                        ctypes.POINTER(ctypes.c_double), c_int32_p]),
     'pcbqs_gb300_via_inductance': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_double, c_void_p,
@@ -149,6 +151,10 @@ PROTOTYPES = {
                                                c_void_p, c_void_p]),
     'pcbqs_gb300_dense_apply_single': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64,
                                                       c_void_p, c_void_p, c_void_p]),
+    'pcbqs_gb300_dense_apply_tensor': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64,
+                                                      c_void_p, c_void_p, ctypes.c_int, ctypes.c_uint64, c_void_p]),
+    'pcbqs_gb300_dense_apply_sliced': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_void_p, ctypes.c_int64,
+                                                      c_void_p, c_void_p, ctypes.c_int, ctypes.c_uint64, c_void_p]),
     'pcbqs_gb300_to_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p]),
     'pcbqs_gb300_peec_single': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
                                                ctypes.c_int64]),

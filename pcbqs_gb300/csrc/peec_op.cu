@@ -33,6 +33,7 @@
 #include "factor.cuh"
 #include "pool.cuh"
 #include "solve.cuh"
+#include "tcgemm.cuh"
 #include "trsolve.cuh"
 
 namespace pq {
@@ -550,9 +551,106 @@ struct PeecOp : Operator {
     float *xf = nullptr;       // packed FP32 right-hand sides of the single-precision products
     int64_t capf = 0;
 
+    // The single-precision products over at least TC_MIN_COLUMNS right-hand sides run on the tensor cores
+    // (tc_real_product): L's, P's and P's imaginary part's BF16 part planes (tc_terms parts) are packed on first use
+    // after peec_single, the right-hand sides per product. tc_terms = 0 keeps the FP32 product throughout.
+    static constexpr int TC_MIN_COLUMNS = 16;
+    int tc_terms = 3;
+    void *plane[3] = {};
+    size_t plane_cap[3] = {};
+    bool packed[3] = {};
+    void *tcs = nullptr;       // the right-hand sides' plane
+    size_t tcs_cap = 0;
+    int *tc_error = nullptr;   // ERR_TIMEOUT from a product whose bounded wait gave up
+
+    cudaError_t tensor_product(int which, int64_t rows, int k, const float *Mf, int64_t ldf, const cd *x, cd *y,
+                               cudaStream_t s) {
+        cudaError_t e;
+        if (!tc_error) {
+            if ((e = dev_alloc(&tc_error, 1, s)) || (e = cudaMemsetAsync(tc_error, 0, sizeof(int), s))) return e;
+        }
+        const size_t pb = tc_real_plane_bytes(rows, rows, tc_terms);
+        if (!packed[which] || plane_cap[which] < pb) {
+            if (plane_cap[which] < pb) {
+                dev_free(plane[which], s);
+                plane[which] = nullptr;
+                plane_cap[which] = 0;
+                if ((e = dev_alloc(reinterpret_cast<uint8_t **>(&plane[which]), pb, s))) return e;
+                plane_cap[which] = pb;
+            }
+            if ((e = tc_pack_real(rows, rows, Mf, ldf, tc_terms, plane[which], s))) return e;
+            packed[which] = true;
+        }
+        const size_t sb = tc_real_scratch_bytes(rows, k, tc_terms);
+        if (sb > tcs_cap) {
+            dev_free(tcs, s);
+            tcs = nullptr;
+            tcs_cap = 0;
+            if ((e = dev_alloc(reinterpret_cast<uint8_t **>(&tcs), sb, s))) return e;
+            tcs_cap = sb;
+        }
+        return tc_real_product(rows, rows, plane[which], k, reinterpret_cast<const double2 *>(x), k,
+                               reinterpret_cast<double2 *>(y), k, tc_terms, tcs, tc_error, wait_cycles(), s);
+    }
+
+    void unpack() {
+        for (bool &p : packed) p = false;
+    }
+
+    // The FP64 products over at least EXACT_MIN_COLUMNS right-hand sides on the tensor cores when exact_slices > 0
+    // (tc_exact_product: L's, P's and P's imaginary part's integer slice planes, packed on first use; FP64's
+    // accuracy); exact_slices = 0 keeps them on the FP64 pipe.
+    static constexpr int EXACT_MIN_COLUMNS = 4;
+    int exact_slices = 0;
+    void *xplane[3] = {};
+    size_t xplane_cap[3] = {};
+    bool xpacked[3] = {};
+    void *xs = nullptr;        // the right-hand sides' slices
+    size_t xs_cap = 0;
+
+    cudaError_t sliced_product(int which, int64_t rows, int k, const double *M, int64_t ld, const cd *x, cd *y,
+                               cudaStream_t s) {
+        cudaError_t e;
+        if (!tc_error) {
+            if ((e = dev_alloc(&tc_error, 1, s)) || (e = cudaMemsetAsync(tc_error, 0, sizeof(int), s))) return e;
+        }
+        const size_t pb = tc_exact_plane_bytes(rows, rows, exact_slices);
+        if (!xpacked[which] || xplane_cap[which] < pb) {
+            if (xplane_cap[which] < pb) {
+                dev_free(xplane[which], s);
+                xplane[which] = nullptr;
+                xplane_cap[which] = 0;
+                if ((e = dev_alloc(reinterpret_cast<uint8_t **>(&xplane[which]), pb, s))) return e;
+                xplane_cap[which] = pb;
+            }
+            if ((e = tc_slice_exact(rows, rows, M, ld, exact_slices, xplane[which], s))) return e;
+            xpacked[which] = true;
+        }
+        const size_t sb = tc_exact_scratch_bytes(rows, k, exact_slices);
+        if (sb > xs_cap) {
+            dev_free(xs, s);
+            xs = nullptr;
+            xs_cap = 0;
+            if ((e = dev_alloc(reinterpret_cast<uint8_t **>(&xs), sb, s))) return e;
+            xs_cap = sb;
+        }
+        return tc_exact_product(rows, rows, xplane[which], k, reinterpret_cast<const double2 *>(x), k,
+                                reinterpret_cast<double2 *>(y), k, exact_slices, xs, tc_error, wait_cycles(), s);
+    }
+
     cudaError_t dense(bool single, int64_t rows, int k, const double *M, int64_t ld, const float *Mf, int64_t ldf,
                       const cd *x, cd *y, cudaStream_t s) {
-        if (!single) return dense_sym_apply<double, 2>(rows, k, M, ld, x, y, s);
+        if (!single) {
+            if (exact_slices && k >= EXACT_MIN_COLUMNS) {
+                const int which = M == L ? 0 : M == P ? 1 : M == Pim ? 2 : -1;
+                if (which >= 0) return sliced_product(which, rows, k, M, ld, x, y, s);
+            }
+            return dense_sym_apply<double, 2>(rows, k, M, ld, x, y, s);
+        }
+        if (tc_terms && k >= TC_MIN_COLUMNS) {
+            const int which = Mf == Lf ? 0 : Mf == Pf ? 1 : Mf == Pfim ? 2 : -1;
+            if (which >= 0) return tensor_product(which, rows, k, Mf, ldf, x, y, s);
+        }
         const int64_t need = std::max(ne, nn) * (int64_t)DENSE_NC;
         if (need > capf) {
             dev_free(xf, s);
@@ -596,6 +694,11 @@ struct PeecOp : Operator {
         for (double *p : {omega, zscale, walpha, inv_z, inv_p}) dev_free(p);
         dev_free(rscale);
         dev_free(xf);
+        for (void *p : plane) dev_free(p);
+        for (void *p : xplane) dev_free(p);
+        dev_free(xs);
+        dev_free(tcs);
+        dev_free(tc_error);
     }
 };
 
@@ -1005,6 +1108,19 @@ int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *d, pcbqs_gb300_peec **o
 
 void pcbqs_gb300_peec_destroy(pcbqs_gb300_peec *h) { delete h; }
 
+// ERR_TIMEOUT (and the flag cleared) when a tensor-core product of this operator gave up a bounded wait since the
+// last check; synchronizes `st`.
+static int take_product_timeout(PeecOp &op, cudaStream_t st, const char *what) {
+    if (!op.tc_error) return OK;
+    int timed_out = 0;
+    cudaError_t e = cudaMemcpyAsync(&timed_out, op.tc_error, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    if (!e && timed_out) e = cudaMemsetAsync(op.tc_error, 0, sizeof(int), st);
+    if (e) return pfail(cuda_status(e), "%s: %s", what, cudaGetErrorString(e));
+    if (timed_out) return pfail(ERR_TIMEOUT, "%s: a bounded wait of a tensor-core product gave up", what);
+    return OK;
+}
+
 int pcbqs_gb300_peec_apply(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, const double *in, double *out,
                            void *stream) {
     if (!h || k <= 0 || !sys_host || !in || !out) return pfail(ERR_ARGUMENT, "peec_apply: invalid argument");
@@ -1018,7 +1134,7 @@ int pcbqs_gb300_peec_apply(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
     if (!e) e = cudaStreamSynchronize(st);
     dev_free(sys, st);
     if (e) return pfail(cuda_status(e), "peec_apply: %s", cudaGetErrorString(e));
-    return OK;
+    return take_product_timeout(h->op, st, "peec_apply");
 }
 
 int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double *krk, void *stream) {
@@ -1226,6 +1342,22 @@ int pcbqs_gb300_peec_set_captured(pcbqs_gb300_peec *h, int captured) {
     return OK;
 }
 
+int pcbqs_gb300_peec_set_fp64_product(pcbqs_gb300_peec *h, int slices) {
+    if (!h || slices < 0 || slices == 1 || slices > 7)
+        return pfail(ERR_ARGUMENT, "peec_set_fp64_product: slices 0 or 2..7");
+    if (slices != h->op.exact_slices)
+        for (bool &p : h->op.xpacked) p = false;
+    h->op.exact_slices = slices;
+    return OK;
+}
+
+int pcbqs_gb300_peec_set_product(pcbqs_gb300_peec *h, int terms) {
+    if (!h || (terms != 0 && terms != 3 && terms != 6)) return pfail(ERR_ARGUMENT, "peec_set_product: terms 0, 3 or 6");
+    if (terms != h->op.tc_terms) h->op.unpack();
+    h->op.tc_terms = terms;
+    return OK;
+}
+
 int pcbqs_gb300_peec_factor_updates(const pcbqs_gb300_peec *h, double *update_ms, double *update_flops,
                                     int32_t *launches) {
     if (!h || !update_ms || !update_flops || !launches)
@@ -1277,6 +1409,7 @@ int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
     cudaError_t e = gmres_batched(h->op, M, k, sys_host,
                                   reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x), opt, rep, st);
     if (e) return pfail(cuda_status(e), "peec_gmres: %s", cudaGetErrorString(e));
+    if (int status = take_product_timeout(h->op, static_cast<cudaStream_t>(stream), "peec_gmres")) return status;
     bool ok = true;
     for (int s = 0; s < k; ++s) {
         if (iterations) iterations[s] = rep.iterations[s];
@@ -1310,6 +1443,64 @@ int pcbqs_gb300_dense_apply_single(int64_t rows, int k, const float *Mf, int64_t
     return OK;
 }
 
+int pcbqs_gb300_dense_apply_tensor(int64_t rows, int k, const float *Mf, int64_t ld, const double *X, double *Y,
+                                   int terms, uint64_t wait_cycles, void *stream) {
+    if (rows <= 0 || k <= 0 || !Mf || ld < rows || !X || !Y || (terms != 3 && terms != 6) || wait_cycles == 0)
+        return pfail(ERR_ARGUMENT, "dense_apply_tensor: invalid argument (terms 3 or 6, ld >= rows, wait_cycles > 0)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint8_t *plane = nullptr, *scratch = nullptr;
+    int *flag = nullptr;
+    cudaError_t e;
+    if ((e = dev_alloc(&plane, tc_real_plane_bytes(rows, rows, terms), st)) ||
+        (e = dev_alloc(&scratch, tc_real_scratch_bytes(rows, k, terms), st)) || (e = dev_alloc(&flag, 1, st))) {
+        dev_free(plane, st);
+        dev_free(scratch, st);
+        return pfail(ERR_MEMORY, "dense_apply_tensor: %s", cudaGetErrorString(e));
+    }
+    int timed_out = 0;
+    if (!(e = cudaMemsetAsync(flag, 0, sizeof(int), st)) && !(e = tc_pack_real(rows, rows, Mf, ld, terms, plane, st)))
+        e = tc_real_product(rows, rows, plane, k, reinterpret_cast<const double2 *>(X), k,
+                            reinterpret_cast<double2 *>(Y), k, terms, scratch, flag, (unsigned long long)wait_cycles,
+                            st);
+    if (!e) e = cudaMemcpyAsync(&timed_out, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    dev_free(plane, st);
+    dev_free(scratch, st);
+    dev_free(flag, st);
+    if (e) return pfail(cuda_status(e), "dense_apply_tensor: %s", cudaGetErrorString(e));
+    if (timed_out) return pfail(ERR_TIMEOUT, "dense_apply_tensor: a bounded wait of the tensor-core product gave up");
+    return OK;
+}
+
+int pcbqs_gb300_dense_apply_sliced(int64_t rows, int k, const double *M, int64_t ld, const double *X, double *Y,
+                                   int slices, uint64_t wait_cycles, void *stream) {
+    if (rows <= 0 || k <= 0 || !M || ld < rows || !X || !Y || slices < 2 || slices > 7 || wait_cycles == 0)
+        return pfail(ERR_ARGUMENT, "dense_apply_sliced: invalid argument (slices 2..7, ld >= rows, wait_cycles > 0)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint8_t *plane = nullptr, *scratch = nullptr;
+    int *flag = nullptr;
+    cudaError_t e;
+    if ((e = dev_alloc(&plane, tc_exact_plane_bytes(rows, rows, slices), st)) ||
+        (e = dev_alloc(&scratch, tc_exact_scratch_bytes(rows, k, slices), st)) || (e = dev_alloc(&flag, 1, st))) {
+        dev_free(plane, st);
+        dev_free(scratch, st);
+        return pfail(ERR_MEMORY, "dense_apply_sliced: %s", cudaGetErrorString(e));
+    }
+    int timed_out = 0;
+    if (!(e = cudaMemsetAsync(flag, 0, sizeof(int), st)) && !(e = tc_slice_exact(rows, rows, M, ld, slices, plane, st)))
+        e = tc_exact_product(rows, rows, plane, k, reinterpret_cast<const double2 *>(X), k,
+                             reinterpret_cast<double2 *>(Y), k, slices, scratch, flag, (unsigned long long)wait_cycles,
+                             st);
+    if (!e) e = cudaMemcpyAsync(&timed_out, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    dev_free(plane, st);
+    dev_free(scratch, st);
+    dev_free(flag, st);
+    if (e) return pfail(cuda_status(e), "dense_apply_sliced: %s", cudaGetErrorString(e));
+    if (timed_out) return pfail(ERR_TIMEOUT, "dense_apply_sliced: a bounded wait of the tensor-core product gave up");
+    return OK;
+}
+
 int pcbqs_gb300_to_single(const double *in, float *out, int64_t count, void *stream) {
     if (!in || !out || count < 0) return pfail(ERR_ARGUMENT, "to_single: invalid argument");
     if (!count) return OK;
@@ -1323,6 +1514,7 @@ int pcbqs_gb300_peec_single(pcbqs_gb300_peec *h, const float *Lf, int64_t ldlf, 
                             int64_t ldpf) {
     if (!h || !Lf || ldlf < h->op.ne || (h->op.nn > 0 && (!Pf || ldpf < h->op.nn)))
         return pfail(ERR_ARGUMENT, "peec_single: invalid single-precision matrices");
+    h->op.unpack();
     h->op.Lf = Lf;
     h->op.ldlf = ldlf;
     h->op.Pf = Pf;
@@ -1357,9 +1549,11 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *h, int k, const int32_t *sys_
     opt.captured = h->captured;
     GmresReport rep;
     int steps = 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = refine_batched(h->op, single, M, k, sys_host, reinterpret_cast<const cd *>(b),
-                                   reinterpret_cast<cd *>(x), opt, rep, steps, static_cast<cudaStream_t>(stream));
+                                   reinterpret_cast<cd *>(x), opt, rep, steps, st);
     if (e) return pfail(cuda_status(e), "peec_solve_mixed: %s", cudaGetErrorString(e));
+    if (int status = take_product_timeout(h->op, st, "peec_solve_mixed")) return status;
     if (outer_steps) *outer_steps = steps;
     bool ok = true;
     for (int s = 0; s < k; ++s) {

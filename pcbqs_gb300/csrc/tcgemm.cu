@@ -122,6 +122,153 @@ __global__ void __launch_bounds__(256) k_pack_b(int64_t cols, int k, int kp, int
     }
 }
 
+// ---- the FP64-accurate product (integer slices) ----
+// A value x of a row (column) whose entries are all below 2^e in magnitude is x = 2^(e-7) sum_s a_s 2^(-8s) + r with
+// integer slices |a_s| <= 128 (exact in BF16) and |r| <= 2^(e-7) 2^(-8S-1) after S slices: a_0 = rint(x 2^(7-e)),
+// then each remainder times 256 rounded again. A product of two slices is an integer below 2^14 in magnitude, so a
+// chunk of 256 of them sums exactly in the tensor core's FP32 accumulator; the fold warps add the chunks as 32-bit
+// integers and carry the sum of every level (slice pairs (i, j) of equal i + j, weight 2^(-8(i+j))) into the FP64
+// result. Pairs above level S - 1 are dropped; they weigh less than the representation error.
+constexpr int MAX_SLICES = 7;
+constexpr int MAX_PAIRS = MAX_SLICES * (MAX_SLICES + 1) / 2;
+// the pairs (i, j) in order of level i + j: the first S (S + 1) / 2 are those of S slices
+__constant__ int8_t PAIR_A[MAX_PAIRS] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4, 0, 1, 2, 3, 4, 5, 0, 1, 2, 3, 4, 5, 6};
+__constant__ int8_t PAIR_B[MAX_PAIRS] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0, 4, 3, 2, 1, 0, 5, 4, 3, 2, 1, 0, 6, 5, 4, 3, 2, 1, 0};
+__constant__ int8_t PAIR_LEVEL[MAX_PAIRS] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 4,
+                                             5, 5, 5, 5, 5, 5, 6, 6, 6, 6, 6, 6, 6};
+
+// e such that |x| < 2^e (-1022 for zero and subnormals)
+__device__ __forceinline__ int bound_exponent(double x) {
+    return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1022;
+}
+
+__device__ __forceinline__ void write_slices(double x, int e, int slices, int64_t kp, int64_t t, __nv_bfloat16 *row) {
+    double v = ldexp(x, 7 - e);
+    for (int s = 0; s < slices; ++s) {
+        const double a = rint(v);
+        row[s * kp + t] = __double2bfloat16(a);
+        v = (v - a) * 256.0;
+    }
+}
+
+// M's slice plane (rows x slices x kp, row-major FP64 M with leading dimension ldm) and its row exponents; one
+// block per row: the row's bound exponent, then its slices (zero for kdim <= t < kp).
+__global__ void __launch_bounds__(256) k_slice_rows(int64_t rows, int64_t kdim, int64_t kp, int slices,
+                                                    const double *M, int64_t ldm, __nv_bfloat16 *out, int *row_exp) {
+    __shared__ int part[8];
+    for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const double *src = M + r * ldm;
+        int e = -1022;
+        for (int64_t t = threadIdx.x; t < kdim; t += 256) e = max(e, bound_exponent(src[t]));
+        for (int o = 16; o; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = e;
+        __syncthreads();
+        e = part[0];
+        for (int w = 1; w < 8; ++w) e = max(e, part[w]);
+        __syncthreads();
+        __nv_bfloat16 *row = out + r * kp * slices;
+        for (int64_t t = threadIdx.x; t < kp; t += 256) write_slices(t < kdim ? src[t] : 0.0, e, slices, kp, t, row);
+        if (threadIdx.x == 0) row_exp[r] = e;
+    }
+}
+
+// Column bound exponents of X (kdim x ncols real, row-major, leading dimension ldxr) into col_exp (preset to a value
+// below -1022): 32 columns (one per lane) by a stretch of 256 rows per block.
+__global__ void __launch_bounds__(256) k_column_exponents(int64_t kdim, int64_t ncols, const double *X, int64_t ldxr,
+                                                          int *col_exp) {
+    __shared__ int part[8][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t j = (int64_t)blockIdx.y * 32 + lane;
+    int e = -1022;
+    if (j < ncols)
+        for (int64_t t = (int64_t)blockIdx.x * 256 + w; t < kdim && t < (int64_t)(blockIdx.x + 1) * 256; t += 8)
+            e = max(e, bound_exponent(X[t * ldxr + j]));
+    part[w][lane] = e;
+    __syncthreads();
+    if (w == 0 && j < ncols) {
+        for (int i = 1; i < 8; ++i) e = max(e, part[i][lane]);
+        atomicMax(col_exp + j, e);
+    }
+}
+
+// X's slice plane: plane row j (X's real column j) holds its slices along t, scaled by its column exponent; 32 x 32
+// blocks transposed through shared memory.
+__global__ void __launch_bounds__(256) k_slice_cols(int64_t kdim, int64_t kp, int64_t ncols, int slices,
+                                                    const double *X, int64_t ldxr, const int *col_exp,
+                                                    __nv_bfloat16 *out) {
+    __shared__ double tile[32][33];
+    const int64_t t0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int i = ty; i < 32; i += 8) {
+        const int64_t t = t0 + i, j = j0 + tx;
+        tile[i][tx] = (t < kdim && j < ncols) ? X[t * ldxr + j] : 0.0;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+        const int64_t j = j0 + i;
+        if (j >= ncols) continue;
+        write_slices(tile[tx][i], max(col_exp[j], -1022), slices, kp, t0 + tx, out + j * kp * slices);
+    }
+}
+
+// Y (rows x cols complex128) times 2^(row exponent + column exponent - 14): the slices' scales. A bound exponent
+// of 1025 marks a NaN or infinity in the row or column: its results are NaN.
+__device__ __forceinline__ double scaled(double v, int er, int ec) {
+    return (er > 1024 || ec > 1024) ? __longlong_as_double(0x7ff8000000000000LL) : ldexp(v, er + ec - 14);
+}
+
+__global__ void k_exact_scale(int64_t rows, int64_t cols, double2 *Y, int64_t ldy, const int *row_exp,
+                              const int *col_exp) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows * cols;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / cols, c = i - r * cols;
+        double2 *p = Y + r * ldy + c;
+        double2 v = *p;
+        v.x = scaled(v.x, row_exp[r], max(col_exp[2 * c], -1022));
+        v.y = scaled(v.y, row_exp[r], max(col_exp[2 * c + 1], -1022));
+        *p = v;
+    }
+}
+
+// The real operand's plane (the dense product Y = M X): row r, segment s, position t = part SEG_A[s] of M[r, t] (M
+// row-major FP32, leading dimension ldm); zero for kdim <= t < kp.
+__global__ void __launch_bounds__(256) k_pack_rows(int64_t rows, int64_t kdim, int64_t kp, int terms, const float *M,
+                                                   int64_t ldm, __nv_bfloat16 *out) {
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) {
+        const float *src = M + r * ldm;
+        __nv_bfloat16 *row = out + r * kp * terms;
+        for (int64_t t = (int64_t)blockIdx.x * 256 + threadIdx.x; t < kp; t += (int64_t)gridDim.x * 256) {
+            __nv_bfloat16 h, m, l;
+            split3(t < kdim ? src[t] : 0.f, h, m, l);
+            for (int s = 0; s < terms; ++s) row[s * kp + t] = pick(SEG_A[s], h, m, l);
+        }
+    }
+}
+
+// The right-hand sides' plane: X (kdim x cols complex128, row-major, leading dimension ldx) seen as the real
+// kdim x 2cols matrix Xr; plane row j holds column j of Xr (so rows 2c, 2c + 1 are Re and Im of column c), each
+// value rounded to FP32 and its part SEG_B[s] written in segment s. 32 x 32 blocks transposed through shared memory.
+__global__ void __launch_bounds__(256) k_pack_cols(int64_t kdim, int64_t kp, int64_t ncols, int terms,
+                                                   const double *X, int64_t ldxr, __nv_bfloat16 *out) {
+    __shared__ float tile[32][33];
+    const int64_t t0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int i = ty; i < 32; i += 8) {
+        const int64_t t = t0 + i, j = j0 + tx;
+        tile[i][tx] = (t < kdim && j < ncols) ? (float)X[t * ldxr + j] : 0.f;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+        const int64_t j = j0 + i;
+        if (j >= ncols) continue;
+        const int64_t t = t0 + tx;
+        __nv_bfloat16 h, m, l;
+        split3(tile[tx][i], h, m, l);
+        __nv_bfloat16 *row = out + j * kp * terms;
+        for (int s = 0; s < terms; ++s) row[s * kp + t] = pick(SEG_B[s], h, m, l);
+    }
+}
+
 // ---- tcgen05 / TMA primitives (inline PTX, sm_100 family) ----
 
 // Shared-memory matrix descriptor of a K-major operand tile in the 128-byte swizzle layout that TMA writes with
@@ -180,6 +327,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
@@ -203,12 +360,21 @@ struct TileArgs {
     int64_t rows, cols;          // C's size (complex)
     float2 *C;
     int64_t ldc;
+    double2 *Y;                  // the real-operand product's output (row-major, leading dimension ldy)
+    int64_t ldy;
     int kblocks;                 // K / 64
+    int seg_kblocks;             // the FP64-accurate product: 64-wide K slices per slice segment
     int tiles_m, tiles_n;        // row and column tiles
     int *error;
     unsigned long long wait;
 };
 
+// MODE 0: C -= D into a column-major complex64 C (the complex update); 1: Y = D into a row-major complex128 Y, D's
+// columns 2c, 2c + 1 being column c's real and imaginary parts (the real-operand product); 2: the same Y from
+// integer slices (the FP64-accurate product): K runs over the slice pairs in level order, each pair a segment of
+// seg_kblocks slices of its A and B slice planes, and the fold warps keep 32-bit integer sums that they carry into Y
+// (FP64) at every change of level, before 511 chunks could overflow them, and at the end.
+template <int MODE>
 __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant__ CUtensorMap map_a,
                                                           const __grid_constant__ CUtensorMap map_b, TileArgs args) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -276,8 +442,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
                 }
                 mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
                 const uint32_t a_dst = ring + s * STAGE_BYTES, b_dst = a_dst + A_BYTES;
-                tma_load_2d(a_dst, &map_a, kb * BK, (int)m0, smem_addr(&full[s]));
-                tma_load_2d(b_dst, &map_b, kb * BK, n_tile * BN, smem_addr(&full[s]));
+                int xa = kb * BK, xb = kb * BK;
+                if (MODE == 2) {
+                    const int p = kb / args.seg_kblocks, off = (kb - p * args.seg_kblocks) * BK;
+                    xa = PAIR_A[p] * args.seg_kblocks * BK + off;
+                    xb = PAIR_B[p] * args.seg_kblocks * BK + off;
+                }
+                tma_load_2d(a_dst, &map_a, xa, (int)m0, smem_addr(&full[s]));
+                tma_load_2d(b_dst, &map_b, xb, n_tile * BN, smem_addr(&full[s]));
                 issued_last[s] = kb;
             }
             if (!ok) {
@@ -329,32 +501,94 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
         // column being 256 contiguous bytes
         const int q = warp & 3, h = warp >> 2;
         const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + h * (BN / 2);
-        float acc[BN / 2];
+        float acc[BN / 2];        // MODE 2: the bits of 32-bit integer sums
 #pragma unroll
         for (int i = 0; i < BN / 2; ++i) acc[i] = 0.f;
         bool good = true;
-        for (int c = 0; c < nchunks; ++c) {
-            const int buf = c & 1;
-            const bool landed = wait_bounded(&cfull[buf], (c >> 1) & 1, args.wait, abort);
-            if (!__all_sync(0xffffffffu, landed)) {
-                good = false;
-                break;
-            }
-            fence_after_sync();
+        if (MODE == 2) {
+            // runs of chunks of one level (at most 511: |sum| < 2^31), each carried into Y after its last chunk
+            bool stored = false;  // Y holds this tile's earlier runs
+            for (int c = 0; c < nchunks && good;) {
+                const int level = PAIR_LEVEL[(c * CHUNK) / args.seg_kblocks];
+                int end = c + 1;
+                while (end < nchunks && end - c < 511 && PAIR_LEVEL[(end * CHUNK) / args.seg_kblocks] == level) ++end;
+                // an integer-valued FP32 sum |v| <= 2^22 as an integer: the bits of v + 1.5 * 2^23 are
+                // v + 0x4B400000; the sums carry that offset once per chunk (wrapping), removed at the carry
+                const unsigned offset = (unsigned)(end - c) * 0x4B400000u;
+                for (; c < end; ++c) {
+                    const int buf = c & 1;
+                    const bool landed = wait_bounded(&cfull[buf], (c >> 1) & 1, args.wait, abort);
+                    if (!__all_sync(0xffffffffu, landed)) {
+                        good = false;
+                        break;
+                    }
+                    fence_after_sync();
 #pragma unroll
-            for (int j = 0; j < BN / 2 / 32; ++j) {
-                uint32_t r[32];
-                tmem_ld32(taddr + buf * BN + j * 32, r);
+                    for (int j = 0; j < BN / 2 / 16; ++j) {
+                        uint32_t r[16];
+                        tmem_ld16(taddr + buf * BN + j * 16, r);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) acc[j * 32 + i] += __uint_as_float(r[i]);
+                        for (int i = 0; i < 16; ++i)
+                            acc[j * 16 + i] = __int_as_float(__float_as_int(acc[j * 16 + i]) +
+                                                             __float_as_int(__uint_as_float(r[i]) + 12582912.0f));
+                    }
+                    fence_before_sync();
+                    mbar_arrive(&cempty[buf]);
+                }
+                if (!good) break;
+                const int64_t row = m0 + q * 32 + lane;
+                const int64_t c0 = (int64_t)n_tile * (BN / 2) + h * (BN / 4);
+                const double w = __longlong_as_double((long long)(1023 - 8 * level) << 52);
+                if (row < args.rows) {
+                    double2 *base = args.Y + row * args.ldy + c0;
+#pragma unroll
+                    for (int j = 0; j < BN / 4; ++j)
+                        if (c0 + j < args.cols) {
+                            double2 v = stored ? base[j] : make_double2(0.0, 0.0);
+                            v.x = fma((double)(int)(__float_as_uint(acc[2 * j]) - offset), w, v.x);
+                            v.y = fma((double)(int)(__float_as_uint(acc[2 * j + 1]) - offset), w, v.y);
+                            base[j] = v;
+                        }
+                }
+#pragma unroll
+                for (int i = 0; i < BN / 2; ++i) acc[i] = 0.f;
+                stored = true;
             }
-            fence_before_sync();
-            mbar_arrive(&cempty[buf]);
+        } else {
+            for (int c = 0; c < nchunks; ++c) {
+                const int buf = c & 1;
+                const bool landed = wait_bounded(&cfull[buf], (c >> 1) & 1, args.wait, abort);
+                if (!__all_sync(0xffffffffu, landed)) {
+                    good = false;
+                    break;
+                }
+                fence_after_sync();
+#pragma unroll
+                for (int j = 0; j < BN / 2 / 32; ++j) {
+                    uint32_t r[32];
+                    tmem_ld32(taddr + buf * BN + j * 32, r);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) acc[j * 32 + i] += __uint_as_float(r[i]);
+                }
+                fence_before_sync();
+                mbar_arrive(&cempty[buf]);
+            }
         }
         if (!good) {
             if (lane == 0) {
                 *abort = 1;
                 atomicExch(args.error, ERR_TIMEOUT);
+            }
+        } else if (MODE == 2) {
+            // Y complete (its scales applied by k_exact_scale)
+        } else if (!*abort && MODE == 1) {
+            const int64_t row = m0 + q * 32 + lane;
+            const int64_t c0 = (int64_t)n_tile * (BN / 2) + h * (BN / 4);
+            if (row < args.rows) {
+                double2 *base = args.Y + row * args.ldy;
+#pragma unroll
+                for (int j = 0; j < BN / 4; ++j)
+                    if (c0 + j < args.cols) base[c0 + j] = make_double2(acc[2 * j], acc[2 * j + 1]);
             }
         } else if (!*abort) {
             const int64_t row = m0 + q * 32 + lane;
@@ -417,6 +651,25 @@ bool plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int 
 
 int64_t padded_k(int k) { return ((int64_t)k + KPAD - 1) / KPAD * KPAD; }
 int64_t align1k(int64_t b) { return (b + 1023) / 1024 * 1024; }
+// the real product's inner dimension per segment: a whole number of 64-wide K slices
+int64_t padded_real(int64_t kdim) { return (kdim + BK - 1) / BK * BK; }
+// the FP64-accurate product's segment: whole chunks, so no chunk mixes two slice pairs
+int64_t padded_exact(int64_t kdim) { return (kdim + CHUNK * BK - 1) / (CHUNK * BK) * (CHUNK * BK); }
+
+cudaError_t configure() {
+    static bool configured[64] = {};
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e) return e;
+    if (device < 64 && !configured[device]) {
+        if ((e = cudaFuncSetAttribute(k_tc_update<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
+            (e = cudaFuncSetAttribute(k_tc_update<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
+            (e = cudaFuncSetAttribute(k_tc_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
+            return e;
+        configured[device] = true;
+    }
+    return cudaSuccess;
+}
 
 }  // namespace
 
@@ -432,15 +685,8 @@ cudaError_t tc_update_c64(int64_t rows, int64_t cols, int k, const float2 *A, in
     if ((terms != 3 && terms != 6) || !A || !B || !C || !scratch || !error || lda < rows || ldb < k || ldc < rows ||
         rows > (int64_t)0x7fffff00 || 2 * cols > (int64_t)0x7fffff00)
         return cudaErrorInvalidValue;
-    static bool configured[64] = {};
-    int device = 0;
-    cudaError_t e = cudaGetDevice(&device);
+    cudaError_t e = configure();
     if (e) return e;
-    if (device < 64 && !configured[device]) {
-        if ((e = cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
-            return e;
-        configured[device] = true;
-    }
     const int kp = (int)padded_k(k);
     const int64_t K = (int64_t)terms * 2 * kp;
     auto *pa = static_cast<__nv_bfloat162 *>(scratch);
@@ -462,15 +708,149 @@ cudaError_t tc_update_c64(int64_t rows, int64_t cols, int k, const float2 *A, in
     args.cols = cols;
     args.C = C;
     args.ldc = ldc;
+    args.Y = nullptr;
+    args.ldy = 0;
     args.kblocks = (int)(K / BK);
+    args.seg_kblocks = 1;
     args.tiles_m = (int)((rows + BM - 1) / BM);
     args.tiles_n = (int)((2 * cols + BN - 1) / BN);
     args.error = error;
     args.wait = wait_cycles;
     const int64_t tiles = (int64_t)args.tiles_m * args.tiles_n;
     if (tiles > 0x7fffffff) return cudaErrorInvalidValue;
-    k_tc_update<<<(unsigned)tiles, THREADS, SMEM, stream>>>(ma, mb, args);
+    k_tc_update<0><<<(unsigned)tiles, THREADS, SMEM, stream>>>(ma, mb, args);
     note_launches(1);
+    return cudaGetLastError();
+}
+
+size_t tc_real_plane_bytes(int64_t rows, int64_t kdim, int terms) {
+    return (size_t)align1k(rows * terms * padded_real(kdim) * 2);
+}
+
+size_t tc_real_scratch_bytes(int64_t kdim, int64_t cols, int terms) {
+    return (size_t)align1k(2 * cols * terms * padded_real(kdim) * 2);
+}
+
+cudaError_t tc_pack_real(int64_t rows, int64_t kdim, const float *M, int64_t ldm, int terms, void *plane,
+                         cudaStream_t stream) {
+    if (rows <= 0 || kdim <= 0) return cudaSuccess;
+    if ((terms != 3 && terms != 6) || !M || !plane || ldm < kdim) return cudaErrorInvalidValue;
+    const int64_t kp = padded_real(kdim);
+    const dim3 grid((unsigned)std::min<int64_t>((kp + 255) / 256, 64), (unsigned)std::min<int64_t>(rows, 65535));
+    k_pack_rows<<<grid, 256, 0, stream>>>(rows, kdim, kp, terms, M, ldm, static_cast<__nv_bfloat16 *>(plane));
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_real_product(int64_t rows, int64_t kdim, const void *plane, int64_t cols, const double2 *X,
+                            int64_t ldx, double2 *Y, int64_t ldy, int terms, void *scratch, int *error,
+                            unsigned long long wait_cycles, cudaStream_t stream) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    if ((terms != 3 && terms != 6) || kdim <= 0 || !plane || !X || !Y || !scratch || !error || ldx < cols ||
+        ldy < cols || rows > (int64_t)0x7fffff00 || 2 * cols > (int64_t)0x7fffff00 || (2 * cols + 31) / 32 > 65535)
+        return cudaErrorInvalidValue;
+    cudaError_t e = configure();
+    if (e) return e;
+    const int64_t kp = padded_real(kdim), K = terms * kp;
+    {
+        const dim3 grid((unsigned)(kp / 32), (unsigned)((2 * cols + 31) / 32));
+        k_pack_cols<<<grid, 256, 0, stream>>>(kdim, kp, 2 * cols, terms, reinterpret_cast<const double *>(X),
+                                              2 * ldx, static_cast<__nv_bfloat16 *>(scratch));
+        note_launches(1);
+    }
+    CUtensorMap ma, mb;
+    if (!plane_map(&ma, plane, rows, K, BM) || !plane_map(&mb, scratch, 2 * cols, K, BN))
+        return cudaErrorNotSupported;
+    TileArgs args;
+    args.rows = rows;
+    args.cols = cols;
+    args.C = nullptr;
+    args.ldc = 0;
+    args.Y = Y;
+    args.ldy = ldy;
+    args.kblocks = (int)(K / BK);
+    args.seg_kblocks = 1;
+    args.tiles_m = (int)((rows + BM - 1) / BM);
+    args.tiles_n = (int)((2 * cols + BN - 1) / BN);
+    args.error = error;
+    args.wait = wait_cycles;
+    const int64_t tiles = (int64_t)args.tiles_m * args.tiles_n;
+    if (tiles > 0x7fffffff || K / BK > 0x7fffffff) return cudaErrorInvalidValue;
+    k_tc_update<1><<<(unsigned)tiles, THREADS, SMEM, stream>>>(ma, mb, args);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+size_t tc_exact_plane_bytes(int64_t rows, int64_t kdim, int slices) {
+    return (size_t)(align1k(rows * slices * padded_exact(kdim) * 2) + align1k(rows * 4));
+}
+
+size_t tc_exact_scratch_bytes(int64_t kdim, int64_t cols, int slices) {
+    return (size_t)(align1k(2 * cols * slices * padded_exact(kdim) * 2) + align1k(2 * cols * 4));
+}
+
+cudaError_t tc_slice_exact(int64_t rows, int64_t kdim, const double *M, int64_t ldm, int slices, void *plane,
+                           cudaStream_t stream) {
+    if (rows <= 0 || kdim <= 0) return cudaSuccess;
+    if (slices < 2 || slices > MAX_SLICES || !M || !plane || ldm < kdim) return cudaErrorInvalidValue;
+    const int64_t kp = padded_exact(kdim);
+    auto *out = static_cast<__nv_bfloat16 *>(plane);
+    int *row_exp = reinterpret_cast<int *>(static_cast<uint8_t *>(plane) + align1k(rows * slices * kp * 2));
+    k_slice_rows<<<(unsigned)std::min<int64_t>(rows, 1 << 20), 256, 0, stream>>>(rows, kdim, kp, slices, M, ldm, out,
+                                                                                row_exp);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_exact_product(int64_t rows, int64_t kdim, const void *plane, int64_t cols, const double2 *X,
+                             int64_t ldx, double2 *Y, int64_t ldy, int slices, void *scratch, int *error,
+                             unsigned long long wait_cycles, cudaStream_t stream) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    const int64_t kp = padded_exact(kdim);
+    const int pairs = slices * (slices + 1) / 2;
+    if (slices < 2 || slices > MAX_SLICES || kdim <= 0 || !plane || !X || !Y || !scratch || !error || ldx < cols ||
+        ldy < cols || rows > (int64_t)0x7fffff00 || 2 * cols > (int64_t)0x7fffff00 ||
+        (2 * cols + 31) / 32 > 65535 || (int64_t)slices * kp > (int64_t)0x7fffff00 ||
+        (int64_t)pairs * (kp / BK) > (int64_t)0x7fffffff)
+        return cudaErrorInvalidValue;
+    cudaError_t e = configure();
+    if (e) return e;
+    const int64_t ncols = 2 * cols, K = (int64_t)slices * kp;
+    auto *bplane = static_cast<__nv_bfloat16 *>(scratch);
+    int *col_exp = reinterpret_cast<int *>(static_cast<uint8_t *>(scratch) + align1k(ncols * slices * kp * 2));
+    const int *row_exp =
+        reinterpret_cast<const int *>(static_cast<const uint8_t *>(plane) + align1k(rows * slices * kp * 2));
+    const double *Xr = reinterpret_cast<const double *>(X);
+    if ((e = cudaMemsetAsync(col_exp, 0x80, (size_t)ncols * sizeof(int), stream))) return e;   // below -1022
+    {
+        const dim3 grid((unsigned)std::min<int64_t>((kdim + 255) / 256, 65535), (unsigned)((ncols + 31) / 32));
+        k_column_exponents<<<grid, 256, 0, stream>>>(std::min<int64_t>(kdim, (int64_t)grid.x * 256), ncols, Xr,
+                                                     2 * ldx, col_exp);
+        const dim3 g2((unsigned)(kp / 32), (unsigned)((ncols + 31) / 32));
+        k_slice_cols<<<g2, 256, 0, stream>>>(kdim, kp, ncols, slices, Xr, 2 * ldx, col_exp, bplane);
+        note_launches(2);
+    }
+    CUtensorMap ma, mb;
+    if (!plane_map(&ma, plane, rows, K, BM) || !plane_map(&mb, bplane, ncols, K, BN)) return cudaErrorNotSupported;
+    TileArgs args;
+    args.rows = rows;
+    args.cols = cols;
+    args.C = nullptr;
+    args.ldc = 0;
+    args.Y = Y;
+    args.ldy = ldy;
+    args.kblocks = (int)(pairs * (kp / BK));
+    args.seg_kblocks = (int)(kp / BK);
+    args.tiles_m = (int)((rows + BM - 1) / BM);
+    args.tiles_n = (int)((ncols + BN - 1) / BN);
+    args.error = error;
+    args.wait = wait_cycles;
+    const int64_t tiles = (int64_t)args.tiles_m * args.tiles_n;
+    if (tiles > 0x7fffffff) return cudaErrorInvalidValue;
+    k_tc_update<2><<<(unsigned)tiles, THREADS, SMEM, stream>>>(ma, mb, args);
+    k_exact_scale<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((rows * cols + 255) / 256, 152 * 16)), 256, 0,
+                    stream>>>(rows, cols, Y, ldy, row_exp, col_exp);
+    note_launches(2);
     return cudaGetLastError();
 }
 

@@ -21,4 +21,34 @@ cudaError_t tc_update_c64(int64_t rows, int64_t cols, int k, const float2 *A, in
                           int64_t ldb, float2 *C, int64_t ldc, int terms, void *scratch, bool a_packed,
                           int *error, unsigned long long wait_cycles, cudaStream_t stream);
 
+// The dense product over many right-hand sides on the same GEMM: Y (rows x cols complex128) = M (rows x kdim, real)
+// X (kdim x cols complex128), X and Y row-major with leading dimensions ldx, ldy (in complex elements). M is
+// packed once into its BF16 part plane (tc_pack_real into tc_real_plane_bytes) and reused by every product; each
+// product packs X (rounded to FP32) into `scratch` (tc_real_scratch_bytes) and runs one real GEMM of inner
+// dimension terms · kdim against X's real and imaginary columns side by side, writing Y whole. The result carries
+// the relative error of the parts kept (terms 3: about 2^-16; 6: FP32's). `error`, `wait_cycles` and `stream` as in
+// tc_update_c64.
+size_t tc_real_plane_bytes(int64_t rows, int64_t kdim, int terms);
+size_t tc_real_scratch_bytes(int64_t kdim, int64_t cols, int terms);
+cudaError_t tc_pack_real(int64_t rows, int64_t kdim, const float *M, int64_t ldm, int terms, void *plane,
+                         cudaStream_t stream);
+cudaError_t tc_real_product(int64_t rows, int64_t kdim, const void *plane, int64_t cols, const double2 *X,
+                            int64_t ldx, double2 *Y, int64_t ldy, int terms, void *scratch, int *error,
+                            unsigned long long wait_cycles, cudaStream_t stream);
+
+// The same product to FP64's accuracy from a real FP64 M and complex128 X: every row of M and every real column of X
+// is cut into `slices` (2..7) integer slices of 8 bits under its own power-of-two scale, so each slice is exact in
+// BF16 and every slice product sums exactly in FP32 over the tensor core's 256-long chunks; the levels of slice
+// pairs are carried into Y in FP64. The truncation error is about 2^(-8 slices) of max_t |M[r, t]| times
+// sum_t |X[t, c]| (slices 6: about 2^-48). M's plane (tc_slice_exact into tc_exact_plane_bytes) holds its slices and
+// row exponents; `scratch` (tc_exact_scratch_bytes) X's. Non-finite entries make their rows or columns of Y
+// non-finite.
+size_t tc_exact_plane_bytes(int64_t rows, int64_t kdim, int slices);
+size_t tc_exact_scratch_bytes(int64_t kdim, int64_t cols, int slices);
+cudaError_t tc_slice_exact(int64_t rows, int64_t kdim, const double *M, int64_t ldm, int slices, void *plane,
+                           cudaStream_t stream);
+cudaError_t tc_exact_product(int64_t rows, int64_t kdim, const void *plane, int64_t cols, const double2 *X,
+                             int64_t ldx, double2 *Y, int64_t ldy, int slices, void *scratch, int *error,
+                             unsigned long long wait_cycles, cudaStream_t stream);
+
 }  // namespace pq

@@ -510,8 +510,11 @@ class PeecModel(PeecTopology):
     FACTOR_MATH = {'fp32': 0, 'bf16x9': 1, 'bf16x9-blocked': 2, 'fp32-blocked': 3, 'tc3-blocked': 4,
                    'tc6-blocked': 5}
 
+    PRODUCT = {'fp32': 0, 'tc3': 3, 'tc6': 6}
+    FP64_PRODUCT = {'fp64': 0, 'sliced5': 5, 'sliced6': 6, 'sliced7': 7}
+
     def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='tc6-blocked', anchors=None,
-              captured=False):
+              captured=False, product='tc3', fp64_product=None):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
 
         precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
@@ -528,7 +531,13 @@ class PeecModel(PeecTopology):
         at its middle frequency (default: one factor per frequency). Every column still reaches the tolerance of
         its own frequency's FP64 system; farther from the anchor it takes more iterations. captured=True: each GMRES
         restart cycle is one CUDA graph launch (its Arnoldi steps in a device-controlled conditional loop, no host
-        synchronization between steps; pcbqs_gb300_peec_set_captured), with the same results."""
+        synchronization between steps; pcbqs_gb300_peec_set_captured), with the same results. product (mixed only):
+        the inner dense products over 16 or more columns on the tensor cores with three ('tc3', the default) or six
+        ('tc6') BF16 part products, or 'fp32' on the CUDA cores throughout (pcbqs_gb300_peec_set_product); the FP64
+        refinement holds the answer to the same tolerance either way. fp64_product: the FP64 operator's dense
+        products over 4 or more columns (the mixed solve's outer residuals, the FP64 GMRES): 'fp64' on the FP64 pipe,
+        or 'sliced6' (5, 7) on the tensor cores from integer slices at FP64's accuracy
+        (pcbqs_gb300_peec_set_fp64_product); default 'sliced6' for mixed=True, 'fp64' (the plain path) otherwise."""
         if self.L is None:
             self.assemble()
         f = np.atleast_1d(np.asarray(freqs, float))
@@ -538,6 +547,12 @@ class PeecModel(PeecTopology):
             raise ValueError(f'precondition must be one of {sorted(self.PRECONDITIONERS)}')
         if factor_math not in self.FACTOR_MATH:
             raise ValueError(f'factor_math must be one of {sorted(self.FACTOR_MATH)}')
+        if product not in self.PRODUCT:
+            raise ValueError(f'product must be one of {sorted(self.PRODUCT)}')
+        if fp64_product is None:
+            fp64_product = 'sliced6' if mixed else 'fp64'
+        if fp64_product not in self.FP64_PRODUCT:
+            raise ValueError(f'fp64_product must be one of {sorted(self.FP64_PRODUCT)}')
         nf = len(f)
         if anchors is None:
             anchors = nf
@@ -573,6 +588,8 @@ class PeecModel(PeecTopology):
             updates[:] += (a.value, b.value, c.value)
         try:
             _lib.check(lib.pcbqs_gb300_peec_set_captured(handle, int(bool(captured))), lib)
+            _lib.check(lib.pcbqs_gb300_peec_set_product(handle, self.PRODUCT[product]), lib)
+            _lib.check(lib.pcbqs_gb300_peec_set_fp64_product(handle, self.FP64_PRODUCT[fp64_product]), lib)
             t1 = time.perf_counter()
             if mode == 2:
                 # the first complex64 factorization depends only on L, P and the frequency: it runs on a side

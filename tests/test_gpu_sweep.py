@@ -48,3 +48,35 @@ def test_sweep_16_ports_64_frequencies_matches_reference(device_library):
             err = np.abs(res.impedance[fi] - Zr).max() / np.abs(Zr).max()
             print(f'{f:.4g} Hz: port Z error {err:.2e}')
             assert err < 1e-6, err
+
+
+def test_tensor_core_inner_products_match_the_fp32_ones(device_library):
+    """Nine frequencies x 2 ports = 18 columns in one batch: the mixed refinement's inner products run on the
+    tensor cores (16 or more columns). With three or six BF16 parts or the FP32 CUDA-core product, and with the
+    outer FP64 residuals on the FP64 pipe or from integer slices on the tensor cores, every column reaches 1e-8 on
+    its FP64 system and the port impedances agree with each other and with the reference at its three frequencies;
+    the captured cycles repeat the host-driven ones bit for bit on the tensor-core path too."""
+    from conftest import GOLDEN
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel
+    freqs = np.geomspace(1e5, 1e7, 9)
+    model = PeecModel(Board.load('strip'))
+    model.assemble(mixed=True)
+    runs = {p: model.solve(freqs, precondition='lu32', mixed=True, anchors=1, product=p, fp64_product='fp64')
+            for p in ('fp32', 'tc3', 'tc6')}
+    runs['tc3+sliced6'] = model.solve(freqs, precondition='lu32', mixed=True, anchors=1, product='tc3',
+                                      fp64_product='sliced6')
+    graph = model.solve(freqs, precondition='lu32', mixed=True, anchors=1, product='tc3', fp64_product='fp64',
+                        captured=True)
+    assert np.array_equal(graph.impedance, runs['tc3'].impedance)
+    assert np.array_equal(graph.iterations, runs['tc3'].iterations)
+    Zf = runs['fp32'].impedance
+    with np.load(GOLDEN / 'peec_strip.npz') as g:
+        Zr = g['Z']
+    for p, res in runs.items():
+        assert (res.residual <= 1e-8).all(), (p, res.residual.max())
+        assert np.abs(res.impedance - Zf).max() / np.abs(Zf).max() < 1e-7, p
+        err = np.abs(res.impedance[::4] - Zr).max() / np.abs(Zr).max()
+        print(f'{p}: inner iterations {res.iterations.max()}, outer {res.timings.get("outer_steps")}, '
+              f'error vs reference {err:.2e}')
+        assert err < 1e-6, (p, err)

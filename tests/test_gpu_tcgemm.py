@@ -96,3 +96,181 @@ def test_complex_update_bounded_wait_returns_timeout(device_library):
     exact = c.to(torch.complex128) - a.to(torch.complex128) @ b.to(torch.complex128)
     scale = torch.linalg.norm(a.abs().double() @ b.abs().double() + c.abs().double()).item()
     assert torch.linalg.norm(ct.T.to(torch.complex128) - exact).item() / scale < TOL[6]
+
+
+# ---- pcbqs_gb300_dense_apply_tensor: Y = M X for a real M and complex128 X on the same GEMM ----
+
+def _apply_tensor(lib, M, X, terms, wait=1 << 32):
+    import torch
+    rows, ld = M.shape[0], M.stride(0)
+    Y = torch.full_like(X, float('nan'))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    status = lib.pcbqs_gb300_dense_apply_tensor(rows, X.shape[1], M.data_ptr(), ld, X.data_ptr(), Y.data_ptr(),
+                                                terms, wait, stream)
+    return status, Y
+
+
+# relative to |M| |X|: three parts about 2^-16 per product, six FP32's (plus X's rounding to FP32)
+APPLY_TOL = {3: 1e-4, 6: 1e-6}
+
+
+@pytest.mark.parametrize('terms', [3, 6])
+@pytest.mark.parametrize('rows,k', [(1, 1), (100, 16), (700, 33), (1000, 128), (4099, 130), (2500, 300)])
+def test_dense_apply_tensor_matches_complex128(device_library, rows, k, terms):
+    """The mixed solve's inner products over many right-hand sides: a symmetric FP32 M (leading dimension above
+    its size) against complex128 X, to the parts' accuracy, and against the FP32 CUDA-core product."""
+    import torch
+    from pcbqs_gb300 import _lib
+    g = torch.Generator(device='cuda').manual_seed(rows * 11 + k + terms)
+    A = torch.randn(rows, rows, device='cuda', generator=g)
+    store = torch.randn(rows, rows + 7, device='cuda', generator=g)
+    store[:, :rows] = A + A.T
+    M = store[:, :rows]
+    X = torch.complex(torch.randn(rows, k, device='cuda', generator=g, dtype=torch.float64),
+                      torch.randn(rows, k, device='cuda', generator=g, dtype=torch.float64))
+    status, Y = _apply_tensor(device_library, store, X, terms)
+    _lib.check(status, device_library)
+    Md = M.double()
+    exact = torch.complex(Md @ X.real, Md @ X.imag)
+    scale = torch.linalg.norm(torch.complex(Md.abs() @ X.real.abs(), Md.abs() @ X.imag.abs())).item()
+    err = torch.linalg.norm(Y - exact).item() / scale
+    single = torch.empty_like(X)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(device_library.pcbqs_gb300_dense_apply_single(rows, k, store.data_ptr(), store.stride(0), X.data_ptr(),
+                                                              single.data_ptr(), stream), device_library)
+    fp32 = torch.linalg.norm(single - exact).item() / scale
+    print(f'apply {rows} x {k} terms {terms}: error {err:.3e} of |M||X|, FP32 CUDA-core product {fp32:.3e}')
+    assert err < APPLY_TOL[terms], err
+
+
+@pytest.mark.parametrize('terms', [3, 6])
+def test_dense_apply_tensor_exact_on_small_integers(device_library, terms):
+    """Small integers are exact in BF16 and their sums exact in FP32: the product equals the exact one bit for bit,
+    so every tile, row, column and K slice (3000 is not a multiple of 64 or 128) lands where it belongs."""
+    import torch
+    from pcbqs_gb300 import _lib
+    g = torch.Generator(device='cuda').manual_seed(17 + terms)
+    rows, k = 3000, 150
+    A = torch.randint(-8, 9, (rows, rows), device='cuda', generator=g).float()
+    M = (A + A.T).contiguous()
+    ints = lambda: torch.randint(-8, 9, (rows, k), device='cuda', generator=g).double()
+    X = torch.complex(ints(), ints())
+    status, Y = _apply_tensor(device_library, M, X, terms)
+    _lib.check(status, device_library)
+    Md = M.double()
+    assert torch.equal(Y, torch.complex(Md @ X.real, Md @ X.imag))
+
+
+def test_dense_apply_tensor_bounded_wait_returns_timeout(device_library):
+    import torch
+    from pcbqs_gb300 import _lib
+    g = torch.Generator(device='cuda').manual_seed(9)
+    M = torch.randn(1024, 1024, device='cuda', generator=g)
+    X = torch.complex(torch.randn(1024, 64, device='cuda', generator=g, dtype=torch.float64),
+                      torch.randn(1024, 64, device='cuda', generator=g, dtype=torch.float64))
+    status, _ = _apply_tensor(device_library, M, X, 3, wait=1)
+    assert status == _lib.ERR_TIMEOUT, status
+    torch.cuda.synchronize()
+    status, Y = _apply_tensor(device_library, M, X, 3)
+    assert status == 0
+    Md = M.double()
+    exact = torch.complex(Md @ X.real, Md @ X.imag)
+    scale = torch.linalg.norm(torch.complex(Md.abs() @ X.real.abs(), Md.abs() @ X.imag.abs())).item()
+    assert torch.linalg.norm(Y - exact).item() / scale < APPLY_TOL[3]
+
+
+# ---- pcbqs_gb300_dense_apply_sliced: the FP64 product from integer slices on the same GEMM ----
+
+def _apply_sliced(lib, M, X, slices, wait=1 << 32):
+    import torch
+    Y = torch.full_like(X, float('nan'))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    status = lib.pcbqs_gb300_dense_apply_sliced(M.shape[0], X.shape[1], M.data_ptr(), M.stride(0), X.data_ptr(),
+                                                Y.data_ptr(), slices, wait, stream)
+    return status, Y
+
+
+def _wide_range(rows, g):
+    """A symmetric FP64 matrix whose entries span many binades (decaying off the diagonal, as L and P do)."""
+    import torch
+    i = torch.arange(rows, device='cuda', dtype=torch.float64)
+    decay = 1.0 / (1.0 + (i[:, None] - i[None, :]).abs())
+    A = torch.randn(rows, rows, device='cuda', generator=g, dtype=torch.float64) * decay
+    A = A + A.T
+    A.diagonal().add_(4.0)
+    return A * 1e-7
+
+
+@pytest.mark.parametrize('slices', [5, 6, 7])
+@pytest.mark.parametrize('rows,k', [(1, 1), (100, 4), (700, 33), (1000, 128), (3000, 130)])
+def test_dense_apply_sliced_matches_fp64(device_library, rows, k, slices):
+    """Errors within 2^(4 - 8 slices) of max_t |M[r,t]| sum_t |X[t,c]| per entry. Relative to |M| |X| that bound
+    grows by about the ratio of a row's largest entry times sum |X| to sum |M| |X| (hundreds for this decaying
+    matrix): seven slices are within FP64's own rounding, six within 1e-12, far below the 1e-8 residuals they
+    check."""
+    import torch
+    from pcbqs_gb300 import _lib
+    g = torch.Generator(device='cuda').manual_seed(rows * 13 + k + slices)
+    store = torch.randn(rows, rows + 3, device='cuda', generator=g, dtype=torch.float64)
+    store[:, :rows] = _wide_range(rows, g)
+    M = store[:, :rows]
+    X = torch.complex(torch.randn(rows, k, device='cuda', generator=g, dtype=torch.float64),
+                      torch.randn(rows, k, device='cuda', generator=g, dtype=torch.float64)) * 3e4
+    status, Y = _apply_sliced(device_library, store, X, slices)
+    _lib.check(status, device_library)
+    exact = torch.complex(M @ X.real, M @ X.imag)
+    rowmax = M.abs().amax(1, keepdim=True)
+    bound_re = rowmax * X.real.abs().sum(0, keepdim=True)
+    bound_im = rowmax * X.imag.abs().sum(0, keepdim=True)
+    err = max(((Y.real - exact.real).abs() / bound_re).max().item(),
+              ((Y.imag - exact.imag).abs() / bound_im).max().item())
+    scale = torch.linalg.norm(torch.complex(M.abs() @ X.real.abs(), M.abs() @ X.imag.abs())).item()
+    normwise = torch.linalg.norm(Y - exact).item() / scale
+    print(f'sliced {rows} x {k}, {slices} slices: {err:.3e} of the slice bound, {normwise:.3e} of |M||X|')
+    assert err <= 2.0 ** (4 - 8 * slices), err
+    assert normwise < {5: 1e-10, 6: 1e-12, 7: 1e-14}[slices], normwise
+
+
+@pytest.mark.parametrize('slices', [3, 6])
+def test_dense_apply_sliced_exact_on_integers(device_library, slices):
+    """Integers of 14 bits are whole in two slices, so with three slices or more no slice pair they need is dropped:
+    the product equals FP64's bit for bit, so every tile, row, column, slice pair and level carry lands where it
+    belongs (3000 is not a multiple of 128 or 256)."""
+    import torch
+    from pcbqs_gb300 import _lib
+    g = torch.Generator(device='cuda').manual_seed(29 + slices)
+    rows, k = 3000, 150
+    A = torch.randint(-8000, 8001, (rows, rows), device='cuda', generator=g).double()
+    M = (A + A.T).contiguous()
+    ints = lambda: torch.randint(-8000, 8001, (rows, k), device='cuda', generator=g).double()
+    X = torch.complex(ints(), ints())
+    status, Y = _apply_sliced(device_library, M, X, slices)
+    _lib.check(status, device_library)
+    assert torch.equal(Y, torch.complex(M @ X.real, M @ X.imag))
+
+
+def test_dense_apply_sliced_non_finite_and_timeout(device_library):
+    """A NaN in one column of X makes that column of Y NaN and leaves the others exact to the bound; a wait limit
+    too short for the first copy returns status 6, and the next call is correct."""
+    import torch
+    from pcbqs_gb300 import _lib
+    g = torch.Generator(device='cuda').manual_seed(31)
+    rows, k = 1024, 64
+    M = _wide_range(rows, g)
+    X = torch.complex(torch.randn(rows, k, device='cuda', generator=g, dtype=torch.float64),
+                      torch.randn(rows, k, device='cuda', generator=g, dtype=torch.float64))
+    exact = torch.complex(M @ X.real, M @ X.imag)
+    bad = X.clone()
+    bad[7, 3] = complex(float('nan'), 1.0)
+    status, Y = _apply_sliced(device_library, M, bad, 6)
+    _lib.check(status, device_library)
+    assert torch.isnan(Y[:, 3].real).all() and torch.isfinite(Y[:, 3].imag).all()
+    keep = [c for c in range(k) if c != 3]
+    scale = torch.linalg.norm(exact[:, keep]).item()
+    assert torch.linalg.norm(Y[:, keep] - exact[:, keep]).item() / scale < 1e-11
+    status, _ = _apply_sliced(device_library, M, X, 6, wait=1)
+    assert status == _lib.ERR_TIMEOUT, status
+    torch.cuda.synchronize()
+    status, Y = _apply_sliced(device_library, M, X, 6)
+    assert status == 0
+    assert torch.linalg.norm(Y - exact).item() / torch.linalg.norm(exact).item() < 1e-11
