@@ -142,13 +142,42 @@ __device__ __forceinline__ int bound_exponent(double x) {
     return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1022;
 }
 
-__device__ __forceinline__ void write_slices(double x, int e, int slices, int64_t kp, int64_t t, __nv_bfloat16 *row) {
-    double v = ldexp(x, 7 - e);
-    for (int s = 0; s < slices; ++s) {
-        const double a = rint(v);
-        row[s * kp + t] = __double2bfloat16(a);
-        v = (v - a) * 256.0;
+// x's slices under bound exponent e, most significant first, in integer arithmetic on x's bits (the FP64 pipe is
+// slow): q = x 2^(7 - e + 8 (slices - 1)) rounded to an integer (|q| <= 2^(7 + 8 (slices - 1))), then q's balanced
+// base-256 digits (the lower ones in [-128, 127], the leading one in [-128, 128]). NaN and infinity give zeros (their
+// rows and columns are marked by their exponent 1025).
+__device__ __forceinline__ void slice_digits(double x, int e, int slices, int (&d)[MAX_SLICES]) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((bits >> 52) & 0x7ff);
+    long long q = 0;
+    if (E != 0x7ff) {
+        unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
+        if (E) m |= 1ull << 52;
+        const int ex = E ? E - 1075 : -1074;                   // x = +-m 2^ex
+        const int sh = -(ex + 7 - e + 8 * (slices - 1));       // q = m 2^-sh
+        unsigned long long mag;
+        if (sh <= 0) mag = m << (-sh);                         // sh >= -2 since |x| < 2^e and slices <= 7
+        else if (sh >= 60) mag = 0;                            // m < 2^53: rounds to zero
+        else mag = (m + (1ull << (sh - 1))) >> sh;
+        q = (bits >> 63) ? -(long long)mag : (long long)mag;
     }
+#pragma unroll
+    for (int s = MAX_SLICES - 1; s >= 1; --s) {
+        if (s < slices) {
+            const long long digit = ((q + 128) & 255) - 128;
+            d[s] = (int)digit;
+            q = (q - digit) / 256;                             // exact
+        }
+    }
+    d[0] = (int)q;
+}
+
+__device__ __forceinline__ void write_slices(double x, int e, int slices, int64_t kp, int64_t t, __nv_bfloat16 *row) {
+    int d[MAX_SLICES];
+    slice_digits(x, e, slices, d);
+#pragma unroll
+    for (int s = 0; s < MAX_SLICES; ++s)
+        if (s < slices) row[s * kp + t] = __int2bfloat16_rn(d[s]);
 }
 
 // M's slice plane (rows x slices x kp, row-major FP64 M with leading dimension ldm) and its row exponents; one
@@ -166,8 +195,19 @@ __global__ void __launch_bounds__(256) k_slice_rows(int64_t rows, int64_t kdim, 
         e = part[0];
         for (int w = 1; w < 8; ++w) e = max(e, part[w]);
         __syncthreads();
-        __nv_bfloat16 *row = out + r * kp * slices;
-        for (int64_t t = threadIdx.x; t < kp; t += 256) write_slices(t < kdim ? src[t] : 0.0, e, slices, kp, t, row);
+        // two neighbouring entries per thread, stored as BF16 pairs (kp is even)
+        __nv_bfloat162 *row = reinterpret_cast<__nv_bfloat162 *>(out + r * kp * slices);
+        const int64_t half = kp / 2;
+        for (int64_t u = threadIdx.x; u < half; u += 256) {
+            const int64_t t = 2 * u;
+            int d0[MAX_SLICES], d1[MAX_SLICES];
+            slice_digits(t < kdim ? src[t] : 0.0, e, slices, d0);
+            slice_digits(t + 1 < kdim ? src[t + 1] : 0.0, e, slices, d1);
+#pragma unroll
+            for (int s = 0; s < MAX_SLICES; ++s)
+                if (s < slices)
+                    row[s * half + u] = __halves2bfloat162(__int2bfloat16_rn(d0[s]), __int2bfloat16_rn(d1[s]));
+        }
         if (threadIdx.x == 0) row_exp[r] = e;
     }
 }
