@@ -122,6 +122,58 @@ __global__ void __launch_bounds__(256) k_pack_b(int64_t cols, int k, int kp, int
     }
 }
 
+// ---- the row-major complex update (the triangular solves' products) ----
+// A's plane from a row-major complex64 A (row r contiguous in t): the same layout as k_pack_a.
+__global__ void __launch_bounds__(256) k_pack_a_rows(int64_t rows, int k, int kp, int terms, const float2 *A,
+                                                     int64_t lda, __nv_bfloat162 *out) {
+    const int64_t K2 = kp;
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) {
+        const float2 *src = A + r * lda;
+        __nv_bfloat162 *row = out + r * (K2 * terms);
+        for (int t = blockIdx.x * 256 + threadIdx.x; t < kp; t += gridDim.x * 256) {
+            const float2 v = t < k ? src[t] : make_float2(0.f, 0.f);
+            __nv_bfloat16 rh, rm, rl, ih, im, il;
+            split3(v.x, rh, rm, rl);
+            split3(v.y, ih, im, il);
+            for (int s = 0; s < terms; ++s) {
+                const int p = SEG_A[s];
+                row[s * K2 + t] = __halves2bfloat162(pick(p, rh, rm, rl), pick(p, ih, im, il));
+            }
+        }
+    }
+}
+
+// B's plane from a row-major complex64 B (k x cols, leading dimension ldb): the layout of k_pack_b, each 32 x 32
+// block transposed through shared memory.
+__global__ void __launch_bounds__(256) k_pack_b_rows(int64_t cols, int k, int kp, int terms, const float2 *B,
+                                                     int64_t ldb, __nv_bfloat162 *out) {
+    __shared__ float2 tile[32][33];
+    const int64_t t0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int i = ty; i < 32; i += 8) {
+        const int64_t t = t0 + i, j = j0 + tx;
+        tile[i][tx] = (t < k && j < cols) ? B[t * ldb + j] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int64_t K2 = kp;
+    for (int i = ty; i < 32; i += 8) {
+        const int64_t j = j0 + i;
+        if (j >= cols) continue;
+        const int64_t t = t0 + tx;
+        const float2 v = tile[tx][i];
+        __nv_bfloat16 rh, rm, rl, ih, im, il;
+        split3(v.x, rh, rm, rl);
+        split3(v.y, ih, im, il);
+        __nv_bfloat162 *re = out + (2 * j) * (K2 * terms), *imr = re + K2 * terms;
+        for (int s = 0; s < terms; ++s) {
+            const int q = SEG_B[s];
+            const __nv_bfloat16 br = pick(q, rh, rm, rl), bi = pick(q, ih, im, il);
+            re[s * K2 + t] = __halves2bfloat162(br, __hneg(bi));
+            imr[s * K2 + t] = __halves2bfloat162(bi, br);
+        }
+    }
+}
+
 // ---- the FP64-accurate product (integer slices) ----
 // A value x of a row (column) whose entries are all below 2^e in magnitude is x = 2^(e-7) sum_s a_s 2^(-8s) + r with
 // integer slices |a_s| <= 128 (exact in BF16) and |r| <= 2^(e-7) 2^(-8S-1) after S slices: a_0 = rint(x 2^(7-e)),
@@ -409,7 +461,7 @@ struct TileArgs {
     unsigned long long wait;
 };
 
-// MODE 0: C -= D into a column-major complex64 C (the complex update); 1: Y = D into a row-major complex128 Y, D's
+// MODE 0: C -= D into a column-major complex64 C (the complex update); 3: the same into a row-major C; 1: Y = D into a row-major complex128 Y, D's
 // columns 2c, 2c + 1 being column c's real and imaginary parts (the real-operand product); 2: the same Y from
 // integer slices (the FP64-accurate product): K runs over the slice pairs in level order, each pair a segment of
 // seg_kblocks slices of its A and B slice planes, and the fold warps keep 32-bit integer sums that they carry into Y
@@ -621,6 +673,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
             }
         } else if (MODE == 2) {
             // Y complete (its scales applied by k_exact_scale)
+        } else if (!*abort && MODE == 3) {
+            const int64_t row = m0 + q * 32 + lane;
+            const int64_t c0 = (int64_t)n_tile * (BN / 2) + h * (BN / 4);
+            if (row < args.rows) {
+                float2 *base = args.C + row * args.ldc;
+#pragma unroll
+                for (int j = 0; j < BN / 4; ++j)
+                    if (c0 + j < args.cols) {
+                        float2 v = base[c0 + j];
+                        v.x -= acc[2 * j];
+                        v.y -= acc[2 * j + 1];
+                        base[c0 + j] = v;
+                    }
+            }
         } else if (!*abort && MODE == 1) {
             const int64_t row = m0 + q * 32 + lane;
             const int64_t c0 = (int64_t)n_tile * (BN / 2) + h * (BN / 4);
@@ -704,7 +770,8 @@ cudaError_t configure() {
     if (device < 64 && !configured[device]) {
         if ((e = cudaFuncSetAttribute(k_tc_update<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
             (e = cudaFuncSetAttribute(k_tc_update<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
-            (e = cudaFuncSetAttribute(k_tc_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
+            (e = cudaFuncSetAttribute(k_tc_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
+            (e = cudaFuncSetAttribute(k_tc_update<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
             return e;
         configured[device] = true;
     }
@@ -891,6 +958,66 @@ cudaError_t tc_exact_product(int64_t rows, int64_t kdim, const void *plane, int6
     k_exact_scale<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((rows * cols + 255) / 256, 152 * 16)), 256, 0,
                     stream>>>(rows, cols, Y, ldy, row_exp, col_exp);
     note_launches(2);
+    return cudaGetLastError();
+}
+
+size_t tc_rows_plane_bytes(int64_t rows, int k, int terms) {
+    return (size_t)align1k(rows * terms * 2 * padded_k(k) * 2);
+}
+
+size_t tc_rows_row_bytes(int k, int terms) { return (size_t)(terms * 2 * padded_k(k) * 2); }
+
+size_t tc_rows_scratch_bytes(int64_t cols, int k, int terms) {
+    return (size_t)align1k(2 * cols * terms * 2 * padded_k(k) * 2);
+}
+
+cudaError_t tc_pack_rows_c64(int64_t rows, int k, const float2 *A, int64_t lda, int terms, void *plane,
+                             cudaStream_t stream) {
+    if (rows <= 0 || k <= 0) return cudaSuccess;
+    if ((terms != 3 && terms != 6) || !A || !plane || lda < k) return cudaErrorInvalidValue;
+    const int kp = (int)padded_k(k);
+    const dim3 grid((unsigned)std::max(1, std::min((kp + 255) / 256, 64)), (unsigned)std::min<int64_t>(rows, 65535));
+    k_pack_a_rows<<<grid, 256, 0, stream>>>(rows, k, kp, terms, A, lda, static_cast<__nv_bfloat162 *>(plane));
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_update_rows_c64(int64_t rows, int64_t cols, int k, const void *aplane, const float2 *B, int64_t ldb,
+                               float2 *C, int64_t ldc, int terms, void *scratch, int *error,
+                               unsigned long long wait_cycles, cudaStream_t stream) {
+    if (rows <= 0 || cols <= 0 || k <= 0) return cudaSuccess;
+    if ((terms != 3 && terms != 6) || !aplane || !B || !C || !scratch || !error || ldb < cols || ldc < cols ||
+        rows > (int64_t)0x7fffff00 || 2 * cols > (int64_t)0x7fffff00 || (cols + 31) / 32 > 65535)
+        return cudaErrorInvalidValue;
+    cudaError_t e = configure();
+    if (e) return e;
+    const int kp = (int)padded_k(k);
+    const int64_t K = (int64_t)terms * 2 * kp;
+    auto *pb = static_cast<__nv_bfloat162 *>(scratch);
+    {
+        const dim3 grid((unsigned)(kp / 32), (unsigned)((cols + 31) / 32));
+        k_pack_b_rows<<<grid, 256, 0, stream>>>(cols, k, kp, terms, B, ldb, pb);
+        note_launches(1);
+    }
+    CUtensorMap ma, mb;
+    if (!plane_map(&ma, aplane, rows, K, BM) || !plane_map(&mb, pb, 2 * cols, K, BN)) return cudaErrorNotSupported;
+    TileArgs args;
+    args.rows = rows;
+    args.cols = cols;
+    args.C = C;
+    args.ldc = ldc;
+    args.Y = nullptr;
+    args.ldy = 0;
+    args.kblocks = (int)(K / BK);
+    args.seg_kblocks = 1;
+    args.tiles_m = (int)((rows + BM - 1) / BM);
+    args.tiles_n = (int)((2 * cols + BN - 1) / BN);
+    args.error = error;
+    args.wait = wait_cycles;
+    const int64_t tiles = (int64_t)args.tiles_m * args.tiles_n;
+    if (tiles > 0x7fffffff) return cudaErrorInvalidValue;
+    k_tc_update<3><<<(unsigned)tiles, THREADS, SMEM, stream>>>(ma, mb, args);
+    note_launches(1);
     return cudaGetLastError();
 }
 

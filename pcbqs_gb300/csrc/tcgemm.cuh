@@ -21,6 +21,20 @@ cudaError_t tc_update_c64(int64_t rows, int64_t cols, int k, const float2 *A, in
                           int64_t ldb, float2 *C, int64_t ldc, int terms, void *scratch, bool a_packed,
                           int *error, unsigned long long wait_cycles, cudaStream_t stream);
 
+// The same update with row-major operands and A packed once for many updates (the triangular solves' products with
+// a fixed factor): C (rows x cols, row-major complex64, leading dimension ldc) -= A B, A's plane (rows x k, packed
+// by tc_pack_rows_c64 from a row-major complex64 A with leading dimension lda, into tc_rows_plane_bytes; a plane of
+// more rows may be used from any row on, its rows being tc_rows_row_bytes(k, terms) bytes apart) and B
+// (k x cols, row-major complex64, leading dimension ldb) packed into `scratch` (tc_rows_scratch_bytes) per call.
+size_t tc_rows_plane_bytes(int64_t rows, int k, int terms);
+size_t tc_rows_row_bytes(int k, int terms);
+size_t tc_rows_scratch_bytes(int64_t cols, int k, int terms);
+cudaError_t tc_pack_rows_c64(int64_t rows, int k, const float2 *A, int64_t lda, int terms, void *plane,
+                             cudaStream_t stream);
+cudaError_t tc_update_rows_c64(int64_t rows, int64_t cols, int k, const void *aplane, const float2 *B, int64_t ldb,
+                               float2 *C, int64_t ldc, int terms, void *scratch, int *error,
+                               unsigned long long wait_cycles, cudaStream_t stream);
+
 // The dense product over many right-hand sides on the same GEMM: Y (rows x cols complex128) = M (rows x kdim, real)
 // X (kdim x cols complex128), X and Y row-major with leading dimensions ldx, ldy (in complex elements). M is
 // packed once into its BF16 part plane (tc_pack_real into tc_real_plane_bytes) and reused by every product; each

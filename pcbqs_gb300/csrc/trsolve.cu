@@ -556,128 +556,140 @@ int TriSolver::method_for(int k) const {
     return it == plans.end() ? -1 : it->second.method;
 }
 
-// The diagonal TRI_PANEL-row block of the blocked solve, for 8 right-hand sides per CTA (grid kpad / 8), in the
-// original view: forward (lower = true) U^T_II y_I = b_I with U^T lower, backward L^T_II z_I = y_I with L^T unit
-// upper, T[r][c] = lu[r n + c]. The block is walked in TRI_BLOCK-row sub-blocks (forward first to last, backward
-// last to first): acc = rhs_s - T[s, solved] x[solved], the solved part staged in shared memory and T's rows in
-// 64-column tiles, then x_s = inv_s acc with the precomputed inverse of the sub-block's diagonal block.
-constexpr int DIAG_COLS = 8, DIAG_TILE = 64, DIAG_THREADS = 256;
-constexpr size_t DIAG_SMEM = sizeof(float2) * ((size_t)TRI_PANEL * DIAG_COLS + (size_t)B * DIAG_TILE);
-
-__global__ void __launch_bounds__(DIAG_THREADS) k_diag_block(const float2 *lu, int64_t n, int64_t I0, int nb,
-                                                             const float2 *inv, const float2 *rhs, float2 *x, int kp,
-                                                             int lower) {
-    extern __shared__ float2 diag_smem[];
-    float2 *xs = diag_smem;                                  // [TRI_PANEL][DIAG_COLS] the block's solution
-    float2 *ut = diag_smem + (size_t)TRI_PANEL * DIAG_COLS;  // [B][DIAG_TILE] a tile of T's rows
-    const int c0 = blockIdx.x * DIAG_COLS;
-    const int t = threadIdx.x;
-    const int r = t >> 1, ch = (t & 1) * 4;                  // this thread's row of the sub-block and 4 columns
-    const int nsub = (nb + B - 1) / B;
-    for (int q = 0; q < nsub; ++q) {
-        const int s = lower ? q : nsub - 1 - q;
-        const int s0 = s * B, rows = min(B, nb - s0);
-        // solved columns of T's rows: forward [0, s0), backward [s0 + rows, nb)
-        const int j0 = lower ? 0 : s0 + rows, j1 = lower ? s0 : nb;
-        float2 acc[4];
+// C (R x Cn) = A X (mode 0) or C -= A X (mode 1) for row-major complex64 A (R x Kd, leading dimension lda), X
+// (Kd x Cn) and C: the blocked solve's steps inside a diagonal block. 32 x 32 outputs per CTA (each thread one
+// column of four rows), K in tiles of 32 staged in shared memory, each tile's partial sums added to the running
+// sums (rounding errors grow with the tile count rather than the whole inner dimension).
+__global__ void __launch_bounds__(256) k_cgemm_small(int R, int Cn, int Kd, const float2 *A, int64_t lda,
+                                                     const float2 *X, int64_t ldx, float2 *C, int64_t ldc, int mode) {
+    __shared__ float2 As[32][33], Xs[32][33];
+    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    float2 acc[4];
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
-            acc[c] = r < rows ? rhs[(I0 + s0 + r) * kp + c0 + ch + c] : make_float2(0.f, 0.f);
-        for (int jt = j0; jt < j1; jt += DIAG_TILE) {
-            const int w = min(DIAG_TILE, j1 - jt);
-            __syncthreads();
-            for (int e = t; e < B * DIAG_TILE; e += DIAG_THREADS) {
-                const int rr = e / DIAG_TILE, jj = e % DIAG_TILE;
-                ut[e] = (rr < rows && jj < w) ? lu[(I0 + s0 + rr) * n + I0 + jt + jj] : make_float2(0.f, 0.f);
-            }
-            __syncthreads();
-            if (r < rows) {
-                // the tile's partial sums first, then into the running sums: rounding errors grow with the tile
-                // length and the tile count rather than with the whole row
-                float2 part[4] = {};
-                for (int jj = 0; jj < w; ++jj) {
-                    const float2 u = ut[r * DIAG_TILE + jj];
+    for (int i = 0; i < 4; ++i) acc[i] = make_float2(0.f, 0.f);
+    for (int k0 = 0; k0 < Kd; k0 += 32) {
+        for (int i = ty; i < 32; i += 8) {
+            As[i][tx] = (r0 + i < R && k0 + tx < Kd) ? A[(int64_t)(r0 + i) * lda + k0 + tx] : make_float2(0.f, 0.f);
+            Xs[i][tx] = (k0 + i < Kd && c0 + tx < Cn) ? X[(int64_t)(k0 + i) * ldx + c0 + tx] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        float2 part[4];
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const float2 v = xs[(jt + jj) * DIAG_COLS + ch + c];
-                        part[c].x += u.x * v.x - u.y * v.y;
-                        part[c].y += u.x * v.y + u.y * v.x;
-                    }
-                }
+        for (int i = 0; i < 4; ++i) part[i] = make_float2(0.f, 0.f);
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) {
+            const float2 v = Xs[j][tx];
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    acc[c].x -= part[c].x;
-                    acc[c].y -= part[c].y;
-                }
+            for (int i = 0; i < 4; ++i) {
+                const float2 a = As[ty + 8 * i][j];
+                part[i].x += a.x * v.x - a.y * v.y;
+                part[i].y += a.x * v.y + a.y * v.x;
             }
         }
-        // acc staged in the sub-block's rows of xs, then x_s = inv_s acc (inv row-major B x B)
-        __syncthreads();
-        if (r < B)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) xs[(s0 + r) * DIAG_COLS + ch + c] = r < rows ? acc[c] : make_float2(0.f, 0.f);
+        for (int i = 0; i < 4; ++i) {
+            acc[i].x += part[i].x;
+            acc[i].y += part[i].y;
+        }
         __syncthreads();
-        float2 out[4] = {};
-        const float2 *iv = inv + ((size_t)(I0 / B + s) * B + r) * B;
-        if (r < rows)
-            for (int b = 0; b < rows; ++b) {
-                const float2 m = iv[b];
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const float2 v = xs[(s0 + b) * DIAG_COLS + ch + c];
-                    out[c].x += m.x * v.x - m.y * v.y;
-                    out[c].y += m.x * v.y + m.y * v.x;
-                }
-            }
-        __syncthreads();
-        if (r < rows)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) xs[(s0 + r) * DIAG_COLS + ch + c] = out[c];
     }
-    __syncthreads();
-    for (int e = t; e < nb * DIAG_COLS; e += DIAG_THREADS)
-        x[(I0 + e / DIAG_COLS) * kp + c0 + e % DIAG_COLS] = xs[e];
+    const int c = c0 + tx;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = r0 + ty + 8 * i;
+        if (r < R && c < Cn) {
+            float2 *p = C + (int64_t)r * ldc + c;
+            if (mode == 0) {
+                *p = acc[i];
+            } else {
+                float2 v = *p;
+                v.x -= acc[i].x;
+                v.y -= acc[i].y;
+                *p = v;
+            }
+        }
+    }
 }
 
-// The blocked solve for many right-hand sides. Each TRI_PANEL-row step solves its diagonal block (k_diag_block)
-// and subtracts the block's product with the off-diagonal panel from the rows still to come, on the tcgen05 update
-// with six BF16 part products (FP32's accuracy), in the transposed view: the work arrays (n, kpad) row-major are the
-// column-major kpad x n matrices B^T, Y^T, Z^T, and with T[r][c] = lu[r n + c] (A = U^T L^T P^T read row-major) the
-// forward update b_rest^T -= y_I^T U_(I, rest) takes U_(I, rest) as the column-major nb x rest block at
-// lu + I1 n + I0 (leading dimension n), the backward y_above^T -= z_I^T L_(I, above) the block at lu + I0. The
-// factor is read once per sweep for all columns instead of once per 8.
+static void launch_cgemm_small(int R, int Cn, int Kd, const float2 *A, int64_t lda, const float2 *X, int64_t ldx,
+                               float2 *C, int64_t ldc, int mode, cudaStream_t s) {
+    if (R <= 0 || Cn <= 0) return;
+    const dim3 grid((unsigned)((Cn + 31) / 32), (unsigned)((R + 31) / 32));
+    k_cgemm_small<<<grid, 256, 0, s>>>(R, Cn, Kd, A, lda, X, ldx, C, ldc, mode);
+}
+
+// The blocked solve for many right-hand sides. Each TRI_PANEL-row step solves its diagonal block
+// (TRI_BLOCK-row sub-blocks in order: x_s = inv_s b_s with the precomputed inverse, then the panel's rows still to
+// come lose T[rows, s] x_s; k_cgemm_small) and subtracts the block's product with the off-diagonal panel from the
+// rows still to come, on the tcgen05 update
+// with `update_terms` BF16 part products (six: FP32's accuracy). With T[r][c] = lu[r n + c] (A = U^T L^T P^T read
+// row-major) and the work arrays (n, kpad) row-major, the forward update b_rest -= T[rest, I] y_I and the backward
+// y_above -= T[above, I] z_I both take rows of T's column panel I, which is packed once per factor (all n rows) into
+// its BF16 part plane: each sweep then reads the factor's planes once for all columns, and packs only the solved
+// block of the right-hand sides per step.
 cudaError_t TriSolver::solve_blocked(Plan *p, int k, const cd *in, cd *out, cudaStream_t s) {
     cudaError_t e;
     const int kp = p->kpad;
+    const int64_t steps = (n + TRI_PANEL - 1) / TRI_PANEL;
+    auto panel_width = [&](int64_t I) { return (int)(std::min<int64_t>((I + 1) * TRI_PANEL, n) - I * TRI_PANEL); };
+    if (!panel_planes) {
+        size_t bytes = 0;
+        for (int64_t I = 0; I < steps; ++I) bytes += (size_t)n * tc_rows_row_bytes(panel_width(I), update_terms);
+        if ((e = pool_alloc(&panel_planes, bytes, s))) return e;
+        uint8_t *at = static_cast<uint8_t *>(panel_planes);
+        for (int64_t I = 0; I < steps; ++I) {
+            if ((e = tc_pack_rows_c64(n, panel_width(I), lu + I * TRI_PANEL, n, update_terms, at, s))) return e;
+            at += (size_t)n * tc_rows_row_bytes(panel_width(I), update_terms);
+        }
+    }
     if (!p->planes) {
-        if ((e = cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DIAG_SMEM)) ||
-            (e = pool_alloc(&p->planes, tc_update_scratch_bytes(kp, n, TRI_PANEL, 6), s)) ||
+        if ((e = pool_alloc(&p->planes, tc_rows_scratch_bytes(kp, TRI_PANEL, update_terms), s)) ||
             (e = pool_alloc_n(&p->update_error, 1, s)) || (e = cudaMemsetAsync(p->update_error, 0, sizeof(int), s)))
             return e;
     }
     k_tri_in<<<blocks_for(n * kp), 256, 0, s>>>(n, k, kp, in, p->b);
-    const int64_t steps = (n + TRI_PANEL - 1) / TRI_PANEL;
     const unsigned long long wait = wait_cycles();
-    const unsigned diag_grid = (unsigned)(kp / DIAG_COLS);
     int launches = 2;
-    // forward: U^T y = b, block by block; the rest of b then loses the block's product (y^T U = b^T transposed)
+    std::vector<const uint8_t *> panel((size_t)steps);
+    {
+        const uint8_t *at = static_cast<const uint8_t *>(panel_planes);
+        for (int64_t I = 0; I < steps; ++I) {
+            panel[I] = at;
+            at += (size_t)n * tc_rows_row_bytes(panel_width(I), update_terms);
+        }
+    }
+    // forward: U^T y = b, block by block; the rest of b then loses T[rest, I] y_I
     for (int64_t I = 0; I < steps; ++I) {
         const int64_t I0 = I * TRI_PANEL, I1 = std::min<int64_t>(I0 + TRI_PANEL, n);
         const int nb = (int)(I1 - I0);
-        k_diag_block<<<diag_grid, DIAG_THREADS, DIAG_SMEM, s>>>(lu, n, I0, nb, inv_lower, p->b, p->y, kp, 1);
-        ++launches;
-        if (I1 < n && (e = tc_update_c64(kp, n - I1, nb, p->y + I0 * kp, kp, lu + I1 * n + I0, n, p->b + I1 * kp, kp,
-                                         6, p->planes, false, p->update_error, wait, s)))
+        for (int64_t g0 = I0; g0 < I1; g0 += B) {
+            const int rows = (int)std::min<int64_t>(B, I1 - g0);
+            launch_cgemm_small(rows, kp, rows, inv_lower + (g0 / B) * B * B, B, p->b + g0 * kp, kp, p->y + g0 * kp, kp,
+                               0, s);
+            launch_cgemm_small((int)(I1 - g0 - rows), kp, rows, lu + (g0 + rows) * n + g0, n, p->y + g0 * kp, kp,
+                               p->b + (g0 + rows) * kp, kp, 1, s);
+            launches += 2;
+        }
+        if (I1 < n && (e = tc_update_rows_c64(n - I1, kp, nb, panel[I] + I1 * tc_rows_row_bytes(nb, update_terms),
+                                              p->y + I0 * kp, kp, p->b + I1 * kp, kp, update_terms, p->planes,
+                                              p->update_error, wait, s)))
             return e;
     }
-    // backward: L^T z = y, last block first; the rows above then lose the block's product (z^T L = y^T)
+    // backward: L^T z = y, last block first; the rows above then lose T[above, I] z_I
     for (int64_t I = steps - 1; I >= 0; --I) {
         const int64_t I0 = I * TRI_PANEL, I1 = std::min<int64_t>(I0 + TRI_PANEL, n);
         const int nb = (int)(I1 - I0);
-        k_diag_block<<<diag_grid, DIAG_THREADS, DIAG_SMEM, s>>>(lu, n, I0, nb, inv_upper, p->y, p->z, kp, 0);
-        ++launches;
-        if (I0 > 0 && (e = tc_update_c64(kp, I0, nb, p->z + I0 * kp, kp, lu + I0, n, p->y, kp, 6, p->planes, false,
-                                         p->update_error, wait, s)))
+        for (int64_t g0 = I0 + (nb - 1) / B * B; g0 >= I0; g0 -= B) {
+            const int rows = (int)std::min<int64_t>(B, I1 - g0);
+            launch_cgemm_small(rows, kp, rows, inv_upper + (g0 / B) * B * B, B, p->y + g0 * kp, kp, p->z + g0 * kp, kp,
+                               0, s);
+            launch_cgemm_small((int)(g0 - I0), kp, rows, lu + I0 * n + g0, n, p->z + g0 * kp, kp, p->y + I0 * kp, kp,
+                               1, s);
+            launches += 2;
+        }
+        if (I0 > 0 && (e = tc_update_rows_c64(I0, kp, nb, panel[I], p->z + I0 * kp, kp, p->y, kp, update_terms,
+                                              p->planes, p->update_error, wait, s)))
             return e;
     }
     k_tri_out<<<blocks_for(n * k), 256, 0, s>>>(n, k, kp, p->z, gather, out);
@@ -756,6 +768,8 @@ void TriSolver::release() {
 
     plans.clear();
     method_by_bucket.clear();
+    pool_free(panel_planes, nullptr);
+    panel_planes = nullptr;
     pool_free(inv_lower, nullptr);
     pool_free(inv_upper, nullptr);
     pool_free(gather, nullptr);

@@ -36,6 +36,10 @@ struct TriSolver {
         int *update_error = nullptr;  // its updates' timeout flag
     };
     std::map<int, Plan> plans;
+    // The blocked solve's factor panels (TRI_PANEL columns of T = the row-major view of lu, all n rows each) as
+    // BF16 part planes of `update_terms` products, packed at its first use and kept with the factor.
+    int update_terms = 6;
+    void *panel_planes = nullptr;
     std::map<int, int> method_by_bucket;     // the timed choice per power-of-two column bucket
     int grid = 0;                     // co-resident thread blocks of the sweep kernel
 
