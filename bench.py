@@ -515,6 +515,29 @@ def kernel_case(spec):
     CASES[name](*values)
 
 
+BLOCKED_LU_MATH = {'fp32-blocked': 0, 'bf16x9-blocked': 1, 'tc3-blocked': 2, 'tc6-blocked': 3}
+
+
+def autotune_lu_panel(lib, n, args, widths=(1024, 2048, 3072)):
+    """The blocked LU's panel width for this order and math, from the tuning file (PCBQS_GB300_TUNE_FILE) when it
+    holds one, else timed now (pcbqs_gb300_tune_lu_panel, outside the timed region); peec_factor then uses it."""
+    import ctypes
+    import torch
+    from pcbqs_gb300 import _lib
+    math = BLOCKED_LU_MATH.get(args.factor_math)
+    if math is None:
+        return None
+    v = ctypes.c_int32()
+    key = f'lu_panel n={n} math={math}'.encode()
+    if lib.pcbqs_gb300_tune_lookup(key, ctypes.byref(v)) == 0:
+        return dict(lu_panel=v.value, source='tuning file')
+    w = np.array(widths, np.int32)
+    t0 = time.perf_counter()
+    _lib.check(lib.pcbqs_gb300_tune_lu_panel(n, math, _lib.ptr(w, ctypes.c_int32), len(w), ctypes.byref(v),
+                                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
+    return dict(lu_panel=v.value, candidates=list(widths), source='timed', tuning_s=round(time.perf_counter() - t0, 2))
+
+
 def main():
     args = parse()
     if args.case:
@@ -543,6 +566,7 @@ def main():
         model.assemble(mixed=mode_mixed)
         return model.solve([freq], precondition=args.precondition, mixed=mode_mixed, factor_math=args.factor_math)
 
+    autotune = autotune_lu_panel(lib, model.n, args) if args.precondition == 'lu32' else None
     for _ in range(args.warmup):
         result = step()
     torch.cuda.synchronize()
@@ -646,6 +670,7 @@ def main():
                 host_s={k: round(statistics.median(t.get(k, 0) for t in timings), 3)
                         for k in ('equilibrium_s', 'potential_solve_s', 'operator_setup_s', 'rhs_s', 'solve_s')},
                 gpu_launches=int(launches),
+                autotune=autotune,
                 clocks=clock_info,
                 roofline=(factor_roofline(model, timings, args.factor_math)
                           if args.precondition == 'lu32' else fill_roofline(model, head_fill_ms, mixed, peaks)),
@@ -678,6 +703,7 @@ def main():
             torch.cuda.empty_cache()
             model = PeecModel(Board.load(args.sweep_board), device=local)
         model.assemble(mixed=mixed)
+        sweep_tune = autotune_lu_panel(lib, model.n, args)
         torch.cuda.synchronize()
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record()
@@ -698,6 +724,7 @@ def main():
                 sweep_err = errs or None
         line['sweep'] = dict(board=args.sweep_board, unknowns=model.n, captured_cycles=True,
                              inner_product=args.product, outer_steps=rs.timings.get('outer_steps'),
+                             autotune=sweep_tune,
                              port_z_max_rel_err_vs_reference=sweep_err,
                              frequencies=len(fs), range_hz=[1e3, 1e8], ports=len(model.names),
                              columns=int(its.size), anchors=rs.timings['factorizations'],

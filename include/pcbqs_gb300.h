@@ -280,6 +280,24 @@ int pcbqs_gb300_peec_set_product(pcbqs_gb300_peec *op, int terms);
  * once), 0 (the default) on the FP64 pipe. No counterpart in the reference, whose products are NumPy's FP64
  * (src/pcbqs/peec_iterative.py:253-256). */
 int pcbqs_gb300_peec_set_fp64_product(pcbqs_gb300_peec *op, int slices);
+
+/* The autotuner. Choices timed at first use are remembered per device (name and SM count) and problem size: the FP32
+ * dense product's shape ("dense_f32 rows=R"), the triangular solves' method per column bucket ("trisolve n=N
+ * columns=C": 0 streaming sweeps, 1 blocked) and the blocked LU's panel width ("lu_panel n=N math=M", timed only by
+ * pcbqs_gb300_tune_lu_panel). pcbqs_gb300_tune_file sets a file (null or "": none) whose entries are merged in at
+ * once and which is rewritten after every new choice; without a call, PCBQS_GB300_TUNE_FILE names it. No
+ * counterpart in the reference (its solvers have no tunable shapes). */
+int pcbqs_gb300_tune_file(const char *path);
+/* The choice recorded for `key` on the current device; status 1 when none is. */
+int pcbqs_gb300_tune_lookup(const char *key, int32_t *value);
+/* Records a choice for `key` on the current device (as a timing would; e.g. to pin one by hand). */
+int pcbqs_gb300_tune_record(const char *key, int32_t value);
+int64_t pcbqs_gb300_tune_count(void);
+void pcbqs_gb300_tune_clear(void);
+/* Times pcbqs_gb300_lu_factor_c64's blocked factorization (math 0..3) of a synthetic diagonally dominant n x n
+ * complex64 matrix with each panel width and records the fastest (*best) for pcbqs_gb300_peec_factor. Allocates
+ * n^2 complex64 and synchronizes `stream`. */
+int pcbqs_gb300_tune_lu_panel(int64_t n, int math, const int32_t *widths, int count, int32_t *best, void *stream);
 /* The tcgen05 trailing updates of the last pcbqs_gb300_peec_factor with math 4 or 5: their summed CUDA-event time
  * (ms, on the factorization's stream), complex flops (8 rows cols k each) and count; zeros after any other math.
  * No counterpart in the reference; for the roofline of the update kernel. */

@@ -122,6 +122,13 @@ PROTOTYPES = {
     'pcbqs_gb300_peec_set_captured': (ctypes.c_int, [c_void_p, ctypes.c_int]),
     'pcbqs_gb300_peec_set_product': (ctypes.c_int, [c_void_p, ctypes.c_int]),
     'pcbqs_gb300_peec_set_fp64_product': (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    'pcbqs_gb300_tune_file': (ctypes.c_int, [ctypes.c_char_p]),
+    'pcbqs_gb300_tune_lookup': (ctypes.c_int, [ctypes.c_char_p, c_int32_p]),
+    'pcbqs_gb300_tune_count': (ctypes.c_int64, []),
+    'pcbqs_gb300_tune_record': (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32]),
+    'pcbqs_gb300_tune_clear': (None, []),
+    'pcbqs_gb300_tune_lu_panel': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int, c_int32_p, ctypes.c_int, c_int32_p,
+                                                 c_void_p]),
     'pcbqs_gb300_peec_factor_updates': (ctypes.c_int, [c_void_p, ctypes.POINTER(ctypes.c_double),
                                                        ctypes.POINTER(ctypes.c_double), c_int32_p]),
     'pcbqs_gb300_via_inductance': (ctypes.c_int, [ctypes.c_int64, c_void_p, ctypes.c_double, c_void_p,

@@ -15,6 +15,7 @@
 //                 row U12; the next panel's columns updated (GEMM into scratch, k_trailing_subtract); (event: the
 //                 next panel may start); triangular solve and update of the remaining columns.
 #include <algorithm>
+#include <string>
 #include <cstdio>
 #include <vector>
 
@@ -24,6 +25,7 @@
 #include "../../include/pcbqs_gb300.h"
 #include "common.cuh"
 #include "factor.cuh"
+#include "tune.cuh"
 #include "pool.cuh"
 #include "tcgemm.cuh"
 
@@ -461,6 +463,79 @@ extern "C" int pcbqs_gb300_cholesky_f32(int64_t n, float *a, int64_t lda, int bl
     const cudaError_t e = pq::potrf_blocked(n, a, lda, block, math, static_cast<cudaStream_t>(stream), &order);
     *info = order;
     if (e) return pq::fail(pq::ERR_CUDA, "cholesky_f32: %s", cudaGetErrorString(e));
+    return pq::OK;
+}
+
+namespace pq {
+
+namespace {
+std::string panel_key(int64_t n, int math) {
+    return "lu_panel n=" + std::to_string(n) + " math=" + std::to_string(math);
+}
+
+// A diagonally dominant complex64 matrix for timing the factorization: a hashed value in [-1, 1) off the diagonal,
+// n on it.
+__global__ void k_timing_matrix(int64_t n, unsigned seed, float2 *A) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+        unsigned h = (unsigned)(t * 2654435761ull) ^ seed;
+        h ^= h >> 16;
+        h *= 0x7feb352du;
+        h ^= h >> 15;
+        const float a = (float)(h & 0xffff) / 32768.f - 1.f, b = (float)(h >> 16) / 32768.f - 1.f;
+        A[t] = (t / n == t % n) ? make_float2((float)n, 0.f) : make_float2(a, b);
+    }
+}
+}  // namespace
+
+int lu_panel_width(int64_t n, int math) {
+    const int w = tune_get(panel_key(n, math));
+    return w >= 32 && w <= MAX_BLOCK_PUBLIC ? w : 2048;
+}
+
+}  // namespace pq
+
+extern "C" int pcbqs_gb300_tune_lu_panel(int64_t n, int math, const int32_t *widths, int count, int32_t *best,
+                                         void *stream) {
+    if (n <= 0 || math < 0 || math > 3 || !widths || count <= 0 || !best)
+        return pq::fail(pq::ERR_ARGUMENT, "tune_lu_panel: invalid argument (math 0..3)");
+    for (int i = 0; i < count; ++i)
+        if (widths[i] < 32 || widths[i] > pq::MAX_BLOCK_PUBLIC)
+            return pq::fail(pq::ERR_ARGUMENT, "tune_lu_panel: widths 32..%d", pq::MAX_BLOCK_PUBLIC);
+    auto st = static_cast<cudaStream_t>(stream);
+    float2 *A = nullptr;
+    int *ipiv = nullptr;
+    cudaError_t e;
+    if ((e = pq::pool_alloc_n(&A, (size_t)n * n, st)) || (e = pq::pool_alloc_n(&ipiv, (size_t)n, st))) {
+        pq::pool_free(A, st);
+        return pq::fail(pq::ERR_MEMORY, "tune_lu_panel: %s", cudaGetErrorString(e));
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_ms = 1e30f;
+    int choice = -1;
+    for (int i = 0; i < count && !e; ++i) {
+        int zero = 0;
+        pq::k_timing_matrix<<<152 * 8, 256, 0, st>>>(n, 12345u, A);
+        pq::note_launches(1);
+        if ((e = cudaEventRecord(e0, st))) break;
+        if ((e = pq::getrf_blocked(n, A, ipiv, widths[i], math, st, &zero))) break;
+        if ((e = cudaEventRecord(e1, st)) || (e = cudaEventSynchronize(e1))) break;
+        float ms = 0;
+        if ((e = cudaEventElapsedTime(&ms, e0, e1))) break;
+        if (ms < best_ms) {
+            best_ms = ms;
+            choice = widths[i];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    pq::pool_free(A, st);
+    pq::pool_free(ipiv, st);
+    if (e) return pq::fail(e == cudaErrorLaunchTimeout ? pq::ERR_TIMEOUT : pq::ERR_CUDA, "tune_lu_panel: %s",
+                           cudaGetErrorString(e));
+    pq::tune_put(pq::panel_key(n, math), choice);
+    *best = choice;
     return pq::OK;
 }
 

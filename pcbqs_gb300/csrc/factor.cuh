@@ -37,6 +37,10 @@ struct LuUpdateStats {
 cudaError_t getrf_blocked(int64_t n, float2 *A, int *ipiv, int block, int math, cudaStream_t stream, int *singular,
                           LuUpdateStats *stats = nullptr);
 
+// The panel width of getrf_blocked for order n and `math`: the autotuner's choice (pcbqs_gb300_tune_lu_panel) when
+// one is recorded for this device, else 2048.
+int lu_panel_width(int64_t n, int math);
+
 // Factors the n x n column-major symmetric positive definite FP32 matrix A (leading dimension lda >= n, best a
 // multiple of 32 so that the GEMMs take their aligned forms; the lower triangle is read) in place as A = L L^T,
 // L in the lower triangle (cusolverDnSpotrf's layout; the strict upper triangle is left with intermediate values). Right-looking in `block`-column panels: the diagonal block by

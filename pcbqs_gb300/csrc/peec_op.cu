@@ -35,6 +35,7 @@
 #include "solve.cuh"
 #include "tcgemm.cuh"
 #include "trsolve.cuh"
+#include "tune.cuh"
 
 namespace pq {
 
@@ -414,8 +415,6 @@ static const DenseF32Variant DENSE_F32_VARIANTS[] = {
     {4, 2, k_dense_apply_f32<4, 2>}, {4, 4, k_dense_apply_f32<4, 4>}};
 constexpr int DENSE_F32_COUNT = sizeof(DENSE_F32_VARIANTS) / sizeof(DENSE_F32_VARIANTS[0]);
 
-static std::mutex g_dense_tune_mutex;
-static std::map<std::pair<int, int64_t>, int> g_dense_tune;     // (device, rows) -> variant
 
 static cudaError_t launch_dense_f32(int v, int64_t rows, const float *M, int64_t ld, const float *xf, int xcols,
                                    int c0, int nc, double *Y, cudaStream_t s) {
@@ -427,15 +426,11 @@ static cudaError_t launch_dense_f32(int v, int64_t rows, const float *M, int64_t
 
 static cudaError_t tuned_dense_f32(int64_t rows, const float *M, int64_t ld, const float *xf, int xcols, int c0,
                                    int nc, double *Y, cudaStream_t s, int &choice) {
-    int device = 0;
-    cudaGetDevice(&device);
-    {
-        std::lock_guard<std::mutex> lock(g_dense_tune_mutex);
-        auto it = g_dense_tune.find({device, rows});
-        if (it != g_dense_tune.end()) {
-            choice = it->second;
-            return cudaSuccess;
-        }
+    const std::string key = "dense_f32 rows=" + std::to_string(rows);
+    const int known = tune_get(key);
+    if (known >= 0 && known < DENSE_F32_COUNT) {
+        choice = known;
+        return cudaSuccess;
     }
     cudaEvent_t e0, e1;
     cudaError_t e;
@@ -460,8 +455,7 @@ static cudaError_t tuned_dense_f32(int64_t rows, const float *M, int64_t ld, con
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e) return e;
-    std::lock_guard<std::mutex> lock(g_dense_tune_mutex);
-    g_dense_tune[{device, rows}] = choice;
+    tune_put(key, choice);
     return cudaSuccess;
 }
 
@@ -1275,7 +1269,7 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     if (math >= 2) {
         int singular = 0;
         const int gemm = math == 2 ? LU_GEMM_BF16X9 : math == 3 ? LU_GEMM_FP32 : math == 4 ? LU_GEMM_TC3 : LU_GEMM_TC6;
-        e = getrf_blocked(n, lu->lu, lu->ipiv, LU_BLOCK, gemm, st, &singular, &h->updates);
+        e = getrf_blocked(n, lu->lu, lu->ipiv, lu_panel_width(n, gemm), gemm, st, &singular, &h->updates);
         cudaEventRecord(t.ev[2], st);
         if (e || singular) {
             delete lu;

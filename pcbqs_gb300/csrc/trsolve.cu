@@ -10,12 +10,14 @@
 // about a second sets a status and every block returns), so the dependency chain of 2 x n / TRI_BLOCK steps costs
 // a barrier each rather than a kernel launch. The factor is read once per sweep, 8 right-hand sides at a time.
 #include <algorithm>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
 #include "pool.cuh"
 #include "tcgemm.cuh"
 #include "trsolve.cuh"
+#include "tune.cuh"
 
 namespace pq {
 
@@ -521,9 +523,15 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s, bool 
     // column counts in one power-of-two bucket share the timing (a GMRES active set shrinks through many counts)
     int bucket = 4 * KC;
     while (bucket < p->kpad) bucket *= 2;
+    const std::string key = "trisolve n=" + std::to_string(n) + " columns=" + std::to_string(bucket);
     if (p->method < 0) {
         auto it = method_by_bucket.find(bucket);
-        if (it != method_by_bucket.end()) p->method = it->second;
+        if (it != method_by_bucket.end()) {
+            p->method = it->second;
+        } else {
+            const int known = tune_get(key);        // timed by an earlier factor of this size (or process)
+            if (known == 0 || known == 1) p->method = method_by_bucket[bucket] = known;
+        }
     }
     if (p->method < 0 && !deferred) {
         // the first call with this many columns: the blocked solve once to set it up, then each method timed once;
@@ -542,6 +550,7 @@ cudaError_t TriSolver::solve(int k, const cd *in, cd *out, cudaStream_t s, bool 
         if (e) return e;
         p->method = blocked < streaming ? 1 : 0;
         method_by_bucket[bucket] = p->method;
+        tune_put(key, p->method);
         return read_status(k, s);
     }
     if (p->method == 1) {
