@@ -281,6 +281,33 @@ int pcbqs_gb300_peec_set_product(pcbqs_gb300_peec *op, int terms);
  * (src/pcbqs/peec_iterative.py:253-256). */
 int pcbqs_gb300_peec_set_fp64_product(pcbqs_gb300_peec *op, int slices);
 
+/* An H-matrix as pcbqs_gb300.hmatrix.DeviceHMatrix packs it (the arrays of pcbqs_gb300_hmatrix_apply), device arrays;
+ * nslots: the product's slot count. */
+typedef struct pcbqs_gb300_hmat {
+    int64_t n, nblocks, nslots;
+    const int64_t *meta, *slot0, *idx, *row_ptr, *slots_of_row;
+    const double *store;
+    int32_t max_rank;
+} pcbqs_gb300_hmat;
+/* The compressed operator (the descriptor's L and P may then be null): L's first L->n rows (the RWG edges) from the
+ * inductance H-matrix, the nv via segments after them from the dense block `via` (nv x nv, FP64, may be null when
+ * nv = 0), and P = W^T H W from the triangle potential's H-matrix with W (triangles x nodes, A_t / A_node) and its
+ * transpose Wt. Every product of the operator then goes through them (FP64); the complex64 factor and the mixed
+ * solve need the dense matrices. Mirrors matrix_backend='hierarchical' (src/pcbqs/mqs.py:452-455; the products of
+ * peec_iterative.py:267-278 through HMatrix._native_matmat and compressed.PotentialOperator, compressed.py:194-204). */
+int pcbqs_gb300_peec_set_compressed(pcbqs_gb300_peec *op, const pcbqs_gb300_hmat *L, const double *via, int64_t nv,
+                                    const pcbqs_gb300_hmat *P, const pcbqs_gb300_csr *W, const pcbqs_gb300_csr *Wt);
+/* Block-Jacobi (as pcbqs_gb300_peec_block_jacobi) from diagonal blocks the caller computed: klk and tpt (nblk, bs, bs)
+ * device arrays of K^T L K and T^T P T (the compressed operator's, from exact entries). */
+int pcbqs_gb300_peec_block_jacobi_blocks(pcbqs_gb300_peec *op, int32_t bs, const double *krk, const double *klk,
+                                         const double *tpt, void *stream);
+/* P x = b (nn x k complex128, device) by GMRES on the operator's own P products (dense or compressed) with the
+ * Jacobi preconditioner diag (nn, device): the equilibrium charge of the compressed model (the dense model's is
+ * pcbqs_gb300_dense_gmres). Status 5 when a column did not converge. */
+int pcbqs_gb300_peec_potential_gmres(pcbqs_gb300_peec *op, int k, const double *b, double *x, const double *diag,
+                                     double tol, int maxiter, int restart, int32_t *iterations, double *residual,
+                                     void *stream);
+
 /* The autotuner. Choices timed at first use are remembered per device (name and SM count) and problem size: the FP32
  * dense product's shape ("dense_f32 rows=R"), the triangular solves' method per column bucket ("trisolve n=N
  * columns=C": 0 streaming sweeps, 1 blocked) and the blocked LU's panel width ("lu_panel n=N math=M", timed only by

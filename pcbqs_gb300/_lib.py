@@ -39,6 +39,13 @@ class CsrDesc(ctypes.Structure):
                 ('val', c_void_p)]
 
 
+class HmatDesc(ctypes.Structure):
+    """pcbqs_gb300_hmat: a packed H-matrix's device arrays."""
+    _fields_ = [('n', ctypes.c_int64), ('nblocks', ctypes.c_int64), ('nslots', ctypes.c_int64), ('meta', c_void_p),
+                ('slot0', c_void_p), ('idx', c_void_p), ('row_ptr', c_void_p), ('slots_of_row', c_void_p),
+                ('store', c_void_p), ('max_rank', ctypes.c_int32)]
+
+
 class PeecDesc(ctypes.Structure):
     """pcbqs_gb300_peec_desc: the loop/tree PEEC operator's device arrays and frequencies."""
     _fields_ = [('n', ctypes.c_int64), ('nb', ctypes.c_int64), ('ne', ctypes.c_int64), ('nn', ctypes.c_int64),
@@ -121,6 +128,13 @@ PROTOTYPES = {
                                                      ctypes.POINTER(ctypes.c_double)]),
     'pcbqs_gb300_peec_set_captured': (ctypes.c_int, [c_void_p, ctypes.c_int]),
     'pcbqs_gb300_peec_set_product': (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    'pcbqs_gb300_peec_set_compressed': (ctypes.c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_int64, c_void_p,
+                                                       c_void_p, c_void_p]),
+    'pcbqs_gb300_peec_block_jacobi_blocks': (ctypes.c_int, [c_void_p, ctypes.c_int32, c_void_p, c_void_p, c_void_p,
+                                                            c_void_p]),
+    'pcbqs_gb300_peec_potential_gmres': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p,
+                                                        ctypes.c_double, ctypes.c_int, ctypes.c_int, c_int32_p,
+                                                        c_void_p, c_void_p]),
     'pcbqs_gb300_peec_set_fp64_product': (ctypes.c_int, [c_void_p, ctypes.c_int]),
     'pcbqs_gb300_tune_file': (ctypes.c_int, [ctypes.c_char_p]),
     'pcbqs_gb300_tune_lookup': (ctypes.c_int, [ctypes.c_char_p, c_int32_p]),

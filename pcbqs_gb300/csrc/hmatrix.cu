@@ -16,6 +16,7 @@
 
 #include "../../include/pcbqs_gb300.h"
 #include "common.cuh"
+#include "hmatrix.cuh"
 #include "pairs.cuh"
 
 namespace pq {
@@ -462,14 +463,11 @@ extern "C" int pcbqs_gb300_hmatrix_build(const pcbqs_gb300_ctx *ctx, double near
     return err ? fail(ERR_CUDA, "hmatrix_build: %s", cudaGetErrorString(err)) : OK;
 }
 
-extern "C" int pcbqs_gb300_hmatrix_apply(int64_t n, int64_t nb, const int64_t *meta, const int64_t *slot0,
-                                         const int64_t *idx, const double *store, const int64_t *row_ptr,
-                                         const int64_t *slots_of_row, int max_rank, int k, const double *x, double *y,
-                                         double *slots, void *stream) {
-    if (n <= 0 || nb < 0 || !meta || !slot0 || !idx || !store || !row_ptr || !slots_of_row || k <= 0 || !x || !y ||
-        !slots || max_rank < 0)
-        return fail(ERR_ARGUMENT, "hmatrix_apply: invalid argument");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
+namespace pq {
+
+cudaError_t hmatrix_apply(int64_t n, int64_t nb, const int64_t *meta, const int64_t *slot0, const int64_t *idx,
+                          const double *store, const int64_t *row_ptr, const int64_t *slots_of_row, int max_rank,
+                          int k, const double *x, double *y, double *slots, cudaStream_t st) {
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -481,6 +479,19 @@ extern "C" int pcbqs_gb300_hmatrix_apply(int64_t n, int64_t nb, const int64_t *m
     k_hm_apply_rows<<<(unsigned)std::min<int64_t>((n * k + 255) / 256, (int64_t)sms * 16), 256, 0, st>>>(
         n, k, row_ptr, slots_of_row, reinterpret_cast<const double2 *>(slots), reinterpret_cast<double2 *>(y));
     note_launches(nb ? 2 : 1);
-    cudaError_t err = cudaGetLastError();
-    return err ? fail(ERR_CUDA, "hmatrix_apply: %s", cudaGetErrorString(err)) : OK;
+    return cudaGetLastError();
+}
+
+}  // namespace pq
+
+extern "C" int pcbqs_gb300_hmatrix_apply(int64_t n, int64_t nb, const int64_t *meta, const int64_t *slot0,
+                                         const int64_t *idx, const double *store, const int64_t *row_ptr,
+                                         const int64_t *slots_of_row, int max_rank, int k, const double *x, double *y,
+                                         double *slots, void *stream) {
+    if (n <= 0 || nb < 0 || !meta || !slot0 || !idx || !store || !row_ptr || !slots_of_row || k <= 0 || !x || !y ||
+        !slots || max_rank < 0)
+        return pq::fail(pq::ERR_ARGUMENT, "hmatrix_apply: invalid argument");
+    const cudaError_t err = pq::hmatrix_apply(n, nb, meta, slot0, idx, store, row_ptr, slots_of_row, max_rank, k, x, y,
+                                              slots, static_cast<cudaStream_t>(stream));
+    return err ? pq::fail(pq::ERR_CUDA, "hmatrix_apply: %s", cudaGetErrorString(err)) : pq::OK;
 }

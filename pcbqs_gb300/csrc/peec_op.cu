@@ -33,6 +33,7 @@
 #include "factor.cuh"
 #include "pool.cuh"
 #include "solve.cuh"
+#include "hmatrix.cuh"
 #include "tcgemm.cuh"
 #include "trsolve.cuh"
 #include "tune.cuh"
@@ -632,19 +633,66 @@ struct PeecOp : Operator {
                                 reinterpret_cast<double2 *>(y), k, exact_slices, xs, tc_error, wait_cycles(), s);
     }
 
-    cudaError_t dense(bool single, int64_t rows, int k, const double *M, int64_t ld, const float *Mf, int64_t ldf,
-                      const cd *x, cd *y, cudaStream_t s) {
+    // The compressed operator (pcbqs_gb300_peec_set_compressed): L's edge rows from an H-matrix with the via
+    // segments' dense block after them, P = W^T H W from the triangle potential's H-matrix; every product of the
+    // operator (FP64, single view included) then goes through them.
+    struct HMat {
+        int64_t n = 0, nblocks = 0, nslots = 0;
+        const int64_t *meta = nullptr, *slot0 = nullptr, *idx = nullptr, *row_ptr = nullptr, *slots_of_row = nullptr;
+        const double *store = nullptr;
+        int max_rank = 0;
+    };
+    bool compressed = false;
+    HMat hl, hp;
+    int64_t nvia = 0;
+    const double *via = nullptr;      // nvia x nvia, leading dimension nvia
+    Csr W, Wt;                        // triangles x nodes and its transpose
+    cd *hslots = nullptr, *tri_x = nullptr, *tri_y = nullptr;
+    int64_t hcap = 0;                 // columns the three buffers hold
+
+    cudaError_t hm_apply(const HMat &H, int k, const cd *x, cd *y, cudaStream_t s) {
+        return hmatrix_apply(H.n, H.nblocks, H.meta, H.slot0, H.idx, H.store, H.row_ptr, H.slots_of_row, H.max_rank,
+                             k, reinterpret_cast<const double *>(x), reinterpret_cast<double *>(y),
+                             reinterpret_cast<double *>(hslots), s);
+    }
+
+    cudaError_t compressed_product(int which, int k, const cd *x, cd *y, cudaStream_t s) {
+        if (which == 2) return cudaErrorNotSupported;       // no complex P with the compressed operator
+        cudaError_t e;
+        if (k > hcap) {
+            for (cd *p : {hslots, tri_x, tri_y}) dev_free(p, s);
+            hslots = tri_x = tri_y = nullptr;
+            hcap = 0;
+            const int64_t slots = std::max<int64_t>(1, std::max(hl.nslots, hp.nslots));
+            if ((e = dev_alloc(&hslots, (size_t)slots * k, s)) ||
+                (e = dev_alloc(&tri_x, (size_t)std::max<int64_t>(1, hp.n) * k, s)) ||
+                (e = dev_alloc(&tri_y, (size_t)std::max<int64_t>(1, hp.n) * k, s)))
+                return e;
+            hcap = k;
+        }
+        if (which == 0) {
+            if ((e = hm_apply(hl, k, x, y, s))) return e;
+            if (nvia) return dense_sym_apply<double, 2>(nvia, k, via, nvia, x + hl.n * k, y + hl.n * k, s);
+            return cudaSuccess;
+        }
+        k_spmm<<<grid_of(hp.n * k), 256, 0, s>>>(W, k, x, tri_x, nullptr, nullptr, 0);
+        if ((e = hm_apply(hp, k, tri_x, tri_y, s))) return e;
+        k_spmm<<<grid_of(nn * k), 256, 0, s>>>(Wt, k, tri_y, y, nullptr, nullptr, 0);
+        note_launches(2);
+        return cudaGetLastError();
+    }
+
+    // which: 0 L, 1 P, 2 P's imaginary part
+    cudaError_t dense(int which, bool single, int64_t rows, int k, const double *M, int64_t ld, const float *Mf,
+                      int64_t ldf, const cd *x, cd *y, cudaStream_t s) {
+        if (compressed) return compressed_product(which, k, x, y, s);
+        if (!M) return cudaErrorInvalidValue;
         if (!single) {
-            if (exact_slices && k >= EXACT_MIN_COLUMNS) {
-                const int which = M == L ? 0 : M == P ? 1 : M == Pim ? 2 : -1;
-                if (which >= 0) return sliced_product(which, rows, k, M, ld, x, y, s);
-            }
+            if (exact_slices && k >= EXACT_MIN_COLUMNS) return sliced_product(which, rows, k, M, ld, x, y, s);
             return dense_sym_apply<double, 2>(rows, k, M, ld, x, y, s);
         }
-        if (tc_terms && k >= TC_MIN_COLUMNS) {
-            const int which = Mf == Lf ? 0 : Mf == Pf ? 1 : Mf == Pfim ? 2 : -1;
-            if (which >= 0) return tensor_product(which, rows, k, Mf, ldf, x, y, s);
-        }
+        if (!Mf) return cudaErrorInvalidValue;
+        if (tc_terms && k >= TC_MIN_COLUMNS) return tensor_product(which, rows, k, Mf, ldf, x, y, s);
         const int64_t need = std::max(ne, nn) * (int64_t)DENSE_NC;
         if (need > capf) {
             dev_free(xf, s);
@@ -661,14 +709,14 @@ struct PeecOp : Operator {
         if (e) return e;
         k_tree_scale<<<grid_of(n_ * k), 256, 0, s>>>(n_, k, is_tree, walpha, sys, in, u);
         k_spmm<<<grid_of(nb * k), 256, 0, s>>>(K, k, u, branch, nullptr, sys, 0);
-        if ((e = dense(single, ne, k, L, ldl, Lf, ldlf, branch, lb, s))) return e;
+        if ((e = dense(0, single, ne, k, L, ldl, Lf, ldlf, branch, lb, s))) return e;
         k_impedance<<<grid_of(nb * k), 256, 0, s>>>(R, nb, k, branch, lb, omega, rscale, nscaled, sys, v);
         k_spmm<<<grid_of(n_ * k), 256, 0, s>>>(Kt, k, v, out, inv_z, sys, 0);
         if (nn > 0) {
             k_spmm<<<grid_of(nn * k), 256, 0, s>>>(T, k, in, tq, nullptr, sys, 0);
-            if ((e = dense(single, nn, k, P, ldp, Pf, ldpf, tq, pq, s))) return e;
+            if ((e = dense(1, single, nn, k, P, ldp, Pf, ldpf, tq, pq, s))) return e;
             if (Pim) {          // complex P: P_re q + j (P_im q)
-                if ((e = dense(single, nn, k, Pim, ldp, Pfim, ldpf, tq, pq2, s))) return e;
+                if ((e = dense(2, single, nn, k, Pim, ldp, Pfim, ldpf, tq, pq2, s))) return e;
                 k_add_times_j<<<grid_of(nn * k), 256, 0, s>>>(nn * k, pq2, pq);
                 note_launches(1);
             }
@@ -691,6 +739,7 @@ struct PeecOp : Operator {
         for (void *p : plane) dev_free(p);
         for (void *p : xplane) dev_free(p);
         dev_free(xs);
+        for (cd *p : {hslots, tri_x, tri_y}) dev_free(p);
         dev_free(tcs);
         dev_free(tc_error);
     }
@@ -1013,6 +1062,15 @@ struct Jacobi : Preconditioner {
     }
 };
 
+// P alone (nn x nn) through the operator's own P products (dense or compressed), for the equilibrium charge.
+struct PotentialView : Operator {
+    PeecOp *op = nullptr;
+    int64_t n() const override { return op->nn; }
+    cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        return op->dense(1, false, op->nn, k, op->P, op->ldp, nullptr, 0, in, out, s);
+    }
+};
+
 }  // namespace pq
 
 using namespace pq;
@@ -1059,7 +1117,7 @@ int pcbqs_gb300_peec_create(const pcbqs_gb300_peec_desc *d, pcbqs_gb300_peec **o
     if (!d || !out) return pfail(ERR_ARGUMENT, "peec_create: null argument");
     *out = nullptr;
     if (d->n <= 0 || d->nb <= 0 || d->ne < 0 || d->ne > d->nb || d->nn < 0 || d->nsys <= 0 || !d->omega ||
-        !d->zscale || !d->L || !d->is_tree || (d->nn > 0 && !d->P) || !(d->pscale > 0))
+        !d->zscale || !d->is_tree || !(d->pscale > 0))
         return pfail(ERR_ARGUMENT, "peec_create: invalid sizes or arrays");
     if (d->K.rows != d->nb || d->K.cols != d->n || d->Kt.rows != d->n || d->Kt.cols != d->nb ||
         d->R.rows != d->ne || (d->nn > 0 && (d->T.rows != d->nn || d->T.cols != d->n || d->Tt.rows != d->n)))
@@ -1131,9 +1189,12 @@ int pcbqs_gb300_peec_apply(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
     return take_product_timeout(h->op, st, "peec_apply");
 }
 
-int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double *krk, void *stream) {
+static int block_jacobi_impl(pcbqs_gb300_peec *h, int32_t bs, const double *krk, const double *klk_given,
+                             const double *tpt_given, void *stream) {
     if (!h || bs <= 0 || bs > 64 || !krk) return pfail(ERR_ARGUMENT, "block_jacobi: invalid argument");
     PeecOp &op = h->op;
+    if (!klk_given && (op.compressed || !op.L || (op.nn > 0 && !op.P)))
+        return pfail(ERR_ARGUMENT, "block_jacobi: the blocks of a compressed operator are given by the caller");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t nblk = (op.n_ + bs - 1) / bs;
     const size_t bsz = (size_t)nblk * bs * bs;
@@ -1151,11 +1212,16 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     }
     cudaMemsetAsync(singular, 0, sizeof(int), st);
     cudaMemsetAsync(tpt, 0, sizeof(double) * bsz, st);
-    k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Kt, op.L, op.ldl, klk);
-    if (op.nn > 0) k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Tt, op.P, op.ldp, tpt);
-    if (op.Pim) {
-        k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Tt, op.Pim, op.ldp, tpt_im);
-        note_launches(1);
+    if (klk_given) {
+        cudaMemcpyAsync(klk, klk_given, sizeof(double) * bsz, cudaMemcpyDeviceToDevice, st);
+        if (tpt_given) cudaMemcpyAsync(tpt, tpt_given, sizeof(double) * bsz, cudaMemcpyDeviceToDevice, st);
+    } else {
+        k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Kt, op.L, op.ldl, klk);
+        if (op.nn > 0) k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Tt, op.P, op.ldp, tpt);
+        if (op.Pim) {
+            k_block_gather<<<(unsigned)nblk, 256, 0, st>>>(op.n_, bs, op.Tt, op.Pim, op.ldp, tpt_im);
+            note_launches(1);
+        }
     }
     dim3 grid((unsigned)nblk, (unsigned)op.nsys);
     const size_t smem = sizeof(cd) * bs * 2 * bs;
@@ -1180,6 +1246,81 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double 
     return OK;
 }
 
+int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *h, int32_t bs, const double *krk, void *stream) {
+    return block_jacobi_impl(h, bs, krk, nullptr, nullptr, stream);
+}
+
+int pcbqs_gb300_peec_block_jacobi_blocks(pcbqs_gb300_peec *h, int32_t bs, const double *krk, const double *klk,
+                                         const double *tpt, void *stream) {
+    if (!klk || (h && h->op.nn > 0 && !tpt)) return pfail(ERR_ARGUMENT, "block_jacobi_blocks: blocks missing");
+    if (h && h->op.Pim) return pfail(ERR_ARGUMENT, "block_jacobi_blocks: complex P is not supported");
+    return block_jacobi_impl(h, bs, krk, klk, tpt, stream);
+}
+
+static bool hmat_ok(const pcbqs_gb300_hmat *m) {
+    return m && m->n > 0 && m->nblocks >= 0 && m->nslots >= 0 && m->meta && m->slot0 && m->idx && m->row_ptr &&
+           m->slots_of_row && m->store && m->max_rank >= 0;
+}
+
+static PeecOp::HMat hmat_of(const pcbqs_gb300_hmat &m) {
+    PeecOp::HMat h;
+    h.n = m.n; h.nblocks = m.nblocks; h.nslots = m.nslots;
+    h.meta = m.meta; h.slot0 = m.slot0; h.idx = m.idx; h.row_ptr = m.row_ptr; h.slots_of_row = m.slots_of_row;
+    h.store = m.store;
+    h.max_rank = m.max_rank;
+    return h;
+}
+
+int pcbqs_gb300_peec_set_compressed(pcbqs_gb300_peec *h, const pcbqs_gb300_hmat *L, const double *via, int64_t nv,
+                                    const pcbqs_gb300_hmat *P, const pcbqs_gb300_csr *W, const pcbqs_gb300_csr *Wt) {
+    if (!h || !hmat_ok(L) || nv < 0 || (nv > 0 && !via) || L->n + nv != h->op.ne)
+        return pfail(ERR_ARGUMENT, "peec_set_compressed: L's H-matrix rows plus the via rows must be the branch count");
+    PeecOp &op = h->op;
+    if (op.nn > 0 && (!hmat_ok(P) || !W || !Wt || W->rows != P->n || W->cols != op.nn || Wt->rows != op.nn ||
+                      Wt->cols != P->n))
+        return pfail(ERR_ARGUMENT, "peec_set_compressed: P's H-matrix (triangles) and W (triangles x nodes) needed");
+    if (op.Pim) return pfail(ERR_ARGUMENT, "peec_set_compressed: complex P is not supported");
+    op.hl = hmat_of(*L);
+    if (op.nn > 0) {
+        op.hp = hmat_of(*P);
+        op.W = csr_of(*W);
+        op.Wt = csr_of(*Wt);
+    }
+    op.via = via;
+    op.nvia = nv;
+    op.compressed = true;
+    return OK;
+}
+
+int pcbqs_gb300_peec_potential_gmres(pcbqs_gb300_peec *h, int k, const double *b, double *x, const double *diag,
+                                     double tol, int maxiter, int restart, int32_t *iterations, double *residual,
+                                     void *stream) {
+    if (!h || k <= 0 || !b || !x || !diag || !(tol > 0) || maxiter <= 0 || restart <= 0 || h->op.nn <= 0)
+        return pfail(ERR_ARGUMENT, "peec_potential_gmres: invalid argument");
+    if (!h->op.compressed && !h->op.P) return pfail(ERR_ARGUMENT, "peec_potential_gmres: no P");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    PotentialView view;
+    view.op = &h->op;
+    Jacobi J;
+    J.n = h->op.nn;
+    J.d = const_cast<double *>(diag);
+    std::vector<int32_t> sys(k, 0);
+    GmresOptions opt;
+    opt.tol = tol; opt.maxiter = maxiter; opt.restart = restart;
+    GmresReport rep;
+    cudaError_t e = gmres_batched(view, &J, k, sys.data(), reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x),
+                                  opt, rep, st);
+    if (e) return pfail(cuda_status(e), "peec_potential_gmres: %s", cudaGetErrorString(e));
+    bool ok = true;
+    for (int s = 0; s < k; ++s) {
+        if (iterations) iterations[s] = rep.iterations[s];
+        if (residual) residual[s] = rep.residual[s];
+        ok = ok && rep.residual[s] <= tol;
+    }
+    if (!ok) return pfail(ERR_CONVERGENCE, "peec_potential_gmres: not every column reached the tolerance");
+    return OK;
+}
+
 int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream) {
     if (!h || !krk || sys < 0 || sys >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_factor: invalid argument");
     if (math < 0 || math > 5)
@@ -1188,6 +1329,8 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     PeecOp &op = h->op;
     const int64_t n = op.n_;
     if (krk->rows != n || krk->cols != n) return pfail(ERR_ARGUMENT, "peec_factor: K^T R K must be n x n");
+    if (op.compressed || !op.L || (op.nn > 0 && !op.P))
+        return pfail(ERR_ARGUMENT, "peec_factor: the complex64 factor needs the dense L and P");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e;
     const size_t nn2 = (size_t)n * n;
@@ -1508,6 +1651,7 @@ int pcbqs_gb300_peec_single(pcbqs_gb300_peec *h, const float *Lf, int64_t ldlf, 
                             int64_t ldpf) {
     if (!h || !Lf || ldlf < h->op.ne || (h->op.nn > 0 && (!Pf || ldpf < h->op.nn)))
         return pfail(ERR_ARGUMENT, "peec_single: invalid single-precision matrices");
+    if (h->op.compressed) return pfail(ERR_ARGUMENT, "peec_single: the compressed operator has no single-precision copy");
     h->op.unpack();
     h->op.Lf = Lf;
     h->op.ldlf = ldlf;

@@ -236,6 +236,48 @@ class DeviceHMatrix:
                          bytes=self.bytes, dense_bytes=self.n * self.n * 8, evaluated_entries=self.entries,
                          tolerance=self.tol, leaf=self.leaf, eta=self.eta)
 
+    def dense_entries(self, pairs, host=False):
+        """Exact entries H[a][:, b] for each (a, b) pair of index arrays, evaluated on the device by the build's dense
+        path (the fill's context is needed): a list of (len(a), len(b)) float64 device tensors (host=True: NumPy
+        arrays, copied back at once)."""
+        if self.fill is None:
+            raise ValueError('a loaded H-matrix evaluates no new entries')
+        dev = self.fill.device
+        meta, idx, offset, ioff, shapes = [], [], 0, 0, []
+        for a, b in pairs:
+            la, lb = len(a), len(b)
+            meta.append([ioff, la, ioff + la, lb, offset, 0, 0, -1])
+            idx += [np.asarray(a, np.int64), np.asarray(b, np.int64)]
+            shapes.append((offset, la, lb))
+            ioff += la + lb
+            offset += la * lb
+        if not pairs:
+            return []
+        meta_d = torch.as_tensor(np.asarray(meta, np.int64), device=dev)
+        idx_d = torch.as_tensor(np.concatenate(idx), device=dev)
+        store = torch.empty(max(offset, 1), dtype=torch.float64, device=dev)
+        ids = torch.arange(len(pairs), dtype=torch.int64, device=dev)
+        near = float(self.fill.near)
+        lib = _lib.load()
+        _lib.check(lib.pcbqs_gb300_hmatrix_build(
+            self.fill.dev.handle, -1.0 if np.isinf(near) else near, int(self.fill.outer_levels), self.kind,
+            self._edges[0].data_ptr(), self._edges[1].data_ptr(), self._edges[2].data_ptr(), self.ne,
+            self.factor, meta_d.data_ptr(), ids.data_ptr(), len(pairs), None, 0, idx_d.data_ptr(),
+            self.tol, store.data_ptr(), None, 0, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
+        if host:
+            flat = store.cpu().numpy()
+            return [flat[o:o + la * lb].reshape(la, lb) for o, la, lb in shapes]
+        return [store[o:o + la * lb].view(la, lb) for o, la, lb in shapes]
+
+    def desc(self):
+        """The packed arrays as the C ABI's pcbqs_gb300_hmat (valid while this object lives)."""
+        d = _lib.HmatDesc()
+        d.n, d.nblocks, d.nslots = self.n, self.nblocks, self.nslots
+        d.meta, d.slot0, d.idx = self.meta.data_ptr(), self.slot0.data_ptr(), self.idx.data_ptr()
+        d.row_ptr, d.slots_of_row, d.store = self.row_ptr.data_ptr(), self.slots_of_row.data_ptr(), self.store.data_ptr()
+        d.max_rank = self.max_rank
+        return d
+
     _ARRAYS = ('store', 'meta', 'idx', 'slot0', 'row_ptr', 'slots_of_row')
 
     def __getstate__(self):

@@ -276,9 +276,23 @@ class PeecModel(PeecTopology):
     stack (MQS dielectric='stack', src/pcbqs/mqs.py:555-563)."""
 
     def __init__(self, board, near=3.0, outer_levels=1, device=0, block_size=32, tol=1e-8, maxiter=2000,
-                 restart=100, log=None, inner_tol=1e-4, conductor_loss='dc', conductor_faces=2, stack=None):
+                 restart=100, log=None, inner_tol=1e-4, conductor_loss='dc', conductor_faces=2, stack=None,
+                 matrix='dense', hmatrix=None):
+        """matrix='hierarchical': L and P as device H-matrices (DeviceHMatrix; `hmatrix` overrides their options,
+        default tol 1e-6, leaf 256, eta 1, rank 32) instead of dense matrices, as the reference's
+        matrix_backend='hierarchical' (src/pcbqs/mqs.py:452-455): every product of the solve goes through them, in
+        FP64, and block-Jacobi takes its blocks from exact entries. The complex64 factor ('lu32') and the mixed solve
+        need the dense matrices."""
         if conductor_loss not in ('dc', 'slab') or conductor_faces not in (1, 2):
             raise ValueError('conductor_loss must be dc or slab; conductor_faces must be 1 or 2')
+        if matrix not in ('dense', 'hierarchical'):
+            raise ValueError("matrix must be 'dense' or 'hierarchical'")
+        if matrix == 'hierarchical' and stack is not None:
+            raise ValueError('the compressed operator takes a homogeneous dielectric')
+        self.matrix = matrix
+        self.hmatrix_options = dict(tol=1e-6, leaf=256, eta=1.0, rank=32)
+        self.hmatrix_options.update(hmatrix or {})
+        self.HL = self.HP = None
         self.tol, self.maxiter, self.restart, self.inner_tol = tol, maxiter, restart, inner_tol
         self.conductor_loss, self.conductor_faces = conductor_loss, conductor_faces
         self.stack = stack
@@ -310,7 +324,11 @@ class PeecModel(PeecTopology):
     # -- device matrices --
     def assemble(self, mixed=False):
         """Fill L and P on the device (moments, combine, aggregation); frees the moment planes. mixed=True: far
-        pairs in FP32 local coordinates (near pairs FP64), FP32 combine; L and P kept in FP64 and FP32."""
+        pairs in FP32 local coordinates (near pairs FP64), FP32 combine; L and P kept in FP64 and FP32.
+        matrix='hierarchical': build the H-matrices of L's edges and of the triangle potential instead."""
+        if self.matrix == 'hierarchical':
+            self._nearblk = self._papply = None
+            return self._assemble_compressed(mixed)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         self.L = self.P = self.Lf = self.Pf = self.Pim = self.Pfim = None
         ev[0].record()
@@ -383,7 +401,10 @@ class PeecModel(PeecTopology):
         d.n, d.nb, d.ne, d.nn = self.n, len(self.passive), self.ni, self.nn
         for name in ('K', 'Kt', 'T', 'Tt', 'R'):
             setattr(d, name, _csr_struct(self._dev[name]))
-        d.L, d.ldl, d.P, d.ldp = self.L.data_ptr(), self.L.stride(0), self.P.data_ptr(), self.P.stride(0)
+        if self.matrix == 'hierarchical':
+            d.L, d.ldl, d.P, d.ldp = None, 0, None, 0
+        else:
+            d.L, d.ldl, d.P, d.ldp = self.L.data_ptr(), self.L.stride(0), self.P.data_ptr(), self.P.stride(0)
         d.is_tree = self._dev['is_tree'].data_ptr()
         d.pscale = self.pscale
         d.Pim = self.Pim.data_ptr() if self.Pim is not None else None
@@ -397,7 +418,107 @@ class PeecModel(PeecTopology):
         lib = _lib.load()
         handle = ctypes.c_void_p()
         _lib.check(lib.pcbqs_gb300_peec_create(ctypes.byref(d), ctypes.byref(handle)), lib)
+        if self.matrix == 'hierarchical':
+            hl, hp = self.HL.desc(), self.HP.desc()
+            w, wt = _csr_struct(self._Wdev), _csr_struct(self._Wtdev)
+            status = lib.pcbqs_gb300_peec_set_compressed(handle, ctypes.byref(hl), self.Lvia.data_ptr(),
+                                                          self.board.nv, ctypes.byref(hp), ctypes.byref(w),
+                                                          ctypes.byref(wt))
+            if status:
+                lib.pcbqs_gb300_peec_destroy(handle)
+                _lib.check(status, lib)
+        self._live_handle = handle
         return handle, zscale
+
+    def _assemble_compressed(self, mixed):
+        if mixed:
+            raise ValueError('the compressed operator runs its products in FP64 (mixed=False)')
+        from .hmatrix import DeviceHMatrix
+        t0 = time.perf_counter()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        self.L = self.P = self.Lf = self.Pf = self.Pim = self.Pfim = None
+        ev[0].record()
+        self.HL = DeviceHMatrix(self.fill, kernel='inductance', **self.hmatrix_options)
+        ev[1].record()
+        self.HP = DeviceHMatrix(self.fill, kernel='potential', er=self.board.er, **self.hmatrix_options)
+        ev[2].record()
+        dev = self.device
+        nv = self.board.nv
+        self.Lvia = torch.zeros((max(nv, 1), max(nv, 1)), dtype=torch.float64, device=dev)
+        if nv:
+            via_inductance(self.board.via_seg, self.Lvia, dev)
+        # W[t, node] = A_t / A_node and its transpose, device CSR
+        node_of = np.asarray(self.board.node_of)
+        nt, nn = len(node_of), self.nn
+        area_t = np.asarray(self.fill.geometry.area)
+        area_n = np.bincount(node_of, weights=area_t, minlength=nn)
+        self._w = area_t / area_n[node_of]
+        W = csr_matrix((self._w, (np.arange(nt), node_of)), shape=(nt, nn))
+        self._Wdev, self._Wtdev = _dev_csr(W, dev), _dev_csr(W.T.tocsr(), dev)
+        self._tris_of = np.split(np.argsort(node_of, kind='stable'), np.cumsum(np.bincount(node_of, minlength=nn))[:-1])
+        # diagonals: L's edges and vias, P's nodes (exact entries)
+        ne = self.ne
+        ld = self.HL.dense_entries([(np.array([e]), np.array([e])) for e in range(ne)], host=True)
+        ldiag = np.array([m[0, 0] for m in ld])
+        if nv:
+            ldiag = np.r_[ldiag, torch.diagonal(self.Lvia).cpu().numpy()]
+        pdiag = self._node_blocks([np.array([i]) for i in range(nn)])
+        self.pdiag = torch.as_tensor(np.array([b[0, 0] for b in pdiag]), device=dev)
+        torch.cuda.synchronize()
+        self.ldiag = ldiag
+        self.pscale = float(self.pdiag.abs().max())
+        self._pinvb = None
+        self.mixed_fill = False
+        self.analytic = None
+        self.timings.update(fill_ms=ev[0].elapsed_time(ev[1]), combine_ms=0.0, potential_ms=ev[1].elapsed_time(ev[2]),
+                            hmatrix_s=time.perf_counter() - t0, hmatrix_L=self.HL.info, hmatrix_P=self.HP.info)
+        return self
+
+    def _node_blocks(self, groups):
+        """P[N, N] = W_N^T H[T, T] W_N for each node set N (T: its triangles), from exact triangle entries; host
+        arrays."""
+        tris = [np.concatenate([self._tris_of[i] for i in g]) for g in groups]
+        blocks = self.HP.dense_entries([(t, t) for t in tris], host=True)
+        node_of = np.asarray(self.board.node_of)
+        out = []
+        for g, t, H in zip(groups, tris, blocks):
+            pos = {int(i): k for k, i in enumerate(g)}
+            Wb = np.zeros((len(t), len(g)))
+            Wb[np.arange(len(t)), [pos[int(node_of[x])] for x in t]] = self._w[t]
+            out.append(Wb.T @ H @ Wb)
+        return out
+
+    def _near_blocks(self):
+        """The diagonal blocks of K^T L K and T^T P T for block-Jacobi from exact entries (the compressed
+        operator has no dense L and P to gather from): (nblk, bs, bs) device arrays."""
+        bs, n, ne = self.bs, self.n, self.ne
+        Kt = csr_matrix(self.Kp.T)
+        Tt = csr_matrix(self.Tp.T)
+        nblk = (n + bs - 1) // bs
+        klk = np.zeros((nblk, bs, bs))
+        tpt = np.zeros((nblk, bs, bs))
+        spans = [(b * bs, min(n, (b + 1) * bs)) for b in range(nblk)]
+        ksub = [Kt[a:z] for a, z in spans]
+        branches = [np.unique(s.indices) for s in ksub]
+        edges = [br[br < ne] for br in branches]
+        Le = self.HL.dense_entries([(e, e) for e in edges], host=True)
+        Lvia = self.Lvia.cpu().numpy()
+        tsub = [Tt[a:z] for a, z in spans]
+        nodes = [np.unique(s.indices) for s in tsub]
+        Pn = self._node_blocks(nodes) if self.nn else [np.zeros((0, 0))] * nblk
+        for b, ((a, z), ks, br, e, ts, nd) in enumerate(zip(spans, ksub, branches, edges, tsub, nodes)):
+            Lb = np.zeros((len(br), len(br)))
+            m = len(e)
+            Lb[:m, :m] = Le[b]
+            v = br[m:] - ne
+            Lb[m:, m:] = Lvia[np.ix_(v, v)]
+            Kb = ks[:, br].toarray()
+            klk[b, :z - a, :z - a] = Kb @ Lb @ Kb.T
+            if self.nn:
+                Tb = ts[:, nd].toarray()
+                tpt[b, :z - a, :z - a] = Tb @ Pn[b] @ Tb.T
+        dev = self.device
+        return torch.as_tensor(klk, device=dev), torch.as_tensor(tpt, device=dev)
 
     def _krk_blocks(self):
         bs, n = self.bs, self.n
@@ -444,6 +565,14 @@ class PeecModel(PeecTopology):
         its = np.zeros(k, np.int32)
         res = np.zeros(k)
         lib = _lib.load()
+        if self.matrix == 'hierarchical':
+            # Jacobi-preconditioned GMRES on the compressed P, through the live operator
+            _lib.check(lib.pcbqs_gb300_peec_potential_gmres(
+                self._live_handle, k, b.data_ptr(), x.data_ptr(), self.pdiag.data_ptr(), self.tol * 1e-2, 4000,
+                self.restart, _lib.ptr(its, ctypes.c_int32), _lib.ptr(res),
+                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
+            self.timings['potential_solve_iterations'] = its.tolist()
+            return x.cpu().numpy()
         Pim = self.Pim.data_ptr() if self.Pim is not None else None
         _lib.check(lib.pcbqs_gb300_dense_gmres(self.nn, self.P.data_ptr(), Pim, self.P.stride(0), k, b.data_ptr(),
                                                x.data_ptr(), self.tol * 1e-2, 4000, self.restart, precondition,
@@ -453,10 +582,23 @@ class PeecModel(PeecTopology):
         return x.cpu().numpy()
 
     def _mv_L(self, X):
-        """L X for complex branch vectors X (ne, k), FP64 on the device (pcbqs_gb300_dense_apply)."""
+        """L X for complex branch vectors X (ne, k), FP64 on the device (pcbqs_gb300_dense_apply, or the compressed
+        product)."""
+        if self.matrix == 'hierarchical':
+            Xt = torch.as_tensor(np.ascontiguousarray(X, complex), device=self.device).reshape(self.ni, -1)
+            Y = torch.empty_like(Xt)
+            Y[:self.ne] = self.HL.matmat(Xt[:self.ne])
+            if self.board.nv:
+                Y[self.ne:] = self.Lvia.to(torch.complex128) @ Xt[self.ne:]
+            return Y.cpu().numpy().reshape(np.shape(X))
         return self._dense(self.L, X)
 
     def _mv_P(self, X):
+        if self.matrix == 'hierarchical':
+            Xt = torch.as_tensor(np.ascontiguousarray(X, complex), device=self.device).reshape(self.nn, -1)
+            if getattr(self, '_papply', None) is None:
+                self._papply = self.HP.potential_operator(self.board.node_of)
+            return self._papply(Xt).cpu().numpy().reshape(np.shape(X))
         Y = self._dense(self.P, X)
         return Y if self.Pim is None else Y + 1j * self._dense(self.Pim, X)
 
@@ -538,7 +680,7 @@ class PeecModel(PeecTopology):
         products over 4 or more columns (the mixed solve's outer residuals, the FP64 GMRES): 'fp64' on the FP64 pipe,
         or 'sliced6' (5, 7) on the tensor cores from integer slices at FP64's accuracy
         (pcbqs_gb300_peec_set_fp64_product); default 'sliced6' for mixed=True, 'fp64' (the plain path) otherwise."""
-        if self.L is None:
+        if self.L is None and self.HL is None:
             self.assemble()
         f = np.atleast_1d(np.asarray(freqs, float))
         if f.ndim != 1 or not np.isfinite(f).all() or (f <= 0).any():
@@ -553,6 +695,8 @@ class PeecModel(PeecTopology):
             fp64_product = 'sliced6' if mixed else 'fp64'
         if fp64_product not in self.FP64_PRODUCT:
             raise ValueError(f'fp64_product must be one of {sorted(self.FP64_PRODUCT)}')
+        if self.matrix == 'hierarchical' and (mixed or precondition == 'lu32'):
+            raise ValueError("the compressed operator solves in FP64 with precondition 'block_jacobi' or 'none'")
         nf = len(f)
         if anchors is None:
             anchors = nf
@@ -629,8 +773,15 @@ class PeecModel(PeecTopology):
             if mode == 1:
                 e0, e1 = timed()
                 e0.record()
-                _lib.check(lib.pcbqs_gb300_peec_block_jacobi(handle, self.bs, self._krk_blocks().data_ptr(), stream),
-                           lib)
+                if self.matrix == 'hierarchical':
+                    if getattr(self, '_nearblk', None) is None:
+                        self._nearblk = self._near_blocks()
+                    klk, tpt = self._nearblk
+                    _lib.check(lib.pcbqs_gb300_peec_block_jacobi_blocks(handle, self.bs, self._krk_blocks().data_ptr(),
+                                                                        klk.data_ptr(), tpt.data_ptr(), stream), lib)
+                else:
+                    _lib.check(lib.pcbqs_gb300_peec_block_jacobi(handle, self.bs, self._krk_blocks().data_ptr(),
+                                                                 stream), lib)
                 e1.record()
                 torch.cuda.synchronize()
                 precondition_ms += e0.elapsed_time(e1)
