@@ -475,8 +475,10 @@ def case_potrf(n, *blocks):
                       f'{n ** 3 / 3 / ms / 1e9:.1f} TFLOP/s', flush=True)
 
 
-def case_dense(n, k=8):
-    """A random symmetric n x n matrix (FP64 and its FP32 copy) against k complex columns (k_dense_sym_apply)."""
+def case_dense(n, k=8, *forms):
+    """A random symmetric n x n matrix (FP64 and its FP32 copy) against k complex columns: forms fp64 and fp32
+    (k_dense_sym_apply, k_dense_apply_f32), tensor3 (the BF16x3 real-operand product, k_tc_update<1>) and sliced6
+    (the FP64-accurate integer-slice product, k_tc_update<2>); the tensor forms pack M in each call. Default all."""
     import ctypes
     import torch
     from pcbqs_gb300 import _lib
@@ -489,19 +491,54 @@ def case_dense(n, k=8):
     X = torch.randn((n, k), dtype=torch.complex128, device='cuda', generator=g)
     Y = torch.empty_like(X)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for name, fn in (('fp64', lambda: lib.pcbqs_gb300_dense_apply(n, k, M.data_ptr(), n, X.data_ptr(), Y.data_ptr(),
-                                                                   stream)),
-                     ('fp32', lambda: lib.pcbqs_gb300_dense_apply_single(n, k, Mf.data_ptr(), n, X.data_ptr(),
-                                                                          Y.data_ptr(), stream))):
+    calls = dict(
+        fp64=lambda: lib.pcbqs_gb300_dense_apply(n, k, M.data_ptr(), n, X.data_ptr(), Y.data_ptr(), stream),
+        fp32=lambda: lib.pcbqs_gb300_dense_apply_single(n, k, Mf.data_ptr(), n, X.data_ptr(), Y.data_ptr(), stream),
+        tensor3=lambda: lib.pcbqs_gb300_dense_apply_tensor(n, k, Mf.data_ptr(), n, X.data_ptr(), Y.data_ptr(), 3,
+                                                           1 << 31, stream),
+        sliced6=lambda: lib.pcbqs_gb300_dense_apply_sliced(n, k, M.data_ptr(), n, X.data_ptr(), Y.data_ptr(), 6,
+                                                           1 << 31, stream))
+    for name in (forms or tuple(calls)):
+        fn = calls[name]
         for _ in range(3):
             ms, status = _event_ms(fn)
             _lib.check(status, lib)
-            bytes_ = n * n * (8 if name == 'fp64' else 4)
+            bytes_ = n * n * {'fp64': 8, 'fp32': 4, 'tensor3': 4, 'sliced6': 8}[name]
             print(f'dense {name} n={n} k={k}: {ms:.3f} ms, {bytes_ / ms / 1e6:.0f} GB/s of matrix, '
                   f'{2 * n * n * 2 * k / ms / 1e9:.3f} TFLOP/s', flush=True)
 
 
-CASES = dict(fill=case_fill, lu=case_lu, getrf=case_getrf, potrf=case_potrf, dense=case_dense, update=case_update)
+def case_lusolve(board, k=128, method=3, math=2):
+    """A board's complex64 PEEC factor at 1 MHz (math 2: cuBLAS BF16x9 updates, so that no tcgen05 update precedes
+    the solves), then two triangular solves of k columns by `method` (0 auto, 1 getrs, 2 streaming sweeps, 3 the
+    blocked solve: k_cgemm_small, k_tc_update<3>, the factor's panels packed by the first)."""
+    import ctypes
+    import torch
+    from pcbqs_gb300 import _lib
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel, _csr_struct
+    k, method, math = int(k), int(method), int(math)
+    m = PeecModel(Board.load(board))
+    m.assemble(mixed=True)
+    lib = _lib.load()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    handle, _ = m._operator(np.array([2 * np.pi * 1e6]))
+    try:
+        desc = _csr_struct(m._krk_device())
+        _lib.check(lib.pcbqs_gb300_peec_factor(handle, ctypes.byref(desc), 0, math, stream), lib)
+        g = torch.Generator(device='cuda').manual_seed(1)
+        x = torch.randn(m.n, k, dtype=torch.complex128, device='cuda', generator=g)
+        y = torch.empty_like(x)
+        for _ in range(2):
+            ms, _ = _event_ms(lambda: _lib.check(lib.pcbqs_gb300_peec_lu_solve(handle, k, x.data_ptr(), y.data_ptr(),
+                                                                               method, stream), lib))
+            print(f'lu_solve n={m.n} k={k} method {method}: {ms:.2f} ms', flush=True)
+    finally:
+        lib.pcbqs_gb300_peec_destroy(handle)
+
+
+CASES = dict(fill=case_fill, lu=case_lu, getrf=case_getrf, potrf=case_potrf, dense=case_dense, update=case_update,
+             lusolve=case_lusolve)
 
 
 def kernel_case(spec):

@@ -804,16 +804,17 @@ __global__ void k_transpose(const double *W, int64_t rows, int64_t cols, int64_t
 }
 
 // A[i, j] = (j w KLK[i,j]) d_j / zs + TPT[i,j] / ps as complex64, d_j = 1 (loop) or j w alpha (tree). Grid
-// (column chunks, rows strided by gridDim.y): no per-element division.
+// (column chunks, rows strided by gridDim.y). The scalings are products with precomputed factors (a division per
+// entry costs the slow FP64 pipe more than the whole pass's memory traffic; the result is rounded to FP32).
 __global__ void k_assemble_c64(int64_t n, const double *klk, const double *tpt, const double *tpt_im,
                                const int8_t *is_tree, double w, double zs, double ps, float2 *A) {
+  const double f = w * zs / ps, wz = w / zs, ips = 1.0 / ps;
   for (int64_t i = blockIdx.y; i < n; i += gridDim.y) {
-    const double f = w * zs / ps;
     const bool tree_i = is_tree[i];
     const double *krow = klk + i * n, *trow = tpt + i * n, *tirow = tpt_im ? tpt_im + i * n : nullptr;
     float2 *arow = A + i * n;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        double re = 0, im = w * krow[j] / zs;
+        double re = 0, im = wz * krow[j];
         const bool tree_j = is_tree[j];
         if (tree_j) {                // times j f
             const double r2 = -f * im;
@@ -821,8 +822,8 @@ __global__ void k_assemble_c64(int64_t n, const double *klk, const double *tpt, 
             re = r2;
         }
         if (tree_i && tree_j) {
-            re += trow[j] / ps;
-            if (tirow) im += tirow[j] / ps;
+            re += ips * trow[j];
+            if (tirow) im += ips * tirow[j];
         }
         arow[j] = make_float2((float)re, (float)im);
     }
