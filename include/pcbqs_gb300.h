@@ -297,6 +297,34 @@ typedef struct pcbqs_gb300_hmat {
  * peec_iterative.py:267-278 through HMatrix._native_matmat and compressed.PotentialOperator, compressed.py:194-204). */
 int pcbqs_gb300_peec_set_compressed(pcbqs_gb300_peec *op, const pcbqs_gb300_hmat *L, const double *via, int64_t nv,
                                     const pcbqs_gb300_hmat *P, const pcbqs_gb300_csr *W, const pcbqs_gb300_csr *Wt);
+/* An H-matrix's low-rank blocks packed for the tensor cores by pcbqs_gb300.hmatrix.DeviceHMatrix.lowrank_plan
+ * (device arrays): the dense blocks alone (meta_dense, slot0_dense: ndense records in the hmat's layout), the left
+ * factors' plane (lrows x 128 BF16), the right factors' plane (128 x 2 rwidth BF16), the groups (one per block and
+ * direction, 40-byte records: a_row0, rows, a_x0, b_x0, kb, t_row0, rank, pad as int32, slot0 as int64), the phase-two
+ * tiles (ntiles pairs of group and row tile) and every row's position in the padded cluster order (n_pad wide). */
+typedef struct pcbqs_gb300_lowrank {
+    const int64_t *meta_dense, *slot0_dense;
+    int64_t ndense;
+    const void *lplane;
+    int64_t lrows;
+    const void *rplane;
+    int64_t rwidth;
+    const void *groups;
+    int32_t ngroups, ntiles;
+    const int32_t *tile_group, *tile_m, *pad_pos;
+    int64_t n_pad;
+} pcbqs_gb300_lowrank;
+/* Y = H X with the dense blocks in FP64 and the low-rank blocks' stacked U (V^T X) products on the tcgen05 tensor
+ * cores: BF16 three-part products, FP32 accumulation (phase one R X[J] for every block and direction, one tile each;
+ * phase two L T into the block's slots; the rows then sum their slots in block order). X, Y (n, k) complex128 device
+ * arrays, k <= 128; relative error about 2^-16 of the low-rank part. Synchronizes `stream`; status 6 when a bounded
+ * wait gave up. The benchmark spec's BF16 low-rank products; the reference's are FP64 (core/hmatrix_kernels.hpp:20-100). */
+int pcbqs_gb300_hmatrix_apply_lowrank(const pcbqs_gb300_hmat *H, const pcbqs_gb300_lowrank *lr, int k,
+                                      const double *x, double *y, void *stream);
+/* The compressed operator's single-precision view (the mixed solve's inner products): the H-matrix of L (which 0)
+ * or of P (1) applied with its low-rank blocks on the tensor cores as pcbqs_gb300_hmatrix_apply_lowrank; the FP64
+ * products (outer residuals) keep FP64 throughout. */
+int pcbqs_gb300_peec_set_lowrank(pcbqs_gb300_peec *op, int which, const pcbqs_gb300_lowrank *lr);
 /* Block-Jacobi (as pcbqs_gb300_peec_block_jacobi) from diagonal blocks the caller computed: klk and tpt (nblk, bs, bs)
  * device arrays of K^T L K and T^T P T (the compressed operator's, from exact entries). */
 int pcbqs_gb300_peec_block_jacobi_blocks(pcbqs_gb300_peec *op, int32_t bs, const double *krk, const double *klk,

@@ -46,6 +46,14 @@ class HmatDesc(ctypes.Structure):
                 ('store', c_void_p), ('max_rank', ctypes.c_int32)]
 
 
+class LowRankDesc(ctypes.Structure):
+    """pcbqs_gb300_lowrank: an H-matrix's low-rank blocks packed for the tensor cores."""
+    _fields_ = [('meta_dense', c_void_p), ('slot0_dense', c_void_p), ('ndense', ctypes.c_int64), ('lplane', c_void_p),
+                ('lrows', ctypes.c_int64), ('rplane', c_void_p), ('rwidth', ctypes.c_int64), ('groups', c_void_p),
+                ('ngroups', ctypes.c_int32), ('ntiles', ctypes.c_int32), ('tile_group', c_void_p),
+                ('tile_m', c_void_p), ('pad_pos', c_void_p), ('n_pad', ctypes.c_int64)]
+
+
 class PeecDesc(ctypes.Structure):
     """pcbqs_gb300_peec_desc: the loop/tree PEEC operator's device arrays and frequencies."""
     _fields_ = [('n', ctypes.c_int64), ('nb', ctypes.c_int64), ('ne', ctypes.c_int64), ('nn', ctypes.c_int64),
@@ -128,6 +136,9 @@ PROTOTYPES = {
                                                      ctypes.POINTER(ctypes.c_double)]),
     'pcbqs_gb300_peec_set_captured': (ctypes.c_int, [c_void_p, ctypes.c_int]),
     'pcbqs_gb300_peec_set_product': (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    'pcbqs_gb300_hmatrix_apply_lowrank': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int, c_void_p, c_void_p,
+                                                         c_void_p]),
+    'pcbqs_gb300_peec_set_lowrank': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p]),
     'pcbqs_gb300_peec_set_compressed': (ctypes.c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_int64, c_void_p,
                                                        c_void_p, c_void_p]),
     'pcbqs_gb300_peec_block_jacobi_blocks': (ctypes.c_int, [c_void_p, ctypes.c_int32, c_void_p, c_void_p, c_void_p,

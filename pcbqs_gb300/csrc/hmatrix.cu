@@ -465,6 +465,31 @@ extern "C" int pcbqs_gb300_hmatrix_build(const pcbqs_gb300_ctx *ctx, double near
 
 namespace pq {
 
+cudaError_t hmatrix_blocks(int64_t nb, const int64_t *meta, const int64_t *slot0, const int64_t *idx,
+                           const double *store, int max_rank, int k, const double *x, double *slots, cudaStream_t st) {
+    if (!nb) return cudaSuccess;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t smem = sizeof(double2) * (size_t)std::max(1, max_rank) * k;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_hm_apply_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_hm_apply_blocks<<<(unsigned)std::min<int64_t>(nb, (int64_t)sms * 8), 256, smem, st>>>(
+        meta, nb, slot0, idx, store, k, reinterpret_cast<const double2 *>(x), reinterpret_cast<double2 *>(slots));
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t hmatrix_rows(int64_t n, const int64_t *row_ptr, const int64_t *slots_of_row, int k, const double *slots,
+                         double *y, cudaStream_t st) {
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_hm_apply_rows<<<(unsigned)std::min<int64_t>((n * k + 255) / 256, (int64_t)sms * 16), 256, 0, st>>>(
+        n, k, row_ptr, slots_of_row, reinterpret_cast<const double2 *>(slots), reinterpret_cast<double2 *>(y));
+    note_launches(1);
+    return cudaGetLastError();
+}
+
 cudaError_t hmatrix_apply(int64_t n, int64_t nb, const int64_t *meta, const int64_t *slot0, const int64_t *idx,
                           const double *store, const int64_t *row_ptr, const int64_t *slots_of_row, int max_rank,
                           int k, const double *x, double *y, double *slots, cudaStream_t st) {

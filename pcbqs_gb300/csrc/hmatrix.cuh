@@ -12,4 +12,11 @@ cudaError_t hmatrix_apply(int64_t n, int64_t nb, const int64_t *meta, const int6
                           const double *store, const int64_t *row_ptr, const int64_t *slots_of_row, int max_rank,
                           int k, const double *x, double *y, double *slots, cudaStream_t st);
 
+// The two passes of hmatrix_apply: the blocks' contributions into their slots (nb blocks of `meta`), and the rows'
+// sums of their slots in block order.
+cudaError_t hmatrix_blocks(int64_t nb, const int64_t *meta, const int64_t *slot0, const int64_t *idx,
+                           const double *store, int max_rank, int k, const double *x, double *slots, cudaStream_t st);
+cudaError_t hmatrix_rows(int64_t n, const int64_t *row_ptr, const int64_t *slots_of_row, int k, const double *slots,
+                         double *y, cudaStream_t st);
+
 }  // namespace pq

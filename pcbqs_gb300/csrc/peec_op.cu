@@ -641,6 +641,12 @@ struct PeecOp : Operator {
         const int64_t *meta = nullptr, *slot0 = nullptr, *idx = nullptr, *row_ptr = nullptr, *slots_of_row = nullptr;
         const double *store = nullptr;
         int max_rank = 0;
+        // the single view's low-rank blocks on the tensor cores (pcbqs_gb300_peec_set_lowrank)
+        bool lr = false;
+        LowRankPlan plan;
+        const int64_t *meta_dense = nullptr, *slot0_dense = nullptr;
+        int64_t ndense = 0;
+        void *scratch = nullptr;      // tc_lowrank_scratch_bytes, zeroed when allocated
     };
     bool compressed = false;
     HMat hl, hp;
@@ -650,13 +656,31 @@ struct PeecOp : Operator {
     cd *hslots = nullptr, *tri_x = nullptr, *tri_y = nullptr;
     int64_t hcap = 0;                 // columns the three buffers hold
 
-    cudaError_t hm_apply(const HMat &H, int k, const cd *x, cd *y, cudaStream_t s) {
-        return hmatrix_apply(H.n, H.nblocks, H.meta, H.slot0, H.idx, H.store, H.row_ptr, H.slots_of_row, H.max_rank,
-                             k, reinterpret_cast<const double *>(x), reinterpret_cast<double *>(y),
-                             reinterpret_cast<double *>(hslots), s);
+    cudaError_t hm_apply(HMat &H, bool single, int k, const cd *x, cd *y, cudaStream_t s) {
+        if (!single || !H.lr || k > 128)
+            return hmatrix_apply(H.n, H.nblocks, H.meta, H.slot0, H.idx, H.store, H.row_ptr, H.slots_of_row,
+                                 H.max_rank, k, reinterpret_cast<const double *>(x), reinterpret_cast<double *>(y),
+                                 reinterpret_cast<double *>(hslots), s);
+        cudaError_t e;
+        if (!tc_error) {
+            if ((e = dev_alloc(&tc_error, 1, s)) || (e = cudaMemsetAsync(tc_error, 0, sizeof(int), s))) return e;
+        }
+        if (!H.scratch) {
+            const size_t bytes = tc_lowrank_scratch_bytes(H.plan.n_pad, H.plan.ngroups);
+            if ((e = dev_alloc(reinterpret_cast<uint8_t **>(&H.scratch), bytes, s)) ||
+                (e = cudaMemsetAsync(H.scratch, 0, bytes, s)))
+                return e;
+        }
+        if ((e = hmatrix_blocks(H.ndense, H.meta_dense, H.slot0_dense, H.idx, H.store, H.max_rank, k,
+                                reinterpret_cast<const double *>(x), reinterpret_cast<double *>(hslots), s)) ||
+            (e = tc_lowrank_product(H.plan, k, reinterpret_cast<const double2 *>(x), reinterpret_cast<double2 *>(hslots),
+                                    H.scratch, tc_error, wait_cycles(), s)))
+            return e;
+        return hmatrix_rows(H.n, H.row_ptr, H.slots_of_row, k, reinterpret_cast<const double *>(hslots),
+                            reinterpret_cast<double *>(y), s);
     }
 
-    cudaError_t compressed_product(int which, int k, const cd *x, cd *y, cudaStream_t s) {
+    cudaError_t compressed_product(int which, bool single, int k, const cd *x, cd *y, cudaStream_t s) {
         if (which == 2) return cudaErrorNotSupported;       // no complex P with the compressed operator
         cudaError_t e;
         if (k > hcap) {
@@ -671,12 +695,12 @@ struct PeecOp : Operator {
             hcap = k;
         }
         if (which == 0) {
-            if ((e = hm_apply(hl, k, x, y, s))) return e;
+            if ((e = hm_apply(hl, single, k, x, y, s))) return e;
             if (nvia) return dense_sym_apply<double, 2>(nvia, k, via, nvia, x + hl.n * k, y + hl.n * k, s);
             return cudaSuccess;
         }
         k_spmm<<<grid_of(hp.n * k), 256, 0, s>>>(W, k, x, tri_x, nullptr, nullptr, 0);
-        if ((e = hm_apply(hp, k, tri_x, tri_y, s))) return e;
+        if ((e = hm_apply(hp, single, k, tri_x, tri_y, s))) return e;
         k_spmm<<<grid_of(nn * k), 256, 0, s>>>(Wt, k, tri_y, y, nullptr, nullptr, 0);
         note_launches(2);
         return cudaGetLastError();
@@ -685,7 +709,7 @@ struct PeecOp : Operator {
     // which: 0 L, 1 P, 2 P's imaginary part
     cudaError_t dense(int which, bool single, int64_t rows, int k, const double *M, int64_t ld, const float *Mf,
                       int64_t ldf, const cd *x, cd *y, cudaStream_t s) {
-        if (compressed) return compressed_product(which, k, x, y, s);
+        if (compressed) return compressed_product(which, single, k, x, y, s);
         if (!M) return cudaErrorInvalidValue;
         if (!single) {
             if (exact_slices && k >= EXACT_MIN_COLUMNS) return sliced_product(which, rows, k, M, ld, x, y, s);
@@ -740,6 +764,8 @@ struct PeecOp : Operator {
         for (void *p : xplane) dev_free(p);
         dev_free(xs);
         for (cd *p : {hslots, tri_x, tri_y}) dev_free(p);
+        dev_free(hl.scratch);
+        dev_free(hp.scratch);
         dev_free(tcs);
         dev_free(tc_error);
     }
@@ -1293,6 +1319,54 @@ int pcbqs_gb300_peec_set_compressed(pcbqs_gb300_peec *h, const pcbqs_gb300_hmat 
     return OK;
 }
 
+static int lowrank_of(const pcbqs_gb300_lowrank *lr, int64_t n, int max_rank, PeecOp::HMat &H, const char *what) {
+    if (!lr || !lr->lplane || !lr->rplane || !lr->groups || lr->ngroups <= 0 || lr->ntiles <= 0 || !lr->tile_group ||
+        !lr->tile_m || !lr->pad_pos || lr->n_pad < n || lr->n_pad % 64 || lr->rwidth % 64 || lr->lrows < 128 ||
+        lr->ndense < 0 || (lr->ndense > 0 && (!lr->meta_dense || !lr->slot0_dense)) || max_rank > 64)
+        return pfail(ERR_ARGUMENT, "%s: invalid low-rank plan (ranks up to 64)", what);
+    H.plan.lplane = lr->lplane;
+    H.plan.lrows = lr->lrows;
+    H.plan.rplane = lr->rplane;
+    H.plan.rwidth = lr->rwidth;
+    H.plan.groups = static_cast<const LrGroup *>(lr->groups);
+    H.plan.ngroups = lr->ngroups;
+    H.plan.tile_group = lr->tile_group;
+    H.plan.tile_m = lr->tile_m;
+    H.plan.ntiles = lr->ntiles;
+    H.plan.pad_pos = lr->pad_pos;
+    H.plan.n = n;
+    H.plan.n_pad = lr->n_pad;
+    H.meta_dense = lr->meta_dense;
+    H.slot0_dense = lr->slot0_dense;
+    H.ndense = lr->ndense;
+    H.lr = true;
+    return OK;
+}
+
+int pcbqs_gb300_peec_set_lowrank(pcbqs_gb300_peec *h, int which, const pcbqs_gb300_lowrank *lr) {
+    if (!h || !h->op.compressed || (which != 0 && which != 1) || (which == 1 && h->op.nn <= 0))
+        return pfail(ERR_ARGUMENT, "peec_set_lowrank: a compressed operator and which 0 (L) or 1 (P)");
+    PeecOp::HMat &H = which == 0 ? h->op.hl : h->op.hp;
+    return lowrank_of(lr, H.n, H.max_rank, H, "peec_set_lowrank");
+}
+
+int pcbqs_gb300_hmatrix_apply_lowrank(const pcbqs_gb300_hmat *Hd, const pcbqs_gb300_lowrank *lr, int k,
+                                      const double *x, double *y, void *stream) {
+    if (!hmat_ok(Hd) || k <= 0 || k > 128 || !x || !y)
+        return pfail(ERR_ARGUMENT, "hmatrix_apply_lowrank: invalid argument (k 1..128)");
+    PeecOp op;                  // a carrier for the product's buffers
+    op.hl = hmat_of(*Hd);
+    if (int status = lowrank_of(lr, Hd->n, Hd->max_rank, op.hl, "hmatrix_apply_lowrank")) return status;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = dev_alloc(&op.hslots, (size_t)std::max<int64_t>(1, Hd->nslots) * k, st);
+    if (!e) {
+        op.hcap = k;
+        e = op.hm_apply(op.hl, true, k, reinterpret_cast<const cd *>(x), reinterpret_cast<cd *>(y), st);
+    }
+    if (e) return pfail(cuda_status(e), "hmatrix_apply_lowrank: %s", cudaGetErrorString(e));
+    return take_product_timeout(op, st, "hmatrix_apply_lowrank");
+}
+
 int pcbqs_gb300_peec_potential_gmres(pcbqs_gb300_peec *h, int k, const double *b, double *x, const double *diag,
                                      double tol, int maxiter, int restart, int32_t *iterations, double *residual,
                                      void *stream) {
@@ -1670,7 +1744,8 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *h, int k, const int32_t *sys_
     if (!h || k <= 0 || !sys_host || !b || !x || !(tol > 0) || !(inner_tol > 0) || max_outer < 0 ||
         inner_maxiter <= 0 || restart <= 0)
         return pfail(ERR_ARGUMENT, "peec_solve_mixed: invalid argument");
-    if (!h->op.Lf) return pfail(ERR_ARGUMENT, "peec_solve_mixed: no single-precision L and P set");
+    if (!h->op.Lf && !h->op.compressed)
+        return pfail(ERR_ARGUMENT, "peec_solve_mixed: no single-precision L and P set");
     for (int s = 0; s < k; ++s)
         if (sys_host[s] < 0 || sys_host[s] >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_solve_mixed: system");
     if (precondition == 1 && !h->bj) return pfail(ERR_ARGUMENT, "peec_solve_mixed: no block-Jacobi set up");

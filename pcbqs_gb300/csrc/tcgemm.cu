@@ -122,6 +122,34 @@ __global__ void __launch_bounds__(256) k_pack_b(int64_t cols, int k, int kp, int
     }
 }
 
+// ---- the low-rank product (the H-matrix's far blocks) ----
+// X (n x k complex128, row-major) into its transposed BF16 plane: row c = real column c (2c' = Re, 2c' + 1 = Im of
+// column c'), part h at pad_pos[i], part m at n_pad + pad_pos[i]. 32 x 32 blocks transposed through shared memory.
+__global__ void __launch_bounds__(256) k_pack_xt(int64_t n, int ncols, const double *X, const int32_t *pad_pos,
+                                                 int64_t n_pad, __nv_bfloat16 *out) {
+    __shared__ float tile[32][33];
+    const int64_t i0 = (int64_t)blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t i = i0 + r;
+        const int c = c0 + tx;
+        tile[r][tx] = (i < n && c < ncols) ? (float)X[i * ncols + c] : 0.f;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int c = c0 + r;
+        const int64_t i = i0 + tx;
+        if (c >= ncols || i >= n) continue;
+        __nv_bfloat16 h, m, l;
+        split3(tile[tx][r], h, m, l);
+        __nv_bfloat16 *row = out + (int64_t)c * 2 * n_pad;
+        const int64_t p = pad_pos[i];
+        row[p] = h;
+        row[n_pad + p] = m;
+    }
+}
+
 // ---- the row-major complex update (the triangular solves' products) ----
 // A's plane from a row-major complex64 A (row r contiguous in t): the same layout as k_pack_a.
 __global__ void __launch_bounds__(256) k_pack_a_rows(int64_t rows, int k, int kp, int terms, const float2 *A,
@@ -449,7 +477,12 @@ __device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t parity, uns
 }
 
 struct TileArgs {
-    int64_t rows, cols;          // C's size (complex)
+    int64_t rows, cols;          // C's size (complex); the low-rank modes: cols = right-hand sides
+    const LrGroup *groups;       // the low-rank modes' groups
+    const int *tile_group, *tile_m;   // MODE 5: each tile's group and row tile
+    int a_pitch, b_pitch;        // the low-rank modes: part pitch (elements) of the A and B planes along K
+    __nv_bfloat16 *tplane;       // MODE 4's output: the T plane (MODE 5's B operand)
+    double2 *slots;              // MODE 5's output rows
     float2 *C;
     int64_t ldc;
     double2 *Y;                  // the real-operand product's output (row-major, leading dimension ldy)
@@ -461,6 +494,10 @@ struct TileArgs {
     unsigned long long wait;
 };
 
+// MODE 4 / 5: the two phases of the low-rank product (LrGroup): 4 T_g = R_g X[J_g] (A = R's plane, 128 rows
+// of which rank_g hold R_g; B = X's transposed plane at J_g's padded range; K = 3 part segments of kb slices), its
+// tile written as the BF16 parts of T_g^T into the T plane; 5 Y[I_g] = L_g T_g (A = L's plane at a_row0, B = the
+// T plane at t_row0, K = 3 one-slice segments), each tile stored into its group's slot rows.
 // MODE 0: C -= D into a column-major complex64 C (the complex update); 3: the same into a row-major C; 1: Y = D into a row-major complex128 Y, D's
 // columns 2c, 2c + 1 being column c's real and imaginary parts (the real-operand product); 2: the same Y from
 // integer slices (the FP64-accurate product): K runs over the slice pairs in level order, each pair a segment of
@@ -487,9 +524,21 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
     const int first_m = (int)(blockIdx.x / per_group) * GROUP;
     const int in_group = (int)(blockIdx.x % per_group);
     const int gm = min(GROUP, args.tiles_m - first_m);
-    const int m_tile = first_m + in_group % gm, n_tile = in_group / gm;
+    int m_tile = first_m + in_group % gm, n_tile = in_group / gm;
+    int kb_total = args.kblocks;
+    LrGroup grp{};
+    if (MODE == 4) {                       // one tile per group
+        grp = args.groups[blockIdx.x];
+        m_tile = 0;
+        n_tile = 0;
+        kb_total = 3 * grp.kb;
+    } else if (MODE == 5) {
+        grp = args.groups[args.tile_group[blockIdx.x]];
+        m_tile = args.tile_m[blockIdx.x];
+        n_tile = 0;
+        kb_total = 3;
+    }
     const int64_t m0 = (int64_t)m_tile * BM;
-    const int kb_total = args.kblocks;
     const int nchunks = (kb_total + CHUNK - 1) / CHUNK;
 
     if (threadIdx.x == 0) {
@@ -534,14 +583,25 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
                 }
                 mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
                 const uint32_t a_dst = ring + s * STAGE_BYTES, b_dst = a_dst + A_BYTES;
-                int xa = kb * BK, xb = kb * BK;
+                int xa = kb * BK, xb = kb * BK, ya = (int)m0, yb = n_tile * BN;
                 if (MODE == 2) {
                     const int p = kb / args.seg_kblocks, off = (kb - p * args.seg_kblocks) * BK;
                     xa = PAIR_A[p] * args.seg_kblocks * BK + off;
                     xb = PAIR_B[p] * args.seg_kblocks * BK + off;
+                } else if (MODE == 4) {
+                    const int sg = kb / grp.kb, off = (kb - sg * grp.kb) * BK;
+                    xa = SEG_A[sg] * args.a_pitch + grp.b_x0 + off;
+                    xb = SEG_B[sg] * args.b_pitch + grp.a_x0 + off;
+                    ya = 0;
+                    yb = 0;
+                } else if (MODE == 5) {
+                    xa = SEG_A[kb] * BK;
+                    xb = SEG_B[kb] * BK;
+                    ya = grp.a_row0 + (int)m0;
+                    yb = grp.t_row0;
                 }
-                tma_load_2d(a_dst, &map_a, xa, (int)m0, smem_addr(&full[s]));
-                tma_load_2d(b_dst, &map_b, xb, n_tile * BN, smem_addr(&full[s]));
+                tma_load_2d(a_dst, &map_a, xa, ya, smem_addr(&full[s]));
+                tma_load_2d(b_dst, &map_b, xb, yb, smem_addr(&full[s]));
                 issued_last[s] = kb;
             }
             if (!ok) {
@@ -673,6 +733,33 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
             }
         } else if (MODE == 2) {
             // Y complete (its scales applied by k_exact_scale)
+        } else if (!*abort && MODE == 4) {
+            // rows of D: ranks j; columns: the right-hand sides' real columns c. T^T's plane row c holds the parts
+            // h, m of T[j, c] at j and 64 + j (zero from the group's rank to 64).
+            const int j = q * 32 + lane;
+            if (j < 64) {
+                const int c0 = h * (BN / 2);
+                __nv_bfloat16 *trow = args.tplane + (int64_t)grp.t_row0 * 128;
+#pragma unroll
+                for (int i = 0; i < BN / 2; ++i) {
+                    const int c = c0 + i;
+                    if (c < 2 * args.cols) {
+                        __nv_bfloat16 vh, vm, vl;
+                        split3(j < grp.rank ? acc[i] : 0.f, vh, vm, vl);
+                        trow[(int64_t)c * 128 + j] = vh;
+                        trow[(int64_t)c * 128 + 64 + j] = vm;
+                    }
+                }
+            }
+        } else if (!*abort && MODE == 5) {
+            const int64_t row = m0 + q * 32 + lane;
+            const int64_t c0 = h * (BN / 4);
+            if (row < grp.rows) {
+                double2 *base = args.slots + (grp.slot0 + row) * args.cols;
+#pragma unroll
+                for (int j = 0; j < BN / 4; ++j)
+                    if (c0 + j < args.cols) base[c0 + j] = make_double2(acc[2 * j], acc[2 * j + 1]);
+            }
         } else if (!*abort && MODE == 3) {
             const int64_t row = m0 + q * 32 + lane;
             const int64_t c0 = (int64_t)n_tile * (BN / 2) + h * (BN / 4);
@@ -771,7 +858,9 @@ cudaError_t configure() {
         if ((e = cudaFuncSetAttribute(k_tc_update<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
             (e = cudaFuncSetAttribute(k_tc_update<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
             (e = cudaFuncSetAttribute(k_tc_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
-            (e = cudaFuncSetAttribute(k_tc_update<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
+            (e = cudaFuncSetAttribute(k_tc_update<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
+            (e = cudaFuncSetAttribute(k_tc_update<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
+            (e = cudaFuncSetAttribute(k_tc_update<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
             return e;
         configured[device] = true;
     }
@@ -1018,6 +1107,53 @@ cudaError_t tc_update_rows_c64(int64_t rows, int64_t cols, int k, const void *ap
     if (tiles > 0x7fffffff) return cudaErrorInvalidValue;
     k_tc_update<3><<<(unsigned)tiles, THREADS, SMEM, stream>>>(ma, mb, args);
     note_launches(1);
+    return cudaGetLastError();
+}
+
+size_t tc_lowrank_scratch_bytes(int64_t n_pad, int ngroups) {
+    return (size_t)(align1k(256 * 2 * n_pad * 2) + align1k((int64_t)ngroups * 256 * 128 * 2));
+}
+
+cudaError_t tc_lowrank_product(const LowRankPlan &p, int k, const double2 *X, double2 *slots, void *scratch,
+                               int *error, unsigned long long wait_cycles, cudaStream_t stream) {
+    if (p.ngroups <= 0) return cudaSuccess;
+    if (k <= 0 || k > BN / 2 || !X || !slots || !scratch || !error || !p.lplane || !p.rplane || !p.groups ||
+        !p.tile_group || !p.tile_m || !p.pad_pos || p.n <= 0 || p.n_pad <= 0 || p.n_pad % BK || p.rwidth % BK ||
+        p.lrows < BM || p.ntiles <= 0)
+        return cudaErrorInvalidValue;
+    cudaError_t e = configure();
+    if (e) return e;
+    auto *xt = static_cast<__nv_bfloat16 *>(scratch);
+    auto *tplane = reinterpret_cast<__nv_bfloat16 *>(static_cast<uint8_t *>(scratch) + align1k(256 * 2 * p.n_pad * 2));
+    {
+        const dim3 grid((unsigned)((p.n + 31) / 32), (unsigned)((2 * k + 31) / 32));
+        k_pack_xt<<<grid, 256, 0, stream>>>(p.n, 2 * k, reinterpret_cast<const double *>(X), p.pad_pos, p.n_pad, xt);
+        note_launches(1);
+    }
+    CUtensorMap ma, mb;
+    TileArgs args{};
+    args.cols = k;
+    args.groups = p.groups;
+    args.error = error;
+    args.wait = wait_cycles;
+    args.tiles_m = 1;
+    args.tiles_n = 1;
+    args.seg_kblocks = 1;
+    // phase one: T_g = R_g X[J_g], one tile per group
+    if (!plane_map(&ma, p.rplane, BM, 2 * p.rwidth, BM) || !plane_map(&mb, xt, 256, 2 * p.n_pad, BN))
+        return cudaErrorNotSupported;
+    args.a_pitch = (int)p.rwidth;
+    args.b_pitch = (int)p.n_pad;
+    args.tplane = tplane;
+    k_tc_update<4><<<(unsigned)p.ngroups, THREADS, SMEM, stream>>>(ma, mb, args);
+    // phase two: L_g T_g into the slots
+    if (!plane_map(&ma, p.lplane, p.lrows, 128, BM) || !plane_map(&mb, tplane, (int64_t)p.ngroups * 256, 128, BN))
+        return cudaErrorNotSupported;
+    args.tile_group = p.tile_group;
+    args.tile_m = p.tile_m;
+    args.slots = slots;
+    k_tc_update<5><<<(unsigned)p.ntiles, THREADS, SMEM, stream>>>(ma, mb, args);
+    note_launches(2);
     return cudaGetLastError();
 }
 

@@ -7,6 +7,48 @@
 
 namespace pq {
 
+// One low-rank contribution Y[I] += L (R X[J]) of an H-matrix product on the tensor cores (tc_lowrank_product):
+// L (|I| x rank) and R (rank x |J|) are a block's factors (U and V, or V^T and U^T for its transposed half), R X[J]
+// summed over J's range of the padded cluster order. Layout shared with pcbqs_gb300.hmatrix (40 bytes).
+struct LrGroup {
+    int32_t a_row0;   // first row of L in the left plane
+    int32_t rows;     // |I|
+    int32_t a_x0;     // J's padded start in the right-hand sides' plane (a multiple of 64)
+    int32_t b_x0;     // R's start in the right plane (a multiple of 64)
+    int32_t kb;       // 64-wide slices of J's padded range
+    int32_t t_row0;   // the group's 256 rows in the T plane
+    int32_t rank;     // <= 64
+    int32_t pad;
+    int64_t slot0;    // first slot row of the output
+};
+
+// One H-matrix's low-rank blocks packed for the tensor cores (device arrays): the left factors' plane (lrows x 128
+// BF16: parts h and m of L at 0 and 64, zero from the rank on), the right factors' plane (128 x 2 rwidth BF16: part
+// h at 0, m at rwidth; group g's R in rows 0 .. rank - 1 from b_x0, at the padded positions of J), the groups, and
+// the phase-two tiles (group, row tile); pad_pos: each row's position in the padded cluster order (n_pad wide).
+struct LowRankPlan {
+    const void *lplane = nullptr;
+    int64_t lrows = 0;
+    const void *rplane = nullptr;
+    int64_t rwidth = 0;
+    const LrGroup *groups = nullptr;
+    int ngroups = 0;
+    const int32_t *tile_group = nullptr, *tile_m = nullptr;
+    int ntiles = 0;
+    const int32_t *pad_pos = nullptr;
+    int64_t n = 0, n_pad = 0;
+};
+
+// Scratch of tc_lowrank_product: the right-hand sides' transposed plane (256 x 2 n_pad BF16) and the T plane
+// (ngroups x 256 x 128 BF16); zeroed once when allocated (padding positions are never written).
+size_t tc_lowrank_scratch_bytes(int64_t n_pad, int ngroups);
+// The low-rank blocks' contributions to Y = H X (X: n x k complex128 row-major, k <= 128) in BF16 three-part
+// products with FP32 accumulation: phase one T_g = R_g X[J_g] for every group (one tile each), written as T_g^T's
+// BF16 parts; phase two L_g T_g into the group's slot rows (slots: complex128, k wide), summed with the dense blocks'
+// slots afterwards. `error`, `wait_cycles`, `stream` as in tc_update_c64.
+cudaError_t tc_lowrank_product(const LowRankPlan &plan, int k, const double2 *X, double2 *slots, void *scratch,
+                               int *error, unsigned long long wait_cycles, cudaStream_t stream);
+
 // Scratch of one trailing update (the BF16 operand planes), sized by tc_update_scratch_bytes.
 size_t tc_update_scratch_bytes(int64_t rows, int64_t cols, int k, int terms);
 

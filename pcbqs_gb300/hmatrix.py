@@ -120,6 +120,7 @@ class DeviceHMatrix:
         lib = _lib.load()
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         blocks, stores = [], []       # final (a_ids, b_ids, store index, offset, rank, cap, same)
+        self._nodes = []              # each block's (row cluster, column cluster) tree nodes
         level = [(0, 0)]              # the block (root, root), then each level's undecided blocks
         self.entries = 0
         while level:
@@ -139,6 +140,7 @@ class DeviceHMatrix:
                     if rk >= 0:
                         self.entries += cap * (tree.size(i) + tree.size(j))
                         blocks.append((tree.ids(i), tree.ids(j), len(stores), off, int(rk), cap, False))
+                        self._nodes.append((i, j))
                     elif tree.leaf(i) and tree.leaf(j):
                         exact.append((i, j))                # ACA not accepted on two leaves: a dense block
                     else:
@@ -201,6 +203,7 @@ class DeviceHMatrix:
         for (i, j), m in zip(pairs, meta):
             self.entries += tree.size(i) * tree.size(j)
             blocks.append((tree.ids(i), tree.ids(j), len(stores), m[4], -1, 0, i == j))
+            self._nodes.append((i, j))
         stores.append(store)
 
     def _pack(self, blocks, stores):
@@ -277,6 +280,106 @@ class DeviceHMatrix:
         d.row_ptr, d.slots_of_row, d.store = self.row_ptr.data_ptr(), self.slots_of_row.data_ptr(), self.store.data_ptr()
         d.max_rank = self.max_rank
         return d
+
+    def lowrank_plan(self):
+        """The low-rank blocks packed for the tensor cores (pcbqs_gb300_hmatrix_apply_lowrank): each block gives a
+        group per direction, Y[I] += L (R X[J]) with (L, R) = (U, V) forward and (V^T, U^T) transposed, the factors
+        split into BF16 parts h, m. X is read in a padded cluster order, each leaf's range rounded up to 64, so every
+        cluster is a 64-aligned range the tensor copies can address. Returns (arrays kept alive, the C struct), or
+        None when no block is low rank."""
+        tree, dev = self.tree, self.store.device
+        meta = self.meta.cpu().numpy()
+        slot0 = self.slot0.cpu().numpy()
+        low = np.flatnonzero(meta[:, 7] >= 0)
+        if not len(low):
+            return None
+        if self.max_rank > 64:
+            raise ValueError('the tensor-core low-rank product takes ranks up to 64')
+        leaves = sorted((k for k in range(len(tree.start)) if tree.leaf(k)), key=lambda k: tree.start[k])
+        pos = np.empty(self.n, np.int32)
+        pstart_of_start, pend_of_stop, off = {}, {}, 0
+        for k in leaves:
+            a, b = int(tree.start[k]), int(tree.stop[k])
+            pos[tree.perm[a:b]] = off + np.arange(b - a)
+            pstart_of_start[a] = off
+            off += -(-(b - a) // 64) * 64
+            pend_of_stop[b] = off
+        n_pad = off
+        span = lambda k: (pstart_of_start[int(tree.start[k])], pend_of_stop[int(tree.stop[k])])
+        store = self.store
+        groups, lefts, rights = [], [], []
+        a_row0, b_x0 = 0, 0
+        for w in low:
+            la, lb, so, cap, rk = (int(meta[w, 1]), int(meta[w, 3]), int(meta[w, 4]), int(meta[w, 5]),
+                                   int(meta[w, 7]))
+            i, j = self._nodes[w]
+            U = store[so:so + la * cap].view(cap, la)[:rk].T          # la x rk
+            V = store[so + la * cap:so + la * cap + cap * lb].view(cap, lb)[:rk]   # rk x lb
+            for L, R, rows_node, cols_node, slot in ((U, V, i, j, slot0[w, 0]), (V.T, U.T, j, i, slot0[w, 1])):
+                p0, p1 = span(cols_node)
+                cols_pos = torch.as_tensor(pos[tree.ids(cols_node)] - p0, device=dev, dtype=torch.int64)
+                rows = L.shape[0]
+                groups.append((a_row0, rows, p0, b_x0, (p1 - p0) // 64, 256 * len(groups), rk, 0, int(slot)))
+                lefts.append(L)
+                rights.append((R, b_x0, cols_pos))
+                a_row0 += rows
+                b_x0 += p1 - p0
+                if meta[w, 6]:                      # a diagonal block has no transposed half (none is low rank)
+                    break
+        lrows = a_row0 + 128
+        rwidth = max(b_x0, 64)
+
+        def parts(x):
+            h = x.float().to(torch.bfloat16)
+            return h, (x.float() - h.float()).to(torch.bfloat16)
+        lplane = torch.zeros((lrows, 128), dtype=torch.bfloat16, device=dev)
+        rplane = torch.zeros((128, 2 * rwidth), dtype=torch.bfloat16, device=dev)
+        for g, L in zip(groups, lefts):
+            h, m = parts(L)
+            r0, rows, rk = g[0], g[1], g[6]
+            lplane[r0:r0 + rows, :rk] = h
+            lplane[r0:r0 + rows, 64:64 + rk] = m
+        for g, (R, x0, cols_pos) in zip(groups, rights):
+            h, m = parts(R)
+            rk = g[6]
+            rplane[:rk, x0 + cols_pos] = h
+            rplane[:rk, rwidth + x0 + cols_pos] = m
+        gdt = np.dtype([('a_row0', '<i4'), ('rows', '<i4'), ('a_x0', '<i4'), ('b_x0', '<i4'), ('kb', '<i4'),
+                        ('t_row0', '<i4'), ('rank', '<i4'), ('pad', '<i4'), ('slot0', '<i8')])
+        assert gdt.itemsize == 40
+        garr = np.array(groups, dtype=gdt)
+        tiles = [(g, t) for g, grp in enumerate(groups) for t in range(-(-grp[1] // 128))]
+        dense = np.flatnonzero(meta[:, 7] < 0)
+        t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dt), device=dev)
+        keep = dict(lplane=lplane, rplane=rplane, groups=t(garr.view(np.uint8), np.uint8),
+                    tile_group=t([g for g, _ in tiles], np.int32), tile_m=t([m for _, m in tiles], np.int32),
+                    pad_pos=t(pos, np.int32), meta_dense=t(meta[dense], np.int64), slot0_dense=t(slot0[dense], np.int64))
+        d = _lib.LowRankDesc()
+        d.meta_dense, d.slot0_dense, d.ndense = keep['meta_dense'].data_ptr(), keep['slot0_dense'].data_ptr(), len(dense)
+        d.lplane, d.lrows = lplane.data_ptr(), lrows
+        d.rplane, d.rwidth = rplane.data_ptr(), rwidth
+        d.groups, d.ngroups, d.ntiles = keep['groups'].data_ptr(), len(groups), len(tiles)
+        d.tile_group, d.tile_m, d.pad_pos = (keep['tile_group'].data_ptr(), keep['tile_m'].data_ptr(),
+                                             keep['pad_pos'].data_ptr())
+        d.n_pad = n_pad
+        return keep, d
+
+    def matmat_lowrank(self, X):
+        """Y = H X with the low-rank blocks on the tensor cores in BF16 (pcbqs_gb300_hmatrix_apply_lowrank); the
+        dense blocks in FP64. X (n, k <= 128) complex128 on the device."""
+        if getattr(self, '_lowrank', None) is None:
+            self._lowrank = self.lowrank_plan()
+        X = X.reshape(self.n, -1).to(torch.complex128).contiguous()
+        if self._lowrank is None:
+            return self.matmat(X)
+        Y = torch.empty_like(X)
+        lib = _lib.load()
+        d = self.desc()
+        _lib.check(lib.pcbqs_gb300_hmatrix_apply_lowrank(ctypes.byref(d), ctypes.byref(self._lowrank[1]), X.shape[1],
+                                                         X.data_ptr(), Y.data_ptr(),
+                                                         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                   lib)
+        return Y
 
     _ARRAYS = ('store', 'meta', 'idx', 'slot0', 'row_ptr', 'slots_of_row')
 

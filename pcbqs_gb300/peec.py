@@ -281,8 +281,9 @@ class PeecModel(PeecTopology):
         """matrix='hierarchical': L and P as device H-matrices (DeviceHMatrix; `hmatrix` overrides their options,
         default tol 1e-6, leaf 256, eta 1, rank 32) instead of dense matrices, as the reference's
         matrix_backend='hierarchical' (src/pcbqs/mqs.py:452-455): every product of the solve goes through them, in
-        FP64, and block-Jacobi takes its blocks from exact entries. The complex64 factor ('lu32') and the mixed solve
-        need the dense matrices."""
+        FP64, and block-Jacobi takes its blocks from exact entries; solve(mixed=True) runs the inner GMRES with the
+        low-rank blocks' products in BF16 on the tensor cores (stacked U (V^T X), FP32 accumulation) under FP64 outer
+        residuals. The complex64 factor ('lu32') needs the dense matrices."""
         if conductor_loss not in ('dc', 'slab') or conductor_faces not in (1, 2):
             raise ValueError('conductor_loss must be dc or slab; conductor_faces must be 1 or 2')
         if matrix not in ('dense', 'hierarchical'):
@@ -431,8 +432,7 @@ class PeecModel(PeecTopology):
         return handle, zscale
 
     def _assemble_compressed(self, mixed):
-        if mixed:
-            raise ValueError('the compressed operator runs its products in FP64 (mixed=False)')
+        """The H-matrices (the same for mixed=True: its inner products then take their low-rank blocks in BF16)."""
         from .hmatrix import DeviceHMatrix
         t0 = time.perf_counter()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -695,8 +695,8 @@ class PeecModel(PeecTopology):
             fp64_product = 'sliced6' if mixed else 'fp64'
         if fp64_product not in self.FP64_PRODUCT:
             raise ValueError(f'fp64_product must be one of {sorted(self.FP64_PRODUCT)}')
-        if self.matrix == 'hierarchical' and (mixed or precondition == 'lu32'):
-            raise ValueError("the compressed operator solves in FP64 with precondition 'block_jacobi' or 'none'")
+        if self.matrix == 'hierarchical' and precondition == 'lu32':
+            raise ValueError("the compressed operator solves with precondition 'block_jacobi' or 'none'")
         nf = len(f)
         if anchors is None:
             anchors = nf
@@ -785,7 +785,14 @@ class PeecModel(PeecTopology):
                 e1.record()
                 torch.cuda.synchronize()
                 precondition_ms += e0.elapsed_time(e1)
-            if mixed:
+            if mixed and self.matrix == 'hierarchical':
+                # the inner products: the H-matrices' low-rank blocks in BF16 on the tensor cores (dense leaves FP64)
+                for which, H in ((0, self.HL), (1, self.HP)):
+                    if getattr(H, '_lowrank', None) is None:
+                        H._lowrank = H.lowrank_plan()
+                    if H._lowrank is not None:
+                        _lib.check(lib.pcbqs_gb300_peec_set_lowrank(handle, which, ctypes.byref(H._lowrank[1])), lib)
+            elif mixed:
                 # single-precision copies of L and P for the inner products; FP64 outer residuals
                 Lf, Pf = self.Lf, self.Pf
                 if Lf is None:
@@ -803,7 +810,7 @@ class PeecModel(PeecTopology):
                 precondition_ms += factored.result()
                 factored = None
                 factor_stages()
-            if mixed:
+            if mixed and self.matrix != 'hierarchical':
                 Pfim = self.Pfim.data_ptr() if self.Pfim is not None else None
                 _lib.check(lib.pcbqs_gb300_peec_single(handle, Lf.data_ptr(), Lf.stride(0), Pf.data_ptr(), Pfim,
                                                        Pf.stride(0)), lib)

@@ -74,8 +74,47 @@ def test_compressed_rejects_what_needs_dense_matrices(device_library):
     from pcbqs_gb300.board import Board
     from pcbqs_gb300.peec import PeecModel
     model = PeecModel(Board.load('tiny'), matrix='hierarchical', hmatrix=dict(leaf=64))
-    with pytest.raises(ValueError, match='FP64'):
-        model.assemble(mixed=True)
     model.assemble()
     with pytest.raises(ValueError, match='block_jacobi'):
         model.solve([1e6], precondition='lu32')
+
+
+@pytest.mark.parametrize('kernel,k', [('inductance', 16), ('inductance', 128), ('potential', 40)])
+def test_lowrank_product_on_tensor_cores(device_library, kernel, k):
+    """The H-matrix product with its low-rank blocks in BF16 three-part products on the tensor cores against the
+    FP64 product: the difference stays at BF16x3's level relative to the low-rank blocks' share."""
+    import torch
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.fill import DeviceFill
+    from pcbqs_gb300.hmatrix import DeviceHMatrix
+    b = Board.load('strip')
+    fill = DeviceFill(b.nodes, b.tris, b.z, 1, 3.0)
+    H = DeviceHMatrix(fill, tol=1e-8, leaf=64, kernel=kernel)
+    assert H.low_rank > 0
+    g = torch.Generator(device='cuda').manual_seed(5)
+    X = torch.complex(torch.randn(H.n, k, device='cuda', generator=g, dtype=torch.float64),
+                      torch.randn(H.n, k, device='cuda', generator=g, dtype=torch.float64))
+    ref = H.matmat(X)
+    ours = H.matmat_lowrank(X)
+    err = (torch.linalg.norm(ours - ref) / torch.linalg.norm(ref)).item()
+    print(f'{kernel} k={k}: {H.low_rank} low-rank blocks, BF16 product against FP64 {err:.2e}')
+    assert err < 1e-4, err
+    again = H.matmat_lowrank(X)
+    assert torch.equal(again, ours)               # deterministic (slot rows summed in block order)
+
+
+@pytest.mark.parametrize('board', ['strip', 'viapair'])
+def test_compressed_mixed_solve_matches_reference(device_library, board):
+    """The mixed compressed solve: inner GMRES with the low-rank blocks in BF16 on the tensor cores, FP64 outer
+    residuals through the FP64 H-matrix products; every column to 1e-8 and the port impedances to the reference."""
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel
+    g = _golden(board)
+    model = PeecModel(Board.load(board), matrix='hierarchical', hmatrix=dict(tol=1e-9, leaf=64))
+    model.assemble(mixed=True)
+    res = model.solve(g['freqs'], precondition='block_jacobi', mixed=True)
+    err = np.abs(res.impedance - g['Z']).max() / np.abs(g['Z']).max()
+    print(f'{board} mixed compressed: GMRES steps {res.iterations.max()}, outer {res.timings.get("outer_steps")}, '
+          f'port Z error {err:.2e}')
+    assert (res.residual <= 1e-8).all()
+    assert err < 1e-6, err
