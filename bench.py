@@ -537,8 +537,33 @@ def case_lusolve(board, k=128, method=3, math=2):
         lib.pcbqs_gb300_peec_destroy(handle)
 
 
+def case_lowrank(board, k=128, leaf=256, tol=1e-6):
+    """A board's inductance H-matrix (ACA to `tol`, leaves of `leaf`), then its product with k complex columns three
+    times in FP64 (k_hm_apply_blocks) and three times with the low-rank blocks in BF16 on the tensor cores
+    (k_pack_xt, k_tc_update<4>, k_tc_update<5>; the dense leaves in FP64)."""
+    import torch
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.fill import DeviceFill
+    from pcbqs_gb300.hmatrix import DeviceHMatrix
+    k, leaf, tol = int(k), int(leaf), float(tol)
+    b = Board.load(board)
+    fill = DeviceFill(b.nodes, b.tris, b.z, 1, 3.0)
+    t0 = time.perf_counter()
+    H = DeviceHMatrix(fill, tol=tol, leaf=leaf, kernel='inductance')
+    print(f'hmatrix {board}: n={H.n}, {H.nblocks} blocks ({H.low_rank} low rank, rank <= {H.max_rank}), '
+          f'{H.bytes / 1e9:.2f} GB of {H.n * H.n * 8 / 1e9:.2f} GB dense, built in {time.perf_counter() - t0:.1f} s',
+          flush=True)
+    g = torch.Generator(device='cuda').manual_seed(1)
+    X = torch.randn(H.n, k, dtype=torch.complex128, device='cuda', generator=g)
+    H.matmat_lowrank(X)                              # packs the low-rank plan
+    for name, fn in (('fp64', H.matmat), ('bf16 low-rank', H.matmat_lowrank)):
+        for _ in range(3):
+            ms, Y = _event_ms(lambda: fn(X))
+            print(f'hmatrix product {name} k={k}: {ms:.2f} ms', flush=True)
+
+
 CASES = dict(fill=case_fill, lu=case_lu, getrf=case_getrf, potrf=case_potrf, dense=case_dense, update=case_update,
-             lusolve=case_lusolve)
+             lusolve=case_lusolve, lowrank=case_lowrank)
 
 
 def kernel_case(spec):
