@@ -562,8 +562,63 @@ def case_lowrank(board, k=128, leaf=256, tol=1e-6):
             print(f'hmatrix product {name} k={k}: {ms:.2f} ms', flush=True)
 
 
+def case_c5(k=32, leaf=256, tol=1e-6):
+    """The large compressed board (tests/golden/c5.npz, config C5's shape): the inductance H-matrix of its RWG edges
+    and the potential H-matrix of its triangles (ACA to `tol`, leaves of `leaf`, rank up to 32), their products
+    with k complex columns in FP64 and with the low-rank blocks in BF16 on the tensor cores, and the Biot-Savart
+    field of random sheet currents on a 256 x 256 grid 1 mm above the board (h_grid). Prints one JSON line. No PEEC
+    solve: block-Jacobi does not converge on pours, and the dense complex64 factor of its ~320,000 unknowns would
+    take 820 GB."""
+    import json as _json
+    import torch
+    from pcbqs_gb300.biot import h_grid
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.fill import DeviceFill
+    from pcbqs_gb300.hmatrix import DeviceHMatrix
+    k, leaf, tol = int(k), int(leaf), float(tol)
+    b = Board.load('c5')
+    out = dict(case='c5', triangles=int(len(b.tris)), vias=int(b.nv), ports=len(b.ports), k=k, leaf=leaf, tol=tol)
+    t0 = time.perf_counter()
+    fill = DeviceFill(b.nodes, b.tris, b.z, 1, 3.0)
+    out['geometry_s'] = round(time.perf_counter() - t0, 2)
+    g = torch.Generator(device='cuda').manual_seed(1)
+    for name, kernel in (('L', 'inductance'), ('P', 'potential')):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H = DeviceHMatrix(fill, tol=tol, leaf=leaf, kernel=kernel, er=b.er)
+        torch.cuda.synchronize()
+        rec = dict(n=H.n, build_s=round(time.perf_counter() - t0, 2), blocks=H.nblocks, low_rank=H.low_rank,
+                   max_rank=H.max_rank, gbytes=round(H.bytes / 1e9, 3), dense_gbytes=round(H.n * H.n * 8 / 1e9, 1),
+                   entries_per_s=round(H.entries / (time.perf_counter() - t0), 1))
+        X = torch.randn(H.n, k, dtype=torch.complex128, device='cuda', generator=g)
+        ref = H.matmat(X)
+        H.matmat_lowrank(X)
+        rec['fp64_ms'] = round(min(_event_ms(lambda: H.matmat(X))[0] for _ in range(3)), 2)
+        rec['bf16_lowrank_ms'] = round(min(_event_ms(lambda: H.matmat_lowrank(X))[0] for _ in range(3)), 2)
+        rec['bf16_vs_fp64'] = float((torch.linalg.norm(H.matmat_lowrank(X) - ref) / torch.linalg.norm(ref)).item())
+        out[name] = rec
+        print(name, rec, flush=True)
+        del H, X, ref
+        torch.cuda.empty_cache()
+    from pcbqs_gb300.rwg import RWG
+    r = RWG(b.nodes, b.tris)                          # the board's own coordinates (the fill's are centred)
+    rng = np.random.default_rng(2)
+    I = rng.standard_normal(r.Ne) + 1j * rng.standard_normal(r.Ne)
+    lt = {int(l): np.flatnonzero(b.layer == l) for l in np.unique(b.layer)}
+    lo, hi = b.nodes.min(0), b.nodes.max(0)
+    x, y = np.linspace(lo[0], hi[0], 256), np.linspace(lo[1], hi[1], 256)
+    top = float(np.max(b.z)) + 1e-3
+    h_grid(r, lt, b.z, I, x, y, [top])                # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Hf = h_grid(r, lt, b.z, I, x, y, [top])
+    torch.cuda.synchronize()
+    out['h_grid'] = dict(points=256 * 256, seconds=round(time.perf_counter() - t0, 3), finite=bool(np.isfinite(Hf).all()))
+    print(_json.dumps(out), flush=True)
+
+
 CASES = dict(fill=case_fill, lu=case_lu, getrf=case_getrf, potrf=case_potrf, dense=case_dense, update=case_update,
-             lusolve=case_lusolve, lowrank=case_lowrank)
+             lusolve=case_lusolve, lowrank=case_lowrank, c5=case_c5)
 
 
 def kernel_case(spec):

@@ -20,6 +20,8 @@ The boards themselves are synthetic stand-ins with the shapes and sizes of the b
     PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py viapair    (that board alone; the others keep their meshes)
     PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py planes16   (the plane pair with 16 ports, the batched
                                                    sweep's board)
+    PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py c5         (config C5's shape: four 100 x 80 mm pours with
+                                                   voids, 200 plated vias, 16 ports, about 200,000 triangles)
     PCBQS_REFERENCE_SRC=<checkout>/src python tests/golden/make_meshes.py train      (train_0 .. train_5: seeded random small boards, alternately a
                                                    plane pair and a via-joined strip pair of random sizes, vias and
                                                    mesh sizes; the learned preconditioner's training systems)
@@ -264,6 +266,67 @@ def viapair(core, length=10.0, width=2.0, gap=0.2, h=0.3):
                     vias)
 
 
+def c5(core, size=(100.0, 80.0), z=(0.0, 0.2, 1.4, 1.6), n_vias=200, n_ports=16, h=0.6, seed=11, voids=3):
+    """Four copper pours of size[0] x size[1] mm at heights z mm, each with `voids` seeded circular cutouts (12-gons,
+    r 2-5 mm); `n_vias` plated vias (r 0.15 mm) at seeded sites, each joining a pair of layers (1-2, 3-4, 2-3, 1-4 in
+    turn: a hexagonal ring and its fan in both, an antipad in the layers between), and `n_ports` ports from a 0.6 mm
+    pad on layer 2 to one on layer 1 at the same place. About 200,000 triangles at h = 0.6 mm."""
+    rng = np.random.default_rng(seed)
+    W, H = size
+    r_via, r_anti, pad = 0.15, 0.35, 0.3
+    holes_of = []
+    for s in range(len(z)):
+        holes_of.append([(float(rng.uniform(8, W - 8)), float(rng.uniform(8, H - 8)), float(rng.uniform(2, 5)))
+                         for _ in range(voids)])
+    clear = lambda x, y, m: all(np.hypot(x - a, y - b) > r + m for hs in holes_of for a, b, r in hs)
+    sites = []
+    for _ in range(200000):
+        if len(sites) == n_vias + n_ports:
+            break
+        x, y = float(rng.uniform(2, W - 2)), float(rng.uniform(2, H - 2))
+        if clear(x, y, 1.0) and all(np.hypot(x - a, y - b) > 1.6 for a, b in sites):
+            sites.append((x, y))
+    if len(sites) < n_vias + n_ports:
+        raise ValueError('board too small for its vias and ports')
+    vias, port_sites = sites[:n_vias], sites[n_vias:]
+    joins = [(0, 1), (2, 3), (1, 2), (0, 3)]
+    sheets, fans, barrels = [], [], []
+    fan_index = {}
+    for s, zz in enumerate(z):
+        loops, holes, points = [], [], []
+        for k, (x, y) in enumerate(vias):
+            a, b = joins[k % len(joins)]
+            if s in (a, b):
+                loops.append(ngon(x, y, r_via, 6))
+                points.append((x, y))
+                fan_index[(k, s)] = len(fans)
+                fans.append((s, (x, y)))
+            elif a < s < b:
+                holes.append(ngon(x, y, r_anti, 8, np.pi / 8))
+        for x, y, r in holes_of[s]:
+            holes.append(ngon(x, y, r, 12))
+        if s in (0, 1):
+            for (x, y) in port_sites:
+                loops.append(rect_loop(x - pad, y - pad, x + pad, y + pad, 0.3))
+        vert, tri = mesh_sheet(core, rect_loop(0, 0, W, H, h), loops, holes, points, h)
+        sheets.append((vert, tri, zz))
+        print(f'c5 layer {s}: {len(tri)} triangles', flush=True)
+    for k, (x, y) in enumerate(vias):
+        a, b = joins[k % len(joins)]
+        barrels.append((x, y, r_via, a, b, fan_index[(k, a)], fan_index[(k, b)]))
+    terminals, ports = {}, []
+    for i, (x, y) in enumerate(port_sites):
+        box = (x - pad, y - pad, x + pad, y + pad)
+        terminals[f'pwr{i}'] = [(1, box)]
+        terminals[f'gnd{i}'] = [(0, box)]
+        ports.append((f'port{i}', f'pwr{i}', f'gnd{i}'))
+    return assemble(sheets, terminals, fans, ports,
+                    dict(thickness=0.035e-3, sigma=5.8e7, er=4.3,
+                         description=f'{W:g} x {H:g} mm four-layer board, {voids} voids per pour, {n_vias} vias, '
+                                     f'{n_ports} ports, h {h} mm'),
+                    barrels)
+
+
 def training_board(core, seed):
     """A seeded random small board: a plane pair (even seeds) or a via-joined strip pair (odd seeds)."""
     rng = np.random.default_rng(1000 + seed)
@@ -311,6 +374,12 @@ if __name__ == '__main__':
         data = planes(reference_core(), n_ports=16)
         np.savez_compressed(HERE / 'planes16.npz', **data)
         print('planes16', len(data['tris']), 'triangles', len(data['nodes']), 'nodes')
+    elif sys.argv[1:] == ['c5']:
+        # the large compressed board (config C5's shape: four layers, 100 x 80 mm, pours, 200 vias)
+        RNG = np.random.default_rng(5)
+        data = c5(reference_core())
+        np.savez_compressed(HERE / 'c5.npz', **data)
+        print('c5', len(data['tris']), 'triangles', len(data['nodes']), 'nodes', len(data['via_seg']), 'vias')
     elif sys.argv[1:] == ['train']:
         core = reference_core()
         for i in range(6):
