@@ -539,8 +539,9 @@ def case_lusolve(board, k=128, method=3, math=2):
 
 def case_lowrank(board, k=128, leaf=256, tol=1e-6):
     """A board's inductance H-matrix (ACA to `tol`, leaves of `leaf`), then its product with k complex columns three
-    times in FP64 (k_hm_apply_blocks) and three times with the low-rank blocks in BF16 on the tensor cores
-    (k_pack_xt, k_tc_update<4>, k_tc_update<5>; the dense leaves in FP64)."""
+    times each: in FP64 (k_hm_apply_blocks), with the low-rank blocks in BF16 on the tensor cores (k_pack_xt,
+    k_tc_update<4>, k_tc_update<5>; the dense leaves in FP64), and with every block on the tensor cores (the dense
+    leaves by k_tc_update<6>)."""
     import torch
     from pcbqs_gb300.board import Board
     from pcbqs_gb300.fill import DeviceFill
@@ -555,8 +556,10 @@ def case_lowrank(board, k=128, leaf=256, tol=1e-6):
           flush=True)
     g = torch.Generator(device='cuda').manual_seed(1)
     X = torch.randn(H.n, k, dtype=torch.complex128, device='cuda', generator=g)
-    H.matmat_lowrank(X)                              # packs the low-rank plan
-    for name, fn in (('fp64', H.matmat), ('bf16 low-rank', H.matmat_lowrank)):
+    H.matmat_lowrank(X)                              # packs the low-rank plans
+    H.matmat_lowrank(X, dense=True)
+    for name, fn in (('fp64', H.matmat), ('bf16 low-rank', H.matmat_lowrank),
+                     ('bf16 all blocks', lambda v: H.matmat_lowrank(v, dense=True))):
         for _ in range(3):
             ms, Y = _event_ms(lambda: fn(X))
             print(f'hmatrix product {name} k={k}: {ms:.2f} ms', flush=True)
@@ -593,9 +596,14 @@ def case_c5(k=32, leaf=256, tol=1e-6):
         X = torch.randn(H.n, k, dtype=torch.complex128, device='cuda', generator=g)
         ref = H.matmat(X)
         H.matmat_lowrank(X)
+        H.matmat_lowrank(X, dense=True)
         rec['fp64_ms'] = round(min(_event_ms(lambda: H.matmat(X))[0] for _ in range(3)), 2)
         rec['bf16_lowrank_ms'] = round(min(_event_ms(lambda: H.matmat_lowrank(X))[0] for _ in range(3)), 2)
-        rec['bf16_vs_fp64'] = float((torch.linalg.norm(H.matmat_lowrank(X) - ref) / torch.linalg.norm(ref)).item())
+        rec['bf16_all_ms'] = round(min(_event_ms(lambda: H.matmat_lowrank(X, dense=True))[0] for _ in range(3)), 2)
+        rec['bf16_lowrank_vs_fp64'] = float((torch.linalg.norm(H.matmat_lowrank(X) - ref) /
+                                             torch.linalg.norm(ref)).item())
+        rec['bf16_all_vs_fp64'] = float((torch.linalg.norm(H.matmat_lowrank(X, dense=True) - ref) /
+                                         torch.linalg.norm(ref)).item())
         out[name] = rec
         print(name, rec, flush=True)
         del H, X, ref

@@ -313,6 +313,13 @@ typedef struct pcbqs_gb300_lowrank {
     int32_t ngroups, ntiles;
     const int32_t *tile_group, *tile_m, *pad_pos;
     int64_t n_pad;
+    /* optional (dplane null: the dense leaves stay FP64): the dense leaves on the tensor cores, their plane
+     * (drows x 2 dpitch BF16), groups and tiles in the same formats; meta_dense is then empty */
+    const void *dplane;
+    int64_t drows, dpitch;
+    const void *dgroups;
+    int32_t ndgroups, ndtiles;
+    const int32_t *dtile_group, *dtile_m;
 } pcbqs_gb300_lowrank;
 /* Y = H X with the dense blocks in FP64 and the low-rank blocks' stacked U (V^T X) products on the tcgen05 tensor
  * cores: BF16 three-part products, FP32 accumulation (phase one R X[J] for every block and direction, one tile each;

@@ -51,7 +51,10 @@ class LowRankDesc(ctypes.Structure):
     _fields_ = [('meta_dense', c_void_p), ('slot0_dense', c_void_p), ('ndense', ctypes.c_int64), ('lplane', c_void_p),
                 ('lrows', ctypes.c_int64), ('rplane', c_void_p), ('rwidth', ctypes.c_int64), ('groups', c_void_p),
                 ('ngroups', ctypes.c_int32), ('ntiles', ctypes.c_int32), ('tile_group', c_void_p),
-                ('tile_m', c_void_p), ('pad_pos', c_void_p), ('n_pad', ctypes.c_int64)]
+                ('tile_m', c_void_p), ('pad_pos', c_void_p), ('n_pad', ctypes.c_int64), ('dplane', c_void_p),
+                ('drows', ctypes.c_int64), ('dpitch', ctypes.c_int64), ('dgroups', c_void_p),
+                ('ndgroups', ctypes.c_int32), ('ndtiles', ctypes.c_int32), ('dtile_group', c_void_p),
+                ('dtile_m', c_void_p)]
 
 
 class PeecDesc(ctypes.Structure):

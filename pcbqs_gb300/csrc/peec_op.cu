@@ -1320,10 +1320,24 @@ int pcbqs_gb300_peec_set_compressed(pcbqs_gb300_peec *h, const pcbqs_gb300_hmat 
 }
 
 static int lowrank_of(const pcbqs_gb300_lowrank *lr, int64_t n, int max_rank, PeecOp::HMat &H, const char *what) {
-    if (!lr || !lr->lplane || !lr->rplane || !lr->groups || lr->ngroups <= 0 || lr->ntiles <= 0 || !lr->tile_group ||
-        !lr->tile_m || !lr->pad_pos || lr->n_pad < n || lr->n_pad % 64 || lr->rwidth % 64 || lr->lrows < 128 ||
-        lr->ndense < 0 || (lr->ndense > 0 && (!lr->meta_dense || !lr->slot0_dense)) || max_rank > 64)
+    const bool low = lr && lr->ngroups > 0, dense = lr && lr->dplane && lr->ndgroups > 0;
+    if (!lr || (!low && !dense) || !lr->pad_pos || lr->n_pad < n || lr->n_pad % 64 || lr->ndense < 0 ||
+        (lr->ndense > 0 && (!lr->meta_dense || !lr->slot0_dense)) || max_rank > 64 ||
+        (low && (!lr->lplane || !lr->rplane || !lr->groups || lr->ntiles <= 0 || !lr->tile_group || !lr->tile_m ||
+                 lr->rwidth % 64 || lr->lrows < 128)) ||
+        (dense && (!lr->dgroups || lr->ndtiles <= 0 || !lr->dtile_group || !lr->dtile_m || lr->dpitch % 64 ||
+                   lr->drows < 128)))
         return pfail(ERR_ARGUMENT, "%s: invalid low-rank plan (ranks up to 64)", what);
+    if (dense) {
+        H.plan.dplane = lr->dplane;
+        H.plan.drows = lr->drows;
+        H.plan.dpitch = lr->dpitch;
+        H.plan.dgroups = static_cast<const LrGroup *>(lr->dgroups);
+        H.plan.ndgroups = lr->ndgroups;
+        H.plan.dtile_group = lr->dtile_group;
+        H.plan.dtile_m = lr->dtile_m;
+        H.plan.ndtiles = lr->ndtiles;
+    }
     H.plan.lplane = lr->lplane;
     H.plan.lrows = lr->lrows;
     H.plan.rplane = lr->rplane;

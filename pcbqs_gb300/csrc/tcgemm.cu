@@ -494,6 +494,8 @@ struct TileArgs {
     unsigned long long wait;
 };
 
+// MODE 6: the dense leaves, Y[I] = D_g X[J_g] over (group, row tile) tiles: A = the dense plane at a_row0 (K: J's
+// padded range in parts of dpitch), B = X's transposed plane at J's padded range; stored into the slot rows.
 // MODE 4 / 5: the two phases of the low-rank product (LrGroup): 4 T_g = R_g X[J_g] (A = R's plane, 128 rows
 // of which rank_g hold R_g; B = X's transposed plane at J_g's padded range; K = 3 part segments of kb slices), its
 // tile written as the BF16 parts of T_g^T into the T plane; 5 Y[I_g] = L_g T_g (A = L's plane at a_row0, B = the
@@ -537,6 +539,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
         m_tile = args.tile_m[blockIdx.x];
         n_tile = 0;
         kb_total = 3;
+    } else if (MODE == 6) {
+        grp = args.groups[args.tile_group[blockIdx.x]];
+        m_tile = args.tile_m[blockIdx.x];
+        n_tile = 0;
+        kb_total = 3 * grp.kb;
     }
     const int64_t m0 = (int64_t)m_tile * BM;
     const int nchunks = (kb_total + CHUNK - 1) / CHUNK;
@@ -599,6 +606,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
                     xb = SEG_B[kb] * BK;
                     ya = grp.a_row0 + (int)m0;
                     yb = grp.t_row0;
+                } else if (MODE == 6) {
+                    const int sg = kb / grp.kb, off = (kb - sg * grp.kb) * BK;
+                    xa = SEG_A[sg] * args.a_pitch + off;
+                    xb = SEG_B[sg] * args.b_pitch + grp.a_x0 + off;
+                    ya = grp.a_row0 + (int)m0;
+                    yb = 0;
                 }
                 tma_load_2d(a_dst, &map_a, xa, ya, smem_addr(&full[s]));
                 tma_load_2d(b_dst, &map_b, xb, yb, smem_addr(&full[s]));
@@ -751,7 +764,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_update(const __grid_constant_
                     }
                 }
             }
-        } else if (!*abort && MODE == 5) {
+        } else if (!*abort && (MODE == 5 || MODE == 6)) {
             const int64_t row = m0 + q * 32 + lane;
             const int64_t c0 = h * (BN / 4);
             if (row < grp.rows) {
@@ -860,7 +873,8 @@ cudaError_t configure() {
             (e = cudaFuncSetAttribute(k_tc_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
             (e = cudaFuncSetAttribute(k_tc_update<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
             (e = cudaFuncSetAttribute(k_tc_update<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
-            (e = cudaFuncSetAttribute(k_tc_update<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
+            (e = cudaFuncSetAttribute(k_tc_update<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)) ||
+            (e = cudaFuncSetAttribute(k_tc_update<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM)))
             return e;
         configured[device] = true;
     }
@@ -1116,10 +1130,15 @@ size_t tc_lowrank_scratch_bytes(int64_t n_pad, int ngroups) {
 
 cudaError_t tc_lowrank_product(const LowRankPlan &p, int k, const double2 *X, double2 *slots, void *scratch,
                                int *error, unsigned long long wait_cycles, cudaStream_t stream) {
-    if (p.ngroups <= 0) return cudaSuccess;
-    if (k <= 0 || k > BN / 2 || !X || !slots || !scratch || !error || !p.lplane || !p.rplane || !p.groups ||
-        !p.tile_group || !p.tile_m || !p.pad_pos || p.n <= 0 || p.n_pad <= 0 || p.n_pad % BK || p.rwidth % BK ||
-        p.lrows < BM || p.ntiles <= 0)
+    if (p.ngroups <= 0 && p.ndgroups <= 0) return cudaSuccess;
+    if (p.ndgroups > 0 && (!p.dplane || !p.dgroups || !p.dtile_group || !p.dtile_m || p.ndtiles <= 0 ||
+                           p.drows < BM || p.dpitch % BK))
+        return cudaErrorInvalidValue;
+    if (k <= 0 || k > BN / 2 || !X || !slots || !scratch || !error || !p.pad_pos || p.n <= 0 || p.n_pad <= 0 ||
+        p.n_pad % BK)
+        return cudaErrorInvalidValue;
+    if (p.ngroups > 0 && (!p.lplane || !p.rplane || !p.groups || !p.tile_group || !p.tile_m || p.rwidth % BK ||
+                          p.lrows < BM || p.ntiles <= 0))
         return cudaErrorInvalidValue;
     cudaError_t e = configure();
     if (e) return e;
@@ -1139,6 +1158,20 @@ cudaError_t tc_lowrank_product(const LowRankPlan &p, int k, const double2 *X, do
     args.tiles_m = 1;
     args.tiles_n = 1;
     args.seg_kblocks = 1;
+    if (p.ndgroups > 0) {         // the dense leaves: D_g X[J_g] into their slot rows
+        if (!plane_map(&ma, p.dplane, p.drows, 2 * p.dpitch, BM) || !plane_map(&mb, xt, 256, 2 * p.n_pad, BN))
+            return cudaErrorNotSupported;
+        TileArgs d = args;
+        d.groups = p.dgroups;
+        d.tile_group = p.dtile_group;
+        d.tile_m = p.dtile_m;
+        d.a_pitch = (int)p.dpitch;
+        d.b_pitch = (int)p.n_pad;
+        d.slots = slots;
+        k_tc_update<6><<<(unsigned)p.ndtiles, THREADS, SMEM, stream>>>(ma, mb, d);
+        note_launches(1);
+    }
+    if (p.ngroups <= 0) return cudaGetLastError();
     // phase one: T_g = R_g X[J_g], one tile per group
     if (!plane_map(&ma, p.rplane, BM, 2 * p.rwidth, BM) || !plane_map(&mb, xt, 256, 2 * p.n_pad, BN))
         return cudaErrorNotSupported;

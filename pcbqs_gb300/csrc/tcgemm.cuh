@@ -37,12 +37,21 @@ struct LowRankPlan {
     int ntiles = 0;
     const int32_t *pad_pos = nullptr;
     int64_t n = 0, n_pad = 0;
+    // the dense leaves on the tensor cores too (optional): their plane (drows x 2 dpitch BF16: parts h at 0, m at
+    // dpitch; group g's block in rows a_row0 .., its columns at J's padded positions), groups and tiles
+    const void *dplane = nullptr;
+    int64_t drows = 0, dpitch = 0;
+    const LrGroup *dgroups = nullptr;
+    int ndgroups = 0;
+    const int32_t *dtile_group = nullptr, *dtile_m = nullptr;
+    int ndtiles = 0;
 };
 
 // Scratch of tc_lowrank_product: the right-hand sides' transposed plane (256 x 2 n_pad BF16) and the T plane
 // (ngroups x 256 x 128 BF16); zeroed once when allocated (padding positions are never written).
 size_t tc_lowrank_scratch_bytes(int64_t n_pad, int ngroups);
-// The low-rank blocks' contributions to Y = H X (X: n x k complex128 row-major, k <= 128) in BF16 three-part
+// The low-rank blocks' contributions to Y = H X (and the dense leaves', when the plan holds them: MODE 6, Y[I] = D X[J]
+// in three part products, one group per block and direction, written to its slot rows) (X: n x k complex128 row-major, k <= 128) in BF16 three-part
 // products with FP32 accumulation: phase one T_g = R_g X[J_g] for every group (one tile each), written as T_g^T's
 // BF16 parts; phase two L_g T_g into the group's slot rows (slots: complex128, k wide), summed with the dense blocks'
 // slots afterwards. `error`, `wait_cycles`, `stream` as in tc_update_c64.

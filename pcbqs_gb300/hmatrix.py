@@ -281,17 +281,18 @@ class DeviceHMatrix:
         d.max_rank = self.max_rank
         return d
 
-    def lowrank_plan(self):
+    def lowrank_plan(self, dense=False):
         """The low-rank blocks packed for the tensor cores (pcbqs_gb300_hmatrix_apply_lowrank): each block gives a
         group per direction, Y[I] += L (R X[J]) with (L, R) = (U, V) forward and (V^T, U^T) transposed, the factors
         split into BF16 parts h, m. X is read in a padded cluster order, each leaf's range rounded up to 64, so every
-        cluster is a 64-aligned range the tensor copies can address. Returns (arrays kept alive, the C struct), or
-        None when no block is low rank."""
+        cluster is a 64-aligned range the tensor copies can address. dense=True packs the dense leaves too (one
+        group per block and direction, D or D^T at J's padded positions), so the whole product runs on the tensor
+        cores. Returns (arrays kept alive, the C struct), or None when there is nothing to pack."""
         tree, dev = self.tree, self.store.device
         meta = self.meta.cpu().numpy()
         slot0 = self.slot0.cpu().numpy()
         low = np.flatnonzero(meta[:, 7] >= 0)
-        if not len(low):
+        if not len(low) and not dense:
             return None
         if self.max_rank > 64:
             raise ValueError('the tensor-core low-rank product takes ranks up to 64')
@@ -328,6 +329,22 @@ class DeviceHMatrix:
                     break
         lrows = a_row0 + 128
         rwidth = max(b_x0, 64)
+        dgroups, dmats = [], []
+        d_row0 = 0
+        if dense:
+            for w in np.flatnonzero(meta[:, 7] < 0):
+                la, lb, so = int(meta[w, 1]), int(meta[w, 3]), int(meta[w, 4])
+                i, j = self._nodes[w]
+                D = store[so:so + la * lb].view(la, lb)
+                for M, rows_node, cols_node, slot in ((D, i, j, slot0[w, 0]), (D.T, j, i, slot0[w, 1])):
+                    p0, p1 = span(cols_node)
+                    cols_pos = torch.as_tensor(pos[tree.ids(cols_node)] - p0, device=dev, dtype=torch.int64)
+                    dgroups.append((d_row0, M.shape[0], p0, 0, (p1 - p0) // 64, 0, 0, 0, int(slot)))
+                    dmats.append((M, cols_pos))
+                    d_row0 += M.shape[0]
+                    if meta[w, 6]:                  # a diagonal block is stored whole: one direction
+                        break
+        dpitch = max([g[4] * 64 for g in dgroups] + [64])
 
         def parts(x):
             h = x.float().to(torch.bfloat16)
@@ -349,13 +366,28 @@ class DeviceHMatrix:
         assert gdt.itemsize == 40
         garr = np.array(groups, dtype=gdt)
         tiles = [(g, t) for g, grp in enumerate(groups) for t in range(-(-grp[1] // 128))]
-        dense = np.flatnonzero(meta[:, 7] < 0)
+        fp64_dense = np.flatnonzero(meta[:, 7] < 0) if not dense else np.zeros(0, np.int64)
         t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dt), device=dev)
         keep = dict(lplane=lplane, rplane=rplane, groups=t(garr.view(np.uint8), np.uint8),
-                    tile_group=t([g for g, _ in tiles], np.int32), tile_m=t([m for _, m in tiles], np.int32),
-                    pad_pos=t(pos, np.int32), meta_dense=t(meta[dense], np.int64), slot0_dense=t(slot0[dense], np.int64))
+                    tile_group=t([g for g, _ in tiles] or [0], np.int32), tile_m=t([m for _, m in tiles] or [0], np.int32),
+                    pad_pos=t(pos, np.int32), meta_dense=t(meta[fp64_dense].reshape(-1, 8), np.int64),
+                    slot0_dense=t(slot0[fp64_dense].reshape(-1, 2), np.int64))
         d = _lib.LowRankDesc()
-        d.meta_dense, d.slot0_dense, d.ndense = keep['meta_dense'].data_ptr(), keep['slot0_dense'].data_ptr(), len(dense)
+        d.meta_dense, d.slot0_dense, d.ndense = (keep['meta_dense'].data_ptr(), keep['slot0_dense'].data_ptr(),
+                                                 len(fp64_dense))
+        if dgroups:
+            dplane = torch.zeros((d_row0 + 128, 2 * dpitch), dtype=torch.bfloat16, device=dev)
+            for g, (M, cols_pos) in zip(dgroups, dmats):
+                h, m = parts(M)
+                r0, rows = g[0], g[1]
+                dplane[r0:r0 + rows][:, cols_pos] = h
+                dplane[r0:r0 + rows][:, dpitch + cols_pos] = m
+            dtiles = [(g, tt) for g, grp in enumerate(dgroups) for tt in range(-(-grp[1] // 128))]
+            keep.update(dplane=dplane, dgroups=t(np.array(dgroups, dtype=gdt).view(np.uint8), np.uint8),
+                        dtile_group=t([g for g, _ in dtiles], np.int32), dtile_m=t([m for _, m in dtiles], np.int32))
+            d.dplane, d.drows, d.dpitch = dplane.data_ptr(), d_row0 + 128, dpitch
+            d.dgroups, d.ndgroups, d.ndtiles = keep['dgroups'].data_ptr(), len(dgroups), len(dtiles)
+            d.dtile_group, d.dtile_m = keep['dtile_group'].data_ptr(), keep['dtile_m'].data_ptr()
         d.lplane, d.lrows = lplane.data_ptr(), lrows
         d.rplane, d.rwidth = rplane.data_ptr(), rwidth
         d.groups, d.ngroups, d.ntiles = keep['groups'].data_ptr(), len(groups), len(tiles)
@@ -364,18 +396,20 @@ class DeviceHMatrix:
         d.n_pad = n_pad
         return keep, d
 
-    def matmat_lowrank(self, X):
+    def matmat_lowrank(self, X, dense=False):
         """Y = H X with the low-rank blocks on the tensor cores in BF16 (pcbqs_gb300_hmatrix_apply_lowrank); the
-        dense blocks in FP64. X (n, k <= 128) complex128 on the device."""
-        if getattr(self, '_lowrank', None) is None:
-            self._lowrank = self.lowrank_plan()
+        dense blocks in FP64, or (dense=True) on the tensor cores too. X (n, k <= 128) complex128 on the device."""
+        plans = self.__dict__.setdefault('_plans', {})
+        if dense not in plans:
+            plans[dense] = self.lowrank_plan(dense=dense)
+        plan = plans[dense]
         X = X.reshape(self.n, -1).to(torch.complex128).contiguous()
-        if self._lowrank is None:
+        if plan is None:
             return self.matmat(X)
         Y = torch.empty_like(X)
         lib = _lib.load()
         d = self.desc()
-        _lib.check(lib.pcbqs_gb300_hmatrix_apply_lowrank(ctypes.byref(d), ctypes.byref(self._lowrank[1]), X.shape[1],
+        _lib.check(lib.pcbqs_gb300_hmatrix_apply_lowrank(ctypes.byref(d), ctypes.byref(plan[1]), X.shape[1],
                                                          X.data_ptr(), Y.data_ptr(),
                                                          ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
                    lib)
@@ -388,7 +422,7 @@ class DeviceHMatrix:
         index arrays go to host memory; the fill (its device context, the exact-entry source) is not kept, so a
         loaded matrix applies its blocks but evaluates no new entries. The triangle areas stay for
         potential_operator."""
-        state = {k: v for k, v in self.__dict__.items() if k not in ('fill', '_edges') + self._ARRAYS}
+        state = {k: v for k, v in self.__dict__.items() if k not in ('fill', '_edges', '_plans') + self._ARRAYS}
         for k in self._ARRAYS:
             state[k] = getattr(self, k).cpu().numpy()
         state['area'] = np.asarray(self.fill.geometry.area) if self.fill is not None else self.__dict__.get('area')

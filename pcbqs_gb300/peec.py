@@ -786,12 +786,13 @@ class PeecModel(PeecTopology):
                 torch.cuda.synchronize()
                 precondition_ms += e0.elapsed_time(e1)
             if mixed and self.matrix == 'hierarchical':
-                # the inner products: the H-matrices' low-rank blocks in BF16 on the tensor cores (dense leaves FP64)
+                # the inner products: the H-matrices' blocks, low rank and dense, in BF16 on the tensor cores
                 for which, H in ((0, self.HL), (1, self.HP)):
-                    if getattr(H, '_lowrank', None) is None:
-                        H._lowrank = H.lowrank_plan()
-                    if H._lowrank is not None:
-                        _lib.check(lib.pcbqs_gb300_peec_set_lowrank(handle, which, ctypes.byref(H._lowrank[1])), lib)
+                    plans = H.__dict__.setdefault('_plans', {})
+                    if True not in plans:
+                        plans[True] = H.lowrank_plan(dense=True)
+                    if plans[True] is not None:
+                        _lib.check(lib.pcbqs_gb300_peec_set_lowrank(handle, which, ctypes.byref(plans[True][1])), lib)
             elif mixed:
                 # single-precision copies of L and P for the inner products; FP64 outer residuals
                 Lf, Pf = self.Lf, self.Pf

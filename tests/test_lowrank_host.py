@@ -21,8 +21,20 @@ def _fake(seed=3, n=700, leaf=50):
     tree = ClusterTree(pts, pts, leaf)
     nodes = range(len(tree.start))
     pairs = [(i, j) for i in nodes for j in nodes if i < j and tree.separated(i, j, 1.0)][:12]
+    leaves = [k for k in nodes if tree.leaf(k)]
+    near = [(leaves[0], leaves[0]), (leaves[1], leaves[2]), (leaves[3], leaves[3]), (leaves[2], leaves[5])]
     meta, slot0, store, so, ioff = [], [], [], 0, 0
-    blocks = []
+    blocks, dense = [], []
+    for i, j in near:                                 # dense leaves (a diagonal one stored whole)
+        la, lb = tree.size(i), tree.size(j)
+        D = rng.standard_normal((la, lb))
+        if i == j:
+            D = D + D.T
+        store.append(D.ravel())
+        meta.append([ioff, la, ioff + la, lb, so, 0, int(i == j), -1])
+        dense.append((tree.ids(i), tree.ids(j), D, i == j))
+        so += la * lb
+        ioff += la + lb
     for i, j in pairs:
         la, lb = tree.size(i), tree.size(j)
         cap = 8
@@ -37,23 +49,27 @@ def _fake(seed=3, n=700, leaf=50):
     s = 0
     for m in meta:
         slot0.append([s, s + m[1]])
-        s += m[1] + m[3]
+        s += m[1] + (0 if m[6] else m[3])
     f = _Stand()
     f.tree, f.n, f.max_rank = tree, n, 8
     f.meta = torch.as_tensor(np.array(meta, np.int64))
     f.slot0 = torch.as_tensor(np.array(slot0, np.int64))
     f.store = torch.as_tensor(np.concatenate(store))
-    f._nodes = pairs
-    return f, blocks, s
+    f._nodes = near + pairs
+    return f, blocks, dense, s
 
 
 def _bf(x):
     return torch.as_tensor(x).float().to(torch.bfloat16).double().numpy()
 
 
+GDT = np.dtype([('a_row0', '<i4'), ('rows', '<i4'), ('a_x0', '<i4'), ('b_x0', '<i4'), ('kb', '<i4'),
+                ('t_row0', '<i4'), ('rank', '<i4'), ('pad', '<i4'), ('slot0', '<i8')])
+
+
 def test_lowrank_plan_emulated_matches_direct_sum():
-    f, blocks, nslots = _fake()
-    keep, d = DeviceHMatrix.lowrank_plan(f)
+    f, blocks, dense, nslots = _fake()
+    keep, d = DeviceHMatrix.lowrank_plan(f, dense=True)
     n, k = f.n, 5
     rng = np.random.default_rng(7)
     X = rng.standard_normal((n, k)) + 1j * rng.standard_normal((n, k))
@@ -68,9 +84,7 @@ def test_lowrank_plan_emulated_matches_direct_sum():
     xt[:2 * k, n_pad + pos] = m.T
     rp = keep['rplane'].double().numpy()
     lp = keep['lplane'].double().numpy()
-    groups = keep['groups'].numpy().view(np.dtype([('a_row0', '<i4'), ('rows', '<i4'), ('a_x0', '<i4'),
-                                                   ('b_x0', '<i4'), ('kb', '<i4'), ('t_row0', '<i4'),
-                                                   ('rank', '<i4'), ('pad', '<i4'), ('slot0', '<i8')]))
+    groups = keep['groups'].numpy().view(GDT)
     tplane = np.zeros((len(groups) * 256, 128))
     for g in groups:                                  # phase one: one tile, rows = ranks, columns = real columns
         D = np.zeros((128, 256))
@@ -96,11 +110,34 @@ def test_lowrank_plan_emulated_matches_direct_sum():
                                                                   SEG_B[s] * 64:SEG_B[s] * 64 + 64].T
         rows = min(128, g['rows'] - 128 * mt)
         slots[g['slot0'] + 128 * mt:g['slot0'] + 128 * mt + rows] = D[:rows, :2 * k]
+    # the dense leaves (MODE 6): D at J's padded positions against X's plane, into the slot rows
+    dp = keep['dplane'].double().numpy()
+    dpitch = d.dpitch
+    dgroups = keep['dgroups'].numpy().view(GDT)
+    for gi, mt in zip(keep['dtile_group'].numpy(), keep['dtile_m'].numpy()):
+        g = dgroups[gi]
+        r0 = g['a_row0'] + 128 * mt
+        a = dp[r0:r0 + 128]
+        a = np.vstack([a, np.zeros((128 - len(a), 2 * dpitch))])
+        D = np.zeros((128, 256))
+        for s in range(3):
+            for kk in range(g['kb']):
+                xa = SEG_A[s] * dpitch + kk * 64
+                xb = SEG_B[s] * n_pad + g['a_x0'] + kk * 64
+                D += a[:, xa:xa + 64] @ xt[:, xb:xb + 64].T
+        rows = min(128, g['rows'] - 128 * mt)
+        slots[g['slot0'] + 128 * mt:g['slot0'] + 128 * mt + rows] = D[:rows, :2 * k]
     # the slot rows of block w: forward rows a (slot0[w,0] ...), transposed rows b (slot0[w,1] ...)
     Y = np.zeros((n, 2 * k))
     exact = np.zeros((n, k), complex)
     s0 = f.slot0.numpy()
-    for w, (a_ids, b_ids, U, V) in enumerate(blocks):
+    for w, (a_ids, b_ids, D, same) in enumerate(dense):
+        Y[a_ids] += slots[s0[w, 0]:s0[w, 0] + len(a_ids)]
+        exact[a_ids] += D @ X[b_ids]
+        if not same:
+            Y[b_ids] += slots[s0[w, 1]:s0[w, 1] + len(b_ids)]
+            exact[b_ids] += D.T @ X[a_ids]
+    for w, (a_ids, b_ids, U, V) in enumerate(blocks, start=len(dense)):
         Y[a_ids] += slots[s0[w, 0]:s0[w, 0] + len(a_ids)]
         Y[b_ids] += slots[s0[w, 1]:s0[w, 1] + len(b_ids)]
         exact[a_ids] += U @ (V @ X[b_ids])
@@ -109,4 +146,5 @@ def test_lowrank_plan_emulated_matches_direct_sum():
     err = np.linalg.norm(Yc - exact) / np.linalg.norm(exact)
     assert err < 2e-4, err
     assert d.ngroups == 2 * len(blocks) and n_pad % 64 == 0 and rwidth % 64 == 0
+    assert d.ndgroups == sum(1 if same else 2 for *_, same in dense) and d.ndense == 0
     assert sorted(np.unique(pos)) == sorted(pos.tolist()) and pos.max() < n_pad
