@@ -63,7 +63,9 @@ def parse():
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--sweep', type=int, default=0,
                    help='also time a sweep of this many log-spaced frequencies (1 kHz to 100 MHz), all ports')
-    p.add_argument('--anchors', type=int, default=8, help='complex64 factors shared across the sweep')
+    p.add_argument('--anchors', type=int, default=6,
+                   help='complex64 factors shared across the sweep (64 frequencies: 4 -> 15.4 s, 6 -> 14.0 s, 8 -> '
+                        '14.9 s, 12 -> 21.0 s on one GB300)')
     p.add_argument('--sweep-board', default='planes16', help='the sweep\'s board (default: the 16-port plane pair)')
     p.add_argument('--product', default='tc3', choices=['tc3', 'tc6', 'fp32'],
                    help='the mixed solve\'s inner dense products over 16 or more columns')

@@ -581,13 +581,17 @@ class PeecModel(PeecTopology):
         self.timings['potential_solve_iterations'] = its.tolist()
         return x.cpu().numpy()
 
+    HM_COLUMNS = 64     # columns per compressed FP64 product (its blocks stage rank x columns in shared memory)
+
     def _mv_L(self, X):
         """L X for complex branch vectors X (ne, k), FP64 on the device (pcbqs_gb300_dense_apply, or the compressed
         product)."""
         if self.matrix == 'hierarchical':
             Xt = torch.as_tensor(np.ascontiguousarray(X, complex), device=self.device).reshape(self.ni, -1)
             Y = torch.empty_like(Xt)
-            Y[:self.ne] = self.HL.matmat(Xt[:self.ne])
+            for c in range(0, Xt.shape[1], self.HM_COLUMNS):
+                part = slice(c, c + self.HM_COLUMNS)
+                Y[:self.ne, part] = self.HL.matmat(Xt[:self.ne, part])
             if self.board.nv:
                 Y[self.ne:] = self.Lvia.to(torch.complex128) @ Xt[self.ne:]
             return Y.cpu().numpy().reshape(np.shape(X))
@@ -598,18 +602,28 @@ class PeecModel(PeecTopology):
             Xt = torch.as_tensor(np.ascontiguousarray(X, complex), device=self.device).reshape(self.nn, -1)
             if getattr(self, '_papply', None) is None:
                 self._papply = self.HP.potential_operator(self.board.node_of)
-            return self._papply(Xt).cpu().numpy().reshape(np.shape(X))
+            Y = torch.cat([self._papply(Xt[:, c:c + self.HM_COLUMNS].contiguous())
+                           for c in range(0, Xt.shape[1], self.HM_COLUMNS)], dim=1)
+            return Y.cpu().numpy().reshape(np.shape(X))
         Y = self._dense(self.P, X)
         return Y if self.Pim is None else Y + 1j * self._dense(self.Pim, X)
 
     def _dense(self, M, X):
+        """M X in FP64's accuracy: on the FP64 pipe below 4 columns, else from integer slices on the tensor cores
+        (pcbqs_gb300_dense_apply_sliced, six slices)."""
         Xt = torch.as_tensor(np.ascontiguousarray(X, complex), device=self.device)
+        shape = Xt.shape
+        Xt = Xt.reshape(shape[0], -1)
         Y = torch.empty_like(Xt)
         lib = _lib.load()
-        _lib.check(lib.pcbqs_gb300_dense_apply(M.shape[0], Xt.shape[1], M.data_ptr(), M.stride(0), Xt.data_ptr(),
-                                               Y.data_ptr(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
-                   lib)
-        return Y.cpu().numpy()
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        if Xt.shape[1] >= 4:
+            _lib.check(lib.pcbqs_gb300_dense_apply_sliced(M.shape[0], Xt.shape[1], M.data_ptr(), M.stride(0),
+                                                          Xt.data_ptr(), Y.data_ptr(), 6, 1 << 31, stream), lib)
+        else:
+            _lib.check(lib.pcbqs_gb300_dense_apply(M.shape[0], Xt.shape[1], M.data_ptr(), M.stride(0), Xt.data_ptr(),
+                                                   Y.data_ptr(), stream), lib)
+        return Y.cpu().numpy().reshape(shape)
 
     PRECONDITIONERS = {'none': 0, 'block_jacobi': 1, 'lu32': 2}
 
@@ -871,21 +885,23 @@ class PeecModel(PeecTopology):
                 except Exception:  # noqa: BLE001 -- the first error is the one raised
                     pass
             lib.pcbqs_gb300_peec_destroy(handle)
-        # back to the unclustered order, then currents, charges and source voltages (peec_iterative.py:331-341)
+        # back to the unclustered order, then currents, charges and source voltages (peec_iterative.py:331-341), for
+        # every (frequency, port) column at once: one P product over all of them
         Xo = np.empty_like(X)
         Xo[self.order] = X
         Z = np.zeros((len(f), npo, npo), complex)
         currents = np.zeros((len(f), self.nb, npo), complex)
         Kc, Kt = self.K[:, :self.nl], self.K[:, self.nl:]
+        correction = Xo[self.nl:] * np.repeat(zscale / self.pscale, npo)[None]
+        pcorrection = self._mv_P(np.asarray(self.T @ correction))
+        voltages = np.asarray(self.A[:, self.sources].T @ pcorrection)
+        loop_part = np.asarray(Kc @ Xo[:self.nl])
+        tree_part = np.asarray(Kt @ correction)
         for fi, w in enumerate(omegas):
-            xs = Xo[:, fi * npo:(fi + 1) * npo]
-            alpha = zscale[fi] / self.pscale
-            correction = alpha * xs[self.nl:]
-            currents[fi] = baseline + Kc @ xs[:self.nl] + 1j * w * (Kt @ correction)
+            cols = slice(fi * npo, (fi + 1) * npo)
+            currents[fi] = baseline + loop_part[:, cols] + 1j * w * tree_part[:, cols]
             currents[fi][self.sources] = excitation
-            pcorrection = self._mv_P(np.asarray(self.T @ correction))
-            voltage = source_voltage / (1j * w) + np.asarray(self.A[:, self.sources].T @ pcorrection)
-            Z[fi] = voltage
+            Z[fi] = source_voltage / (1j * w) + voltages[:, cols]
         self.timings['solve_s'] = time.perf_counter() - t0
         if not converged:
             raise RuntimeError(f'GMRES did not reach {self.tol:g}: residuals {res.max():.3g}, iterations {its.max()}')
