@@ -38,6 +38,12 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = 'fill+solve s/freq at 1e-8 residual: learned/mixed vs plain FP64 GPU; fill GB/s'
 FAR_FLOP, NEAR_FLOP = 210, {0: 936, 1: 3744, 2: 14976}   # algorithmic flops per pair (full moments)
+# transcendental evaluations per near pair (the analytic inner integrals: one log of positive terms and one
+# arctangent per (observation point, edge) of the 3-point rule at level 0, 4x that per refinement level), which the
+# algebraic flop count leaves out; and the FP64-pipe activity of k_fill_near measured by ncu on the plane pair's
+# first 8,000 triangles (sm__pipe_fp64_cycles_active, the near kernel's bound)
+NEAR_TRANSCENDENTALS = {0: 72, 1: 288, 2: 1152}
+NEAR_FP64_PIPE_ACTIVE = 0.871
 
 
 def parse():
@@ -159,10 +165,14 @@ def fill_roofline(model, fill_ms, mixed, peaks):
     # the 32 B of the four FP32 planes written once), scaled by this launch's pair count; the FP64 fill has no
     # capture at a size above L2, so no figure
     traffic = round(pairs * 989.2e6 / 32004000) if mixed else None
+    transcendentals = near0 * NEAR_TRANSCENDENTALS[0] + near1 * NEAR_TRANSCENDENTALS[model.fill.outer_levels]
     return dict(bound=bound, kernel='k_fill_tiles+k_fill_near', achieved=round(achieved, 4), peak=round(peak, 4),
                 unit='TFLOP/s', frac=round(achieved / peak, 4), traffic=traffic, flops_per_launch=flops,
                 far_pairs=far, near_pairs=[near0, near1], peak_source=source,
-                traffic_source='ncu dram bytes of k_fill_tiles on 8,000 triangles, scaled by pairs' if mixed else None)
+                traffic_source='ncu dram bytes of k_fill_tiles on 8,000 triangles, scaled by pairs' if mixed else None,
+                near_transcendentals_per_launch=transcendentals,
+                near_fp64_pipe_active=NEAR_FP64_PIPE_ACTIVE,
+                near_fp64_pipe_source='profiles/k_fill_near_planes_8k.md (sm__pipe_fp64_cycles_active, ncu)')
 
 
 def measured_peaks():
