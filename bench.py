@@ -73,6 +73,8 @@ def parse():
                    help='complex64 factors shared across the sweep (64 frequencies: 4 -> 15.4 s, 6 -> 14.0 s, 8 -> '
                         '14.9 s, 12 -> 21.0 s on one GB300)')
     p.add_argument('--sweep-board', default='planes16', help='the sweep\'s board (default: the 16-port plane pair)')
+    p.add_argument('--inner-tol', type=float, default=1e-4,
+                   help="the mixed solve's inner GMRES tolerance (relative to each outer step's residual)")
     p.add_argument('--product', default='tc3', choices=['tc3', 'tc6', 'fp32'],
                    help='the mixed solve\'s inner dense products over 16 or more columns')
     p.add_argument('--case', default=None,
@@ -695,7 +697,7 @@ def main():
     from pcbqs_gb300.peec import PeecModel
     board = Board.load(args.board)
     freq = replica_frequency(args.freq, rank)
-    model = PeecModel(board, device=local)
+    model = PeecModel(board, device=local, inner_tol=args.inner_tol)
 
     mixed = args.mode == 'mixed'
 
@@ -756,7 +758,7 @@ def main():
     for _ in range(3):
         torch.cuda.synchronize()
         t_e2e = time.perf_counter()
-        m2 = PeecModel(Board.load(args.board), device=local)
+        m2 = PeecModel(Board.load(args.board), device=local, inner_tol=args.inner_tol)
         m2.assemble(mixed=mixed)
         r2 = m2.solve([freq], precondition=args.precondition, mixed=mixed, factor_math=args.factor_math)
         torch.cuda.synchronize()
@@ -838,7 +840,7 @@ def main():
         if args.sweep_board != args.board:
             del model
             torch.cuda.empty_cache()
-            model = PeecModel(Board.load(args.sweep_board), device=local)
+            model = PeecModel(Board.load(args.sweep_board), device=local, inner_tol=args.inner_tol)
         model.assemble(mixed=mixed)
         sweep_tune = autotune_lu_panel(lib, model.n, args)
         torch.cuda.synchronize()

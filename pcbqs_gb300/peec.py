@@ -288,6 +288,10 @@ class PeecModel(PeecTopology):
             raise ValueError('conductor_loss must be dc or slab; conductor_faces must be 1 or 2')
         if matrix not in ('dense', 'hierarchical'):
             raise ValueError("matrix must be 'dense' or 'hierarchical'")
+        if not 1e-5 <= inner_tol < 1:
+            # the inner products are BF16 parts or FP32: a tighter inner tolerance is out of their reach, and every
+            # inner solve would then run to maxiter
+            raise ValueError('inner_tol must lie in [1e-5, 1)')
         if matrix == 'hierarchical' and stack is not None:
             raise ValueError('the compressed operator takes a homogeneous dielectric')
         self.matrix = matrix
