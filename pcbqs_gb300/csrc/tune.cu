@@ -22,15 +22,23 @@ std::map<std::string, int> g_entries;
 std::string g_path;
 bool g_env_read = false;
 
+// "<name>/<SM count>/" of the current device, looked up once per device (a lookup runs on every tuned call)
 std::string device_prefix() {
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex prefix_mutex;
+    static std::string prefixes[MAX_DEVICES];
     int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return "unknown/0/";
+    std::lock_guard<std::mutex> lock(prefix_mutex);
+    if (device >= 0 && device < MAX_DEVICES && !prefixes[device].empty()) return prefixes[device];
     cudaDeviceProp prop;
-    if (cudaGetDevice(&device) != cudaSuccess || cudaGetDeviceProperties(&prop, device) != cudaSuccess)
-        return "unknown/0/";
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return "unknown/0/";
     std::string name = prop.name;
     for (char &c : name)
         if (c == '\t' || c == '\n' || c == '/') c = ' ';
-    return name + "/" + std::to_string(prop.multiProcessorCount) + "/";
+    name += "/" + std::to_string(prop.multiProcessorCount) + "/";
+    if (device >= 0 && device < MAX_DEVICES) prefixes[device] = name;
+    return name;
 }
 
 // Merges the file's entries (lines "key<TAB>value"); a missing file is an empty one. Caller holds g_mutex.
