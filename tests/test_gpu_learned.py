@@ -51,26 +51,39 @@ def test_training_lowers_the_preconditioned_residual(device_library):
     assert history[-1] < 0.9 * history[0]
 
 
-def test_trained_network_beats_block_jacobi_on_held_out_boards(device_library):
-    """On boards outside the training set (the strip pair joined by vias, the tiny plane pair), at frequencies of
-    the training range, the trained gains lower the preconditioned residual of fresh probes and the GMRES steps to
-    1e-8 (every column still converges: the learned preconditioner is only an accelerator)."""
+def _held_out_steps(name, params):
+    import torch
     from pcbqs_gb300 import learned as L
     from pcbqs_gb300.board import Board
     from pcbqs_gb300.peec import PeecModel
-    params = L.load()
+    model = PeecModel(Board.load(name)).assemble()
     total_bj = total_l = 0
-    for name in ('viapair', 'tiny'):
-        model = PeecModel(Board.load(name)).assemble()
-        for f in (3e5, 3e6):
-            s = L.block_system_of(model, f)
-            Z = L.probes(s, 8, 11)
-            import torch
-            base = L.loss_and_gradient(s, torch.zeros_like(params), Z)[0]
-            learned = L.loss_and_gradient(s, params, Z)[0]
-            assert learned < base, (name, f, learned, base)
-            its_bj, its_l, res = L.compare(s, params)
-            assert (res <= 1e-8).all()
-            total_bj += int(its_bj.sum())
-            total_l += int(its_l.sum())
-    assert total_l < total_bj, (total_l, total_bj)
+    for f in (3e5, 3e6):
+        s = L.block_system_of(model, f)
+        Z = L.probes(s, 8, 11)
+        base = L.loss_and_gradient(s, torch.zeros_like(params), Z)[0]
+        learned = L.loss_and_gradient(s, params, Z)[0]
+        assert learned < base, (name, f, learned, base)
+        its_bj, its_l, res = L.compare(s, params)
+        assert (res <= 1e-8).all()
+        total_bj += int(its_bj.sum())
+        total_l += int(its_l.sum())
+    return total_bj, total_l
+
+
+@pytest.mark.parametrize('name', ['viapair', 'tiny'])
+def test_trained_network_beats_block_jacobi_on_held_out_boards(device_library, name):
+    """On each board outside the training set (the strip pair joined by vias, the tiny plane pair), at frequencies
+    of the training range, the trained gains lower the preconditioned residual of fresh probes and the GMRES steps
+    to 1e-8 (every column still converges: the learned preconditioner is only an accelerator)."""
+    from pcbqs_gb300 import learned as L
+    total_bj, total_l = _held_out_steps(name, L.load())
+    assert total_l < total_bj, (name, total_l, total_bj)
+
+
+@pytest.mark.xfail(strict=True, reason='the one-layer strip, a geometry outside the training set, converges more '
+                                       'slowly with the learned gains than with block-Jacobi alone')
+def test_trained_network_on_the_one_layer_strip(device_library):
+    from pcbqs_gb300 import learned as L
+    total_bj, total_l = _held_out_steps('strip', L.load())
+    assert total_l < total_bj, ('strip', total_l, total_bj)
