@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(256) k_slice_rows(int64_t rows, int64_t kdim, 
 }
 
 // Column bound exponents of X (kdim x ncols real, row-major, leading dimension ldxr) into col_exp (preset to a value
-// below -1022): 32 columns (one per lane) by a stretch of 256 rows per block.
+// below -1022): 32 columns (one per lane) by stretches of 256 rows, gridDim.x stretches apart.
 __global__ void __launch_bounds__(256) k_column_exponents(int64_t kdim, int64_t ncols, const double *X, int64_t ldxr,
                                                           int *col_exp) {
     __shared__ int part[8][32];
@@ -301,8 +301,8 @@ __global__ void __launch_bounds__(256) k_column_exponents(int64_t kdim, int64_t 
     const int64_t j = (int64_t)blockIdx.y * 32 + lane;
     int e = -1022;
     if (j < ncols)
-        for (int64_t t = (int64_t)blockIdx.x * 256 + w; t < kdim && t < (int64_t)(blockIdx.x + 1) * 256; t += 8)
-            e = max(e, bound_exponent(X[t * ldxr + j]));
+        for (int64_t t0 = (int64_t)blockIdx.x * 256; t0 < kdim; t0 += (int64_t)gridDim.x * 256)
+            for (int64_t t = t0 + w; t < kdim && t < t0 + 256; t += 8) e = max(e, bound_exponent(X[t * ldxr + j]));
     part[w][lane] = e;
     __syncthreads();
     if (w == 0 && j < ncols) {
@@ -1034,8 +1034,7 @@ cudaError_t tc_exact_product(int64_t rows, int64_t kdim, const void *plane, int6
     if ((e = cudaMemsetAsync(col_exp, 0x80, (size_t)ncols * sizeof(int), stream))) return e;   // below -1022
     {
         const dim3 grid((unsigned)std::min<int64_t>((kdim + 255) / 256, 65535), (unsigned)((ncols + 31) / 32));
-        k_column_exponents<<<grid, 256, 0, stream>>>(std::min<int64_t>(kdim, (int64_t)grid.x * 256), ncols, Xr,
-                                                     2 * ldx, col_exp);
+        k_column_exponents<<<grid, 256, 0, stream>>>(kdim, ncols, Xr, 2 * ldx, col_exp);
         const dim3 g2((unsigned)(kp / 32), (unsigned)((ncols + 31) / 32));
         k_slice_cols<<<g2, 256, 0, stream>>>(kdim, kp, ncols, slices, Xr, 2 * ldx, col_exp, bplane);
         note_launches(2);
