@@ -808,6 +808,26 @@ __global__ void k_rows_combine(Csr St, const double *M, int64_t ldm, int64_t nco
     }
 }
 
+// The same with two columns per thread as one 16-byte load and store (ncols, ldm and ldo even, M and out 16-byte
+// aligned): half the memory instructions for the FP64 pipe's and the memory system's queues.
+__global__ void k_rows_combine2(Csr St, const double *M, int64_t ldm, int64_t ncols, double *out, int64_t ldo) {
+    const int64_t half = ncols / 2;
+    for (int64_t j = blockIdx.y; j < St.rows; j += gridDim.y) {
+        const int64_t a0 = St.ptr[j], a1 = St.ptr[j + 1];
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < half;
+             c += (int64_t)gridDim.x * blockDim.x) {
+            double2 acc = make_double2(0.0, 0.0);
+            for (int64_t a = a0; a < a1; ++a) {
+                const double v = St.val[a];
+                const double2 m = reinterpret_cast<const double2 *>(M + (int64_t)St.idx[a] * ldm)[c];
+                acc.x += v * m.x;
+                acc.y += v * m.y;
+            }
+            reinterpret_cast<double2 *>(out + j * ldo)[c] = acc;
+        }
+    }
+}
+
 // Grid of (x, rows) blocks with the row count within the launch limit; the kernels stride over the rows.
 static dim3 row_grid(unsigned x, int64_t rows) {
     return dim3(x, (unsigned)std::min<int64_t>(std::max<int64_t>(rows, 1), 65535));
@@ -1455,11 +1475,18 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
         }
         const unsigned chunks = 8;
         const dim3 g1 = row_grid(chunks, n);
+        auto aligned = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+        auto combine = [&](const Csr &St, const double *M, int64_t ldm, int64_t cols, double *out, int64_t ldo) {
+            if (cols % 2 == 0 && ldm % 2 == 0 && ldo % 2 == 0 && aligned(M) && aligned(out))
+                k_rows_combine2<<<g1, 256, 0, st>>>(St, M, ldm, cols, out, ldo);
+            else
+                k_rows_combine<<<g1, 256, 0, st>>>(St, M, ldm, cols, out, ldo);
+        };
         auto triple = [&](const Csr &St, const double *M, int64_t ldm, int64_t m, double *out) {
-            k_rows_combine<<<g1, 256, 0, st>>>(St, M, ldm, m, w, m);
+            combine(St, M, ldm, m, w, m);
             dim3 gt((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
             k_transpose<<<gt, dim3(32, 8), 0, st>>>(w, n, m, m, wt, n);
-            k_rows_combine<<<g1, 256, 0, st>>>(St, wt, n, n, out, n);
+            combine(St, wt, n, n, out, n);
         };
         triple(op.Kt, op.L, op.ldl, op.ne, h->klk);
         if (op.nn > 0) {
