@@ -136,3 +136,20 @@ def test_cluster_tree_partition_covers_each_entry_once(board):
         level = deeper
     assert far > 0
     np.testing.assert_array_equal(count, 1)
+
+
+def test_peec_model_rejects_bad_options_before_touching_the_device():
+    """Option checks of PeecModel run before any device work (no GPU needed): the inner tolerance must lie within
+    the inner products' reach, and the compressed operator takes a homogeneous dielectric."""
+    import pytest
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel
+    b = Board.load('tiny')
+    with pytest.raises(ValueError, match='inner_tol'):
+        PeecModel(b, inner_tol=1e-7)
+    with pytest.raises(ValueError, match='inner_tol'):
+        PeecModel(b, inner_tol=1.0)
+    with pytest.raises(ValueError, match="'dense' or 'hierarchical'"):
+        PeecModel(b, matrix='sparse')
+    with pytest.raises(ValueError, match='homogeneous'):
+        PeecModel(b, matrix='hierarchical', stack=object())
