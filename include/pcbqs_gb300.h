@@ -258,6 +258,42 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *op, int32_t bs, const double
  * (pcbqs_gb300_lu_factor_c64, 2048-column panels) with BF16x9 / FP32 GEMMs. Mirrors MixedLU (src/pcbqs/kernels.py:125-181): a complex64 factor
  * with the FP64 operator's GMRES on top in place of its refinement loop. */
 int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream);
+/* The graph preconditioner's structure and its values at one frequency (pcbqs_gb300_peec_graph); every pointer a
+ * device array, complex values interleaved (re, im). Unknowns in the operator's order; "kept" nodes are all but each
+ * component's root, whose equation T[keep] drops. */
+typedef struct pcbqs_gb300_graph {
+    int64_t nkeep;                 /* kept nodes */
+    int64_t ncomp;                 /* components of the passive branches' graph */
+    int64_t nbranch;               /* passive branches (the length of zdiag, dinv) */
+    pcbqs_gb300_csr ac;            /* nkeep x n: each loop's defining branch's incidence, +1 first end, -1 second */
+    const int64_t *lap_ptr;        /* nkeep + 1: each kept node's passive branches (self-loops left out) */
+    const int32_t *lap_branch;     /*   the branch */
+    const int32_t *lap_other;      /*   its other end's kept row, -1 at a root */
+    pcbqs_gb300_csr tinv;          /* n x nkeep: T[keep]^-1 (the spanning forest's path sums), rows of tree unknowns */
+    pcbqs_gb300_csr tinvt;         /* nkeep x n: its transpose */
+    const int32_t *branch;         /* n: each unknown's branch (a loop's defining branch, a tree unknown's own) */
+    const int32_t *loop_ends;      /* n x 2: a loop's defining branch's ends as kept rows (-1 at a root) */
+    const int32_t *comp;           /* nkeep: each kept node's component */
+    const int64_t *member_ptr;     /* ncomp + 1 */
+    const int32_t *members;        /* the kept rows of each component */
+    const double *zdiag;           /* nbranch complex: each branch's own impedance r R_ii + j w L_ii */
+    const double *dinv;            /* nbranch complex: 1 / zdiag, |zdiag| raised to 1e-12 zscale where smaller */
+    const double *pinv;            /* nkeep complex: 1 / P_ii at the kept nodes */
+    const double *total;           /* ncomp complex: the sum of 1 / P_ii over each component's nodes */
+} pcbqs_gb300_graph;
+/* The reference's graph preconditioner (_graph_preconditioner and the charge-tree solve of _tree_preconditioner,
+ * src/pcbqs/peec_iterative.py:19-84, without face-sheet pairs) at system index sys, for precondition 3 of
+ * pcbqs_gb300_peec_gmres and pcbqs_gb300_peec_solve_mixed: the loop currents from the graph Laplacian
+ * Ap diag(dinv) Ap^T [keep][:, keep] (assembled dense on the device and LU-factored in complex64 with this library's
+ * tcgen05 updates, in place of the reference's sparse incomplete LU; refine = 1 adds one FP64 residual correction
+ * of each Laplacian solve), the tree unknowns' charges through the explicit T[keep]^-1 and the components'
+ * equilibrium. Works with the dense and the compressed operator; the structure's arrays must outlive the handle
+ * (the frequency's values are copied). Status 4 when the dense Laplacian does not fit in device memory, 3 when its
+ * factor meets a zero pivot. */
+int pcbqs_gb300_peec_graph(pcbqs_gb300_peec *op, const pcbqs_gb300_graph *g, int32_t sys, int refine, void *stream);
+/* out = M in for k columns (device, (n, k) complex128 row-major) with the graph preconditioner set up last
+ * (validation of the preconditioner alone); synchronizes `stream`. */
+int pcbqs_gb300_peec_graph_apply(pcbqs_gb300_peec *op, int k, const double *in, double *out, void *stream);
 /* CUDA-event times (ms, on the factorization's stream) of the last pcbqs_gb300_peec_factor: the dense system's
  * assembly (with K^T L K and T^T P T when first formed) and the LU itself. No counterpart in the reference (its
  * factor is LAPACK on the host); for the roofline of the factorization. */
@@ -408,7 +444,8 @@ int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *op, int k, const double *in, dou
                               void *stream);
 /* Batched right-preconditioned restarted GMRES on k columns (b, x device; x holds the initial guess), relative
  * residual tol per column; iterations and residual (host, k) receive each column's Arnoldi steps and true
- * relative residual; precondition 0 none, 1 block-Jacobi, 2 the single-precision factor (every column uses it).
+ * relative residual; precondition 0 none, 1 block-Jacobi, 2 the single-precision factor, 3 the graph
+ * preconditioner (every column uses the factor or the graph preconditioner set up last).
  * Status 5 when a column did not converge. Replaces peec_iterative._gmres
  * (src/pcbqs/peec_iterative.py:100-112) and mqs_iterative._lockstep_gmres (src/pcbqs/mqs_iterative.py:109-170). */
 int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *op, int k, const int32_t *sys, const double *b, double *x, double tol,

@@ -1,13 +1,16 @@
 """Pure-Python restatement of the PEEC spanning forest and loop basis, kept as the checker for the native
-pcbqs_gb300_loop_basis (test infrastructure only: nothing in the package imports this module).
+pcbqs_gb300_loop_basis, and of the graph preconditioner, the checker for pcbqs_gb300_peec_graph (test
+infrastructure only: nothing in the package imports this module).
 
 Follows src/pcbqs/mqs.py:48-130 (spanning_tree: breadth-first forest from each island's most central node, other
-branches only joining islands) and src/pcbqs/mqs.py:592-637 (_loops: each non-tree branch's fundamental cycle).
+branches only joining islands), src/pcbqs/mqs.py:592-637 (_loops: each non-tree branch's fundamental cycle) and
+src/pcbqs/peec_iterative.py:19-84 (_tree_preconditioner, _graph_preconditioner; boards without face-sheet pairs).
 """
 import collections
 
 import numpy as np
-from scipy.sparse import coo_matrix
+from scipy.sparse import coo_matrix, diags
+from scipy.sparse.linalg import splu
 
 
 def spanning_tree(n_nodes, ends, is_src, first=None):
@@ -137,3 +140,43 @@ def loop_basis(n_nodes, ends, is_src, n_rwg, ideal_terminals=True):
         col += 1
     C = coo_matrix((vals, (rows, cols)), shape=(nb, col)).tocsc()
     return C, src_cols, tree, np.asarray(col_branch, np.int64)
+
+
+def graph_preconditioner(K, A, T, B, nl, keep, passive, cotree, diagonal, zscale, pscale, pdiag):
+    """apply(y) of the reference's graph preconditioner in its own unknown order (the nl loops, then the tree
+    branches), with exact sparse LU factors (SuperLU) where the reference takes an incomplete LU of the Laplacian
+    with drop tolerance 1e-6: K (branches x unknowns) the loop/tree basis, A (nodes x branches) the incidence,
+    T = A K[:, nl:], B (nodes x components) the component indicator, keep the non-root nodes, passive the passive
+    branches, cotree each loop's defining branch, diagonal (branches) each branch's own impedance, zscale / pscale
+    the system's scales, pdiag P's diagonal. peec_iterative.py:44-84 (the loop part) over :19-42 (the charge tree)."""
+    Kc, Kt = K[:, :nl], K[:, nl:]
+    position = np.full(A.shape[1], -1)
+    position[passive] = np.arange(len(passive))
+    d = np.asarray(diagonal)[passive].astype(complex)
+    d[np.abs(d) < zscale * 1e-12] = zscale * 1e-12
+    Ap = A[:, passive]
+    Dinv = diags(1 / d).tocsr()
+    Zb = diags(np.asarray(diagonal, complex)).tocsc()
+    laplacian = splu((Ap @ Dinv @ Ap.T).tocsc()[keep][:, keep].tocsc())
+    tree_lu = splu(T[keep].astype(complex).tocsc())
+    inverse = 1 / np.asarray(pdiag, complex)
+    total = np.asarray(B.T @ inverse).ravel()
+
+    def apply(y):
+        force = np.zeros(A.shape[1], complex)
+        force[cotree] = zscale * y[:nl]
+        trial = Dinv @ force[passive]
+        voltage = np.zeros(A.shape[0], complex)
+        voltage[keep] = laplacian.solve(np.asarray(Ap @ trial).ravel()[keep])
+        loop = (trial - Dinv @ (Ap.T @ voltage))[position[cotree]]
+        rhs = np.array(y, complex)
+        rhs[nl:] -= np.asarray(Kt.T @ (Zb @ (Kc @ loop))).ravel() / zscale
+        v = np.zeros(T.shape[0], complex)
+        v[keep] = tree_lu.solve(rhs[nl:], trans='T')
+        common = np.asarray(B.T @ (inverse * v)).ravel() / total
+        charge = inverse * (v - B @ common)
+        out = np.empty(K.shape[1], complex)
+        out[nl:] = pscale * tree_lu.solve(charge[keep])
+        out[:nl] = loop
+        return out
+    return apply

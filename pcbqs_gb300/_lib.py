@@ -46,6 +46,15 @@ class HmatDesc(ctypes.Structure):
                 ('store', c_void_p), ('max_rank', ctypes.c_int32)]
 
 
+class GraphDesc(ctypes.Structure):
+    """pcbqs_gb300_graph: the graph preconditioner's device arrays and one frequency's values."""
+    _fields_ = [('nkeep', ctypes.c_int64), ('ncomp', ctypes.c_int64), ('nbranch', ctypes.c_int64), ('ac', CsrDesc),
+                ('lap_ptr', c_void_p), ('lap_branch', c_void_p), ('lap_other', c_void_p), ('tinv', CsrDesc),
+                ('tinvt', CsrDesc), ('branch', c_void_p), ('loop_ends', c_void_p), ('comp', c_void_p),
+                ('member_ptr', c_void_p), ('members', c_void_p), ('zdiag', c_void_p), ('dinv', c_void_p),
+                ('pinv', c_void_p), ('total', c_void_p)]
+
+
 class LowRankDesc(ctypes.Structure):
     """pcbqs_gb300_lowrank: an H-matrix's low-rank blocks packed for the tensor cores."""
     _fields_ = [('meta_dense', c_void_p), ('slot0_dense', c_void_p), ('ndense', ctypes.c_int64), ('lplane', c_void_p),
@@ -131,6 +140,9 @@ PROTOTYPES = {
     'pcbqs_gb300_peec_destroy': (None, [c_void_p]),
     'pcbqs_gb300_peec_apply': (ctypes.c_int, [c_void_p, ctypes.c_int, c_int32_p, c_void_p, c_void_p, c_void_p]),
     'pcbqs_gb300_peec_block_jacobi': (ctypes.c_int, [c_void_p, ctypes.c_int32, c_void_p, c_void_p]),
+    'pcbqs_gb300_peec_graph': (ctypes.c_int, [c_void_p, ctypes.POINTER(GraphDesc), ctypes.c_int32, ctypes.c_int,
+                                              c_void_p]),
+    'pcbqs_gb300_peec_graph_apply': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p]),
     'pcbqs_gb300_peec_factor': (ctypes.c_int, [c_void_p, ctypes.POINTER(CsrDesc), ctypes.c_int32, ctypes.c_int,
                                                c_void_p]),
     'pcbqs_gb300_peec_lu_solve': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p, c_void_p, ctypes.c_int,

@@ -1118,6 +1118,267 @@ struct PotentialView : Operator {
     }
 };
 
+// ---- graph preconditioner (src/pcbqs/peec_iterative.py:19-84, without face-sheet pairs) ----
+//
+// For y (n x k, the operator's order), with d the passive branches' own impedance (zdiag), Dinv = 1/d, zs the
+// system's zscale, ps the potential scale, and kept nodes all but each component's root:
+//   trial_j = zs dinv_b(j) y_j on each loop j (b(j) its defining branch), v = G^-1 (Ap trial)[keep],
+//   G = Ap Dinv Ap^T [keep][:, keep] (dense complex64 LU, optionally one FP64 residual correction);
+//   out_j = trial_j - dinv_b(j) (v_a - v_b) on each loop (a, b the ends of b(j), v = 0 at a root);
+//   rt_j = y_j - d_b(j) / zs (K_loops out)_b(j) on each tree unknown;
+//   v2 = T[keep]^-T rt, m_c = sum_{i in c} pinv_i v2_i / total_c, charge_i = pinv_i (v2_i - m_c(i));
+//   out_j = ps (T[keep]^-1 charge)_j on each tree unknown.
+// Every kernel below takes (rows x k) row-major complex128 arrays, one thread per (row, column).
+
+static __device__ __forceinline__ cd zmul(cd a, cd b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// G (nkeep x nkeep, row-major = column-major: G is symmetric) from the branches at each kept node: the diagonal the
+// sum of their 1/d, -1/d at the other end's column (none at a root). One thread per row; G zeroed beforehand.
+__global__ void k_graph_laplacian(int64_t nkeep, const int64_t *lap_ptr, const int32_t *lap_branch,
+                                  const int32_t *lap_other, const cd *dinv, float2 *G) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nkeep; i += (int64_t)gridDim.x * blockDim.x) {
+        double re = 0, im = 0;
+        float2 *row = G + i * nkeep;
+        for (int64_t a = lap_ptr[i]; a < lap_ptr[i + 1]; ++a) {
+            const cd w = dinv[lap_branch[a]];
+            re += w.x;
+            im += w.y;
+            const int32_t o = lap_other[a];
+            if (o >= 0) {
+                row[o].x -= (float)w.x;
+                row[o].y -= (float)w.y;
+            }
+        }
+        row[i].x += (float)re;
+        row[i].y += (float)im;
+    }
+}
+
+// rhs[i, c] = sum over the loops j incident to kept node i of ac_ij zs dinv_b(j) y[j, c]   (Ap trial)
+__global__ void k_graph_node_rhs(Csr ac, int k, const int32_t *branch, const cd *dinv, double zs, const cd *y,
+                                 cd *rhs) {
+    const int64_t total = ac.rows * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / k;
+        const int c = (int)(t % k);
+        cd acc = make_double2(0, 0);
+        for (int64_t a = ac.ptr[i]; a < ac.ptr[i + 1]; ++a) {
+            const int32_t j = ac.idx[a];
+            const cd w = dinv[branch[j]];
+            const double f = zs * ac.val[a];
+            const cd p = zmul(make_double2(f * w.x, f * w.y), y[(int64_t)j * k + c]);
+            acc.x += p.x;
+            acc.y += p.y;
+        }
+        rhs[t] = acc;
+    }
+}
+
+// r = rhs - G v with G from the branches in FP64 (the Laplacian solve's residual correction).
+__global__ void k_graph_residual(int64_t nkeep, int k, const int64_t *lap_ptr, const int32_t *lap_branch,
+                                 const int32_t *lap_other, const cd *dinv, const cd *v, const cd *rhs, cd *r) {
+    const int64_t total = nkeep * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / k;
+        const int c = (int)(t % k);
+        const cd vi = v[t];
+        cd acc = rhs[t];
+        for (int64_t a = lap_ptr[i]; a < lap_ptr[i + 1]; ++a) {
+            const int32_t o = lap_other[a];
+            const cd vo = o >= 0 ? v[(int64_t)o * k + c] : make_double2(0, 0);
+            const cd p = zmul(dinv[lap_branch[a]], make_double2(vi.x - vo.x, vi.y - vo.y));
+            acc.x -= p.x;
+            acc.y -= p.y;
+        }
+        r[t] = acc;
+    }
+}
+
+__global__ void k_graph_add(int64_t count, const cd *x, cd *y) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+        y[t].x += x[t].x;
+        y[t].y += x[t].y;
+    }
+}
+
+// The loop unknowns' outputs: trial_j - dinv_b(j) (v_a - v_b).
+__global__ void k_graph_loops(int64_t n, int k, const int8_t *is_tree, const int32_t *branch, const int32_t *ends,
+                              const cd *dinv, double zs, const cd *y, const cd *v, cd *out) {
+    const int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = t / k;
+        if (is_tree[j]) continue;
+        const int c = (int)(t % k);
+        const cd w = dinv[branch[j]];
+        const int32_t a = ends[2 * j], b = ends[2 * j + 1];
+        const cd va = a >= 0 ? v[(int64_t)a * k + c] : make_double2(0, 0);
+        const cd vb = b >= 0 ? v[(int64_t)b * k + c] : make_double2(0, 0);
+        const cd trial = zmul(make_double2(zs * w.x, zs * w.y), y[t]);
+        const cd drop = zmul(w, make_double2(va.x - vb.x, va.y - vb.y));
+        out[t] = make_double2(trial.x - drop.x, trial.y - drop.y);
+    }
+}
+
+// The tree unknowns' right-hand side: rt_j = y_j - d_b / zs sum over the loop columns of K's row b of K_bl out_l,
+// b = branch[j] (K: passive branches x unknowns). Loop rows of rt are set to zero.
+__global__ void k_graph_tree_rhs(int64_t n, int k, const int8_t *is_tree, const int32_t *branch, Csr K,
+                                 const cd *zdiag, double inv_zs, const cd *y, const cd *out, cd *rt) {
+    const int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = t / k;
+        if (!is_tree[j]) {
+            rt[t] = make_double2(0, 0);
+            continue;
+        }
+        const int c = (int)(t % k);
+        const int32_t b = branch[j];
+        cd acc = make_double2(0, 0);
+        for (int64_t a = K.ptr[b]; a < K.ptr[b + 1]; ++a) {
+            const int32_t l = K.idx[a];
+            if (is_tree[l]) continue;
+            const cd x = out[(int64_t)l * k + c];
+            acc.x += K.val[a] * x.x;
+            acc.y += K.val[a] * x.y;
+        }
+        const cd z = zdiag[b];
+        const cd p = zmul(make_double2(z.x * inv_zs, z.y * inv_zs), acc);
+        rt[t] = make_double2(y[t].x - p.x, y[t].y - p.y);
+    }
+}
+
+// m[c, col] = rtotal_c sum over component c's kept rows i of pinv_i v2[i, col]. Block (32 columns, 16 row
+// strides) per (component, 32-column chunk); a fixed summation order.
+__global__ void __launch_bounds__(512) k_graph_common(int k, const int64_t *member_ptr, const int32_t *members,
+                                                      const cd *pinv, const cd *rtotal, const cd *v2, cd *m) {
+    __shared__ cd part[16][32];
+    const int comp = blockIdx.x;
+    const int c = blockIdx.y * 32 + threadIdx.x;
+    cd acc = make_double2(0, 0);
+    if (c < k)
+        for (int64_t a = member_ptr[comp] + threadIdx.y; a < member_ptr[comp + 1]; a += 16) {
+            const int32_t i = members[a];
+            const cd p = zmul(pinv[i], v2[(int64_t)i * k + c]);
+            acc.x += p.x;
+            acc.y += p.y;
+        }
+    part[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0 && c < k) {
+        cd s = part[0][threadIdx.x];
+        for (int r = 1; r < 16; ++r) {
+            s.x += part[r][threadIdx.x].x;
+            s.y += part[r][threadIdx.x].y;
+        }
+        m[(int64_t)comp * k + c] = zmul(s, rtotal[comp]);
+    }
+}
+
+// charge (in place of v2) = pinv_i (v2_i - m_comp(i)).
+__global__ void k_graph_charge(int64_t nkeep, int k, const int32_t *comp, const cd *pinv, const cd *m, cd *v2) {
+    const int64_t total = nkeep * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / k;
+        const int c = (int)(t % k);
+        const cd mm = m[(int64_t)comp[i] * k + c];
+        v2[t] = zmul(pinv[i], make_double2(v2[t].x - mm.x, v2[t].y - mm.y));
+    }
+}
+
+// The tree unknowns' outputs: ps (T[keep]^-1 charge)_j; loop rows untouched.
+__global__ void k_graph_tree_out(int64_t n, int k, const int8_t *is_tree, Csr tinv, double ps, const cd *charge,
+                                 cd *out) {
+    const int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = t / k;
+        if (!is_tree[j]) continue;
+        const int c = (int)(t % k);
+        double re = 0, im = 0;
+        for (int64_t a = tinv.ptr[j]; a < tinv.ptr[j + 1]; ++a) {
+            const cd x = charge[(int64_t)tinv.idx[a] * k + c];
+            re += tinv.val[a] * x.x;
+            im += tinv.val[a] * x.y;
+        }
+        out[t] = make_double2(ps * re, ps * im);
+    }
+}
+
+struct GraphPrecond : Preconditioner {
+    int64_t n = 0, nkeep = 0, ncomp = 0, nbranch = 0;
+    Csr ac, tinv, tinvt, K;
+    const int64_t *lap_ptr = nullptr, *member_ptr = nullptr;
+    const int32_t *lap_branch = nullptr, *lap_other = nullptr, *branch = nullptr, *loop_ends = nullptr,
+                  *comp = nullptr, *members = nullptr;
+    const int8_t *is_tree = nullptr;
+    cd *zdiag = nullptr, *dinv = nullptr, *pinv = nullptr, *rtotal = nullptr;   // owned (rtotal = 1 / total)
+    double zs = 1, ps = 1;
+    bool refine = false;
+    float2 *G = nullptr;     // the Laplacian's complex64 LU
+    int *ipiv = nullptr;
+    TriSolver tri;
+    int cap = 0, deferred_k = 0;
+    cd *rhs = nullptr, *v = nullptr, *corr = nullptr, *rt = nullptr, *v2 = nullptr, *m = nullptr;
+
+    void free_work() {
+        for (cd *p : {rhs, v, corr, rt, v2, m}) dev_free(p);
+        rhs = v = corr = rt = v2 = m = nullptr;
+        cap = 0;
+    }
+    ~GraphPrecond() override {
+        tri.release();
+        free_work();
+        for (void *p : {(void *)zdiag, (void *)dinv, (void *)pinv, (void *)rtotal, (void *)G, (void *)ipiv})
+            dev_free(p);
+    }
+    cudaError_t reserve(int k, cudaStream_t s) {
+        if (k <= cap) return cudaSuccess;
+        free_work();
+        cudaError_t e;
+        if ((e = dev_alloc(&rhs, (size_t)nkeep * k, s)) || (e = dev_alloc(&v, (size_t)nkeep * k, s)) ||
+            (e = dev_alloc(&corr, (size_t)nkeep * k, s)) || (e = dev_alloc(&rt, (size_t)n * k, s)) ||
+            (e = dev_alloc(&v2, (size_t)nkeep * k, s)) || (e = dev_alloc(&m, (size_t)ncomp * k, s))) {
+            free_work();
+            return e;
+        }
+        cap = k;
+        return cudaSuccess;
+    }
+    cudaError_t run(int k, const cd *in, cd *out, cudaStream_t s, bool deferred) {
+        cudaError_t e;
+        k_graph_node_rhs<<<grid_of(nkeep * k), 256, 0, s>>>(ac, k, branch, dinv, zs, in, rhs);
+        if ((e = tri.solve(k, rhs, v, s, deferred))) return e;
+        if (refine) {
+            k_graph_residual<<<grid_of(nkeep * k), 256, 0, s>>>(nkeep, k, lap_ptr, lap_branch, lap_other, dinv, v,
+                                                                rhs, corr);
+            if ((e = tri.solve(k, corr, rhs, s, deferred))) return e;
+            k_graph_add<<<grid_of(nkeep * k), 256, 0, s>>>(nkeep * k, rhs, v);
+            note_launches(2);
+        }
+        k_graph_loops<<<grid_of(n * k), 256, 0, s>>>(n, k, is_tree, branch, loop_ends, dinv, zs, in, v, out);
+        k_graph_tree_rhs<<<grid_of(n * k), 256, 0, s>>>(n, k, is_tree, branch, K, zdiag, 1.0 / zs, in, out, rt);
+        k_spmm<<<grid_of(nkeep * k), 256, 0, s>>>(tinvt, k, rt, v2, nullptr, nullptr, 0);
+        k_graph_common<<<dim3((unsigned)ncomp, (unsigned)((k + 31) / 32)), dim3(32, 16), 0, s>>>(
+            k, member_ptr, members, pinv, rtotal, v2, m);
+        k_graph_charge<<<grid_of(nkeep * k), 256, 0, s>>>(nkeep, k, comp, pinv, m, v2);
+        k_graph_tree_out<<<grid_of(n * k), 256, 0, s>>>(n, k, is_tree, tinv, ps, v2, out);
+        note_launches(7);
+        return cudaGetLastError();
+    }
+    cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        cudaError_t e = reserve(k, s);
+        return e ? e : run(k, in, out, s, false);
+    }
+    cudaError_t apply_deferred(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
+        if (k > cap) return cudaErrorInvalidValue;      // one apply with this k comes first (no allocation here)
+        deferred_k = k;
+        return run(k, in, out, s, true);
+    }
+    cudaError_t deferred_status(cudaStream_t s) override {
+        return deferred_k ? tri.read_status(deferred_k, s) : cudaSuccess;
+    }
+};
+
 }  // namespace pq
 
 using namespace pq;
@@ -1126,6 +1387,7 @@ struct pcbqs_gb300_peec {
     PeecOp op;
     BlockJacobi *bj = nullptr;
     LuPrecond *lu = nullptr;
+    GraphPrecond *graph = nullptr;
     double *klk = nullptr, *tpt = nullptr;   // dense K^T L K and T^T P T (n x n), made once for the factors
     double *tpt_im = nullptr;                // T^T P_im T when P is complex
     float assemble_ms = 0, getrf_ms = 0;     // CUDA-event times of the last factorization's two stages
@@ -1134,6 +1396,7 @@ struct pcbqs_gb300_peec {
     ~pcbqs_gb300_peec() {
         delete bj;
         delete lu;
+        delete graph;
         dev_free(klk);
         dev_free(tpt);
         dev_free(tpt_im);
@@ -1581,6 +1844,96 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     return OK;
 }
 
+int pcbqs_gb300_peec_graph(pcbqs_gb300_peec *h, const pcbqs_gb300_graph *g, int32_t sys, int refine, void *stream) {
+    if (!h || !g || sys < 0 || sys >= h->op.nsys || (refine != 0 && refine != 1))
+        return pfail(ERR_ARGUMENT, "peec_graph: invalid argument");
+    PeecOp &op = h->op;
+    const int64_t n = op.n_, nk = g->nkeep;
+    if (nk < 1 || g->ncomp < 1 || g->ncomp > nk + 1 || g->ncomp > 65535 || g->nbranch != op.nb)
+        return pfail(ERR_ARGUMENT, "peec_graph: %lld kept nodes, %lld components, %lld branches (the operator has %lld)",
+                     (long long)nk, (long long)g->ncomp, (long long)g->nbranch, (long long)op.nb);
+    if (g->ac.rows != nk || g->ac.cols != n || g->tinv.rows != n || g->tinv.cols != nk || g->tinvt.rows != nk ||
+        g->tinvt.cols != n)
+        return pfail(ERR_ARGUMENT, "peec_graph: ac (kept x n), tinv (n x kept), tinvt (kept x n) shapes");
+    if (!g->ac.ptr || !g->tinv.ptr || !g->tinvt.ptr || !g->lap_ptr || !g->lap_branch || !g->lap_other ||
+        !g->branch || !g->loop_ends || !g->comp || !g->member_ptr || !g->members || !g->zdiag || !g->dinv ||
+        !g->pinv || !g->total)
+        return pfail(ERR_ARGUMENT, "peec_graph: null array");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto *gp = new (std::nothrow) GraphPrecond();
+    if (!gp) return pfail(ERR_MEMORY, "peec_graph: host allocation");
+    gp->n = n;
+    gp->nkeep = nk;
+    gp->ncomp = g->ncomp;
+    gp->nbranch = g->nbranch;
+    gp->ac = csr_of(g->ac);
+    gp->tinv = csr_of(g->tinv);
+    gp->tinvt = csr_of(g->tinvt);
+    gp->K = op.K;
+    gp->lap_ptr = g->lap_ptr;
+    gp->lap_branch = g->lap_branch;
+    gp->lap_other = g->lap_other;
+    gp->branch = g->branch;
+    gp->loop_ends = g->loop_ends;
+    gp->comp = g->comp;
+    gp->member_ptr = g->member_ptr;
+    gp->members = g->members;
+    gp->is_tree = op.is_tree;
+    gp->refine = refine != 0;
+    gp->ps = op.pscale;
+    cudaMemcpy(&gp->zs, op.zscale + sys, sizeof(double), cudaMemcpyDeviceToHost);
+    cudaError_t e;
+    const size_t nk2 = (size_t)nk * nk;
+    if ((e = dev_alloc(&gp->zdiag, g->nbranch, st)) || (e = dev_alloc(&gp->dinv, g->nbranch, st)) ||
+        (e = dev_alloc(&gp->pinv, nk, st)) || (e = dev_alloc(&gp->rtotal, g->ncomp, st)) ||
+        (e = dev_alloc(&gp->ipiv, nk, st))) {
+        delete gp;
+        return pfail(ERR_MEMORY, "peec_graph: %s", cudaGetErrorString(e));
+    }
+    if ((e = dev_alloc(&gp->G, nk2, st))) {
+        delete gp;
+        return pfail(ERR_MEMORY, "peec_graph: the dense Laplacian of %lld nodes (%.1f GB): %s", (long long)nk,
+                     8e-9 * (double)nk2, cudaGetErrorString(e));
+    }
+    cudaMemcpyAsync(gp->zdiag, g->zdiag, sizeof(cd) * g->nbranch, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(gp->dinv, g->dinv, sizeof(cd) * g->nbranch, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(gp->pinv, g->pinv, sizeof(cd) * nk, cudaMemcpyDeviceToDevice, st);
+    // 1 / total per component, on the host (a handful of values)
+    std::vector<cd> tot((size_t)g->ncomp);
+    cudaMemcpyAsync(tot.data(), g->total, sizeof(cd) * g->ncomp, cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st))) {
+        delete gp;
+        return pfail(cuda_status(e), "peec_graph: %s", cudaGetErrorString(e));
+    }
+    for (cd &t : tot) {
+        const double a = t.x * t.x + t.y * t.y;
+        if (!(a > 0) || !std::isfinite(a)) {
+            delete gp;
+            return pfail(ERR_NONFINITE, "peec_graph: a component's total 1 / P_ii is zero or not finite");
+        }
+        t = make_double2(t.x / a, -t.y / a);
+    }
+    cudaMemcpyAsync(gp->rtotal, tot.data(), sizeof(cd) * g->ncomp, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(gp->G, 0, sizeof(float2) * nk2, st);
+    k_graph_laplacian<<<grid_of(nk), 256, 0, st>>>(nk, g->lap_ptr, g->lap_branch, g->lap_other, gp->dinv, gp->G);
+    note_launches(1);
+    int singular = 0;
+    LuUpdateStats stats;
+    e = getrf_blocked(nk, gp->G, gp->ipiv, lu_panel_width(nk, LU_GEMM_TC6), LU_GEMM_TC6, st, &singular, &stats);
+    if (e || singular) {
+        delete gp;
+        return pfail(singular ? ERR_NONFINITE : cuda_status(e), "peec_graph: Laplacian LU failed (zero pivot %d, %s)",
+                     singular, cudaGetErrorString(e));
+    }
+    if ((e = gp->tri.prepare(gp->G, nk, gp->ipiv, st))) {
+        delete gp;
+        return pfail(cuda_status(e), "peec_graph: triangular-solve set-up: %s", cudaGetErrorString(e));
+    }
+    delete h->graph;
+    h->graph = gp;
+    return OK;
+}
+
 int pcbqs_gb300_peec_factor_times(const pcbqs_gb300_peec *h, double *assemble_ms, double *getrf_ms) {
     if (!h || !assemble_ms || !getrf_ms) return pfail(ERR_ARGUMENT, "peec_factor_times: invalid argument");
     if (!h->lu) return pfail(ERR_ARGUMENT, "peec_factor_times: no factor set up");
@@ -1642,6 +1995,16 @@ int pcbqs_gb300_peec_lu_solve(pcbqs_gb300_peec *h, int k, const double *in, doub
     return OK;
 }
 
+int pcbqs_gb300_peec_graph_apply(pcbqs_gb300_peec *h, int k, const double *in, double *out, void *stream) {
+    if (!h || k <= 0 || !in || !out) return pfail(ERR_ARGUMENT, "peec_graph_apply: invalid argument");
+    if (!h->graph) return pfail(ERR_ARGUMENT, "peec_graph_apply: no graph preconditioner set up");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = h->graph->apply(k, nullptr, reinterpret_cast<const cd *>(in), reinterpret_cast<cd *>(out), st);
+    if (!e) e = cudaStreamSynchronize(st);
+    if (e) return pfail(cuda_status(e), "peec_graph_apply: %s", cudaGetErrorString(e));
+    return OK;
+}
+
 int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, const double *b, double *x,
                            double tol, int maxiter, int restart, int precondition, int32_t *iterations,
                            double *residual, void *stream) {
@@ -1651,14 +2014,17 @@ int pcbqs_gb300_peec_gmres(pcbqs_gb300_peec *h, int k, const int32_t *sys_host, 
         if (sys_host[s] < 0 || sys_host[s] >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_gmres: system index");
     if (precondition == 1 && !h->bj) return pfail(ERR_ARGUMENT, "peec_gmres: no block-Jacobi preconditioner set up");
     if (precondition == 2 && !h->lu) return pfail(ERR_ARGUMENT, "peec_gmres: no factor set up");
-    if (precondition < 0 || precondition > 2) return pfail(ERR_ARGUMENT, "peec_gmres: preconditioner 0, 1 or 2");
+    if (precondition == 3 && !h->graph) return pfail(ERR_ARGUMENT, "peec_gmres: no graph preconditioner set up");
+    if (precondition < 0 || precondition > 3) return pfail(ERR_ARGUMENT, "peec_gmres: preconditioner 0 .. 3");
     GmresOptions opt;
     opt.tol = tol; opt.maxiter = maxiter; opt.restart = restart;
     opt.captured = h->captured;
     GmresReport rep;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    Preconditioner *M = precondition == 1 ? static_cast<Preconditioner *>(h->bj)
-                        : precondition == 2 ? static_cast<Preconditioner *>(h->lu) : nullptr;
+    Preconditioner *M = precondition == 1   ? static_cast<Preconditioner *>(h->bj)
+                        : precondition == 2 ? static_cast<Preconditioner *>(h->lu)
+                        : precondition == 3 ? static_cast<Preconditioner *>(h->graph)
+                                            : nullptr;
     cudaError_t e = gmres_batched(h->op, M, k, sys_host,
                                   reinterpret_cast<const cd *>(b), reinterpret_cast<cd *>(x), opt, rep, st);
     if (e) return pfail(cuda_status(e), "peec_gmres: %s", cudaGetErrorString(e));
@@ -1791,8 +2157,12 @@ int pcbqs_gb300_peec_solve_mixed(pcbqs_gb300_peec *h, int k, const int32_t *sys_
         if (sys_host[s] < 0 || sys_host[s] >= h->op.nsys) return pfail(ERR_ARGUMENT, "peec_solve_mixed: system");
     if (precondition == 1 && !h->bj) return pfail(ERR_ARGUMENT, "peec_solve_mixed: no block-Jacobi set up");
     if (precondition == 2 && !h->lu) return pfail(ERR_ARGUMENT, "peec_solve_mixed: no factor set up");
-    Preconditioner *M = precondition == 1 ? static_cast<Preconditioner *>(h->bj)
-                        : precondition == 2 ? static_cast<Preconditioner *>(h->lu) : nullptr;
+    if (precondition == 3 && !h->graph) return pfail(ERR_ARGUMENT, "peec_solve_mixed: no graph preconditioner set up");
+    if (precondition < 0 || precondition > 3) return pfail(ERR_ARGUMENT, "peec_solve_mixed: preconditioner 0 .. 3");
+    Preconditioner *M = precondition == 1   ? static_cast<Preconditioner *>(h->bj)
+                        : precondition == 2 ? static_cast<Preconditioner *>(h->lu)
+                        : precondition == 3 ? static_cast<Preconditioner *>(h->graph)
+                                            : nullptr;
     SingleView single;
     single.op = &h->op;
     RefineOptions opt;

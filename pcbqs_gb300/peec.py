@@ -230,6 +230,7 @@ class PeecTopology:
         keep[roots] = False
         self.tree_lu = splu(T[keep].astype(complex).tocsc()) if T.shape[1] else None
         self.A, self.K, self.T, self.B, self.keep, self.nl = A, K, T, B, keep, nl
+        self.ends, self.labels, self.tree = np.asarray(ends, np.int64).reshape(-1, 2), labels, tree
         self.sources, self.passive, self.nn, self.nb = sources, passive, nn, nb
         self.source_components = np.asarray((A[:, sources].T @ B).todense())
         self.R = sheet_resistance(r, b.sigma, b.thickness)
@@ -245,6 +246,7 @@ class PeecTopology:
             pos_branch = np.r_[pos_branch, np.c_[v[:, :2], 1e3 * (v[:, 3] + v[:, 4]) / 2]]
         own = np.r_[col_branch[cycles], np.flatnonzero(tree)]
         assert len(own) == n and own.max() < ne + nv
+        self.own = own
         self.order = cluster_order(pos_branch[own], self.bs)
         self.Kp = K[passive][:, self.order].tocsc()           # passive rows, clustered columns
         Tfull = hstack((csr_matrix((nn, nl)), T), format='csc')     # loop columns carry no charge
@@ -255,6 +257,93 @@ class PeecTopology:
         self.host_csr = dict(K=_host_csr(self.Kp), Kt=_host_csr(self.Kp.T), T=_host_csr(self.Tp),
                              Tt=_host_csr(self.Tp.T), R=_host_csr(self.R))
         self.log(f'peec: {nn:,} nodes, {ne:,} edges, {n:,} unknowns ({nl:,} loops), {nc} components')
+
+    def graph_structure(self):
+        """The frequency-independent arrays of the graph preconditioner (src/pcbqs/peec_iterative.py:44-84, boards
+        without face-sheet pairs), indexed by the clustered unknowns, made once per topology (host arrays):
+
+        keep_row (nn): each node's row among the kept nodes, -1 at each component's root (the lowest-numbered node,
+        whose equation T[keep] drops, peec_iterative.py:150); ac (nkeep x n): each loop's defining (cotree) branch's
+        incidence, +1 at its first end and -1 at its second (Ap on the loops' trial currents); lap_ptr / lap_branch /
+        lap_other: each kept node's passive branches and their other ends' rows (-1 at a root), the graph Laplacian
+        Ap Dinv Ap^T [keep][:, keep] by its edges; tinv (n x nkeep, rows of the tree unknowns) = T[keep]^-1 and tinvt
+        its transpose, explicit: T[keep] is the incidence of the spanning forest without its roots, so with the
+        forest rooted there the current in tree branch e is A[c, e] times the sum of the right-hand side over the
+        nodes below e (c the lower end of e), and a node's potential is the signed sum of the right-hand side over
+        the branches of its path to the root (nonzeros: the sum of the nodes' depths); branch (n): each unknown's
+        branch (a loop's defining branch, a tree unknown's own); loop_ends (n x 2): a loop's defining branch's ends
+        as kept rows; comp (nkeep), member_ptr / members: the kept nodes of each component."""
+        g = self.__dict__.get('_graph')
+        if g is not None:
+            return g
+        from scipy.sparse.csgraph import breadth_first_order
+        nn, n, ni = self.nn, self.n, self.ni
+        ea, eb = self.ends[:, 0], self.ends[:, 1]
+        keep = self.keep
+        nkeep = int(keep.sum())
+        kidx = np.full(nn, -1, np.int64)
+        kidx[keep] = np.arange(nkeep)
+        branch = np.asarray(self.own)[self.order]
+        is_tree = self.is_tree.astype(bool)
+        if int(is_tree.sum()) != nkeep:
+            raise ValueError('graph preconditioner: the spanning forest does not span the components')
+        loops = np.flatnonzero(~is_tree)
+        la, lb = kidx[ea[branch[loops]]], kidx[eb[branch[loops]]]
+        rows, cols = np.r_[la, lb], np.r_[loops, loops]
+        vals = np.r_[np.ones(len(loops)), -np.ones(len(loops))]
+        ok = rows >= 0
+        ac = csr_matrix((vals[ok], (rows[ok], cols[ok])), shape=(nkeep, n))
+        ac.sum_duplicates()
+        ac.eliminate_zeros()
+        loop_ends = np.full((n, 2), -1, np.int32)
+        loop_ends[loops, 0], loop_ends[loops, 1] = la, lb
+        # the Laplacian's edges at each kept node, in branch order
+        p = np.flatnonzero(ea[:ni] != eb[:ni])
+        r = np.r_[kidx[ea[p]], kidx[eb[p]]]
+        br = np.r_[p, p]
+        oth = np.r_[kidx[eb[p]], kidx[ea[p]]]
+        ok = r >= 0
+        r, br, oth = r[ok], br[ok], oth[ok]
+        o = np.lexsort((br, r))
+        r, br, oth = r[o], br[o], oth[o]
+        lap_ptr = np.r_[0, np.cumsum(np.bincount(r, minlength=nkeep))].astype(np.int64)
+        # the spanning forest rooted at the dropped nodes: each node's parent and the branch to it
+        tb = np.flatnonzero(self.tree)
+        adj = csr_matrix((np.r_[tb, tb] + 1.0, (np.r_[ea[tb], eb[tb]], np.r_[eb[tb], ea[tb]])), shape=(nn, nn))
+        parent = np.full(nn, -1, np.int64)
+        for root in np.flatnonzero(~keep):
+            reached, pred = breadth_first_order(adj, int(root), directed=False, return_predecessors=True)
+            below = reached[1:]
+            parent[below] = pred[below]
+        if (parent[keep] < 0).any():
+            raise ValueError('graph preconditioner: a node is not reached by the spanning forest')
+        up = np.flatnonzero(keep)
+        pbranch = np.full(nn, -1, np.int64)
+        pbranch[up] = np.asarray(adj[up, parent[up]]).ravel().astype(np.int64) - 1
+        tpos = np.full(self.nb, -1, np.int64)
+        tpos[branch[is_tree]] = np.flatnonzero(is_tree)
+        # T[keep]^-1: for every node, an entry in the row of each branch on its path to the root
+        R, C, V = [], [], []
+        cur, start = up.copy(), kidx[up]
+        while cur.size:
+            e = pbranch[cur]
+            R.append(tpos[e])
+            C.append(start)
+            V.append(np.where(ea[e] == cur, 1.0, -1.0))
+            cur = parent[cur]
+            more = keep[cur]
+            cur, start = cur[more], start[more]
+        tinv = csr_matrix((np.concatenate(V), (np.concatenate(R), np.concatenate(C))), shape=(n, nkeep))
+        comp = np.asarray(self.labels)[keep].astype(np.int32)
+        nc = int(self.B.shape[1])
+        members = np.argsort(comp, kind='stable').astype(np.int32)
+        member_ptr = np.r_[0, np.cumsum(np.bincount(comp, minlength=nc))].astype(np.int64)
+        g = dict(nkeep=nkeep, ncomp=nc, keep_row=kidx, ac=_host_csr(ac), lap_ptr=lap_ptr,
+                 lap_branch=br.astype(np.int32), lap_other=oth.astype(np.int32), tinv=_host_csr(tinv),
+                 tinvt=_host_csr(tinv.T), branch=branch.astype(np.int32), loop_ends=loop_ends, comp=comp,
+                 member_ptr=member_ptr, members=members)
+        self._graph = g
+        return g
 
 
 
@@ -369,6 +458,7 @@ class PeecModel(PeecTopology):
         pdiag = torch.diagonal(self.P) if self.Pim is None else torch.complex(torch.diagonal(self.P),
                                                                                torch.diagonal(self.Pim))
         self.pscale = float(pdiag.abs().max())
+        self.pdiag_host = pdiag.cpu().numpy()
         self.ldiag = torch.diagonal(self.L).cpu().numpy()
         self._pinvb = None
         return self
@@ -471,6 +561,7 @@ class PeecModel(PeecTopology):
         torch.cuda.synchronize()
         self.ldiag = ldiag
         self.pscale = float(self.pdiag.abs().max())
+        self.pdiag_host = self.pdiag.cpu().numpy()
         self._pinvb = None
         self.mixed_fill = False
         self.analytic = None
@@ -629,7 +720,7 @@ class PeecModel(PeecTopology):
                                                    Y.data_ptr(), stream), lib)
         return Y.cpu().numpy().reshape(shape)
 
-    PRECONDITIONERS = {'none': 0, 'block_jacobi': 1, 'lu32': 2}
+    PRECONDITIONERS = {'none': 0, 'block_jacobi': 1, 'lu32': 2, 'graph': 3}
 
     def resistance_ratio(self, freqs):
         """R(f) / R_dc per frequency: 1 for conductor_loss='dc'; for 'slab' the finite-thickness sheet impedance
@@ -673,20 +764,64 @@ class PeecModel(PeecTopology):
     PRODUCT = {'fp32': 0, 'tc3': 3, 'tc6': 6}
     FP64_PRODUCT = {'fp64': 0, 'sliced5': 5, 'sliced6': 6, 'sliced7': 7}
 
+    def _graph_device(self):
+        """The graph preconditioner's structure (graph_structure) on the device, uploaded once per model."""
+        gd = self.__dict__.get('_graph_dev')
+        if gd is None:
+            g, dev = self.graph_structure(), self.device
+            up = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+            gd = dict(ac=_dev_csr(g['ac'], dev), tinv=_dev_csr(g['tinv'], dev), tinvt=_dev_csr(g['tinvt'], dev),
+                      **{name: up(g[name]) for name in ('lap_ptr', 'lap_branch', 'lap_other', 'branch', 'loop_ends',
+                                                        'comp', 'member_ptr', 'members')})
+            self._graph_dev = gd
+        return gd
+
+    def _graph_precondition(self, handle, sys_index, freq, refine, stream):
+        """Set up the graph preconditioner of system sys_index (frequency freq) in the live operator: the branches'
+        own impedance d = r(f) R_ii + j w L_ii (the via barrels at their DC resistance, as in the operator), 1/d with
+        |d| raised to 1e-12 zscale where smaller (peec_iterative.py:52), and 1/P_ii with its per-component sums
+        (peec_iterative.py:29-30)."""
+        g, gd = self.graph_structure(), self._graph_device()
+        lib = _lib.load()
+        zs = float(self._zscale[sys_index])
+        rd = np.asarray(self.R.diagonal(), complex)
+        rd[:self.ne] *= self.resistance_ratio([freq])[0]
+        zdiag = rd + 1j * 2 * np.pi * freq * np.asarray(self.ldiag[:self.ni], float)
+        d = zdiag.copy()
+        d[np.abs(d) < zs * 1e-12] = zs * 1e-12
+        pinv = 1 / np.asarray(self.pdiag_host, complex)
+        total = (np.bincount(self.labels, pinv.real, minlength=g['ncomp']) +
+                 1j * np.bincount(self.labels, pinv.imag, minlength=g['ncomp']))
+        vals = {name: torch.as_tensor(np.ascontiguousarray(a, complex), device=self.device)
+                for name, a in (('zdiag', zdiag), ('dinv', 1 / d), ('pinv', pinv[self.keep]), ('total', total))}
+        desc = _lib.GraphDesc()
+        desc.nkeep, desc.ncomp, desc.nbranch = g['nkeep'], g['ncomp'], self.ni
+        for name in ('ac', 'tinv', 'tinvt'):
+            setattr(desc, name, _csr_struct(gd[name]))
+        for name in ('lap_ptr', 'lap_branch', 'lap_other', 'branch', 'loop_ends', 'comp', 'member_ptr', 'members'):
+            setattr(desc, name, gd[name].data_ptr())
+        for name, t in vals.items():
+            setattr(desc, name, t.data_ptr())
+        _lib.check(lib.pcbqs_gb300_peec_graph(handle, ctypes.byref(desc), int(sys_index), int(bool(refine)), stream),
+                   lib)
+
     def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='tc6-blocked', anchors=None,
-              captured=False, product='tc3', fp64_product=None):
+              captured=False, product='tc3', fp64_product=None, graph_refine=True):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
 
         precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
-        dense loop/tree system), or 'none'. mixed=False: FP64 GMRES on the FP64 operator; mixed=True: FP64
-        iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose dense products run
-        in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of the 'lu32'
+        dense loop/tree system), 'graph' (the reference's graph preconditioner, peec_iterative.py:44-84: loop
+        currents from the branches' graph Laplacian, factored dense in complex64 on the device, with one FP64
+        correction of each of its solves unless graph_refine=False; tree charges through the spanning forest's
+        explicit inverse; dense or compressed operator), or 'none'. mixed=False: FP64 GMRES on the FP64 operator;
+        mixed=True: FP64 iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose
+        dense products run in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of the 'lu32'
         factorization: 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy) through cuSOLVER's getrf;
         through this library's blocked LU (2048-column panels factored ahead of the trailing updates) 'fp32-blocked'
         or 'bf16x9-blocked' with cuBLAS trailing GEMMs, or 'tc6-blocked' (the default) / 'tc3-blocked' with this
         library's tcgen05 update on six / three BF16 part products (six: FP32's accuracy; three: about 16 bits, a
         weaker preconditioner that costs GMRES steps). anchors ('lu32'
-        only): how many factorizations a sweep shares; the frequencies, in increasing order, are split into that
+        and 'graph'): how many factorizations a sweep shares; the frequencies, in increasing order, are split into that
         many runs and every run is solved as one batch of (frequency, port) columns preconditioned by the factor
         at its middle frequency (default: one factor per frequency). Every column still reaches the tolerance of
         its own frequency's FP64 system; farther from the anchor it takes more iterations. captured=True: each GMRES
@@ -714,7 +849,7 @@ class PeecModel(PeecTopology):
         if fp64_product not in self.FP64_PRODUCT:
             raise ValueError(f'fp64_product must be one of {sorted(self.FP64_PRODUCT)}')
         if self.matrix == 'hierarchical' and precondition == 'lu32':
-            raise ValueError("the compressed operator solves with precondition 'block_jacobi' or 'none'")
+            raise ValueError("the compressed operator solves with precondition 'block_jacobi', 'graph' or 'none'")
         nf = len(f)
         if anchors is None:
             anchors = nf
@@ -726,7 +861,7 @@ class PeecModel(PeecTopology):
         excitation = np.eye(npo, dtype=complex)
         omegas = 2 * np.pi * f
         handle, zscale = self._operator(omegas)
-        if mode == 2:
+        if mode in (2, 3):
             runs = np.array_split(np.argsort(f, kind='stable'), anchors)
             groups = [(int(run[len(run) // 2]), run) for run in runs]
         else:
@@ -835,6 +970,13 @@ class PeecModel(PeecTopology):
                                                        Pf.stride(0)), lib)
             converged = True
             for g, (anchor, members) in enumerate(groups):
+                if mode == 3:
+                    e0, e1 = timed()
+                    e0.record()
+                    self._graph_precondition(handle, anchor, f[anchor], graph_refine, stream)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    precondition_ms += e0.elapsed_time(e1)
                 if mode == 2 and g > 0:
                     e0, e1 = timed()
                     e0.record()
@@ -876,7 +1018,7 @@ class PeecModel(PeecTopology):
                     x_all[:, torch.as_tensor(sel, device=self.device)] = x
                 its[sel], res[sel] = its_g, res_g
             self.timings.update(precondition_ms=precondition_ms, gmres_ms=gmres_ms, gmres_iterations=its.tolist(),
-                                factorizations=len(groups) if mode == 2 else 0, factor_assemble_ms=stage_ms[0],
+                                factorizations=len(groups) if mode in (2, 3) else 0, factor_assemble_ms=stage_ms[0],
                                 factor_lu_ms=stage_ms[1], factor_update_ms=updates[0],
                                 factor_update_flops=updates[1], factor_update_launches=int(updates[2]))
             if mixed:

@@ -1,0 +1,89 @@
+"""The graph preconditioner's host-built structure (PeecTopology.graph_structure: kept-node rows, the loops' node
+incidence, the Laplacian's edge lists, the spanning forest's explicit inverse, the components) against the
+oracle's restatement of the reference's graph preconditioner (oracle/graph.py, src/pcbqs/peec_iterative.py:19-84),
+on the CPU: the device kernels' steps replayed in numpy from the structure give the reference's output to rounding,
+and the explicit inverse is T[keep]^-1."""
+import numpy as np
+import pytest
+from scipy.sparse import csr_matrix
+
+
+def _topology(board):
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecTopology
+    from pcbqs_gb300.rwg import RWG
+    b = Board.load(board)
+    return PeecTopology(b, RWG(b.nodes, b.tris))
+
+
+def _csr(h):
+    ptr, idx, val, shape = h
+    return csr_matrix((val, idx, ptr), shape=shape)
+
+
+def _kernel_steps(t, g, zdiag, dinv, zs, ps, pinv_keep, total, y):
+    """The steps of the device preconditioner (k_graph_* in csrc/peec_op.cu) in numpy, the Laplacian solved
+    densely."""
+    is_tree = t.is_tree.astype(bool)
+    br, nk = g['branch'], g['nkeep']
+    ac, tinv, tinvt = _csr(g['ac']), _csr(g['tinv']), _csr(g['tinvt'])
+    tw = np.where(is_tree, 0, zs * dinv[br])
+    rhs = ac @ (tw * y)
+    rows = np.repeat(np.arange(nk), np.diff(g['lap_ptr']))
+    w = dinv[g['lap_branch']]
+    G = csr_matrix((w, (rows, rows)), shape=(nk, nk)).toarray()
+    m = g['lap_other'] >= 0
+    G -= csr_matrix((w[m], (rows[m], g['lap_other'][m])), shape=(nk, nk)).toarray()
+    v = np.linalg.solve(G, rhs)
+    out = np.zeros(t.n, complex)
+    loops = ~is_tree
+    ka, kb = g['loop_ends'][:, 0], g['loop_ends'][:, 1]
+    va = np.where(ka >= 0, v[np.maximum(ka, 0)], 0)
+    vb = np.where(kb >= 0, v[np.maximum(kb, 0)], 0)
+    out[loops] = (tw * y - dinv[br] * (va - vb))[loops]
+    current = t.Kp.tocsr()[:, loops] @ out[loops]
+    rt = np.zeros(t.n, complex)
+    rt[is_tree] = (y - zdiag[br] / zs * current[br])[is_tree]
+    v2 = tinvt @ rt
+    mp, mem = g['member_ptr'], g['members']
+    common = np.array([np.sum(pinv_keep[mem[mp[c]:mp[c + 1]]] * v2[mem[mp[c]:mp[c + 1]]])
+                       for c in range(g['ncomp'])]) / total
+    charge = pinv_keep * (v2 - common[g['comp']])
+    out[is_tree] = ps * (tinv @ charge)[is_tree]
+    return out
+
+
+@pytest.mark.parametrize('board', ['tiny', 'strip', 'viapair'])
+def test_graph_structure_replays_the_reference_preconditioner(board):
+    import oracle.graph as G
+    t = _topology(board)
+    g = t.graph_structure()
+    rng = np.random.default_rng(7)
+    ni = t.ni
+    diagonal = np.r_[rng.uniform(0.5, 2, ni) + 1j * rng.uniform(0.1, 5, ni), np.zeros(t.nb - ni)]
+    zs, ps = float(np.abs(diagonal).max()), 3.7
+    pdiag = rng.uniform(1, 2, t.nn)
+    apply = G.graph_preconditioner(t.K, t.A, t.T, t.B, t.nl, t.keep, t.passive, t.own[:t.nl], diagonal, zs, ps, pdiag)
+    d = diagonal[:ni].copy()
+    d[np.abs(d) < zs * 1e-12] = zs * 1e-12
+    pinv = 1 / pdiag
+    total = np.bincount(t.labels, pinv, minlength=g['ncomp']).astype(complex)
+    for _ in range(2):
+        y = rng.standard_normal(t.n) + 1j * rng.standard_normal(t.n)
+        ref = apply(y)
+        got = _kernel_steps(t, g, diagonal[:ni], 1 / d, zs, ps, pinv[t.keep], total, y[t.order])
+        assert np.abs(got - ref[t.order]).max() <= 1e-11 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize('board', ['tiny', 'viapair'])
+def test_explicit_tree_inverse_is_the_inverse(board):
+    t = _topology(board)
+    g = t.graph_structure()
+    is_tree = t.is_tree.astype(bool)
+    Tk = t.Tp.tocsr()[t.keep][:, np.flatnonzero(is_tree)]          # kept nodes x tree unknowns (clustered)
+    tinv = _csr(g['tinv'])[np.flatnonzero(is_tree)]
+    eye = (tinv @ Tk).toarray()
+    assert np.array_equal(eye, np.eye(g['nkeep']))
+    assert np.array_equal(_csr(g['tinvt']).toarray()[:, is_tree], tinv.T.toarray())
+    assert g['member_ptr'][-1] == g['nkeep'] and len(g['comp']) == g['nkeep']
+    assert (g['keep_row'] >= 0).sum() == g['nkeep']
