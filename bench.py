@@ -80,7 +80,8 @@ def parse():
     p.add_argument('--case', default=None,
                    help='time one kernel case small enough for a full ncu capture instead of the benchmark: '
                         'fill:BOARD[:TRIANGLES] | lu:BOARD[:K...] | dense:N[:K] | getrf:N[:BLOCK[:MATH...]] | '
-                        'potrf:N[:BLOCK...] | update:ROWS:COLS:K (CUDA-event times after a warm-up call)')
+                        'potrf:N[:BLOCK...] | update:ROWS:COLS:K (CUDA-event times after a warm-up call) | '
+                        'c5 | c5solve[:FREQ[:MIXED[:PARTS]]] (the large compressed board)')
     return p.parse_args()
 
 
@@ -639,8 +640,46 @@ def case_c5(k=32, leaf=256, tol=1e-6):
     print(_json.dumps(out), flush=True)
 
 
+def case_c5solve(freq=1e6, mixed=1, parts=0):
+    """The PEEC solve of the large compressed board (tests/golden/c5.npz: 212,297 triangles, 16 ports): every port
+    driven alone at one frequency through the compressed operator (H-matrices at tol 1e-6, leaves 256, rank <= 32),
+    preconditioned by the graph preconditioner with its Laplacian split into domains (parts 0: by its size), the
+    FP64 GMRES (mixed=0) or FP64 refinement around inner GMRES on BF16 products (mixed=1), to 1e-8. Prints one JSON
+    line with the stage times, steps, residuals and the port matrix's diagonal."""
+    import json as _json
+    import torch
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.peec import PeecModel
+    freq, mixed, parts = float(freq), bool(int(mixed)), int(parts) or None
+    b = Board.load('c5')
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    model = PeecModel(b, matrix='hierarchical')
+    model.assemble()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    res = model.solve([freq], precondition='graph', mixed=mixed, graph_parts=parts)
+    t2 = time.perf_counter()
+    tm = model.timings
+    Z = res.impedance[0]
+    g = model.graph_structure()
+    out = dict(case='c5solve', triangles=int(len(b.tris)), unknowns=int(model.n), loops=int(model.nl),
+               nodes=int(model.nn), ports=len(b.ports), freq=freq, mixed=mixed,
+               graph_parts=int(model._graph_parts(parts)), laplacian_rows=int(g['nkeep']),
+               tree_inverse_entries=int(len(g['tinv'][1])), assemble_s=round(t1 - t0, 2), solve_s=round(t2 - t1, 2),
+               hmatrix_s=round(tm.get('hmatrix_s', 0.0), 2), host_topology_s=round(tm.get('host_topology_s', 0.0), 2),
+               equilibrium_s=round(tm.get('equilibrium_s', 0.0), 2),
+               precondition_ms=round(tm['precondition_ms'], 1), gmres_ms=round(tm['gmres_ms'], 1),
+               gmres_steps_max=int(res.iterations.max()), outer_steps=tm.get('outer_steps'),
+               residual_max=float(res.residual.max()),
+               reciprocity=float(np.abs(Z - Z.T).max() / np.abs(Z).max()),
+               z_diag=[[float(z.real), float(z.imag)] for z in np.diag(Z)],
+               torch_peak_gbytes=round(torch.cuda.max_memory_allocated() / 1e9, 2))
+    print(_json.dumps(out), flush=True)
+
+
 CASES = dict(fill=case_fill, lu=case_lu, getrf=case_getrf, potrf=case_potrf, dense=case_dense, update=case_update,
-             lusolve=case_lusolve, lowrank=case_lowrank, c5=case_c5)
+             lusolve=case_lusolve, lowrank=case_lowrank, c5=case_c5, c5solve=case_c5solve)
 
 
 def kernel_case(spec):

@@ -258,9 +258,24 @@ int pcbqs_gb300_peec_block_jacobi(pcbqs_gb300_peec *op, int32_t bs, const double
  * (pcbqs_gb300_lu_factor_c64, 2048-column panels) with BF16x9 / FP32 GEMMs. Mirrors MixedLU (src/pcbqs/kernels.py:125-181): a complex64 factor
  * with the FP64 operator's GMRES on top in place of its refinement loop. */
 int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *op, const pcbqs_gb300_csr *krk, int32_t sys, int math, void *stream);
+/* A split of the graph Laplacian's kept rows into `parts` domains whose interiors share no edge, and a separator
+ * (pcbqs_gb300_graph.domains). New order: the domains' interiors one after another, then the separator. dom_ptr
+ * and bnd_ptr are HOST arrays, the rest device arrays. */
+typedef struct pcbqs_gb300_graph_domains {
+    int64_t parts;
+    int64_t n_int;                 /* interior rows (the separator has nkeep - n_int) */
+    const int64_t *perm;           /* nkeep: the kept row at each new position */
+    const int64_t *pos;            /* nkeep: each kept row's new position */
+    const int64_t *dom_ptr;        /* host, parts + 1: each domain's first new position (dom_ptr[parts] = n_int) */
+    const int64_t *bnd_ptr;        /* host, parts + 1: each domain's first boundary entry */
+    const int32_t *bnd;            /* per boundary entry: the separator node's position within the separator */
+    const int64_t *bnd_nptr;       /* per boundary entry + 1: its interior neighbours in the domain */
+    const int32_t *bnd_local;      /*   the neighbour's row within its domain */
+    const int32_t *bnd_branch;     /*   the branch between them */
+} pcbqs_gb300_graph_domains;
 /* The graph preconditioner's structure and its values at one frequency (pcbqs_gb300_peec_graph); every pointer a
- * device array, complex values interleaved (re, im). Unknowns in the operator's order; "kept" nodes are all but each
- * component's root, whose equation T[keep] drops. */
+ * device array, complex values interleaved (re, im). Unknowns in the operator's order; "kept" nodes are all but one
+ * grounded node per component, whose equation T[keep] drops. */
 typedef struct pcbqs_gb300_graph {
     int64_t nkeep;                 /* kept nodes */
     int64_t ncomp;                 /* components of the passive branches' graph */
@@ -280,16 +295,19 @@ typedef struct pcbqs_gb300_graph {
     const double *dinv;            /* nbranch complex: 1 / zdiag, |zdiag| raised to 1e-12 zscale where smaller */
     const double *pinv;            /* nkeep complex: 1 / P_ii at the kept nodes */
     const double *total;           /* ncomp complex: the sum of 1 / P_ii over each component's nodes */
+    const pcbqs_gb300_graph_domains *domains;   /* host struct, or NULL: the Laplacian dense */
 } pcbqs_gb300_graph;
 /* The reference's graph preconditioner (_graph_preconditioner and the charge-tree solve of _tree_preconditioner,
  * src/pcbqs/peec_iterative.py:19-84, without face-sheet pairs) at system index sys, for precondition 3 of
  * pcbqs_gb300_peec_gmres and pcbqs_gb300_peec_solve_mixed: the loop currents from the graph Laplacian
- * Ap diag(dinv) Ap^T [keep][:, keep] (assembled dense on the device and LU-factored in complex64 with this library's
- * tcgen05 updates, in place of the reference's sparse incomplete LU; refine = 1 adds one FP64 residual correction
- * of each Laplacian solve), the tree unknowns' charges through the explicit T[keep]^-1 and the components'
- * equilibrium. Works with the dense and the compressed operator; the structure's arrays must outlive the handle
- * (the frequency's values are copied). Status 4 when the dense Laplacian does not fit in device memory, 3 when its
- * factor meets a zero pivot. */
+ * G = Ap diag(dinv) Ap^T [keep][:, keep] in place of the reference's sparse incomplete LU: domains NULL, G assembled
+ * dense on the device and LU-factored in complex64 with this library's tcgen05 updates; else split into domains
+ * (explicit complex64 inverses of their blocks, applied as GEMMs) and a dense Schur complement on the separator
+ * (complex64 LU); `refine` (0..3) FP64 residual corrections of each Laplacian solve. The tree unknowns' charges
+ * through the explicit T[keep]^-1 and the components' equilibrium. Works with the dense and the compressed
+ * operator; the domain split's solves cannot be captured (captured GMRES cycles need domains NULL). The structure's
+ * arrays must outlive the handle (the frequency's values are copied). Status 4 when the Laplacian's factors do not
+ * fit in device memory, 3 when a factor meets a zero pivot. */
 int pcbqs_gb300_peec_graph(pcbqs_gb300_peec *op, const pcbqs_gb300_graph *g, int32_t sys, int refine, void *stream);
 /* out = M in for k columns (device, (n, k) complex128 row-major) with the graph preconditioner set up last
  * (validation of the preconditioner alone); synchronizes `stream`. */

@@ -46,13 +46,20 @@ class HmatDesc(ctypes.Structure):
                 ('store', c_void_p), ('max_rank', ctypes.c_int32)]
 
 
+class GraphDomainsDesc(ctypes.Structure):
+    """pcbqs_gb300_graph_domains: the Laplacian's domain split (dom_ptr, bnd_ptr host arrays)."""
+    _fields_ = [('parts', ctypes.c_int64), ('n_int', ctypes.c_int64), ('perm', c_void_p), ('pos', c_void_p),
+                ('dom_ptr', c_void_p), ('bnd_ptr', c_void_p), ('bnd', c_void_p), ('bnd_nptr', c_void_p),
+                ('bnd_local', c_void_p), ('bnd_branch', c_void_p)]
+
+
 class GraphDesc(ctypes.Structure):
     """pcbqs_gb300_graph: the graph preconditioner's device arrays and one frequency's values."""
     _fields_ = [('nkeep', ctypes.c_int64), ('ncomp', ctypes.c_int64), ('nbranch', ctypes.c_int64), ('ac', CsrDesc),
                 ('lap_ptr', c_void_p), ('lap_branch', c_void_p), ('lap_other', c_void_p), ('tinv', CsrDesc),
                 ('tinvt', CsrDesc), ('branch', c_void_p), ('loop_ends', c_void_p), ('comp', c_void_p),
                 ('member_ptr', c_void_p), ('members', c_void_p), ('zdiag', c_void_p), ('dinv', c_void_p),
-                ('pinv', c_void_p), ('total', c_void_p)]
+                ('pinv', c_void_p), ('total', c_void_p), ('domains', ctypes.POINTER(GraphDomainsDesc))]
 
 
 class LowRankDesc(ctypes.Structure):

@@ -1304,6 +1304,261 @@ __global__ void k_graph_tree_out(int64_t n, int k, const int8_t *is_tree, Csr ti
     }
 }
 
+// The graph Laplacian's solve, x = G^-1 r for k columns ((nkeep, k) complex128 row-major, kept-row order).
+struct LapSolver {
+    virtual ~LapSolver() = default;
+    // deferred: capturable (no host synchronization or allocation; after one call with this k)
+    virtual cudaError_t solve(int k, const cd *r, cd *x, cudaStream_t s, bool deferred) = 0;
+    virtual cudaError_t status(int k, cudaStream_t s) { return cudaSuccess; }
+};
+
+// G dense in complex64, LU-factored by getrf_blocked (tcgen05 updates), solved by the streaming/blocked TriSolver.
+struct DenseLap : LapSolver {
+    float2 *G = nullptr;
+    int *ipiv = nullptr;
+    TriSolver tri;
+    ~DenseLap() override {
+        tri.release();
+        dev_free(G);
+        dev_free(ipiv);
+    }
+    cudaError_t solve(int k, const cd *r, cd *x, cudaStream_t s, bool deferred) override {
+        return tri.solve(k, r, x, s, deferred);
+    }
+    cudaError_t status(int k, cudaStream_t s) override { return tri.read_status(k, s); }
+};
+
+// rows new position p of `in` (kept-row order) -> out[p] = in[perm[p]]; and back.
+__global__ void k_rows_gather(int64_t rows, int k, const int64_t *perm, const cd *in, cd *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * k; t += (int64_t)gridDim.x * blockDim.x)
+        out[t] = in[perm[t / k] * k + t % k];
+}
+
+__global__ void k_rows_scatter(int64_t rows, int k, const int64_t *perm, const cd *in, cd *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * k; t += (int64_t)gridDim.x * blockDim.x)
+        out[perm[t / k] * k + t % k] = in[t];
+}
+
+// out (n, k) row-major complex128 += in (n x k column-major complex64)
+__global__ void k_from_c64_cols_add(int64_t n, int k, const float2 *in, cd *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = in[(t % k) * n + t / k];
+        out[t].x += v.x;
+        out[t].y += v.y;
+    }
+}
+
+// One domain's block of G (nd x nd, rows = columns: symmetric), zeroed beforehand: the diagonal sums every branch of
+// the row's node, the off-diagonal entries only the branches to the domain's own interior.
+__global__ void k_domain_block(int64_t off, int64_t nd, const int64_t *perm, const int64_t *pos,
+                               const int64_t *lap_ptr, const int32_t *lap_branch, const int32_t *lap_other,
+                               const cd *dinv, float2 *A) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kr = perm[off + i];
+        double re = 0, im = 0;
+        for (int64_t a = lap_ptr[kr]; a < lap_ptr[kr + 1]; ++a) {
+            const cd w = dinv[lap_branch[a]];
+            re += w.x;
+            im += w.y;
+            const int32_t o = lap_other[a];
+            if (o < 0) continue;
+            const int64_t q = pos[o] - off;
+            if (q >= 0 && q < nd) {
+                A[i * nd + q].x -= (float)w.x;
+                A[i * nd + q].y -= (float)w.y;
+            }
+        }
+        A[i * nd + i].x += (float)re;
+        A[i * nd + i].y += (float)im;
+    }
+}
+
+__global__ void k_identity_c64(int64_t n, float2 *A) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x)
+        A[t] = make_float2(t / n == t % n ? 1.f : 0.f, 0.f);
+}
+
+// The separator block G_SS (ns x ns, zeroed beforehand): rows at new positions n_int + p.
+__global__ void k_separator_block(int64_t ns, int64_t n_int, const int64_t *perm, const int64_t *pos,
+                                  const int64_t *lap_ptr, const int32_t *lap_branch, const int32_t *lap_other,
+                                  const cd *dinv, float2 *S) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < ns; p += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kr = perm[n_int + p];
+        double re = 0, im = 0;
+        for (int64_t a = lap_ptr[kr]; a < lap_ptr[kr + 1]; ++a) {
+            const cd w = dinv[lap_branch[a]];
+            re += w.x;
+            im += w.y;
+            const int32_t o = lap_other[a];
+            if (o < 0) continue;
+            const int64_t q = pos[o] - n_int;
+            if (q >= 0) {
+                S[p * ns + q].x -= (float)w.x;
+                S[p * ns + q].y -= (float)w.y;
+            }
+        }
+        S[p * ns + p].x += (float)re;
+        S[p * ns + p].y += (float)im;
+    }
+}
+
+// One domain's Schur term: S[bnd_p, bnd_q] -= sum_{i ~ p} sum_{j ~ q} w_pi Ainv[i, j] w_qj over its m boundary
+// entries (nptr: each entry's interior neighbours, local rows and branches). One thread per (p, q).
+__global__ void k_schur_domain(int64_t m, const int32_t *bnd, const int64_t *nptr, const int32_t *local,
+                               const int32_t *branch, const cd *dinv, const float2 *Ainv, int64_t nd, float2 *S,
+                               int64_t ns) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * m; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = t / m, q = t % m;
+        cd acc = make_double2(0, 0);
+        for (int64_t a = nptr[p]; a < nptr[p + 1]; ++a) {
+            const cd wa = dinv[branch[a]];
+            cd row = make_double2(0, 0);
+            for (int64_t b = nptr[q]; b < nptr[q + 1]; ++b) {
+                const float2 v = Ainv[(int64_t)local[a] + (int64_t)local[b] * nd];
+                const cd pr = zmul(make_double2(v.x, v.y), dinv[branch[b]]);
+                row.x += pr.x;
+                row.y += pr.y;
+            }
+            const cd pr = zmul(wa, row);
+            acc.x += pr.x;
+            acc.y += pr.y;
+        }
+        float2 &e = S[(int64_t)bnd[p] * ns + bnd[q]];
+        e.x -= (float)acc.x;
+        e.y -= (float)acc.y;
+    }
+}
+
+// r_S = r_S + sum over each separator row's interior neighbours of w y_I   (r_S - G_SI y_I)
+__global__ void k_separator_rhs(int64_t ns, int k, int64_t n_int, const int64_t *perm, const int64_t *pos,
+                                const int64_t *lap_ptr, const int32_t *lap_branch, const int32_t *lap_other,
+                                const cd *dinv, const cd *rn, const cd *yI, cd *rS) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ns * k; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = t / k;
+        const int c = (int)(t % k);
+        const int64_t kr = perm[n_int + p];
+        cd acc = rn[(n_int + p) * k + c];
+        for (int64_t a = lap_ptr[kr]; a < lap_ptr[kr + 1]; ++a) {
+            const int32_t o = lap_other[a];
+            if (o < 0) continue;
+            const int64_t q = pos[o];
+            if (q >= n_int) continue;
+            const cd pr = zmul(dinv[lap_branch[a]], yI[q * k + c]);
+            acc.x += pr.x;
+            acc.y += pr.y;
+        }
+        rS[t] = acc;
+    }
+}
+
+// t_I = sum over each interior row's separator neighbours of w x_S   (-G_IS x_S)
+__global__ void k_interior_coupling(int64_t n_int, int k, const int64_t *perm, const int64_t *pos,
+                                    const int64_t *lap_ptr, const int32_t *lap_branch, const int32_t *lap_other,
+                                    const cd *dinv, const cd *xS, cd *tI) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_int * k;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = t / k;
+        const int c = (int)(t % k);
+        const int64_t kr = perm[p];
+        cd acc = make_double2(0, 0);
+        for (int64_t a = lap_ptr[kr]; a < lap_ptr[kr + 1]; ++a) {
+            const int32_t o = lap_other[a];
+            if (o < 0) continue;
+            const int64_t q = pos[o];
+            if (q < n_int) continue;
+            const cd pr = zmul(dinv[lap_branch[a]], xS[(q - n_int) * k + c]);
+            acc.x += pr.x;
+            acc.y += pr.y;
+        }
+        tI[t] = acc;
+    }
+}
+
+// G split into `parts` domain interiors (no edges between them) and a separator S:
+//   G = [A_I  G_IS; G_SI  G_SS],  A_I = diag(A_d),  Schur S = G_SS - sum_d G_Sd A_d^-1 G_dS,
+//   y_I = A_I^-1 r_I,  x_S = S^-1 (r_S - G_SI y_I),  x_I = y_I - A_I^-1 G_IS x_S.
+// The domains' inverses are explicit in complex64 (cuSOLVER getrf + getrs against the identity at set-up), applied
+// per domain as cuBLAS complex64 GEMMs over all columns; S is dense in complex64, LU-factored by getrf_blocked and
+// solved by the TriSolver. Not capturable (its cuBLAS calls stay outside CUDA graphs).
+struct DomainLap : LapSolver {
+    int64_t nk = 0, n_int = 0, ns = 0, parts = 0;
+    std::vector<int64_t> dom_ptr, bnd_ptr, blk_off;
+    const int64_t *perm = nullptr, *pos = nullptr, *lap_ptr = nullptr;
+    const int32_t *lap_branch = nullptr, *lap_other = nullptr;
+    const cd *dinv = nullptr;
+    float2 *Ainv = nullptr, *S = nullptr;
+    int *ipiv = nullptr;
+    TriSolver tri;
+    cublasHandle_t blas = nullptr;
+    int cap = 0;
+    cd *rn = nullptr, *yI = nullptr, *rS = nullptr, *xS = nullptr, *tI = nullptr;
+    float2 *f1 = nullptr, *f2 = nullptr;
+    void free_work() {
+        for (void *p : {(void *)rn, (void *)yI, (void *)rS, (void *)xS, (void *)tI, (void *)f1, (void *)f2}) dev_free(p);
+        rn = yI = rS = xS = tI = nullptr;
+        f1 = f2 = nullptr;
+        cap = 0;
+    }
+    ~DomainLap() override {
+        tri.release();
+        free_work();
+        dev_free(Ainv);
+        dev_free(S);
+        dev_free(ipiv);
+        if (blas) cublasDestroy(blas);
+    }
+    cudaError_t reserve(int k, cudaStream_t s) {
+        if (k <= cap) return cudaSuccess;
+        free_work();
+        cudaError_t e;
+        if ((e = dev_alloc(&rn, (size_t)nk * k, s)) || (e = dev_alloc(&yI, (size_t)n_int * k, s)) ||
+            (e = dev_alloc(&rS, (size_t)ns * k, s)) || (e = dev_alloc(&xS, (size_t)ns * k, s)) ||
+            (e = dev_alloc(&tI, (size_t)n_int * k, s)) || (e = dev_alloc(&f1, (size_t)n_int * k, s)) ||
+            (e = dev_alloc(&f2, (size_t)n_int * k, s))) {
+            free_work();
+            return e;
+        }
+        cap = k;
+        return cudaSuccess;
+    }
+    // f2 = A_I^-1 f1, both (n_int x k) column-major complex64
+    cudaError_t domains_apply(int k, cudaStream_t s) {
+        cublasSetStream(blas, s);
+        const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
+        for (int64_t d = 0; d < parts; ++d) {
+            const int64_t off = dom_ptr[d], nd = dom_ptr[d + 1] - off;
+            if (!nd) continue;
+            if (cublasCgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)nd, k, (int)nd, &one,
+                            reinterpret_cast<const cuComplex *>(Ainv + blk_off[d]), (int)nd,
+                            reinterpret_cast<const cuComplex *>(f1 + off), (int)n_int, &zero,
+                            reinterpret_cast<cuComplex *>(f2 + off), (int)n_int) != CUBLAS_STATUS_SUCCESS)
+                return cudaErrorUnknown;
+        }
+        return cudaSuccess;
+    }
+    cudaError_t solve(int k, const cd *r, cd *x, cudaStream_t s, bool deferred) override {
+        if (deferred) return cudaErrorNotSupported;
+        cudaError_t e;
+        if ((e = reserve(k, s))) return e;
+        k_rows_gather<<<grid_of(nk * k), 256, 0, s>>>(nk, k, perm, r, rn);
+        k_to_c64_cols<<<grid_of(n_int * k), 256, 0, s>>>(n_int, k, rn, f1);
+        if ((e = domains_apply(k, s))) return e;
+        k_from_c64_cols<<<grid_of(n_int * k), 256, 0, s>>>(n_int, k, f2, yI);
+        k_separator_rhs<<<grid_of(ns * k), 256, 0, s>>>(ns, k, n_int, perm, pos, lap_ptr, lap_branch, lap_other,
+                                                         dinv, rn, yI, rS);
+        if ((e = tri.solve(k, rS, xS, s, false))) return e;
+        k_interior_coupling<<<grid_of(n_int * k), 256, 0, s>>>(n_int, k, perm, pos, lap_ptr, lap_branch, lap_other,
+                                                                dinv, xS, tI);
+        k_to_c64_cols<<<grid_of(n_int * k), 256, 0, s>>>(n_int, k, tI, f1);
+        if ((e = domains_apply(k, s))) return e;
+        k_from_c64_cols_add<<<grid_of(n_int * k), 256, 0, s>>>(n_int, k, f2, yI);
+        k_rows_scatter<<<grid_of(n_int * k), 256, 0, s>>>(n_int, k, perm, yI, x);
+        k_rows_scatter<<<grid_of(ns * k), 256, 0, s>>>(ns, k, perm + n_int, xS, x);
+        note_launches(10 + 2 * (int)parts);
+        return cudaGetLastError();
+    }
+};
+
 struct GraphPrecond : Preconditioner {
     int64_t n = 0, nkeep = 0, ncomp = 0, nbranch = 0;
     Csr ac, tinv, tinvt, K;
@@ -1313,10 +1568,8 @@ struct GraphPrecond : Preconditioner {
     const int8_t *is_tree = nullptr;
     cd *zdiag = nullptr, *dinv = nullptr, *pinv = nullptr, *rtotal = nullptr;   // owned (rtotal = 1 / total)
     double zs = 1, ps = 1;
-    bool refine = false;
-    float2 *G = nullptr;     // the Laplacian's complex64 LU
-    int *ipiv = nullptr;
-    TriSolver tri;
+    int refine = 0;          // FP64 residual corrections of each Laplacian solve
+    LapSolver *lap = nullptr;
     int cap = 0, deferred_k = 0;
     cd *rhs = nullptr, *v = nullptr, *corr = nullptr, *rt = nullptr, *v2 = nullptr, *m = nullptr;
 
@@ -1326,10 +1579,9 @@ struct GraphPrecond : Preconditioner {
         cap = 0;
     }
     ~GraphPrecond() override {
-        tri.release();
+        delete lap;
         free_work();
-        for (void *p : {(void *)zdiag, (void *)dinv, (void *)pinv, (void *)rtotal, (void *)G, (void *)ipiv})
-            dev_free(p);
+        for (void *p : {(void *)zdiag, (void *)dinv, (void *)pinv, (void *)rtotal}) dev_free(p);
     }
     cudaError_t reserve(int k, cudaStream_t s) {
         if (k <= cap) return cudaSuccess;
@@ -1347,12 +1599,12 @@ struct GraphPrecond : Preconditioner {
     cudaError_t run(int k, const cd *in, cd *out, cudaStream_t s, bool deferred) {
         cudaError_t e;
         k_graph_node_rhs<<<grid_of(nkeep * k), 256, 0, s>>>(ac, k, branch, dinv, zs, in, rhs);
-        if ((e = tri.solve(k, rhs, v, s, deferred))) return e;
-        if (refine) {
+        if ((e = lap->solve(k, rhs, v, s, deferred))) return e;
+        for (int it = 0; it < refine; ++it) {
             k_graph_residual<<<grid_of(nkeep * k), 256, 0, s>>>(nkeep, k, lap_ptr, lap_branch, lap_other, dinv, v,
                                                                 rhs, corr);
-            if ((e = tri.solve(k, corr, rhs, s, deferred))) return e;
-            k_graph_add<<<grid_of(nkeep * k), 256, 0, s>>>(nkeep * k, rhs, v);
+            if ((e = lap->solve(k, corr, v2, s, deferred))) return e;
+            k_graph_add<<<grid_of(nkeep * k), 256, 0, s>>>(nkeep * k, v2, v);
             note_launches(2);
         }
         k_graph_loops<<<grid_of(n * k), 256, 0, s>>>(n, k, is_tree, branch, loop_ends, dinv, zs, in, v, out);
@@ -1375,7 +1627,7 @@ struct GraphPrecond : Preconditioner {
         return run(k, in, out, s, true);
     }
     cudaError_t deferred_status(cudaStream_t s) override {
-        return deferred_k ? tri.read_status(deferred_k, s) : cudaSuccess;
+        return deferred_k ? lap->status(deferred_k, s) : cudaSuccess;
     }
 };
 
@@ -1844,8 +2096,180 @@ int pcbqs_gb300_peec_factor(pcbqs_gb300_peec *h, const pcbqs_gb300_csr *krk, int
     return OK;
 }
 
+// The dense Laplacian: assembled from the branches, factored by getrf_blocked (tcgen05 updates).
+static int graph_dense_lap(const pcbqs_gb300_graph *g, const cd *dinv, cudaStream_t st, LapSolver **out) {
+    const int64_t nk = g->nkeep;
+    const size_t nk2 = (size_t)nk * nk;
+    auto *lap = new (std::nothrow) DenseLap();
+    if (!lap) return pfail(ERR_MEMORY, "peec_graph: host allocation");
+    cudaError_t e;
+    if ((e = dev_alloc(&lap->ipiv, nk, st)) || (e = dev_alloc(&lap->G, nk2, st))) {
+        delete lap;
+        return pfail(ERR_MEMORY, "peec_graph: the dense Laplacian of %lld nodes (%.1f GB): %s", (long long)nk,
+                     8e-9 * (double)nk2, cudaGetErrorString(e));
+    }
+    cudaMemsetAsync(lap->G, 0, sizeof(float2) * nk2, st);
+    k_graph_laplacian<<<grid_of(nk), 256, 0, st>>>(nk, g->lap_ptr, g->lap_branch, g->lap_other, dinv, lap->G);
+    note_launches(1);
+    int singular = 0;
+    LuUpdateStats stats;
+    e = getrf_blocked(nk, lap->G, lap->ipiv, lu_panel_width(nk, LU_GEMM_TC6), LU_GEMM_TC6, st, &singular, &stats);
+    if (e || singular) {
+        delete lap;
+        return pfail(singular ? ERR_NONFINITE : cuda_status(e), "peec_graph: Laplacian LU failed (zero pivot %d, %s)",
+                     singular, cudaGetErrorString(e));
+    }
+    if ((e = lap->tri.prepare(lap->G, nk, lap->ipiv, st))) {
+        delete lap;
+        return pfail(cuda_status(e), "peec_graph: triangular-solve set-up: %s", cudaGetErrorString(e));
+    }
+    *out = lap;
+    return OK;
+}
+
+// The domain-split Laplacian: each domain's block inverted explicitly, the separator's Schur complement factored.
+static int graph_domain_lap(const pcbqs_gb300_graph *g, const cd *dinv, cudaStream_t st, LapSolver **out) {
+    const pcbqs_gb300_graph_domains *dm = g->domains;
+    const int64_t nk = g->nkeep, parts = dm->parts, n_int = dm->n_int, ns = nk - n_int;
+    if (parts < 1 || n_int < 0 || ns < 1 || !dm->dom_ptr || !dm->bnd_ptr || !dm->perm || !dm->pos || !dm->bnd ||
+        !dm->bnd_nptr || !dm->bnd_local || !dm->bnd_branch || dm->dom_ptr[0] != 0 || dm->dom_ptr[parts] != n_int ||
+        dm->bnd_ptr[0] != 0)
+        return pfail(ERR_ARGUMENT, "peec_graph: domain split (%lld parts, %lld interior of %lld kept rows)",
+                     (long long)parts, (long long)n_int, (long long)nk);
+    auto *lap = new (std::nothrow) DomainLap();
+    if (!lap) return pfail(ERR_MEMORY, "peec_graph: host allocation");
+    lap->nk = nk;
+    lap->n_int = n_int;
+    lap->ns = ns;
+    lap->parts = parts;
+    lap->dom_ptr.assign(dm->dom_ptr, dm->dom_ptr + parts + 1);
+    lap->bnd_ptr.assign(dm->bnd_ptr, dm->bnd_ptr + parts + 1);
+    lap->perm = dm->perm;
+    lap->pos = dm->pos;
+    lap->lap_ptr = g->lap_ptr;
+    lap->lap_branch = g->lap_branch;
+    lap->lap_other = g->lap_other;
+    lap->dinv = dinv;
+    int64_t total = 0, nmax = 0;
+    for (int64_t d = 0; d < parts; ++d) {
+        const int64_t nd = lap->dom_ptr[d + 1] - lap->dom_ptr[d];
+        if (nd < 0 || lap->bnd_ptr[d + 1] < lap->bnd_ptr[d]) {
+            delete lap;
+            return pfail(ERR_ARGUMENT, "peec_graph: domain %lld's offsets", (long long)d);
+        }
+        lap->blk_off.push_back(total);
+        total += nd * nd;
+        nmax = std::max(nmax, nd);
+    }
+    if (nmax > 65536) {
+        delete lap;
+        return pfail(ERR_ARGUMENT, "peec_graph: a domain of %lld rows (at most 65,536)", (long long)nmax);
+    }
+    cusolverDnHandle_t solver = nullptr;
+    float2 *scratch = nullptr, *ws = nullptr;
+    int *dpiv = nullptr, *info = nullptr;
+    auto cleanup = [&]() {
+        dev_free(scratch, st);
+        dev_free(ws, st);
+        dev_free(dpiv, st);
+        dev_free(info, st);
+        if (solver) cusolverDnDestroy(solver);
+    };
+    cudaError_t e;
+    int lwork = 0;
+    if (cublasCreate(&lap->blas) != CUBLAS_STATUS_SUCCESS || cusolverDnCreate(&solver) != CUSOLVER_STATUS_SUCCESS) {
+        cleanup();
+        delete lap;
+        return pfail(ERR_CUDA, "peec_graph: cuBLAS / cuSOLVER handle");
+    }
+    cusolverDnSetStream(solver, st);
+    if ((e = dev_alloc(&lap->Ainv, (size_t)std::max<int64_t>(total, 1), st)) ||
+        (e = dev_alloc(&lap->S, (size_t)ns * ns, st)) || (e = dev_alloc(&lap->ipiv, ns, st)) ||
+        (e = dev_alloc(&scratch, (size_t)std::max<int64_t>(nmax * nmax, 1), st)) ||
+        (e = dev_alloc(&dpiv, std::max<int64_t>(nmax, 1), st)) || (e = dev_alloc(&info, 2 * parts, st))) {
+        cleanup();
+        delete lap;
+        return pfail(ERR_MEMORY, "peec_graph: domain inverses (%.2f GB) and Schur complement (%.2f GB): %s",
+                     8e-9 * (double)total, 8e-9 * (double)ns * (double)ns, cudaGetErrorString(e));
+    }
+    if (nmax > 0 && cusolverDnCgetrf_bufferSize(solver, (int)nmax, (int)nmax, reinterpret_cast<cuComplex *>(scratch),
+                                                (int)nmax, &lwork) != CUSOLVER_STATUS_SUCCESS) {
+        cleanup();
+        delete lap;
+        return pfail(ERR_CUDA, "peec_graph: workspace query");
+    }
+    if ((e = dev_alloc(&ws, (size_t)std::max(lwork, 1), st))) {
+        cleanup();
+        delete lap;
+        return pfail(ERR_MEMORY, "peec_graph: workspace");
+    }
+    cudaMemsetAsync(info, 0, sizeof(int) * 2 * parts, st);      // getrf's status per domain, then getrs's
+    for (int64_t d = 0; d < parts; ++d) {
+        const int64_t off = lap->dom_ptr[d], nd = lap->dom_ptr[d + 1] - off;
+        if (!nd) continue;
+        float2 *inv = lap->Ainv + lap->blk_off[d];
+        cudaMemsetAsync(scratch, 0, sizeof(float2) * nd * nd, st);
+        k_domain_block<<<grid_of(nd), 256, 0, st>>>(off, nd, lap->perm, lap->pos, g->lap_ptr, g->lap_branch,
+                                                     g->lap_other, dinv, scratch);
+        k_identity_c64<<<grid_of(nd * nd), 256, 0, st>>>(nd, inv);
+        note_launches(2);
+        if (cusolverDnCgetrf(solver, (int)nd, (int)nd, reinterpret_cast<cuComplex *>(scratch), (int)nd,
+                             reinterpret_cast<cuComplex *>(ws), dpiv, info + d) != CUSOLVER_STATUS_SUCCESS ||
+            cusolverDnCgetrs(solver, CUBLAS_OP_N, (int)nd, (int)nd, reinterpret_cast<const cuComplex *>(scratch),
+                             (int)nd, dpiv, reinterpret_cast<cuComplex *>(inv), (int)nd,
+                             info + parts + d) != CUSOLVER_STATUS_SUCCESS) {
+            cleanup();
+            delete lap;
+            return pfail(ERR_CUDA, "peec_graph: domain %lld's LU", (long long)d);
+        }
+    }
+    std::vector<int> infos((size_t)(2 * parts));
+    cudaMemcpyAsync(infos.data(), info, sizeof(int) * 2 * parts, cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st))) {
+        cleanup();
+        delete lap;
+        return pfail(cuda_status(e), "peec_graph: domain inverses: %s", cudaGetErrorString(e));
+    }
+    for (int64_t d = 0; d < 2 * parts; ++d)
+        if (infos[d]) {
+            cleanup();
+            delete lap;
+            return pfail(ERR_NONFINITE, "peec_graph: domain %lld's block: %s info %d", (long long)(d % parts),
+                         d < parts ? "getrf" : "getrs", infos[d]);
+        }
+    // the Schur complement: G_SS, then each domain's term in turn (a fixed order)
+    cudaMemsetAsync(lap->S, 0, sizeof(float2) * ns * ns, st);
+    k_separator_block<<<grid_of(ns), 256, 0, st>>>(ns, n_int, lap->perm, lap->pos, g->lap_ptr, g->lap_branch,
+                                                    g->lap_other, dinv, lap->S);
+    note_launches(1);
+    for (int64_t d = 0; d < parts; ++d) {
+        const int64_t b0 = lap->bnd_ptr[d], mcount = lap->bnd_ptr[d + 1] - b0;
+        const int64_t nd = lap->dom_ptr[d + 1] - lap->dom_ptr[d];
+        if (!mcount || !nd) continue;
+        k_schur_domain<<<grid_of(mcount * mcount), 256, 0, st>>>(mcount, dm->bnd + b0, dm->bnd_nptr + b0,
+                                                                  dm->bnd_local, dm->bnd_branch, dinv,
+                                                                  lap->Ainv + lap->blk_off[d], nd, lap->S, ns);
+        note_launches(1);
+    }
+    int singular = 0;
+    LuUpdateStats stats;
+    e = getrf_blocked(ns, lap->S, lap->ipiv, lu_panel_width(ns, LU_GEMM_TC6), LU_GEMM_TC6, st, &singular, &stats);
+    cleanup();
+    if (e || singular) {
+        delete lap;
+        return pfail(singular ? ERR_NONFINITE : cuda_status(e), "peec_graph: Schur LU failed (zero pivot %d, %s)",
+                     singular, cudaGetErrorString(e));
+    }
+    if ((e = lap->tri.prepare(lap->S, ns, lap->ipiv, st))) {
+        delete lap;
+        return pfail(cuda_status(e), "peec_graph: triangular-solve set-up: %s", cudaGetErrorString(e));
+    }
+    *out = lap;
+    return OK;
+}
+
 int pcbqs_gb300_peec_graph(pcbqs_gb300_peec *h, const pcbqs_gb300_graph *g, int32_t sys, int refine, void *stream) {
-    if (!h || !g || sys < 0 || sys >= h->op.nsys || (refine != 0 && refine != 1))
+    if (!h || !g || sys < 0 || sys >= h->op.nsys || refine < 0 || refine > 3)
         return pfail(ERR_ARGUMENT, "peec_graph: invalid argument");
     PeecOp &op = h->op;
     const int64_t n = op.n_, nk = g->nkeep;
@@ -1879,21 +2303,14 @@ int pcbqs_gb300_peec_graph(pcbqs_gb300_peec *h, const pcbqs_gb300_graph *g, int3
     gp->member_ptr = g->member_ptr;
     gp->members = g->members;
     gp->is_tree = op.is_tree;
-    gp->refine = refine != 0;
+    gp->refine = refine;
     gp->ps = op.pscale;
     cudaMemcpy(&gp->zs, op.zscale + sys, sizeof(double), cudaMemcpyDeviceToHost);
     cudaError_t e;
-    const size_t nk2 = (size_t)nk * nk;
     if ((e = dev_alloc(&gp->zdiag, g->nbranch, st)) || (e = dev_alloc(&gp->dinv, g->nbranch, st)) ||
-        (e = dev_alloc(&gp->pinv, nk, st)) || (e = dev_alloc(&gp->rtotal, g->ncomp, st)) ||
-        (e = dev_alloc(&gp->ipiv, nk, st))) {
+        (e = dev_alloc(&gp->pinv, nk, st)) || (e = dev_alloc(&gp->rtotal, g->ncomp, st))) {
         delete gp;
         return pfail(ERR_MEMORY, "peec_graph: %s", cudaGetErrorString(e));
-    }
-    if ((e = dev_alloc(&gp->G, nk2, st))) {
-        delete gp;
-        return pfail(ERR_MEMORY, "peec_graph: the dense Laplacian of %lld nodes (%.1f GB): %s", (long long)nk,
-                     8e-9 * (double)nk2, cudaGetErrorString(e));
     }
     cudaMemcpyAsync(gp->zdiag, g->zdiag, sizeof(cd) * g->nbranch, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(gp->dinv, g->dinv, sizeof(cd) * g->nbranch, cudaMemcpyDeviceToDevice, st);
@@ -1914,20 +2331,11 @@ int pcbqs_gb300_peec_graph(pcbqs_gb300_peec *h, const pcbqs_gb300_graph *g, int3
         t = make_double2(t.x / a, -t.y / a);
     }
     cudaMemcpyAsync(gp->rtotal, tot.data(), sizeof(cd) * g->ncomp, cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(gp->G, 0, sizeof(float2) * nk2, st);
-    k_graph_laplacian<<<grid_of(nk), 256, 0, st>>>(nk, g->lap_ptr, g->lap_branch, g->lap_other, gp->dinv, gp->G);
-    note_launches(1);
-    int singular = 0;
-    LuUpdateStats stats;
-    e = getrf_blocked(nk, gp->G, gp->ipiv, lu_panel_width(nk, LU_GEMM_TC6), LU_GEMM_TC6, st, &singular, &stats);
-    if (e || singular) {
+    const int status = g->domains ? graph_domain_lap(g, gp->dinv, st, &gp->lap) : graph_dense_lap(g, gp->dinv, st,
+                                                                                                  &gp->lap);
+    if (status != OK) {
         delete gp;
-        return pfail(singular ? ERR_NONFINITE : cuda_status(e), "peec_graph: Laplacian LU failed (zero pivot %d, %s)",
-                     singular, cudaGetErrorString(e));
-    }
-    if ((e = gp->tri.prepare(gp->G, nk, gp->ipiv, st))) {
-        delete gp;
-        return pfail(cuda_status(e), "peec_graph: triangular-solve set-up: %s", cudaGetErrorString(e));
+        return status;
     }
     delete h->graph;
     h->graph = gp;

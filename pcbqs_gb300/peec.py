@@ -262,8 +262,9 @@ class PeecTopology:
         """The frequency-independent arrays of the graph preconditioner (src/pcbqs/peec_iterative.py:44-84, boards
         without face-sheet pairs), indexed by the clustered unknowns, made once per topology (host arrays):
 
-        keep_row (nn): each node's row among the kept nodes, -1 at each component's root (the lowest-numbered node,
-        whose equation T[keep] drops, peec_iterative.py:150); ac (nkeep x n): each loop's defining (cotree) branch's
+        kept (nn) / keep_row (nn): each node's row among the kept nodes, -1 at each component's grounded node (whose
+        equation T[keep] drops; the reference drops the lowest-numbered node, peec_iterative.py:150, here the tree's
+        centre, see below); ac (nkeep x n): each loop's defining (cotree) branch's
         incidence, +1 at its first end and -1 at its second (Ap on the loops' trial currents); lap_ptr / lap_branch /
         lap_other: each kept node's passive branches and their other ends' rows (-1 at a root), the graph Laplacian
         Ap Dinv Ap^T [keep][:, keep] by its edges; tinv (n x nkeep, rows of the tree unknowns) = T[keep]^-1 and tinvt
@@ -279,7 +280,21 @@ class PeecTopology:
         from scipy.sparse.csgraph import breadth_first_order
         nn, n, ni = self.nn, self.n, self.ni
         ea, eb = self.ends[:, 0], self.ends[:, 1]
-        keep = self.keep
+        tb = np.flatnonzero(self.tree)
+        adj = csr_matrix((np.r_[tb, tb] + 1.0, (np.r_[ea[tb], eb[tb]], np.r_[eb[tb], ea[tb]])), shape=(nn, nn))
+        # The grounded node of each component: the preconditioner's output does not depend on it (a constant added
+        # to the node potentials cancels in the branch drops and in the charges, whose sum over a component is
+        # zero, so the dropped node's equation holds by itself), so each tree is rooted at its centre, the middle
+        # of a longest path (two breadth-first sweeps), rather than at the reference's lowest-numbered node: half
+        # the depth, half the entries of T[keep]^-1.
+        keep = np.ones(nn, bool)
+        for first in np.unique(self.labels, return_index=True)[1]:
+            reached = breadth_first_order(adj, int(first), directed=False, return_predecessors=False)
+            far, pred = breadth_first_order(adj, int(reached[-1]), directed=False, return_predecessors=True)
+            path = [int(far[-1])]
+            while pred[path[-1]] >= 0:
+                path.append(int(pred[path[-1]]))
+            keep[path[len(path) // 2]] = False
         nkeep = int(keep.sum())
         kidx = np.full(nn, -1, np.int64)
         kidx[keep] = np.arange(nkeep)
@@ -308,8 +323,6 @@ class PeecTopology:
         r, br, oth = r[o], br[o], oth[o]
         lap_ptr = np.r_[0, np.cumsum(np.bincount(r, minlength=nkeep))].astype(np.int64)
         # the spanning forest rooted at the dropped nodes: each node's parent and the branch to it
-        tb = np.flatnonzero(self.tree)
-        adj = csr_matrix((np.r_[tb, tb] + 1.0, (np.r_[ea[tb], eb[tb]], np.r_[eb[tb], ea[tb]])), shape=(nn, nn))
         parent = np.full(nn, -1, np.int64)
         for root in np.flatnonzero(~keep):
             reached, pred = breadth_first_order(adj, int(root), directed=False, return_predecessors=True)
@@ -338,12 +351,78 @@ class PeecTopology:
         nc = int(self.B.shape[1])
         members = np.argsort(comp, kind='stable').astype(np.int32)
         member_ptr = np.r_[0, np.cumsum(np.bincount(comp, minlength=nc))].astype(np.int64)
-        g = dict(nkeep=nkeep, ncomp=nc, keep_row=kidx, ac=_host_csr(ac), lap_ptr=lap_ptr,
+        g = dict(nkeep=nkeep, ncomp=nc, kept=keep, keep_row=kidx, ac=_host_csr(ac), lap_ptr=lap_ptr,
                  lap_branch=br.astype(np.int32), lap_other=oth.astype(np.int32), tinv=_host_csr(tinv),
                  tinvt=_host_csr(tinv.T), branch=branch.astype(np.int32), loop_ends=loop_ends, comp=comp,
                  member_ptr=member_ptr, members=members)
         self._graph = g
         return g
+
+    def graph_domains(self, parts):
+        """A nested-dissection-style split of the graph Laplacian's kept nodes for boards whose Laplacian is too large
+        to factor dense (made once per topology and part count; host arrays): the nodes (triangle centroids, averaged
+        over merged triangles) are cut by recursive coordinate bisection in the board's plane into `parts` (a power of
+        two) parts; the node of each Laplacian edge between two parts that lies in the higher-numbered part joins the
+        separator, so no edge joins two parts' interiors. New order: the parts' interiors one after another
+        (dom_ptr), then the separator; perm[p] the kept row at new position p, pos its inverse. For the Schur
+        complement, each part's boundary (the separator nodes next to its interior, bnd_ptr / bnd as separator
+        positions) with each boundary node's interior neighbours (bnd_nptr / bnd_local / bnd_branch: local row in the
+        part, and the branch)."""
+        cache = self.__dict__.setdefault('_graph_domain_cache', {})
+        if parts in cache:
+            return cache[parts]
+        if parts < 2 or parts & (parts - 1):
+            raise ValueError('graph domains: the part count must be a power of two >= 2')
+        g = self.graph_structure()
+        nk = g['nkeep']
+        b = self.board
+        nn = self.nn
+        cent = np.asarray(b.nodes)[np.asarray(b.tris)].mean(axis=1)
+        node_of = np.asarray(b.node_of)
+        cnt = np.maximum(np.bincount(node_of, minlength=nn), 1)
+        xy = np.c_[np.bincount(node_of, cent[:, 0], minlength=nn), np.bincount(node_of, cent[:, 1], minlength=nn)]
+        xy = (xy / cnt[:, None])[np.flatnonzero(g['kept'])]
+        part = np.zeros(nk, np.int64)
+        groups = [np.arange(nk)]
+        while len(groups) < parts:
+            nxt = []
+            for idx in groups:
+                ext = xy[idx].max(axis=0) - xy[idx].min(axis=0) if len(idx) else np.zeros(2)
+                o = idx[np.argsort(xy[idx, int(np.argmax(ext))], kind='stable')]
+                nxt += [o[:len(o) // 2], o[len(o) // 2:]]
+            groups = nxt
+        for d, idx in enumerate(groups):
+            part[idx] = d
+        rows = np.repeat(np.arange(nk), np.diff(g['lap_ptr']))
+        oth = g['lap_other'].astype(np.int64)
+        cut = (oth >= 0) & (part[rows] != part[np.maximum(oth, 0)])
+        sep = np.zeros(nk, bool)
+        r, o = rows[cut], oth[cut]
+        sep[np.where(part[r] > part[o], r, o)] = True
+        interior = [np.sort(idx[~sep[idx]]) for idx in groups]
+        perm = np.concatenate(interior + [np.flatnonzero(sep)]).astype(np.int64)
+        pos = np.empty(nk, np.int64)
+        pos[perm] = np.arange(nk)
+        dom_ptr = np.r_[0, np.cumsum([len(i) for i in interior])].astype(np.int64)
+        n_int = int(dom_ptr[-1])
+        # each part's boundary: interior row r of part d next to separator node s, through branch br
+        m = (oth >= 0) & ~sep[rows] & sep[np.maximum(oth, 0)]
+        r, s_, br = rows[m], oth[m], g['lap_branch'][m]
+        d = part[r]
+        sl = pos[s_] - n_int
+        il = pos[r] - dom_ptr[d]
+        o = np.lexsort((il, sl, d))
+        d, sl, il, br = d[o], sl[o], il[o], br[o]
+        first = np.r_[True, (d[1:] != d[:-1]) | (sl[1:] != sl[:-1])] if len(d) else np.zeros(0, bool)
+        entry = np.cumsum(first) - 1
+        nent = int(first.sum())
+        bnd = sl[first].astype(np.int32)
+        bnd_ptr = np.r_[0, np.cumsum(np.bincount(d[first], minlength=parts))].astype(np.int64)
+        bnd_nptr = np.r_[0, np.cumsum(np.bincount(entry, minlength=nent))].astype(np.int64)
+        out = dict(parts=parts, perm=perm, pos=pos, dom_ptr=dom_ptr, n_int=n_int, n_sep=nk - n_int, bnd_ptr=bnd_ptr,
+                   bnd=bnd, bnd_nptr=bnd_nptr, bnd_local=il.astype(np.int32), bnd_branch=br.astype(np.int32))
+        cache[parts] = out
+        return out
 
 
 
@@ -776,7 +855,39 @@ class PeecModel(PeecTopology):
             self._graph_dev = gd
         return gd
 
-    def _graph_precondition(self, handle, sys_index, freq, refine, stream):
+    GRAPH_DENSE_BYTES = 16e9     # the graph Laplacian dense up to this size (about 44,700 kept nodes)
+    GRAPH_DOMAIN_ROWS = 1500     # above it, domains of about this many rows
+
+    def _graph_parts(self, parts):
+        """0 (the dense Laplacian) or the domain count: `parts` if given, else by the Laplacian's size."""
+        if parts is not None:
+            if parts != 0 and (parts < 2 or parts & (parts - 1)):
+                raise ValueError('graph_parts must be 0 (dense) or a power of two >= 2')
+            return int(parts)
+        nk = self.graph_structure()['nkeep']
+        if 8.0 * nk * nk <= self.GRAPH_DENSE_BYTES:
+            return 0
+        return 2 ** max(1, int(round(np.log2(nk / self.GRAPH_DOMAIN_ROWS))))
+
+    def _graph_domains_device(self, parts):
+        """The domain split (graph_domains) as its C struct over device arrays, uploaded once per part count."""
+        cache = self.__dict__.setdefault('_graph_dom_dev', {})
+        if parts not in cache:
+            dm = self.graph_domains(parts)
+            up = lambda a: torch.as_tensor(np.ascontiguousarray(a if len(a) else np.zeros(1, a.dtype)),
+                                           device=self.device)
+            arrays = {name: up(dm[name]) for name in ('perm', 'pos', 'bnd', 'bnd_nptr', 'bnd_local', 'bnd_branch')}
+            host = {name: np.ascontiguousarray(dm[name], np.int64) for name in ('dom_ptr', 'bnd_ptr')}
+            desc = _lib.GraphDomainsDesc()
+            desc.parts, desc.n_int = dm['parts'], dm['n_int']
+            for name, t in arrays.items():
+                setattr(desc, name, t.data_ptr())
+            for name, a in host.items():
+                setattr(desc, name, a.ctypes.data)
+            cache[parts] = (desc, arrays, host)
+        return cache[parts][0]
+
+    def _graph_precondition(self, handle, sys_index, freq, refine, stream, parts=0):
         """Set up the graph preconditioner of system sys_index (frequency freq) in the live operator: the branches'
         own impedance d = r(f) R_ii + j w L_ii (the via barrels at their DC resistance, as in the operator), 1/d with
         |d| raised to 1e-12 zscale where smaller (peec_iterative.py:52), and 1/P_ii with its per-component sums
@@ -793,7 +904,7 @@ class PeecModel(PeecTopology):
         total = (np.bincount(self.labels, pinv.real, minlength=g['ncomp']) +
                  1j * np.bincount(self.labels, pinv.imag, minlength=g['ncomp']))
         vals = {name: torch.as_tensor(np.ascontiguousarray(a, complex), device=self.device)
-                for name, a in (('zdiag', zdiag), ('dinv', 1 / d), ('pinv', pinv[self.keep]), ('total', total))}
+                for name, a in (('zdiag', zdiag), ('dinv', 1 / d), ('pinv', pinv[g['kept']]), ('total', total))}
         desc = _lib.GraphDesc()
         desc.nkeep, desc.ncomp, desc.nbranch = g['nkeep'], g['ncomp'], self.ni
         for name in ('ac', 'tinv', 'tinvt'):
@@ -802,18 +913,20 @@ class PeecModel(PeecTopology):
             setattr(desc, name, gd[name].data_ptr())
         for name, t in vals.items():
             setattr(desc, name, t.data_ptr())
-        _lib.check(lib.pcbqs_gb300_peec_graph(handle, ctypes.byref(desc), int(sys_index), int(bool(refine)), stream),
-                   lib)
+        desc.domains = ctypes.pointer(self._graph_domains_device(parts)) if parts else None
+        _lib.check(lib.pcbqs_gb300_peec_graph(handle, ctypes.byref(desc), int(sys_index), int(refine), stream), lib)
 
     def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='tc6-blocked', anchors=None,
-              captured=False, product='tc3', fp64_product=None, graph_refine=True):
+              captured=False, product='tc3', fp64_product=None, graph_parts=None, graph_refine=None):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
 
         precondition: 'block_jacobi' (geometric blocks of the loop/tree unknowns), 'lu32' (the complex64 LU of the
         dense loop/tree system), 'graph' (the reference's graph preconditioner, peec_iterative.py:44-84: loop
-        currents from the branches' graph Laplacian, factored dense in complex64 on the device, with one FP64
-        correction of each of its solves unless graph_refine=False; tree charges through the spanning forest's
-        explicit inverse; dense or compressed operator), or 'none'. mixed=False: FP64 GMRES on the FP64 operator;
+        currents from the branches' graph Laplacian, factored on the device in complex64: dense up to about 44,700
+        nodes, else (or graph_parts, a power of two) split into domains with explicit inverses and a dense Schur
+        complement on their separator; graph_refine FP64 corrections of each Laplacian solve (default 1 dense, 2
+        split); tree charges through the spanning forest's explicit inverse; dense or compressed operator), or
+        'none'. mixed=False: FP64 GMRES on the FP64 operator;
         mixed=True: FP64 iterative refinement (true residuals with the FP64 operator) around an inner GMRES whose
         dense products run in single precision, both to the same 1e-8 relative residual. factor_math: arithmetic of the 'lu32'
         factorization: 'fp32' or 'bf16x9' (FP32 emulated on the tensor cores, same accuracy) through cuSOLVER's getrf;
@@ -856,6 +969,12 @@ class PeecModel(PeecTopology):
         if not isinstance(anchors, (int, np.integer)) or not 1 <= anchors <= nf:
             raise ValueError('anchors must be an integer between 1 and the number of frequencies')
         mode = self.PRECONDITIONERS[precondition]
+        parts = self._graph_parts(graph_parts) if mode == 3 else 0
+        refine = (2 if parts else 1) if graph_refine is None else int(graph_refine)
+        if not 0 <= refine <= 3:
+            raise ValueError('graph_refine must lie in 0..3')
+        if parts and captured:
+            raise ValueError('captured GMRES cycles need the dense graph Laplacian (graph_parts=0)')
         t0 = time.perf_counter()
         npo = len(self.names)
         excitation = np.eye(npo, dtype=complex)
@@ -973,7 +1092,7 @@ class PeecModel(PeecTopology):
                 if mode == 3:
                     e0, e1 = timed()
                     e0.record()
-                    self._graph_precondition(handle, anchor, f[anchor], graph_refine, stream)
+                    self._graph_precondition(handle, anchor, f[anchor], refine, stream, parts)
                     e1.record()
                     torch.cuda.synchronize()
                     precondition_ms += e0.elapsed_time(e1)

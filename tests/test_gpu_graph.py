@@ -10,14 +10,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _apply_on_device(model, freq, refine, y):
+def _apply_on_device(model, freq, refine, y, parts=0):
     import torch
     from pcbqs_gb300 import _lib
     lib = _lib.load()
     handle, zscale = model._operator(np.array([2 * np.pi * freq]))
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     try:
-        model._graph_precondition(handle, 0, freq, refine, stream)
+        model._graph_precondition(handle, 0, freq, refine, stream, parts)
         x = torch.as_tensor(np.ascontiguousarray(y), device='cuda')
         out = torch.empty_like(x)
         _lib.check(lib.pcbqs_gb300_peec_graph_apply(handle, y.shape[1], x.data_ptr(), out.data_ptr(), stream), lib)
@@ -26,10 +26,12 @@ def _apply_on_device(model, freq, refine, y):
         lib.pcbqs_gb300_peec_destroy(handle)
 
 
-@pytest.mark.parametrize('board', ['tiny', 'strip', 'viapair'])
-def test_graph_preconditioner_matches_oracle(device_library, board):
+@pytest.mark.parametrize('board,parts', [('tiny', 0), ('strip', 0), ('viapair', 0), ('tiny', 4), ('strip', 8)])
+def test_graph_preconditioner_matches_oracle(device_library, board, parts):
     """Three random columns through the device preconditioner and through the restatement, at 1 MHz: within 1e-5
-    of the largest output with the FP64 correction of the Laplacian solves (their complex64 factor alone: 1e-2)."""
+    of the largest output with FP64 corrections of the Laplacian solves (one for the dense Laplacian, two for the
+    domain split), within 1e-2 without (the complex64 factors alone). parts > 0: the Laplacian split into domains
+    (explicit block inverses, Schur complement on the separator)."""
     import oracle.graph as G
     from pcbqs_gb300.board import Board
     from pcbqs_gb300.peec import PeecModel
@@ -38,8 +40,8 @@ def test_graph_preconditioner_matches_oracle(device_library, board):
     rng = np.random.default_rng(3)
     y = rng.standard_normal((model.n, 3)) + 1j * rng.standard_normal((model.n, 3))
     errs = []
-    for refine, bound in ((1, 1e-5), (0, 1e-2)):
-        got, zs = _apply_on_device(model, freq, refine, y)
+    for refine, bound in ((2 if parts else 1, 1e-5), (0, 1e-2)):
+        got, zs = _apply_on_device(model, freq, refine, y, parts)
         diagonal = np.zeros(model.nb, complex)
         rd = np.asarray(model.R.diagonal(), complex)
         rd[:model.ne] *= model.resistance_ratio([freq])[0]
@@ -53,12 +55,12 @@ def test_graph_preconditioner_matches_oracle(device_library, board):
             err = np.abs(got[:, c] - ref).max() / np.abs(ref).max()
             errs.append(err)
             assert err < bound, (refine, err)
-    print(f'{board}: device graph preconditioner against the restatement: {max(errs[:3]):.2e} (FP64 correction), '
-          f'{max(errs[3:]):.2e} (complex64 factor alone)')
+    print(f'{board} (parts {parts}): device graph preconditioner against the restatement: {max(errs[:3]):.2e} '
+          f'(FP64 corrections), {max(errs[3:]):.2e} (complex64 factors alone)')
 
 
-@pytest.mark.parametrize('board', ['tiny', 'strip', 'viapair'])
-def test_graph_gmres_matches_reference_iterative_solve(device_library, board):
+@pytest.mark.parametrize('board,parts', [('tiny', 0), ('strip', 0), ('viapair', 0), ('strip', 8)])
+def test_graph_gmres_matches_reference_iterative_solve(device_library, board, parts):
     """GMRES to 1e-8 with the device graph preconditioner against the reference's GMRES with its own: the port
     impedances within 1e-5 (the reference's solve is on its compressed operator) and about the reference's step
     counts (at most 1.5 times + 5); the captured restart cycles (the preconditioner inside the CUDA graph) reach
@@ -69,14 +71,18 @@ def test_graph_gmres_matches_reference_iterative_solve(device_library, board):
     with np.load(GOLDEN / f'graph_{board}.npz') as g:
         freqs, its_ref, Zg = g['freqs'], g['iterations'], g['Z']
     model = PeecModel(Board.load(board))
-    res = model.solve(freqs, precondition='graph')
+    res = model.solve(freqs, precondition='graph', graph_parts=parts)
     its = res.iterations.reshape(len(freqs), -1)
     err = np.abs(res.impedance - Zg).max() / np.abs(Zg).max()
-    print(f'{board} graph: GMRES steps {its.max(axis=1).tolist()} (reference {its_ref.max(axis=1).tolist()}), '
+    print(f'{board} graph (parts {parts}): GMRES steps {its.max(axis=1).tolist()} (reference {its_ref.max(axis=1).tolist()}), '
           f'port Z against the reference iterative solve {err:.2e}, set-up {model.timings["precondition_ms"]:.1f} ms')
     assert (res.residual <= 1e-8).all()
     assert err < 1e-5, err
     assert (its.max(axis=1) <= 1.5 * its_ref.max(axis=1) + 5).all()
+    if parts:
+        with pytest.raises(ValueError, match='captured'):
+            model.solve(freqs, precondition='graph', graph_parts=parts, captured=True)
+        return
     cap = model.solve(freqs, precondition='graph', captured=True)
     assert (cap.residual <= 1e-8).all()
     assert np.abs(cap.impedance - res.impedance).max() <= 1e-9 * np.abs(res.impedance).max()
@@ -85,7 +91,8 @@ def test_graph_gmres_matches_reference_iterative_solve(device_library, board):
 def test_graph_preconditions_the_compressed_plane_pair(device_library):
     """The 22,554-triangle plane pair with the compressed operator (H-matrices at their default tolerance 1e-6),
     which block-Jacobi does not bring to 1e-8 within 2,000 steps: the graph preconditioner does, for the FP64 GMRES
-    and for the mixed solve (BF16 low-rank inner products), and the port impedances agree with the reference's dense
+    and for the mixed solve (BF16 low-rank inner products), with the dense Laplacian and split into 16 domains, and
+    the port impedances agree with the reference's dense
     solve (tests/golden/peec_planes.npz) within 1e-4 of the largest."""
     from conftest import GOLDEN
     from pcbqs_gb300.board import Board
@@ -93,11 +100,11 @@ def test_graph_preconditions_the_compressed_plane_pair(device_library):
     with np.load(GOLDEN / 'peec_planes.npz') as g:
         f, Zr = float(g['freqs'][0]), g['Z'][0]
     model = PeecModel(Board.load('planes'), matrix='hierarchical').assemble()
-    for mixed in (False, True):
-        res = model.solve([f], precondition='graph', mixed=mixed)
+    for mixed, parts in ((False, 0), (True, 0), (True, 16)):
+        res = model.solve([f], precondition='graph', mixed=mixed, graph_parts=parts)
         err = np.abs(res.impedance[0] - Zr).max() / np.abs(Zr).max()
         t = model.timings
-        print(f'planes compressed, graph, mixed={mixed}: GMRES steps {res.iterations.max()}, port Z error {err:.2e}, '
+        print(f'planes compressed, graph (parts {parts}), mixed={mixed}: GMRES steps {res.iterations.max()}, port Z error {err:.2e}, '
               f'preconditioner {t["precondition_ms"]:.0f} ms, GMRES {t["gmres_ms"]:.0f} ms')
         assert (res.residual <= 1e-8).all()
         assert err < 1e-4, err

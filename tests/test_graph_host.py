@@ -71,7 +71,7 @@ def test_graph_structure_replays_the_reference_preconditioner(board):
     for _ in range(2):
         y = rng.standard_normal(t.n) + 1j * rng.standard_normal(t.n)
         ref = apply(y)
-        got = _kernel_steps(t, g, diagonal[:ni], 1 / d, zs, ps, pinv[t.keep], total, y[t.order])
+        got = _kernel_steps(t, g, diagonal[:ni], 1 / d, zs, ps, pinv[g['kept']], total, y[t.order])
         assert np.abs(got - ref[t.order]).max() <= 1e-11 * np.abs(ref).max()
 
 
@@ -80,10 +80,62 @@ def test_explicit_tree_inverse_is_the_inverse(board):
     t = _topology(board)
     g = t.graph_structure()
     is_tree = t.is_tree.astype(bool)
-    Tk = t.Tp.tocsr()[t.keep][:, np.flatnonzero(is_tree)]          # kept nodes x tree unknowns (clustered)
+    Tk = t.Tp.tocsr()[g['kept']][:, np.flatnonzero(is_tree)]       # kept nodes x tree unknowns (clustered)
     tinv = _csr(g['tinv'])[np.flatnonzero(is_tree)]
     eye = (tinv @ Tk).toarray()
     assert np.array_equal(eye, np.eye(g['nkeep']))
     assert np.array_equal(_csr(g['tinvt']).toarray()[:, is_tree], tinv.T.toarray())
     assert g['member_ptr'][-1] == g['nkeep'] and len(g['comp']) == g['nkeep']
     assert (g['keep_row'] >= 0).sum() == g['nkeep']
+
+
+@pytest.mark.parametrize('board,parts', [('tiny', 4), ('strip', 8), ('viapair', 4)])
+def test_domain_split_solves_the_laplacian(board, parts):
+    """PeecTopology.graph_domains: no Laplacian edge joins two domains' interiors; the Schur complement built from
+    the boundary lists as k_schur_domain builds it equals G_SS - G_SI A_I^-1 G_IS; and the two-stage solve
+    (y_I = A_I^-1 r_I, x_S = S^-1 (r_S - G_SI y_I), x_I = y_I - A_I^-1 G_IS x_S) is G^-1 r."""
+    t = _topology(board)
+    g = t.graph_structure()
+    dm = t.graph_domains(parts)
+    nk, ni_, ns = g['nkeep'], dm['n_int'], dm['n_sep']
+    rng = np.random.default_rng(5)
+    dinv = rng.uniform(0.5, 2, t.ni) + 1j * rng.uniform(-3, -0.1, t.ni)
+    rows = np.repeat(np.arange(nk), np.diff(g['lap_ptr']))
+    w = dinv[g['lap_branch']]
+    G = csr_matrix((w, (rows, rows)), shape=(nk, nk)).toarray()
+    m = g['lap_other'] >= 0
+    G -= csr_matrix((w[m], (rows[m], g['lap_other'][m])), shape=(nk, nk)).toarray()
+    perm, dp = dm['perm'], dm['dom_ptr']
+    Gn = G[perm][:, perm]
+    part_of = np.full(nk, parts)
+    for d in range(parts):
+        part_of[dp[d]:dp[d + 1]] = d
+    inner = np.nonzero(Gn[:ni_, :ni_])
+    assert (part_of[inner[0]] == part_of[inner[1]]).all()
+    inv = [np.linalg.inv(Gn[dp[d]:dp[d + 1], dp[d]:dp[d + 1]]) for d in range(parts)]
+    S = Gn[ni_:, ni_:].copy()
+    bp, bn = dm['bnd_ptr'], dm['bnd_nptr']
+    for d in range(parts):
+        for p in range(bp[d], bp[d + 1]):
+            for q in range(bp[d], bp[d + 1]):
+                val = 0
+                for a in range(bn[p], bn[p + 1]):
+                    for b_ in range(bn[q], bn[q + 1]):
+                        val += dinv[dm['bnd_branch'][a]] * inv[d][dm['bnd_local'][a], dm['bnd_local'][b_]] * \
+                            dinv[dm['bnd_branch'][b_]]
+                S[dm['bnd'][p], dm['bnd'][q]] -= val
+    AI = np.zeros((ni_, ni_), complex)
+    for d in range(parts):
+        AI[dp[d]:dp[d + 1], dp[d]:dp[d + 1]] = inv[d]
+    Sref = Gn[ni_:, ni_:] - Gn[ni_:, :ni_] @ AI @ Gn[:ni_, ni_:]
+    assert np.abs(S - Sref).max() <= 1e-12 * np.abs(Sref).max()
+    r = rng.standard_normal((nk, 2)) + 1j * rng.standard_normal((nk, 2))
+    rn = r[perm]
+    yI = AI @ rn[:ni_]
+    xS = np.linalg.solve(S, rn[ni_:] - Gn[ni_:, :ni_] @ yI)
+    xI = yI - AI @ (Gn[:ni_, ni_:] @ xS)
+    x = np.empty_like(r)
+    x[perm] = np.r_[xI, xS]
+    ref = np.linalg.solve(G, r)
+    assert np.abs(x - ref).max() <= 1e-9 * np.abs(ref).max()
+    assert ns == nk - ni_ and ns > 0
