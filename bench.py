@@ -646,6 +646,7 @@ def case_c5solve(freq=1e6, mixed=1, parts=0):
     preconditioned by the graph preconditioner with its Laplacian split into domains (parts 0: by its size), the
     FP64 GMRES (mixed=0) or FP64 refinement around inner GMRES on BF16 products (mixed=1), to 1e-8. Prints one JSON
     line with the stage times, steps, residuals and the port matrix's diagonal."""
+    import ctypes
     import json as _json
     import torch
     from pcbqs_gb300.board import Board
@@ -663,6 +664,34 @@ def case_c5solve(freq=1e6, mixed=1, parts=0):
     tm = model.timings
     Z = res.impedance[0]
     g = model.graph_structure()
+    # per-application costs at the solve's column count: the FP64 operator, the graph preconditioner, and the BF16
+    # H-matrix products of the inner solves (CUDA events, best of three after a warm-up)
+    from pcbqs_gb300 import _lib
+    lib = _lib.load()
+    k = len(b.ports)
+    nparts = model._graph_parts(parts)
+    handle, _ = model._operator(np.array([2 * np.pi * freq]))
+    gen = torch.Generator(device='cuda').manual_seed(3)
+    rnd = lambda rows: torch.complex(torch.randn(rows, k, device='cuda', generator=gen, dtype=torch.float64),
+                                     torch.randn(rows, k, device='cuda', generator=gen, dtype=torch.float64))
+    per = {}
+    try:
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        model._graph_precondition(handle, 0, freq, 2 if nparts else 1, stream, nparts)
+        X = rnd(model.n)
+        Y = torch.empty_like(X)
+        sysidx = np.zeros(k, np.int32)
+        calls = dict(graph_apply_ms=lambda: _lib.check(lib.pcbqs_gb300_peec_graph_apply(
+                         handle, k, X.data_ptr(), Y.data_ptr(), stream), lib),
+                     fp64_operator_ms=lambda: _lib.check(lib.pcbqs_gb300_peec_apply(
+                         handle, k, _lib.ptr(sysidx, ctypes.c_int32), X.data_ptr(), Y.data_ptr(), stream), lib))
+        Xe, Xt = rnd(model.HL.n), rnd(model.HP.n)
+        calls['bf16_L_ms'] = lambda: model.HL.matmat_lowrank(Xe, dense=True)
+        calls['bf16_P_ms'] = lambda: model.HP.matmat_lowrank(Xt, dense=True)
+        for name, fn in calls.items():
+            per[name] = round(min(_event_ms(fn)[0] for _ in range(3)), 2)
+    finally:
+        lib.pcbqs_gb300_peec_destroy(handle)
     out = dict(case='c5solve', triangles=int(len(b.tris)), unknowns=int(model.n), loops=int(model.nl),
                nodes=int(model.nn), ports=len(b.ports), freq=freq, mixed=mixed,
                graph_parts=int(model._graph_parts(parts)), laplacian_rows=int(g['nkeep']),
@@ -670,6 +699,8 @@ def case_c5solve(freq=1e6, mixed=1, parts=0):
                hmatrix_s=round(tm.get('hmatrix_s', 0.0), 2), host_topology_s=round(tm.get('host_topology_s', 0.0), 2),
                equilibrium_s=round(tm.get('equilibrium_s', 0.0), 2),
                precondition_ms=round(tm['precondition_ms'], 1), gmres_ms=round(tm['gmres_ms'], 1),
+               graph_host_s=round(tm.get('graph_host_s', 0.0), 2), lowrank_plan_s=round(tm.get('lowrank_plan_s', 0.0), 2),
+               rhs_s=round(tm.get('rhs_s', 0.0), 2), post_s=round(tm.get('post_s', 0.0), 2), per_application=per,
                gmres_steps_max=int(res.iterations.max()), outer_steps=tm.get('outer_steps'),
                residual_max=float(res.residual.max()),
                reciprocity=float(np.abs(Z - Z.T).max() / np.abs(Z).max()),

@@ -382,6 +382,14 @@ typedef struct pcbqs_gb300_lowrank {
  * wait gave up. The benchmark spec's BF16 low-rank products; the reference's are FP64 (core/hmatrix_kernels.hpp:20-100). */
 int pcbqs_gb300_hmatrix_apply_lowrank(const pcbqs_gb300_hmat *H, const pcbqs_gb300_lowrank *lr, int k,
                                       const double *x, double *y, void *stream);
+/* The BF16 part planes of pcbqs_gb300_lowrank from the H-matrix's FP64 store (device arrays; no counterpart in the
+ * reference): jobs (njobs x 8 int64: base, si, sj, ni, nj, row0, colbase, map_off) each write the entries
+ * x = store[base + i si + j sj], i < ni, j < nj, split as h = bf16(x), m = bf16(x - h) (x rounded to FP32, every
+ * rounding to nearest even), to plane[(row0 + i) pitch + c] and plane[(row0 + i) pitch + off2 + c],
+ * c = colbase + map[map_off + j] (colbase + j when map_off < 0); the jobs' destinations must not overlap. Ordered
+ * on `stream`. */
+int pcbqs_gb300_pack_bf16_parts(const double *store, const int64_t *jobs, int64_t njobs, const int32_t *map,
+                                void *plane, int64_t pitch, int64_t off2, void *stream);
 /* The compressed operator's single-precision view (the mixed solve's inner products): the H-matrix of L (which 0)
  * or of P (1) applied with its low-rank blocks on the tensor cores as pcbqs_gb300_hmatrix_apply_lowrank; the FP64
  * products (outer residuals) keep FP64 throughout. */

@@ -149,6 +149,8 @@ PROTOTYPES = {
     'pcbqs_gb300_peec_block_jacobi': (ctypes.c_int, [c_void_p, ctypes.c_int32, c_void_p, c_void_p]),
     'pcbqs_gb300_peec_graph': (ctypes.c_int, [c_void_p, ctypes.POINTER(GraphDesc), ctypes.c_int32, ctypes.c_int,
                                               c_void_p]),
+    'pcbqs_gb300_pack_bf16_parts': (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
+                                                   ctypes.c_int64, ctypes.c_int64, c_void_p]),
     'pcbqs_gb300_peec_graph_apply': (ctypes.c_int, [c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p]),
     'pcbqs_gb300_peec_factor': (ctypes.c_int, [c_void_p, ctypes.POINTER(CsrDesc), ctypes.c_int32, ctypes.c_int,
                                                c_void_p]),

@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <cstdint>
 
+#include <cuda_bf16.h>
+
 #include "../../include/pcbqs_gb300.h"
 #include "common.cuh"
 #include "hmatrix.cuh"
@@ -507,6 +509,28 @@ cudaError_t hmatrix_apply(int64_t n, int64_t nb, const int64_t *meta, const int6
     return cudaGetLastError();
 }
 
+// The BF16 part planes of the tensor-core low-rank product, one thread block per job (a block's factor or dense
+// leaf in one direction): job = (base, si, sj, ni, nj, row0, colbase, map_off); for i < ni, j < nj the FP64 entry
+// x = store[base + i si + j sj] is rounded to FP32 and split as h = bf16(x), m = bf16(x - h) (both to nearest
+// even), written to plane[(row0 + i) pitch + c] and plane[(row0 + i) pitch + off2 + c], c = colbase + map[map_off + j]
+// (c = colbase + j when map_off < 0). The jobs' destinations do not overlap.
+__global__ void k_pack_parts(const double *store, const int64_t *jobs, const int32_t *map, __nv_bfloat16 *plane,
+                             int64_t pitch, int64_t off2) {
+    const int64_t *job = jobs + 8 * (int64_t)blockIdx.x;
+    const int64_t base = job[0], si = job[1], sj = job[2], ni = job[3], nj = job[4], row0 = job[5], colbase = job[6],
+                  map_off = job[7];
+    for (int64_t t = threadIdx.x; t < ni * nj; t += blockDim.x) {
+        const int64_t i = t / nj, j = t % nj;
+        const float x = (float)store[base + i * si + j * sj];
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        const __nv_bfloat16 m = __float2bfloat16_rn(x - __bfloat162float(h));
+        const int64_t c = colbase + (map_off < 0 ? j : (int64_t)map[map_off + j]);
+        __nv_bfloat16 *row = plane + (row0 + i) * pitch;
+        row[c] = h;
+        row[off2 + c] = m;
+    }
+}
+
 }  // namespace pq
 
 extern "C" int pcbqs_gb300_hmatrix_apply(int64_t n, int64_t nb, const int64_t *meta, const int64_t *slot0,
@@ -519,4 +543,17 @@ extern "C" int pcbqs_gb300_hmatrix_apply(int64_t n, int64_t nb, const int64_t *m
     const cudaError_t err = pq::hmatrix_apply(n, nb, meta, slot0, idx, store, row_ptr, slots_of_row, max_rank, k, x, y,
                                               slots, static_cast<cudaStream_t>(stream));
     return err ? pq::fail(pq::ERR_CUDA, "hmatrix_apply: %s", cudaGetErrorString(err)) : pq::OK;
+}
+
+extern "C" int pcbqs_gb300_pack_bf16_parts(const double *store, const int64_t *jobs, int64_t njobs,
+                                           const int32_t *map, void *plane, int64_t pitch, int64_t off2,
+                                           void *stream) {
+    if (njobs < 0 || njobs > 0x7fffffff || (njobs && (!store || !jobs || !plane)) || pitch <= 0 || off2 < 0)
+        return pq::fail(pq::ERR_ARGUMENT, "pack_bf16_parts: invalid argument");
+    if (!njobs) return pq::OK;
+    pq::k_pack_parts<<<(unsigned)njobs, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        store, jobs, map, static_cast<__nv_bfloat16 *>(plane), pitch, off2);
+    pq::note_launches(1);
+    const cudaError_t err = cudaGetLastError();
+    return err ? pq::fail(pq::ERR_CUDA, "pack_bf16_parts: %s", cudaGetErrorString(err)) : pq::OK;
 }

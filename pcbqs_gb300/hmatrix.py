@@ -91,6 +91,49 @@ def support_boxes(fill):
     return lo_t[support].min(1), hi_t[support].max(1)
 
 
+def _pack_parts(store, jobs, map_all, plane, off2):
+    """Write the BF16 parts of H-matrix entries into a tensor-core plane (pcbqs_gb300_pack_bf16_parts): each job
+    (base, si, sj, ni, nj, row0, colbase, map_off) takes x = store[base + i si + j sj], i < ni, j < nj, and writes
+    h = bf16(x) and m = bf16(x - h) to plane[row0 + i, c] and plane[row0 + i, off2 + c], c = colbase +
+    map_all[map_off + j] (colbase + j when map_off < 0). Every read and write is checked on the host first."""
+    if not jobs:
+        return
+    J = np.asarray(jobs, np.int64)
+    base, si, sj, ni, nj, row0, colbase, moff = J.T
+    assert (ni >= 0).all() and (nj >= 0).all()
+    mapped = moff >= 0
+    seg = nj - 1                                  # each job's largest column offset
+    if mapped.any():
+        # a list's maps are consecutive runs of map_all (never empty: a cluster has members); each run's maximum
+        # by one reduceat over their span
+        starts, counts = moff[mapped], nj[mapped]
+        assert (counts > 0).all() and (np.diff(starts) == counts[:-1]).all()
+        lo, hi = starts[0], starts[-1] + counts[-1]
+        assert hi <= len(map_all) and map_all[lo:hi].min() >= 0
+        seg[mapped] = np.maximum.reduceat(map_all[lo:hi], starts - lo)
+    live = (ni > 0) & (nj > 0)                    # a rank-0 block's factors write nothing
+    if not live.any():
+        return
+    J, base, si, sj, ni, nj, row0, colbase, seg = (a[live] for a in (J, base, si, sj, ni, nj, row0, colbase, seg))
+    assert base.min() >= 0 and (base + (ni - 1) * si + (nj - 1) * sj).max() < store.numel()
+    assert row0.min() >= 0 and (row0 + ni).max() <= plane.shape[0]
+    assert colbase.min() >= 0 and (colbase + seg + off2).max() < plane.shape[1]
+    assert plane.dtype == torch.bfloat16 and plane.is_contiguous() and store.dtype == torch.float64
+    _pack_launch(store, np.ascontiguousarray(J), map_all, plane, off2)
+
+
+def _pack_launch(store, J, map_all, plane, off2):
+    """The launch of pcbqs_gb300_pack_bf16_parts for jobs checked by _pack_parts."""
+    dev = plane.device
+    jobs_d = torch.as_tensor(J, device=dev)
+    map_d = torch.as_tensor(map_all, device=dev)
+    lib = _lib.load()
+    _lib.check(lib.pcbqs_gb300_pack_bf16_parts(store.data_ptr(), jobs_d.data_ptr(), len(J), map_d.data_ptr(),
+                                               plane.data_ptr(), plane.shape[1], off2,
+                                               ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)), lib)
+    torch.cuda.current_stream(dev).synchronize()
+
+
 class DeviceHMatrix:
     META = 8
 
@@ -308,59 +351,54 @@ class DeviceHMatrix:
         n_pad = off
         span = lambda k: (pstart_of_start[int(tree.start[k])], pend_of_stop[int(tree.stop[k])])
         store = self.store
-        groups, lefts, rights = [], [], []
-        a_row0, b_x0 = 0, 0
+        # pack jobs (base, si, sj, ni, nj, row0, colbase, map_off): entry (i, j) = store[base + i si + j sj]. A block's
+        # U (la x rk) holds U[r, c] = store[so + c la + r], its V (rk x lb) V[c, r] = store[so + la cap + c lb + r];
+        # forward the group's left factor is U and its right V, transposed V^T and U^T.
+        groups, ljobs, rjobs, maps = [], [], [], []
+        a_row0, b_x0, map_n = 0, 0, 0
         for w in low:
             la, lb, so, cap, rk = (int(meta[w, 1]), int(meta[w, 3]), int(meta[w, 4]), int(meta[w, 5]),
                                    int(meta[w, 7]))
             i, j = self._nodes[w]
-            U = store[so:so + la * cap].view(cap, la)[:rk].T          # la x rk
-            V = store[so + la * cap:so + la * cap + cap * lb].view(cap, lb)[:rk]   # rk x lb
-            for L, R, rows_node, cols_node, slot in ((U, V, i, j, slot0[w, 0]), (V.T, U.T, j, i, slot0[w, 1])):
+            for lbase, rows, rbase, ncols, cols_node, slot in ((so, la, so + la * cap, lb, j, slot0[w, 0]),
+                                                               (so + la * cap, lb, so, la, i, slot0[w, 1])):
                 p0, p1 = span(cols_node)
-                cols_pos = torch.as_tensor(pos[tree.ids(cols_node)] - p0, device=dev, dtype=torch.int64)
-                rows = L.shape[0]
+                cols_pos = pos[tree.ids(cols_node)] - p0
                 groups.append((a_row0, rows, p0, b_x0, (p1 - p0) // 64, 256 * len(groups), rk, 0, int(slot)))
-                lefts.append(L)
-                rights.append((R, b_x0, cols_pos))
+                ljobs.append((lbase, 1, rows, rows, rk, a_row0, 0, -1))
+                rjobs.append((rbase, ncols, 1, rk, ncols, 0, b_x0, map_n))
+                maps.append(cols_pos)
+                map_n += len(cols_pos)
                 a_row0 += rows
                 b_x0 += p1 - p0
                 if meta[w, 6]:                      # a diagonal block has no transposed half (none is low rank)
                     break
         lrows = a_row0 + 128
         rwidth = max(b_x0, 64)
-        dgroups, dmats = [], []
+        dgroups, djobs = [], []
         d_row0 = 0
         if dense:
             for w in np.flatnonzero(meta[:, 7] < 0):
                 la, lb, so = int(meta[w, 1]), int(meta[w, 3]), int(meta[w, 4])
                 i, j = self._nodes[w]
-                D = store[so:so + la * lb].view(la, lb)
-                for M, rows_node, cols_node, slot in ((D, i, j, slot0[w, 0]), (D.T, j, i, slot0[w, 1])):
+                # D (la x lb) row-major at so; forward D, transposed D^T
+                for rows, ncols, si, sj, cols_node, slot in ((la, lb, lb, 1, j, slot0[w, 0]),
+                                                             (lb, la, 1, lb, i, slot0[w, 1])):
                     p0, p1 = span(cols_node)
-                    cols_pos = torch.as_tensor(pos[tree.ids(cols_node)] - p0, device=dev, dtype=torch.int64)
-                    dgroups.append((d_row0, M.shape[0], p0, 0, (p1 - p0) // 64, 0, 0, 0, int(slot)))
-                    dmats.append((M, cols_pos))
-                    d_row0 += M.shape[0]
+                    cols_pos = pos[tree.ids(cols_node)] - p0
+                    dgroups.append((d_row0, rows, p0, 0, (p1 - p0) // 64, 0, 0, 0, int(slot)))
+                    djobs.append((so, si, sj, rows, ncols, d_row0, 0, map_n))
+                    maps.append(cols_pos)
+                    map_n += len(cols_pos)
+                    d_row0 += rows
                     if meta[w, 6]:                  # a diagonal block is stored whole: one direction
                         break
         dpitch = max([g[4] * 64 for g in dgroups] + [64])
-
-        def parts(x):
-            h = x.float().to(torch.bfloat16)
-            return h, (x.float() - h.float()).to(torch.bfloat16)
+        map_all = np.concatenate(maps).astype(np.int32) if maps else np.zeros(1, np.int32)
         lplane = torch.zeros((lrows, 128), dtype=torch.bfloat16, device=dev)
         rplane = torch.zeros((128, 2 * rwidth), dtype=torch.bfloat16, device=dev)
-        for g, L in zip(groups, lefts):
-            h, m = parts(L)
-            r0, rows, rk = g[0], g[1], g[6]
-            lplane[r0:r0 + rows, :rk] = h
-            lplane[r0:r0 + rows, 64:64 + rk] = m
-        for g, (R, x0, cols_pos) in zip(groups, rights):
-            h, m = parts(R)
-            rk = g[6]
-            rplane[:rk, x0 + cols_pos] = h
-            rplane[:rk, rwidth + x0 + cols_pos] = m
+        _pack_parts(store, ljobs, map_all, lplane, 64)
+        _pack_parts(store, rjobs, map_all, rplane, rwidth)
         gdt = np.dtype([('a_row0', '<i4'), ('rows', '<i4'), ('a_x0', '<i4'), ('b_x0', '<i4'), ('kb', '<i4'),
                         ('t_row0', '<i4'), ('rank', '<i4'), ('pad', '<i4'), ('slot0', '<i8')])
         assert gdt.itemsize == 40
@@ -377,11 +415,7 @@ class DeviceHMatrix:
                                                  len(fp64_dense))
         if dgroups:
             dplane = torch.zeros((d_row0 + 128, 2 * dpitch), dtype=torch.bfloat16, device=dev)
-            for g, (M, cols_pos) in zip(dgroups, dmats):
-                h, m = parts(M)
-                r0, rows = g[0], g[1]
-                dplane[r0:r0 + rows][:, cols_pos] = h
-                dplane[r0:r0 + rows][:, dpitch + cols_pos] = m
+            _pack_parts(store, djobs, map_all, dplane, dpitch)
             dtiles = [(g, tt) for g, grp in enumerate(dgroups) for tt in range(-(-grp[1] // 128))]
             keep.update(dplane=dplane, dgroups=t(np.array(dgroups, dtype=gdt).view(np.uint8), np.uint8),
                         dtile_group=t([g for g, _ in dtiles], np.int32), dtile_m=t([m for _, m in dtiles], np.int32))

@@ -335,25 +335,37 @@ class PeecTopology:
         pbranch[up] = np.asarray(adj[up, parent[up]]).ravel().astype(np.int64) - 1
         tpos = np.full(self.nb, -1, np.int64)
         tpos[branch[is_tree]] = np.flatnonzero(is_tree)
-        # T[keep]^-1: for every node, an entry in the row of each branch on its path to the root
-        R, C, V = [], [], []
+        # T[keep]^-T row by row: each kept node's row holds the branches of its path to the root, nearest first
+        # (level l of the walk is entry l of the row), so its CSR is filled in place; T[keep]^-1 is its transpose
+        levels = []
+        depth = np.zeros(nkeep, np.int64)
         cur, start = up.copy(), kidx[up]
         while cur.size:
             e = pbranch[cur]
-            R.append(tpos[e])
-            C.append(start)
-            V.append(np.where(ea[e] == cur, 1.0, -1.0))
+            levels.append((start, tpos[e].astype(np.int32), np.where(ea[e] == cur, 1.0, -1.0)))
+            depth[start] += 1
             cur = parent[cur]
             more = keep[cur]
             cur, start = cur[more], start[more]
-        tinv = csr_matrix((np.concatenate(V), (np.concatenate(R), np.concatenate(C))), shape=(n, nkeep))
+        tptr = np.r_[0, np.cumsum(depth)].astype(np.int64)
+        tidx = np.empty(int(tptr[-1]), np.int32)
+        tval = np.empty(int(tptr[-1]))
+        for level, (rows_l, cols_l, vals_l) in enumerate(levels):
+            at = tptr[rows_l] + level
+            tidx[at] = cols_l
+            tval[at] = vals_l
+        del levels
+        tinvt = (tptr, tidx, tval, (nkeep, n))
+        tinv_csc = csr_matrix((tval, tidx, tptr), shape=(nkeep, n)).tocsc()
+        tinv = (tinv_csc.indptr.astype(np.int64), tinv_csc.indices.astype(np.int32), tinv_csc.data, (n, nkeep))
+        del tinv_csc
         comp = np.asarray(self.labels)[keep].astype(np.int32)
         nc = int(self.B.shape[1])
         members = np.argsort(comp, kind='stable').astype(np.int32)
         member_ptr = np.r_[0, np.cumsum(np.bincount(comp, minlength=nc))].astype(np.int64)
         g = dict(nkeep=nkeep, ncomp=nc, kept=keep, keep_row=kidx, ac=_host_csr(ac), lap_ptr=lap_ptr,
-                 lap_branch=br.astype(np.int32), lap_other=oth.astype(np.int32), tinv=_host_csr(tinv),
-                 tinvt=_host_csr(tinv.T), branch=branch.astype(np.int32), loop_ends=loop_ends, comp=comp,
+                 lap_branch=br.astype(np.int32), lap_other=oth.astype(np.int32), tinv=tinv,
+                 tinvt=tinvt, branch=branch.astype(np.int32), loop_ends=loop_ends, comp=comp,
                  member_ptr=member_ptr, members=members)
         self._graph = g
         return g
@@ -1057,14 +1069,23 @@ class PeecModel(PeecTopology):
                 e1.record()
                 torch.cuda.synchronize()
                 precondition_ms += e0.elapsed_time(e1)
+            if mode == 3:
+                # the graph preconditioner's host structure and its upload: once per model (and part count)
+                t3 = time.perf_counter()
+                self._graph_device()
+                if parts:
+                    self._graph_domains_device(parts)
+                self.timings['graph_host_s'] = time.perf_counter() - t3
             if mixed and self.matrix == 'hierarchical':
                 # the inner products: the H-matrices' blocks, low rank and dense, in BF16 on the tensor cores
+                t3 = time.perf_counter()
                 for which, H in ((0, self.HL), (1, self.HP)):
                     plans = H.__dict__.setdefault('_plans', {})
                     if True not in plans:
                         plans[True] = H.lowrank_plan(dense=True)
                     if plans[True] is not None:
                         _lib.check(lib.pcbqs_gb300_peec_set_lowrank(handle, which, ctypes.byref(plans[True][1])), lib)
+                self.timings['lowrank_plan_s'] = time.perf_counter() - t3
             elif mixed:
                 # single-precision copies of L and P for the inner products; FP64 outer residuals
                 Lf, Pf = self.Lf, self.Pf
@@ -1152,6 +1173,7 @@ class PeecModel(PeecTopology):
             lib.pcbqs_gb300_peec_destroy(handle)
         # back to the unclustered order, then currents, charges and source voltages (peec_iterative.py:331-341), for
         # every (frequency, port) column at once: one P product over all of them
+        t4 = time.perf_counter()
         Xo = np.empty_like(X)
         Xo[self.order] = X
         Z = np.zeros((len(f), npo, npo), complex)
@@ -1167,6 +1189,7 @@ class PeecModel(PeecTopology):
             currents[fi] = baseline + loop_part[:, cols] + 1j * w * tree_part[:, cols]
             currents[fi][self.sources] = excitation
             Z[fi] = source_voltage / (1j * w) + voltages[:, cols]
+        self.timings['post_s'] = time.perf_counter() - t4
         self.timings['solve_s'] = time.perf_counter() - t0
         if not converged:
             raise RuntimeError(f'GMRES did not reach {self.tol:g}: residuals {res.max():.3g}, iterations {its.max()}')

@@ -105,6 +105,26 @@ def test_lowrank_product_on_tensor_cores(device_library, kernel, k, dense):
     assert torch.equal(again, ours)               # deterministic (slot rows summed in block order)
 
 
+@pytest.mark.parametrize('kernel', ['inductance', 'potential'])
+def test_plane_packing_kernel_matches_restatement(device_library, monkeypatch, kernel):
+    """The tensor-core planes of the low-rank plan (left, right and dense-leaf planes) as k_pack_parts writes them
+    equal, bit for bit, the same plan packed by the kernel's restatement (tests/test_lowrank_host.py)."""
+    import torch
+    import pcbqs_gb300.hmatrix as hm
+    from pcbqs_gb300.board import Board
+    from pcbqs_gb300.fill import DeviceFill
+    from test_lowrank_host import emulate_pack_parts
+    b = Board.load('strip')
+    fill = DeviceFill(b.nodes, b.tris, b.z, 1, 3.0)
+    H = hm.DeviceHMatrix(fill, tol=1e-8, leaf=64, kernel=kernel, er=b.er)
+    keep, _ = H.lowrank_plan(dense=True)
+    monkeypatch.setattr(hm, '_pack_launch', emulate_pack_parts)
+    ref, _ = H.lowrank_plan(dense=True)
+    for name in ('lplane', 'rplane', 'dplane'):
+        assert torch.equal(keep[name].view(torch.int16), ref[name].view(torch.int16)), name
+    assert int((keep['lplane'] != 0).sum()) > 0 and int((keep['dplane'] != 0).sum()) > 0
+
+
 @pytest.mark.parametrize('board', ['strip', 'viapair'])
 def test_compressed_mixed_solve_matches_reference(device_library, board):
     """The mixed compressed solve: inner GMRES with the low-rank blocks in BF16 on the tensor cores, FP64 outer

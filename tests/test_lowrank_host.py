@@ -2,7 +2,9 @@
 emulating the two GEMM phases exactly as the kernel addresses its planes (k_tc_update modes 4 and 5: the part
 segments (h, m) x (h, m, h), the 64-wide K slices, the padded cluster order, the group and tile tables, the slot
 rows), against the direct sum of U V^T x over the blocks in both directions. No GPU: a stand-in object carries a
-real ClusterTree and random low-rank blocks in the packed layout of DeviceHMatrix._pack."""
+real ClusterTree and random low-rank blocks in the packed layout of DeviceHMatrix._pack, and the planes' packing
+kernel's launch (k_pack_parts, after the host's bounds checks) is replaced by its restatement here (the GPU tests
+hold the kernel to it bit for bit)."""
 import numpy as np
 import torch
 
@@ -63,11 +65,31 @@ def _bf(x):
     return torch.as_tensor(x).float().to(torch.bfloat16).double().numpy()
 
 
+def emulate_pack_parts(store, jobs, map_all, plane, off2):
+    """k_pack_parts (csrc/hmatrix.cu) restated with torch's CPU roundings: each job writes h = bf16(fp32(x)) and
+    m = bf16(fp32(x) - h) of its entries x = store[base + i si + j sj] to plane rows row0 + i, columns c and
+    off2 + c, c = colbase + map_all[map_off + j] (colbase + j when map_off < 0)."""
+    st = store.detach().cpu().numpy()
+    out = torch.zeros(plane.shape, dtype=torch.bfloat16)
+    for base, si, sj, ni, nj, row0, colbase, moff in np.asarray(jobs, np.int64).reshape(-1, 8):
+        if ni == 0 or nj == 0:
+            continue
+        x = torch.as_tensor(st[base + np.arange(ni)[:, None] * si + np.arange(nj)[None, :] * sj]).float()
+        h = x.to(torch.bfloat16)
+        m = (x - h.float()).to(torch.bfloat16)
+        cols = torch.as_tensor(colbase + (np.arange(nj) if moff < 0 else map_all[moff:moff + nj].astype(np.int64)))
+        out[row0:row0 + ni][:, cols] = h
+        out[row0:row0 + ni][:, off2 + cols] = m
+    plane.copy_(out.to(plane.device))
+
+
 GDT = np.dtype([('a_row0', '<i4'), ('rows', '<i4'), ('a_x0', '<i4'), ('b_x0', '<i4'), ('kb', '<i4'),
                 ('t_row0', '<i4'), ('rank', '<i4'), ('pad', '<i4'), ('slot0', '<i8')])
 
 
-def test_lowrank_plan_emulated_matches_direct_sum():
+def test_lowrank_plan_emulated_matches_direct_sum(monkeypatch):
+    import pcbqs_gb300.hmatrix as hm
+    monkeypatch.setattr(hm, '_pack_launch', emulate_pack_parts)
     f, blocks, dense, nslots = _fake()
     keep, d = DeviceHMatrix.lowrank_plan(f, dense=True)
     n, k = f.n, 5
