@@ -1286,13 +1286,14 @@ __global__ void k_graph_charge(int64_t nkeep, int k, const int32_t *comp, const 
     }
 }
 
-// The tree unknowns' outputs: ps (T[keep]^-1 charge)_j; loop rows untouched.
-__global__ void k_graph_tree_out(int64_t n, int k, const int8_t *is_tree, Csr tinv, double ps, const cd *charge,
-                                 cd *out) {
+// The tree unknowns' outputs: ps (T[keep]^-1 charge)_j; loop rows and the long rows (k_graph_tree_out_long)
+// untouched.
+__global__ void k_graph_tree_out(int64_t n, int k, const int8_t *is_tree, const int8_t *long_row, Csr tinv, double ps,
+                                 const cd *charge, cd *out) {
     const int64_t total = n * k;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = t / k;
-        if (!is_tree[j]) continue;
+        if (!is_tree[j] || long_row[j]) continue;
         const int c = (int)(t % k);
         double re = 0, im = 0;
         for (int64_t a = tinv.ptr[j]; a < tinv.ptr[j + 1]; ++a) {
@@ -1559,8 +1560,51 @@ struct DomainLap : LapSolver {
     }
 };
 
+// The same for the rows of T[keep]^-1 longer than GRAPH_LONG_ROW entries (the branches near a root: their subtrees
+// hold most of the nodes), one thread block per row: the threads stride over the row's entries with
+// GRAPH_ROW_COLS columns at a time in registers, then a fixed-order tree reduction in shared memory.
+constexpr int GRAPH_LONG_ROW = 512;
+constexpr int GRAPH_ROW_COLS = 8;
+
+__global__ void __launch_bounds__(256) k_graph_tree_out_long(const int32_t *rows, int k, Csr tinv, double ps,
+                                                             const cd *charge, cd *out) {
+    __shared__ cd part[256][GRAPH_ROW_COLS];
+    const int64_t j = rows[blockIdx.x];
+    const int64_t a0 = tinv.ptr[j], a1 = tinv.ptr[j + 1];
+    for (int c0 = 0; c0 < k; c0 += GRAPH_ROW_COLS) {
+        const int nc = min(GRAPH_ROW_COLS, k - c0);
+        cd acc[GRAPH_ROW_COLS];
+        for (int c = 0; c < GRAPH_ROW_COLS; ++c) acc[c] = make_double2(0, 0);
+        for (int64_t a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
+            const double v = tinv.val[a];
+            const cd *x = charge + (int64_t)tinv.idx[a] * k + c0;
+            for (int c = 0; c < GRAPH_ROW_COLS; ++c)
+                if (c < nc) {
+                    acc[c].x += v * x[c].x;
+                    acc[c].y += v * x[c].y;
+                }
+        }
+        for (int c = 0; c < GRAPH_ROW_COLS; ++c) part[threadIdx.x][c] = acc[c];
+        __syncthreads();
+        for (int stride = blockDim.x / 2; stride > 0; stride >>= 1) {
+            if ((int)threadIdx.x < stride)
+                for (int c = 0; c < GRAPH_ROW_COLS; ++c) {
+                    part[threadIdx.x][c].x += part[threadIdx.x + stride][c].x;
+                    part[threadIdx.x][c].y += part[threadIdx.x + stride][c].y;
+                }
+            __syncthreads();
+        }
+        if ((int)threadIdx.x < nc)
+            out[j * k + c0 + threadIdx.x] = make_double2(ps * part[0][threadIdx.x].x, ps * part[0][threadIdx.x].y);
+        __syncthreads();
+    }
+}
+
 struct GraphPrecond : Preconditioner {
     int64_t n = 0, nkeep = 0, ncomp = 0, nbranch = 0;
+    int32_t *long_rows = nullptr;     // the tree unknowns whose row of T[keep]^-1 is longer than GRAPH_LONG_ROW
+    int8_t *long_flag = nullptr;      // n: 1 on those rows
+    int64_t nlong = 0;
     Csr ac, tinv, tinvt, K;
     const int64_t *lap_ptr = nullptr, *member_ptr = nullptr;
     const int32_t *lap_branch = nullptr, *lap_other = nullptr, *branch = nullptr, *loop_ends = nullptr,
@@ -1581,7 +1625,9 @@ struct GraphPrecond : Preconditioner {
     ~GraphPrecond() override {
         delete lap;
         free_work();
-        for (void *p : {(void *)zdiag, (void *)dinv, (void *)pinv, (void *)rtotal}) dev_free(p);
+        for (void *p : {(void *)zdiag, (void *)dinv, (void *)pinv, (void *)rtotal, (void *)long_rows,
+                        (void *)long_flag})
+            dev_free(p);
     }
     cudaError_t reserve(int k, cudaStream_t s) {
         if (k <= cap) return cudaSuccess;
@@ -1613,8 +1659,9 @@ struct GraphPrecond : Preconditioner {
         k_graph_common<<<dim3((unsigned)ncomp, (unsigned)((k + 31) / 32)), dim3(32, 16), 0, s>>>(
             k, member_ptr, members, pinv, rtotal, v2, m);
         k_graph_charge<<<grid_of(nkeep * k), 256, 0, s>>>(nkeep, k, comp, pinv, m, v2);
-        k_graph_tree_out<<<grid_of(n * k), 256, 0, s>>>(n, k, is_tree, tinv, ps, v2, out);
-        note_launches(7);
+        k_graph_tree_out<<<grid_of(n * k), 256, 0, s>>>(n, k, is_tree, long_flag, tinv, ps, v2, out);
+        if (nlong) k_graph_tree_out_long<<<(unsigned)nlong, 256, 0, s>>>(long_rows, k, tinv, ps, v2, out);
+        note_launches(nlong ? 8 : 7);
         return cudaGetLastError();
     }
     cudaError_t apply(int k, const int32_t *, const cd *in, cd *out, cudaStream_t s) override {
@@ -2331,6 +2378,35 @@ int pcbqs_gb300_peec_graph(pcbqs_gb300_peec *h, const pcbqs_gb300_graph *g, int3
         t = make_double2(t.x / a, -t.y / a);
     }
     cudaMemcpyAsync(gp->rtotal, tot.data(), sizeof(cd) * g->ncomp, cudaMemcpyHostToDevice, st);
+    // the long rows of T[keep]^-1, found on the host from its row pointers
+    {
+        std::vector<int64_t> tptr((size_t)n + 1);
+        std::vector<int8_t> tree((size_t)n), flag((size_t)n, 0);
+        std::vector<int32_t> rows;
+        cudaMemcpyAsync(tptr.data(), g->tinv.ptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(tree.data(), op.is_tree, (size_t)n, cudaMemcpyDeviceToHost, st);
+        if ((e = cudaStreamSynchronize(st))) {
+            delete gp;
+            return pfail(cuda_status(e), "peec_graph: %s", cudaGetErrorString(e));
+        }
+        for (int64_t j = 0; j < n; ++j)
+            if (tree[j] && tptr[j + 1] - tptr[j] > GRAPH_LONG_ROW) {
+                rows.push_back((int32_t)j);
+                flag[j] = 1;
+            }
+        gp->nlong = (int64_t)rows.size();
+        if ((e = dev_alloc(&gp->long_flag, n, st)) || (e = dev_alloc(&gp->long_rows, std::max<size_t>(rows.size(), 1), st))) {
+            delete gp;
+            return pfail(ERR_MEMORY, "peec_graph: %s", cudaGetErrorString(e));
+        }
+        cudaMemcpyAsync(gp->long_flag, flag.data(), (size_t)n, cudaMemcpyHostToDevice, st);
+        if (!rows.empty())
+            cudaMemcpyAsync(gp->long_rows, rows.data(), sizeof(int32_t) * rows.size(), cudaMemcpyHostToDevice, st);
+        if ((e = cudaStreamSynchronize(st))) {          // the host vectors go out of scope here
+            delete gp;
+            return pfail(cuda_status(e), "peec_graph: %s", cudaGetErrorString(e));
+        }
+    }
     const int status = g->domains ? graph_domain_lap(g, gp->dinv, st, &gp->lap) : graph_dense_lap(g, gp->dinv, st,
                                                                                                   &gp->lap);
     if (status != OK) {
