@@ -928,6 +928,40 @@ class PeecModel(PeecTopology):
         desc.domains = ctypes.pointer(self._graph_domains_device(parts)) if parts else None
         _lib.check(lib.pcbqs_gb300_peec_graph(handle, ctypes.byref(desc), int(sys_index), int(refine), stream), lib)
 
+    @classmethod
+    def solve_options(cls, matrix, freqs, precondition, mixed, factor_math, anchors, captured, product, fp64_product,
+                      graph_parts, graph_refine):
+        """The checks of solve's options, made before any device work: (frequencies, preconditioner mode, anchors,
+        fp64_product) with the defaults filled in; ValueError for an invalid one."""
+        f = np.atleast_1d(np.asarray(freqs, float))
+        if f.ndim != 1 or not len(f) or not np.isfinite(f).all() or (f <= 0).any():
+            raise ValueError('frequencies must be finite and positive')
+        if precondition not in cls.PRECONDITIONERS:
+            raise ValueError(f'precondition must be one of {sorted(cls.PRECONDITIONERS)}')
+        if factor_math not in cls.FACTOR_MATH:
+            raise ValueError(f'factor_math must be one of {sorted(cls.FACTOR_MATH)}')
+        if product not in cls.PRODUCT:
+            raise ValueError(f'product must be one of {sorted(cls.PRODUCT)}')
+        if fp64_product is None:
+            fp64_product = 'sliced6' if mixed else 'fp64'
+        if fp64_product not in cls.FP64_PRODUCT:
+            raise ValueError(f'fp64_product must be one of {sorted(cls.FP64_PRODUCT)}')
+        if matrix == 'hierarchical' and precondition == 'lu32':
+            raise ValueError("the compressed operator solves with precondition 'block_jacobi', 'graph' or 'none'")
+        if anchors is None:
+            anchors = len(f)
+        if not isinstance(anchors, (int, np.integer)) or isinstance(anchors, bool) or not 1 <= anchors <= len(f):
+            raise ValueError('anchors must be an integer between 1 and the number of frequencies')
+        if graph_parts is not None and (not isinstance(graph_parts, (int, np.integer)) or isinstance(graph_parts, bool)
+                                        or (graph_parts != 0 and (graph_parts < 2 or graph_parts & (graph_parts - 1)))):
+            raise ValueError('graph_parts must be 0 (dense) or a power of two >= 2')
+        if graph_refine is not None and (not isinstance(graph_refine, (int, np.integer))
+                                         or isinstance(graph_refine, bool) or not 0 <= graph_refine <= 3):
+            raise ValueError('graph_refine must be an integer in 0..3')
+        if captured and graph_parts and precondition == 'graph':
+            raise ValueError('captured GMRES cycles need the dense graph Laplacian (graph_parts=0)')
+        return f, cls.PRECONDITIONERS[precondition], int(anchors), fp64_product
+
     def solve(self, freqs, precondition='block_jacobi', mixed=False, factor_math='tc6-blocked', anchors=None,
               captured=False, product='tc3', fp64_product=None, graph_parts=None, graph_refine=None):
         """Port impedance matrix (nf, np, np): column j drives port j with 1 A (the others 0).
@@ -958,33 +992,14 @@ class PeecModel(PeecTopology):
         products over 4 or more columns (the mixed solve's outer residuals, the FP64 GMRES): 'fp64' on the FP64 pipe,
         or 'sliced6' (5, 7) on the tensor cores from integer slices at FP64's accuracy
         (pcbqs_gb300_peec_set_fp64_product); default 'sliced6' for mixed=True, 'fp64' (the plain path) otherwise."""
+        f, mode, anchors, fp64_product = self.solve_options(self.matrix, freqs, precondition, mixed, factor_math,
+                                                            anchors, captured, product, fp64_product, graph_parts,
+                                                            graph_refine)
         if self.L is None and self.HL is None:
             self.assemble()
-        f = np.atleast_1d(np.asarray(freqs, float))
-        if f.ndim != 1 or not np.isfinite(f).all() or (f <= 0).any():
-            raise ValueError('frequencies must be finite and positive')
-        if precondition not in self.PRECONDITIONERS:
-            raise ValueError(f'precondition must be one of {sorted(self.PRECONDITIONERS)}')
-        if factor_math not in self.FACTOR_MATH:
-            raise ValueError(f'factor_math must be one of {sorted(self.FACTOR_MATH)}')
-        if product not in self.PRODUCT:
-            raise ValueError(f'product must be one of {sorted(self.PRODUCT)}')
-        if fp64_product is None:
-            fp64_product = 'sliced6' if mixed else 'fp64'
-        if fp64_product not in self.FP64_PRODUCT:
-            raise ValueError(f'fp64_product must be one of {sorted(self.FP64_PRODUCT)}')
-        if self.matrix == 'hierarchical' and precondition == 'lu32':
-            raise ValueError("the compressed operator solves with precondition 'block_jacobi', 'graph' or 'none'")
         nf = len(f)
-        if anchors is None:
-            anchors = nf
-        if not isinstance(anchors, (int, np.integer)) or not 1 <= anchors <= nf:
-            raise ValueError('anchors must be an integer between 1 and the number of frequencies')
-        mode = self.PRECONDITIONERS[precondition]
         parts = self._graph_parts(graph_parts) if mode == 3 else 0
         refine = (2 if parts else 1) if graph_refine is None else int(graph_refine)
-        if not 0 <= refine <= 3:
-            raise ValueError('graph_refine must lie in 0..3')
         if parts and captured:
             raise ValueError('captured GMRES cycles need the dense graph Laplacian (graph_parts=0)')
         t0 = time.perf_counter()

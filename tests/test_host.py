@@ -153,3 +153,48 @@ def test_peec_model_rejects_bad_options_before_touching_the_device():
         PeecModel(b, matrix='sparse')
     with pytest.raises(ValueError, match='homogeneous'):
         PeecModel(b, matrix='hierarchical', stack=object())
+
+
+def test_solve_options_are_checked_before_device_work():
+    """PeecModel.solve_options (run first in solve, no GPU needed): frequencies, preconditioner names, the graph
+    preconditioner's part count (0 or a power of two), its refinement count (0..3), captured cycles only with the
+    dense Laplacian, and the complex64 factor only for the dense operator."""
+    import numpy as np
+    import pytest
+    from pcbqs_gb300.peec import PeecModel
+    base = dict(matrix='dense', freqs=[1e6], precondition='graph', mixed=False, factor_math='tc6-blocked',
+                anchors=None, captured=False, product='tc3', fp64_product=None, graph_parts=None, graph_refine=None)
+
+    def check(**kw):
+        return PeecModel.solve_options(**{**base, **kw})
+    f, mode, anchors, fp64 = check()
+    assert mode == 3 and anchors == 1 and fp64 == 'fp64' and np.array_equal(f, [1e6])
+    assert check(mixed=True)[3] == 'sliced6'
+    assert check(graph_parts=0, captured=True)[1] == 3
+    assert check(graph_parts=16, graph_refine=0)[1] == 3
+    for kw, match in ((dict(freqs=[0.0]), 'frequencies'), (dict(freqs=[]), 'frequencies'),
+                      (dict(freqs=[np.inf]), 'frequencies'), (dict(precondition='ilu'), 'precondition'),
+                      (dict(graph_parts=3), 'graph_parts'), (dict(graph_parts=1), 'graph_parts'),
+                      (dict(graph_parts=True), 'graph_parts'), (dict(graph_refine=4), 'graph_refine'),
+                      (dict(graph_refine=-1), 'graph_refine'), (dict(graph_refine=1.5), 'graph_refine'),
+                      (dict(graph_parts=8, captured=True), 'captured'),
+                      (dict(matrix='hierarchical', precondition='lu32'), 'compressed'),
+                      (dict(anchors=2), 'anchors'), (dict(product='bf16'), 'product'),
+                      (dict(fp64_product='sliced9'), 'fp64_product'), (dict(factor_math='fp16'), 'factor_math')):
+        with pytest.raises(ValueError, match=match):
+            check(**kw)
+
+
+def test_graph_entries_reject_bad_arguments_without_a_device():
+    """The graph preconditioner's and the plane packer's C entries check their arguments before any CUDA call."""
+    import ctypes
+    from pcbqs_gb300 import _lib, build
+    build.build()
+    lib = _lib.load()
+    g = _lib.GraphDesc()
+    assert lib.pcbqs_gb300_peec_graph(None, ctypes.byref(g), 0, 1, None) == 1
+    assert lib.pcbqs_gb300_peec_graph_apply(None, 1, None, None, None) == 1
+    assert lib.pcbqs_gb300_pack_bf16_parts(None, None, -1, None, None, 64, 0, None) == 1
+    assert lib.pcbqs_gb300_pack_bf16_parts(None, None, 1, None, None, 64, 0, None) == 1     # null arrays
+    assert lib.pcbqs_gb300_pack_bf16_parts(None, None, 0, None, None, 64, 0, None) == 0     # nothing to pack
+    assert b'invalid argument' in lib.pcbqs_gb300_last_error()
