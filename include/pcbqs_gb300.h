@@ -379,7 +379,7 @@ typedef struct pcbqs_gb300_lowrank {
  * cores: BF16 three-part products, FP32 accumulation (phase one R X[J] for every block and direction, one tile each;
  * phase two L T into the block's slots; the rows then sum their slots in block order). X, Y (n, k) complex128 device
  * arrays, k <= 128; relative error about 2^-16 of the low-rank part. Synchronizes `stream`; status 6 when a bounded
- * wait gave up. The benchmark spec's BF16 low-rank products; the reference's are FP64 (core/hmatrix_kernels.hpp:20-100). */
+ * wait gave up. The reference's low-rank products are FP64 (core/hmatrix_kernels.hpp:20-100). */
 int pcbqs_gb300_hmatrix_apply_lowrank(const pcbqs_gb300_hmat *H, const pcbqs_gb300_lowrank *lr, int k,
                                       const double *x, double *y, void *stream);
 /* The BF16 part planes of pcbqs_gb300_lowrank from the H-matrix's FP64 store (device arrays; no counterpart in the

@@ -1,5 +1,5 @@
-"""Pure-Python restatement of the PEEC spanning forest and loop basis, kept as the checker for the native
-pcbqs_gb300_loop_basis, and of the graph preconditioner, the checker for pcbqs_gb300_peec_graph (test
+"""Pure-Python restatement of the PEEC spanning forest and loop basis, the oracle the tests hold the native
+pcbqs_gb300_loop_basis to, and of the graph preconditioner, the oracle for pcbqs_gb300_peec_graph (test
 infrastructure only: nothing in the package imports this module).
 
 Follows src/pcbqs/mqs.py:48-130 (spanning_tree: breadth-first forest from each island's most central node, other

@@ -1,7 +1,7 @@
 """CPU restatement (NumPy) of the learned block preconditioner, for checking the device kernels: the edge network's
 forward pass and its parameter gradients, the preconditioner's application and the training loss.
 
-Test infrastructure only: tests/ alone imports this module, as the checker of pcbqs_gb300_learned_* (the product
+Test infrastructure only: tests/ alone imports this module, as the oracle of pcbqs_gb300_learned_* (the product
 path runs those kernels, never this).
 
     M^-1 x = y - sum_e g_e D_b^-1 A_bc y_c,  y = D^-1 x        (edges e = (b <- c), blocks of bs unknowns)

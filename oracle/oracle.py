@@ -1,11 +1,11 @@
 """CPU oracle of the pcbqs static fill -- TEST INFRASTRUCTURE ONLY.
 
-Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this module, as the checker (and as
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this module, as the oracle (and as
 the timed CPU restatement of the reference's compiled core). The product (pcbqs_gb300) never imports it.
 
 Contents:
   * prepare()         FillGeometry.prepare restated (src/pcbqs/static_backends.py:104-130), written independently
-                      of the product's copy so the checker does not share the code it checks;
+                      of the product's copy so the oracle does not share the code it tests;
   * C restatement     liboracle.so built from oracle/pcbqs_oracle.c (make -C oracle): og_pair, og_kind,
                       og_pairs, og_fill, og_combine, og_potential (file:line citations in the C source);
   * rwg()             the RWG basis (src/pcbqs/_numerics/base.py:10-41);

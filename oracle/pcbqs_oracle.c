@@ -3,7 +3,7 @@
  * near/far classification, whole-matrix reciprocal fill, RWG combine and area-weighted potential aggregation.
  *
  * TEST INFRASTRUCTURE ONLY. Nothing in the product links or calls this file: only the tests, the smoke check and
- * the CPU-baseline leg of bench.py load it, as the checker and as the timed CPU restatement of the reference's
+ * the CPU-baseline leg of bench.py load it, as the oracle and as the timed CPU restatement of the reference's
  * compiled core. Parity is pinned against the reference itself (see tests/golden/make_golden.py: vectors produced
  * by the reference's own NumPy and compiled paths, and tests/test_oracle_golden.py).
  *

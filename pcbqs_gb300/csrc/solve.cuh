@@ -44,7 +44,7 @@ struct GmresReport {
     std::vector<int> iterations;      // per column
     std::vector<double> residual;     // true relative residual per column at exit
     int cycles = 0;
-    int launches = 0;                 // kernels launched by the driver (operator and preconditioner excluded)
+    int launches = 0;                 // kernels launched by the GMRES loop itself (operator and preconditioner excluded)
 };
 
 // Solve A_s x_s = b_s for k columns (b, x on the device, (n, k) layout); x holds the initial guess on entry.
