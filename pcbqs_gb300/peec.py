@@ -370,6 +370,20 @@ class PeecTopology:
         self._graph = g
         return g
 
+    GRAPH_DENSE_BYTES = 16e9     # the graph Laplacian dense up to this size (about 44,700 kept nodes)
+    GRAPH_DOMAIN_ROWS = 1500     # above it, domains of about this many rows
+
+    def _graph_parts(self, parts):
+        """0 (the dense Laplacian) or the domain count: `parts` if given, else by the Laplacian's size."""
+        if parts is not None:
+            if parts != 0 and (parts < 2 or parts & (parts - 1)):
+                raise ValueError('graph_parts must be 0 (dense) or a power of two >= 2')
+            return int(parts)
+        nk = self.graph_structure()['nkeep']
+        if 8.0 * nk * nk <= self.GRAPH_DENSE_BYTES:
+            return 0
+        return 2 ** max(1, int(round(np.log2(nk / self.GRAPH_DOMAIN_ROWS))))
+
     def graph_domains(self, parts):
         """A nested-dissection-style split of the graph Laplacian's kept nodes for boards whose Laplacian is too large
         to factor dense (made once per topology and part count; host arrays): the nodes (triangle centroids, averaged
@@ -866,20 +880,6 @@ class PeecModel(PeecTopology):
                                                         'comp', 'member_ptr', 'members')})
             self._graph_dev = gd
         return gd
-
-    GRAPH_DENSE_BYTES = 16e9     # the graph Laplacian dense up to this size (about 44,700 kept nodes)
-    GRAPH_DOMAIN_ROWS = 1500     # above it, domains of about this many rows
-
-    def _graph_parts(self, parts):
-        """0 (the dense Laplacian) or the domain count: `parts` if given, else by the Laplacian's size."""
-        if parts is not None:
-            if parts != 0 and (parts < 2 or parts & (parts - 1)):
-                raise ValueError('graph_parts must be 0 (dense) or a power of two >= 2')
-            return int(parts)
-        nk = self.graph_structure()['nkeep']
-        if 8.0 * nk * nk <= self.GRAPH_DENSE_BYTES:
-            return 0
-        return 2 ** max(1, int(round(np.log2(nk / self.GRAPH_DOMAIN_ROWS))))
 
     def _graph_domains_device(self, parts):
         """The domain split (graph_domains) as its C struct over device arrays, uploaded once per part count."""

@@ -139,3 +139,35 @@ def test_domain_split_solves_the_laplacian(board, parts):
     ref = np.linalg.solve(G, r)
     assert np.abs(x - ref).max() <= 1e-9 * np.abs(ref).max()
     assert ns == nk - ni_ and ns > 0
+
+
+def test_part_count_and_split_at_full_size():
+    """The Laplacian's form by its size: dense for the plane pair (22,224 kept nodes, 4 GB as complex64), split for
+    the C5-shaped board (210,072 kept nodes, 353 GB dense) into 128 domains of about 1,500 rows; the split leaves no
+    Laplacian edge between two domains' interiors, and every boundary entry's neighbours lie in its own domain."""
+    for board, want in (('planes', 0), ('c5', 128)):
+        t = _topology(board)
+        parts = t._graph_parts(None)
+        assert parts == want, (board, parts)
+        if not parts:
+            continue
+        g = t.graph_structure()
+        dm = t.graph_domains(parts)
+        nk, n_int, dp = g['nkeep'], dm['n_int'], dm['dom_ptr']
+        assert len(dp) == parts + 1 and dp[-1] == n_int and 0 < dm['n_sep'] < nk // 10
+        assert np.array_equal(np.sort(dm['perm']), np.arange(nk)) and np.array_equal(dm['pos'][dm['perm']],
+                                                                                        np.arange(nk))
+        dom = np.searchsorted(dp, np.arange(nk), side='right') - 1          # the domain of each new position
+        dom[n_int:] = -1
+        rows = np.repeat(np.arange(nk), np.diff(g['lap_ptr']))
+        m = g['lap_other'] >= 0
+        a, b = dm['pos'][rows[m]], dm['pos'][g['lap_other'][m]]
+        inner = (a < n_int) & (b < n_int)
+        assert (dom[a[inner]] == dom[b[inner]]).all()
+        sizes = np.diff(dp)
+        assert sizes.max() <= 2 * 1500 and sizes.min() > 0
+        bp, bn = dm['bnd_ptr'], dm['bnd_nptr']
+        assert bp[-1] == len(dm['bnd']) and bn[-1] == len(dm['bnd_local'])
+        ent_dom = np.repeat(np.arange(parts), np.diff(bp))
+        nb_dom = np.repeat(ent_dom, np.diff(bn))
+        assert (dm['bnd_local'] < sizes[nb_dom]).all() and (dm['bnd'] < dm['n_sep']).all()
